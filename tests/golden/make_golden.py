@@ -1,0 +1,297 @@
+"""Generate golden fixtures by running the unmodified reference (shenfun 4.3.0).
+
+TEST INFRASTRUCTURE ONLY.  Run in a container that has the reference checkout
+and the compiled reference kernels (``python oracle/build_ref.py`` first):
+
+    python tests/golden/make_golden.py
+
+Every fixture is a small ``.npz`` written next to this script.  The inputs are
+seeded (numpy ``default_rng``), so re-running reproduces the files.  FFTW is
+absent here; the shims reproduce its unnormalised conventions with scipy.fft,
+so the transform fixtures pin the reference's scaling, stencil and solver
+arithmetic, not FFTW's own rounding.
+"""
+import os
+import sys
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+warnings.simplefilter("ignore")
+
+from refimport import import_reference  # noqa: E402
+
+sf = import_reference()
+from shenfun import (FunctionSpace, TensorProductSpace, Array, Function,  # noqa: E402
+                     TrialFunction, TestFunction, inner, div, grad, la, chebyshev,
+                     comm, Dx)
+import sympy as sp  # noqa: E402
+
+OUT = {}
+
+
+def put(name, **arrays):
+    OUT.setdefault(name, {}).update({k: np.asarray(v) for k, v in arrays.items()})
+
+
+def save():
+    for name, d in OUT.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        size = os.path.getsize(os.path.join(HERE, name + ".npz"))
+        print(f"{name}.npz: {len(d)} arrays, {size/1024:.1f} KiB")
+
+
+rng = np.random.default_rng(20261204)
+
+
+# --------------------------------------------------------------------------
+# 1D Chebyshev transforms: Orthogonal (T), ShenDirichlet (SD), ShenBiharmonic (SB)
+# chebyshev/bases.py:315-353 (DCT scaling), spectralbase.py:1450-1474 (stencil)
+def cheb_1d():
+    for N in (8, 9, 16, 17, 33, 64):
+        for tag, bc in (("T", None), ("SD", (0, 0)), ("SB", (0, 0, 0, 0))):
+            if tag == "SB" and N < 12:
+                continue
+            V = FunctionSpace(N, "C", bc=bc) if bc else FunctionSpace(N, "C")
+            f = rng.standard_normal(N)
+            sp_ = V.scalar_product(f.copy(), np.zeros(N)).copy()
+            fw = V.forward(f.copy(), np.zeros(N)).copy()
+            dim = V.dim()
+            uh = np.zeros(N)
+            uh[:dim] = rng.standard_normal(dim)
+            bw = V.backward(uh.copy(), np.zeros(N)).copy()
+            x, w = V.points_and_weights()
+            put("cheb_1d", **{f"{tag}{N}_f": f, f"{tag}{N}_sp": sp_,
+                               f"{tag}{N}_fw": fw, f"{tag}{N}_uh": uh,
+                               f"{tag}{N}_bw": bw, f"{tag}{N}_x": x,
+                               f"{tag}{N}_w": w})
+
+
+# --------------------------------------------------------------------------
+# 1D Fourier: fourier/bases.py:131-162 (forward 1/N), :380-407 (backward)
+def fourier_1d():
+    for N in (8, 9, 16, 64):
+        R = FunctionSpace(N, "F", dtype="d")
+        f = rng.standard_normal(N)
+        fw = R.forward(f.copy(), np.zeros(N // 2 + 1, complex)).copy()
+        uh = rng.standard_normal(N // 2 + 1) + 1j * rng.standard_normal(N // 2 + 1)
+        uh[0] = uh[0].real
+        if N % 2 == 0:
+            uh[-1] = uh[-1].real
+        bw = R.backward(uh.copy(), np.zeros(N)).copy()
+        C = FunctionSpace(N, "F", dtype="D")
+        fc = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        fwc = C.forward(fc.copy(), np.zeros(N, complex)).copy()
+        uhc = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        bwc = C.backward(uhc.copy(), np.zeros(N, complex)).copy()
+        put("fourier_1d", **{f"R{N}_f": f, f"R{N}_fw": fw, f"R{N}_uh": uh,
+                              f"R{N}_bw": bw, f"C{N}_f": fc, f"C{N}_fw": fwc,
+                              f"C{N}_uh": uhc, f"C{N}_bw": bwc,
+                              f"R{N}_k": R.wavenumbers(bcast=False),
+                              f"C{N}_k": C.wavenumbers(bcast=False)})
+
+
+# --------------------------------------------------------------------------
+# Banded solvers: la.py:331-393 (TDMA), :450-543 (PDMA); la.pyx:213-252,496-532
+def banded():
+    for N in (16, 17, 32):
+        SD = FunctionSpace(N, "C", bc=(0, 0))
+        u, v = TrialFunction(SD), TestFunction(SD)
+        B = inner(u, v)
+        data = np.zeros((3, N - 2))
+        data[0, :-2] = B[-2] if np.ndim(B[-2]) else B[-2] * np.ones(N - 4)
+        data[1] = B[0]
+        data[2, 2:] = B[2] if np.ndim(B[2]) else B[2] * np.ones(N - 4)
+        raw = data.copy()
+        sol = la.TDMA(B)
+        b1 = rng.standard_normal(N - 2)
+        x1 = sol(b1.copy())
+        b2 = rng.standard_normal((N - 2, 5)) + 1j * rng.standard_normal((N - 2, 5))
+        x2 = la.TDMA(B)(b2.copy(), axis=0)
+        b3 = rng.standard_normal((4, N - 2))
+        x3 = la.TDMA(B)(b3.copy(), axis=1)
+        lu = data.copy()
+        la.TDMA.LU(lu)
+        put("banded", **{f"tdma{N}_raw": raw, f"tdma{N}_lu": lu, f"tdma{N}_b1": b1,
+                         f"tdma{N}_x1": x1, f"tdma{N}_b2": b2, f"tdma{N}_x2": x2,
+                         f"tdma{N}_b3": b3, f"tdma{N}_x3": x3})
+        SB = FunctionSpace(N, "C", bc=(0, 0, 0, 0))
+        u, v = TrialFunction(SB), TestFunction(SB)
+        B = inner(u, v)
+        n = N - 4
+        data = np.zeros((5, n))
+        data[0, :-4] = B[-4]
+        data[1, :-2] = B[-2]
+        data[2] = B[0]
+        data[3, 2:] = B[2]
+        data[4, 4:] = B[4]
+        raw = data.copy()
+        b1 = rng.standard_normal(n)
+        x1 = la.PDMA(B)(b1.copy())
+        b2 = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+        x2 = la.PDMA(B)(b2.copy(), axis=0)
+        lu = data.copy()
+        la.PDMA.LU(lu)
+        put("banded", **{f"pdma{N}_raw": raw, f"pdma{N}_lu": lu, f"pdma{N}_b1": b1,
+                         f"pdma{N}_x1": x1, f"pdma{N}_b2": b2, f"pdma{N}_x2": x2})
+
+
+# --------------------------------------------------------------------------
+# Chebyshev Dirichlet Helmholtz: chebyshev/la.py:131-351, la.pyx:717-947
+def helmholtz():
+    for (Nx, Ny, Nz, c) in ((8, 8, 17, 1000.0), (6, 4, 16, 0.0), (4, 6, 33, 50.0)):
+        F0 = FunctionSpace(Nx, "F", dtype="D")
+        F1 = FunctionSpace(Ny, "F", dtype="d")
+        SD = FunctionSpace(Nz, "C", bc=(0, 0))
+        T = TensorProductSpace(comm, (F0, F1, SD))
+        u, v = TrialFunction(T), TestFunction(T)
+        mats = inner(v, -div(grad(u)) + c * u)
+        H = chebyshev.la.Helmholtz(*mats)
+        fh = Function(T)
+        shp = fh.shape
+        fh[:] = rng.standard_normal(shp) + 1j * rng.standard_normal(shp)
+        fh[..., -2:] = 0
+        if c == 0.0:
+            fh[0, 0] = 0
+        uh = Function(T)
+        uh = H(fh.copy(), uh)
+        mv = np.zeros_like(uh)
+        mv = H.matvec(uh.copy(), mv)
+        key = f"h{Nx}x{Ny}x{Nz}"
+        put("helmholtz", **{key + "_c": c, key + "_alfa": H.alfa, key + "_beta": H.beta,
+                            key + "_d0": H.u0, key + "_d1": H.u1, key + "_d2": H.u2,
+                            key + "_L": H.L, key + "_f": fh, key + "_u": uh,
+                            key + "_mv": mv})
+    # 2D case with the solve axis first (the reference's 1D entry converts a
+    # 1-element scale array to a scalar, which numpy 2 rejects: la.pyx:718)
+    SD = FunctionSpace(20, "C", bc=(0, 0))
+    F1 = FunctionSpace(6, "F", dtype="d")
+    T = TensorProductSpace(comm, (SD, F1), axes=(0, 1))
+    u, v = TrialFunction(T), TestFunction(T)
+    mats = inner(v, -div(grad(u)) + 7.5 * u)
+    H = chebyshev.la.Helmholtz(*mats)
+    f = Function(T)
+    f[:] = rng.standard_normal(f.shape) + 1j * rng.standard_normal(f.shape)
+    f[-2:] = 0
+    x = H(f.copy(), Function(T))
+    put("helmholtz", h2d_f=f, h2d_u=x, h2d_d0=H.u0, h2d_d1=H.u1, h2d_d2=H.u2,
+        h2d_L=H.L, h2d_alfa=H.alfa, h2d_beta=H.beta)
+
+
+# --------------------------------------------------------------------------
+# Full round trips (forward -> solve -> backward) on tensor-product spaces.
+def roundtrips():
+    # cfg1: 2D Poisson, F64 x SD64, manufactured solution.
+    N = (64, 64)
+    K0 = FunctionSpace(N[0], "F", dtype="d")
+    SD = FunctionSpace(N[1], "C", bc=(0, 0))
+    T = TensorProductSpace(comm, (K0, SD), axes=(1, 0))
+    u, v = TrialFunction(T), TestFunction(T)
+    x, y = sp.symbols("x,y", real=True)
+    ue = sp.sin(2 * x) * (1 - y ** 2) * sp.cos(sp.pi * y / 2)
+    fe = -(ue.diff(x, 2) + ue.diff(y, 2))
+    fj = Array(T, buffer=fe)
+    f_hat = inner(v, fj)
+    mats = inner(v, -div(grad(u)))
+    H = chebyshev.la.Helmholtz(*mats)
+    u_hat = H(f_hat.copy(), Function(T))
+    g = la.SolverGeneric1ND(mats)
+    u_hat2 = g(f_hat.copy(), Function(T))
+    uq = u_hat.backward()
+    uj = Array(T, buffer=ue)
+    mesh = T.local_mesh(True)
+    put("cfg1_poisson2d", fj=fj, f_hat=f_hat, u_hat=u_hat, u_hat_generic=u_hat2,
+        uq=uq, uj=uj, x=mesh[0], y=mesh[1], fw=uj.forward())
+
+    # cfg2 shape family at small size: C2C x R2C x SD, alpha=k^2+1/(nu dt)
+    for (Nx, Ny, Nz) in ((8, 8, 17), (16, 12, 24)):
+        F0 = FunctionSpace(Nx, "F", dtype="D")
+        F1 = FunctionSpace(Ny, "F", dtype="d")
+        SD = FunctionSpace(Nz, "C", bc=(0, 0))
+        T = TensorProductSpace(comm, (F0, F1, SD))
+        u, v = TrialFunction(T), TestFunction(T)
+        mats = inner(v, -div(grad(u)) + 1000.0 * u)
+        H = chebyshev.la.Helmholtz(*mats)
+        fj = Array(T)
+        fj[:] = rng.standard_normal(fj.shape)
+        f_hat = inner(v, fj)
+        u_hat = H(f_hat.copy(), Function(T))
+        uq = u_hat.backward()
+        fw = fj.forward()
+        put(f"cfg2_{Nx}x{Ny}x{Nz}", fj=fj, f_hat=f_hat, u_hat=u_hat, uq=uq, fw=fw,
+            fwbw=fw.backward())
+
+
+# --------------------------------------------------------------------------
+# Biharmonic: chebyshev/la.py:354-558 (even N), la.SolverGeneric1ND (odd N)
+def biharmonic():
+    x, y, z = sp.symbols("x,y,z", real=True)
+    ue = sp.sin(x) * sp.cos(y) * (1 - z ** 2) ** 2
+    fe = ue.diff(x, 4) + ue.diff(y, 4) + ue.diff(z, 4) + 2 * ue.diff(x, 2, y, 2) + \
+        2 * ue.diff(x, 2, z, 2) + 2 * ue.diff(y, 2, z, 2)
+    for (Nx, Ny, Nz) in ((8, 8, 16), (8, 8, 17)):
+        F0 = FunctionSpace(Nx, "F", dtype="D")
+        F1 = FunctionSpace(Ny, "F", dtype="d")
+        SB = FunctionSpace(Nz, "C", bc=(0, 0, 0, 0))
+        T = TensorProductSpace(comm, (F0, F1, SB))
+        u, v = TrialFunction(T), TestFunction(T)
+        fj = Array(T, buffer=fe)
+        f_hat = inner(v, fj)
+        mats = inner(v, div(grad(div(grad(u)))))
+        g = la.SolverGeneric1ND(mats)
+        u_hat = g(f_hat.copy(), Function(T))
+        d = dict(fj=fj, f_hat=f_hat, u_hat_generic=u_hat, uq=u_hat.backward(),
+                 uj=Array(T, buffer=ue))
+        if Nz % 2 == 0:
+            Hb = chebyshev.la.Biharmonic(*mats)
+            u_hat_b = Hb(f_hat.copy(), Function(T))
+            d["u_hat_biharmonic"] = u_hat_b
+        put(f"biharmonic_{Nx}x{Ny}x{Nz}", **d)
+
+
+# --------------------------------------------------------------------------
+# Legendre: nodes/weights (fastgl), SD transforms (recursive + vandermonde),
+# Fourier x Legendre Poisson via SolverGeneric1ND/TDMA.
+def legendre():
+    for N in (4, 8, 16, 33, 100):
+        L = FunctionSpace(N, "L")
+        xw = L.points_and_weights()
+        put("legendre", **{f"xw{N}_x": xw[0], f"xw{N}_w": xw[1]})
+    for N in (16, 33, 64):
+        for tag, bc in (("L", None), ("LD", (0, 0))):
+            V = FunctionSpace(N, "L", bc=bc) if bc else FunctionSpace(N, "L")
+            f = rng.standard_normal(N)
+            dim = V.dim()
+            uh = np.zeros(N)
+            uh[:dim] = rng.uniform(-1, 1, dim) * (np.arange(dim) + 1.0) ** -2
+            d = {f"{tag}{N}_f": f, f"{tag}{N}_uh": uh}
+            for kind in ("recursive", "vandermonde"):
+                d[f"{tag}{N}_sp_{kind}"] = V.scalar_product(f.copy(), np.zeros(N), kind=kind).copy()
+                d[f"{tag}{N}_bw_{kind}"] = V.backward(uh.copy(), np.zeros(N), kind=kind).copy()
+                d[f"{tag}{N}_fw_{kind}"] = V.forward(f.copy(), np.zeros(N), kind=kind).copy()
+            put("legendre", **d)
+    # 2D Fourier x Legendre Dirichlet Helmholtz via SolverGeneric1ND
+    K0 = FunctionSpace(16, "F", dtype="d")
+    LD = FunctionSpace(24, "L", bc=(0, 0))
+    T = TensorProductSpace(comm, (K0, LD), axes=(1, 0))
+    u, v = TrialFunction(T), TestFunction(T)
+    fj = Array(T)
+    fj[:] = rng.standard_normal(fj.shape)
+    f_hat = inner(v, fj)
+    mats = inner(v, -div(grad(u)) + 3.0 * u)
+    g = la.SolverGeneric1ND(mats)
+    u_hat = g(f_hat.copy(), Function(T))
+    put("legendre", p2d_fj=fj, p2d_fhat=f_hat, p2d_uhat=u_hat, p2d_uq=u_hat.backward())
+
+
+if __name__ == "__main__":
+    cheb_1d()
+    fourier_1d()
+    banded()
+    helmholtz()
+    roundtrips()
+    biharmonic()
+    legendre()
+    save()
