@@ -1,0 +1,140 @@
+"""Pin the CPU oracle against fixtures recorded from the unmodified reference
+(tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import spectral as S, la, problems as P
+
+TOL = 1e-13
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("N", [8, 9, 16, 17, 33, 64])
+@pytest.mark.parametrize("tag", ["T", "SD", "SB"])
+def test_chebyshev_1d(golden, N, tag):
+    d = golden("cheb_1d")
+    if f"{tag}{N}_f" not in d:
+        pytest.skip("not recorded")
+    f = d[f"{tag}{N}_f"]
+    assert rel(S.cheb_scalar_product(f, tag), d[f"{tag}{N}_sp"]) < TOL
+    assert rel(S.cheb_forward(f, tag), d[f"{tag}{N}_fw"]) < TOL
+    assert rel(S.cheb_backward(d[f"{tag}{N}_uh"], tag), d[f"{tag}{N}_bw"]) < TOL
+    assert rel(S.cheb_gc_points_weights(N)[0], d[f"{tag}{N}_x"]) < TOL
+
+
+@pytest.mark.parametrize("N", [8, 9, 16, 64])
+def test_fourier_1d(golden, N):
+    d = golden("fourier_1d")
+    assert rel(S.r2c_forward(d[f"R{N}_f"]), d[f"R{N}_fw"]) < TOL
+    assert rel(S.r2c_backward(d[f"R{N}_uh"], N), d[f"R{N}_bw"]) < TOL
+    assert rel(S.c2c_forward(d[f"C{N}_f"]), d[f"C{N}_fw"]) < TOL
+    assert rel(S.c2c_backward(d[f"C{N}_uh"]), d[f"C{N}_bw"]) < TOL
+    assert np.array_equal(S.r2c_wavenumbers(N), d[f"R{N}_k"])
+    assert np.array_equal(S.c2c_wavenumbers(N), d[f"C{N}_k"])
+
+
+@pytest.mark.parametrize("N", [16, 17, 32])
+def test_tdma_pdma(golden, N):
+    d = golden("banded")
+    lu = la.tdma_lu(d[f"tdma{N}_raw"].copy())
+    assert rel(lu, d[f"tdma{N}_lu"]) < TOL
+    assert rel(la.tdma_solve(d[f"tdma{N}_b1"], lu), d[f"tdma{N}_x1"]) < TOL
+    assert rel(la.tdma_solve(d[f"tdma{N}_b2"], lu), d[f"tdma{N}_x2"]) < TOL
+    assert rel(la.tdma_solve(d[f"tdma{N}_b3"], lu, axis=1), d[f"tdma{N}_x3"]) < TOL
+    lu = la.pdma_lu(d[f"pdma{N}_raw"].copy())
+    assert rel(lu, d[f"pdma{N}_lu"]) < TOL
+    assert rel(la.pdma_solve(d[f"pdma{N}_b1"], lu), d[f"pdma{N}_x1"]) < TOL
+    assert rel(la.pdma_solve(d[f"pdma{N}_b2"], lu), d[f"pdma{N}_x2"]) < TOL
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 17, 1000.0), (6, 4, 16, 0.0), (4, 6, 33, 50.0)])
+def test_helmholtz(golden, shape):
+    Nx, Ny, Nz, c = shape
+    d = golden("helmholtz")
+    k = f"h{Nx}x{Ny}x{Nz}"
+    bases = [("fourier", "C2C", Nx), ("fourier", "R2C", Ny), ("chebyshev", "SD", Nz)]
+    assert np.all(d[k + "_alfa"] == -1.0)
+    assert rel(P.fourier_k2(bases, 2) + c, d[k + "_beta"]) == 0.0
+    d0, d1, d2, L = la.helmholtz_lu(Nz, d[k + "_alfa"].reshape(-1), d[k + "_beta"].reshape(-1))
+    for name, arr in (("_d0", d0), ("_d1", d1), ("_d2", d2), ("_L", L)):
+        assert rel(arr, d[k + name].reshape(-1, Nz)) < TOL
+    u = la.helmholtz_solve(d[k + "_f"].reshape(-1, Nz), d0, d1, d2, L)
+    assert rel(u, d[k + "_u"].reshape(-1, Nz)) < TOL
+    mv = la.helmholtz_matvec(d[k + "_u"].reshape(-1, Nz), d[k + "_alfa"].reshape(-1),
+                             d[k + "_beta"].reshape(-1))
+    assert rel(mv, d[k + "_mv"].reshape(-1, Nz)) < TOL
+
+
+def test_helmholtz_solve_axis0(golden):
+    d = golden("helmholtz")
+    f = np.moveaxis(d["h2d_f"], 0, -1)
+    d0, d1, d2, L = la.helmholtz_lu(20, d["h2d_alfa"].reshape(-1), d["h2d_beta"].reshape(-1))
+    assert rel(d0, np.moveaxis(d["h2d_d0"], 0, -1)) < TOL
+    u = la.helmholtz_solve(f, d0, d1, d2, L)
+    assert rel(u, np.moveaxis(d["h2d_u"], 0, -1)) < TOL
+
+
+def test_cfg1_poisson2d(golden):
+    d = golden("cfg1_poisson2d")
+    bases = [("fourier", "R2C", 64), ("chebyshev", "SD", 64)]
+    assert rel(P.scalar_product(d["fj"], bases, axes=(1, 0)), d["f_hat"]) < TOL
+    assert rel(P.helmholtz_solve(d["f_hat"], bases, 0.0, 1), d["u_hat"]) < TOL
+    assert rel(P.backward(d["u_hat"], bases, axes=(1, 0)), d["uq"]) < TOL
+    assert rel(P.forward(d["uj"], bases, axes=(1, 0)), d["fw"]) < TOL
+    assert np.abs(d["uq"] - d["uj"]).max() < 1e-12   # manufactured solution
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 17), (16, 12, 24)])
+def test_cfg2_roundtrip(golden, shape):
+    d = golden("cfg2_%dx%dx%d" % shape)
+    bases = [("fourier", "C2C", shape[0]), ("fourier", "R2C", shape[1]), ("chebyshev", "SD", shape[2])]
+    u, fh, uh = P.helmholtz_roundtrip(d["fj"], bases, 1000.0, 2)
+    assert rel(fh, d["f_hat"]) < TOL
+    assert rel(uh, d["u_hat"]) < TOL
+    assert rel(u, d["uq"]) < TOL
+    fw = P.forward(d["fj"], bases)
+    assert rel(fw, d["fw"]) < TOL
+    assert rel(P.backward(d["fw"], bases), d["fwbw"]) < TOL
+
+
+@pytest.mark.parametrize("Nz", [16, 17])
+def test_biharmonic(golden, Nz):
+    d = golden(f"biharmonic_8x8x{Nz}")
+    bases = [("fourier", "C2C", 8), ("fourier", "R2C", 8), ("chebyshev", "SB", Nz)]
+    assert rel(P.scalar_product(d["fj"], bases), d["f_hat"]) < TOL
+    uh = P.biharmonic_solve(d["f_hat"], bases, 2)
+    assert rel(uh, d["u_hat_generic"]) < 1e-12
+    assert rel(P.backward(uh, bases), d["uq"]) < 1e-12
+    if "u_hat_biharmonic" in d:
+        assert rel(uh, d["u_hat_biharmonic"]) < 1e-12
+
+
+@pytest.mark.parametrize("N", [4, 8, 16, 33, 100])
+def test_legendre_nodes(golden, N):
+    d = golden("legendre")
+    x, w = S.leg_lg_points_weights(N)
+    assert rel(x, d[f"xw{N}_x"]) < 1e-15
+    assert rel(w, d[f"xw{N}_w"]) < 1e-13
+
+
+@pytest.mark.parametrize("N", [16, 33, 64])
+@pytest.mark.parametrize("kind", ["recursive", "vandermonde"])
+def test_legendre_1d(golden, N, kind):
+    d = golden("legendre")
+    for tag, b in (("L", "L"), ("LD", "SD")):
+        assert rel(S.leg_scalar_product(d[f"{tag}{N}_f"], b, kind=kind), d[f"{tag}{N}_sp_{kind}"]) < 1e-13
+        assert rel(S.leg_backward(d[f"{tag}{N}_uh"], b, kind=kind), d[f"{tag}{N}_bw_{kind}"]) < 1e-14
+        assert rel(S.leg_forward(d[f"{tag}{N}_f"], b, kind=kind), d[f"{tag}{N}_fw_{kind}"]) < 1e-12
+
+
+def test_legendre_poisson2d(golden):
+    d = golden("legendre")
+    bases = [("fourier", "R2C", 16), ("legendre", "SD", 24)]
+    assert rel(P.scalar_product(d["p2d_fj"], bases, axes=(1, 0)), d["p2d_fhat"]) < 1e-13
+    beta = P.fourier_k2(bases, 1) + 3.0
+    fs, shp = P._systems(d["p2d_fhat"], 1)
+    us = la.leg_helmholtz_solve(fs, np.ones(fs.shape[0]), beta.reshape(-1))
+    assert rel(np.moveaxis(us.reshape(shp), -1, 1), d["p2d_uhat"]) < 1e-13
