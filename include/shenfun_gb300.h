@@ -1,0 +1,135 @@
+/*
+ * shenfun_gb300 C ABI: GB300 (sm_103a) kernels for the tensor-product
+ * spectral-Galerkin forward / banded-solve / backward path of shenfun.
+ *
+ * Conventions
+ *  - Every pointer argument named in/out/u/b/d0/... is a DEVICE pointer to
+ *    C-contiguous FP64 (or interleaved complex FP64) data.  The caller owns all
+ *    memory; no entry point below allocates device memory except
+ *    sgpu_plan_create (tables, once per plan) and sgpu_*_workspace queries
+ *    return sizes the caller allocates.
+ *  - An N-D array is handed over as a 3-D view (outer, n, inner) around the
+ *    axis being transformed or solved: element (o, k, i) lives at
+ *    o*n*inner + k*inner + i.  This covers every axis of a C-contiguous array
+ *    (outer = product of the dims before the axis, inner = after it), which is
+ *    how the reference's `axis` argument is mapped.
+ *  - Scale arrays (alpha, beta) have one entry per system, laid out as
+ *    (outer, inner) - the reference's broadcast shape with the solve axis
+ *    collapsed to 1.
+ *  - Every entry point returns an int status (0 = ok); none throws.  Kernels
+ *    are enqueued on `stream` (0 = legacy default stream) and are asynchronous.
+ *
+ * Each declaration cites the reference (shenfun 4.3.0) interface it replaces;
+ * paths are inside the reference project.
+ */
+#ifndef SHENFUN_GB300_H
+#define SHENFUN_GB300_H
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SGPU_OK 0
+#define SGPU_ERR_ARG 1          /* bad shape / pointer / enum            */
+#define SGPU_ERR_UNSUPPORTED 2  /* valid request this library does not do */
+#define SGPU_ERR_CUDA 3         /* a CUDA runtime call failed            */
+#define SGPU_ERR_NOMEM 4        /* plan tables could not be allocated    */
+#define SGPU_ERR_NONFINITE 5    /* non-finite value detected in input    */
+#define SGPU_ERR_ZERO_PIVOT 6   /* zero pivot in a factorisation         */
+#define SGPU_ERR_TIMEOUT 7      /* a bounded device wait ran out         */
+
+/* data kinds */
+#define SGPU_REAL 0     /* float64                     */
+#define SGPU_COMPLEX 1  /* complex128 (re, im interleaved) */
+
+/* 1D bases of the Chebyshev / Legendre families */
+#define SGPU_BASIS_ORTHO 0  /* T_k (Chebyshev) / L_k (Legendre)        */
+#define SGPU_BASIS_SD 1     /* ShenDirichlet  phi_k = P_k - P_{k+2}    */
+#define SGPU_BASIS_SB 2     /* ShenBiharmonic (chebyshev/bases.py:1249) */
+
+/* transform kinds */
+#define SGPU_XF_R2C 1        /* rfft along axis, n -> n/2+1 (FFTW r2c)             */
+#define SGPU_XF_C2R 2        /* irfft along axis, n/2+1 -> n, unnormalised (c2r)   */
+#define SGPU_XF_C2C_FWD 3    /* fft along axis (FFTW_FORWARD)                      */
+#define SGPU_XF_C2C_BWD 4    /* ifft along axis, unnormalised (FFTW_BACKWARD)      */
+#define SGPU_XF_DCT2 5       /* FFTW REDFT10                                       */
+#define SGPU_XF_DCT3 6       /* FFTW REDFT01                                       */
+#define SGPU_XF_CHEB_SCALAR 7   /* Chebyshev GC scalar product of a basis      */
+#define SGPU_XF_CHEB_FORWARD 8  /* scalar product + inverse mass (forward)     */
+#define SGPU_XF_CHEB_BACKWARD 9 /* to_ortho + GC backward                      */
+
+/* arithmetic form */
+#define SGPU_PLAIN_F64 0   /* all FP64                                        */
+
+const char* sgpu_status_string(int status);
+int sgpu_version(void);
+/* 1 if the library was built with device code for sm_103a and a device is visible */
+int sgpu_device_ok(void);
+
+/* ---- transform plans ----------------------------------------------------
+ * Replace the per-axis serial plan objects created in the bases' plan()
+ * (mpi4py_fft.fftw.dctn/rfftn/irfftn/fftn/ifftn; chebyshev/bases.py:407-469,
+ * fourier/bases.py:218-279) together with the scaling and Shen-stencil work
+ * the reference does around them:
+ *   SGPU_XF_R2C / C2C_FWD   = FourierBase._evaluate_scalar_product (fourier/bases.py:157-162) when scale = 1/n
+ *   SGPU_XF_C2R / C2C_BWD   = R2C/C2C._evaluate_expansion_all (fourier/bases.py:380-407, 526-533)
+ *   SGPU_XF_CHEB_SCALAR     = Orthogonal._evaluate_scalar_product (chebyshev/bases.py:340-347)
+ *                             + CompositeBase._evaluate_scalar_product (spectralbase.py:1462-1474)
+ *   SGPU_XF_CHEB_FORWARD    = SpectralBase.forward (spectralbase.py:235-263), homogeneous BCs
+ *   SGPU_XF_CHEB_BACKWARD   = CompositeBase._evaluate_expansion_all (spectralbase.py:1450-1460)
+ *                             + Orthogonal._evaluate_expansion_all (chebyshev/bases.py:315-329)
+ * `scale` multiplies the result of the raw kinds (1 = FFTW's unnormalised
+ * output); the Chebyshev kinds ignore it (their scaling is the reference's).
+ */
+typedef struct sgpu_plan sgpu_plan;
+int sgpu_plan_create(sgpu_plan** plan, int kind, int n, int basis, int form);
+int sgpu_plan_destroy(sgpu_plan* plan);
+/* in: (outer, n_in, inner), out: (outer, n_out, inner).  data_kind applies to
+ * the Chebyshev/DCT kinds (real or complex lines); Fourier kinds fix it. */
+int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
+                      int64_t inner, int data_kind, double scale, cudaStream_t stream);
+
+/* ---- banded solvers (optimization/cython/la.pyx) ------------------------
+ * TDMA: offsets (-2, 0, 2); data is (3, n): data[0,:-2] = ld, data[1] = d,
+ * data[2,2:] = ud (la.py:331-393).  PDMA: offsets (-4..4) in (5, n) rows
+ * a, b, d, e, f with the same offset convention (la.py:450-543).
+ */
+/* la.pyx:243 TDMA_LU(data) - in place */
+int sgpu_TDMA_LU(double* data, int64_t n, cudaStream_t stream);
+/* la.pyx:77 TDMA_Solve(u, data, axis) + TDMA_inner_solve_ptr (la.pyx:516-532) */
+int sgpu_TDMA_Solve(void* u, const double* data, int64_t outer, int64_t n, int64_t inner,
+                    int data_kind, cudaStream_t stream);
+/* la.pyx:213 PDMA_LU(data) - in place */
+int sgpu_PDMA_LU(double* data, int64_t n, cudaStream_t stream);
+/* la.pyx:61 PDMA_Solve(u, data, axis) + PDMA_inner_solve_ptr (la.pyx:496-514) */
+int sgpu_PDMA_Solve(void* u, const double* data, int64_t outer, int64_t n, int64_t inner,
+                    int data_kind, cudaStream_t stream);
+
+/* ---- Chebyshev Dirichlet Helmholtz (chebyshev/la.py:131-351) -------------
+ * (alfa A + beta B) u = b with A = ASDSD, B = BSDSD of a ShenDirichlet space
+ * of N modes, one system per (outer, inner) index.  Factor arrays d0, d1, d2,
+ * L have the reference's layout (outer, N, inner).  neumann != 0 (ShenNeumann)
+ * returns SGPU_ERR_UNSUPPORTED.
+ */
+/* la.pyx:708 LU_Helmholtz(A, B, As, Bs, neumann, d0, d1, d2, L, axis) */
+int sgpu_LU_Helmholtz(int64_t N, const double* alfa, const double* beta, int neumann,
+                      double* d0, double* d1, double* d2, double* L, int64_t outer,
+                      int64_t inner, cudaStream_t stream);
+/* la.pyx:845 Solve_Helmholtz(b, u, neumann, d0, d1, d2, L, axis) */
+int sgpu_Solve_Helmholtz(const void* b, void* u, int neumann, const double* d0,
+                         const double* d1, const double* d2, const double* L,
+                         int64_t outer, int64_t N, int64_t inner, int data_kind,
+                         cudaStream_t stream);
+/* Matvec.pyx:697 Helmholtz_matvec(v, b, alfa, beta, A, B, axis): b = (alfa A + beta B) v */
+int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa, const double* beta,
+                          int64_t outer, int64_t N, int64_t inner, int data_kind,
+                          cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SHENFUN_GB300_H */

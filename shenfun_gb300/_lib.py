@@ -1,0 +1,83 @@
+"""ctypes binding of the in-tree CUDA library ``libshenfun_gb300.so``.
+
+The library is the product's only compute path: there is no CPU fallback.
+Importing the package does not need a GPU, but any call that would compute
+raises ``SgpuError`` when the library or a CUDA device is missing.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libshenfun_gb300.so")
+
+# status codes (include/shenfun_gb300.h)
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_NONFINITE, ERR_ZERO_PIVOT, ERR_TIMEOUT = range(8)
+REAL, COMPLEX = 0, 1
+BASIS_ORTHO, BASIS_SD, BASIS_SB = 0, 1, 2
+XF_R2C, XF_C2R, XF_C2C_FWD, XF_C2C_BWD, XF_DCT2, XF_DCT3, XF_CHEB_SCALAR, XF_CHEB_FORWARD, \
+    XF_CHEB_BACKWARD = range(1, 10)
+PLAIN_F64 = 0
+
+
+class SgpuError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        msg = _status_string(status)
+        super().__init__(f"{where}: {msg} (status {status})" if where else msg)
+
+
+_lib = None
+
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+_vp = ctypes.c_void_p
+_dbl = ctypes.c_double
+
+# name: (restype, argtypes)
+SIGNATURES = {
+    "sgpu_status_string": (ctypes.c_char_p, [_int]),
+    "sgpu_version": (_int, []),
+    "sgpu_device_ok": (_int, []),
+    "sgpu_plan_create": (_int, [ctypes.POINTER(_vp), _int, _int, _int, _int]),
+    "sgpu_plan_destroy": (_int, [_vp]),
+    "sgpu_plan_execute": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp]),
+    "sgpu_TDMA_LU": (_int, [_vp, _i64, _vp]),
+    "sgpu_TDMA_Solve": (_int, [_vp, _vp, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_PDMA_LU": (_int, [_vp, _i64, _vp]),
+    "sgpu_PDMA_Solve": (_int, [_vp, _vp, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_LU_Helmholtz": (_int, [_i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _i64, _i64, _vp]),
+    "sgpu_Solve_Helmholtz": (_int, [_vp, _vp, _int, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_Helmholtz_matvec": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
+}
+
+
+def _status_string(status):
+    if _lib is not None:
+        return _lib.sgpu_status_string(status).decode()
+    return f"status {status}"
+
+
+def load(path=LIB_PATH):
+    """Load the library (once) and declare every exported signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise SgpuError(ERR_UNSUPPORTED,
+                        f"CUDA library not built ({path}); run shenfun_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def call(name, *args):
+    """Call an entry point and raise on a non-zero status."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != OK:
+        raise SgpuError(st, name)
+    return st

@@ -1,0 +1,5 @@
+"""Chebyshev namespace mirroring ``shenfun.chebyshev`` (bases + la)."""
+from ..spaces import (ChebyshevOrthogonal as Orthogonal,  # noqa: F401
+                      ChebyshevShenDirichlet as ShenDirichlet,
+                      ChebyshevShenBiharmonic as ShenBiharmonic)
+from . import la  # noqa: F401

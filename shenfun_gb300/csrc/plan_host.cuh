@@ -1,0 +1,278 @@
+// Host-side construction of a LinePlan and its tables (twiddles, Rader
+// permutations and kernel spectrum, DCT post-twiddles, Shen stencil rows and
+// the LU'd mass bands).  Used by sgpu_plan_create (which uploads the tables)
+// and by the CPU index-check harness (which keeps them in host memory).
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fft_line.cuh"
+
+namespace sgpu {
+
+struct HostTables {
+  std::vector<cd> tw, rk, post;
+  std::vector<int> rin, rout;
+  std::vector<double> mass, sten;
+};
+
+namespace planhost {
+
+typedef long double ld_t;
+const ld_t kPi = 3.141592653589793238462643383279502884L;
+
+bool is_prime(int n) {
+  if (n < 2) return false;
+  for (int d = 2; d * d <= n; ++d)
+    if (n % d == 0) return false;
+  return true;
+}
+
+int powmod(long long b, long long e, long long m) {
+  long long r = 1 % m;
+  b %= m;
+  while (e > 0) {
+    if (e & 1) r = r * b % m;
+    b = b * b % m;
+    e >>= 1;
+  }
+  return (int)r;
+}
+
+int primitive_root(int p) {
+  std::vector<int> qs;
+  int phi = p - 1, x = phi;
+  for (int d = 2; d * d <= x; ++d)
+    if (x % d == 0) {
+      qs.push_back(d);
+      while (x % d == 0) x /= d;
+    }
+  if (x > 1) qs.push_back(x);
+  for (int g = 2; g < p; ++g) {
+    bool ok = true;
+    for (int q : qs)
+      if (powmod(g, phi / q, p) == 1) {
+        ok = false;
+        break;
+      }
+    if (ok) return g;
+  }
+  return -1;
+}
+
+// radix sequence for a length-m Stockham FFT: 4s first, then 2, 3, 5, then
+// remaining primes through the generic radix.
+bool factorize(int m, int* radix, int* ns) {
+  int k = 0;
+  while (m % 4 == 0) {
+    radix[k++] = 4;
+    m /= 4;
+  }
+  const int small[3] = {2, 3, 5};
+  for (int r : small)
+    while (m % r == 0) {
+      radix[k++] = r;
+      m /= r;
+    }
+  for (int p = 7; m > 1; p += 2) {
+    while (m % p == 0) {
+      if (p > SGPU_MAX_GENERIC_RADIX || k >= SGPU_MAX_STAGES) return false;
+      radix[k++] = p;
+      m /= p;
+    }
+  }
+  *ns = k;
+  return k <= SGPU_MAX_STAGES;
+}
+
+}  // namespace planhost
+
+
+// Fill p (device pointers left null) and the host tables; returns a status.
+inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, HostTables& T) {
+  using namespace planhost;
+  if (n < 2 || n > (1 << 20)) return SGPU_ERR_ARG;
+  if (kind < SGPU_XF_R2C || kind > SGPU_XF_CHEB_BACKWARD) return SGPU_ERR_ARG;
+  if (form != SGPU_PLAIN_F64) return SGPU_ERR_UNSUPPORTED;
+  const bool cheb = kind >= SGPU_XF_DCT2;
+  const bool composite = kind >= SGPU_XF_CHEB_SCALAR;
+  if (composite && (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SB)) return SGPU_ERR_ARG;
+  if (composite && n < 2 + 2 * basis_nbcs(basis)) return SGPU_ERR_ARG;
+  std::memset(&p, 0, sizeof(p));
+  p.kind = kind;
+  p.basis = composite ? basis : SGPU_BASIS_ORTHO;
+  p.n = n;
+  p.n_in = (kind == SGPU_XF_C2R) ? n / 2 + 1 : n;
+  p.n_out = (kind == SGPU_XF_R2C) ? n / 2 + 1 : n;
+  p.rader = (is_prime(n) && n >= 11) ? 1 : 0;
+  p.m = p.rader ? n - 1 : n;
+  if (!factorize(p.m, p.radix, &p.nstages)) return SGPU_ERR_UNSUPPORTED;
+  p.ld = n;  // >= m
+  p.nthreads = 256;
+  // lines per CTA: X, A, B line buffers within ~96 KB of shared memory
+  const size_t per_line = 3 * sizeof(cd) * (size_t)p.ld + 2 * sizeof(cd);
+  int tlc = (int)((96 * 1024) / per_line);
+  if (tlc > 16) tlc = 16;
+  if (tlc < 1) tlc = 1;
+  p.tlc = tlc;
+  p.smem = smem_bytes<double>(p.tlc, p.ld);
+  if (p.smem > 220 * 1024) return SGPU_ERR_UNSUPPORTED;
+
+  // ---- host tables -------------------------------------------------------
+  const int m = p.m;
+  std::vector<cd>& tw = T.tw;
+  std::vector<cd>& rk = T.rk;
+  std::vector<cd>& post = T.post;
+  std::vector<int>& rin = T.rin;
+  std::vector<int>& rout = T.rout;
+  std::vector<double>& mass = T.mass;
+  std::vector<double>& sten = T.sten;
+  tw.resize(m);
+  for (int e = 0; e < m; ++e) {
+    ld_t a = -2 * kPi * (ld_t)e / (ld_t)m;
+    tw[e] = cx<double>((double)cosl(a), (double)sinl(a));
+  }
+  if (p.rader) {
+    const int g = primitive_root(n);
+    const int ginv = powmod(g, n - 2, n);
+    rin.resize(m);
+    rout.resize(m);
+    for (int q = 0; q < m; ++q) {
+      rin[q] = powmod(g, q, n);
+      rout[q] = powmod(ginv, q, n);
+    }
+    // rk = DFT_m(b) / m with b_q = exp(-2 pi i ginv^q / n)
+    std::vector<ld_t> br(m), bi(m);
+    for (int q = 0; q < m; ++q) {
+      ld_t a = -2 * kPi * (ld_t)rout[q] / (ld_t)n;
+      br[q] = cosl(a);
+      bi[q] = sinl(a);
+    }
+    rk.resize(m);
+    for (int s = 0; s < m; ++s) {
+      ld_t sr = 0, si = 0;
+      for (int q = 0; q < m; ++q) {
+        long long e = (long long)q * s % m;
+        ld_t a = -2 * kPi * (ld_t)e / (ld_t)m;
+        ld_t c = cosl(a), sn = sinl(a);
+        sr += br[q] * c - bi[q] * sn;
+        si += br[q] * sn + bi[q] * c;
+      }
+      rk[s] = cx<double>((double)(sr / m), (double)(si / m));
+    }
+  }
+  if (cheb) {
+    post.resize(n);
+    for (int k = 0; k < n; ++k) {
+      ld_t a = -kPi * (ld_t)k / (ld_t)(2 * n);
+      post[k] = cx<double>((double)cosl(a), (double)sinl(a));
+    }
+  }
+  if (p.basis == SGPU_BASIS_SB) {
+    // K2(k) = -(2k+4)/(k+3), K4(k) = (k+1)/(k+3), zero for k >= n-4
+    sten.assign(2 * (size_t)n, 0.0);
+    for (int k = 0; k < n - 4; ++k) {
+      sten[k] = -(2.0 * k + 4) / (k + 3.0);
+      sten[n + k] = (k + 1.0) / (k + 3.0);
+    }
+  }
+  if (kind == SGPU_XF_CHEB_FORWARD) {
+    // Chebyshev mass matrices (chebyshev/matrices.py:238-246, :515-528), LU'd
+    // as la.pyx:213-252 do, diagonal row replaced by its reciprocal.
+    const double pi = 3.14159265358979323846;
+    std::vector<double> h(n, pi / 2);
+    h[0] = pi;
+    if (p.basis == SGPU_BASIS_ORTHO) {
+      mass.resize(n);
+      for (int k = 0; k < n; ++k) mass[k] = 1.0 / h[k];
+    } else if (p.basis == SGPU_BASIS_SD) {
+      const int dim = n - 2;
+      mass.assign(3 * (size_t)dim, 0.0);
+      double* ldg = &mass[0];
+      double* d = &mass[dim];
+      double* ud = &mass[2 * dim + 2];
+      for (int k = 0; k < dim; ++k) d[k] = h[k] + h[k + 2];
+      for (int k = 0; k < dim - 2; ++k) ldg[k] = ud[k] = -h[1];
+      for (int i = 2; i < dim; ++i) {
+        ldg[i - 2] = ldg[i - 2] / d[i - 2];
+        d[i] = d[i] - ldg[i - 2] * ud[i - 2];
+      }
+      for (int k = 0; k < dim; ++k) d[k] = 1.0 / d[k];
+    } else {
+      const int dim = n - 4;
+      std::vector<double> K2(n, 0.0), K4(n, 0.0);
+      for (int k = 0; k < n - 4; ++k) {
+        K2[k] = -(2.0 * k + 4) / (k + 3.0);
+        K4[k] = (k + 1.0) / (k + 3.0);
+      }
+      mass.assign(5 * (size_t)dim, 0.0);
+      double* a = &mass[0];
+      double* b = &mass[dim];
+      double* d = &mass[2 * dim];
+      double* e = &mass[3 * dim + 2];
+      double* f = &mass[4 * dim + 4];
+      for (int k = 0; k < dim; ++k) d[k] = h[k] + h[k + 2] * K2[k] * K2[k] + h[k + 4] * K4[k] * K4[k];
+      for (int k = 0; k < dim - 2; ++k)
+        b[k] = e[k] = h[k + 2] * K2[k] + h[k + 4] * K4[k] * K2[k + 2];
+      for (int k = 0; k < dim - 4; ++k) a[k] = f[k] = h[k + 4] * K4[k];
+      const int kk = 2;
+      for (int i = 0; i < dim - 2 * kk; ++i) {
+        double lam = b[i] / d[i];
+        d[i + kk] -= lam * e[i];
+        e[i + kk] -= lam * f[i];
+        b[i] = lam;
+        lam = a[i] / d[i];
+        b[i + kk] -= lam * e[i];
+        d[i + 2 * kk] -= lam * f[i];
+        a[i] = lam;
+      }
+      for (int i = dim - 4; i <= dim - 3; ++i) {
+        double lam = b[i] / d[i];
+        d[i + kk] -= lam * e[i];
+        b[i] = lam;
+      }
+      for (int k = 0; k < dim; ++k) d[k] = 1.0 / d[k];
+    }
+  }
+
+  return SGPU_OK;
+}
+
+// Point a plan's table pointers into one contiguous table image at `base`
+// (device or host); `offsets` receives the byte layout.  Returns total bytes.
+inline size_t table_layout(const HostTables& T, size_t off[7]) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t sz = 0;
+  off[0] = sz; sz += al(sizeof(cd) * T.tw.size());
+  off[1] = sz; sz += al(sizeof(cd) * T.rk.size());
+  off[2] = sz; sz += al(sizeof(int) * T.rin.size());
+  off[3] = sz; sz += al(sizeof(int) * T.rout.size());
+  off[4] = sz; sz += al(sizeof(cd) * T.post.size());
+  off[5] = sz; sz += al(sizeof(double) * T.mass.size());
+  off[6] = sz; sz += al(sizeof(double) * T.sten.size());
+  return sz;
+}
+
+inline void table_image(const HostTables& T, const size_t off[7], unsigned char* img) {
+  if (!T.tw.empty()) std::memcpy(img + off[0], T.tw.data(), sizeof(cd) * T.tw.size());
+  if (!T.rk.empty()) std::memcpy(img + off[1], T.rk.data(), sizeof(cd) * T.rk.size());
+  if (!T.rin.empty()) std::memcpy(img + off[2], T.rin.data(), sizeof(int) * T.rin.size());
+  if (!T.rout.empty()) std::memcpy(img + off[3], T.rout.data(), sizeof(int) * T.rout.size());
+  if (!T.post.empty()) std::memcpy(img + off[4], T.post.data(), sizeof(cd) * T.post.size());
+  if (!T.mass.empty()) std::memcpy(img + off[5], T.mass.data(), sizeof(double) * T.mass.size());
+  if (!T.sten.empty()) std::memcpy(img + off[6], T.sten.data(), sizeof(double) * T.sten.size());
+}
+
+inline void bind_tables(LinePlan& p, const HostTables& T, const size_t off[7], unsigned char* b) {
+  p.tw = (const cd*)(b + off[0]);
+  p.rk = T.rk.empty() ? nullptr : (const cd*)(b + off[1]);
+  p.rin = T.rin.empty() ? nullptr : (const int*)(b + off[2]);
+  p.rout = T.rout.empty() ? nullptr : (const int*)(b + off[3]);
+  p.post = T.post.empty() ? nullptr : (const cd*)(b + off[4]);
+  p.mass = T.mass.empty() ? nullptr : (const double*)(b + off[5]);
+  p.sten = T.sten.empty() ? nullptr : (const double*)(b + off[6]);
+}
+
+}  // namespace sgpu

@@ -1,0 +1,141 @@
+// C ABI of the batched banded solvers (see solvers.cuh for the algorithms).
+#include "solvers.cuh"
+
+using namespace sgpu;
+
+namespace {
+
+const int kThreads = 128;
+
+inline int finish() {
+  return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
+}
+
+inline unsigned nblk(int64_t nsys) { return (unsigned)((nsys + kThreads - 1) / kThreads); }
+
+}  // namespace
+
+__global__ void k_tdma_lu(double* data, int64_t n) { tdma_lu_prog(data, n); }
+__global__ void k_pdma_lu(double* data, int64_t n) { pdma_lu_prog(data, n); }
+
+template <class T>
+__global__ void k_tdma_solve(T* u, const double* data, int64_t n, int64_t inner, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) tdma_solve_prog<T>(u, data, n, inner, s);
+}
+
+template <class T>
+__global__ void k_pdma_solve(T* u, const double* data, int64_t n, int64_t inner, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) pdma_solve_prog<T>(u, data, n, inner, s);
+}
+
+__global__ void k_helmholtz_lu(int64_t N, const double* alfa, const double* beta, double* d0,
+                               double* d1, double* d2, double* L, int64_t inner, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) helmholtz_lu_prog(N, alfa, beta, d0, d1, d2, L, inner, s);
+}
+
+template <class T>
+__global__ void k_helmholtz_solve(const T* b, T* u, const double* d0, const double* d1,
+                                  const double* d2, const double* L, int64_t N, int64_t inner,
+                                  int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) helmholtz_solve_prog<T>(b, u, d0, d1, d2, L, N, inner, s);
+}
+
+template <class T>
+__global__ void k_helmholtz_matvec(const T* v, T* b, const double* alfa, const double* beta,
+                                   int64_t N, int64_t inner, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) helmholtz_matvec_prog<T>(v, b, alfa, beta, N, inner, s);
+}
+
+extern "C" int sgpu_TDMA_LU(double* data, int64_t n, cudaStream_t stream) {
+  if (!data || n < 3) return SGPU_ERR_ARG;
+  k_tdma_lu<<<1, 1, 0, stream>>>(data, n);
+  return finish();
+}
+
+extern "C" int sgpu_PDMA_LU(double* data, int64_t n, cudaStream_t stream) {
+  if (!data || n < 5) return SGPU_ERR_ARG;
+  k_pdma_lu<<<1, 1, 0, stream>>>(data, n);
+  return finish();
+}
+
+extern "C" int sgpu_TDMA_Solve(void* u, const double* data, int64_t outer, int64_t n,
+                               int64_t inner, int data_kind, cudaStream_t stream) {
+  if (!u || !data || n < 3 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_tdma_solve<cd><<<nblk(nsys), kThreads, 0, stream>>>((cd*)u, data, n, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_tdma_solve<double><<<nblk(nsys), kThreads, 0, stream>>>((double*)u, data, n, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+extern "C" int sgpu_PDMA_Solve(void* u, const double* data, int64_t outer, int64_t n,
+                               int64_t inner, int data_kind, cudaStream_t stream) {
+  if (!u || !data || n < 5 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_pdma_solve<cd><<<nblk(nsys), kThreads, 0, stream>>>((cd*)u, data, n, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_pdma_solve<double><<<nblk(nsys), kThreads, 0, stream>>>((double*)u, data, n, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+extern "C" int sgpu_LU_Helmholtz(int64_t N, const double* alfa, const double* beta, int neumann,
+                                 double* d0, double* d1, double* d2, double* L, int64_t outer,
+                                 int64_t inner, cudaStream_t stream) {
+  if (neumann) return SGPU_ERR_UNSUPPORTED;
+  if (!alfa || !beta || !d0 || !d1 || !d2 || !L || N < 8 || outer < 0 || inner < 1)
+    return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  k_helmholtz_lu<<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, d0, d1, d2, L, inner, nsys);
+  return finish();
+}
+
+extern "C" int sgpu_Solve_Helmholtz(const void* b, void* u, int neumann, const double* d0,
+                                    const double* d1, const double* d2, const double* L,
+                                    int64_t outer, int64_t N, int64_t inner, int data_kind,
+                                    cudaStream_t stream) {
+  if (neumann) return SGPU_ERR_UNSUPPORTED;
+  if (!b || !u || !d0 || !d1 || !d2 || !L || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_helmholtz_solve<cd><<<nblk(nsys), kThreads, 0, stream>>>((const cd*)b, (cd*)u, d0, d1, d2, L,
+                                                               N, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_helmholtz_solve<double><<<nblk(nsys), kThreads, 0, stream>>>(
+        (const double*)b, (double*)u, d0, d1, d2, L, N, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+extern "C" int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa,
+                                     const double* beta, int64_t outer, int64_t N, int64_t inner,
+                                     int data_kind, cudaStream_t stream) {
+  if (!v || !b || !alfa || !beta || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  if (v == b) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_helmholtz_matvec<cd><<<nblk(nsys), kThreads, 0, stream>>>((const cd*)v, (cd*)b, alfa, beta,
+                                                                N, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_helmholtz_matvec<double><<<nblk(nsys), kThreads, 0, stream>>>(
+        (const double*)v, (double*)b, alfa, beta, N, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}

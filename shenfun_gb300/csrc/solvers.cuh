@@ -1,0 +1,217 @@
+// Batched banded solvers, one system per (outer, inner) index of a
+// (outer, n, inner) array: TDMA / PDMA (la.pyx:213-252, 496-532) and the
+// Chebyshev Dirichlet Helmholtz LU / solve / matvec (la.pyx:717-912,
+// Matvec.pyx:656-695).  One thread owns one system and runs the reference's
+// sequential recurrence, so the per-system operation order follows the
+// reference.  With inner > 1 consecutive threads own consecutive systems and
+// every step of the recurrence is a coalesced row access.
+#pragma once
+
+#include "sgpu_common.cuh"
+
+namespace sgpu {
+
+SGPU_HD double mulr(double a, double s) { return a * s; }
+SGPU_HD cd mulr(cd a, double s) { return scale(a, s); }
+SGPU_HD double zero_of(double) { return 0.0; }
+SGPU_HD cd zero_of(cd) { return cx<double>(0.0, 0.0); }
+
+// strided line view: element k of system s
+template <class T>
+struct Line {
+  T* base;
+  int64_t st;
+  SGPU_HD T& operator[](int64_t k) const { return base[k * st]; }
+};
+
+SGPU_HD int64_t sys_base(int64_t s, int64_t n, int64_t inner) {
+  int64_t o = s / inner, i = s - o * inner;
+  return o * n * inner + i;
+}
+
+// ---- TDMA / PDMA ----------------------------------------------------------
+SGPU_HD void tdma_lu_prog(double* data, int64_t n) {
+  double* ld = data;
+  double* d = data + n;
+  double* ud = data + 2 * n + 2;
+  for (int64_t i = 2; i < n; ++i) {
+    ld[i - 2] = ld[i - 2] / d[i - 2];
+    d[i] = d[i] - ld[i - 2] * ud[i - 2];
+  }
+}
+
+template <class T>
+SGPU_HD void tdma_solve_prog(T* u_all, const double* data, int64_t n, int64_t inner, int64_t s) {
+  Line<T> u{u_all + sys_base(s, n, inner), inner};
+  const double* ld = data;
+  const double* d = data + n;
+  const double* ud = data + 2 * n + 2;
+  for (int64_t i = 2; i < n; ++i) u[i] = u[i] - mulr(u[i - 2], ld[i - 2]);
+  u[n - 1] = mulr(u[n - 1], 1.0 / d[n - 1]);
+  u[n - 2] = mulr(u[n - 2], 1.0 / d[n - 2]);
+  for (int64_t i = n - 3; i >= 0; --i) u[i] = mulr(u[i] - mulr(u[i + 2], ud[i]), 1.0 / d[i]);
+}
+
+SGPU_HD void pdma_lu_prog(double* data, int64_t n) {
+  double* a = data;
+  double* b = data + n;
+  double* d = data + 2 * n;
+  double* e = data + 3 * n + 2;
+  double* f = data + 4 * n + 4;
+  const int64_t k = 2;
+  for (int64_t i = 0; i < n - 2 * k; ++i) {
+    double lam = b[i] / d[i];
+    d[i + k] -= lam * e[i];
+    e[i + k] -= lam * f[i];
+    b[i] = lam;
+    lam = a[i] / d[i];
+    b[i + k] -= lam * e[i];
+    d[i + 2 * k] -= lam * f[i];
+    a[i] = lam;
+  }
+  for (int64_t i = n - 4; i <= n - 3; ++i) {
+    double lam = b[i] / d[i];
+    d[i + k] -= lam * e[i];
+    b[i] = lam;
+  }
+}
+
+template <class T>
+SGPU_HD void pdma_solve_prog(T* u_all, const double* data, int64_t n, int64_t inner, int64_t s) {
+  Line<T> u{u_all + sys_base(s, n, inner), inner};
+  const double* a = data;
+  const double* b = data + n;
+  const double* d = data + 2 * n;
+  const double* e = data + 3 * n + 2;
+  const double* f = data + 4 * n + 4;
+  u[2] = u[2] - mulr(u[0], b[0]);
+  u[3] = u[3] - mulr(u[1], b[1]);
+  for (int64_t k = 4; k < n; ++k) u[k] = u[k] - (mulr(u[k - 2], b[k - 2]) + mulr(u[k - 4], a[k - 4]));
+  u[n - 1] = mulr(u[n - 1], 1.0 / d[n - 1]);
+  u[n - 2] = mulr(u[n - 2], 1.0 / d[n - 2]);
+  u[n - 3] = mulr(u[n - 3] - mulr(u[n - 1], e[n - 3]), 1.0 / d[n - 3]);
+  u[n - 4] = mulr(u[n - 4] - mulr(u[n - 2], e[n - 4]), 1.0 / d[n - 4]);
+  for (int64_t k = n - 5; k >= 0; --k)
+    u[k] = mulr(u[k] - mulr(u[k + 2], e[k]) - mulr(u[k + 4], f[k]), 1.0 / d[k]);
+}
+
+// ---- Chebyshev Dirichlet Helmholtz ---------------------------------------
+// ASDSD / BSDSD coefficients in the reference's evaluation order
+// (chebyshev/matrices.py:1061-1079, :238-246).
+SGPU_HD double hA0(int64_t k) { return ((-2.0 * 3.141592653589793) * (k + 1.0)) * (k + 2.0); }
+SGPU_HD double hA2(int64_t k) { return (-4.0 * 3.141592653589793) * (k + 1.0); }
+SGPU_HD double hB0(int64_t k) { return k == 0 ? 3.141592653589793 + 1.5707963267948966 : 3.141592653589793; }
+SGPU_HD double hB2() { return -1.5707963267948966; }
+
+// LU_Helmholtz_1D (la.pyx:717-763); N = number of basis functions, the
+// factor lines have N entries with the last two untouched.
+SGPU_HD void helmholtz_lu_prog(int64_t N, const double* alfa, const double* beta, double* d0_all,
+                               double* d1_all, double* d2_all, double* L_all, int64_t inner,
+                               int64_t s) {
+  const int64_t b0 = sys_base(s, N, inner);
+  Line<double> d0{d0_all + b0, inner}, d1{d1_all + b0, inner}, d2{d2_all + b0, inner},
+      L{L_all + b0, inner};
+  const double a = alfa[s], b = beta[s];
+  const int64_t M = N - 2;
+  d0[0] = a * hA0(0) + b * hB0(0);
+  d0[1] = a * hA0(1) + b * hB0(1);
+  d1[0] = a * hA2(0) + b * hB2();
+  d1[1] = a * hA2(1) + b * hB2();
+  d2[0] = a * hA2(0);
+  d2[1] = a * hA2(1);
+  for (int64_t i = 2; i < M; ++i) {
+    double l = b * hB2() / d0[i - 2];
+    L[i - 2] = l;
+    d0[i] = a * hA0(i) + b * hB0(i) - l * d1[i - 2];
+    if (i < M - 2) d1[i] = a * hA2(i) + b * hB2() - l * d2[i - 2];
+    if (i < M - 4) d2[i] = a * hA2(i) - l * d2[i - 2];
+  }
+}
+
+// Solve_Helmholtz_1D_ptr (la.pyx:871-912).  y is kept in u.
+template <class T>
+SGPU_HD void helmholtz_solve_prog(const T* b_all, T* u_all, const double* d0_all,
+                                  const double* d1_all, const double* d2_all, const double* L_all,
+                                  int64_t Nb, int64_t inner, int64_t s) {
+  const int64_t b0 = sys_base(s, Nb, inner);
+  Line<const T> f{b_all + b0, inner};
+  Line<T> u{u_all + b0, inner};
+  Line<const double> d0{d0_all + b0, inner}, d1{d1_all + b0, inner}, d2{d2_all + b0, inner},
+      L{L_all + b0, inner};
+  const int64_t N = Nb - 2;
+  T y0 = f[0], y1 = f[1];
+  u[0] = y0;
+  u[1] = y1;
+  for (int64_t i = 2; i < N; ++i) {
+    T y = f[i] - mulr(y0, L[i - 2]);
+    u[i] = y;
+    y0 = y1;
+    y1 = y;
+  }
+  T un1 = mulr(u[N - 1], 1.0 / d0[N - 1]);
+  T un2 = mulr(u[N - 2], 1.0 / d0[N - 2]);
+  u[N - 1] = un1;
+  u[N - 2] = un2;
+  T un3 = mulr(u[N - 3] - mulr(un1, d1[N - 3]), 1.0 / d0[N - 3]);
+  T un4 = mulr(u[N - 4] - mulr(un2, d1[N - 4]), 1.0 / d0[N - 4]);
+  u[N - 3] = un3;
+  u[N - 4] = un4;
+  // running state: u[i+2], u[i+4] of each parity
+  T se = zero_of(T()), so = zero_of(T());
+  T up2 = un3, up4 = un1;  // parity of N-5: u[N-3], u[N-1]
+  T uq2 = un4, uq4 = un2;  // other parity: u[N-4], u[N-2]
+  for (int64_t i = N - 5; i >= 0; --i) {
+    T ui = u[i] - mulr(up2, d1[i]);
+    if (i % 2 == 0) {
+      se = se + up4;
+      ui = ui - mulr(se, d2[i]);
+    } else {
+      so = so + up4;
+      ui = ui - mulr(so, d2[i]);
+    }
+    ui = mulr(ui, 1.0 / d0[i]);
+    u[i] = ui;
+    // shift: the next i (i-1) has the other parity
+    T t2 = uq2, t4 = uq4;
+    uq4 = up2;
+    uq2 = ui;
+    up2 = t2;
+    up4 = t4;
+  }
+}
+
+// Helmholtz_matvec_ptr (Matvec.pyx:656-695): b = (alfa A + beta B) v, tail zero.
+template <class T>
+SGPU_HD void helmholtz_matvec_prog(const T* v_all, T* b_all, const double* alfa,
+                                   const double* beta, int64_t Nb, int64_t inner, int64_t s) {
+  const int64_t b0 = sys_base(s, Nb, inner);
+  Line<const T> v{v_all + b0, inner};
+  Line<T> b{b_all + b0, inner};
+  const int64_t M = Nb - 2;
+  const double alf = alfa[s], bet = beta[s];
+  const double h = 1.5707963267948966;
+  int64_t k = M - 1;
+  b[k] = mulr(v[k], hA0(k) * alf + hB0(k) * bet) - mulr(v[k - 2], h * bet);
+  b[k - 1] = mulr(v[k - 1], hA0(k - 1) * alf + hB0(k - 1) * bet) - mulr(v[k - 3], h * bet);
+  T s1 = zero_of(T()), s2 = zero_of(T());
+  for (k = M - 3; k > 1; --k) {
+    double p = hA2(k) * alf;
+    if (k % 2 == 0) {
+      s2 = s2 + v[k + 2];
+      b[k] = mulr(v[k], hA0(k) * alf + hB0(k) * bet) - mulr(v[k - 2] + v[k + 2], h * bet) + mulr(s2, p);
+    } else {
+      s1 = s1 + v[k + 2];
+      b[k] = mulr(v[k], hA0(k) * alf + hB0(k) * bet) - mulr(v[k - 2] + v[k + 2], h * bet) + mulr(s1, p);
+    }
+  }
+  k = 1;
+  s1 = s1 + v[k + 2];
+  s2 = s2 + v[k + 1];
+  b[k] = mulr(v[k], hA0(k) * alf + hB0(k) * bet) - mulr(v[k + 2], h * bet) + mulr(s1, hA2(k) * alf);
+  b[k - 1] = mulr(v[k - 1], hA0(k - 1) * alf + hB0(k - 1) * bet) - mulr(v[k + 1], h * bet) +
+             mulr(s2, hA2(k - 1) * alf);
+  b[M] = zero_of(T());
+  b[M + 1] = zero_of(T());
+}
+
+}  // namespace sgpu

@@ -1,0 +1,294 @@
+"""Forms API on the GPU path: Array/Function, Test/TrialFunction, div/grad/Dx,
+inner and project (forms/arguments.py, forms/inner.py, forms/project.py).
+
+Only what the hot path needs is provided: linear forms ``inner(v, Array)``
+(the scalar product transform) and bilinear forms built from constant
+multiples of derivatives of the trial function, which assemble into
+``TPMatrix`` objects with per-wavenumber scale arrays (the reference's
+``get_simplified_tpmatrices`` result, matrixbase.py:1648-1678).
+"""
+import numbers
+
+import numpy as np
+import torch
+
+from .spaces import TensorProductSpace, FourierBase, SpectralBase
+from . import matrices as M
+
+
+# ---------------------------------------------------------------------------
+class _ShenfunArray(torch.Tensor):
+    """torch.Tensor subclass bound to a function space (DistArray analogue)."""
+
+    _space = None
+
+    @staticmethod
+    def _new(cls, space, data):
+        obj = torch.Tensor._make_subclass(cls, data, False)
+        obj._space = space
+        return obj
+
+    def function_space(self):
+        return self._space
+
+    @property
+    def v(self):
+        return self.as_subclass(torch.Tensor)
+
+    def __array__(self, dtype=None):
+        a = self.detach().cpu().as_subclass(torch.Tensor).numpy()
+        return a.astype(dtype) if dtype is not None else a
+
+    @classmethod
+    def __torch_function__(cls, func, types, args=(), kwargs=None):
+        # results of torch ops are plain tensors (no space attached)
+        kwargs = kwargs or {}
+        with torch._C.DisableTorchFunctionSubclass():
+            return func(*args, **kwargs)
+
+
+def _fill(space, forward_output, val, buffer):
+    shape = space.shape(forward_output)
+    dt = space.torch_dtype(forward_output) if isinstance(space, TensorProductSpace) else \
+        (torch.complex128 if (forward_output and isinstance(space, FourierBase)) else torch.float64)
+    t = torch.empty(shape, dtype=dt, device="cuda")
+    if buffer is None:
+        t.fill_(val)
+        return t, None
+    if hasattr(buffer, "free_symbols"):
+        return t, buffer  # sympy expression: evaluate on the mesh
+    src = torch.as_tensor(np.asarray(buffer)) if not isinstance(buffer, torch.Tensor) else buffer
+    t.copy_(src.to(device="cuda", dtype=dt).reshape(shape))
+    return t, None
+
+
+def _eval_sympy(space, expr):
+    import sympy as sp
+    syms = sorted(expr.free_symbols, key=lambda s: "xyzrs".index(str(s)))
+    mesh = space.mesh() if isinstance(space, TensorProductSpace) else [space.mesh()]
+    args = [mesh["xyzrs".index(str(s))] for s in syms]
+    vals = sp.lambdify(syms, expr, "numpy")(*args)
+    return np.broadcast_to(vals, space.shape(False)).astype(float)
+
+
+class Array(_ShenfunArray):
+    """Physical-space values on the quadrature mesh (forms/arguments.py:1891)."""
+
+    def __new__(cls, space, val=0, buffer=None):
+        t, sym = _fill(space, False, val, buffer)
+        if sym is not None:
+            t.copy_(torch.as_tensor(_eval_sympy(space, sym), device="cuda"))
+        return _ShenfunArray._new(cls, space, t)
+
+    def forward(self, output_array=None, kind=None):
+        if output_array is None:
+            output_array = Function(self._space)
+        self._space.forward(self.v, output_array.v if isinstance(output_array, _ShenfunArray) else output_array)
+        return output_array
+
+
+class Function(_ShenfunArray):
+    """Spectral expansion coefficients (forms/arguments.py:1427)."""
+
+    def __new__(cls, space, val=0, buffer=None):
+        t, sym = _fill(space, True, val, buffer)
+        obj = _ShenfunArray._new(cls, space, t)
+        if sym is not None:
+            a = Array(space, buffer=sym)
+            a.forward(obj)
+        return obj
+
+    def backward(self, output_array=None, kind=None, mesh=None):
+        if output_array is None:
+            output_array = Array(self._space)
+        self._space.backward(self.v, output_array.v if isinstance(output_array, _ShenfunArray) else output_array)
+        return output_array
+
+
+# ---------------------------------------------------------------------------
+class Expr:
+    """Linear combination of derivatives of a basis function:
+    terms = [(coefficient, derivative order per axis)]."""
+
+    def __init__(self, basis, terms):
+        self.basis = basis
+        self.terms = list(terms)
+
+    def function_space(self):
+        return self.basis.function_space()
+
+    def __add__(self, other):
+        other = _as_expr(other)
+        assert other.basis is self.basis or other.basis.space is self.basis.space
+        return Expr(self.basis, self.terms + other.terms)
+
+    def __sub__(self, other):
+        return self + (-_as_expr(other))
+
+    def __neg__(self):
+        return Expr(self.basis, [(-c, d) for c, d in self.terms])
+
+    def __mul__(self, a):
+        if not isinstance(a, numbers.Number):
+            return NotImplemented
+        return Expr(self.basis, [(a * c, d) for c, d in self.terms])
+
+    __rmul__ = __mul__
+
+
+class BasisFunction(Expr):
+    def __init__(self, space, argument):
+        self.space = space
+        self.argument = argument
+        nd = space.dimensions if isinstance(space, TensorProductSpace) else 1
+        Expr.__init__(self, self, [(1.0, (0,) * nd)])
+
+    def function_space(self):
+        return self.space
+
+
+def TestFunction(space):
+    return BasisFunction(space, 0)
+
+
+def TrialFunction(space):
+    return BasisFunction(space, 1)
+
+
+def _as_expr(e):
+    if isinstance(e, Expr):
+        return e
+    raise TypeError(f"cannot use {type(e)} in a form")
+
+
+def Dx(e, axis=0, k=1):
+    e = _as_expr(e)
+    out = []
+    for c, d in e.terms:
+        d = list(d)
+        d[axis] += k
+        out.append((c, tuple(d)))
+    return Expr(e.basis, out)
+
+
+class _Grad:
+    def __init__(self, e):
+        self.e = _as_expr(e)
+
+
+def grad(e):
+    return _Grad(e)
+
+
+def div(g):
+    if not isinstance(g, _Grad):
+        raise NotImplementedError("div of a general vector expression")
+    e = g.e
+    nd = len(e.terms[0][1])
+    out = None
+    for ax in range(nd):
+        t = Dx(e, ax, 2)
+        out = t if out is None else out + t
+    return out
+
+
+# ---------------------------------------------------------------------------
+class TPMatrix:
+    """scale * (identity on the Fourier axes) x pmat on the non-periodic axis.
+
+    ``scale`` has the spectral shape with the non-periodic axis collapsed to
+    one; it carries the Fourier factors (i k)^d of every term that shares
+    ``pmat`` (TPMatrix / get_simplified_tpmatrices, matrixbase.py:1275-1678).
+    """
+
+    def __init__(self, pmat, scale, space, axis):
+        self.pmat = pmat
+        self.scale = scale
+        self.space = space
+        self.axis = axis
+        self.mats = pmat
+
+    def get_key(self):
+        return self.pmat.key
+
+    @property
+    def tensorproductspace(self):
+        return self.space
+
+    def __repr__(self):
+        return f"TPMatrix({self.pmat.key}, axis={self.axis})"
+
+
+def _bilinear(test, expr):
+    T = test.function_space()
+    if isinstance(T, SpectralBase):
+        # 1D: plain SpectralMatrix list
+        out = {}
+        for c, d in expr.terms:
+            m = M.galerkin_matrix(T, d[0])
+            key = d[0]
+            if key in out:
+                out[key][1] += c
+            else:
+                out[key] = [m, c]
+        res = []
+        for m, c in out.values():
+            m.scale = c
+            res.append(m)
+        return res
+    np_axes = T.get_nonperiodic_axes()
+    if len(np_axes) != 1:
+        raise NotImplementedError("exactly one non-periodic axis is on the GPU path")
+    ax = np_axes[0]
+    shape = list(T.shape(True))
+    shape[ax] = 1
+    ks = []
+    for i, b in enumerate(T.bases):
+        if isinstance(b, FourierBase):
+            k = np.asarray(b.wavenumbers(scaled=True), dtype=float)
+            s = [1] * len(shape)
+            s[i] = len(k)
+            ks.append((i, k.reshape(s)))
+    groups = {}
+    for c, d in expr.terms:
+        sc = np.full(shape, c, dtype=complex)
+        for i, k in ks:
+            if d[i]:
+                sc = sc * (1j * k) ** d[i]
+        key = d[ax]
+        groups[key] = groups.get(key, 0) + sc
+    out = []
+    base = T.bases[ax]
+    for order, sc in sorted(groups.items(), key=lambda kv: -kv[0]):
+        if np.abs(sc.imag).max() > 0:
+            raise NotImplementedError("odd derivatives along Fourier axes")
+        out.append(TPMatrix(M.galerkin_matrix(base, order), np.ascontiguousarray(sc.real), T, ax))
+    return out
+
+
+def inner(test, trial, output_array=None, kind=None):
+    """Scalar product (linear form) or matrix assembly (bilinear form)
+    (forms/inner.py:16-511)."""
+    if isinstance(test, BasisFunction) and isinstance(trial, torch.Tensor):
+        T = test.function_space()
+        if output_array is None:
+            output_array = Function(T)
+        out = output_array.v if isinstance(output_array, _ShenfunArray) else output_array
+        inp = trial.v if isinstance(trial, _ShenfunArray) else trial
+        T.scalar_product(inp, out)
+        return output_array
+    if isinstance(test, BasisFunction) and isinstance(trial, (Expr, BasisFunction)):
+        return _bilinear(test, trial)
+    if isinstance(trial, BasisFunction) and isinstance(test, (Expr,)):
+        return _bilinear(trial, test)
+    raise NotImplementedError("inner of these arguments")
+
+
+def project(uh, T, output_array=None):
+    """Projection of an Array on the space's mesh: the forward transform
+    (forms/project.py:117-122)."""
+    if output_array is None:
+        output_array = Function(T)
+    src = uh.v if isinstance(uh, _ShenfunArray) else uh
+    T.forward(src, output_array.v if isinstance(output_array, _ShenfunArray) else output_array)
+    return output_array

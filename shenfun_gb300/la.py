@@ -1,0 +1,210 @@
+"""Linear-algebra solvers on the GPU (la.py and chebyshev/la.py of the
+reference): TDMA, PDMA, SolverGeneric1ND and the Chebyshev Helmholtz solver.
+
+Factorisations happen once at construction (on the device) and are reused by
+every call, like the reference's ``perform_lu`` / ``LU_Helmholtz``.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from .device import ptr, stream_handle, view3, data_kind, require_cuda
+from .forms import TPMatrix, _ShenfunArray
+from .matrices import SpectralMatrix
+
+
+def _raw(t):
+    return t.v if isinstance(t, _ShenfunArray) else t
+
+
+def _band_data(mat, offsets):
+    """Pack a banded SpectralMatrix into the reference's (len(offsets), n)
+    data layout: row r holds offset offsets[r] starting at column max(0, off)."""
+    n = mat.shape[0]
+    data = np.zeros((len(offsets), n))
+    for r, off in enumerate(offsets):
+        d = mat.get(off, 0.0)
+        d = np.broadcast_to(np.atleast_1d(np.asarray(d, dtype=float)), (n - abs(off),))
+        s = mat.scale if np.isscalar(mat.scale) else 1.0
+        if off >= 0:
+            data[r, off:] = d * s
+        else:
+            data[r, :n + off] = d * s
+    return data
+
+
+class _BandedSolver:
+    offsets = None
+    lu_entry = None
+    solve_entry = None
+
+    def __init__(self, mat):
+        require_cuda()
+        if isinstance(mat, list):
+            mat = mat[0] if len(mat) == 1 else _sum_mats(mat)
+        self.mat = mat
+        self.n = mat.shape[0]
+        data = _band_data(mat, self.offsets)
+        self._lu = torch.as_tensor(data, device="cuda").contiguous()
+        _lib.call(self.lu_entry, ptr(self._lu), self.n, stream_handle())
+
+    def __call__(self, b, u=None, axis=0, constraints=()):
+        b = _raw(b)
+        if u is None:
+            u = b
+        else:
+            u = _raw(u)
+            if u.data_ptr() != b.data_ptr():
+                u.copy_(b)
+        shape = tuple(u.shape)
+        outer, n, inner = view3(shape, axis)
+        if n < self.n:
+            raise _lib.SgpuError(_lib.ERR_ARG, "array shorter than the matrix along axis")
+        if n == self.n:
+            _lib.call(self.solve_entry, ptr(u), ptr(self._lu), outer, n, inner, data_kind(u),
+                      stream_handle())
+        else:
+            # the first n entries along axis are the dofs (the rest are boundary dofs)
+            sub = u.narrow(axis, 0, self.n).contiguous()
+            _lib.call(self.solve_entry, ptr(sub), ptr(self._lu), outer, self.n, inner,
+                      data_kind(sub), stream_handle())
+            u.narrow(axis, 0, self.n).copy_(sub)
+        return u
+
+
+class TDMA(_BandedSolver):
+    """Offsets (-2, 0, 2) (la.py:331-393; kernels la.pyx:77, 243, 516)."""
+
+    offsets = (-2, 0, 2)
+    lu_entry = "sgpu_TDMA_LU"
+    solve_entry = "sgpu_TDMA_Solve"
+
+
+class PDMA(_BandedSolver):
+    """Offsets (-4, -2, 0, 2, 4) (la.py:450-543; kernels la.pyx:61, 213, 496)."""
+
+    offsets = (-4, -2, 0, 2, 4)
+    lu_entry = "sgpu_PDMA_LU"
+    solve_entry = "sgpu_PDMA_Solve"
+
+
+def _sum_mats(mats):
+    d = {}
+    for m in mats:
+        s = m.scale if np.isscalar(m.scale) else 1.0
+        for off, v in m.items():
+            d[off] = d.get(off, 0.0) + s * np.asarray(v, dtype=float)
+    out = SpectralMatrix(mats[0].key, d, mats[0].shape)
+    return out
+
+
+# ---------------------------------------------------------------------------
+class Helmholtz:
+    """Chebyshev Dirichlet Helmholtz solver (chebyshev/la.py:131-351):
+    (alfa A + beta B) u = b along one axis, one system per Fourier wavenumber.
+
+    Accepts the two TPMatrix objects of ``inner(v, -div(grad(u)) + c*u)`` (or
+    ``(A, B, alfa, beta)`` with SpectralMatrix A, B and scalars/arrays).
+    """
+
+    def __init__(self, *args):
+        require_cuda()
+        if len(args) == 1:
+            args = tuple(args[0])
+        if len(args) == 2 and all(isinstance(a, TPMatrix) for a in args):
+            by = {a.get_key(): a for a in args}
+            A, B = by["ASDSDmat"], by["BSDSDmat"]
+            self.T = A.space
+            self.axis = A.axis
+            alfa, beta = A.scale, B.scale
+            self.N = self.T.bases[self.axis].N
+        elif len(args) == 4:
+            A, B, alfa, beta = args
+            self.T = None
+            self.axis = 0
+            self.N = A.shape[0] + 2
+            alfa = np.atleast_1d(np.asarray(alfa, dtype=float))
+            beta = np.atleast_1d(np.asarray(beta, dtype=float))
+        else:
+            raise ValueError("Helmholtz(A_tp, B_tp) or Helmholtz(A, B, alfa, beta)")
+        alfa = np.asarray(alfa, dtype=float)
+        beta = np.asarray(beta, dtype=float)
+        shape = np.broadcast_shapes(alfa.shape, beta.shape)
+        self.alfa = torch.as_tensor(np.ascontiguousarray(np.broadcast_to(alfa, shape)), device="cuda")
+        self.beta = torch.as_tensor(np.ascontiguousarray(np.broadcast_to(beta, shape)), device="cuda")
+        self._scale_shape = shape
+        fshape = list(shape) if len(shape) else [1]
+        if self.T is not None:
+            fshape[self.axis] = self.N
+        else:
+            fshape = [self.N] + list(shape[1:]) if len(shape) > 1 else [self.N]
+        self.u0 = torch.zeros(fshape, dtype=torch.float64, device="cuda")
+        self.u1 = torch.zeros_like(self.u0)
+        self.u2 = torch.zeros_like(self.u0)
+        self.L = torch.zeros_like(self.u0)
+        outer, _, inner = view3(tuple(fshape), self.axis)
+        if outer * inner != self.alfa.numel():
+            raise _lib.SgpuError(_lib.ERR_ARG, "scale arrays do not match the systems")
+        self._outer, self._inner = outer, inner
+        _lib.call("sgpu_LU_Helmholtz", self.N, ptr(self.alfa), ptr(self.beta), 0, ptr(self.u0),
+                  ptr(self.u1), ptr(self.u2), ptr(self.L), outer, inner, stream_handle())
+
+    def __call__(self, b, u=None, constraints=()):
+        b = _raw(b)
+        if u is None:
+            u = torch.zeros_like(b)
+        ur = _raw(u)
+        outer, n, inner = view3(tuple(b.shape), self.axis)
+        if n != self.N or (outer, inner) != (self._outer, self._inner):
+            raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
+        _lib.call("sgpu_Solve_Helmholtz", ptr(b), ptr(ur), 0, ptr(self.u0), ptr(self.u1),
+                  ptr(self.u2), ptr(self.L), outer, n, inner, data_kind(b), stream_handle())
+        if constraints:
+            idx = [0] * ur.dim()
+            ur[tuple(idx)] = constraints[0][1]
+        return u
+
+    def matvec(self, v, c):
+        v, cr = _raw(v), _raw(c)
+        outer, n, inner = view3(tuple(v.shape), self.axis)
+        _lib.call("sgpu_Helmholtz_matvec", ptr(v), ptr(cr), ptr(self.alfa), ptr(self.beta),
+                  outer, n, inner, data_kind(v), stream_handle())
+        return c
+
+
+class SolverGeneric1ND:
+    """One non-periodic axis, one banded system per Fourier wavenumber
+    (la.py:1183-1434).  Dispatches on the basis of the non-periodic axis:
+    Chebyshev ShenDirichlet -> the Helmholtz kernels (the reference falls back
+    to a sparse LU per wavenumber there, la.py:1299-1364)."""
+
+    def __init__(self, mats):
+        mats = list(mats)
+        T = mats[0].space
+        ax = mats[0].axis
+        base = T.bases[ax]
+        keys = {m.get_key() for m in mats}
+        self.T, self.axis = T, ax
+        if base.family() == "chebyshev" and base.short_name() == "SD" and keys <= {"ASDSDmat", "BSDSDmat"}:
+            by = {m.get_key(): m for m in mats}
+            shape = list(T.shape(True))
+            shape[ax] = 1
+            A = by.get("ASDSDmat")
+            B = by.get("BSDSDmat")
+            alfa = A.scale if A is not None else np.zeros(shape)
+            beta = B.scale if B is not None else np.zeros(shape)
+            self._impl = Helmholtz(_tp("ASDSDmat", alfa, T, ax), _tp("BSDSDmat", beta, T, ax))
+        else:
+            raise NotImplementedError(f"SolverGeneric1ND for {base.family()} {base.short_name()} {keys}")
+
+    def __call__(self, b, u=None, constraints=()):
+        return self._impl(b, u, constraints)
+
+
+def _tp(key, scale, T, ax):
+    from .matrices import galerkin_matrix
+    order = {"ASDSDmat": 2, "BSDSDmat": 0}[key]
+    return TPMatrix(galerkin_matrix(T.bases[ax], order), np.asarray(scale, dtype=float), T, ax)
+
+
+Solver = SolverGeneric1ND

@@ -1,0 +1,48 @@
+"""Per-axis transform plans: owners of the C-ABI ``sgpu_plan`` handles.
+
+The counterpart of the serial FFTW plan objects the reference creates in each
+basis' ``plan()`` (mpi4py_fft.fftw.dctn/rfftn/irfftn/fftn/ifftn,
+chebyshev/bases.py:407-469, fourier/bases.py:218-279): built once per
+(kind, n, basis) and reused; the tables live on the device.
+"""
+import ctypes
+
+from . import _lib
+from .device import ptr, stream_handle, view3, data_kind
+
+_cache = {}
+
+
+class LinePlan:
+    def __init__(self, kind, n, basis=_lib.BASIS_ORTHO, form=_lib.PLAIN_F64):
+        self.kind, self.n, self.basis, self.form = kind, n, basis, form
+        h = ctypes.c_void_p()
+        _lib.call("sgpu_plan_create", ctypes.byref(h), kind, n, basis, form)
+        self._h = h
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().sgpu_plan_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def __call__(self, inp, out, axis, scale=1.0, stream=None):
+        """Transform `inp` into `out` along `axis` (both C-contiguous CUDA tensors)."""
+        outer, n_in, inner = view3(tuple(inp.shape), axis)
+        o2, n_out, i2 = view3(tuple(out.shape), axis)
+        if (outer, inner) != (o2, i2):
+            raise _lib.SgpuError(_lib.ERR_ARG, "input/output shapes differ off the axis")
+        _lib.call("sgpu_plan_execute", self._h, ptr(inp), ptr(out), outer, inner,
+                  data_kind(inp), float(scale), stream_handle(stream))
+        return out
+
+
+def get_plan(kind, n, basis=_lib.BASIS_ORTHO, form=_lib.PLAIN_F64):
+    key = (kind, n, basis, form)
+    p = _cache.get(key)
+    if p is None:
+        p = LinePlan(kind, n, basis, form)
+        _cache[key] = p
+    return p

@@ -1,0 +1,459 @@
+"""1D function spaces and the tensor-product space, on the GPU.
+
+Mirrors the reference's L3a/L4 layers (spectralbase.py, fourier/bases.py,
+chebyshev/bases.py, tensorproductspace.py) for the spaces on the hot path:
+Fourier R2C/C2C, Chebyshev Orthogonal / ShenDirichlet / ShenBiharmonic (GC
+quadrature) and Legendre (see legendre.py).  Arrays are CUDA tensors; each
+per-axis transform is one kernel launch of a cached ``LinePlan``.
+"""
+import copy
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import require_cuda
+from .plans import get_plan
+
+
+class Domain(tuple):
+    pass
+
+
+# ---------------------------------------------------------------------------
+class SpectralBase:
+    """Common 1D space interface (spectralbase.py:200-648)."""
+
+    family_name = None
+    padding_factor = 1
+
+    def __init__(self, N, dtype=float):
+        self.N = int(N)
+        self.axis = 0
+        self.tensorproductspace = None
+        self._dtype = np.dtype(dtype)
+
+    # -- shape / meta --------------------------------------------------------
+    def family(self):
+        return self.family_name
+
+    def dim(self):
+        return self.N
+
+    def shape(self, forward_output=True):
+        return self.N
+
+    @property
+    def dtype(self):
+        return self._dtype
+
+    def dimensions(self):
+        return 1
+
+    def num_bcs(self):
+        return 0
+
+    def get_unplanned(self, **kw):
+        return copy.copy(self)
+
+    # -- 1D transforms along self.axis of a tensor ---------------------------
+    def _out(self, inp, forward_output, output_array):
+        if output_array is not None:
+            return output_array
+        shape = list(inp.shape)
+        shape[self.axis % inp.dim()] = self.shape(forward_output)
+        return torch.empty(shape, dtype=self._out_dtype(inp, forward_output), device=inp.device)
+
+    def _out_dtype(self, inp, forward_output):
+        return inp.dtype
+
+
+# ---------------------------------------------------------------------------
+class FourierBase(SpectralBase):
+    """fourier/bases.py:44-279."""
+
+    family_name = "fourier"
+
+    def __init__(self, N, dtype, domain=(0.0, 2 * np.pi)):
+        SpectralBase.__init__(self, N, dtype)
+        self.domain = Domain(domain)
+
+    def domain_factor(self):
+        a, b = self.domain
+        return 2 * np.pi / (b - a)
+
+    def points_and_weights(self, N=None, map_true_domain=False, **kw):
+        N = self.N if N is None else N
+        points = np.arange(N, dtype=float) * 2 * np.pi / N
+        if map_true_domain:
+            points = points / self.domain_factor() + self.domain[0]
+        return points, np.full(N, 2 * np.pi / N)
+
+    def mesh(self, bcast=True, map_true_domain=True):
+        return self.points_and_weights(map_true_domain=map_true_domain)[0]
+
+    def get_normalization(self):
+        return 1.0 / self.N
+
+    @staticmethod
+    def boundary_condition():
+        return "Periodic"
+
+
+class R2C(FourierBase):
+    """Real-to-complex Fourier space (fourier/bases.py:282-475)."""
+
+    def __init__(self, N, domain=(0.0, 2 * np.pi), **kw):
+        FourierBase.__init__(self, N, float, domain)
+
+    def shape(self, forward_output=True):
+        return self.N // 2 + 1 if forward_output else self.N
+
+    def wavenumbers(self, bcast=False, scaled=False, eliminate_highest_freq=False):
+        k = np.fft.rfftfreq(self.N, 1.0 / self.N).astype(int)
+        if self.N % 2 == 0 and eliminate_highest_freq:
+            k[-1] = 0
+        return k * self.domain_factor() if scaled else k
+
+    @staticmethod
+    def short_name():
+        return "R2C"
+
+    def _out_dtype(self, inp, forward_output):
+        return torch.complex128 if forward_output else torch.float64
+
+    def scalar_product(self, input_array, output_array=None, axis=None):
+        require_cuda()
+        ax = self.axis if axis is None else axis
+        out = self._out(input_array, True, output_array)
+        return get_plan(_lib.XF_R2C, self.N)(input_array, out, ax, 1.0 / self.N)
+
+    forward = scalar_product
+
+    def backward(self, input_array, output_array=None, axis=None):
+        require_cuda()
+        ax = self.axis if axis is None else axis
+        out = self._out(input_array, False, output_array)
+        return get_plan(_lib.XF_C2R, self.N)(input_array, out, ax, 1.0)
+
+
+class C2C(FourierBase):
+    """Complex-to-complex Fourier space (fourier/bases.py:478-641)."""
+
+    def __init__(self, N, domain=(0.0, 2 * np.pi), **kw):
+        FourierBase.__init__(self, N, complex, domain)
+
+    def wavenumbers(self, bcast=False, scaled=False, eliminate_highest_freq=False):
+        k = np.fft.fftfreq(self.N, 1.0 / self.N).astype(int)
+        if self.N % 2 == 0 and eliminate_highest_freq:
+            k[self.N // 2] = 0
+        return k * self.domain_factor() if scaled else k
+
+    @staticmethod
+    def short_name():
+        return "C2C"
+
+    def scalar_product(self, input_array, output_array=None, axis=None):
+        require_cuda()
+        ax = self.axis if axis is None else axis
+        out = self._out(input_array, True, output_array)
+        return get_plan(_lib.XF_C2C_FWD, self.N)(input_array, out, ax, 1.0 / self.N)
+
+    forward = scalar_product
+
+    def backward(self, input_array, output_array=None, axis=None):
+        require_cuda()
+        ax = self.axis if axis is None else axis
+        out = self._out(input_array, False, output_array)
+        return get_plan(_lib.XF_C2C_BWD, self.N)(input_array, out, ax, 1.0)
+
+
+# ---------------------------------------------------------------------------
+class ChebyshevBase(SpectralBase):
+    """Chebyshev spaces with Gauss-Chebyshev quadrature (chebyshev/bases.py).
+
+    scalar_product / forward / backward run the fused GC transforms: the DCT
+    with the pi/(2N) scale and the Shen stencil epilogue, the TDMA/PDMA mass
+    solve (forward), or the to_ortho prologue with the DCT-III (backward).
+    """
+
+    family_name = "chebyshev"
+    basis_id = _lib.BASIS_ORTHO
+    quad = "GC"
+
+    def __init__(self, N, quad="GC", domain=(-1.0, 1.0), dtype=float, **kw):
+        if quad != "GC":
+            raise NotImplementedError("only Gauss-Chebyshev quadrature is on the GPU path")
+        SpectralBase.__init__(self, N, dtype)
+        self.domain = Domain(domain)
+
+    def domain_factor(self):
+        a, b = self.domain
+        return 2.0 / (b - a)
+
+    def points_and_weights(self, N=None, map_true_domain=False, **kw):
+        N = self.N if N is None else N
+        j = np.arange(N)
+        x = np.cos(np.pi * (2 * j + 1) / (2 * N))
+        if map_true_domain:
+            a, b = self.domain
+            x = (x + 1) * (b - a) / 2 + a
+        return x, np.full(N, np.pi / N)
+
+    def mesh(self, bcast=True, map_true_domain=True):
+        return self.points_and_weights(map_true_domain=map_true_domain)[0]
+
+    def dim(self):
+        return self.N - self.num_bcs()
+
+    def _run(self, kind, input_array, output_array, axis):
+        require_cuda()
+        if self.domain_factor() != 1:
+            raise NotImplementedError("only the reference domain [-1, 1] is on the GPU path")
+        ax = self.axis if axis is None else axis
+        out = self._out(input_array, True, output_array)
+        return get_plan(kind, self.N, self.basis_id)(input_array, out, ax)
+
+    def scalar_product(self, input_array, output_array=None, axis=None):
+        return self._run(_lib.XF_CHEB_SCALAR, input_array, output_array, axis)
+
+    def forward(self, input_array, output_array=None, axis=None):
+        return self._run(_lib.XF_CHEB_FORWARD, input_array, output_array, axis)
+
+    def backward(self, input_array, output_array=None, axis=None):
+        return self._run(_lib.XF_CHEB_BACKWARD, input_array, output_array, axis)
+
+
+class ChebyshevOrthogonal(ChebyshevBase):
+    """chebyshev/bases.py:118-470."""
+
+    @staticmethod
+    def short_name():
+        return "T"
+
+    @staticmethod
+    def boundary_condition():
+        return ""
+
+
+class ChebyshevShenDirichlet(ChebyshevBase):
+    """phi_k = T_k - T_{k+2} (chebyshev/bases.py:476-581)."""
+
+    basis_id = _lib.BASIS_SD
+
+    def num_bcs(self):
+        return 2
+
+    @staticmethod
+    def short_name():
+        return "SD"
+
+    @staticmethod
+    def boundary_condition():
+        return "Dirichlet"
+
+
+class ChebyshevShenBiharmonic(ChebyshevBase):
+    """phi_k = T_k - 2(k+2)/(k+3) T_{k+2} + (k+1)/(k+3) T_{k+4}
+    (chebyshev/bases.py:1175-1258)."""
+
+    basis_id = _lib.BASIS_SB
+
+    def num_bcs(self):
+        return 4
+
+    @staticmethod
+    def short_name():
+        return "SB"
+
+    @staticmethod
+    def boundary_condition():
+        return "Biharmonic"
+
+
+# ---------------------------------------------------------------------------
+def FunctionSpace(N, family="Fourier", bc=None, dtype="d", quad=None, domain=None, **kw):
+    """Pick the 1D space from family and boundary conditions
+    (forms/arguments.py:30-418; bc tuples of zeros only - homogeneous)."""
+    fam = family.lower()
+    if fam in ("f", "fourier"):
+        dom = domain if domain is not None else (0.0, 2 * np.pi)
+        if np.dtype(dtype).char in "FDG":
+            return C2C(N, domain=dom)
+        return R2C(N, domain=dom)
+    nb = 0 if bc is None else len(bc)
+    if bc is not None and any(v != 0 for v in bc):
+        raise NotImplementedError("only homogeneous boundary conditions are on the GPU path")
+    dom = domain if domain is not None else (-1.0, 1.0)
+    if fam in ("c", "chebyshev"):
+        q = quad or "GC"
+        if nb == 0:
+            return ChebyshevOrthogonal(N, quad=q, domain=dom)
+        if nb == 2:
+            return ChebyshevShenDirichlet(N, quad=q, domain=dom)
+        if nb == 4:
+            return ChebyshevShenBiharmonic(N, quad=q, domain=dom)
+    if fam in ("l", "legendre"):
+        from . import legendre
+        return legendre.space(N, nb, quad=quad or "LG", domain=dom)
+    raise NotImplementedError(f"family {family!r} with {nb} boundary conditions")
+
+
+# ---------------------------------------------------------------------------
+class _Chain:
+    """A chain of per-axis transforms with preallocated work arrays, the
+    counterpart of Forward/Backward/ScalarTransform (tensorproductspace.py:45-259)."""
+
+    def __init__(self, T, op):
+        self.T = T
+        self.op = op  # 'forward' | 'scalar_product' | 'backward'
+        self._input = None
+        self._output = None
+
+    @property
+    def input_array(self):
+        if self._input is None:
+            fo = self.op == "backward"
+            self._input = torch.zeros(self.T.shape(fo), dtype=self.T.torch_dtype(fo), device="cuda")
+        return self._input
+
+    @property
+    def output_array(self):
+        if self._output is None:
+            fo = self.op != "backward"
+            self._output = torch.zeros(self.T.shape(fo), dtype=self.T.torch_dtype(fo), device="cuda")
+        return self._output
+
+    def __call__(self, input_array=None, output_array=None, kind=None, **kw):
+        require_cuda()
+        inp = self.input_array if input_array is None else input_array
+        out = self.output_array if output_array is None else output_array
+        if isinstance(inp, torch.Tensor) and not inp.is_cuda:
+            inp = inp.cuda()
+        return self.T._execute(self.op, inp, out, kind)
+
+
+class TensorProductSpace:
+    """Tensor product of 1D spaces on one GPU (tensorproductspace.py:262-469).
+
+    The last axis of ``axes`` is transformed first in forward/scalar_product
+    and last in backward, as in the reference.  There is no pencil
+    decomposition: every axis transform reads and writes the whole array.
+    """
+
+    def __init__(self, comm=None, bases=(), axes=None, dtype=None, **kw):
+        self.comm = comm
+        self.bases = tuple(b.get_unplanned() for b in bases)
+        nd = len(self.bases)
+        for i, b in enumerate(self.bases):
+            b.axis = i
+            b.tensorproductspace = self
+        self.axes = tuple(range(nd)) if axes is None else tuple(int(a) % nd for a in axes)
+        first = self.bases[self.axes[-1]]
+        if dtype is None:
+            dtype = complex if isinstance(first, C2C) else float
+        self._dtype = np.dtype(dtype)
+        if isinstance(first, R2C):
+            assert self._dtype.char in "fdg"
+        r2c = [i for i, b in enumerate(self.bases) if isinstance(b, R2C)]
+        if len(r2c) > 1 or (r2c and r2c[0] != self.axes[-1]):
+            raise ValueError("the R2C axis must be the first one transformed (axes[-1])")
+        self.forward = _Chain(self, "forward")
+        self.backward = _Chain(self, "backward")
+        self.scalar_product = _Chain(self, "scalar_product")
+        self._work = {}
+
+    # -- meta ----------------------------------------------------------------
+    def __len__(self):
+        return len(self.bases)
+
+    @property
+    def dimensions(self):
+        return len(self.bases)
+
+    def shape(self, forward_output=False):
+        return tuple(b.shape(forward_output) for b in self.bases)
+
+    def global_shape(self, forward_output=False):
+        return self.shape(forward_output)
+
+    def dims(self):
+        return self.shape(True)
+
+    def dtype(self, forward_output=False):
+        if forward_output:
+            if any(isinstance(b, FourierBase) for b in self.bases) or self._dtype.char in "FDG":
+                return np.dtype(complex)
+            return np.dtype(float)
+        return self._dtype
+
+    def torch_dtype(self, forward_output=False):
+        return torch.complex128 if self.dtype(forward_output).char in "FDG" else torch.float64
+
+    def local_slice(self, forward_output=True):
+        return tuple(slice(0, n) for n in self.shape(forward_output))
+
+    def get_nonperiodic_axes(self):
+        return [i for i, b in enumerate(self.bases) if not isinstance(b, FourierBase)]
+
+    def local_wavenumbers(self, broadcast=False, scaled=False, eliminate_highest_freq=False):
+        ks = []
+        nd = len(self.bases)
+        for i, b in enumerate(self.bases):
+            if isinstance(b, FourierBase):
+                k = b.wavenumbers(scaled=scaled, eliminate_highest_freq=eliminate_highest_freq)
+            else:
+                k = np.arange(b.N)
+            s = [1] * nd
+            s[i] = len(k)
+            k = np.asarray(k).reshape(s)
+            ks.append(np.broadcast_to(k, self.shape(True)) if broadcast else k)
+        return ks
+
+    def mesh(self, map_true_domain=True):
+        out = []
+        nd = len(self.bases)
+        for i, b in enumerate(self.bases):
+            x = b.mesh(map_true_domain=map_true_domain)
+            s = [1] * nd
+            s[i] = len(x)
+            out.append(x.reshape(s))
+        return out
+
+    local_mesh = mesh
+
+    # -- execution -----------------------------------------------------------
+    def _buf(self, key, shape, dtype):
+        t = self._work.get(key)
+        if t is None or tuple(t.shape) != tuple(shape) or t.dtype != dtype:
+            t = torch.empty(shape, dtype=dtype, device="cuda")
+            self._work[key] = t
+        return t
+
+    def _execute(self, op, inp, out, kind=None):
+        order = list(reversed(self.axes)) if op != "backward" else list(self.axes)
+        shape = list(inp.shape)
+        cur = inp
+        nsteps = len(order)
+        for step, ax in enumerate(order):
+            b = self.bases[ax]
+            fo = op != "backward"
+            new_shape = list(shape)
+            new_shape[ax] = b.shape(fo)
+            if isinstance(b, R2C):
+                dt = torch.complex128 if fo else torch.float64
+            else:
+                dt = cur.dtype
+            last = step == nsteps - 1
+            if last:
+                dst = out
+            elif cur is not inp and tuple(new_shape) == tuple(cur.shape) and dt == cur.dtype:
+                dst = cur  # same-size transform: in place on a work array
+            else:
+                dst = self._buf(("w", step % 2, tuple(new_shape), dt), new_shape, dt)
+                if dst is cur:
+                    dst = self._buf(("w", (step + 1) % 2, tuple(new_shape), dt), new_shape, dt)
+            getattr(b, op)(cur, dst, axis=ax)
+            cur = dst
+            shape = new_shape
+        return out

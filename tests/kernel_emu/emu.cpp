@@ -1,0 +1,174 @@
+// CPU harness for the kernels' block programs (test infrastructure).
+//
+// Runs the exact __host__ __device__ block programs of the CUDA library with
+// one emulated thread per block, on exactly-sized heap buffers, so that a
+// build with -fsanitize=address,undefined reports any index that leaves its
+// buffer.  Shared memory is poisoned with NaN to expose reads of unwritten
+// staging data.  Driven by tests/test_kernel_emu.py through binary files.
+//
+//   emu xform  kind n basis outer inner data_kind scale in.bin out.bin
+//   emu hlu    N outer inner alfa.bin beta.bin out.bin        (d0|d1|d2|L)
+//   emu hsolve N outer inner data_kind b.bin fac.bin out.bin   (fac = d0|d1|d2|L)
+//   emu hmatvec N outer inner data_kind v.bin alfa.bin beta.bin out.bin
+//   emu tdma|pdma n outer inner data_kind raw.bin u.bin out.bin (LU then solve)
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../shenfun_gb300/csrc/plan_host.cuh"
+#include "../../shenfun_gb300/csrc/solvers.cuh"
+
+using namespace sgpu;
+
+static double* read_exact(const char* path, size_t count) {
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    fprintf(stderr, "cannot open %s\n", path);
+    exit(2);
+  }
+  double* buf = (double*)malloc(sizeof(double) * (count ? count : 1));
+  size_t got = fread(buf, sizeof(double), count, f);
+  fclose(f);
+  if (got != count) {
+    fprintf(stderr, "%s: expected %zu doubles, got %zu\n", path, count, got);
+    exit(2);
+  }
+  return buf;
+}
+
+static void write_exact(const char* path, const double* buf, size_t count) {
+  FILE* f = fopen(path, "wb");
+  fwrite(buf, sizeof(double), count, f);
+  fclose(f);
+}
+
+static int xform(int argc, char** argv) {
+  if (argc < 11) return 2;
+  int kind = atoi(argv[2]), n = atoi(argv[3]), basis = atoi(argv[4]);
+  long long outer = atoll(argv[5]), inner = atoll(argv[6]);
+  int data_kind = atoi(argv[7]);
+  double scl = atof(argv[8]);
+  LinePlan p;
+  HostTables T;
+  int st = build_plan_host(kind, n, basis, SGPU_PLAIN_F64, p, T);
+  if (st != SGPU_OK) {
+    fprintf(stderr, "plan status %d\n", st);
+    return 3;
+  }
+  size_t off[7];
+  size_t sz = table_layout(T, off);
+  unsigned char* img = (unsigned char*)malloc(sz);
+  table_image(T, off, img);
+  bind_tables(p, T, off, img);
+  const int dc = data_complex_for(p, data_kind);
+  int in_c = dc, out_c = dc;
+  if (kind == SGPU_XF_R2C) {
+    in_c = 0;
+    out_c = 1;
+  }
+  if (kind == SGPU_XF_C2R) {
+    in_c = 1;
+    out_c = 0;
+  }
+  const size_t nin = (size_t)outer * p.n_in * inner * (in_c ? 2 : 1);
+  const size_t nout = (size_t)outer * p.n_out * inner * (out_c ? 2 : 1);
+  double* in = read_exact(argv[9], nin);
+  double* out = (double*)malloc(sizeof(double) * (nout ? nout : 1));
+  for (size_t i = 0; i < nout; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
+  const long long nlines = outer * inner;
+  const int lpb = lines_per_block(p, dc);
+  const long long nblocks = (nlines + lpb - 1) / lpb;
+  const size_t nsm = p.smem / sizeof(double);
+  for (long long b = 0; b < nblocks; ++b) {
+    double* smem = (double*)malloc(p.smem);
+    for (size_t i = 0; i < nsm; ++i) smem[i] = std::numeric_limits<double>::quiet_NaN();
+    prog_dispatch<double>(p, in, out, dc, nlines, inner, scl, b, smem, 0, 1);
+    free(smem);
+  }
+  write_exact(argv[10], out, nout);
+  free(in);
+  free(out);
+  free(img);
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 2) return 2;
+  std::string mode = argv[1];
+  if (mode == "xform") return xform(argc, argv);
+  if (mode == "hlu") {
+    long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    long long ns = outer * inner;
+    double* a = read_exact(argv[5], ns);
+    double* b = read_exact(argv[6], ns);
+    std::vector<double*> f(4);
+    size_t cnt = (size_t)outer * N * inner;
+    double* all = (double*)calloc(4 * cnt, sizeof(double));
+    for (int i = 0; i < 4; ++i) f[i] = all + i * cnt;
+    for (long long s = 0; s < ns; ++s) helmholtz_lu_prog(N, a, b, f[0], f[1], f[2], f[3], inner, s);
+    write_exact(argv[7], all, 4 * cnt);
+    return 0;
+  }
+  if (mode == "hsolve") {
+    long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]);
+    size_t cnt = (size_t)outer * N * inner;
+    size_t w = dk ? 2 : 1;
+    double* b = read_exact(argv[6], cnt * w);
+    double* fac = read_exact(argv[7], 4 * cnt);
+    double* u = (double*)malloc(sizeof(double) * cnt * w);
+    for (size_t i = 0; i < cnt * w; ++i) u[i] = 0.0;
+    for (long long s = 0; s < outer * inner; ++s) {
+      if (dk)
+        helmholtz_solve_prog<cd>((const cd*)b, (cd*)u, fac, fac + cnt, fac + 2 * cnt, fac + 3 * cnt,
+                                 N, inner, s);
+      else
+        helmholtz_solve_prog<double>(b, u, fac, fac + cnt, fac + 2 * cnt, fac + 3 * cnt, N, inner, s);
+    }
+    write_exact(argv[8], u, cnt * w);
+    return 0;
+  }
+  if (mode == "hmatvec") {
+    long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]);
+    size_t cnt = (size_t)outer * N * inner;
+    size_t w = dk ? 2 : 1;
+    double* v = read_exact(argv[6], cnt * w);
+    double* a = read_exact(argv[7], outer * inner);
+    double* be = read_exact(argv[8], outer * inner);
+    double* out = (double*)malloc(sizeof(double) * cnt * w);
+    for (long long s = 0; s < outer * inner; ++s) {
+      if (dk)
+        helmholtz_matvec_prog<cd>((const cd*)v, (cd*)out, a, be, N, inner, s);
+      else
+        helmholtz_matvec_prog<double>(v, out, a, be, N, inner, s);
+    }
+    write_exact(argv[9], out, cnt * w);
+    return 0;
+  }
+  if (mode == "tdma" || mode == "pdma") {
+    long long n = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]);
+    int rows = mode == "tdma" ? 3 : 5;
+    double* raw = read_exact(argv[6], rows * n);
+    size_t cnt = (size_t)outer * n * inner * (dk ? 2 : 1);
+    double* u = read_exact(argv[7], cnt);
+    if (mode == "tdma") tdma_lu_prog(raw, n); else pdma_lu_prog(raw, n);
+    for (long long s = 0; s < outer * inner; ++s) {
+      if (mode == "tdma") {
+        if (dk) tdma_solve_prog<cd>((cd*)u, raw, n, inner, s);
+        else tdma_solve_prog<double>(u, raw, n, inner, s);
+      } else {
+        if (dk) pdma_solve_prog<cd>((cd*)u, raw, n, inner, s);
+        else pdma_solve_prog<double>(u, raw, n, inner, s);
+      }
+    }
+    write_exact(argv[8], u, cnt);
+    return 0;
+  }
+  return 2;
+}

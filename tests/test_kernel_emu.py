@@ -1,0 +1,209 @@
+"""CPU run of the CUDA block programs (index math, buffer bounds, numerics).
+
+The library's kernel bodies are __host__ __device__ block programs; the
+harness tests/kernel_emu/emu.cpp runs them on the CPU (one emulated thread per
+block) under AddressSanitizer/UBSan on exactly-sized buffers and compares the
+results with the oracle.  This checks every index and every buffer bound of
+each kernel before the code runs on a GPU.  No GPU needed.
+"""
+import hashlib
+import os
+import shutil
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import spectral as S, la
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EMU_DIR = os.path.join(REPO, "tests", "kernel_emu")
+EMU = os.path.join(EMU_DIR, "_build", "emu")
+CSRC = os.path.join(REPO, "shenfun_gb300", "csrc")
+
+# transform kinds / bases (include/shenfun_gb300.h)
+R2C, C2R, C2C_FWD, C2C_BWD, DCT2, DCT3, CHEB_SCALAR, CHEB_FORWARD, CHEB_BACKWARD = range(1, 10)
+BASIS = {"T": 0, "SD": 1, "SB": 2}
+
+
+def _emu_stamp():
+    h = hashlib.sha256()
+    for d in (CSRC, EMU_DIR, os.path.join(REPO, "include")):
+        for f in sorted(os.listdir(d)):
+            p = os.path.join(d, f)
+            if os.path.isfile(p) and f.endswith((".cuh", ".cpp", ".h")):
+                h.update(open(p, "rb").read())
+    return h.hexdigest()
+
+
+@pytest.fixture(scope="module")
+def emu():
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    os.makedirs(os.path.dirname(EMU), exist_ok=True)
+    stamp = _emu_stamp()
+    sf = EMU + ".stamp"
+    if not (os.path.exists(EMU) and os.path.exists(sf) and open(sf).read() == stamp):
+        cuda_inc = "/usr/local/cuda/include"
+        cmd = ["g++", "-O1", "-g", "-std=c++17", "-fsanitize=address,undefined",
+               "-fno-sanitize-recover=all", "-fno-omit-frame-pointer",
+               "-I" + cuda_inc, "-I" + os.path.join(REPO, "include"),
+               os.path.join(EMU_DIR, "emu.cpp"), "-o", EMU]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        open(sf, "w").write(stamp)
+    return EMU
+
+
+def run(emu, args, inputs, out_count):
+    with tempfile.TemporaryDirectory() as td:
+        paths = []
+        for i, arr in enumerate(inputs):
+            p = os.path.join(td, f"in{i}.bin")
+            np.ascontiguousarray(arr).view(np.float64).ravel().tofile(p)
+            paths.append(p)
+        outp = os.path.join(td, "out.bin")
+        env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0:abort_on_error=1")
+        r = subprocess.run([emu] + [str(a) for a in args] + paths + [outp], capture_output=True,
+                           text=True, env=env)
+        assert r.returncode == 0, r.stderr[-3000:]
+        return np.fromfile(outp, dtype=np.float64, count=out_count)
+
+
+def xform(emu, kind, n, basis, arr, axis, data_complex, scale=1.0, n_out=None):
+    """Run a transform along `axis` of arr (C-contiguous) through the emulator."""
+    arr = np.ascontiguousarray(arr)
+    outer = int(np.prod(arr.shape[:axis]))
+    inner = int(np.prod(arr.shape[axis + 1:]))
+    n_out = n_out if n_out is not None else arr.shape[axis]
+    out_complex = {R2C: True, C2R: False}.get(kind, data_complex)
+    shape = list(arr.shape)
+    shape[axis] = n_out
+    cnt = int(np.prod(shape)) * (2 if out_complex else 1)
+    res = run(emu, ["xform", kind, n, basis, outer, inner, 1 if data_complex else 0, repr(scale)],
+              [arr], cnt)
+    if out_complex:
+        res = res.view(np.complex128)
+    return res.reshape(shape)
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+rng = np.random.default_rng(7)
+
+
+@pytest.mark.parametrize("n", [2, 3, 4, 5, 6, 8, 12, 16, 17, 30, 43, 45, 64, 97, 128, 129, 256, 257])
+def test_fourier_r2c_c2r(emu, n):
+    x = rng.standard_normal((3, n, 5))
+    y = xform(emu, R2C, n, 0, x, 1, False, 1.0 / n, n // 2 + 1)
+    assert rel(y, S.r2c_forward(x, axis=1)) < 1e-13
+    z = xform(emu, C2R, n, 0, y, 1, True, 1.0, n)
+    assert rel(z, S.r2c_backward(y, n, axis=1)) < 1e-13
+    # contiguous axis, odd number of lines
+    x2 = rng.standard_normal((7, n))
+    y2 = xform(emu, R2C, n, 0, x2, 1, False, 1.0, n // 2 + 1)
+    assert rel(y2, np.fft.rfft(x2, axis=1)) < 1e-13
+
+
+@pytest.mark.parametrize("n", [2, 3, 7, 8, 11, 16, 43, 60, 64, 129, 256, 257])
+def test_fourier_c2c(emu, n):
+    x = rng.standard_normal((n, 6)) + 1j * rng.standard_normal((n, 6))
+    y = xform(emu, C2C_FWD, n, 0, x, 0, True, 1.0 / n)
+    assert rel(y, S.c2c_forward(x, axis=0)) < 1e-13
+    z = xform(emu, C2C_BWD, n, 0, y, 0, True, 1.0)
+    assert rel(z, S.c2c_backward(y, axis=0)) < 1e-13
+
+
+@pytest.mark.parametrize("n", [4, 5, 8, 9, 16, 17, 33, 64, 129, 257])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_raw_dct(emu, n, cplx):
+    import scipy.fft as sfft
+    x = rng.standard_normal((5, n))
+    if cplx:
+        x = x + 1j * rng.standard_normal((5, n))
+    y = xform(emu, DCT2, n, 0, x, 1, cplx, 1.0)
+    ref = sfft.dct(x.real, 2, axis=1) + (1j * sfft.dct(x.imag, 2, axis=1) if cplx else 0)
+    assert rel(y, ref) < 1e-13
+    y3 = xform(emu, DCT3, n, 0, x, 1, cplx, 0.5)
+    ref3 = (sfft.dct(x.real, 3, axis=1) + (1j * sfft.dct(x.imag, 3, axis=1) if cplx else 0)) * 0.5
+    assert rel(y3, ref3) < 1e-13
+
+
+@pytest.mark.parametrize("n", [12, 16, 17, 33, 64, 129, 257])
+@pytest.mark.parametrize("basis", ["T", "SD", "SB"])
+@pytest.mark.parametrize("layout", ["last", "middle"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_chebyshev(emu, n, basis, layout, cplx):
+    shape = (3, 4, n) if layout == "last" else (2, n, 5)
+    axis = 2 if layout == "last" else 1
+    x = rng.standard_normal(shape)
+    if cplx:
+        x = x + 1j * rng.standard_normal(shape)
+    b = BASIS[basis]
+    sp_ = xform(emu, CHEB_SCALAR, n, b, x, axis, cplx)
+    assert rel(sp_, S.cheb_scalar_product(x, basis, axis)) < 1e-13
+    fw = xform(emu, CHEB_FORWARD, n, b, x, axis, cplx)
+    # The ShenBiharmonic mass solve amplifies input rounding by ~1e3 at
+    # n = 129..257 (a 1e-16 relative input perturbation moves the oracle's own
+    # output by 4e-14..2e-13), so its bound is wider.
+    tol = 1e-12 if basis != "SB" else 5e-11
+    assert rel(fw, S.cheb_forward(x, basis, axis)) < tol
+    bw = xform(emu, CHEB_BACKWARD, n, b, fw, axis, cplx)
+    assert rel(bw, S.cheb_backward(fw, basis, axis)) < 1e-13
+
+
+@pytest.mark.parametrize("N,outer,inner", [(8, 1, 3), (17, 4, 1), (33, 2, 5), (64, 3, 1), (257, 2, 3)])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_helmholtz(emu, N, outer, inner, cplx):
+    ns = outer * inner
+    alfa = -np.ones(ns)
+    beta = rng.uniform(0.5, 2000.0, ns)
+    fac = run(emu, ["hlu", N, outer, inner], [alfa, beta], 4 * outer * N * inner)
+    fac = fac.reshape(4, outer, N, inner)
+    d0, d1, d2, L = la.helmholtz_lu(N, alfa, beta)
+    to_sys = lambda a: np.moveaxis(a, 1, -1).reshape(ns, N)  # noqa: E731
+    for got, ref in zip(fac, (d0, d1, d2, L)):
+        assert rel(to_sys(got), ref) < 1e-14
+    f = rng.standard_normal((outer, N, inner))
+    if cplx:
+        f = f + 1j * rng.standard_normal((outer, N, inner))
+    cnt = outer * N * inner * (2 if cplx else 1)
+    u = run(emu, ["hsolve", N, outer, inner, int(cplx)], [f, fac], cnt)
+    u = u.view(np.complex128) if cplx else u
+    u = u.reshape(outer, N, inner)
+    uref = la.helmholtz_solve(to_sys(f), d0, d1, d2, L)
+    assert rel(to_sys(u)[:, :N - 2], uref[:, :N - 2]) < 1e-13
+    mv = run(emu, ["hmatvec", N, outer, inner, int(cplx)], [u, alfa, beta], cnt)
+    mv = (mv.view(np.complex128) if cplx else mv).reshape(outer, N, inner)
+    assert rel(to_sys(mv), la.helmholtz_matvec(to_sys(u), alfa, beta)) < 1e-13
+    # the matvec undoes the solve on the dofs
+    assert rel(to_sys(mv)[:, :N - 2], to_sys(f)[:, :N - 2]) < 1e-11
+
+
+@pytest.mark.parametrize("n,outer,inner", [(14, 1, 4), (30, 3, 1), (255, 2, 2)])
+@pytest.mark.parametrize("which", ["tdma", "pdma"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_banded(emu, n, outer, inner, which, cplx):
+    rows = 3 if which == "tdma" else 5
+    raw = np.zeros((rows, n))
+    raw[rows // 2] = 4.0 + rng.uniform(0, 1, n)
+    for r in range(rows):
+        if r != rows // 2:
+            raw[r] = rng.uniform(-1, 1, n)
+    u = rng.standard_normal((outer, n, inner))
+    if cplx:
+        u = u + 1j * rng.standard_normal((outer, n, inner))
+    cnt = outer * n * inner * (2 if cplx else 1)
+    got = run(emu, [which, n, outer, inner, int(cplx)], [raw, u], cnt)
+    got = (got.view(np.complex128) if cplx else got).reshape(outer, n, inner)
+    data = raw.copy()
+    if which == "tdma":
+        la.tdma_lu(data)
+        ref = la.tdma_solve(u, data, axis=1)
+    else:
+        la.pdma_lu(data)
+        ref = la.pdma_solve(u, data, axis=1)
+    assert rel(got, ref) < 1e-13
