@@ -64,6 +64,8 @@ extern "C" {
 
 /* arithmetic form */
 #define SGPU_PLAIN_F64 0   /* all FP64                                        */
+#define SGPU_MIXED_DF 1    /* double-float (FP32 pair, ~48-bit) arithmetic on the
+                              FP32 pipes; FP64 in and out (the mixed form)     */
 
 const char* sgpu_status_string(int status);
 int sgpu_version(void);
@@ -128,6 +130,20 @@ int sgpu_Solve_Helmholtz(const void* b, void* u, int neumann, const double* d0,
 int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa, const double* beta,
                           int64_t outer, int64_t N, int64_t inner, int data_kind,
                           cudaStream_t stream);
+
+/* ---- Helmholtz factorisation cache (no reference counterpart as a separate
+ * call: it is LU_Helmholtz's result (la.pyx:717-763) stored for the GPU) ---
+ * fac holds 4 * (N-2) * outer * inner entries of 8 bytes laid out
+ * [q][k][system] for q = (multiplier L, 1/d0, d1, d2): consecutive systems are
+ * contiguous.  form SGPU_PLAIN_F64 stores FP64, SGPU_MIXED_DF double-float
+ * pairs.  The LU is computed in FP64 in the reference's order either way. */
+int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int64_t outer,
+                          int64_t inner, int form, void* fac, cudaStream_t stream);
+/* Solve_Helmholtz (la.pyx:845-947) from the cache: b, u in the (outer, N,
+ * inner) layout; one thread per (system, parity); b may alias u. */
+int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int64_t outer,
+                                int64_t N, int64_t inner, int data_kind, int form,
+                                cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,8 @@ REAL, COMPLEX = 0, 1
 BASIS_ORTHO, BASIS_SD, BASIS_SB = 0, 1, 2
 XF_R2C, XF_C2R, XF_C2C_FWD, XF_C2C_BWD, XF_DCT2, XF_DCT3, XF_CHEB_SCALAR, XF_CHEB_FORWARD, \
     XF_CHEB_BACKWARD = range(1, 10)
-PLAIN_F64 = 0
+PLAIN_F64, MIXED_DF = 0, 1
+FORMS = {"plain": PLAIN_F64, "mixed": MIXED_DF, PLAIN_F64: PLAIN_F64, MIXED_DF: MIXED_DF}
 
 
 class SgpuError(RuntimeError):
@@ -48,6 +49,8 @@ SIGNATURES = {
     "sgpu_LU_Helmholtz": (_int, [_i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _i64, _i64, _vp]),
     "sgpu_Solve_Helmholtz": (_int, [_vp, _vp, _int, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
     "sgpu_Helmholtz_matvec": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_helmholtz_factor": (_int, [_i64, _vp, _vp, _i64, _i64, _int, _vp, _vp]),
+    "sgpu_helmholtz_solve_cached": (_int, [_vp, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp]),
 }
 
 

@@ -16,7 +16,7 @@
 // harness in tests/kernel_emu runs the same code to check indices and bounds.
 #pragma once
 
-#include "sgpu_common.cuh"
+#include "dfloat.cuh"
 
 namespace sgpu {
 
@@ -44,7 +44,39 @@ struct LinePlan {
   const cd* post;    // Chebyshev: post[k] = exp(-i pi k / (2 n)), k in [0, n)
   const double* mass;  // Chebyshev forward: LU'd mass bands (TDMA 3 x dim or PDMA 5 x dim)
   const double* sten;  // SB stencil rows: sten[k] = K2(k), sten[n + k] = K4(k)
+  // the same tables as double-float pairs (mixed form)
+  const Cx<df>* tw_f;
+  const Cx<df>* rk_f;
+  const Cx<df>* post_f;
+  const df* sten_f;
+  int form;          // SGPU_PLAIN_F64 or SGPU_MIXED_DF
 };
+
+// typed table access: FP64 tables for R = double, df tables for R = df
+template <class R>
+SGPU_HD Cx<R> tw_at(const LinePlan& p, int e);
+template <>
+SGPU_HD Cx<double> tw_at<double>(const LinePlan& p, int e) { return p.tw[e]; }
+template <>
+SGPU_HD Cx<df> tw_at<df>(const LinePlan& p, int e) { return p.tw_f[e]; }
+template <class R>
+SGPU_HD Cx<R> rk_at(const LinePlan& p, int e);
+template <>
+SGPU_HD Cx<double> rk_at<double>(const LinePlan& p, int e) { return p.rk[e]; }
+template <>
+SGPU_HD Cx<df> rk_at<df>(const LinePlan& p, int e) { return p.rk_f[e]; }
+template <class R>
+SGPU_HD Cx<R> post_at(const LinePlan& p, int e);
+template <>
+SGPU_HD Cx<double> post_at<double>(const LinePlan& p, int e) { return p.post[e]; }
+template <>
+SGPU_HD Cx<df> post_at<df>(const LinePlan& p, int e) { return p.post_f[e]; }
+template <class R>
+SGPU_HD R sten_at(const LinePlan& p, int e);
+template <>
+SGPU_HD double sten_at<double>(const LinePlan& p, int e) { return p.sten[e]; }
+template <>
+SGPU_HD df sten_at<df>(const LinePlan& p, int e) { return p.sten_f[e]; }
 
 // ---------------------------------------------------------------------------
 // R-point DFT kernels (forward sign, y_s = sum_r v_r exp(-2 pi i r s / R))
@@ -99,7 +131,7 @@ SGPU_HD void dft5(Cx<R>* v) {
 
 // One Stockham butterfly: radix R_, stride Ns, butterfly j of a length-m line.
 template <class R, int R_>
-SGPU_HD void stockham_fixed(const Cx<R>* in, Cx<R>* out, int m, int Ns, int j, const cd* tw) {
+SGPU_HD void stockham_fixed(const Cx<R>* in, Cx<R>* out, int m, int Ns, int j, const LinePlan& p) {
   Cx<R> v[R_];
   const int mr = m / R_;
   const int k = j % Ns;
@@ -109,8 +141,7 @@ SGPU_HD void stockham_fixed(const Cx<R>* in, Cx<R>* out, int m, int Ns, int j, c
   if (k != 0) {
 #pragma unroll
     for (int r = 1; r < R_; ++r) {
-      cd w = tw[r * k * st];
-      v[r] = v[r] * cx<R>(R(w.re), R(w.im));
+      v[r] = v[r] * tw_at<R>(p, r * k * st);
     }
   }
   if (R_ == 2) dft2(v);
@@ -125,7 +156,7 @@ SGPU_HD void stockham_fixed(const Cx<R>* in, Cx<R>* out, int m, int Ns, int j, c
 // Generic odd-prime radix: direct O(R^2) DFT from the m-th roots table.
 template <class R>
 SGPU_HD void stockham_generic(const Cx<R>* in, Cx<R>* out, int m, int Rr, int Ns, int j,
-                              const cd* tw) {
+                              const LinePlan& p) {
   const int mr = m / Rr;
   const int k = j % Ns;
   const int st = mr / Ns;
@@ -136,8 +167,7 @@ SGPU_HD void stockham_generic(const Cx<R>* in, Cx<R>* out, int m, int Rr, int Ns
       Cx<R> x = in[j + r * mr];
       // twiddle W_m^{r k st} then DFT root W_R^{r s} = W_m^{(r s mod R) mr}
       int e = (r * k * st + ((r * s) % Rr) * mr) % m;
-      cd w = tw[e];
-      acc = acc + x * cx<R>(R(w.re), R(w.im));
+      acc = acc + x * tw_at<R>(p, e);
     }
     out[idx + s * Ns] = acc;
   }
@@ -159,11 +189,11 @@ SGPU_HD Cx<R>* fft_stages(const LinePlan& p, Cx<R>* src, Cx<R>* dst, int lines, 
       const Cx<R>* in = src + (size_t)t * p.ld;
       Cx<R>* out = dst + (size_t)t * p.ld;
       switch (Rr) {
-        case 2: stockham_fixed<R, 2>(in, out, m, Ns, j, p.tw); break;
-        case 3: stockham_fixed<R, 3>(in, out, m, Ns, j, p.tw); break;
-        case 4: stockham_fixed<R, 4>(in, out, m, Ns, j, p.tw); break;
-        case 5: stockham_fixed<R, 5>(in, out, m, Ns, j, p.tw); break;
-        default: stockham_generic<R>(in, out, m, Rr, Ns, j, p.tw); break;
+        case 2: stockham_fixed<R, 2>(in, out, m, Ns, j, p); break;
+        case 3: stockham_fixed<R, 3>(in, out, m, Ns, j, p); break;
+        case 4: stockham_fixed<R, 4>(in, out, m, Ns, j, p); break;
+        case 5: stockham_fixed<R, 5>(in, out, m, Ns, j, p); break;
+        default: stockham_generic<R>(in, out, m, Rr, Ns, j, p); break;
       }
     }
     SGPU_SYNC();
@@ -206,8 +236,7 @@ SGPU_HD void dft_lines(const LinePlan& p, Cx<R>* X, Cx<R>* A, Cx<R>* B, Cx<R>* s
   // multiply by the kernel spectrum, conjugate: IDFT(y) = conj(DFT(conj(y)))
   for (int e = tid; e < lines * m; e += nth) {
     int t = e / m, q = e - t * m;
-    cd k = p.rk[q];
-    r1[(size_t)t * ld + q] = conj(r1[(size_t)t * ld + q] * cx<R>(R(k.re), R(k.im)));
+    r1[(size_t)t * ld + q] = conj(r1[(size_t)t * ld + q] * rk_at<R>(p, q));
   }
   SGPU_SYNC();
   Cx<R>* other = (r1 == A) ? B : A;
@@ -246,14 +275,15 @@ SGPU_HD void tile_map(int64_t e, int TL, int n_arr, int64_t inner, int& t, int& 
 // entries (the 1 and -1 of ShenDirichlet, the leading 1 of ShenBiharmonic)
 // apply to every row, as in the reference's stencil matrix
 // (spectralbase.py:1504-1526); k-dependent entries are zero for k >= dim.
-SGPU_HD double stencil_coef(const LinePlan& p, int off, int k) {
-  if (p.basis == SGPU_BASIS_ORTHO) return off == 0 ? 1.0 : 0.0;
-  if (p.basis == SGPU_BASIS_SD) return off == 0 ? 1.0 : (off == 2 ? -1.0 : 0.0);
+template <class R>
+SGPU_HD R stencil_coef(const LinePlan& p, int off, int k) {
+  if (p.basis == SGPU_BASIS_ORTHO) return off == 0 ? R(1.0) : R(0.0);
+  if (p.basis == SGPU_BASIS_SD) return off == 0 ? R(1.0) : (off == 2 ? R(-1.0) : R(0.0));
   // SB
-  if (off == 0) return 1.0;
-  if (off == 2) return p.sten[k];
-  if (off == 4) return p.sten[p.n + k];
-  return 0.0;
+  if (off == 0) return R(1.0);
+  if (off == 2) return sten_at<R>(p, k);
+  if (off == 4) return sten_at<R>(p, p.n + k);
+  return R(0.0);
 }
 
 SGPU_HD int basis_nbcs(int basis) {
@@ -304,12 +334,12 @@ SGPU_HD void load_tile(const LinePlan& p, const void* in, int in_complex, int64_
       Cx<R> v = cx<R>(R(0), R(0));
       if (l < nlines) {
         const double* src = (const double*)in + 2 * elem_off(l, k, n_arr, inner);
-        v = cx<R>(R(src[0]), R(src[1]));
+        v = cx<R>(from_f64<R>(src[0]), from_f64<R>(src[1]));
       }
       X[(size_t)t * p.ld + k] = v;
     } else {
       R v = R(0);
-      if (l < nlines) v = R(((const double*)in)[elem_off(l, k, n_arr, inner)]);
+      if (l < nlines) v = from_f64<R>(((const double*)in)[elem_off(l, k, n_arr, inner)]);
       Cx<R>& z = X[(size_t)(t >> 1) * p.ld + k];
       if (t & 1)
         z.im = v;
@@ -335,11 +365,11 @@ SGPU_HD void store_tile(const LinePlan& p, void* out, int out_complex, int64_t l
     if (out_complex) {
       Cx<R> v = Y[(size_t)t * p.ld + k];
       double* dst = (double*)out + 2 * elem_off(l, k, n_arr, inner);
-      dst[0] = (double)v.re;
-      dst[1] = (double)v.im;
+      dst[0] = to_f64(v.re);
+      dst[1] = to_f64(v.im);
     } else {
       const Cx<R>& z = Y[(size_t)(t >> 1) * p.ld + k];
-      ((double*)out)[elem_off(l, k, n_arr, inner)] = (double)((t & 1) ? z.im : z.re);
+      ((double*)out)[elem_off(l, k, n_arr, inner)] = to_f64((t & 1) ? z.im : z.re);
     }
   }
 }
@@ -354,7 +384,7 @@ SGPU_HD void prog_r2c(const LinePlan& p, const double* in, double* out, int64_t 
   dft_lines<R>(p, s.X, s.A, s.B, s.slot, p.tlc, tid, nth);
   // separate: P_k = (Z_k + conj Z_{n-k}) / 2, Q_k = (Z_k - conj Z_{n-k}) / (2i)
   const int n = p.n, nh = n / 2 + 1;
-  const R h = R(0.5) * R(scl);
+  const R h = R(0.5) * from_f64<R>(scl);
   for (int e = tid; e < p.tlc * nh; e += nth) {
     int c = e / nh, k = e - c * nh;
     Cx<R> z = s.X[(size_t)c * p.ld + k];
@@ -401,11 +431,11 @@ SGPU_HD void prog_c2r(const LinePlan& p, const double* in, double* out, int64_t 
   }
   SGPU_SYNC();
   dft_lines<R>(p, s.X, s.A, s.B, s.slot, p.tlc, tid, nth);
-  const R sc = R(scl);
+  const R sc = from_f64<R>(scl);
   for (int e = tid; e < p.tlc * n; e += nth) {
     int c = e / n, k = e - c * n;
     Cx<R> z = s.X[(size_t)c * p.ld + k];
-    s.X[(size_t)c * p.ld + k] = cx<R>(z.re * sc, -z.im * sc);
+    s.X[(size_t)c * p.ld + k] = cx<R>(z.re * sc, -(z.im * sc));
   }
   SGPU_SYNC();
   store_tile<R>(p, out, 0, l0, nlines, inner, s.X, tid, nth);
@@ -427,11 +457,11 @@ SGPU_HD void prog_c2c(const LinePlan& p, const double* in, double* out, int64_t 
     SGPU_SYNC();
   }
   dft_lines<R>(p, s.X, s.A, s.B, s.slot, p.tlc, tid, nth);
-  const R sc = R(scl);
+  const R sc = from_f64<R>(scl);
   for (int e = tid; e < p.tlc * p.n; e += nth) {
     int c = e / p.n, k = e - c * p.n;
     Cx<R> z = s.X[(size_t)c * p.ld + k];
-    s.X[(size_t)c * p.ld + k] = bwd ? cx<R>(z.re * sc, -z.im * sc) : scale(z, sc);
+    s.X[(size_t)c * p.ld + k] = bwd ? cx<R>(z.re * sc, -(z.im * sc)) : scale(z, sc);
   }
   SGPU_SYNC();
   store_tile<R>(p, out, 1, l0, nlines, inner, s.X, tid, nth);
@@ -459,18 +489,18 @@ SGPU_HD void prog_dct2(const LinePlan& p, const double* in, double* out, int in_
   // Y_k = 2 Re(exp(-i pi k / 2n) V_k) for each of the two packed real lines.
   R fac;
   if (p.kind == SGPU_XF_DCT2)
-    fac = R(2.0 * scl);
+    fac = from_f64<R>(2.0 * scl);
   else
-    fac = R(3.14159265358979323846264338327950288 / n);  // (pi / 2n) * 2
+    fac = from_f64<R>(3.14159265358979323846264338327950288 / n);  // (pi / 2n) * 2
   for (int e = tid; e < p.tlc * n; e += nth) {
     int c = e / n, k = e - c * n;
     Cx<R> z = s.X[(size_t)c * p.ld + k];
     Cx<R> zc = conj(s.X[(size_t)c * p.ld + (k == 0 ? 0 : n - k)]);
     Cx<R> P = scale(z + zc, R(0.5));
     Cx<R> Q = scale(mul_mi(z - zc), R(0.5));
-    cd w = p.post[k];
-    R yp = (R(w.re) * P.re - R(w.im) * P.im) * fac;
-    R yq = (R(w.re) * Q.re - R(w.im) * Q.im) * fac;
+    Cx<R> w = post_at<R>(p, k);
+    R yp = (w.re * P.re - w.im * P.im) * fac;
+    R yq = (w.re * Q.re - w.im * Q.im) * fac;
     s.A[(size_t)c * p.ld + k] = cx<R>(yp, yq);
   }
   SGPU_SYNC();
@@ -483,8 +513,7 @@ SGPU_HD void prog_dct2(const LinePlan& p, const double* in, double* out, int in_
       Cx<R> acc = y[k];
       for (int off = 2; off <= 4; off += 2) {
         if (k + off < n) {
-          R kc = R(stencil_coef(p, off, k));
-          acc = acc + scale(y[k + off], kc);
+          acc = acc + scale(y[k + off], stencil_coef<R>(p, off, k));
         }
       }
       s.B[(size_t)c * p.ld + k] = acc;
@@ -504,30 +533,30 @@ SGPU_HD void prog_dct2(const LinePlan& p, const double* in, double* out, int in_
         const double* ld_ = p.mass;
         const double* di = p.mass + dim;
         const double* ud = p.mass + 2 * dim + 2;
-        for (int i = 2; i < dim; ++i) u[i] = u[i] - scale(u[i - 2], R(ld_[i - 2]));
-        u[dim - 1] = scale(u[dim - 1], R(di[dim - 1]));
-        u[dim - 2] = scale(u[dim - 2], R(di[dim - 2]));
+        for (int i = 2; i < dim; ++i) u[i] = u[i] - scale(u[i - 2], from_f64<R>(ld_[i - 2]));
+        u[dim - 1] = scale(u[dim - 1], from_f64<R>(di[dim - 1]));
+        u[dim - 2] = scale(u[dim - 2], from_f64<R>(di[dim - 2]));
         for (int i = dim - 3; i >= 0; --i)
-          u[i] = scale(u[i] - scale(u[i + 2], R(ud[i])), R(di[i]));
+          u[i] = scale(u[i] - scale(u[i + 2], from_f64<R>(ud[i])), from_f64<R>(di[i]));
       } else if (nb == 4) {
         const double* a = p.mass;
         const double* b = p.mass + dim;
         const double* di = p.mass + 2 * dim;
         const double* ee = p.mass + 3 * dim + 2;
         const double* f = p.mass + 4 * dim + 4;
-        u[2] = u[2] - scale(u[0], R(b[0]));
-        u[3] = u[3] - scale(u[1], R(b[1]));
+        u[2] = u[2] - scale(u[0], from_f64<R>(b[0]));
+        u[3] = u[3] - scale(u[1], from_f64<R>(b[1]));
         for (int k = 4; k < dim; ++k)
-          u[k] = u[k] - (scale(u[k - 2], R(b[k - 2])) + scale(u[k - 4], R(a[k - 4])));
-        u[dim - 1] = scale(u[dim - 1], R(di[dim - 1]));
-        u[dim - 2] = scale(u[dim - 2], R(di[dim - 2]));
-        u[dim - 3] = scale(u[dim - 3] - scale(u[dim - 1], R(ee[dim - 3])), R(di[dim - 3]));
-        u[dim - 4] = scale(u[dim - 4] - scale(u[dim - 2], R(ee[dim - 4])), R(di[dim - 4]));
+          u[k] = u[k] - (scale(u[k - 2], from_f64<R>(b[k - 2])) + scale(u[k - 4], from_f64<R>(a[k - 4])));
+        u[dim - 1] = scale(u[dim - 1], from_f64<R>(di[dim - 1]));
+        u[dim - 2] = scale(u[dim - 2], from_f64<R>(di[dim - 2]));
+        u[dim - 3] = scale(u[dim - 3] - scale(u[dim - 1], from_f64<R>(ee[dim - 3])), from_f64<R>(di[dim - 3]));
+        u[dim - 4] = scale(u[dim - 4] - scale(u[dim - 2], from_f64<R>(ee[dim - 4])), from_f64<R>(di[dim - 4]));
         for (int k = dim - 5; k >= 0; --k)
-          u[k] = scale(u[k] - scale(u[k + 2], R(ee[k])) - scale(u[k + 4], R(f[k])), R(di[k]));
+          u[k] = scale(u[k] - scale(u[k + 2], from_f64<R>(ee[k])) - scale(u[k + 4], from_f64<R>(f[k])), from_f64<R>(di[k]));
       } else {
         // orthogonal basis: diagonal mass; the table holds 1 / (c_k pi / 2)
-        for (int k = 0; k < n; ++k) u[k] = scale(u[k], R(p.mass[k]));
+        for (int k = 0; k < n; ++k) u[k] = scale(u[k], from_f64<R>(p.mass[k]));
       }
       for (int k = dim; k < n; ++k) u[k] = cx<R>(R(0), R(0));
     }
@@ -558,7 +587,7 @@ SGPU_HD void prog_dct3(const LinePlan& p, const double* in, double* out, int in_
       if (k < dim) acc = u[k];
       for (int off = 2; off <= 4; off += 2) {
         int j = k - off;
-        if (j >= 0 && j < dim) acc = acc + scale(u[j], R(stencil_coef(p, off, j)));
+        if (j >= 0 && j < dim) acc = acc + scale(u[j], stencil_coef<R>(p, off, j));
       }
       s.B[(size_t)c * p.ld + k] = acc;
     }
@@ -583,8 +612,7 @@ SGPU_HD void prog_dct3(const LinePlan& p, const double* in, double* out, int in_
       z = cx<R>(a.re, a.im);  // W_0 = c_0 (both lines)
       if (!gc) z = cx<R>(a.re, a.im);
     } else {
-      cd w = p.post[k];  // exp(-i pi k / 2n); we need its conjugate
-      Cx<R> tw = cx<R>(R(w.re), R(-w.im));
+      Cx<R> tw = conj(post_at<R>(p, k));  // exp(+i pi k / 2n)
       wp = scale(wp * tw, f);
       wq = scale(wq * tw, f);
       z = wp + mul_pi(wq);

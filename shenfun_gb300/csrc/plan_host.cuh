@@ -16,7 +16,16 @@ struct HostTables {
   std::vector<cd> tw, rk, post;
   std::vector<int> rin, rout;
   std::vector<double> mass, sten;
+  std::vector<Cx<df>> tw_f, rk_f, post_f;
+  std::vector<df> sten_f;
 };
+
+// long double -> double-float pair (hi = nearest float, lo = nearest float of the rest)
+inline df ld_to_df(long double x) {
+  float h = (float)x;
+  float l = (float)(x - (long double)h);
+  return df(h, l);
+}
 
 namespace planhost {
 
@@ -95,12 +104,13 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   using namespace planhost;
   if (n < 2 || n > (1 << 20)) return SGPU_ERR_ARG;
   if (kind < SGPU_XF_R2C || kind > SGPU_XF_CHEB_BACKWARD) return SGPU_ERR_ARG;
-  if (form != SGPU_PLAIN_F64) return SGPU_ERR_UNSUPPORTED;
+  if (form != SGPU_PLAIN_F64 && form != SGPU_MIXED_DF) return SGPU_ERR_UNSUPPORTED;
   const bool cheb = kind >= SGPU_XF_DCT2;
   const bool composite = kind >= SGPU_XF_CHEB_SCALAR;
   if (composite && (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SB)) return SGPU_ERR_ARG;
   if (composite && n < 2 + 2 * basis_nbcs(basis)) return SGPU_ERR_ARG;
   std::memset(&p, 0, sizeof(p));
+  p.form = form;
   p.kind = kind;
   p.basis = composite ? basis : SGPU_BASIS_ORTHO;
   p.n = n;
@@ -130,9 +140,11 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   std::vector<double>& mass = T.mass;
   std::vector<double>& sten = T.sten;
   tw.resize(m);
+  T.tw_f.resize(m);
   for (int e = 0; e < m; ++e) {
     ld_t a = -2 * kPi * (ld_t)e / (ld_t)m;
     tw[e] = cx<double>((double)cosl(a), (double)sinl(a));
+    T.tw_f[e] = cx<df>(ld_to_df(cosl(a)), ld_to_df(sinl(a)));
   }
   if (p.rader) {
     const int g = primitive_root(n);
@@ -161,6 +173,7 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
         si += br[q] * sn + bi[q] * c;
       }
       rk[s] = cx<double>((double)(sr / m), (double)(si / m));
+      T.rk_f.push_back(cx<df>(ld_to_df(sr / m), ld_to_df(si / m)));
     }
   }
   if (cheb) {
@@ -168,14 +181,18 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
     for (int k = 0; k < n; ++k) {
       ld_t a = -kPi * (ld_t)k / (ld_t)(2 * n);
       post[k] = cx<double>((double)cosl(a), (double)sinl(a));
+      T.post_f.push_back(cx<df>(ld_to_df(cosl(a)), ld_to_df(sinl(a))));
     }
   }
   if (p.basis == SGPU_BASIS_SB) {
     // K2(k) = -(2k+4)/(k+3), K4(k) = (k+1)/(k+3), zero for k >= n-4
     sten.assign(2 * (size_t)n, 0.0);
+    T.sten_f.assign(2 * (size_t)n, df());
     for (int k = 0; k < n - 4; ++k) {
       sten[k] = -(2.0 * k + 4) / (k + 3.0);
       sten[n + k] = (k + 1.0) / (k + 3.0);
+      T.sten_f[k] = ld_to_df(-(2.0L * k + 4) / (k + 3.0L));
+      T.sten_f[n + k] = ld_to_df((k + 1.0L) / (k + 3.0L));
     }
   }
   if (kind == SGPU_XF_CHEB_FORWARD) {
@@ -241,31 +258,44 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
 }
 
 // Point a plan's table pointers into one contiguous table image at `base`
-// (device or host); `offsets` receives the byte layout.  Returns total bytes.
-inline size_t table_layout(const HostTables& T, size_t off[7]) {
+// (device or host); `off` receives the byte layout.  Returns total bytes.
+#define SGPU_NTAB 11
+inline size_t table_layout(const HostTables& T, size_t off[SGPU_NTAB]) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t sizes[SGPU_NTAB] = {
+      sizeof(cd) * T.tw.size(),       sizeof(cd) * T.rk.size(),
+      sizeof(int) * T.rin.size(),     sizeof(int) * T.rout.size(),
+      sizeof(cd) * T.post.size(),     sizeof(double) * T.mass.size(),
+      sizeof(double) * T.sten.size(), sizeof(Cx<df>) * T.tw_f.size(),
+      sizeof(Cx<df>) * T.rk_f.size(), sizeof(Cx<df>) * T.post_f.size(),
+      sizeof(df) * T.sten_f.size()};
   size_t sz = 0;
-  off[0] = sz; sz += al(sizeof(cd) * T.tw.size());
-  off[1] = sz; sz += al(sizeof(cd) * T.rk.size());
-  off[2] = sz; sz += al(sizeof(int) * T.rin.size());
-  off[3] = sz; sz += al(sizeof(int) * T.rout.size());
-  off[4] = sz; sz += al(sizeof(cd) * T.post.size());
-  off[5] = sz; sz += al(sizeof(double) * T.mass.size());
-  off[6] = sz; sz += al(sizeof(double) * T.sten.size());
+  for (int i = 0; i < SGPU_NTAB; ++i) {
+    off[i] = sz;
+    sz += al(sizes[i]);
+  }
   return sz;
 }
 
-inline void table_image(const HostTables& T, const size_t off[7], unsigned char* img) {
-  if (!T.tw.empty()) std::memcpy(img + off[0], T.tw.data(), sizeof(cd) * T.tw.size());
-  if (!T.rk.empty()) std::memcpy(img + off[1], T.rk.data(), sizeof(cd) * T.rk.size());
-  if (!T.rin.empty()) std::memcpy(img + off[2], T.rin.data(), sizeof(int) * T.rin.size());
-  if (!T.rout.empty()) std::memcpy(img + off[3], T.rout.data(), sizeof(int) * T.rout.size());
-  if (!T.post.empty()) std::memcpy(img + off[4], T.post.data(), sizeof(cd) * T.post.size());
-  if (!T.mass.empty()) std::memcpy(img + off[5], T.mass.data(), sizeof(double) * T.mass.size());
-  if (!T.sten.empty()) std::memcpy(img + off[6], T.sten.data(), sizeof(double) * T.sten.size());
+inline void table_image(const HostTables& T, const size_t off[SGPU_NTAB], unsigned char* img) {
+  auto cp = [&](int i, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(img + off[i], src, bytes);
+  };
+  cp(0, T.tw.data(), sizeof(cd) * T.tw.size());
+  cp(1, T.rk.data(), sizeof(cd) * T.rk.size());
+  cp(2, T.rin.data(), sizeof(int) * T.rin.size());
+  cp(3, T.rout.data(), sizeof(int) * T.rout.size());
+  cp(4, T.post.data(), sizeof(cd) * T.post.size());
+  cp(5, T.mass.data(), sizeof(double) * T.mass.size());
+  cp(6, T.sten.data(), sizeof(double) * T.sten.size());
+  cp(7, T.tw_f.data(), sizeof(Cx<df>) * T.tw_f.size());
+  cp(8, T.rk_f.data(), sizeof(Cx<df>) * T.rk_f.size());
+  cp(9, T.post_f.data(), sizeof(Cx<df>) * T.post_f.size());
+  cp(10, T.sten_f.data(), sizeof(df) * T.sten_f.size());
 }
 
-inline void bind_tables(LinePlan& p, const HostTables& T, const size_t off[7], unsigned char* b) {
+inline void bind_tables(LinePlan& p, const HostTables& T, const size_t off[SGPU_NTAB],
+                        unsigned char* b) {
   p.tw = (const cd*)(b + off[0]);
   p.rk = T.rk.empty() ? nullptr : (const cd*)(b + off[1]);
   p.rin = T.rin.empty() ? nullptr : (const int*)(b + off[2]);
@@ -273,6 +303,10 @@ inline void bind_tables(LinePlan& p, const HostTables& T, const size_t off[7], u
   p.post = T.post.empty() ? nullptr : (const cd*)(b + off[4]);
   p.mass = T.mass.empty() ? nullptr : (const double*)(b + off[5]);
   p.sten = T.sten.empty() ? nullptr : (const double*)(b + off[6]);
+  p.tw_f = (const Cx<df>*)(b + off[7]);
+  p.rk_f = T.rk_f.empty() ? nullptr : (const Cx<df>*)(b + off[8]);
+  p.post_f = T.post_f.empty() ? nullptr : (const Cx<df>*)(b + off[9]);
+  p.sten_f = T.sten_f.empty() ? nullptr : (const df*)(b + off[10]);
 }
 
 }  // namespace sgpu

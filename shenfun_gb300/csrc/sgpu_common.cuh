@@ -18,7 +18,13 @@
 #define SGPU_SYNC() ((void)0)
 #endif
 
+#ifdef __CUDACC__
 #define SGPU_HD __host__ __device__ __forceinline__
+#else
+// plain host compilers (the CPU harness): ordinary inline functions, so the
+// sanitizer build stays small
+#define SGPU_HD inline
+#endif
 
 #include "../../include/shenfun_gb300.h"
 

@@ -139,3 +139,53 @@ extern "C" int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa,
     return SGPU_ERR_ARG;
   return finish();
 }
+
+// ---- factorisation cache + cached solve (both forms) -----------------------
+template <class R>
+__global__ void k_helmholtz_factor(int64_t N, const double* alfa, const double* beta, R* fac,
+                                   int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) helmholtz_factor_prog<R>(N, alfa, beta, fac, nsys, s);
+}
+
+template <class R, class T>
+__global__ void k_helmholtz_cached(const T* b, T* u, const R* fac, int64_t N, int64_t inner,
+                                   int64_t nsys) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 2 * nsys) helmholtz_cached_solve_prog<R, T>(b, u, fac, N, inner, nsys, t >> 1, (int)(t & 1));
+}
+
+extern "C" int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta,
+                                     int64_t outer, int64_t inner, int form, void* fac,
+                                     cudaStream_t stream) {
+  if (!alfa || !beta || !fac || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (form == SGPU_PLAIN_F64)
+    k_helmholtz_factor<double><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, (double*)fac, nsys);
+  else if (form == SGPU_MIXED_DF)
+    k_helmholtz_factor<df><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, (df*)fac, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int64_t outer,
+                                           int64_t N, int64_t inner, int data_kind, int form,
+                                           cudaStream_t stream) {
+  if (!b || !u || !fac || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  const unsigned nb = nblk(2 * nsys);
+  if (form == SGPU_PLAIN_F64 && data_kind == SGPU_COMPLEX)
+    k_helmholtz_cached<double, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (const double*)fac, N, inner, nsys);
+  else if (form == SGPU_PLAIN_F64 && data_kind == SGPU_REAL)
+    k_helmholtz_cached<double, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (const double*)fac, N, inner, nsys);
+  else if (form == SGPU_MIXED_DF && data_kind == SGPU_COMPLEX)
+    k_helmholtz_cached<df, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (const df*)fac, N, inner, nsys);
+  else if (form == SGPU_MIXED_DF && data_kind == SGPU_REAL)
+    k_helmholtz_cached<df, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (const df*)fac, N, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}

@@ -7,7 +7,7 @@
 // every step of the recurrence is a coalesced row access.
 #pragma once
 
-#include "sgpu_common.cuh"
+#include "dfloat.cuh"
 
 namespace sgpu {
 
@@ -212,6 +212,118 @@ SGPU_HD void helmholtz_matvec_prog(const T* v_all, T* b_all, const double* alfa,
              mulr(s2, hA2(k - 1) * alf);
   b[M] = zero_of(T());
   b[M + 1] = zero_of(T());
+}
+
+// ---- factorisation cache: interleaved, reciprocal-pivot layout -------------
+// fac[q][k][s] for q = 0..3 (L, 1/d0, d1, d2), k in [0, M), s a system:
+// consecutive systems are contiguous, so thread s reads row k coalesced.
+// Entries are FP64 (plain form) or double-float pairs (mixed form); both are
+// 8 bytes.  The LU itself is computed in FP64 in the reference's order
+// (la.pyx:717-763) and only then stored.
+template <class R>
+SGPU_HD R store_cast(double x);
+template <>
+SGPU_HD double store_cast<double>(double x) { return x; }
+template <>
+SGPU_HD df store_cast<df>(double x) { return df_from_double(x); }
+
+template <class R>
+SGPU_HD void helmholtz_factor_prog(int64_t N, const double* alfa, const double* beta, R* fac,
+                                   int64_t nsys, int64_t s) {
+  const int64_t M = N - 2;
+  const double a = alfa[s], b = beta[s];
+  R* FL = fac;
+  R* FD = fac + M * nsys;
+  R* F1 = fac + 2 * M * nsys;
+  R* F2 = fac + 3 * M * nsys;
+  double d0m2 = 0, d1m2 = 0, d2m2 = 0, d0m1 = 0, d1m1 = 0, d2m1 = 0;  // rows i-2, i-1
+  for (int64_t i = 0; i < M; ++i) {
+    double l = 0, d0, d1 = 0, d2 = 0;
+    if (i < 2) {
+      d0 = a * hA0(i) + b * hB0(i);
+      d1 = a * hA2(i) + b * hB2();
+      d2 = a * hA2(i);
+    } else {
+      l = b * hB2() / d0m2;
+      d0 = a * hA0(i) + b * hB0(i) - l * d1m2;
+      if (i < M - 2) d1 = a * hA2(i) + b * hB2() - l * d2m2;
+      if (i < M - 4) d2 = a * hA2(i) - l * d2m2;
+    }
+    FL[i * nsys + s] = store_cast<R>(l);
+    FD[i * nsys + s] = store_cast<R>(1.0 / d0);
+    F1[i * nsys + s] = store_cast<R>(d1);
+    F2[i * nsys + s] = store_cast<R>(d2);
+    d0m2 = d0m1; d1m2 = d1m1; d2m2 = d2m1;
+    d0m1 = d0; d1m1 = d1; d2m1 = d2;
+  }
+}
+
+// Solve with cached factors, one thread per (system, parity): the even and
+// odd unknowns of a Chebyshev Dirichlet Helmholtz system are decoupled, so
+// each parity chain runs Solve_Helmholtz_1D_ptr's recurrences (la.pyx:871-912)
+// independently.  T is the element type in memory (double or complex
+// double), R the arithmetic (double or df).
+template <class R, class T>
+struct ElemOps;
+template <class R>
+struct ElemOps<R, double> {
+  typedef R V;
+  static SGPU_HD V load(const double* p) { return from_f64<R>(*p); }
+  static SGPU_HD void store(double* p, V v) { *p = to_f64(v); }
+  static SGPU_HD V zero() { return R(0.0); }
+  static SGPU_HD V mul(V a, R s) { return a * s; }
+};
+template <class R>
+struct ElemOps<R, cd> {
+  typedef Cx<R> V;
+  static SGPU_HD V load(const cd* p) { return cx<R>(from_f64<R>(p->re), from_f64<R>(p->im)); }
+  static SGPU_HD void store(cd* p, V v) { *p = cx<double>(to_f64(v.re), to_f64(v.im)); }
+  static SGPU_HD V zero() { return cx<R>(R(0.0), R(0.0)); }
+  static SGPU_HD V mul(V a, R s) { return scale(a, s); }
+};
+
+template <class R>
+SGPU_HD R fac_at(const R* fac, int64_t q, int64_t k, int64_t M, int64_t nsys, int64_t s) {
+  return fac[(q * M + k) * nsys + s];
+}
+
+template <class R, class T>
+SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac, int64_t Nb,
+                                         int64_t inner, int64_t nsys, int64_t s, int par) {
+  typedef ElemOps<R, T> E;
+  typedef typename E::V V;
+  const int64_t M = Nb - 2;
+  const int64_t base = sys_base(s, Nb, inner);
+  const T* f = b_all + base;
+  T* u = u_all + base;
+  // forward sweep y_i = f_i - L_{i-2} y_{i-2} along the chain i = par, par+2, ...
+  V y = E::zero();
+  int64_t top = par;
+  for (int64_t i = par; i < M; i += 2) {
+    V fi = E::load(f + i * inner);
+    // row i stores the multiplier the reference keeps in L[i-2]
+    if (i >= 2) fi = fi - E::mul(y, fac_at(fac, 0, i, M, nsys, s));
+    y = fi;
+    E::store(u + i * inner, y);
+    top = i;
+  }
+  // back substitution from the top of the chain
+  V up2 = E::zero(), S = E::zero(), pend = E::zero();  // u_{i+2}; sum of u_{>=i+4}
+  bool have2 = false;
+  for (int64_t i = top; i >= 0; i -= 2) {
+    V yi = E::load(u + i * inner);
+    V ui = yi;
+    if (have2) ui = ui - E::mul(up2, fac_at(fac, 2, i, M, nsys, s));
+    if (i <= M - 5) {
+      S = S + pend;
+      ui = ui - E::mul(S, fac_at(fac, 3, i, M, nsys, s));
+    }
+    ui = E::mul(ui, fac_at(fac, 1, i, M, nsys, s));
+    E::store(u + i * inner, ui);
+    pend = up2;
+    up2 = ui;
+    have2 = true;
+  }
 }
 
 }  // namespace sgpu

@@ -20,7 +20,7 @@ extern "C" int sgpu_plan_create(sgpu_plan** out, int kind, int n, int basis, int
   HostTables T;
   int st = build_plan_host(kind, n, basis, form, p, T);
   if (st != SGPU_OK) return st;
-  size_t off[7];
+  size_t off[SGPU_NTAB];
   const size_t sz = table_layout(T, off);
   std::vector<unsigned char> img(sz, 0);
   table_image(T, off, img.data());
@@ -53,12 +53,13 @@ extern "C" int sgpu_plan_destroy(sgpu_plan* plan) {
   return SGPU_OK;
 }
 
+template <class R>
 __global__ void __launch_bounds__(256) sgpu_line_kernel(LinePlan p, const double* in, double* out,
                                                         int data_complex, int64_t nlines,
                                                         int64_t inner, double scl) {
   extern __shared__ __align__(16) unsigned char sgpu_smem[];
-  prog_dispatch<double>(p, in, out, data_complex, nlines, inner, scl, (int64_t)blockIdx.x,
-                        sgpu_smem, (int)threadIdx.x, (int)blockDim.x);
+  prog_dispatch<R>(p, in, out, data_complex, nlines, inner, scl, (int64_t)blockIdx.x, sgpu_smem,
+                   (int)threadIdx.x, (int)blockDim.x);
 }
 
 extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
@@ -75,15 +76,22 @@ extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* ou
   if (nblocks > 0x7fffffffLL) return SGPU_ERR_ARG;
   static bool attr_set = false;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(sgpu_line_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(sgpu_line_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024) != cudaSuccess ||
+        cudaFuncSetAttribute(sgpu_line_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              220 * 1024) != cudaSuccess) {
       cudaGetLastError();
       return SGPU_ERR_CUDA;
     }
     attr_set = true;
   }
-  sgpu_line_kernel<<<(unsigned)nblocks, p.nthreads, p.smem, stream>>>(
-      p, (const double*)in, (double*)out, data_complex_for(p, data_kind), nlines, inner, scale);
+  const int dc = data_complex_for(p, data_kind);
+  if (p.form == SGPU_MIXED_DF)
+    sgpu_line_kernel<df><<<(unsigned)nblocks, p.nthreads, p.smem, stream>>>(
+        p, (const double*)in, (double*)out, dc, nlines, inner, scale);
+  else
+    sgpu_line_kernel<double><<<(unsigned)nblocks, p.nthreads, p.smem, stream>>>(
+        p, (const double*)in, (double*)out, dc, nlines, inner, scale);
   if (cudaGetLastError() != cudaSuccess) return SGPU_ERR_CUDA;
   return SGPU_OK;
 }

@@ -107,7 +107,7 @@ class Helmholtz:
     ``(A, B, alfa, beta)`` with SpectralMatrix A, B and scalars/arrays).
     """
 
-    def __init__(self, *args):
+    def __init__(self, *args, form=None):
         require_cuda()
         if len(args) == 1:
             args = tuple(args[0])
@@ -130,8 +130,8 @@ class Helmholtz:
         alfa = np.asarray(alfa, dtype=float)
         beta = np.asarray(beta, dtype=float)
         shape = np.broadcast_shapes(alfa.shape, beta.shape)
-        self.alfa = torch.as_tensor(np.ascontiguousarray(np.broadcast_to(alfa, shape)), device="cuda")
-        self.beta = torch.as_tensor(np.ascontiguousarray(np.broadcast_to(beta, shape)), device="cuda")
+        self.alfa = torch.as_tensor(np.array(np.broadcast_to(alfa, shape)), device="cuda")
+        self.beta = torch.as_tensor(np.array(np.broadcast_to(beta, shape)), device="cuda")
         self._scale_shape = shape
         fshape = list(shape) if len(shape) else [1]
         if self.T is not None:
@@ -148,6 +148,14 @@ class Helmholtz:
         self._outer, self._inner = outer, inner
         _lib.call("sgpu_LU_Helmholtz", self.N, ptr(self.alfa), ptr(self.beta), 0, ptr(self.u0),
                   ptr(self.u1), ptr(self.u2), ptr(self.L), outer, inner, stream_handle())
+        # factorisation cache used by __call__: reciprocal pivots, interleaved
+        # [q][k][system] layout, FP64 (plain) or double-float pairs (mixed)
+        self.form = _lib.FORMS[form] if form is not None else (
+            self.T.form if self.T is not None else _lib.PLAIN_F64)
+        nsys = outer * inner
+        self._fac = torch.empty(4 * (self.N - 2) * nsys, dtype=torch.float64, device="cuda")
+        _lib.call("sgpu_helmholtz_factor", self.N, ptr(self.alfa), ptr(self.beta), outer, inner,
+                  self.form, ptr(self._fac), stream_handle())
 
     def __call__(self, b, u=None, constraints=()):
         b = _raw(b)
@@ -157,11 +165,20 @@ class Helmholtz:
         outer, n, inner = view3(tuple(b.shape), self.axis)
         if n != self.N or (outer, inner) != (self._outer, self._inner):
             raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
-        _lib.call("sgpu_Solve_Helmholtz", ptr(b), ptr(ur), 0, ptr(self.u0), ptr(self.u1),
-                  ptr(self.u2), ptr(self.L), outer, n, inner, data_kind(b), stream_handle())
+        _lib.call("sgpu_helmholtz_solve_cached", ptr(b), ptr(ur), ptr(self._fac), outer, n, inner,
+                  data_kind(b), self.form, stream_handle())
         if constraints:
             idx = [0] * ur.dim()
             ur[tuple(idx)] = constraints[0][1]
+        return u
+
+    def solve_reference_layout(self, b, u):
+        """Solve through the reference-layout factors u0, u1, u2, L
+        (Solve_Helmholtz, la.pyx:845) instead of the cache."""
+        b, ur = _raw(b), _raw(u)
+        outer, n, inner = view3(tuple(b.shape), self.axis)
+        _lib.call("sgpu_Solve_Helmholtz", ptr(b), ptr(ur), 0, ptr(self.u0), ptr(self.u1),
+                  ptr(self.u2), ptr(self.L), outer, n, inner, data_kind(b), stream_handle())
         return u
 
     def matvec(self, v, c):

@@ -26,6 +26,9 @@ class SpectralBase:
 
     family_name = None
     padding_factor = 1
+    # arithmetic of the transforms: _lib.PLAIN_F64 (FP64) or _lib.MIXED_DF
+    # (double-float on the FP32 pipes); set by TensorProductSpace(form=...)
+    form = _lib.PLAIN_F64
 
     def __init__(self, N, dtype=float):
         self.N = int(N)
@@ -57,11 +60,12 @@ class SpectralBase:
         return copy.copy(self)
 
     # -- 1D transforms along self.axis of a tensor ---------------------------
-    def _out(self, inp, forward_output, output_array):
+    def _out(self, inp, forward_output, output_array, axis=None):
         if output_array is not None:
             return output_array
         shape = list(inp.shape)
-        shape[self.axis % inp.dim()] = self.shape(forward_output)
+        ax = self.axis if axis is None else axis
+        shape[ax % inp.dim()] = self.shape(forward_output)
         return torch.empty(shape, dtype=self._out_dtype(inp, forward_output), device=inp.device)
 
     def _out_dtype(self, inp, forward_output):
@@ -125,16 +129,16 @@ class R2C(FourierBase):
     def scalar_product(self, input_array, output_array=None, axis=None):
         require_cuda()
         ax = self.axis if axis is None else axis
-        out = self._out(input_array, True, output_array)
-        return get_plan(_lib.XF_R2C, self.N)(input_array, out, ax, 1.0 / self.N)
+        out = self._out(input_array, True, output_array, ax)
+        return get_plan(_lib.XF_R2C, self.N, form=self.form)(input_array, out, ax, 1.0 / self.N)
 
     forward = scalar_product
 
     def backward(self, input_array, output_array=None, axis=None):
         require_cuda()
         ax = self.axis if axis is None else axis
-        out = self._out(input_array, False, output_array)
-        return get_plan(_lib.XF_C2R, self.N)(input_array, out, ax, 1.0)
+        out = self._out(input_array, False, output_array, ax)
+        return get_plan(_lib.XF_C2R, self.N, form=self.form)(input_array, out, ax, 1.0)
 
 
 class C2C(FourierBase):
@@ -156,16 +160,16 @@ class C2C(FourierBase):
     def scalar_product(self, input_array, output_array=None, axis=None):
         require_cuda()
         ax = self.axis if axis is None else axis
-        out = self._out(input_array, True, output_array)
-        return get_plan(_lib.XF_C2C_FWD, self.N)(input_array, out, ax, 1.0 / self.N)
+        out = self._out(input_array, True, output_array, ax)
+        return get_plan(_lib.XF_C2C_FWD, self.N, form=self.form)(input_array, out, ax, 1.0 / self.N)
 
     forward = scalar_product
 
     def backward(self, input_array, output_array=None, axis=None):
         require_cuda()
         ax = self.axis if axis is None else axis
-        out = self._out(input_array, False, output_array)
-        return get_plan(_lib.XF_C2C_BWD, self.N)(input_array, out, ax, 1.0)
+        out = self._out(input_array, False, output_array, ax)
+        return get_plan(_lib.XF_C2C_BWD, self.N, form=self.form)(input_array, out, ax, 1.0)
 
 
 # ---------------------------------------------------------------------------
@@ -211,8 +215,8 @@ class ChebyshevBase(SpectralBase):
         if self.domain_factor() != 1:
             raise NotImplementedError("only the reference domain [-1, 1] is on the GPU path")
         ax = self.axis if axis is None else axis
-        out = self._out(input_array, True, output_array)
-        return get_plan(kind, self.N, self.basis_id)(input_array, out, ax)
+        out = self._out(input_array, True, output_array, ax)
+        return get_plan(kind, self.N, self.basis_id, self.form)(input_array, out, ax)
 
     def scalar_product(self, input_array, output_array=None, axis=None):
         return self._run(_lib.XF_CHEB_SCALAR, input_array, output_array, axis)
@@ -341,13 +345,15 @@ class TensorProductSpace:
     decomposition: every axis transform reads and writes the whole array.
     """
 
-    def __init__(self, comm=None, bases=(), axes=None, dtype=None, **kw):
+    def __init__(self, comm=None, bases=(), axes=None, dtype=None, form="plain", **kw):
         self.comm = comm
         self.bases = tuple(b.get_unplanned() for b in bases)
+        self.form = _lib.FORMS[form]
         nd = len(self.bases)
         for i, b in enumerate(self.bases):
             b.axis = i
             b.tensorproductspace = self
+            b.form = self.form
         self.axes = tuple(range(nd)) if axes is None else tuple(int(a) % nd for a in axes)
         first = self.bases[self.axes[-1]]
         if dtype is None:
@@ -355,9 +361,15 @@ class TensorProductSpace:
         self._dtype = np.dtype(dtype)
         if isinstance(first, R2C):
             assert self._dtype.char in "fdg"
-        r2c = [i for i, b in enumerate(self.bases) if isinstance(b, R2C)]
-        if len(r2c) > 1 or (r2c and r2c[0] != self.axes[-1]):
-            raise ValueError("the R2C axis must be the first one transformed (axes[-1])")
+        # the R2C axis needs real data: it must come before every C2C axis in
+        # the forward order (last axis of `axes` first)
+        order = list(reversed(self.axes))
+        r2c = [order.index(i) for i, b in enumerate(self.bases) if isinstance(b, R2C)]
+        c2c = [order.index(i) for i, b in enumerate(self.bases) if isinstance(b, C2C)]
+        if len(r2c) > 1 or (r2c and c2c and min(c2c) < r2c[0]):
+            raise ValueError("the R2C axis must be transformed before every C2C axis")
+        if r2c and self._dtype.char in "FDG":
+            raise ValueError("an R2C axis needs real physical data")
         self.forward = _Chain(self, "forward")
         self.backward = _Chain(self, "backward")
         self.scalar_product = _Chain(self, "scalar_product")

@@ -52,14 +52,15 @@ static int xform(int argc, char** argv) {
   long long outer = atoll(argv[5]), inner = atoll(argv[6]);
   int data_kind = atoi(argv[7]);
   double scl = atof(argv[8]);
+  const int form = getenv("SGPU_EMU_FORM") ? atoi(getenv("SGPU_EMU_FORM")) : SGPU_PLAIN_F64;
   LinePlan p;
   HostTables T;
-  int st = build_plan_host(kind, n, basis, SGPU_PLAIN_F64, p, T);
+  int st = build_plan_host(kind, n, basis, form, p, T);
   if (st != SGPU_OK) {
     fprintf(stderr, "plan status %d\n", st);
     return 3;
   }
-  size_t off[7];
+  size_t off[SGPU_NTAB];
   size_t sz = table_layout(T, off);
   unsigned char* img = (unsigned char*)malloc(sz);
   table_image(T, off, img);
@@ -86,7 +87,10 @@ static int xform(int argc, char** argv) {
   for (long long b = 0; b < nblocks; ++b) {
     double* smem = (double*)malloc(p.smem);
     for (size_t i = 0; i < nsm; ++i) smem[i] = std::numeric_limits<double>::quiet_NaN();
-    prog_dispatch<double>(p, in, out, dc, nlines, inner, scl, b, smem, 0, 1);
+    if (form == SGPU_MIXED_DF)
+      prog_dispatch<df>(p, in, out, dc, nlines, inner, scl, b, smem, 0, 1);
+    else
+      prog_dispatch<double>(p, in, out, dc, nlines, inner, scl, b, smem, 0, 1);
     free(smem);
   }
   write_exact(argv[10], out, nout);
@@ -100,6 +104,22 @@ int main(int argc, char** argv) {
   if (argc < 2) return 2;
   std::string mode = argv[1];
   if (mode == "xform") return xform(argc, argv);
+  if (mode == "dfops") {
+    // dfops count x.bin y.bin out.bin -> [round(x), x+y, x-y, x*y] per pair
+    long long n = atoll(argv[2]);
+    double* x = read_exact(argv[3], n);
+    double* y = read_exact(argv[4], n);
+    double* out = (double*)malloc(sizeof(double) * 4 * n);
+    for (long long i = 0; i < n; ++i) {
+      df a = df_from_double(x[i]), b = df_from_double(y[i]);
+      out[4 * i] = df_to_double(a);
+      out[4 * i + 1] = df_to_double(a + b);
+      out[4 * i + 2] = df_to_double(a - b);
+      out[4 * i + 3] = df_to_double(a * b);
+    }
+    write_exact(argv[5], out, 4 * n);
+    return 0;
+  }
   if (mode == "hlu") {
     long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
     long long ns = outer * inner;
@@ -130,6 +150,33 @@ int main(int argc, char** argv) {
         helmholtz_solve_prog<double>(b, u, fac, fac + cnt, fac + 2 * cnt, fac + 3 * cnt, N, inner, s);
     }
     write_exact(argv[8], u, cnt * w);
+    return 0;
+  }
+  if (mode == "hcached") {
+    // hcached N outer inner data_kind form alfa.bin beta.bin b.bin out.bin
+    long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]), form = atoi(argv[6]);
+    long long ns = outer * inner, M = N - 2;
+    double* a = read_exact(argv[7], ns);
+    double* be = read_exact(argv[8], ns);
+    size_t cnt = (size_t)outer * N * inner * (dk ? 2 : 1);
+    double* b = read_exact(argv[9], cnt);
+    double* u = (double*)malloc(sizeof(double) * cnt);
+    for (size_t i = 0; i < cnt; ++i) u[i] = 0.0;
+    void* fac = malloc(8 * 4 * (size_t)M * ns);
+    for (long long s = 0; s < ns; ++s) {
+      if (form) helmholtz_factor_prog<df>(N, a, be, (df*)fac, ns, s);
+      else helmholtz_factor_prog<double>(N, a, be, (double*)fac, ns, s);
+    }
+    for (long long t = 0; t < 2 * ns; ++t) {
+      long long s = t >> 1;
+      int par = (int)(t & 1);
+      if (form && dk) helmholtz_cached_solve_prog<df, cd>((const cd*)b, (cd*)u, (const df*)fac, N, inner, ns, s, par);
+      else if (form) helmholtz_cached_solve_prog<df, double>(b, u, (const df*)fac, N, inner, ns, s, par);
+      else if (dk) helmholtz_cached_solve_prog<double, cd>((const cd*)b, (cd*)u, (const double*)fac, N, inner, ns, s, par);
+      else helmholtz_cached_solve_prog<double, double>(b, u, (const double*)fac, N, inner, ns, s, par);
+    }
+    write_exact(argv[10], u, cnt);
     return 0;
   }
   if (mode == "hmatvec") {

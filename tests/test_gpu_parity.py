@@ -185,3 +185,50 @@ def test_cfg2_full_size(sg):
     assert rel(mv[..., :-2], f_hat.v[..., :-2]) < 1e-11
     fw = uq.forward()
     assert rel(fw[..., :-2], u_hat.v[..., :-2]) < 1e-11
+
+
+def test_reference_layout_solve_entry(sg, golden):
+    """sgpu_Solve_Helmholtz (reference-layout factors) agrees with the cache path."""
+    d = golden("helmholtz")
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(8, "F", dtype="D"),
+                                     sg.FunctionSpace(8, "F", dtype="d"),
+                                     sg.FunctionSpace(17, "C", bc=(0, 0))))
+    u, v = sg.TrialFunction(T), sg.TestFunction(T)
+    H = sg.chebyshev.la.Helmholtz(*sg.inner(v, -sg.div(sg.grad(u)) + 1000.0 * u))
+    f = dev(d["h8x8x17_f"])
+    out = torch.zeros_like(f)
+    H.solve_reference_layout(f, out)
+    assert rel(out, d["h8x8x17_u"]) < TOL
+
+
+MIXED_TOL = 1e-10   # the mixed form's bound against the FP64 oracle
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 17), (16, 12, 24)])
+def test_mixed_form_small(sg, golden, shape):
+    d = golden("cfg2_%dx%dx%d" % shape)
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(shape[0], "F", dtype="D"),
+                                     sg.FunctionSpace(shape[1], "F", dtype="d"),
+                                     sg.FunctionSpace(shape[2], "C", bc=(0, 0))), form="mixed")
+    u, v = sg.TrialFunction(T), sg.TestFunction(T)
+    H = sg.chebyshev.la.Helmholtz(*sg.inner(v, -sg.div(sg.grad(u)) + 1000.0 * u))
+    f_hat = sg.inner(v, sg.Array(T, buffer=d["fj"]))
+    assert rel(f_hat, d["f_hat"]) < MIXED_TOL
+    u_hat = H(f_hat, sg.Function(T))
+    assert rel(u_hat, d["u_hat"]) < MIXED_TOL
+    assert rel(u_hat.backward(), d["uq"]) < MIXED_TOL
+
+
+def test_mixed_form_cfg2_full_size(sg):
+    Nx, Ny, Nz = 256, 256, 257
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(Nx, "F", dtype="D"),
+                                     sg.FunctionSpace(Ny, "F", dtype="d"),
+                                     sg.FunctionSpace(Nz, "C", bc=(0, 0))), form="mixed")
+    u, v = sg.TrialFunction(T), sg.TestFunction(T)
+    H = sg.chebyshev.la.Helmholtz(*sg.inner(v, -sg.div(sg.grad(u)) + 1000.0 * u))
+    f = np.random.default_rng(0).standard_normal((Nx, Ny, Nz))
+    uq = H(sg.inner(v, sg.Array(T, buffer=f)), sg.Function(T)).backward()
+    bases = [("fourier", "C2C", Nx), ("fourier", "R2C", Ny), ("chebyshev", "SD", Nz)]
+    ref, _, _ = P.helmholtz_roundtrip(f, bases, 1000.0, 2)
+    err = rel(uq, ref)
+    assert err < MIXED_TOL, err

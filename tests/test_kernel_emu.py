@@ -207,3 +207,77 @@ def test_banded(emu, n, outer, inner, which, cplx):
         la.pdma_lu(data)
         ref = la.pdma_solve(u, data, axis=1)
     assert rel(got, ref) < 1e-13
+
+
+# --------------------------------------------------------------------------
+# mixed (double-float) form
+def test_df_conversions_and_ops(emu):
+    n = 20000
+    # magnitudes 1e-15..1e15; below 2^-75 the low word degrades gradually and
+    # below 2^-120 values flush to zero, which the mixed form accepts
+    x = rng.standard_normal(n) * 10.0 ** rng.uniform(-15, 15, n)
+    y = rng.standard_normal(n) * 10.0 ** rng.uniform(-3, 3, n)
+    x[:5] = [0.0, -0.0, 1.0, -1.0, 3.0]
+    y[:5] = [1.0, 2.0, -1.0, 0.0, 1e-20]
+    out = run(emu, ["dfops", n], [x, y], 4 * n).reshape(n, 4)
+    eps = 2.0 ** -46  # df carries ~46-48 significant bits (truncating split, sloppy product)
+    assert np.all(np.abs(out[:, 0] - x) <= eps * np.abs(x))
+    for j, ref in ((1, x + y), (2, x - y), (3, x * y)):
+        scale = np.maximum(np.abs(x), np.abs(y)) if j < 3 else np.abs(x * y)
+        assert np.all(np.abs(out[:, j] - ref) <= 8 * eps * scale + 1e-300), j
+
+
+def xform_df(emu, *a, **k):
+    os.environ["SGPU_EMU_FORM"] = "1"
+    try:
+        return xform(emu, *a, **k)
+    finally:
+        del os.environ["SGPU_EMU_FORM"]
+
+
+DF_TOL = 1e-12
+
+
+@pytest.mark.parametrize("n", [8, 16, 17, 43, 129, 256, 257])
+def test_df_fourier(emu, n):
+    x = rng.standard_normal((3, n, 5))
+    y = xform_df(emu, R2C, n, 0, x, 1, False, 1.0 / n, n // 2 + 1)
+    assert rel(y, S.r2c_forward(x, axis=1)) < DF_TOL
+    z = xform_df(emu, C2R, n, 0, y, 1, True, 1.0, n)
+    assert rel(z, S.r2c_backward(y, n, axis=1)) < DF_TOL
+    xc = rng.standard_normal((n, 4)) + 1j * rng.standard_normal((n, 4))
+    yc = xform_df(emu, C2C_FWD, n, 0, xc, 0, True, 1.0 / n)
+    assert rel(yc, S.c2c_forward(xc, axis=0)) < DF_TOL
+    assert rel(xform_df(emu, C2C_BWD, n, 0, yc, 0, True, 1.0), xc) < DF_TOL
+
+
+@pytest.mark.parametrize("n", [16, 17, 64, 129, 257])
+@pytest.mark.parametrize("basis", ["T", "SD", "SB"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_df_chebyshev(emu, n, basis, cplx):
+    x = rng.standard_normal((3, 2, n))
+    if cplx:
+        x = x + 1j * rng.standard_normal(x.shape)
+    b = BASIS[basis]
+    assert rel(xform_df(emu, CHEB_SCALAR, n, b, x, 2, cplx), S.cheb_scalar_product(x, basis, 2)) < DF_TOL
+    fw = S.cheb_forward(x, basis, 2)
+    assert rel(xform_df(emu, CHEB_BACKWARD, n, b, fw, 2, cplx), S.cheb_backward(fw, basis, 2)) < DF_TOL
+
+
+@pytest.mark.parametrize("N,outer,inner", [(8, 1, 3), (17, 4, 1), (33, 2, 5), (257, 3, 2)])
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("form", [0, 1])
+def test_helmholtz_cached(emu, N, outer, inner, cplx, form):
+    ns = outer * inner
+    alfa = -np.ones(ns)
+    beta = rng.uniform(0.5, 2000.0, ns)
+    f = rng.standard_normal((outer, N, inner))
+    if cplx:
+        f = f + 1j * rng.standard_normal(f.shape)
+    cnt = outer * N * inner * (2 if cplx else 1)
+    u = run(emu, ["hcached", N, outer, inner, int(cplx), form], [alfa, beta, f], cnt)
+    u = (u.view(np.complex128) if cplx else u).reshape(outer, N, inner)
+    to_sys = lambda a: np.moveaxis(a, 1, -1).reshape(ns, N)  # noqa: E731
+    uref = la.helmholtz_solve(to_sys(f), *la.helmholtz_lu(N, alfa, beta))
+    tol = 1e-13 if form == 0 else 1e-12
+    assert rel(to_sys(u)[:, :N - 2], uref[:, :N - 2]) < tol
