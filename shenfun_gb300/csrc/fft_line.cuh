@@ -173,6 +173,12 @@ SGPU_HD void stockham_generic(const Cx<R>* in, Cx<R>* out, int m, int Rr, int Ns
   }
 }
 
+}  // namespace sgpu
+
+#include "fft_reg.cuh"
+
+namespace sgpu {
+
 // Run all stages of a length-m FFT on `lines` lines stored with stride ld.
 // src holds the input; returns the buffer holding the output (src or dst).
 template <class R>
@@ -213,6 +219,7 @@ SGPU_HD void dft_lines(const LinePlan& p, Cx<R>* X, Cx<R>* A, Cx<R>* B, Cx<R>* s
                        int tid, int nth) {
   const int n = p.n, m = p.m, ld = p.ld;
   if (!p.rader) {
+    if (fft_fast<R>(p, X, A, lines, tid, nth)) return;
     Cx<R>* res = fft_stages<R>(p, X, A, lines, tid, nth);
     if (res != X) {
       for (int e = tid; e < lines * n; e += nth) {
@@ -230,7 +237,8 @@ SGPU_HD void dft_lines(const LinePlan& p, Cx<R>* X, Cx<R>* A, Cx<R>* B, Cx<R>* s
   }
   for (int t = tid; t < lines; t += nth) slot[2 * t] = X[(size_t)t * ld];
   SGPU_SYNC();
-  Cx<R>* r1 = fft_stages<R>(p, A, B, lines, tid, nth);
+  Cx<R>* r1 = A;
+  if (!fft_fast<R>(p, A, B, lines, tid, nth)) r1 = fft_stages<R>(p, A, B, lines, tid, nth);
   for (int t = tid; t < lines; t += nth) slot[2 * t + 1] = r1[(size_t)t * ld];
   SGPU_SYNC();
   // multiply by the kernel spectrum, conjugate: IDFT(y) = conj(DFT(conj(y)))
@@ -240,7 +248,8 @@ SGPU_HD void dft_lines(const LinePlan& p, Cx<R>* X, Cx<R>* A, Cx<R>* B, Cx<R>* s
   }
   SGPU_SYNC();
   Cx<R>* other = (r1 == A) ? B : A;
-  Cx<R>* r2 = fft_stages<R>(p, r1, other, lines, tid, nth);
+  Cx<R>* r2 = r1;
+  if (!fft_fast<R>(p, r1, other, lines, tid, nth)) r2 = fft_stages<R>(p, r1, other, lines, tid, nth);
   for (int e = tid; e < lines * m; e += nth) {
     int t = e / m, q = e - t * m;
     X[(size_t)t * ld + p.rout[q]] = slot[2 * t] + conj(r2[(size_t)t * ld + q]);

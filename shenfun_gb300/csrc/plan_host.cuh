@@ -119,7 +119,10 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   p.rader = (is_prime(n) && n >= 11) ? 1 : 0;
   p.m = p.rader ? n - 1 : n;
   if (!factorize(p.m, p.radix, &p.nstages)) return SGPU_ERR_UNSUPPORTED;
-  p.ld = n;  // >= m
+  // line stride: >= n and >= m + P for the two-pass exchange buffer of the
+  // register FFT (P <= 16 for the lengths that have one)
+  const bool fast = p.m == 16 || p.m == 32 || p.m == 64 || p.m == 128 || p.m == 256;
+  p.ld = fast ? (n > p.m + 16 ? n : p.m + 16) : n;
   p.nthreads = 256;
   // lines per CTA: X, A, B line buffers within ~96 KB of shared memory
   const size_t per_line = 3 * sizeof(cd) * (size_t)p.ld + 2 * sizeof(cd);
