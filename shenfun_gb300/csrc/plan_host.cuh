@@ -129,6 +129,8 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   int tlc = (int)((96 * 1024) / per_line);
   if (tlc > 16) tlc = 16;
   if (tlc < 1) tlc = 1;
+  // a power of two, so that the line loops split the 256 threads evenly
+  while (tlc & (tlc - 1)) tlc &= tlc - 1;
   p.tlc = tlc;
   p.smem = smem_bytes<double>(p.tlc, p.ld);
   if (p.smem > 220 * 1024) return SGPU_ERR_UNSUPPORTED;

@@ -104,6 +104,31 @@ int main(int argc, char** argv) {
   if (argc < 2) return 2;
   std::string mode = argv[1];
   if (mode == "xform") return xform(argc, argv);
+  if (mode == "lkcheck") {
+    // lkcheck: every (line, index) pair of the loop decompositions is visited
+    // exactly once for the thread counts the kernels launch with
+    const int Ls[] = {1, 2, 4, 8, 16, 32};
+    const int ns[] = {1, 2, 7, 16, 129, 257, 300};
+    const int nths[] = {1, 32, 128, 256};
+    for (int L : Ls)
+      for (int n : ns)
+        for (int nth : nths)
+          for (int rows = 0; rows < 2; ++rows) {
+            std::vector<int> hits((size_t)L * n, 0);
+            for (int tid = 0; tid < nth; ++tid) {
+              LK m = rows ? lk_rows(L, tid, nth) : lk_lines(L, tid, nth);
+              SGPU_FOR_LK(m, L, n, c, k) hits[(size_t)c * n + k] += 1;
+            }
+            for (int h : hits)
+              if (h != 1) {
+                fprintf(stderr, "lk coverage L=%d n=%d nth=%d rows=%d\n", L, n, nth, rows);
+                return 4;
+              }
+          }
+    FILE* f = fopen(argv[2], "wb");
+    fclose(f);
+    return 0;
+  }
   if (mode == "dfops") {
     // dfops count x.bin y.bin out.bin -> [round(x), x+y, x-y, x*y] per pair
     long long n = atoll(argv[2]);
