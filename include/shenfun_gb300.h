@@ -145,6 +145,45 @@ int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int64_t
                                 int64_t N, int64_t inner, int data_kind, int form,
                                 cudaStream_t stream);
 
+/* ---- per-wavenumber systems: banded + rank-2 upper semiseparable ----------
+ * M_s = sum_t coef[t][s] M_t, offsets -4..4 (even) plus, for term gen_term,
+ * M[k][j] = p_k q_j + r_k t_j for j >= k+2.  Replaces la.SolverGeneric1ND's
+ * per-wavenumber LU (la.py:1183-1434, SolverGeneric1ND_solve_data la.pyx:371)
+ * and chebyshev.la.Biharmonic's LU_Biharmonic / Biharmonic_Solve
+ * (chebyshev/la.py:354-558, la.pyx:975-1492).
+ *   bands [nterms][5][n] (device): row k of offsets -4, -2, 0, 2, 4
+ *   gens  [4][n] (device): p, q, r, t;   coef [nterms][nsys] (device)
+ *   fac   7 * ((n+1)/2) * 2 * nsys doubles (device, caller-allocated)
+ * The solve reads b and writes u in the (outer, Nb, inner) layout; the first
+ * n entries along the axis are the unknowns, the rest are left untouched. */
+int sgpu_band_sep_factor(int n, int nterms, int gen_term, const double* bands,
+                         const double* gens, const double* coef, int64_t nsys, double* fac,
+                         cudaStream_t stream);
+int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double* gens, int n,
+                        int64_t outer, int64_t Nb, int64_t inner, int data_kind,
+                        cudaStream_t stream);
+
+/* ---- Legendre spaces (Gauss-Legendre quadrature) --------------------------
+ * Replace legendre.Orthogonal / ShenDirichlet / ShenBiharmonic's transforms
+ * (legendre/bases.py:76-572): the 'recursive' kind (transforms.pyx:175-325)
+ * and the 'vandermonde' kind (spectralbase.py:472-483, 539-549) are one dense
+ * contraction per direction with the Shen stencil folded into the matrix.
+ */
+/* fastgl_wrap.pyx:31 leggauss(N): nodes ascending, weights; host pointers */
+int sgpu_leggauss(int N, double* x, double* w);
+typedef struct sgpu_legendre_plan sgpu_legendre_plan;
+int sgpu_legendre_plan_create(sgpu_legendre_plan** plan, int N, int basis, int form);
+int sgpu_legendre_plan_destroy(sgpu_legendre_plan* plan);
+/* copy the plan's nodes and weights to host arrays of N entries */
+int sgpu_legendre_nodes(const sgpu_legendre_plan* plan, double* x, double* w);
+/* direction 0: scalar product (SpectralBase.scalar_product, spectralbase.py:200-233)
+ *           1: forward (+ mass solve, spectralbase.py:235-263)
+ *           2: backward (spectralbase.py:265-313)
+ * in and out are (outer, N, inner) arrays and must not alias. */
+int sgpu_legendre_execute(const sgpu_legendre_plan* plan, int direction, const void* in,
+                          void* out, int64_t outer, int64_t inner, int data_kind,
+                          cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,7 +122,6 @@ struct RegDFT<R, 16> {
 template <class R, int P, int Q>
 SGPU_HD void fft_two_pass(const LinePlan& p, Cx<R>* src, Cx<R>* tmp, int lines, int tid,
                           int nth) {
-  const int m = P * Q;
   const int QP = Q + 1;
   // pass 1: P-point DFTs over n1
   for (int e = tid; e < lines * Q; e += nth) {

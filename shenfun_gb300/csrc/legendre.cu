@@ -1,0 +1,369 @@
+// Legendre spaces (Gauss-Legendre quadrature): nodes/weights and the dense
+// Vandermonde transforms of the plain FP64 form.
+//
+// The reference evaluates Legendre transforms with an O(N^2) three-term
+// recurrence per line (transforms.pyx:175-325, the default 'recursive' kind)
+// or a Vandermonde dot product (spectralbase.py:472-483, 539-549).  Both are
+// the same dense contraction; here it is one GEMM per direction with the
+// Shen stencil folded into a precomputed N x N matrix:
+//   scalar product:  out = f . diag(w) V K^T      (V_jk = L_k(x_j))
+//   backward:        u   = c . K V^T              (to_ortho folded in)
+// K is the stencil matrix with the reference's convention that the constant
+// entries of ShenDirichlet apply to every row (spectralbase.py:1504-1526), so
+// the scalar product keeps the orthogonal coefficients in the tail rows.
+// The matrices are built on the host in long double and stored in FP64.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "solvers.cuh"
+
+using namespace sgpu;
+
+typedef long double ld_t;
+
+// Gauss-Legendre nodes (ascending) and weights: Newton iteration on P_N from
+// Tricomi's asymptotic initial guesses, P_N and P_N' by the three-term
+// recurrence in long double (Golub & Welsch 1969 give the same rule; the
+// reference uses Bogaert's 2014 iteration-free method, legendre/fastgl).
+extern "C" int sgpu_leggauss(int N, double* x, double* w) {
+  if (N < 1 || !x || !w) return SGPU_ERR_ARG;
+  const ld_t pi = 3.141592653589793238462643383279502884L;
+  for (int i = 0; i < (N + 1) / 2; ++i) {
+    // i-th largest root
+    ld_t th = pi * (4.0L * (i + 1) - 1) / (4.0L * N + 2);
+    ld_t z = cosl(th) * (1 - (N - 1.0L) / (8.0L * N * N * N));
+    ld_t pp = 0;
+    for (int it = 0; it < 100; ++it) {
+      ld_t p0 = 1, p1 = z;
+      for (int k = 2; k <= N; ++k) {
+        ld_t p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (N == 1) {
+        p1 = z;
+        p0 = 1;
+      }
+      pp = N * (z * p1 - p0) / (z * z - 1);
+      ld_t dz = p1 / pp;
+      z -= dz;
+      if (fabsl(dz) < 1e-19L) {
+        // refresh the derivative at the converged root
+        p0 = 1;
+        p1 = z;
+        for (int k = 2; k <= N; ++k) {
+          ld_t p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+          p0 = p1;
+          p1 = p2;
+        }
+        pp = N * (z * p1 - p0) / (z * z - 1);
+        break;
+      }
+    }
+    ld_t wt = 2 / ((1 - z * z) * pp * pp);
+    x[N - 1 - i] = (double)z;
+    x[i] = (double)(-z);
+    w[i] = w[N - 1 - i] = (double)wt;
+  }
+  if (N % 2 == 1) x[N / 2] = 0.0;
+  return SGPU_OK;
+}
+
+namespace {
+
+// V_jk = L_k(x_j) in long double, x from the FP64 nodes
+void vandermonde(int N, const double* x, std::vector<ld_t>& V) {
+  V.assign((size_t)N * N, 0);
+  for (int j = 0; j < N; ++j) {
+    ld_t z = x[j], p0 = 1, p1 = z;
+    V[(size_t)j * N + 0] = 1;
+    if (N > 1) V[(size_t)j * N + 1] = z;
+    for (int k = 2; k < N; ++k) {
+      ld_t p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+      V[(size_t)j * N + k] = p2;
+      p0 = p1;
+      p1 = p2;
+    }
+  }
+}
+
+// stencil K[k][m] (row k, offset m = 0, 2, 4) of the Legendre bases
+void stencil(int basis, int N, std::vector<ld_t>& K2, std::vector<ld_t>& K4) {
+  K2.assign(N, 0);
+  K4.assign(N, 0);
+  if (basis == SGPU_BASIS_SD) {
+    for (int k = 0; k < N - 2; ++k) K2[k] = -1;  // constant: every row
+  } else if (basis == SGPU_BASIS_SB) {
+    // legendre/bases.py:564 {0: 1, 2: -(4n+10)/(2n+7), 4: (2n+3)/(2n+7)}, zero for k >= N-4
+    for (int k = 0; k < N - 4; ++k) {
+      K2[k] = -(4.0L * k + 10) / (2.0L * k + 7);
+      K4[k] = (2.0L * k + 3) / (2.0L * k + 7);
+    }
+  }
+}
+
+}  // namespace
+
+struct sgpu_legendre_plan {
+  int N, basis, form;
+  double* d_scalar;  // N x N: out = f . Ms
+  double* d_back;    // N x N: u = c . Mb
+  double* d_mass;    // LU'd mass bands (reciprocal diagonal), forward transform
+  double* d_nodes;   // x, w (2N)
+  std::vector<double> x, w;
+};
+
+extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int basis, int form) {
+  if (!out) return SGPU_ERR_ARG;
+  *out = nullptr;
+  if (N < 2 || N > 8192) return SGPU_ERR_ARG;
+  if (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SB) return SGPU_ERR_ARG;
+  if (form != SGPU_PLAIN_F64) return SGPU_ERR_UNSUPPORTED;
+  if (basis == SGPU_BASIS_SD && N < 4) return SGPU_ERR_ARG;
+  if (basis == SGPU_BASIS_SB && N < 8) return SGPU_ERR_ARG;
+  sgpu_legendre_plan* p = new (std::nothrow) sgpu_legendre_plan;
+  if (!p) return SGPU_ERR_NOMEM;
+  p->N = N;
+  p->basis = basis;
+  p->form = form;
+  p->x.resize(N);
+  p->w.resize(N);
+  sgpu_leggauss(N, p->x.data(), p->w.data());
+  std::vector<ld_t> V, K2, K4;
+  vandermonde(N, p->x.data(), V);
+  stencil(basis, N, K2, K4);
+  const int nb = basis == SGPU_BASIS_SD ? 2 : (basis == SGPU_BASIS_SB ? 4 : 0);
+  const int dim = N - nb;
+  // Ms[j][k] = w_j (V_jk + K2_k V_j,k+2 + K4_k V_j,k+4)
+  std::vector<double> Ms((size_t)N * N), Mb((size_t)N * N, 0.0);
+  for (int j = 0; j < N; ++j)
+    for (int k = 0; k < N; ++k) {
+      ld_t v = V[(size_t)j * N + k];
+      if (k + 2 < N) v += K2[k] * V[(size_t)j * N + k + 2];
+      if (k + 4 < N) v += K4[k] * V[(size_t)j * N + k + 4];
+      Ms[(size_t)j * N + k] = (double)((ld_t)p->w[j] * v);
+    }
+  // Mb[k][j] = V_jk + K2_k V_j,k+2 + K4_k V_j,k+4 for k < dim (rows k >= dim zero)
+  for (int k = 0; k < dim; ++k)
+    for (int j = 0; j < N; ++j) {
+      ld_t v = V[(size_t)j * N + k];
+      if (k + 2 < N) v += K2[k] * V[(size_t)j * N + k + 2];
+      if (k + 4 < N) v += K4[k] * V[(size_t)j * N + k + 4];
+      Mb[(size_t)k * N + j] = (double)v;
+    }
+  // mass matrix (legendre/matrices.py:121-135, :179-192) LU'd with TDMA/PDMA_LU
+  std::vector<double> mass;
+  std::vector<ld_t> h(N);
+  for (int k = 0; k < N; ++k) h[k] = 2.0L / (2 * k + 1);
+  if (nb == 0) {
+    mass.resize(N);
+    for (int k = 0; k < N; ++k) mass[k] = (double)(1 / h[k]);
+  } else if (nb == 2) {
+    mass.assign(3 * (size_t)dim, 0.0);
+    double* ld = &mass[0];
+    double* d = &mass[dim];
+    double* ud = &mass[2 * dim + 2];
+    for (int k = 0; k < dim; ++k) d[k] = (double)(h[k] + h[k + 2]);
+    for (int k = 0; k < dim - 2; ++k) ld[k] = ud[k] = (double)(-h[k + 2]);
+    tdma_lu_prog(mass.data(), dim);
+    for (int k = 0; k < dim; ++k) d[k] = 1.0 / d[k];
+  } else {
+    mass.assign(5 * (size_t)dim, 0.0);
+    double* a = &mass[0];
+    double* b = &mass[dim];
+    double* d = &mass[2 * dim];
+    double* e = &mass[3 * dim + 2];
+    double* f = &mass[4 * dim + 4];
+    for (int i = 0; i < dim; ++i) {
+      ld_t I = i;
+      d[i] = (double)((-4 * I - 10) * (-4 * I - 10) * h[i + 2] / ((2 * I + 7) * (2 * I + 7)) +
+                      (2 * I + 3) * (2 * I + 3) * h[i + 4] / ((2 * I + 7) * (2 * I + 7)) + h[i]);
+    }
+    for (int i = 0; i < dim - 2; ++i) {
+      ld_t I = i;
+      b[i] = e[i] = (double)((-4 * I - 18) * (2 * I + 3) * h[i + 4] / ((2 * I + 7) * (2 * I + 11)) +
+                             (-4 * I - 10) * h[i + 2] / (2 * I + 7));
+    }
+    for (int i = 0; i < dim - 4; ++i) {
+      ld_t I = i;
+      a[i] = f[i] = (double)((2 * I + 3) * h[i + 4] / (2 * I + 7));
+    }
+    pdma_lu_prog(mass.data(), dim);
+    for (int k = 0; k < dim; ++k) d[k] = 1.0 / d[k];
+  }
+  size_t nbytes = sizeof(double) * (2 * (size_t)N * N + mass.size() + 2 * (size_t)N);
+  void* dev = nullptr;
+  if (cudaMalloc(&dev, nbytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete p;
+    return SGPU_ERR_NOMEM;
+  }
+  double* b = (double*)dev;
+  p->d_scalar = b;
+  p->d_back = b + (size_t)N * N;
+  p->d_mass = b + 2 * (size_t)N * N;
+  p->d_nodes = p->d_mass + mass.size();
+  cudaError_t e1 = cudaMemcpy(p->d_scalar, Ms.data(), sizeof(double) * Ms.size(), cudaMemcpyHostToDevice);
+  cudaError_t e2 = cudaMemcpy(p->d_back, Mb.data(), sizeof(double) * Mb.size(), cudaMemcpyHostToDevice);
+  cudaError_t e3 = cudaMemcpy(p->d_mass, mass.data(), sizeof(double) * mass.size(), cudaMemcpyHostToDevice);
+  cudaError_t e4 = cudaMemcpy(p->d_nodes, p->x.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+  cudaError_t e5 = cudaMemcpy(p->d_nodes + N, p->w.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+  if (e1 || e2 || e3 || e4 || e5) {
+    cudaFree(dev);
+    cudaGetLastError();
+    delete p;
+    return SGPU_ERR_CUDA;
+  }
+  *out = p;
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_legendre_plan_destroy(sgpu_legendre_plan* p) {
+  if (!p) return SGPU_OK;
+  cudaFree(p->d_scalar);
+  delete p;
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_legendre_nodes(const sgpu_legendre_plan* p, double* x, double* w) {
+  if (!p || !x || !w) return SGPU_ERR_ARG;
+  std::memcpy(x, p->x.data(), sizeof(double) * p->N);
+  std::memcpy(w, p->w.data(), sizeof(double) * p->N);
+  return SGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 GEMM along lines: out(l, k) = sum_j in(l, j) M[j][k] for every line l
+// of a (outer, N, inner) array (complex lines: real and imaginary parts are
+// two rows).  64 x 64 output tiles, K steps of 16, 256 threads with 4 x 4
+// register blocks; rows are (line, part) pairs.
+namespace {
+const int TM = 64, TN = 64, TK = 16;
+}
+
+__global__ void __launch_bounds__(256) k_line_gemm_f64(const double* in, double* out, const double* M,
+                                                       int N, int64_t nrows, int64_t inner,
+                                                       int cplx) {
+  __shared__ double As[TK][TM + 1];
+  __shared__ double Bs[TK][TN + 1];
+  const int tid = threadIdx.x;
+  const int64_t row0 = (int64_t)blockIdx.x * TM;
+  const int col0 = blockIdx.y * TN;
+  const int tr = tid / 16, tc = tid % 16;  // 16 x 16 threads, 4 x 4 each
+  double acc[4][4] = {};
+  // element (row, j): row = line * (1 + cplx) + part
+  auto off = [&](int64_t row, int64_t j) -> int64_t {
+    int64_t l = cplx ? (row >> 1) : row;
+    int part = cplx ? (int)(row & 1) : 0;
+    int64_t o = l / inner, i = l - o * inner;
+    int64_t e = (o * N + j) * inner + i;
+    return cplx ? 2 * e + part : e;
+  };
+  for (int k0 = 0; k0 < N; k0 += TK) {
+    // A tile: TM rows x TK columns (4 per thread)
+    for (int e = tid; e < TM * TK; e += 256) {
+      int r = e / TK, kk = e % TK;
+      int64_t row = row0 + r;
+      int j = k0 + kk;
+      As[kk][r] = (row < nrows && j < N) ? in[off(row, j)] : 0.0;
+    }
+    for (int e = tid; e < TK * TN; e += 256) {
+      int kk = e / TN, c = e % TN;
+      int j = k0 + kk, col = col0 + c;
+      Bs[kk][c] = (j < N && col < N) ? M[(size_t)j * N + col] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][tr * 4 + i];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) b[i] = Bs[kk][tc * 4 + i];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[i][q] = fma(a[i], b[q], acc[i][q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int64_t row = row0 + tr * 4 + i;
+    if (row >= nrows) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int col = col0 + tc * 4 + q;
+      if (col < N) out[off(row, col)] = acc[i][q];
+    }
+  }
+}
+
+// mass solve along lines after the scalar product (forward transform)
+template <class T>
+__global__ void k_legendre_mass(T* u, const double* mass, int N, int basis, int64_t nlines,
+                                int64_t inner) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nlines) return;
+  const int nb = basis == SGPU_BASIS_SD ? 2 : (basis == SGPU_BASIS_SB ? 4 : 0);
+  const int dim = N - nb;
+  T* base = u + sys_base(s, N, inner);
+  Line<T> v{base, inner};
+  if (nb == 0) {
+    for (int k = 0; k < N; ++k) v[k] = mulr(v[k], mass[k]);
+    return;
+  }
+  if (nb == 2) {
+    const double* ld = mass;
+    const double* di = mass + dim;
+    const double* ud = mass + 2 * dim + 2;
+    for (int i = 2; i < dim; ++i) v[i] = v[i] - mulr(v[i - 2], ld[i - 2]);
+    v[dim - 1] = mulr(v[dim - 1], di[dim - 1]);
+    v[dim - 2] = mulr(v[dim - 2], di[dim - 2]);
+    for (int i = dim - 3; i >= 0; --i) v[i] = mulr(v[i] - mulr(v[i + 2], ud[i]), di[i]);
+  } else {
+    const double* a = mass;
+    const double* b = mass + dim;
+    const double* di = mass + 2 * dim;
+    const double* e = mass + 3 * dim + 2;
+    const double* f = mass + 4 * dim + 4;
+    v[2] = v[2] - mulr(v[0], b[0]);
+    v[3] = v[3] - mulr(v[1], b[1]);
+    for (int k = 4; k < dim; ++k) v[k] = v[k] - (mulr(v[k - 2], b[k - 2]) + mulr(v[k - 4], a[k - 4]));
+    v[dim - 1] = mulr(v[dim - 1], di[dim - 1]);
+    v[dim - 2] = mulr(v[dim - 2], di[dim - 2]);
+    v[dim - 3] = mulr(v[dim - 3] - mulr(v[dim - 1], e[dim - 3]), di[dim - 3]);
+    v[dim - 4] = mulr(v[dim - 4] - mulr(v[dim - 2], e[dim - 4]), di[dim - 4]);
+    for (int k = dim - 5; k >= 0; --k)
+      v[k] = mulr(v[k] - mulr(v[k + 2], e[k]) - mulr(v[k + 4], f[k]), di[k]);
+  }
+  for (int k = dim; k < N; ++k) v[k] = zero_of(T());
+}
+
+// direction: 0 = scalar product, 1 = forward (scalar product + mass solve), 2 = backward
+extern "C" int sgpu_legendre_execute(const sgpu_legendre_plan* p, int direction, const void* in,
+                                     void* out, int64_t outer, int64_t inner, int data_kind,
+                                     cudaStream_t stream) {
+  if (!p || !in || !out || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  if (direction < 0 || direction > 2) return SGPU_ERR_ARG;
+  if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
+  if (in == out) return SGPU_ERR_ARG;  // the GEMM reads every input row of a tile
+  const int64_t nlines = outer * inner;
+  if (nlines == 0) return SGPU_OK;
+  const int cplx = data_kind == SGPU_COMPLEX;
+  const int64_t nrows = nlines * (1 + cplx);
+  dim3 grid((unsigned)((nrows + TM - 1) / TM), (unsigned)((p->N + TN - 1) / TN));
+  if (grid.x > 0x7fffffffu) return SGPU_ERR_ARG;
+  const double* M = direction == 2 ? p->d_back : p->d_scalar;
+  k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, nrows, inner, cplx);
+  if (direction == 1) {
+    const unsigned nb = (unsigned)((nlines + 127) / 128);
+    if (cplx)
+      k_legendre_mass<cd><<<nb, 128, 0, stream>>>((cd*)out, p->d_mass, p->N, p->basis, nlines, inner);
+    else
+      k_legendre_mass<double><<<nb, 128, 0, stream>>>((double*)out, p->d_mass, p->N, p->basis, nlines, inner);
+  }
+  return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
+}

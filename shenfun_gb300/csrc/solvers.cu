@@ -189,3 +189,44 @@ extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* f
     return SGPU_ERR_ARG;
   return finish();
 }
+
+// ---- banded + semiseparable per-wavenumber systems --------------------------
+__global__ void k_band_sep_factor(BandSepDesc d, double* fac, int64_t nsys) {
+  int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ch < 2 * nsys) band_sep_factor_prog(d, fac, nsys, ch);
+}
+
+template <class T>
+__global__ void k_band_sep_solve(const T* b, T* u, const double* fac, const double* gens, int n,
+                                 int64_t Nb, int64_t inner, int64_t nsys) {
+  int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ch < 2 * nsys) band_sep_solve_prog<T>(b, u, fac, gens, n, Nb, inner, nsys, ch);
+}
+
+extern "C" int sgpu_band_sep_factor(int n, int nterms, int gen_term, const double* bands,
+                                    const double* gens, const double* coef, int64_t nsys,
+                                    double* fac, cudaStream_t stream) {
+  if (n < 2 || nterms < 1 || nterms > 3 || gen_term >= nterms || !bands || !coef || !fac ||
+      nsys < 0)
+    return SGPU_ERR_ARG;
+  if ((gen_term >= 0) != (gens != nullptr)) return SGPU_ERR_ARG;
+  if (nsys == 0) return SGPU_OK;
+  BandSepDesc d{n, nterms, gen_term, bands, gens, coef};
+  k_band_sep_factor<<<nblk(2 * nsys), kThreads, 0, stream>>>(d, fac, nsys);
+  return finish();
+}
+
+extern "C" int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double* gens,
+                                   int n, int64_t outer, int64_t Nb, int64_t inner, int data_kind,
+                                   cudaStream_t stream) {
+  if (!b || !u || !fac || n < 2 || Nb < n || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_band_sep_solve<cd><<<nblk(2 * nsys), kThreads, 0, stream>>>((const cd*)b, (cd*)u, fac, gens, n, Nb, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_band_sep_solve<double><<<nblk(2 * nsys), kThreads, 0, stream>>>((const double*)b, (double*)u, fac, gens, n, Nb, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}

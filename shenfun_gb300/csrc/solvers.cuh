@@ -214,6 +214,157 @@ SGPU_HD void helmholtz_matvec_prog(const T* v_all, T* b_all, const double* alfa,
   b[M + 1] = zero_of(T());
 }
 
+// ---- banded + rank-2 upper semiseparable systems ---------------------------
+// One system per Fourier wavenumber: M = sum_t c_t M_t over up to 3 terms,
+// where every M_t has even offsets in {-4, -2, 0, 2, 4} and at most one term
+// (gen_term) also has a strictly-upper part of the form
+//   M_t[k][j] = p_k q_j + r_k t_j     for j >= k + 2, j - k even.
+// This covers every per-wavenumber system of the Galerkin spaces here:
+// Chebyshev ShenBiharmonic a0 S + alpha A + beta B (S = SSBSB: rank-2 upper,
+// chebyshev/matrices.py:1444-1458), Chebyshev ShenDirichlet alpha A + beta B
+// (A = ASDSD: constant rows, rank 1), Legendre ShenDirichlet/ShenBiharmonic
+// (banded only, la.py TDMA/PDMA).  Even and odd unknowns decouple; each
+// parity is a chain with offsets -2..2 in chain index.
+//
+// Gaussian elimination without pivoting keeps the structure: row c of U is
+// diag_c, band entries corr1_c (column c+1), corr2_c (column c+2) and the
+// generator part P_c q_j + R_c t_j for j >= c+1; L has two sub-diagonals
+// (L1, L0).  Eliminating column c from rows c+1 and c+2 only rescales their
+// generator coefficients (P, R) and touches O(1) band entries, so factor and
+// solve are O(n) per chain.  (The reference's tailored Chebyshev solvers
+// LU_Helmholtz / LU_Biharmonic, la.pyx:717-763 and la.pyx:975-1233, exploit
+// the same structure with running sums; the reference's generic path for
+// these systems is a sparse LU per wavenumber, la.py:1231-1364.)
+//
+// Factor cache: fac[q][c][chain], q = L0, L1, 1/diag, corr1, corr2, P, R,
+// chain = 2 * system + parity, c < m = (n + 1) / 2.
+struct BandSepDesc {
+  int n;                 // unknowns (dofs) per system
+  int nterms;            // <= 3
+  int gen_term;          // term with the semiseparable upper part, -1 if none
+  const double* bands;   // [nterms][5][n]: offsets -4, -2, 0, 2, 4 at row k
+  const double* gens;    // [4][n]: p_k, q_j, r_k, t_j of gen_term
+  const double* coef;    // [nterms][nsys]
+};
+
+SGPU_HD double bs_band(const BandSepDesc& d, int64_t nsys, int64_t s, int off_idx, int k) {
+  double v = 0.0;
+  for (int t = 0; t < d.nterms; ++t)
+    v += d.coef[t * nsys + s] * d.bands[((size_t)t * 5 + off_idx) * d.n + k];
+  return v;
+}
+
+SGPU_HD void band_sep_factor_prog(const BandSepDesc& d, double* fac, int64_t nsys, int64_t chain) {
+  const int64_t s = chain >> 1;
+  const int par = (int)(chain & 1);
+  const int n = d.n;
+  const int m = (n + 1) / 2;
+  const int64_t nch = 2 * nsys;
+  const double cg = d.gen_term >= 0 ? d.coef[d.gen_term * nsys + s] : 0.0;
+  const double* gp = d.gens;
+  const double* gq = d.gens ? d.gens + n : nullptr;
+  const double* gr = d.gens ? d.gens + 2 * n : nullptr;
+  const double* gt = d.gens ? d.gens + 3 * n : nullptr;
+  // window rows c, c+1, c+2: sub2, sub1, diag, corr1, corr2, P, R
+  double W[3][7];
+  auto load_row = [&](double* r, int c) {
+    const int k = 2 * c + par;
+    if (k >= n) {
+      for (int i = 0; i < 7; ++i) r[i] = 0.0;
+      return;
+    }
+    r[0] = bs_band(d, nsys, s, 0, k);
+    r[1] = bs_band(d, nsys, s, 1, k);
+    r[2] = bs_band(d, nsys, s, 2, k);
+    r[3] = bs_band(d, nsys, s, 3, k);
+    r[4] = bs_band(d, nsys, s, 4, k);
+    r[5] = d.gens ? cg * gp[k] : 0.0;
+    r[6] = d.gens ? cg * gr[k] : 0.0;
+  };
+  auto Q = [&](int c) { const int k = 2 * c + par; return (d.gens && k < n) ? gq[k] : 0.0; };
+  auto T = [&](int c) { const int k = 2 * c + par; return (d.gens && k < n) ? gt[k] : 0.0; };
+  load_row(W[0], 0);
+  load_row(W[1], 1);
+  load_row(W[2], 2);
+  for (int c = 0; c < m; ++c) {
+    double* r0 = W[c % 3];
+    double* r1 = W[(c + 1) % 3];
+    double* r2 = W[(c + 2) % 3];
+    const double piv = r0[2];
+    const double dinv = 1.0 / piv;
+    const double u1 = r0[3] + r0[5] * Q(c + 1) + r0[6] * T(c + 1);  // U(c, c+1)
+    const double u2 = r0[4] + r0[5] * Q(c + 2) + r0[6] * T(c + 2);  // U(c, c+2)
+    double l1 = 0.0, l0 = 0.0;
+    if (c + 1 < m) {
+      l1 = r1[1] * dinv;
+      r1[2] -= l1 * u1;
+      r1[3] -= l1 * r0[4];
+      r1[5] -= l1 * r0[5];
+      r1[6] -= l1 * r0[6];
+    }
+    if (c + 2 < m) {
+      l0 = r2[0] * dinv;
+      r2[1] -= l0 * u1;
+      r2[2] -= l0 * u2;
+      r2[5] -= l0 * r0[5];
+      r2[6] -= l0 * r0[6];
+    }
+    // multipliers belong to the rows they eliminate
+    if (c + 1 < m) fac[((size_t)1 * m + c + 1) * nch + chain] = l1;
+    if (c + 2 < m) fac[((size_t)0 * m + c + 2) * nch + chain] = l0;
+    if (c == 0) {
+      fac[((size_t)1 * m + 0) * nch + chain] = 0.0;
+      fac[((size_t)0 * m + 0) * nch + chain] = 0.0;
+      if (m > 1) fac[((size_t)0 * m + 1) * nch + chain] = 0.0;
+    }
+    fac[((size_t)2 * m + c) * nch + chain] = dinv;
+    fac[((size_t)3 * m + c) * nch + chain] = r0[3];
+    fac[((size_t)4 * m + c) * nch + chain] = r0[4];
+    fac[((size_t)5 * m + c) * nch + chain] = r0[5];
+    fac[((size_t)6 * m + c) * nch + chain] = r0[6];
+    load_row(r0, c + 3);  // slot of row c becomes row c+3
+  }
+}
+
+template <class T>
+SGPU_HD void band_sep_solve_prog(const T* b_all, T* u_all, const double* fac, const double* gens,
+                                 int n, int64_t Nb, int64_t inner, int64_t nsys, int64_t chain) {
+  const int64_t s = chain >> 1;
+  const int par = (int)(chain & 1);
+  const int m = (n + 1) / 2;
+  const int64_t nch = 2 * nsys;
+  const int64_t base = sys_base(s, Nb, inner);
+  const T* f = b_all + base;
+  T* u = u_all + base;
+  auto F = [&](int q, int c) { return fac[((size_t)q * m + c) * nch + chain]; };
+  int top = -1;
+  T y1 = zero_of(T()), y2 = zero_of(T());  // y_{c-1}, y_{c-2}
+  for (int c = 0; c < m; ++c) {
+    const int k = 2 * c + par;
+    if (k >= n) break;
+    T y = f[k * inner] - mulr(y1, F(1, c)) - mulr(y2, F(0, c));
+    u[k * inner] = y;
+    y2 = y1;
+    y1 = y;
+    top = c;
+  }
+  T sq = zero_of(T()), st = zero_of(T());  // sum_{j >= c+1} q_j u_j, t_j u_j
+  T up1 = zero_of(T()), up2 = zero_of(T());
+  for (int c = top; c >= 0; --c) {
+    const int k = 2 * c + par;
+    T v = u[k * inner] - mulr(up1, F(3, c)) - mulr(up2, F(4, c));
+    if (gens) v = v - mulr(sq, F(5, c)) - mulr(st, F(6, c));
+    v = mulr(v, F(2, c));
+    u[k * inner] = v;
+    if (gens) {
+      sq = sq + mulr(v, gens[n + k]);
+      st = st + mulr(v, gens[3 * n + k]);
+    }
+    up2 = up1;
+    up1 = v;
+  }
+}
+
 // ---- factorisation cache: interleaved, reciprocal-pivot layout -------------
 // fac[q][k][s] for q = 0..3 (L, 1/d0, d1, d2), k in [0, M), s a system:
 // consecutive systems are contiguous, so thread s reads row k coalesced.

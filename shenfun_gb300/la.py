@@ -212,10 +212,66 @@ class SolverGeneric1ND:
             beta = B.scale if B is not None else np.zeros(shape)
             self._impl = Helmholtz(_tp("ASDSDmat", alfa, T, ax), _tp("BSDSDmat", beta, T, ax))
         else:
-            raise NotImplementedError(f"SolverGeneric1ND for {base.family()} {base.short_name()} {keys}")
+            self._impl = BandSepSolver(mats)
 
     def __call__(self, b, u=None, constraints=()):
         return self._impl(b, u, constraints)
+
+
+class BandSepSolver:
+    """Per-wavenumber systems sum_t scale_t M_t with banded + rank-2 upper
+    semiseparable M_t, factorised once on the device (sgpu_band_sep_factor)
+    and solved per call (sgpu_band_sep_solve).  Used for Legendre
+    ShenDirichlet / ShenBiharmonic and Chebyshev ShenBiharmonic."""
+
+    def __init__(self, mats):
+        from .matrices import band_sep_term
+        require_cuda()
+        mats = sorted(list(mats), key=lambda m: -m.pmat.order)
+        T, ax = mats[0].space, mats[0].axis
+        base = T.bases[ax]
+        self.T, self.axis, self.N = T, ax, base.N
+        terms = [band_sep_term(base, m.pmat.order) for m in mats]
+        self.n = terms[0][0].shape[1]
+        self.gen_term = next((i for i, (_, g) in enumerate(terms) if g is not None), -1)
+        if sum(g is not None for _, g in terms) > 1:
+            raise NotImplementedError("more than one semiseparable term")
+        bands = np.ascontiguousarray(np.stack([b for b, _ in terms]))
+        shape = list(T.shape(True))
+        shape[ax] = 1
+        coefs = np.stack([np.broadcast_to(np.asarray(m.scale, dtype=float), shape).reshape(-1)
+                          for m in mats])
+        self.nsys = coefs.shape[1]
+        self._outer, _, self._inner = view3(tuple(T.shape(True)), ax)
+        self._bands = torch.as_tensor(bands, device="cuda")
+        self._coef = torch.as_tensor(np.ascontiguousarray(coefs), device="cuda")
+        self._gens = (torch.as_tensor(np.ascontiguousarray(terms[self.gen_term][1]), device="cuda")
+                      if self.gen_term >= 0 else None)
+        m = (self.n + 1) // 2
+        self._fac = torch.empty(7 * m * 2 * self.nsys, dtype=torch.float64, device="cuda")
+        _lib.call("sgpu_band_sep_factor", self.n, len(mats), self.gen_term, ptr(self._bands),
+                  ptr(self._gens) if self._gens is not None else None, ptr(self._coef),
+                  self.nsys, ptr(self._fac), stream_handle())
+
+    def __call__(self, b, u=None, constraints=()):
+        b = _raw(b)
+        if u is None:
+            u = torch.zeros_like(b)
+        ur = _raw(u)
+        outer, Nb, inner = view3(tuple(b.shape), self.axis)
+        if (outer, inner) != (self._outer, self._inner) or Nb != self.N:
+            raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
+        _lib.call("sgpu_band_sep_solve", ptr(b), ptr(ur), ptr(self._fac),
+                  ptr(self._gens) if self._gens is not None else None, self.n, outer, Nb, inner,
+                  data_kind(b), stream_handle())
+        return u
+
+
+class Biharmonic(BandSepSolver):
+    """Chebyshev ShenBiharmonic solver for a0 S + alfa A + beta B
+    (chebyshev/la.py:354-558): the same structured per-wavenumber LU, valid for
+    even and odd N (the reference's tailored kernel assumes equal even/odd
+    lengths, la.pyx:1356-1362; its odd-N path is a sparse LU per wavenumber)."""
 
 
 def _tp(key, scale, T, ax):

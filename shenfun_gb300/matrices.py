@@ -140,14 +140,118 @@ def galerkin_matrix(space, order):
         ("legendre", "SD", 0): leg_sd_B,
         ("legendre", "SB", 0): leg_sb_B,
     }
+    keys = {0: "B", 2: "A", 4: "S"}
     if (fam, name, order) == ("legendre", "SD", 2):
         # (phi''_j, phi_k) = -(phi'_j, phi'_k) = -A (integration by parts)
         M = leg_sd_A(N, space)
         M[0] = -M[0]
         M.key = "ASDSDmat"
         M.sign = -1
-        return M
-    fn = table.get((fam, name, order))
-    if fn is None:
+    elif (fam, name, order) in table:
+        M = table[(fam, name, order)](N, space)
+    elif fam == "legendre" and name == "SB" and order in (2, 4):
+        b, _ = band_sep_term(space, order)
+        n = b.shape[1]
+        diags = {off: b[r, max(0, -off):n - max(0, off)] for r, off in enumerate((-4, -2, 0, 2, 4))
+                 if np.any(b[r])}
+        M = SpectralMatrix(keys[order] + "SBSBmat", diags, (n, n), space, space)
+    else:
         raise NotImplementedError(f"matrix of order {order} for {fam} {name}")
-    return fn(N, space)
+    M.order = order
+    return M
+
+
+# ---------------------------------------------------------------------------
+# Banded + semiseparable description of (phi_j^{(order)}, phi_k) for the
+# per-wavenumber solver (sgpu_band_sep_*): bands[5][n] at offsets -4..4 (row
+# k holds M[k][k+off]) and, for the one term with a dense upper part, the
+# generators p, q, r, t with M[k][j] = p_k q_j + r_k t_j for j >= k+2.
+def band_sep_dense(bands, gens):
+    """Dense matrix of one band/semiseparable term (for tests and checks)."""
+    n = bands.shape[1]
+    M = np.zeros((n, n))
+    for r, off in enumerate((-4, -2, 0, 2, 4)):
+        for k in range(n):
+            if 0 <= k + off < n:
+                M[k, k + off] += bands[r, k]
+    if gens is not None:
+        for k in range(n):
+            for j in range(k + 2, n, 2):
+                M[k, j] += gens[0, k] * gens[1, j] + gens[2, k] * gens[3, j]
+    return M
+
+
+def band_sep_term(space, order):
+    """(bands (5, n), gens (4, n) or None) for one Galerkin matrix."""
+    fam, name, N = space.family(), space.short_name(), space.N
+    nb = {"SD": 2, "SB": 4}[name]
+    n = N - nb
+    k = np.arange(n, dtype=float)
+    bands = np.zeros((5, n))
+    gens = None
+    if fam == "chebyshev" and name == "SD":
+        if order == 0:
+            h = cheb_norm_sq(N)
+            bands[2] = h[:-2] + h[2:]
+            bands[1, 2:] = -h[1]      # M[k][k-2]
+            bands[3, :-2] = -h[1]     # M[k][k+2]
+        elif order == 2:
+            bands[2] = -2 * np.pi * (k + 1) * (k + 2)
+            gens = np.zeros((4, n))
+            gens[0] = -4 * np.pi * (k + 1)
+            gens[1] = 1.0
+        else:
+            raise NotImplementedError(order)
+    elif fam == "chebyshev" and name == "SB":
+        if order == 0:
+            B = cheb_sb_B(N)
+            bands[2] = B[0]
+            bands[3, :-2] = B[2]
+            bands[4, :-4] = B[4]
+            bands[1, 2:] = B[-2]
+            bands[0, 4:] = B[-4]
+        elif order == 2:
+            bands[2] = -4 * ((k + 1) * (k + 2) ** 2) / (k + 3) * np.pi
+            bands[3, :-2] = 2 * (k[:-2] + 1) * (k[:-2] + 2) * np.pi
+            bands[1, 2:] = 2 * (k[2:] - 1) * (k[2:] + 2) * np.pi
+        elif order == 4:
+            bands[2] = np.pi * 8 * (k + 1) ** 2 * (k + 2) * (k + 4)
+            gens = np.zeros((4, n))
+            gens[0] = 8 * np.pi * (k + 1) * (k + 2) * k * (k + 4)
+            gens[1] = 1.0 / (k + 3)
+            gens[2] = 24 * np.pi * (k + 1) * (k + 2)
+            gens[3] = (k + 2) ** 2 / (k + 3)
+        else:
+            raise NotImplementedError(order)
+    elif fam == "legendre" and name == "SD":
+        h = leg_norm_sq(N)
+        if order == 0:
+            bands[2] = h[:-2] + h[2:]
+            bands[3, :-2] = -h[2:-2]        # M[k][k+2] = -h_{k+2}
+            bands[1, 2:] = -h[2:-2]         # M[k][k-2] = -h_k
+        elif order == 2:
+            bands[2] = -(4 * k + 6)
+        else:
+            raise NotImplementedError(order)
+    elif fam == "legendre" and name == "SB":
+        if order == 0:
+            B = leg_sb_B(N)
+            bands[2] = B[0]
+            bands[3, :-2] = B[2]
+            bands[4, :-4] = B[4]
+            bands[1, 2:] = B[-2]
+            bands[0, 4:] = B[-4]
+        elif order == 2:
+            # -(phi'_j, phi'_k): ASBSB {0: 2(2k+3)(1+g_k), +-2: -2(2k+3)} (legendre/matrices.py:318-340)
+            g = (2 * k + 3) / (2 * k + 7)
+            bands[2] = -2 * (2 * k + 3) * (1 + g)
+            bands[3, :-2] = 2 * (2 * k[:-2] + 3)
+            bands[1, 2:] = 2 * (2 * k[:-2] + 3)
+        elif order == 4:
+            # (phi''_j, phi''_k) = 2 (2k+3)^2 (2k+5) (legendre/matrices.py:425-440)
+            bands[2] = 2 * (2 * k + 3) ** 2 * (2 * k + 5)
+        else:
+            raise NotImplementedError(order)
+    else:
+        raise NotImplementedError(f"{fam} {name}")
+    return bands, gens

@@ -459,7 +459,8 @@ class TensorProductSpace:
             last = step == nsteps - 1
             if last:
                 dst = out
-            elif cur is not inp and tuple(new_shape) == tuple(cur.shape) and dt == cur.dtype:
+            elif (cur is not inp and tuple(new_shape) == tuple(cur.shape) and dt == cur.dtype
+                  and getattr(b, "inplace_ok", True)):
                 dst = cur  # same-size transform: in place on a work array
             else:
                 dst = self._buf(("w", step % 2, tuple(new_shape), dt), new_shape, dt)

@@ -204,6 +204,31 @@ int main(int argc, char** argv) {
     write_exact(argv[10], u, cnt);
     return 0;
   }
+  if (mode == "bandsep") {
+    // bandsep n nterms gen_term nsys Nb data_kind bands.bin gens.bin coef.bin b.bin out.bin
+    int n = atoi(argv[2]), nterms = atoi(argv[3]), gen = atoi(argv[4]);
+    long long nsys = atoll(argv[5]), Nb = atoll(argv[6]);
+    int dk = atoi(argv[7]);
+    double* bands = read_exact(argv[8], (size_t)nterms * 5 * n);
+    double* gens = read_exact(argv[9], 4 * (size_t)n);
+    double* coef = read_exact(argv[10], (size_t)nterms * nsys);
+    size_t cnt = (size_t)nsys * Nb * (dk ? 2 : 1);
+    double* b = read_exact(argv[11], cnt);
+    double* u = (double*)malloc(sizeof(double) * cnt);
+    for (size_t i = 0; i < cnt; ++i) u[i] = 0.0;
+    const int m = (n + 1) / 2;
+    double* fac = (double*)malloc(sizeof(double) * 7 * (size_t)m * 2 * nsys);
+    for (size_t i = 0; i < 7 * (size_t)m * 2 * nsys; ++i) fac[i] = std::numeric_limits<double>::quiet_NaN();
+    BandSepDesc d{n, nterms, gen, bands, gen >= 0 ? gens : nullptr, coef};
+    for (long long ch = 0; ch < 2 * nsys; ++ch) band_sep_factor_prog(d, fac, nsys, ch);
+    const double* g = gen >= 0 ? gens : nullptr;
+    for (long long ch = 0; ch < 2 * nsys; ++ch) {
+      if (dk) band_sep_solve_prog<cd>((const cd*)b, (cd*)u, fac, g, n, Nb, 1, nsys, ch);
+      else band_sep_solve_prog<double>(b, u, fac, g, n, Nb, 1, nsys, ch);
+    }
+    write_exact(argv[12], u, cnt);
+    return 0;
+  }
   if (mode == "hmatvec") {
     long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
     int dk = atoi(argv[5]);
