@@ -51,6 +51,8 @@ SIGNATURES = {
     "sgpu_Helmholtz_matvec": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
     "sgpu_helmholtz_factor": (_int, [_i64, _vp, _vp, _i64, _i64, _int, _vp, _vp]),
     "sgpu_helmholtz_solve_cached": (_int, [_vp, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp]),
+    "sgpu_band_sep_factor": (_int, [_int, _int, _int, _vp, _vp, _vp, _i64, _vp, _vp]),
+    "sgpu_band_sep_solve": (_int, [_vp, _vp, _vp, _vp, _int, _i64, _i64, _i64, _int, _vp]),
     "sgpu_leggauss": (_int, [_int, _vp, _vp]),
     "sgpu_legendre_plan_create": (_int, [ctypes.POINTER(_vp), _int, _int, _int]),
     "sgpu_legendre_plan_destroy": (_int, [_vp]),
