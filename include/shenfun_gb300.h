@@ -163,6 +163,26 @@ int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double*
                         int64_t outer, int64_t Nb, int64_t inner, int data_kind,
                         cudaStream_t stream);
 
+/* ---- Helmholtz problem: the whole hot-path step in one call ----------------
+ * (-lap + c) u = f on 2D R2C(N0) x D(N1) or 3D C2C(N0) x R2C(N1) x D(N2), D a
+ * ShenDirichlet space (Chebyshev GC or Legendre LG) along the last axis.  One
+ * solve = inner(v, f) -> H(f_hat, u_hat) -> u_hat.backward(), the sequence of
+ * chebyshev/la.py:288-317 with tensorproductspace.py:45-259 around it.
+ * create factorises every per-wavenumber system (device allocations happen
+ * here); solve allocates nothing and uses the caller's scratch (workspace
+ * size from sgpu_helmholtz_workspace_size, 256-byte aligned).  f and u are
+ * physical-space FP64 arrays (C-contiguous); u may not alias the scratch. */
+#define SGPU_FAMILY_CHEBYSHEV 1
+#define SGPU_FAMILY_LEGENDRE 2
+typedef struct sgpu_helmholtz_problem sgpu_helmholtz_problem;
+int sgpu_helmholtz_create(sgpu_helmholtz_problem** problem, int ndim, const int64_t* N,
+                          int family, double c, int form);
+int sgpu_helmholtz_destroy(sgpu_helmholtz_problem* problem);
+int sgpu_helmholtz_shape(const sgpu_helmholtz_problem* problem, int64_t* phys, int64_t* spec);
+int sgpu_helmholtz_workspace_size(const sgpu_helmholtz_problem* problem, size_t* bytes);
+int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* problem, const double* f, double* u,
+                         void* work, size_t work_bytes, cudaStream_t stream);
+
 /* ---- Legendre spaces (Gauss-Legendre quadrature) --------------------------
  * Replace legendre.Orthogonal / ShenDirichlet / ShenBiharmonic's transforms
  * (legendre/bases.py:76-572): the 'recursive' kind (transforms.pyx:175-325)

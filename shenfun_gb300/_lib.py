@@ -53,6 +53,11 @@ SIGNATURES = {
     "sgpu_helmholtz_solve_cached": (_int, [_vp, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp]),
     "sgpu_band_sep_factor": (_int, [_int, _int, _int, _vp, _vp, _vp, _i64, _vp, _vp]),
     "sgpu_band_sep_solve": (_int, [_vp, _vp, _vp, _vp, _int, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_helmholtz_create": (_int, [ctypes.POINTER(_vp), _int, _vp, _int, _dbl, _int]),
+    "sgpu_helmholtz_destroy": (_int, [_vp]),
+    "sgpu_helmholtz_shape": (_int, [_vp, _vp, _vp]),
+    "sgpu_helmholtz_workspace_size": (_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "sgpu_helmholtz_solve": (_int, [_vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]),
     "sgpu_leggauss": (_int, [_int, _vp, _vp]),
     "sgpu_legendre_plan_create": (_int, [ctypes.POINTER(_vp), _int, _int, _int]),
     "sgpu_legendre_plan_destroy": (_int, [_vp]),

@@ -1,0 +1,261 @@
+// Native Helmholtz problem object: one call runs the whole hot-path step
+// (scalar product of the right-hand side -> per-wavenumber banded solve ->
+// backward transform) on a Fourier x ... x Dirichlet grid with the
+// non-periodic axis last, the step a shenfun time stepper performs with
+// inner(v, f), H(f_hat, u_hat) and u_hat.backward()
+// (chebyshev/la.py:288-317, tensorproductspace.py:45-259).
+//
+// Grids: 2D  R2C(N0) x D(N1)        spectral (N0/2+1, N1)
+//        3D  C2C(N0) x R2C(N1) x D(N2)   spectral (N0, N1/2+1, N2)
+// with D a ShenDirichlet space of the Chebyshev (GC) or Legendre (LG) family.
+// The operator is (-lap + c): alfa = -1, beta = |k|^2 + c per wavenumber.
+//
+// Creation builds the transform plans and factorises every system (device
+// allocations happen there); the solve allocates nothing: its two scratch
+// arrays come from the caller (sgpu_helmholtz_workspace_size).
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "solvers.cuh"
+
+struct sgpu_plan;
+struct sgpu_legendre_plan;
+
+extern "C" {
+int sgpu_plan_create(sgpu_plan** plan, int kind, int n, int basis, int form);
+int sgpu_plan_destroy(sgpu_plan* plan);
+int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
+                      int64_t inner, int data_kind, double scale, cudaStream_t stream);
+int sgpu_legendre_plan_create(sgpu_legendre_plan** plan, int N, int basis, int form);
+int sgpu_legendre_plan_destroy(sgpu_legendre_plan* plan);
+int sgpu_legendre_execute(const sgpu_legendre_plan* plan, int direction, const void* in,
+                          void* out, int64_t outer, int64_t inner, int data_kind,
+                          cudaStream_t stream);
+int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int64_t outer,
+                          int64_t inner, int form, void* fac, cudaStream_t stream);
+int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int64_t outer,
+                                int64_t N, int64_t inner, int data_kind, int form,
+                                cudaStream_t stream);
+int sgpu_band_sep_factor(int n, int nterms, int gen_term, const double* bands,
+                         const double* gens, const double* coef, int64_t nsys, double* fac,
+                         cudaStream_t stream);
+int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double* gens, int n,
+                        int64_t outer, int64_t Nb, int64_t inner, int data_kind,
+                        cudaStream_t stream);
+}
+
+struct sgpu_helmholtz_problem {
+  int ndim, family, form;
+  int64_t N[3];
+  double c;
+  int64_t nsys, nphys, nspec;      // systems, physical and spectral element counts
+  sgpu_plan* fx_f = nullptr;       // 3D: C2C forward / backward along axis 0
+  sgpu_plan* fx_b = nullptr;
+  sgpu_plan* fr_f = nullptr;       // R2C forward / C2R backward (axis 0 in 2D, 1 in 3D)
+  sgpu_plan* fr_b = nullptr;
+  sgpu_plan* d_s = nullptr;        // Chebyshev scalar product / backward (last axis)
+  sgpu_plan* d_b = nullptr;
+  sgpu_legendre_plan* leg = nullptr;
+  double* dev = nullptr;           // alfa | beta | factor cache | bands | coef
+  double* alfa = nullptr;
+  double* beta = nullptr;
+  double* fac = nullptr;
+  double* bands = nullptr;
+  double* coef = nullptr;
+};
+
+namespace {
+
+void destroy_all(sgpu_helmholtz_problem* p) {
+  if (!p) return;
+  sgpu_plan_destroy(p->fx_f);
+  sgpu_plan_destroy(p->fx_b);
+  sgpu_plan_destroy(p->fr_f);
+  sgpu_plan_destroy(p->fr_b);
+  sgpu_plan_destroy(p->d_s);
+  sgpu_plan_destroy(p->d_b);
+  sgpu_legendre_plan_destroy(p->leg);
+  if (p->dev) cudaFree(p->dev);
+  delete p;
+}
+
+int64_t fftfreq(int64_t i, int64_t n) { return i <= (n - 1) / 2 ? i : i - n; }
+
+}  // namespace
+
+extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, const int64_t* N,
+                                     int family, double c, int form) {
+  if (!out || !N) return SGPU_ERR_ARG;
+  *out = nullptr;
+  if (ndim != 2 && ndim != 3) return SGPU_ERR_ARG;
+  if (family != SGPU_FAMILY_CHEBYSHEV && family != SGPU_FAMILY_LEGENDRE) return SGPU_ERR_ARG;
+  if (form != SGPU_PLAIN_F64 && form != SGPU_MIXED_DF) return SGPU_ERR_ARG;
+  for (int i = 0; i < ndim; ++i)
+    if (N[i] < 2 || N[i] > (1 << 16)) return SGPU_ERR_ARG;
+  if (N[ndim - 1] < 8) return SGPU_ERR_ARG;
+  sgpu_helmholtz_problem* p = new (std::nothrow) sgpu_helmholtz_problem;
+  if (!p) return SGPU_ERR_NOMEM;
+  p->ndim = ndim;
+  p->family = family;
+  p->form = form;
+  p->c = c;
+  for (int i = 0; i < 3; ++i) p->N[i] = i < ndim ? N[i] : 1;
+  const int64_t Nd = N[ndim - 1];
+  const int64_t nr = ndim == 2 ? N[0] : N[1];  // R2C axis length
+  p->nsys = ndim == 2 ? (nr / 2 + 1) : N[0] * (nr / 2 + 1);
+  p->nphys = (ndim == 2 ? N[0] : N[0] * N[1]) * Nd;
+  p->nspec = p->nsys * Nd;
+  // Fourier plans use the requested arithmetic; the Dirichlet axis too when
+  // it is Chebyshev (Legendre contractions are FP64 here)
+  int st = SGPU_OK;
+  if (ndim == 3) {
+    st |= sgpu_plan_create(&p->fx_f, SGPU_XF_C2C_FWD, (int)N[0], 0, form);
+    st |= sgpu_plan_create(&p->fx_b, SGPU_XF_C2C_BWD, (int)N[0], 0, form);
+  }
+  st |= sgpu_plan_create(&p->fr_f, SGPU_XF_R2C, (int)nr, 0, form);
+  st |= sgpu_plan_create(&p->fr_b, SGPU_XF_C2R, (int)nr, 0, form);
+  if (family == SGPU_FAMILY_CHEBYSHEV) {
+    st |= sgpu_plan_create(&p->d_s, SGPU_XF_CHEB_SCALAR, (int)Nd, SGPU_BASIS_SD, form);
+    st |= sgpu_plan_create(&p->d_b, SGPU_XF_CHEB_BACKWARD, (int)Nd, SGPU_BASIS_SD, form);
+  } else {
+    st |= sgpu_legendre_plan_create(&p->leg, (int)Nd, SGPU_BASIS_SD, SGPU_PLAIN_F64);
+  }
+  if (st != SGPU_OK) {
+    destroy_all(p);
+    return SGPU_ERR_UNSUPPORTED;
+  }
+  // per-wavenumber scales: alfa = -1, beta = |k|^2 + c
+  std::vector<double> alfa(p->nsys, -1.0), beta(p->nsys);
+  for (int64_t s = 0; s < p->nsys; ++s) {
+    double k2;
+    if (ndim == 2) {
+      k2 = (double)(s * s);
+    } else {
+      const int64_t ix = s / (nr / 2 + 1), iy = s % (nr / 2 + 1);
+      const double kx = (double)fftfreq(ix, N[0]);
+      k2 = kx * kx + (double)(iy * iy);
+    }
+    beta[s] = k2 + c;
+  }
+  const int64_t n = Nd - 2;
+  const int64_t m = (n + 1) / 2;
+  size_t nfac = family == SGPU_FAMILY_CHEBYSHEV ? (size_t)4 * n * p->nsys
+                                                : (size_t)7 * m * 2 * p->nsys;
+  size_t nb = family == SGPU_FAMILY_CHEBYSHEV ? 0 : (size_t)2 * 5 * n;
+  size_t total = 2 * (size_t)p->nsys + nfac + nb + (nb ? 2 * (size_t)p->nsys : 0);
+  if (cudaMalloc((void**)&p->dev, sizeof(double) * total) != cudaSuccess) {
+    cudaGetLastError();
+    destroy_all(p);
+    return SGPU_ERR_NOMEM;
+  }
+  p->alfa = p->dev;
+  p->beta = p->alfa + p->nsys;
+  p->fac = p->beta + p->nsys;
+  cudaMemcpy(p->alfa, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->beta, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
+  if (family == SGPU_FAMILY_CHEBYSHEV) {
+    st = sgpu_helmholtz_factor(Nd, p->alfa, p->beta, p->nsys, 1, SGPU_PLAIN_F64, p->fac, 0);
+  } else {
+    // terms: (phi''_j, phi_k) = -(4k+6) diagonal with coefficient alfa, and the
+    // mass matrix B (legendre/matrices.py:121-135) with coefficient beta
+    p->bands = p->fac + nfac;
+    p->coef = p->bands + nb;
+    std::vector<double> bands(nb, 0.0);
+    std::vector<double> h(Nd);
+    for (int64_t k = 0; k < Nd; ++k) h[k] = 2.0 / (2.0 * k + 1.0);
+    for (int64_t k = 0; k < n; ++k) {
+      bands[(0 * 5 + 2) * n + k] = -(4.0 * k + 6.0);
+      bands[(1 * 5 + 2) * n + k] = h[k] + h[k + 2];
+      if (k + 2 < n) bands[(1 * 5 + 3) * n + k] = -h[k + 2];
+      if (k >= 2) bands[(1 * 5 + 1) * n + k] = -h[k];
+    }
+    cudaMemcpy(p->bands, bands.data(), sizeof(double) * nb, cudaMemcpyHostToDevice);
+    cudaMemcpy(p->coef, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
+    cudaMemcpy(p->coef + p->nsys, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
+    st = sgpu_band_sep_factor((int)n, 2, -1, p->bands, nullptr, p->coef, p->nsys, p->fac, 0);
+  }
+  if (st != SGPU_OK || cudaDeviceSynchronize() != cudaSuccess) {
+    cudaGetLastError();
+    destroy_all(p);
+    return SGPU_ERR_CUDA;
+  }
+  *out = p;
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_helmholtz_destroy(sgpu_helmholtz_problem* p) {
+  destroy_all(p);
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_helmholtz_shape(const sgpu_helmholtz_problem* p, int64_t* phys, int64_t* spec) {
+  if (!p || !phys || !spec) return SGPU_ERR_ARG;
+  for (int i = 0; i < p->ndim; ++i) phys[i] = spec[i] = p->N[i];
+  if (p->ndim == 2)
+    spec[0] = p->N[0] / 2 + 1;
+  else
+    spec[1] = p->N[1] / 2 + 1;
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_helmholtz_workspace_size(const sgpu_helmholtz_problem* p, size_t* bytes) {
+  if (!p || !bytes) return SGPU_ERR_ARG;
+  const size_t r = ((size_t)p->nphys * 8 + 255) & ~(size_t)255;
+  *bytes = r + (size_t)p->nspec * 16;
+  return SGPU_OK;
+}
+
+// the step itself, given scratch arrays wr (real, physical size) and wc
+// (complex, spectral size)
+static int helmholtz_run(const sgpu_helmholtz_problem* p, const double* f, double* u, double* wr,
+                         double* wc, cudaStream_t s) {
+  const int64_t Nd = p->N[p->ndim - 1];
+  const int64_t nlines_d = p->nphys / Nd;  // physical lines along the last axis
+  int st = SGPU_OK;
+  // 1. scalar product along the Dirichlet axis (real data)
+  if (p->family == SGPU_FAMILY_CHEBYSHEV)
+    st |= sgpu_plan_execute(p->d_s, f, wr, nlines_d, 1, SGPU_REAL, 1.0, s);
+  else
+    st |= sgpu_legendre_execute(p->leg, 0, f, wr, nlines_d, 1, SGPU_REAL, s);
+  if (p->ndim == 2) {
+    const int64_t N0 = p->N[0];
+    st |= sgpu_plan_execute(p->fr_f, wr, wc, 1, Nd, SGPU_REAL, 1.0 / N0, s);
+  } else {
+    const int64_t N0 = p->N[0], N1 = p->N[1], Nh = N1 / 2 + 1;
+    st |= sgpu_plan_execute(p->fr_f, wr, wc, N0, Nd, SGPU_REAL, 1.0 / N1, s);
+    st |= sgpu_plan_execute(p->fx_f, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0 / N0, s);
+  }
+  // 2. one banded system per wavenumber, in place on the spectral array
+  if (p->family == SGPU_FAMILY_CHEBYSHEV)
+    st |= sgpu_helmholtz_solve_cached(wc, wc, p->fac, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s);
+  else
+    st |= sgpu_band_sep_solve(wc, wc, p->fac, nullptr, (int)(Nd - 2), p->nsys, Nd, 1, SGPU_COMPLEX, s);
+  // 3. backward
+  if (p->ndim == 2) {
+    st |= sgpu_plan_execute(p->fr_b, wc, wr, 1, Nd, SGPU_COMPLEX, 1.0, s);
+  } else {
+    const int64_t N0 = p->N[0], N1 = p->N[1], Nh = N1 / 2 + 1;
+    st |= sgpu_plan_execute(p->fx_b, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0, s);
+    st |= sgpu_plan_execute(p->fr_b, wc, wr, N0, Nd, SGPU_COMPLEX, 1.0, s);
+  }
+  if (p->family == SGPU_FAMILY_CHEBYSHEV)
+    st |= sgpu_plan_execute(p->d_b, wr, u, nlines_d, 1, SGPU_REAL, 1.0, s);
+  else
+    st |= sgpu_legendre_execute(p->leg, 2, wr, u, nlines_d, 1, SGPU_REAL, s);
+  return st == SGPU_OK ? SGPU_OK : SGPU_ERR_CUDA;
+}
+
+extern "C" int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* p, const double* f, double* u,
+                                    void* work, size_t work_bytes, cudaStream_t stream) {
+  if (!p || !f || !u || !work) return SGPU_ERR_ARG;
+  size_t need = 0;
+  sgpu_helmholtz_workspace_size(p, &need);
+  if (work_bytes < need) return SGPU_ERR_ARG;
+  if (((uintptr_t)work & 255) != 0) return SGPU_ERR_ARG;
+  const size_t r = ((size_t)p->nphys * 8 + 255) & ~(size_t)255;
+  double* wr = (double*)work;
+  double* wc = (double*)((unsigned char*)work + r);
+  return helmholtz_run(p, f, u, wr, wc, stream);
+}

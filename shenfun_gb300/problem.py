@@ -1,0 +1,74 @@
+"""Helmholtz problems as native objects: one call = the whole hot-path step.
+
+``HelmholtzProblem((Nx, Ny, Nz), 'chebyshev', c)`` owns the transform plans
+and the factorised per-wavenumber systems of (-lap + c) u = f on a
+Fourier x ... x ShenDirichlet grid (Dirichlet axis last); ``solve(f)`` runs
+scalar product -> banded solves -> backward in one C-ABI call
+(``sgpu_helmholtz_solve``) on the caller's stream, with a reusable scratch
+buffer.  This is the unit the serving engine caches and schedules.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from .device import require_cuda, ptr, stream_handle
+
+FAMILIES = {"chebyshev": 1, "legendre": 2}
+
+
+class HelmholtzProblem:
+    def __init__(self, N, family="chebyshev", c=0.0, form="plain"):
+        require_cuda()
+        self.N = tuple(int(n) for n in N)
+        self.family = family
+        self.c = float(c)
+        self.form = _lib.FORMS[form]
+        h = ctypes.c_void_p()
+        arr = (ctypes.c_int64 * len(self.N))(*self.N)
+        _lib.call("sgpu_helmholtz_create", ctypes.byref(h), len(self.N), ctypes.cast(arr, ctypes.c_void_p),
+                  FAMILIES[family], self.c, self.form)
+        self._h = h
+        phys = (ctypes.c_int64 * 3)()
+        spec = (ctypes.c_int64 * 3)()
+        _lib.call("sgpu_helmholtz_shape", self._h, ctypes.cast(phys, ctypes.c_void_p),
+                  ctypes.cast(spec, ctypes.c_void_p))
+        self.phys_shape = tuple(phys[i] for i in range(len(self.N)))
+        self.spec_shape = tuple(spec[i] for i in range(len(self.N)))
+        nb = ctypes.c_size_t()
+        _lib.call("sgpu_helmholtz_workspace_size", self._h, ctypes.byref(nb))
+        self.workspace_bytes = int(nb.value)
+        self._work = None
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().sgpu_helmholtz_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    @property
+    def array_bytes(self):
+        n = 1
+        for v in self.phys_shape:
+            n *= v
+        return 8 * n
+
+    def new_workspace(self, device=None):
+        # 256-byte aligned: torch's caching allocator returns 512-byte aligned blocks
+        return torch.empty(self.workspace_bytes, dtype=torch.uint8, device=device or "cuda")
+
+    def solve(self, f, u=None, work=None, stream=None):
+        """u = solution of (-lap + c) u = f on the quadrature grid (FP64)."""
+        if u is None:
+            u = torch.empty_like(f)
+        if work is None:
+            if self._work is None:
+                self._work = self.new_workspace(f.device)
+            work = self._work
+        if tuple(f.shape) != self.phys_shape or tuple(u.shape) != self.phys_shape:
+            raise _lib.SgpuError(_lib.ERR_ARG, f"arrays must have shape {self.phys_shape}")
+        _lib.call("sgpu_helmholtz_solve", self._h, ptr(f), ptr(u), work.data_ptr(),
+                  work.numel(), stream_handle(stream))
+        return u

@@ -1,0 +1,294 @@
+"""Continuous-batching request loop for Helmholtz solves on one GPU.
+
+Requests (2D or 3D grids, Chebyshev or Legendre Dirichlet axis, shift c)
+arrive over time.  The ``Scheduler`` admits them as slots and device memory
+free up (memory-based admission, no head-of-line blocking behind a request
+that does not fit yet), the ``GpuExecutor`` runs each admitted request on one
+of several CUDA streams so that work from different requests overlaps on the
+device, and completions are detected with CUDA events and retired while new
+requests keep arriving.  Factorised problems are cached on the device, keyed
+by (grid, family, c, form), with least-recently-used eviction under a byte
+budget.  Results do not depend on what else is in flight: every request runs
+its own deterministic kernels on its own buffers (no atomics, no shared
+scratch), which tests/test_gpu_serving.py checks bit for bit.
+
+Failure handling is host-side: a request larger than the whole memory budget
+is rejected with an error, a cancelled request is dropped before launch (or
+its result discarded after), and a request that raises during launch is
+marked failed without stopping the loop.
+"""
+import collections
+import time
+
+import numpy as np
+
+QUEUED, RUNNING, DONE, FAILED, CANCELLED, REJECTED = "queued", "running", "done", "failed", \
+    "cancelled", "rejected"
+
+
+class Request:
+    __slots__ = ("id", "N", "family", "c", "f", "arrival", "state", "result", "t_admit", "t_done",
+                 "error", "nbytes", "slot")
+
+    def __init__(self, rid, N, family, c, f, arrival=0.0):
+        self.id = rid
+        self.N = tuple(int(n) for n in N)
+        self.family = family
+        self.c = float(c)
+        self.f = f
+        self.arrival = float(arrival)
+        self.state = QUEUED
+        self.result = None
+        self.t_admit = None
+        self.t_done = None
+        self.error = None
+        self.nbytes = 0
+        self.slot = None
+
+    @property
+    def key(self):
+        return (self.N, self.family, self.c)
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+def array_bytes(N):
+    n = 1
+    for v in N:
+        n *= int(v)
+    return 8 * n
+
+
+def request_bytes(N):
+    """Device bytes one in-flight request holds: RHS + solution + scratch
+    (real physical array + complex spectral array)."""
+    spec = list(N)
+    spec[-2 if len(N) == 3 else 0] = spec[-2 if len(N) == 3 else 0] // 2 + 1
+    nspec = 1
+    for v in spec:
+        nspec *= v
+    return 3 * array_bytes(N) + 16 * nspec + 512
+
+
+def factor_bytes(N, family):
+    """Device bytes of a cached problem (factor arrays and plan tables)."""
+    nd = N[-1]
+    spec = list(N)
+    spec[-2 if len(N) == 3 else 0] = spec[-2 if len(N) == 3 else 0] // 2 + 1
+    nsys = 1
+    for v in spec[:-1]:
+        nsys *= v
+    if family == "chebyshev":
+        return 8 * (4 * (nd - 2) + 2) * nsys + 64 * sum(N)
+    return 8 * (7 * nd + 4) * nsys + 16 * nd * nd + 64 * sum(N)
+
+
+class Scheduler:
+    """Admission and retirement; independent of the device (tests drive it
+    with a fake executor on the CPU)."""
+
+    def __init__(self, executor, max_slots=8, mem_budget=8 << 30, lookahead=16):
+        self.ex = executor
+        self.max_slots = max_slots
+        self.mem_budget = int(mem_budget)
+        self.lookahead = lookahead
+        self.queue = collections.deque()
+        self.running = {}
+        self.finished = []
+        self.mem_used = 0
+        self.free_slots = list(range(max_slots))
+
+    def submit(self, req):
+        need = request_bytes(req.N) + self.ex.factor_cost(req)
+        req.nbytes = request_bytes(req.N)
+        if need > self.mem_budget:
+            req.state = REJECTED
+            req.error = f"needs {need} bytes, budget {self.mem_budget}"
+            self.finished.append(req)
+            return False
+        self.queue.append(req)
+        return True
+
+    def cancel(self, rid):
+        for r in list(self.queue):
+            if r.id == rid:
+                self.queue.remove(r)
+                r.state = CANCELLED
+                self.finished.append(r)
+                return True
+        r = self.running.get(rid)
+        if r is not None:
+            r.state = CANCELLED   # result discarded at retirement
+            return True
+        return False
+
+    def _retire(self, now):
+        for rid in self.ex.poll():
+            r = self.running.pop(rid, None)
+            if r is None:
+                continue
+            self.mem_used -= r.nbytes
+            self.free_slots.append(r.slot)
+            if r.state == CANCELLED:
+                r.result = None
+            elif r.state != FAILED:
+                r.state = DONE
+            r.t_done = now()
+            self.finished.append(r)
+
+    def _admit(self, now):
+        scanned = 0
+        i = 0
+        while self.free_slots and i < len(self.queue) and scanned < self.lookahead:
+            r = self.queue[i]
+            scanned += 1
+            need = r.nbytes + self.ex.factor_cost(r)
+            if self.mem_used + self.ex.cache_bytes() + need > self.mem_budget:
+                # evict cached factorisations (least recently used) to make room
+                self.ex.shrink_cache(self.mem_budget - self.mem_used - need)
+                if self.mem_used + self.ex.cache_bytes() + need > self.mem_budget:
+                    i += 1   # does not fit yet: look further down the queue
+                    continue
+            del self.queue[i]
+            r.slot = self.free_slots.pop()
+            r.t_admit = now()
+            r.state = RUNNING
+            self.mem_used += r.nbytes
+            self.running[r.id] = r
+            try:
+                self.ex.launch(r)
+            except Exception as e:  # launch failure: report, keep serving
+                r.state = FAILED
+                r.error = repr(e)
+                self.running.pop(r.id, None)
+                self.mem_used -= r.nbytes
+                self.free_slots.append(r.slot)
+                r.t_done = now()
+                self.finished.append(r)
+
+    def step(self, now=time.perf_counter):
+        self._retire(now)
+        self._admit(now)
+
+    def idle(self):
+        return not self.queue and not self.running
+
+
+class GpuExecutor:
+    """Runs requests on a pool of CUDA streams with a device-resident,
+    byte-budgeted LRU cache of factorised problems."""
+
+    def __init__(self, nstreams=4, cache_budget=4 << 30, form="plain", keep_results=True):
+        import torch
+        from .problem import HelmholtzProblem
+        self.torch = torch
+        self.Problem = HelmholtzProblem
+        self.streams = [torch.cuda.Stream() for _ in range(nstreams)]
+        self.cache = collections.OrderedDict()
+        self.cache_budget = int(cache_budget)
+        self.form = form
+        self.inflight = {}
+        self.keep_results = keep_results
+        self.hits = 0
+        self.misses = 0
+
+    # -- factorisation cache ---------------------------------------------
+    def cache_bytes(self):
+        return sum(b for _, b in self.cache.values())
+
+    def factor_cost(self, req):
+        return 0 if req.key in self.cache else factor_bytes(req.N, req.family)
+
+    def shrink_cache(self, room):
+        while self.cache and self.cache_bytes() > max(0, min(room, self.cache_budget)):
+            key, _ = next(iter(self.cache.items()))
+            if any(r.key == key for r, _, _ in self.inflight.values()):
+                break  # still in use
+            self.cache.popitem(last=False)
+
+    def problem(self, req):
+        ent = self.cache.get(req.key)
+        if ent is not None:
+            self.cache.move_to_end(req.key)
+            self.hits += 1
+            return ent[0]
+        self.misses += 1
+        p = self.Problem(req.N, req.family, req.c, self.form)
+        self.cache[req.key] = (p, factor_bytes(req.N, req.family))
+        self.shrink_cache(self.cache_budget)
+        return p
+
+    # -- execution ----------------------------------------------------------
+    def launch(self, req):
+        torch = self.torch
+        p = self.problem(req)
+        s = self.streams[req.slot % len(self.streams)]
+        with torch.cuda.stream(s):
+            f_host = req.f if isinstance(req.f, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(req.f))
+            d_f = torch.empty(p.phys_shape, dtype=torch.float64, device="cuda")
+            d_f.copy_(f_host, non_blocking=True)
+            d_u = torch.empty_like(d_f)
+            work = p.new_workspace()
+            p.solve(d_f, d_u, work, stream=s)
+            out = torch.empty(p.phys_shape, dtype=torch.float64, pin_memory=True) if self.keep_results else None
+            if out is not None:
+                out.copy_(d_u, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(s)
+        # keep buffers alive until the event completes
+        self.inflight[req.id] = (req, ev, (d_f, d_u, work, out, f_host))
+        req.result = out
+
+    def poll(self):
+        done = []
+        for rid, (req, ev, bufs) in list(self.inflight.items()):
+            if ev.query():
+                done.append(rid)
+                del self.inflight[rid]
+        return done
+
+
+def make_stream(n, seed=0, rate=None, nmin=32, nmax=512, max_points=2 ** 24, families=("chebyshev", "legendre")):
+    """Synthetic request stream: dim in {2, 3} (50/50), N per axis log-uniform
+    in [nmin, nmax], family uniform, shift c log-uniform in [0.1, 1e4],
+    Poisson arrivals at `rate` requests/s (all at t = 0 when rate is None).
+    Grids with more than `max_points` points are redrawn (device memory)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    while len(out) < n:
+        dim = 2 if rng.random() < 0.5 else 3
+        N = tuple(int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))) for _ in range(dim))
+        N = N[:-1] + (max(N[-1], 8),)
+        if np.prod(N) > max_points:
+            continue
+        fam = families[int(rng.integers(len(families)))]
+        c = float(np.exp(rng.uniform(np.log(0.1), np.log(1e4))))
+        if rate:
+            t += rng.exponential(1.0 / rate)
+        out.append((N, fam, c, t, int(rng.integers(1 << 31))))
+    return out
+
+
+def run_stream(stream, executor, max_slots=8, mem_budget=8 << 30, poll_sleep=0.0):
+    """Drive a stream through the scheduler in wall-clock time; returns the
+    finished requests and the elapsed seconds."""
+    sched = Scheduler(executor, max_slots=max_slots, mem_budget=mem_budget)
+    reqs = []
+    for i, (N, fam, c, t, seed) in enumerate(stream):
+        f = np.random.default_rng(seed).standard_normal(N)
+        reqs.append(Request(i, N, fam, c, f, t))
+    t0 = time.perf_counter()
+    now = lambda: time.perf_counter() - t0  # noqa: E731
+    nxt = 0
+    while nxt < len(reqs) or not sched.idle():
+        tn = now()
+        while nxt < len(reqs) and reqs[nxt].arrival <= tn:
+            sched.submit(reqs[nxt])
+            nxt += 1
+        sched.step(now)
+        if poll_sleep:
+            time.sleep(poll_sleep)
+    return sched.finished, now()
