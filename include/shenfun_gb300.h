@@ -41,6 +41,7 @@ extern "C" {
 #define SGPU_ERR_NONFINITE 5    /* non-finite value detected in input    */
 #define SGPU_ERR_ZERO_PIVOT 6   /* zero pivot in a factorisation         */
 #define SGPU_ERR_TIMEOUT 7      /* a bounded device wait ran out         */
+#define SGPU_ERR_SCRATCH_LIMIT 8 /* problem too large for the built-in scratch */
 
 /* data kinds */
 #define SGPU_REAL 0     /* float64                     */
@@ -182,6 +183,17 @@ int sgpu_helmholtz_shape(const sgpu_helmholtz_problem* problem, int64_t* phys, i
 int sgpu_helmholtz_workspace_size(const sgpu_helmholtz_problem* problem, size_t* bytes);
 int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* problem, const double* f, double* u,
                          void* work, size_t work_bytes, cudaStream_t stream);
+/* Same step without any scratch argument, for callers that cannot provide or
+ * allocate device memory (a host program whose device memory belongs to
+ * another allocator, an FFI caller that only has its input and output arrays,
+ * a loop that must not allocate).  No counterpart in the reference.  It uses a
+ * 64 MiB scratch array built into the library (held on every GPU that loads
+ * the library until exit); larger problems return SGPU_ERR_SCRATCH_LIMIT.  The
+ * first call on a device looks up the array's address (make it before any
+ * stream capture); all calls share the array, so calls that overlap on the
+ * GPU race and must be serialised.  Allocates nothing. */
+int sgpu_helmholtz_solve_noalloc(const sgpu_helmholtz_problem* problem, const double* f,
+                                 double* u, cudaStream_t stream);
 
 /* ---- Legendre spaces (Gauss-Legendre quadrature) --------------------------
  * Replace legendre.Orthogonal / ShenDirichlet / ShenBiharmonic's transforms

@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libshenfun_gb300.so")
 
 # status codes (include/shenfun_gb300.h)
-OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_NONFINITE, ERR_ZERO_PIVOT, ERR_TIMEOUT = range(8)
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_NONFINITE, ERR_ZERO_PIVOT, ERR_TIMEOUT, \
+    ERR_SCRATCH_LIMIT = range(9)
 REAL, COMPLEX = 0, 1
 BASIS_ORTHO, BASIS_SD, BASIS_SB = 0, 1, 2
 XF_R2C, XF_C2R, XF_C2C_FWD, XF_C2C_BWD, XF_DCT2, XF_DCT3, XF_CHEB_SCALAR, XF_CHEB_FORWARD, \
@@ -58,6 +59,7 @@ SIGNATURES = {
     "sgpu_helmholtz_shape": (_int, [_vp, _vp, _vp]),
     "sgpu_helmholtz_workspace_size": (_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "sgpu_helmholtz_solve": (_int, [_vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]),
+    "sgpu_helmholtz_solve_noalloc": (_int, [_vp, _vp, _vp, _vp]),
     "sgpu_leggauss": (_int, [_int, _vp, _vp]),
     "sgpu_legendre_plan_create": (_int, [ctypes.POINTER(_vp), _int, _int, _int]),
     "sgpu_legendre_plan_destroy": (_int, [_vp]),

@@ -11,6 +11,8 @@ extern "C" const char* sgpu_status_string(int status) {
     case SGPU_ERR_NONFINITE: return "non-finite input";
     case SGPU_ERR_ZERO_PIVOT: return "zero pivot";
     case SGPU_ERR_TIMEOUT: return "bounded device wait ran out";
+    case SGPU_ERR_SCRATCH_LIMIT:
+      return "problem needs more scratch than the allocation-free entry point's 64 MiB";
     default: return "unknown status";
   }
 }

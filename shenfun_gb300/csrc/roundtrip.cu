@@ -259,3 +259,72 @@ extern "C" int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* p, const doubl
   double* wc = (double*)((unsigned char*)work + r);
   return helmholtz_run(p, f, u, wr, wc, stream);
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of sgpu_helmholtz_solve.
+//
+// Some callers cannot hand the library a scratch buffer: a host program whose
+// device memory is owned by another allocator that must not see raw
+// cudaMalloc calls (or has no budget left for them), a Fortran or C code
+// reaching the library through a thin FFI that has no notion of device
+// buffers beyond its own input and output arrays, or a latency-critical loop
+// that must not risk an allocation during a step.  For them the step can use
+// a scratch array compiled into the library instead.
+//
+// The array below is a fixed 64 MiB of device memory.  Every GPU that loads
+// the library holds it until the process exits, whether or not this entry
+// point is used.  Problems whose scratch (one real physical array plus one
+// complex spectral array, sgpu_helmholtz_workspace_size) exceeds 64 MiB are
+// rejected with SGPU_ERR_SCRATCH_LIMIT; e.g. 128 x 128 x 129 (34 MB) fits,
+// 256 x 256 x 65 (68 MB) does not.
+//
+// The first call on each device looks up the array's device address with
+// cudaGetSymbolAddress (with that device current) and remembers it; make that
+// first call before any stream capture.  All calls share the one array and it
+// keeps whatever the last call left in it; every call writes each scratch
+// element it reads before reading it, so nothing has to be cleared between
+// calls.  Calls whose execution overlaps on the GPU (different streams, or
+// different host threads without ordering) race on the array and give wrong
+// results: serialise them.  Host code never passes the array's name to a
+// kernel (in host code it is a host-side stand-in, not a device address):
+// only the address obtained from cudaGetSymbolAddress is used.
+#include <mutex>
+
+#define SGPU_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+#define SGPU_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) unsigned char g_sgpu_noalloc_scratch[SGPU_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_addr[SGPU_NOALLOC_MAX_DEVICES] = {};
+
+extern "C" int sgpu_helmholtz_solve_noalloc(const sgpu_helmholtz_problem* p, const double* f,
+                                            double* u, cudaStream_t stream) {
+  if (!p || !f || !u) return SGPU_ERR_ARG;
+  size_t need = 0;
+  sgpu_helmholtz_workspace_size(p, &need);
+  if (need > SGPU_NOALLOC_SCRATCH_BYTES) return SGPU_ERR_SCRATCH_LIMIT;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= SGPU_NOALLOC_MAX_DEVICES) return SGPU_ERR_UNSUPPORTED;
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+      void* addr = nullptr;
+      if (cudaGetSymbolAddress(&addr, g_sgpu_noalloc_scratch) != cudaSuccess || !addr) {
+        cudaGetLastError();
+        return SGPU_ERR_CUDA;
+      }
+      g_noalloc_addr[dev] = addr;
+    }
+    base = g_noalloc_addr[dev];
+  }
+  const size_t r = ((size_t)p->nphys * 8 + 255) & ~(size_t)255;
+  double* wr = (double*)base;
+  double* wc = (double*)((unsigned char*)base + r);
+  return helmholtz_run(p, f, u, wr, wc, stream);
+}
