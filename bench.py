@@ -228,6 +228,89 @@ def stage_times(torch, run, flush, st, reps=5):
     return out
 
 
+def serving_leg(torch, rates=(300.0, None), nreq=200, seed=5):
+    """Serving stream: mixed 2D/3D Fourier x Chebyshev/Legendre Dirichlet
+    Helmholtz requests, N per axis log-uniform in [32, 512] (grids above 2^24
+    points redrawn), c log-uniform in [0.1, 1e4], Poisson arrivals at each
+    rate (None = all at once: saturation).  Latency = completion - arrival."""
+    from shenfun_gb300 import serving as SV
+    out = []
+    for rate in rates:
+        stream = SV.make_stream(nreq, seed=seed, rate=rate)
+        ex = SV.GpuExecutor(nstreams=4, cache_budget=8 << 30, keep_results=False)
+        fin, elapsed = SV.run_stream(stream, ex, max_slots=8, mem_budget=24 << 30)
+        torch.cuda.synchronize()
+        lat = np.array([r.latency for r in fin if r.state == SV.DONE])
+        out.append({"rate_req_per_s": rate, "requests": nreq, "completed": int(len(lat)),
+                    "solves_per_s": len(lat) / elapsed, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                    "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                    "cache_hits": ex.hits, "cache_misses": ex.misses})
+    return out
+
+
+def legendre_leg(torch, N=512, lines=16384, reps=3):
+    """Legendre ShenDirichlet transforms (dense contraction), plain FP64:
+    scalar product and backward of `lines` lines of length N."""
+    from shenfun_gb300.legendre import LegendreShenDirichlet
+    V = LegendreShenDirichlet(N)
+    x = torch.randn(lines, N, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    st = torch.cuda.current_stream()
+    res = {}
+    for name, fn in (("scalar_product", lambda: V.scalar_product(x, y, axis=1)),
+                     ("backward", lambda: V.backward(x, y, axis=1))):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(reps):
+            fn()
+        b.record(st)
+        b.synchronize()
+        ms = a.elapsed_time(b) / reps
+        res[name] = {"ms": ms, "tflops": 2.0 * N * N * lines / (ms * 1e-3) / 1e12}
+    return {"N": N, "lines": lines, "form": "plain FP64", **res}
+
+
+CASES = {
+    # one transform of the channel grid, for profiler captures:  name -> (kind, form)
+    "r2c-plain": ("r2c", "plain"), "r2c-mixed": ("r2c", "mixed"),
+    "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
+    "solve-plain": ("solve", "plain"),
+}
+
+
+def run_case(name, reps=3):
+    """Run one kernel of the workload `reps` times (for ncu); prints 'ok'."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from shenfun_gb300 import _lib
+    from shenfun_gb300.spaces import R2C, ChebyshevShenDirichlet
+    kind, form = CASES[name]
+    x = torch.randn(NX, NY, NZ, dtype=torch.float64, device="cuda")
+    if kind == "r2c":
+        V = R2C(NY)
+        V.form = _lib.FORMS[form]
+        y = torch.empty(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
+        fn = lambda: V.forward(x, y, axis=1)  # noqa: E731
+    elif kind == "cheb":
+        V = ChebyshevShenDirichlet(NZ)
+        V.form = _lib.FORMS[form]
+        y = torch.empty_like(x)
+        fn = lambda: V.scalar_product(x, y, axis=2)  # noqa: E731
+    else:
+        import shenfun_gb300 as sg
+        run = FormRun(sg, form, x.cpu().numpy())
+        b = torch.randn(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
+        fn = lambda: run.H(b, run.u_hat)  # noqa: E731
+    for _ in range(reps):
+        fn()
+    torch.cuda.synchronize()
+    print("ok", name)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,7 +318,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the serving and Legendre legs")
+    ap.add_argument("--case", choices=sorted(CASES), help="run one kernel case (for profilers)")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case)
     if args.impl == "reference":
         return run_reference(args)
     args.warmup = max(args.warmup, 3)
@@ -329,6 +416,11 @@ def main():
     b.synchronize()
     e2e_val = ws * e2e_steps / (a.elapsed_time(b) / 1e3)
 
+    serving = legendre = None
+    if rank == 0 and not args.no_extra:
+        serving = serving_leg(torch)
+        legendre = legendre_leg(torch)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rt, ts = cpu_leg(2, 1, 1)
@@ -360,6 +452,8 @@ def main():
                     "h2d_bytes_per_step": R_BYTES, "d2h_bytes_per_step": R_BYTES},
             "gpu_launches": FormRun.launches_per_step * args.steps * len(runs),
             "clocks": clk.summary(),
+            "serving": serving,
+            "legendre": legendre,
         }
         print(json.dumps(out))
     if dist is not None:
