@@ -178,6 +178,15 @@ int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double*
 typedef struct sgpu_helmholtz_problem sgpu_helmholtz_problem;
 int sgpu_helmholtz_create(sgpu_helmholtz_problem** problem, int ndim, const int64_t* N,
                           int family, double c, int form);
+/* Stream-ordered creation for serving: the per-axis plans come from a
+ * process-wide cache (shared by problems with the same axis lengths), device
+ * memory comes from cudaMallocAsync on `stream` and the factorisation is left
+ * queued on `stream` (no device synchronisation).  Destroying such a problem
+ * frees its memory with cudaFreeAsync on the same stream. */
+int sgpu_helmholtz_create_on(sgpu_helmholtz_problem** problem, int ndim, const int64_t* N,
+                             int family, double c, int form, cudaStream_t stream);
+/* destroy every cached plan (no problem created by _create_on may be in use) */
+int sgpu_plan_cache_clear(void);
 int sgpu_helmholtz_destroy(sgpu_helmholtz_problem* problem);
 int sgpu_helmholtz_shape(const sgpu_helmholtz_problem* problem, int64_t* phys, int64_t* spec);
 int sgpu_helmholtz_workspace_size(const sgpu_helmholtz_problem* problem, size_t* bytes);

@@ -55,6 +55,8 @@ SIGNATURES = {
     "sgpu_band_sep_factor": (_int, [_int, _int, _int, _vp, _vp, _vp, _i64, _vp, _vp]),
     "sgpu_band_sep_solve": (_int, [_vp, _vp, _vp, _vp, _int, _i64, _i64, _i64, _int, _vp]),
     "sgpu_helmholtz_create": (_int, [ctypes.POINTER(_vp), _int, _vp, _int, _dbl, _int]),
+    "sgpu_helmholtz_create_on": (_int, [ctypes.POINTER(_vp), _int, _vp, _int, _dbl, _int, _vp]),
+    "sgpu_plan_cache_clear": (_int, []),
     "sgpu_helmholtz_destroy": (_int, [_vp]),
     "sgpu_helmholtz_shape": (_int, [_vp, _vp, _vp]),
     "sgpu_helmholtz_workspace_size": (_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),

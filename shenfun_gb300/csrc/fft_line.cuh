@@ -21,7 +21,7 @@
 namespace sgpu {
 
 #define SGPU_MAX_STAGES 24
-#define SGPU_MAX_GENERIC_RADIX 127
+#define SGPU_MAX_GENERIC_RADIX 4096
 
 struct LinePlan {
   int kind;          // SGPU_XF_*

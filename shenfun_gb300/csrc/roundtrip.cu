@@ -15,7 +15,10 @@
 // arrays come from the caller (sgpu_helmholtz_workspace_size).
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "solvers.cuh"
@@ -64,29 +67,96 @@ struct sgpu_helmholtz_problem {
   double* fac = nullptr;
   double* bands = nullptr;
   double* coef = nullptr;
+  bool shared_plans = false;       // plans come from the process-wide cache
+  bool stream_ordered = false;     // device memory from cudaMallocAsync
+  cudaStream_t stream = 0;         // creation stream (stream-ordered problems)
 };
 
 namespace {
 
+// Process-wide per-axis plan cache for stream-ordered problems: plans depend
+// only on (kind, n, basis, form), so requests that share an axis length share
+// them.  Plans stay until sgpu_plan_cache_clear or process exit.
+std::mutex g_plan_mutex;
+std::map<std::tuple<int, int, int, int>, sgpu_plan*> g_plans;
+std::map<std::tuple<int, int, int>, sgpu_legendre_plan*> g_leg_plans;
+
+int cached_plan(sgpu_plan** out, int kind, int n, int basis, int form) {
+  std::lock_guard<std::mutex> lock(g_plan_mutex);
+  auto key = std::make_tuple(kind, n, basis, form);
+  auto it = g_plans.find(key);
+  if (it != g_plans.end()) {
+    *out = it->second;
+    return SGPU_OK;
+  }
+  int st = sgpu_plan_create(out, kind, n, basis, form);
+  if (st == SGPU_OK) g_plans[key] = *out;
+  return st;
+}
+
+int cached_leg_plan(sgpu_legendre_plan** out, int n, int basis, int form) {
+  std::lock_guard<std::mutex> lock(g_plan_mutex);
+  auto key = std::make_tuple(n, basis, form);
+  auto it = g_leg_plans.find(key);
+  if (it != g_leg_plans.end()) {
+    *out = it->second;
+    return SGPU_OK;
+  }
+  int st = sgpu_legendre_plan_create(out, n, basis, form);
+  if (st == SGPU_OK) g_leg_plans[key] = *out;
+  return st;
+}
+
 void destroy_all(sgpu_helmholtz_problem* p) {
   if (!p) return;
-  sgpu_plan_destroy(p->fx_f);
-  sgpu_plan_destroy(p->fx_b);
-  sgpu_plan_destroy(p->fr_f);
-  sgpu_plan_destroy(p->fr_b);
-  sgpu_plan_destroy(p->d_s);
-  sgpu_plan_destroy(p->d_b);
-  sgpu_legendre_plan_destroy(p->leg);
-  if (p->dev) cudaFree(p->dev);
+  if (!p->shared_plans) {
+    sgpu_plan_destroy(p->fx_f);
+    sgpu_plan_destroy(p->fx_b);
+    sgpu_plan_destroy(p->fr_f);
+    sgpu_plan_destroy(p->fr_b);
+    sgpu_plan_destroy(p->d_s);
+    sgpu_plan_destroy(p->d_b);
+    sgpu_legendre_plan_destroy(p->leg);
+  }
+  if (p->dev) {
+    if (p->stream_ordered)
+      cudaFreeAsync(p->dev, p->stream);
+    else
+      cudaFree(p->dev);
+  }
   delete p;
 }
 
 int64_t fftfreq(int64_t i, int64_t n) { return i <= (n - 1) / 2 ? i : i - n; }
 
+int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int family, double c,
+                int form, bool ordered, cudaStream_t stream);
+
 }  // namespace
 
 extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, const int64_t* N,
                                      int family, double c, int form) {
+  return create_impl(out, ndim, N, family, c, form, false, 0);
+}
+
+extern "C" int sgpu_helmholtz_create_on(sgpu_helmholtz_problem** out, int ndim,
+                                        const int64_t* N, int family, double c, int form,
+                                        cudaStream_t stream) {
+  return create_impl(out, ndim, N, family, c, form, true, stream);
+}
+
+extern "C" int sgpu_plan_cache_clear(void) {
+  std::lock_guard<std::mutex> lock(g_plan_mutex);
+  for (auto& kv : g_plans) sgpu_plan_destroy(kv.second);
+  for (auto& kv : g_leg_plans) sgpu_legendre_plan_destroy(kv.second);
+  g_plans.clear();
+  g_leg_plans.clear();
+  return SGPU_OK;
+}
+
+namespace {
+int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int family, double c,
+                int form, bool ordered, cudaStream_t stream) {
   if (!out || !N) return SGPU_ERR_ARG;
   *out = nullptr;
   if (ndim != 2 && ndim != 3) return SGPU_ERR_ARG;
@@ -101,6 +171,9 @@ extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, con
   p->family = family;
   p->form = form;
   p->c = c;
+  p->shared_plans = ordered;
+  p->stream_ordered = ordered;
+  p->stream = stream;
   for (int i = 0; i < 3; ++i) p->N[i] = i < ndim ? N[i] : 1;
   const int64_t Nd = N[ndim - 1];
   const int64_t nr = ndim == 2 ? N[0] : N[1];  // R2C axis length
@@ -111,16 +184,16 @@ extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, con
   // it is Chebyshev (Legendre contractions are FP64 here)
   int st = SGPU_OK;
   if (ndim == 3) {
-    st |= sgpu_plan_create(&p->fx_f, SGPU_XF_C2C_FWD, (int)N[0], 0, form);
-    st |= sgpu_plan_create(&p->fx_b, SGPU_XF_C2C_BWD, (int)N[0], 0, form);
+    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fx_f, SGPU_XF_C2C_FWD, (int)N[0], 0, form);
+    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fx_b, SGPU_XF_C2C_BWD, (int)N[0], 0, form);
   }
-  st |= sgpu_plan_create(&p->fr_f, SGPU_XF_R2C, (int)nr, 0, form);
-  st |= sgpu_plan_create(&p->fr_b, SGPU_XF_C2R, (int)nr, 0, form);
+  st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fr_f, SGPU_XF_R2C, (int)nr, 0, form);
+  st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fr_b, SGPU_XF_C2R, (int)nr, 0, form);
   if (family == SGPU_FAMILY_CHEBYSHEV) {
-    st |= sgpu_plan_create(&p->d_s, SGPU_XF_CHEB_SCALAR, (int)Nd, SGPU_BASIS_SD, form);
-    st |= sgpu_plan_create(&p->d_b, SGPU_XF_CHEB_BACKWARD, (int)Nd, SGPU_BASIS_SD, form);
+    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->d_s, SGPU_XF_CHEB_SCALAR, (int)Nd, SGPU_BASIS_SD, form);
+    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->d_b, SGPU_XF_CHEB_BACKWARD, (int)Nd, SGPU_BASIS_SD, form);
   } else {
-    st |= sgpu_legendre_plan_create(&p->leg, (int)Nd, SGPU_BASIS_SD, SGPU_PLAIN_F64);
+    st |= (ordered ? cached_leg_plan : sgpu_legendre_plan_create)(&p->leg, (int)Nd, SGPU_BASIS_SD, SGPU_PLAIN_F64);
   }
   if (st != SGPU_OK) {
     destroy_all(p);
@@ -145,7 +218,9 @@ extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, con
                                                 : (size_t)7 * m * 2 * p->nsys;
   size_t nb = family == SGPU_FAMILY_CHEBYSHEV ? 0 : (size_t)2 * 5 * n;
   size_t total = 2 * (size_t)p->nsys + nfac + nb + (nb ? 2 * (size_t)p->nsys : 0);
-  if (cudaMalloc((void**)&p->dev, sizeof(double) * total) != cudaSuccess) {
+  cudaError_t me = ordered ? cudaMallocAsync((void**)&p->dev, sizeof(double) * total, stream)
+                           : cudaMalloc((void**)&p->dev, sizeof(double) * total);
+  if (me != cudaSuccess) {
     cudaGetLastError();
     destroy_all(p);
     return SGPU_ERR_NOMEM;
@@ -153,10 +228,10 @@ extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, con
   p->alfa = p->dev;
   p->beta = p->alfa + p->nsys;
   p->fac = p->beta + p->nsys;
-  cudaMemcpy(p->alfa, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
-  cudaMemcpy(p->beta, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(p->alfa, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
+  cudaMemcpyAsync(p->beta, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
   if (family == SGPU_FAMILY_CHEBYSHEV) {
-    st = sgpu_helmholtz_factor(Nd, p->alfa, p->beta, p->nsys, 1, SGPU_PLAIN_F64, p->fac, 0);
+    st = sgpu_helmholtz_factor(Nd, p->alfa, p->beta, p->nsys, 1, SGPU_PLAIN_F64, p->fac, stream);
   } else {
     // terms: (phi''_j, phi_k) = -(4k+6) diagonal with coefficient alfa, and the
     // mass matrix B (legendre/matrices.py:121-135) with coefficient beta
@@ -171,12 +246,17 @@ extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, con
       if (k + 2 < n) bands[(1 * 5 + 3) * n + k] = -h[k + 2];
       if (k >= 2) bands[(1 * 5 + 1) * n + k] = -h[k];
     }
-    cudaMemcpy(p->bands, bands.data(), sizeof(double) * nb, cudaMemcpyHostToDevice);
-    cudaMemcpy(p->coef, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
-    cudaMemcpy(p->coef + p->nsys, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice);
-    st = sgpu_band_sep_factor((int)n, 2, -1, p->bands, nullptr, p->coef, p->nsys, p->fac, 0);
+    cudaMemcpyAsync(p->bands, bands.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(p->coef, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(p->coef + p->nsys, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
+    st = sgpu_band_sep_factor((int)n, 2, -1, p->bands, nullptr, p->coef, p->nsys, p->fac, stream);
   }
-  if (st != SGPU_OK || cudaDeviceSynchronize() != cudaSuccess) {
+  // plain creation waits for the factorisation; stream-ordered creation leaves
+  // it queued on `stream` (later work on that stream sees it)
+  const cudaError_t ce = ordered ? cudaGetLastError()
+                                 : (cudaStreamSynchronize(stream) == cudaSuccess ? cudaGetLastError()
+                                                                                : cudaErrorUnknown);
+  if (st != SGPU_OK || ce != cudaSuccess) {
     cudaGetLastError();
     destroy_all(p);
     return SGPU_ERR_CUDA;
@@ -184,6 +264,7 @@ extern "C" int sgpu_helmholtz_create(sgpu_helmholtz_problem** out, int ndim, con
   *out = p;
   return SGPU_OK;
 }
+}  // namespace
 
 extern "C" int sgpu_helmholtz_destroy(sgpu_helmholtz_problem* p) {
   destroy_all(p);

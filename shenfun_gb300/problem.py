@@ -18,7 +18,9 @@ FAMILIES = {"chebyshev": 1, "legendre": 2}
 
 
 class HelmholtzProblem:
-    def __init__(self, N, family="chebyshev", c=0.0, form="plain"):
+    def __init__(self, N, family="chebyshev", c=0.0, form="plain", stream=None):
+        """With `stream`, creation is stream-ordered (shared per-axis plans,
+        factorisation queued on that stream, no device synchronisation)."""
         require_cuda()
         self.N = tuple(int(n) for n in N)
         self.family = family
@@ -26,8 +28,13 @@ class HelmholtzProblem:
         self.form = _lib.FORMS[form]
         h = ctypes.c_void_p()
         arr = (ctypes.c_int64 * len(self.N))(*self.N)
-        _lib.call("sgpu_helmholtz_create", ctypes.byref(h), len(self.N), ctypes.cast(arr, ctypes.c_void_p),
-                  FAMILIES[family], self.c, self.form)
+        if stream is None:
+            _lib.call("sgpu_helmholtz_create", ctypes.byref(h), len(self.N),
+                      ctypes.cast(arr, ctypes.c_void_p), FAMILIES[family], self.c, self.form)
+        else:
+            _lib.call("sgpu_helmholtz_create_on", ctypes.byref(h), len(self.N),
+                      ctypes.cast(arr, ctypes.c_void_p), FAMILIES[family], self.c, self.form,
+                      stream_handle(stream))
         self._h = h
         phys = (ctypes.c_int64 * 3)()
         spec = (ctypes.c_int64 * 3)()

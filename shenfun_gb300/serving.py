@@ -196,7 +196,7 @@ class GpuExecutor:
 
     # -- factorisation cache ---------------------------------------------
     def cache_bytes(self):
-        return sum(b for _, b in self.cache.values())
+        return sum(ent[1] for ent in self.cache.values())
 
     def factor_cost(self, req):
         return 0 if req.key in self.cache else factor_bytes(req.N, req.family)
@@ -208,23 +208,31 @@ class GpuExecutor:
                 break  # still in use
             self.cache.popitem(last=False)
 
-    def problem(self, req):
+    def problem(self, req, stream):
+        """Cached problem for `req`, ready for use on `stream`.  A miss is
+        created stream-ordered on `stream` (no device synchronisation); a hit
+        created on another stream makes `stream` wait for its factorisation."""
         ent = self.cache.get(req.key)
         if ent is not None:
             self.cache.move_to_end(req.key)
             self.hits += 1
-            return ent[0]
+            p, _, ready = ent
+            if ready is not None and ready[1] is not stream:
+                stream.wait_event(ready[0])
+            return p
         self.misses += 1
-        p = self.Problem(req.N, req.family, req.c, self.form)
-        self.cache[req.key] = (p, factor_bytes(req.N, req.family))
+        p = self.Problem(req.N, req.family, req.c, self.form, stream=stream)
+        ev = self.torch.cuda.Event()
+        ev.record(stream)
+        self.cache[req.key] = (p, factor_bytes(req.N, req.family), (ev, stream))
         self.shrink_cache(self.cache_budget)
         return p
 
     # -- execution ----------------------------------------------------------
     def launch(self, req):
         torch = self.torch
-        p = self.problem(req)
         s = self.streams[req.slot % len(self.streams)]
+        p = self.problem(req, s)
         with torch.cuda.stream(s):
             f_host = req.f if isinstance(req.f, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(req.f))
             d_f = torch.empty(p.phys_shape, dtype=torch.float64, device="cuda")

@@ -73,3 +73,39 @@ def test_serving_mix_equals_alone(sg):
         N, fam, c, _, seed = stream[i]
         f = np.random.default_rng(seed).standard_normal(N)
         assert rel(m[i].result.numpy(), oracle_roundtrip(f, N, fam, c)) < 1e-12
+
+
+@pytest.mark.parametrize("N,family", [((16, 12, 24), "chebyshev"), ((24, 31), "legendre")])
+def test_stream_ordered_create_equals_plain(sg, N, family):
+    """A problem created stream-ordered (shared plans, factorisation queued on
+    a side stream) gives bit-for-bit the result of the synchronous creation."""
+    from shenfun_gb300.problem import HelmholtzProblem
+    f = torch.as_tensor(np.random.default_rng(3).standard_normal(N), device="cuda")
+    u0 = HelmholtzProblem(N, family, 3.0).solve(f)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    p = HelmholtzProblem(N, family, 3.0, stream=s)
+    with torch.cuda.stream(s):
+        f.record_stream(s)
+        u1 = p.solve(f, stream=s)
+    s.synchronize()
+    assert torch.equal(u0, u1)
+
+
+def test_serving_shared_keys_across_streams(sg):
+    """Requests that share a cached problem run on other streams than the one
+    that created it: each must wait for the factorisation, and every result
+    equals the request run alone."""
+    from shenfun_gb300 import serving as SV
+    keys = [((24, 20, 32), "chebyshev", 10.0), ((40, 48), "legendre", 2.0),
+            ((16, 16, 64), "chebyshev", 0.3)]
+    stream = [(keys[i % 3][0], keys[i % 3][1], keys[i % 3][2], 0.0, 100 + i) for i in range(18)]
+    alone, _ = SV.run_stream(stream, SV.GpuExecutor(nstreams=1), max_slots=1)
+    ex = SV.GpuExecutor(nstreams=4)
+    mix, _ = SV.run_stream(stream, ex, max_slots=8)
+    torch.cuda.synchronize()
+    assert ex.misses == 3 and ex.hits == 15
+    a = {r.id: r for r in alone}
+    for r in mix:
+        assert r.state == SV.DONE, r.error
+        assert torch.equal(a[r.id].result, r.result), r.id
