@@ -248,28 +248,45 @@ def serving_leg(torch, rates=(300.0, None), nreq=200, seed=5):
     return out
 
 
-def legendre_leg(torch, N=512, lines=16384, reps=3):
-    """Legendre ShenDirichlet transforms (dense contraction), plain FP64:
-    scalar product and backward of `lines` lines of length N."""
+def legendre_leg(torch, flush, st, N=512, lines=16384, reps=5):
+    """Legendre ShenDirichlet lines of length N: coefficients
+    c_k ~ U(-1, 1) (k + 1)^-2 (seed 0), backward then forward, in the plain
+    FP64 form and in the mixed form (BF16 digit slices on the tensor cores).
+    FP64-equivalent rate = 2 N^2 lines per direction / time; L2 flushed before
+    every timed step."""
     from shenfun_gb300.legendre import LegendreShenDirichlet
-    V = LegendreShenDirichlet(N)
-    x = torch.randn(lines, N, dtype=torch.float64, device="cuda")
-    y = torch.empty_like(x)
-    st = torch.cuda.current_stream()
-    res = {}
-    for name, fn in (("scalar_product", lambda: V.scalar_product(x, y, axis=1)),
-                     ("backward", lambda: V.backward(x, y, axis=1))):
-        fn()
+    rng = np.random.default_rng(0)
+    c = rng.uniform(-1, 1, (lines, N)) * (np.arange(N) + 1.0) ** -2
+    c[:, -2:] = 0
+    cd = torch.as_tensor(c, device="cuda")
+    u = torch.empty_like(cd)
+    c2 = torch.empty_like(cd)
+    flops = 2.0 * N * N * lines
+    out = {"N": N, "lines": lines, "data": "c_k ~ U(-1,1)(k+1)^-2, seed 0", "forms": {}}
+    ref = None
+    for form in ("plain", "mixed"):
+        V = LegendreShenDirichlet(N, form=form)
+        bwd = lambda: V.backward(cd, u, axis=1)  # noqa: E731
+        fwd = lambda: V.forward(u, c2, axis=1)  # noqa: E731
+        for _ in range(2):
+            bwd()
+            fwd()
         torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(st)
-        for _ in range(reps):
-            fn()
-        b.record(st)
-        b.synchronize()
-        ms = a.elapsed_time(b) / reps
-        res[name] = {"ms": ms, "tflops": 2.0 * N * N * lines / (ms * 1e-3) / 1e12}
-    return {"N": N, "lines": lines, "form": "plain FP64", **res}
+        tb = float(np.mean(time_steps_gpu(torch, bwd, reps, flush, st)))
+        tf = float(np.mean(time_steps_gpu(torch, fwd, reps, flush, st)))
+        res = {"ms_backward": tb, "ms_forward": tf,
+               "tflops_fp64_equiv_backward": flops / (tb * 1e-3) / 1e12,
+               "tflops_fp64_equiv_forward": flops / (tf * 1e-3) / 1e12}
+        if ref is None:
+            ref = (u.clone(), c2.clone())
+        else:
+            res["rel_err_vs_plain"] = max(float(((u - ref[0]).abs().max() / ref[0].abs().max()).item()),
+                                          float(((c2 - ref[1]).abs().max() / ref[1].abs().max()).item()))
+        res["rel_err_roundtrip"] = float(((c2 - cd).abs().max() / cd.abs().max()).item())
+        out["forms"][form] = res
+    p_, m_ = out["forms"]["plain"], out["forms"]["mixed"]
+    out["mixed_over_plain"] = (p_["ms_backward"] + p_["ms_forward"]) / (m_["ms_backward"] + m_["ms_forward"])
+    return out
 
 
 CASES = {
@@ -277,6 +294,7 @@ CASES = {
     "r2c-plain": ("r2c", "plain"), "r2c-mixed": ("r2c", "mixed"),
     "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
     "solve-plain": ("solve", "plain"),
+    "leg-plain": ("leg", "plain"), "leg-mixed": ("leg", "mixed"),
 }
 
 
@@ -299,6 +317,13 @@ def run_case(name, reps=3):
         V.form = _lib.FORMS[form]
         y = torch.empty_like(x)
         fn = lambda: V.scalar_product(x, y, axis=2)  # noqa: E731
+    elif kind == "leg":
+        # Legendre ShenDirichlet N = 512 backward over 16,384 lines
+        from shenfun_gb300.legendre import LegendreShenDirichlet
+        V = LegendreShenDirichlet(512, form=form)
+        c = torch.randn(16384, 512, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(c)
+        fn = lambda: V.backward(c, y, axis=1)  # noqa: E731
     else:
         import shenfun_gb300 as sg
         run = FormRun(sg, form, x.cpu().numpy())
@@ -419,7 +444,7 @@ def main():
     serving = legendre = None
     if rank == 0 and not args.no_extra:
         serving = serving_leg(torch)
-        legendre = legendre_leg(torch)
+        legendre = legendre_leg(torch, flush, st)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -65,8 +65,11 @@ extern "C" {
 
 /* arithmetic form */
 #define SGPU_PLAIN_F64 0   /* all FP64                                        */
-#define SGPU_MIXED_DF 1    /* double-float (FP32 pair, ~48-bit) arithmetic on the
-                              FP32 pipes; FP64 in and out (the mixed form)     */
+#define SGPU_MIXED_DF 1    /* the mixed form, FP64 in and out: double-float (FP32
+                              pair, ~48-bit) arithmetic on the FP32 pipes for
+                              the FFT/DCT line transforms; BF16 digit slices on
+                              the tensor cores (~48-bit) for the Legendre
+                              contractions                                     */
 
 const char* sgpu_status_string(int status);
 int sgpu_version(void);
@@ -213,6 +216,9 @@ int sgpu_helmholtz_solve_noalloc(const sgpu_helmholtz_problem* problem, const do
 /* fastgl_wrap.pyx:31 leggauss(N): nodes ascending, weights; host pointers */
 int sgpu_leggauss(int N, double* x, double* w);
 typedef struct sgpu_legendre_plan sgpu_legendre_plan;
+/* form SGPU_PLAIN_F64: FP64 contraction.  form SGPU_MIXED_DF: the matrices
+ * are split into BF16 digit slices and contracted on the tensor cores with
+ * FP32 accumulation (about 48 bits; N <= 1024, else SGPU_ERR_UNSUPPORTED). */
 int sgpu_legendre_plan_create(sgpu_legendre_plan** plan, int N, int basis, int form);
 int sgpu_legendre_plan_destroy(sgpu_legendre_plan* plan);
 /* copy the plan's nodes and weights to host arrays of N entries */
@@ -224,6 +230,18 @@ int sgpu_legendre_nodes(const sgpu_legendre_plan* plan, double* x, double* w);
 int sgpu_legendre_execute(const sgpu_legendre_plan* plan, int direction, const void* in,
                           void* out, int64_t outer, int64_t inner, int data_kind,
                           cudaStream_t stream);
+/* device scratch an execution of (outer, N, inner) lines needs (0 for the
+ * plain form); the _ws entry takes it from the caller (256-byte aligned) and
+ * allocates nothing.  sgpu_legendre_execute without it takes the mixed form's
+ * scratch from cudaMallocAsync on `stream` for the call. */
+int sgpu_legendre_workspace_size(const sgpu_legendre_plan* plan, int64_t outer, int64_t inner,
+                                 int data_kind, size_t* bytes);
+int sgpu_legendre_execute_ws(const sgpu_legendre_plan* plan, int direction, const void* in,
+                             void* out, int64_t outer, int64_t inner, int data_kind, void* work,
+                             size_t work_bytes, cudaStream_t stream);
+/* number of bounded device-side waits of the tensor-core kernels that gave up
+ * since load (0 unless a pipeline stalled; such a launch's output is invalid) */
+int sgpu_wait_timeouts(unsigned int* count);
 
 #ifdef __cplusplus
 }

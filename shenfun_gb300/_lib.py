@@ -67,6 +67,9 @@ SIGNATURES = {
     "sgpu_legendre_plan_destroy": (_int, [_vp]),
     "sgpu_legendre_nodes": (_int, [_vp, _vp, _vp]),
     "sgpu_legendre_execute": (_int, [_vp, _int, _vp, _vp, _i64, _i64, _int, _vp]),
+    "sgpu_legendre_workspace_size": (_int, [_vp, _i64, _i64, _int, ctypes.POINTER(ctypes.c_size_t)]),
+    "sgpu_legendre_execute_ws": (_int, [_vp, _int, _vp, _vp, _i64, _i64, _int, _vp, ctypes.c_size_t, _vp]),
+    "sgpu_wait_timeouts": (_int, [ctypes.POINTER(ctypes.c_uint)]),
 }
 
 

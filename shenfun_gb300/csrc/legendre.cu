@@ -12,11 +12,15 @@
 // entries of ShenDirichlet apply to every row (spectralbase.py:1504-1526), so
 // the scalar product keeps the orthogonal coefficients in the tail rows.
 // The matrices are built on the host in long double and stored in FP64.
+// Plain form: FP64 tiled GEMM (k_line_gemm_f64).  Mixed form: the same
+// matrices split into BF16 digit slices and contracted on the tensor cores
+// (ozaki_tc.cu), about 48 bits, for N <= 1024.
 #include <cmath>
 #include <cstring>
 #include <new>
 #include <vector>
 
+#include "ozaki_tc.h"
 #include "solvers.cuh"
 
 using namespace sgpu;
@@ -113,6 +117,7 @@ struct sgpu_legendre_plan {
   double* d_mass;    // LU'd mass bands (reciprocal diagonal), forward transform
   double* d_nodes;   // x, w (2N)
   std::vector<double> x, w;
+  oz::Matrix tc_scalar, tc_back;  // mixed form: split Ms, Mb
 };
 
 extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int basis, int form) {
@@ -120,7 +125,11 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
   *out = nullptr;
   if (N < 2 || N > 8192) return SGPU_ERR_ARG;
   if (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SB) return SGPU_ERR_ARG;
-  if (form != SGPU_PLAIN_F64) return SGPU_ERR_UNSUPPORTED;
+  if (form != SGPU_PLAIN_F64 && form != SGPU_MIXED_DF) return SGPU_ERR_UNSUPPORTED;
+  if (form == SGPU_MIXED_DF) {
+    int W, S;
+    if (oz::pick_digits(N, &W, &S) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
+  }
   if (basis == SGPU_BASIS_SD && N < 4) return SGPU_ERR_ARG;
   if (basis == SGPU_BASIS_SB && N < 8) return SGPU_ERR_ARG;
   sgpu_legendre_plan* p = new (std::nothrow) sgpu_legendre_plan;
@@ -216,6 +225,17 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
     delete p;
     return SGPU_ERR_CUDA;
   }
+  if (form == SGPU_MIXED_DF) {
+    int st = oz::matrix_create(Ms.data(), N, &p->tc_scalar);
+    if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, &p->tc_back);
+    if (st != SGPU_OK) {
+      oz::matrix_destroy(&p->tc_scalar);
+      oz::matrix_destroy(&p->tc_back);
+      cudaFree(dev);
+      delete p;
+      return st;
+    }
+  }
   *out = p;
   return SGPU_OK;
 }
@@ -223,6 +243,8 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
 extern "C" int sgpu_legendre_plan_destroy(sgpu_legendre_plan* p) {
   if (!p) return SGPU_OK;
   cudaFree(p->d_scalar);
+  oz::matrix_destroy(&p->tc_scalar);
+  oz::matrix_destroy(&p->tc_back);
   delete p;
   return SGPU_OK;
 }
@@ -343,9 +365,9 @@ __global__ void k_legendre_mass(T* u, const double* mass, int N, int basis, int6
 }
 
 // direction: 0 = scalar product, 1 = forward (scalar product + mass solve), 2 = backward
-extern "C" int sgpu_legendre_execute(const sgpu_legendre_plan* p, int direction, const void* in,
-                                     void* out, int64_t outer, int64_t inner, int data_kind,
-                                     cudaStream_t stream) {
+static int legendre_run(const sgpu_legendre_plan* p, int direction, const void* in, void* out,
+                        int64_t outer, int64_t inner, int data_kind, void* work, size_t work_bytes,
+                        cudaStream_t stream) {
   if (!p || !in || !out || outer < 0 || inner < 1) return SGPU_ERR_ARG;
   if (direction < 0 || direction > 2) return SGPU_ERR_ARG;
   if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
@@ -353,11 +375,17 @@ extern "C" int sgpu_legendre_execute(const sgpu_legendre_plan* p, int direction,
   const int64_t nlines = outer * inner;
   if (nlines == 0) return SGPU_OK;
   const int cplx = data_kind == SGPU_COMPLEX;
-  const int64_t nrows = nlines * (1 + cplx);
-  dim3 grid((unsigned)((nrows + TM - 1) / TM), (unsigned)((p->N + TN - 1) / TN));
-  if (grid.x > 0x7fffffffu) return SGPU_ERR_ARG;
-  const double* M = direction == 2 ? p->d_back : p->d_scalar;
-  k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, nrows, inner, cplx);
+  if (p->form == SGPU_MIXED_DF) {
+    const oz::Matrix& M = direction == 2 ? p->tc_back : p->tc_scalar;
+    const int st = oz::contract(M, (const double*)in, (double*)out, nlines, inner, cplx, work, work_bytes, stream);
+    if (st != SGPU_OK) return st;
+  } else {
+    const int64_t nrows = nlines * (1 + cplx);
+    dim3 grid((unsigned)((nrows + TM - 1) / TM), (unsigned)((p->N + TN - 1) / TN));
+    if ((nrows + TM - 1) / TM > 0x7fffffff) return SGPU_ERR_ARG;
+    const double* M = direction == 2 ? p->d_back : p->d_scalar;
+    k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, nrows, inner, cplx);
+  }
   if (direction == 1) {
     const unsigned nb = (unsigned)((nlines + 127) / 128);
     if (cplx)
@@ -366,4 +394,42 @@ extern "C" int sgpu_legendre_execute(const sgpu_legendre_plan* p, int direction,
       k_legendre_mass<double><<<nb, 128, 0, stream>>>((double*)out, p->d_mass, p->N, p->basis, nlines, inner);
   }
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
+}
+
+extern "C" int sgpu_legendre_workspace_size(const sgpu_legendre_plan* p, int64_t outer, int64_t inner,
+                                            int data_kind, size_t* bytes) {
+  if (!p || !bytes || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
+  *bytes = p->form == SGPU_MIXED_DF
+               ? oz::workspace_bytes(p->tc_scalar, outer * inner, inner, data_kind == SGPU_COMPLEX)
+               : 0;
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_legendre_execute_ws(const sgpu_legendre_plan* p, int direction, const void* in,
+                                        void* out, int64_t outer, int64_t inner, int data_kind,
+                                        void* work, size_t work_bytes, cudaStream_t stream) {
+  return legendre_run(p, direction, in, out, outer, inner, data_kind, work, work_bytes, stream);
+}
+
+// without a caller workspace the mixed form takes its scratch from the
+// stream-ordered allocator for the duration of the call
+extern "C" int sgpu_legendre_execute(const sgpu_legendre_plan* p, int direction, const void* in,
+                                     void* out, int64_t outer, int64_t inner, int data_kind,
+                                     cudaStream_t stream) {
+  if (!p || p->form != SGPU_MIXED_DF)
+    return legendre_run(p, direction, in, out, outer, inner, data_kind, nullptr, 0, stream);
+  size_t nb = 0;
+  int st = sgpu_legendre_workspace_size(p, outer, inner, data_kind, &nb);
+  if (st != SGPU_OK) return st;
+  if (nb == 0 || outer * inner == 0)
+    return legendre_run(p, direction, in, out, outer, inner, data_kind, nullptr, 0, stream);
+  void* work = nullptr;
+  if (cudaMallocAsync(&work, nb, stream) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_NOMEM;
+  }
+  st = legendre_run(p, direction, in, out, outer, inner, data_kind, work, nb, stream);
+  cudaFreeAsync(work, stream);
+  return st;
 }

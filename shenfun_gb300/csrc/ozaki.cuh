@@ -1,0 +1,278 @@
+// Dense FP64 line contractions on the BF16 tensor cores (tcgen05), exact to
+// about 42 bits, by splitting both operands into BF16 "digit" slices
+// (the Ozaki scheme: Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59, 2012;
+// on FP16/BF16 tensor cores: Ootomo & Yokota, IJHPCA 2022).
+//
+//   out(l, n) = sum_k A(l, k) B(k, n)       A: lines x K (FP64), B: K x Nout
+//
+// Each row of A (and each column of B) is scaled by a power of two 2^e with
+// |x| < 2^{e-1} (one bit of headroom) and rounded to a W*S-bit fixed-point
+// integer X < 2^{WS-1}, which is cut into S balanced digits:
+// X = sum_s d_s 2^{W(S-1-s)},  |d_s| <= 2^{W-1}.  Slice s stores d_s 2^{-W s}
+// in BF16 (exact: at most 8 significant bits).  Then
+//   A B = 2^{eA+eB-2W} sum_{s,t} A_s B_t,
+// and the products with s + t <= S - 1 are kept (W = 7, S = 7: 28 products,
+// 48 bits).  The tensor core sums them into five FP32 accumulators in TMEM:
+// G0 (s+t=0), G1, G2, G3 and G4 (s+t>=4).  Group g holds multiples of
+// 2^{-W g} of magnitude at most (g+1) 2^{2W-2} K units, below 2^24 for
+// g <= 3 when K <= 2^{26-2W}/4 (W=7: K <= 1024), so those FP32 sums are
+// exact; G4 carries terms below 2^{-4W} relative, where FP32 rounding is
+// harmless (a fourth exact group lowers the error ~50x against folding
+// s+t=3 into the rounded one).  The
+// epilogue adds the four in 64-bit fixed point with integer instructions and
+// assembles the FP64 result bit by bit (the FP64 pipe is ~1/64 of FP32 on
+// this part, so no FP64 arithmetic runs per element).
+//
+// Data layout: the split slices are written pre-tiled in the tensor core's
+// canonical no-swizzle K-major layout, one block per (slice, row tile,
+// 32-wide K block): [kgroup 4][rowgroup][row 8][8 elements] (8 KB for the
+// 128-row A tiles, 6 KB for the 96-row B tiles).  A pipeline stage is then
+// 2S plain bulk copies (cp.async.bulk).
+#pragma once
+
+#include <cmath>
+#include <cstring>
+
+#include "sgpu_common.cuh"
+#include "tc_ptx.cuh"
+
+namespace sgpu {
+namespace oz {
+
+const int BM = 128;       // rows (lines) per tile = MMA M
+const int BN = 96;        // output columns per tile = MMA N (NACC * BN <= 512 TMEM columns)
+const int BK = 32;        // K per pipeline stage
+const int STAGES = 2;
+const int NACC = 5;       // accumulators: digit groups 0..3 exact, >= 4 combined
+const int A_ELEMS = BM * BK;            // 4096 bf16 = 8 KB per A slice block
+const int B_ELEMS = BN * BK;            // 3072 bf16 = 6 KB per B slice block
+const int A_BYTES = A_ELEMS * 2;
+const int B_BYTES = B_ELEMS * 2;
+const int LBO_A = BM * 16;              // K-direction core-matrix stride (bytes)
+const int LBO_B = BN * 16;
+const int SBO = 128;                    // row-direction core-matrix stride (bytes)
+
+// index of element (row r, k in the K block) inside a block of `rows` rows:
+// [k / 8][r / 8][r % 8][k % 8]
+SGPU_HD int tile_index(int rows, int r, int k) {
+  return (k >> 3) * rows * 8 + (r >> 3) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+// exponent of a row/column: e with max|x| < 2^{e-1} (one bit of headroom),
+// from the largest biased exponent field (0 for an all-zero or all-subnormal
+// line)
+SGPU_HD int exp_from_field(uint32_t maxfield) { return maxfield ? (int)maxfield - 1021 : 0; }
+
+SGPU_HD uint32_t exp_field(double x) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  return (uint32_t)((b >> 52) & 0x7ff);
+}
+
+// balanced digits of x (|x| < 2^{e-1}) at W*S bits: BF16 bit patterns of
+// d_s 2^{-W s}.  Integer arithmetic only.
+template <int W, int S>
+SGPU_HD void split_digits(double x, int e, uint16_t (&out)[S]) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  const int field = (int)((b >> 52) & 0x7ff);
+  int64_t X = 0;
+  if (field != 0) {
+    const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 1075 + e - W * S - field;  // >= 54 - W*S > 0 since |x| < 2^{e-1}
+    if (sh < 64) X = (int64_t)((m + (1ull << (sh - 1))) >> sh);
+  }
+  const bool neg = (b >> 63) != 0;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const int shs = W * (S - 1 - s);
+    int64_t d;
+    if (s < S - 1) {
+      d = (X + ((int64_t)1 << (shs - 1))) >> shs;
+      X -= d * ((int64_t)1 << shs);
+    } else {
+      d = X;
+    }
+    if (neg) d = -d;
+    // d 2^{-W s} as a float (exact), then its top 16 bits are the BF16 value
+    float f = (float)d;
+    const uint32_t pb = (uint32_t)(127 - W * s) << 23;  // 2^{-W s}
+    float p;
+    memcpy(&p, &pb, 4);
+    f *= p;
+    uint32_t fb;
+    memcpy(&fb, &f, 4);
+    out[s] = (uint16_t)(fb >> 16);
+  }
+}
+
+// round(v * 2^sh) for an FP32 v, as int64, integer instructions only
+// (FP32 subnormals count as zero)
+SGPU_HD int64_t f32_fixed(uint32_t b, int sh) {
+  const int ex = (int)((b >> 23) & 0xff);
+  if (ex == 0) return 0;
+  const int64_t m = (int64_t)((b & 0x7fffffu) | 0x800000u);
+  const int e = ex - 150 + sh;  // v 2^sh = m 2^e
+  int64_t r;
+  if (e >= 0)
+    r = e < 39 ? (m << e) : 0;  // callers keep |v 2^sh| < 2^62
+  else if (e > -40)
+    r = (m + ((int64_t)1 << (-e - 1))) >> (-e);
+  else
+    r = 0;
+  return (b >> 31) ? -r : r;
+}
+
+// T * 2^E as an FP64 bit pattern, round to nearest even; integer instructions
+// except for results outside the normal range (rare, handled with ldexp)
+SGPU_HD double fixed_to_double(int64_t T, int E) {
+  if (T == 0) return 0.0;
+  const uint64_t sign = T < 0 ? (1ull << 63) : 0;
+  const uint64_t a = T < 0 ? (uint64_t)(-T) : (uint64_t)T;
+#if defined(__CUDA_ARCH__)
+  const int msb = 63 - __clzll((long long)a);
+#else
+  const int msb = 63 - __builtin_clzll(a);
+#endif
+  uint64_t mant;
+  int e2;
+  if (msb > 52) {
+    const int s = msb - 52;
+    const uint64_t rem = a & ((1ull << s) - 1), half = 1ull << (s - 1);
+    mant = a >> s;
+    if (rem > half || (rem == half && (mant & 1))) ++mant;
+    e2 = s;
+    if (mant >> 53) {
+      mant >>= 1;
+      ++e2;
+    }
+  } else {
+    mant = a << (52 - msb);
+    e2 = msb - 52;
+  }
+  const int biased = e2 + E + 52 + 1023;
+  if (biased <= 0 || biased >= 2047) {
+    const double v = ldexp((double)mant, e2 + E);
+    return sign ? -v : v;
+  }
+  const uint64_t bits = sign | ((uint64_t)biased << 52) | (mant & 0xFFFFFFFFFFFFFull);
+  double r;
+  memcpy(&r, &bits, 8);
+  return r;
+}
+
+// one output element from the NACC FP32 accumulators (bit patterns) of the
+// digit groups; E = eA + eB - 2W (|G| <= 2^24 each, so the 2^-36 fixed
+// point stays below 2^63)
+SGPU_HD double combine_groups(const uint32_t (&gb)[NACC], int E) {
+  int64_t T = 0;
+  for (int i = 0; i < NACC; ++i) T += f32_fixed(gb[i], 36);
+  return fixed_to_double(T, E - 36);
+}
+
+// geometry of one contraction over lines of a (outer, N, inner) array:
+// rows are lines (complex lines give two rows: real and imaginary parts)
+struct Geom {
+  int64_t nrows;   // rows of A (lines x (1 + cplx))
+  int64_t inner;
+  int N;           // line length (= K = Nout)
+  int cplx;
+  int nkb;         // K blocks of BK (K padded with zeros)
+  int mtiles;      // row tiles of BM
+  int ntiles;      // output-column tiles of BN
+};
+
+SGPU_HD int64_t row_offset(const Geom& g, int64_t row, int64_t j) {
+  const int64_t l = g.cplx ? (row >> 1) : row;
+  const int64_t part = g.cplx ? (row & 1) : 0;
+  const int64_t o = l / g.inner, i = l - o * g.inner;
+  const int64_t e = (o * g.N + j) * g.inner + i;
+  return g.cplx ? 2 * e + part : e;
+}
+
+// bytes of the split operand A (slices + row exponents) for a geometry
+inline size_t a_split_bytes(const Geom& g, int S) {
+  return (size_t)S * g.mtiles * g.nkb * A_BYTES + (size_t)g.mtiles * BM * sizeof(int);
+}
+
+inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx) {
+  Geom g;
+  g.N = N;
+  g.inner = inner;
+  g.cplx = cplx;
+  g.nrows = nlines * (1 + cplx);
+  g.nkb = (N + BK - 1) / BK;
+  g.mtiles = (int)((g.nrows + BM - 1) / BM);
+  g.ntiles = (N + BN - 1) / BN;
+  return g;
+}
+
+// largest exponent field of row `row` over the lanes' strided share
+// (lane, lane + nlane, ...); rows past nrows give 0
+SGPU_HD uint32_t rowexp_partial(const double* in, const Geom& g, int64_t row, int lane, int nlane) {
+  uint32_t mf = 0;
+  if (row < g.nrows)
+    for (int j = lane; j < g.N; j += nlane) {
+      const uint32_t f = exp_field(in[row_offset(g, row, j)]);
+      mf = f > mf ? f : mf;
+    }
+  return mf;
+}
+
+// split thread t: (row rr of tile mt, 8-wide chunk kc of K) -> S 16-byte
+// stores, one per slice block.  t < mtiles * nkb * 4 * BM.
+template <int W, int S>
+SGPU_HD void split_thread(const double* in, const int* eA, uint16_t* At, const Geom& g, int64_t t) {
+  const int64_t nk = (int64_t)g.nkb * 4;
+  const int rr = (int)(t & (BM - 1));
+  const int64_t rest = t >> 7;
+  const int kc = (int)(rest % nk);
+  const int mt = (int)(rest / nk);
+  const int kb = kc >> 2, kg = kc & 3;
+  const int64_t row = (int64_t)mt * BM + rr;
+  const int k0 = kb * BK + kg * 8;
+  const int e = eA[row];
+  uint16_t dig[8][S];
+  for (int q = 0; q < 8; ++q) {
+    const int k = k0 + q;
+    const double x = (row < g.nrows && k < g.N) ? in[row_offset(g, row, k)] : 0.0;
+    split_digits<W, S>(x, e, dig[q]);
+  }
+  for (int s = 0; s < S; ++s) {
+    uint32_t v[4];
+    for (int q = 0; q < 4; ++q) v[q] = (uint32_t)dig[2 * q][s] | ((uint32_t)dig[2 * q + 1][s] << 16);
+    uint16_t* dst = At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + tile_index(BM, rr, kg * 8);
+    memcpy(dst, v, 16);
+  }
+}
+
+// host: split a fixed N x N matrix M (out = in . M, so output column n is
+// M[:, n]) into tiled slices [S][ntiles][nkb][8 KB] and per-column exponents
+template <int W, int S>
+void split_matrix_host(const double* M, int N, uint16_t* tiles, int* ex) {
+  const int nkb = (N + BK - 1) / BK, ntiles = (N + BN - 1) / BN;
+  memset(tiles, 0, sizeof(uint16_t) * (size_t)S * ntiles * nkb * B_ELEMS);
+  memset(ex, 0, sizeof(int) * (size_t)ntiles * BN);
+  for (int n = 0; n < N; ++n) {
+    uint32_t mf = 0;
+    for (int k = 0; k < N; ++k) {
+      const uint32_t f = exp_field(M[(size_t)k * N + n]);
+      mf = f > mf ? f : mf;
+    }
+    ex[n] = exp_from_field(mf);
+    const int nt = n / BN, r = n % BN;
+    for (int k = 0; k < N; ++k) {
+      uint16_t d[S];
+      split_digits<W, S>(M[(size_t)k * N + n], ex[n], d);
+      for (int s = 0; s < S; ++s)
+        tiles[(((size_t)s * ntiles + nt) * nkb + k / BK) * B_ELEMS + tile_index(BN, r, k % BK)] = d[s];
+    }
+  }
+}
+
+inline size_t matrix_tile_elems(int N, int S) {
+  return (size_t)S * ((N + BN - 1) / BN) * ((N + BK - 1) / BK) * B_ELEMS;
+}
+
+}  // namespace oz
+}  // namespace sgpu

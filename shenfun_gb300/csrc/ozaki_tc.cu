@@ -1,0 +1,260 @@
+// Split-BF16 tensor-core contraction along lines (the mixed form of the
+// Legendre Vandermonde transforms).  Kernels:
+//   k_oz_rowexp   one warp per row: the row's power-of-two scale
+//   k_oz_split    one thread per (row, 8-wide K chunk): S digit slices written
+//                 pre-tiled (16-byte stores, coalesced along rows)
+//   k_oz_gemm     one CTA per 128 x 96 output tile: a producer thread streams
+//                 2S slice blocks per K stage with bulk copies, one thread
+//                 issues tcgen05.mma for the S(S+1)/2 slice products into five
+//                 TMEM accumulators, and all four warps run the integer
+//                 epilogue (TMEM -> registers -> FP64 bits -> global).
+// The split matrix operand (B) is built once on the host with the same digit
+// code and uploaded with the plan.
+#include <cstdio>
+#include <new>
+#include <vector>
+
+#include "ozaki.cuh"
+#include "ozaki_tc.h"
+
+using namespace sgpu;
+using namespace sgpu::oz;
+
+// count of bounded waits in these kernels that gave up (read by
+// sgpu_wait_timeouts); stays 0 unless a pipeline stalls
+__device__ unsigned int g_oz_timeouts = 0;
+
+__global__ void __launch_bounds__(256) k_oz_rowexp(const double* __restrict__ in, int* __restrict__ eA, Geom g) {
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= (int64_t)g.mtiles * BM) return;
+  uint32_t mf = rowexp_partial(in, g, warp, threadIdx.x & 31, 32);
+  mf = __reduce_max_sync(0xffffffffu, mf);
+  if ((threadIdx.x & 31) == 0) eA[warp] = exp_from_field(mf);
+}
+
+template <int W, int S>
+__global__ void __launch_bounds__(256) k_oz_split(const double* __restrict__ in, const int* __restrict__ eA,
+                                                  uint16_t* __restrict__ At, Geom g) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)g.mtiles * g.nkb * 4 * BM) return;
+  split_thread<W, S>(in, eA, At, g, t);
+}
+
+// shared memory: STAGES x (S blocks of A, S blocks of B), then the barriers
+template <int S>
+struct GemmSmem {
+  static const size_t stage_bytes = (size_t)S * (A_BYTES + B_BYTES);
+  static const size_t bar_off = STAGES * stage_bytes;
+  // barriers + alignment slack, rounded up to the 227 KB per-CTA maximum so
+  // that every descriptor-addressed operand read stays inside the allocation
+  static const size_t need = bar_off + 256 + 1024;
+  static const size_t bytes = need < 232448 ? 232448 : need;
+};
+static_assert(GemmSmem<7>::need <= 232448, "stages exceed shared memory");
+
+template <int W, int S>
+__global__ void __launch_bounds__(128, 1)
+    k_oz_gemm(const uint16_t* __restrict__ At, const int* __restrict__ eA, const uint16_t* __restrict__ Bt,
+              const int* __restrict__ eB, double* __restrict__ out, Geom g) {
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte aligned base
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + GemmSmem<S>::bar_off);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accf = empty + STAGES;
+  uint32_t* tmem_holder = (uint32_t*)(accf + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
+    tc::mbar_init(accf, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tmem_holder, 512);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_holder;
+  bool ok = true;
+
+  auto sA = [&](int st, int s) { return smem + (size_t)st * GemmSmem<S>::stage_bytes + (size_t)s * A_BYTES; };
+  auto sB = [&](int st, int s) {
+    return smem + (size_t)st * GemmSmem<S>::stage_bytes + (size_t)S * A_BYTES + (size_t)s * B_BYTES;
+  };
+
+  if (warp == 0 && lane == 0) {
+    // producer: stream the slice blocks of both operands through the stages
+    int kb = 0;
+    for (; kb < g.nkb; ++kb) {
+      const int st = kb % STAGES;
+      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+      if (kb >= STAGES && !tc::mbar_wait(&empty[st], ph ^ 1u)) {
+        ok = false;
+        break;
+      }
+      tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (A_BYTES + B_BYTES)));
+      for (int s = 0; s < S; ++s) {
+        tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS, A_BYTES, &full[st]);
+        tc::bulk_g2s(sB(st, s), Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * B_ELEMS, B_BYTES, &full[st]);
+      }
+    }
+    // drain: every copy issued must have landed before the CTA may exit
+    for (int q = kb - STAGES; q < kb; ++q) {
+      if (q < 0) continue;
+      if (!tc::mbar_wait(&full[q % STAGES], (uint32_t)(q / STAGES) & 1u)) ok = false;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    const uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
+    uint32_t inited = 0;
+    for (int kb = 0; kb < g.nkb; ++kb) {
+      const int st = kb % STAGES;
+      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+      if (!tc::mbar_wait(&full[st], ph)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+#pragma unroll
+      for (int ks = 0; ks < BK / 16; ++ks) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const uint64_t ad = tc::sdesc_interleave(tc::smem_u32(sA(st, s)) + ks * 2 * LBO_A, LBO_A, SBO);
+#pragma unroll
+          for (int t = 0; t + s < S; ++t) {
+            const uint64_t bd = tc::sdesc_interleave(tc::smem_u32(sB(st, t)) + ks * 2 * LBO_B, LBO_B, SBO);
+            const int acc = s + t < NACC - 1 ? s + t : NACC - 1;
+            tc::mma_f16(tmem + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
+            inited |= 1u << acc;
+          }
+        }
+      }
+      tc::mma_commit(&empty[st]);  // frees the stage once these MMAs have read it
+    }
+    tc::mma_commit(accf);  // accumulators final (also after an early exit)
+  }
+
+  // epilogue: warp w owns TMEM lanes 32w..32w+31 = tile rows
+  __syncwarp();
+  if (!tc::mbar_wait(accf, 0)) ok = false;
+  __syncwarp();
+  tc::fence_after_sync();
+  const int64_t row = (int64_t)mt * BM + warp * 32 + lane;
+  const bool row_ok = row < g.nrows;
+  const int erow = eA[row] - 2 * W;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  for (int c0 = 0; c0 < BN; c0 += 16) {
+    uint32_t a[NACC][16];
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) tc::tmem_ld16(tmem + lane_base + (uint32_t)(q * BN + c0), a[q]);
+    tc::tmem_ld_wait();
+    if (row_ok) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int col = nt * BN + c0 + j;
+        if (col < g.N) {
+          uint32_t gb[NACC];
+#pragma unroll
+          for (int q = 0; q < NACC; ++q) gb[q] = a[q][j];
+          out[row_offset(g, row, col)] = combine_groups(gb, erow + eB[col]);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (!ok && lane == 0) atomicAdd(&g_oz_timeouts, 1u);
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+namespace sgpu {
+namespace oz {
+
+int pick_digits(int K, int* W, int* S) {
+  *W = 7;
+  *S = 7;
+  return K <= 1365 ? SGPU_OK : SGPU_ERR_UNSUPPORTED;
+}
+
+int matrix_create(const double* M, int N, Matrix* out) {
+  out->N = N;
+  if (pick_digits(N, &out->W, &out->S) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
+  std::vector<uint16_t> tiles(matrix_tile_elems(N, out->S));
+  std::vector<int> ex((size_t)((N + BN - 1) / BN) * BN);
+  split_matrix_host<7, 7>(M, N, tiles.data(), ex.data());
+  const size_t tb = tiles.size() * sizeof(uint16_t), eb = ex.size() * sizeof(int);
+  void* dev = nullptr;
+  if (cudaMalloc(&dev, tb + eb) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_NOMEM;
+  }
+  out->tiles = (uint16_t*)dev;
+  out->exps = (int*)((char*)dev + tb);
+  if (cudaMemcpy(out->tiles, tiles.data(), tb, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(out->exps, ex.data(), eb, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(dev);
+    cudaGetLastError();
+    out->tiles = nullptr;
+    return SGPU_ERR_CUDA;
+  }
+  return SGPU_OK;
+}
+
+void matrix_destroy(Matrix* m) {
+  if (m && m->tiles) cudaFree(m->tiles);
+  if (m) m->tiles = nullptr;
+}
+
+size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx) {
+  const Geom g = make_geom(m.N, nlines, inner, cplx);
+  return a_split_bytes(g, m.S);
+}
+
+template <int W, int S>
+static int run(const Matrix& m, const Geom& g, const double* in, double* out, void* work, cudaStream_t stream) {
+  static bool attr_set = false;  // benign race: every caller sets the same value
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(k_oz_gemm<W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)GemmSmem<S>::bytes) != cudaSuccess)
+      return SGPU_ERR_CUDA;
+    attr_set = true;
+  }
+  uint16_t* At = (uint16_t*)work;
+  int* eA = (int*)((char*)work + (size_t)S * g.mtiles * g.nkb * A_BYTES);
+  const int64_t nrow_pad = (int64_t)g.mtiles * BM;
+  k_oz_rowexp<<<(unsigned)((nrow_pad * 32 + 255) / 256), 256, 0, stream>>>(in, eA, g);
+  const int64_t nsplit = nrow_pad * g.nkb * 4;
+  k_oz_split<W, S><<<(unsigned)((nsplit + 255) / 256), 256, 0, stream>>>(in, eA, At, g);
+  dim3 grid((unsigned)g.mtiles, (unsigned)g.ntiles);
+  k_oz_gemm<W, S><<<grid, 128, GemmSmem<S>::bytes, stream>>>(At, eA, m.tiles, m.exps, out, g);
+  return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
+}
+
+int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int64_t inner, int cplx,
+             void* work, size_t work_bytes, cudaStream_t stream) {
+  if (nlines == 0) return SGPU_OK;
+  const Geom g = make_geom(m.N, nlines, inner, cplx);
+  if (g.mtiles > 0x7fffffff || work_bytes < a_split_bytes(g, m.S) || ((uintptr_t)work & 255)) return SGPU_ERR_ARG;
+  if (m.W != 7 || m.S != 7) return SGPU_ERR_UNSUPPORTED;
+  return run<7, 7>(m, g, in, out, work, stream);
+}
+
+}  // namespace oz
+}  // namespace sgpu
+
+extern "C" int sgpu_wait_timeouts(unsigned int* count) {
+  if (!count) return SGPU_ERR_ARG;
+  return cudaMemcpyFromSymbol(count, g_oz_timeouts, sizeof(unsigned int)) == cudaSuccess ? SGPU_OK
+                                                                                           : SGPU_ERR_CUDA;
+}

@@ -1,0 +1,33 @@
+// Internal C++ interface of the split-BF16 tensor-core line contraction
+// (ozaki_tc.cu), used by the Legendre plans.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace sgpu {
+namespace oz {
+
+// a fixed N x N matrix M (row-major, out(l, n) = sum_k in(l, k) M[k][n]),
+// split into BF16 digit slices and tiled on the device
+struct Matrix {
+  int N = 0, W = 0, S = 0;
+  uint16_t* tiles = nullptr;  // device: slices, then per-column exponents
+  int* exps = nullptr;
+};
+
+// digit width W and count S for contraction length K (exact FP32 sums of the
+// leading three digit groups need 3 * 2^{2W-2} * K <= 2^24); UNSUPPORTED for
+// K beyond that
+int pick_digits(int K, int* W, int* S);
+int matrix_create(const double* M_host, int N, Matrix* out);
+void matrix_destroy(Matrix* m);
+// device scratch one contraction of `nlines` lines needs (256-byte aligned)
+size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx);
+// out = in . M along lines of a (outer, N, inner) array (in != out)
+int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int64_t inner, int cplx,
+             void* work, size_t work_bytes, cudaStream_t stream);
+
+}  // namespace oz
+}  // namespace sgpu

@@ -167,15 +167,23 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
       br[q] = cosl(a);
       bi[q] = sinl(a);
     }
+    // m-th roots of unity once (long double), indexed by q s mod m
+    std::vector<ld_t> wr(m), wi(m);
+    for (int e = 0; e < m; ++e) {
+      const ld_t a = -2 * kPi * (ld_t)e / (ld_t)m;
+      wr[e] = cosl(a);
+      wi[e] = sinl(a);
+    }
     rk.resize(m);
     for (int s = 0; s < m; ++s) {
       ld_t sr = 0, si = 0;
+      int e = 0;  // q * s mod m
       for (int q = 0; q < m; ++q) {
-        long long e = (long long)q * s % m;
-        ld_t a = -2 * kPi * (ld_t)e / (ld_t)m;
-        ld_t c = cosl(a), sn = sinl(a);
+        const ld_t c = wr[e], sn = wi[e];
         sr += br[q] * c - bi[q] * sn;
         si += br[q] * sn + bi[q] * c;
+        e += s;
+        if (e >= m) e -= m;
       }
       rk[s] = cx<double>((double)(sr / m), (double)(si / m));
       T.rk_f.push_back(cx<df>(ld_to_df(sr / m), ld_to_df(si / m)));

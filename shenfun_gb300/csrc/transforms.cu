@@ -1,10 +1,11 @@
-// Transform plans and the line-transform kernel (C ABI: sgpu_plan_*).
+// Transform plans (C ABI: sgpu_plan_*); the kernels are in xf_*.cu.
 #include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "plan_host.cuh"
+#include "xf_kernels.cuh"
 
 using namespace sgpu;
 
@@ -53,15 +54,6 @@ extern "C" int sgpu_plan_destroy(sgpu_plan* plan) {
   return SGPU_OK;
 }
 
-template <class R>
-__global__ void __launch_bounds__(256) sgpu_line_kernel(LinePlan p, const double* in, double* out,
-                                                        int data_complex, int64_t nlines,
-                                                        int64_t inner, double scl) {
-  extern __shared__ __align__(16) unsigned char sgpu_smem[];
-  prog_dispatch<R>(p, in, out, data_complex, nlines, inner, scl, (int64_t)blockIdx.x, sgpu_smem,
-                   (int)threadIdx.x, (int)blockDim.x);
-}
-
 extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
                                  int64_t inner, int data_kind, double scale, cudaStream_t stream) {
   if (!plan || !in || !out) return SGPU_ERR_ARG;
@@ -74,24 +66,15 @@ extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* ou
   const int lpb = lines_per_block(p, data_complex_for(p, data_kind));
   const int64_t nblocks = (nlines + lpb - 1) / lpb;
   if (nblocks > 0x7fffffffLL) return SGPU_ERR_ARG;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(sgpu_line_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024) != cudaSuccess ||
-        cudaFuncSetAttribute(sgpu_line_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024) != cudaSuccess) {
-      cudaGetLastError();
-      return SGPU_ERR_CUDA;
-    }
-    attr_set = true;
-  }
   const int dc = data_complex_for(p, data_kind);
+  const int G = xf_group(p.kind);
+  const bool fourier = G == XF_G_R2C || G == XF_G_C2R || G == XF_G_C2C;
+  const double* src = (const double*)in;
+  double* dst = (double*)out;
+  const unsigned nb = (unsigned)nblocks;
   if (p.form == SGPU_MIXED_DF)
-    sgpu_line_kernel<df><<<(unsigned)nblocks, p.nthreads, p.smem, stream>>>(
-        p, (const double*)in, (double*)out, dc, nlines, inner, scale);
-  else
-    sgpu_line_kernel<double><<<(unsigned)nblocks, p.nthreads, p.smem, stream>>>(
-        p, (const double*)in, (double*)out, dc, nlines, inner, scale);
-  if (cudaGetLastError() != cudaSuccess) return SGPU_ERR_CUDA;
-  return SGPU_OK;
+    return fourier ? xf_launch_fourier_df(G, p, src, dst, dc, nlines, inner, scale, nb, stream)
+                   : xf_launch_cheb_df(G, p, src, dst, dc, nlines, inner, scale, nb, stream);
+  return fourier ? xf_launch_fourier_f64(G, p, src, dst, dc, nlines, inner, scale, nb, stream)
+                 : xf_launch_cheb_f64(G, p, src, dst, dc, nlines, inner, scale, nb, stream);
 }

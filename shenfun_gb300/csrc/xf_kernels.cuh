@@ -1,0 +1,74 @@
+// The line-transform kernel, one instantiation per (arithmetic, program
+// group), so that each compiles as a separate, smaller function and the two
+// arithmetic forms and two program families build in parallel translation
+// units (xf_fourier_f64.cu, xf_fourier_df.cu, xf_cheb_f64.cu, xf_cheb_df.cu).
+//   G = 0 R2C, 1 C2R, 2 C2C, 3 DCT-II family (DCT2, Chebyshev scalar
+//   product, forward), 4 DCT-III family (DCT3, Chebyshev backward)
+#pragma once
+
+#include "fft_line.cuh"
+
+namespace sgpu {
+
+enum { XF_G_R2C = 0, XF_G_C2R = 1, XF_G_C2C = 2, XF_G_DCT2 = 3, XF_G_DCT3 = 4 };
+
+inline int xf_group(int kind) {
+  switch (kind) {
+    case SGPU_XF_R2C: return XF_G_R2C;
+    case SGPU_XF_C2R: return XF_G_C2R;
+    case SGPU_XF_C2C_FWD:
+    case SGPU_XF_C2C_BWD: return XF_G_C2C;
+    case SGPU_XF_DCT3:
+    case SGPU_XF_CHEB_BACKWARD: return XF_G_DCT3;
+    default: return XF_G_DCT2;
+  }
+}
+
+#ifdef __CUDACC__
+template <class R, int G>
+__global__ void __launch_bounds__(256) sgpu_line_kernel(LinePlan p, const double* in, double* out,
+                                                        int data_complex, int64_t nlines,
+                                                        int64_t inner, double scl) {
+  extern __shared__ __align__(16) unsigned char sgpu_smem[];
+  const int64_t blk = (int64_t)blockIdx.x;
+  const int tid = (int)threadIdx.x, nth = (int)blockDim.x;
+  if (G == XF_G_R2C)
+    prog_r2c<R>(p, in, out, nlines, inner, scl, blk, sgpu_smem, tid, nth);
+  else if (G == XF_G_C2R)
+    prog_c2r<R>(p, in, out, nlines, inner, scl, blk, sgpu_smem, tid, nth);
+  else if (G == XF_G_C2C)
+    prog_c2c<R>(p, in, out, nlines, inner, scl, blk, sgpu_smem, tid, nth);
+  else if (G == XF_G_DCT2)
+    prog_dct2<R>(p, in, out, data_complex, nlines, inner, scl, blk, sgpu_smem, tid, nth);
+  else
+    prog_dct3<R>(p, in, out, data_complex, nlines, inner, scl, blk, sgpu_smem, tid, nth);
+}
+
+template <class R, int G>
+int xf_launch_group(const LinePlan& p, const double* in, double* out, int dc, int64_t nlines,
+                    int64_t inner, double scl, unsigned nblocks, cudaStream_t stream) {
+  static bool attr_set = false;  // benign race: every caller sets the same value
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(sgpu_line_kernel<R, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024) != cudaSuccess) {
+      cudaGetLastError();
+      return SGPU_ERR_CUDA;
+    }
+    attr_set = true;
+  }
+  sgpu_line_kernel<R, G><<<nblocks, p.nthreads, p.smem, stream>>>(p, in, out, dc, nlines, inner, scl);
+  return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
+}
+#endif
+
+// per-TU launchers (group G of the family)
+int xf_launch_fourier_f64(int G, const LinePlan& p, const double* in, double* out, int dc,
+                          int64_t nlines, int64_t inner, double scl, unsigned nblocks, cudaStream_t s);
+int xf_launch_fourier_df(int G, const LinePlan& p, const double* in, double* out, int dc,
+                         int64_t nlines, int64_t inner, double scl, unsigned nblocks, cudaStream_t s);
+int xf_launch_cheb_f64(int G, const LinePlan& p, const double* in, double* out, int dc,
+                       int64_t nlines, int64_t inner, double scl, unsigned nblocks, cudaStream_t s);
+int xf_launch_cheb_df(int G, const LinePlan& p, const double* in, double* out, int dc,
+                      int64_t nlines, int64_t inner, double scl, unsigned nblocks, cudaStream_t s);
+
+}  // namespace sgpu

@@ -1,9 +1,10 @@
 """Legendre spaces with Gauss-Legendre quadrature on the GPU path
 (legendre/bases.py:76-572 of the reference).
 
-Transforms are dense contractions (``sgpu_legendre_execute``) with the Shen
-stencil folded into the matrix; the nodes and weights come from the library's
-host routine ``sgpu_leggauss``.  ``kind='vandermonde'`` zeroes the tail rows of
+Transforms are dense contractions (``sgpu_legendre_execute_ws``) with the
+Shen stencil folded into the matrix; the nodes and weights come from the
+library's host routine ``sgpu_leggauss``.  ``form='mixed'`` runs them on the
+tensor cores with BF16 digit slices (about 48 bits, N <= 1024).  ``kind='vandermonde'`` zeroes the tail rows of
 the composite scalar product (spectralbase.py:1466-1469); the default
 ('recursive', the reference's default for Legendre) keeps the orthogonal
 coefficients there, as the reference's stencil product does.
@@ -11,6 +12,7 @@ coefficients there, as the reference's stencil product does.
 import ctypes
 
 import numpy as np
+import torch
 
 from . import _lib
 from .device import require_cuda, ptr, stream_handle, view3, data_kind
@@ -41,10 +43,20 @@ class _Plan:
         except Exception:
             pass
 
-    def __call__(self, direction, inp, out, axis, stream=None):
+    def workspace_bytes(self, outer, inner, kind):
+        nb = ctypes.c_size_t()
+        _lib.call("sgpu_legendre_workspace_size", self._h, outer, inner, kind, ctypes.byref(nb))
+        return int(nb.value)
+
+    def __call__(self, direction, inp, out, axis, stream=None, work=None):
         outer, n, inner = view3(tuple(inp.shape), axis)
-        _lib.call("sgpu_legendre_execute", self._h, direction, ptr(inp), ptr(out), outer, inner,
-                  data_kind(inp), stream_handle(stream))
+        kind = data_kind(inp)
+        nb = self.workspace_bytes(outer, inner, kind)
+        if nb and (work is None or work.numel() < nb):
+            # torch's caching allocator: 512-byte aligned, reused across calls
+            work = torch.empty(nb, dtype=torch.uint8, device=inp.device)
+        _lib.call("sgpu_legendre_execute_ws", self._h, direction, ptr(inp), ptr(out), outer, inner,
+                  kind, work.data_ptr() if nb else None, nb, stream_handle(stream))
         return out
 
 
@@ -68,6 +80,8 @@ class LegendreBase(SpectralBase):
             raise NotImplementedError("only Legendre-Gauss quadrature is on the GPU path")
         SpectralBase.__init__(self, N, dtype)
         self.domain = Domain(domain)
+        if kw.get("form") is not None:
+            self.form = _lib.FORMS[kw["form"]]
 
     def domain_factor(self):
         a, b = self.domain
@@ -95,7 +109,7 @@ class LegendreBase(SpectralBase):
         out = self._out(input_array, True, output_array, ax)
         if out.data_ptr() == input_array.data_ptr():
             raise _lib.SgpuError(_lib.ERR_ARG, "Legendre transforms cannot run in place")
-        get_plan(self.N, self.basis_id)(direction, input_array, out, ax)
+        get_plan(self.N, self.basis_id, self.form)(direction, input_array, out, ax)
         if direction == 0 and kind == "vandermonde" and self.num_bcs():
             out.narrow(ax % out.dim(), self.dim(), self.num_bcs()).zero_()
         return out

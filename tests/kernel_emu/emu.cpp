@@ -11,6 +11,7 @@
 //   emu hsolve N outer inner data_kind b.bin fac.bin out.bin   (fac = d0|d1|d2|L)
 //   emu hmatvec N outer inner data_kind v.bin alfa.bin beta.bin out.bin
 //   emu tdma|pdma n outer inner data_kind raw.bin u.bin out.bin (LU then solve)
+//   emu ozaki  N nlines inner cplx W in.bin M.bin out.bin     (split-BF16 contraction)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -21,6 +22,7 @@
 
 #include "../../shenfun_gb300/csrc/plan_host.cuh"
 #include "../../shenfun_gb300/csrc/solvers.cuh"
+#include "../../shenfun_gb300/csrc/ozaki.cuh"
 
 using namespace sgpu;
 
@@ -100,10 +102,122 @@ static int xform(int argc, char** argv) {
   return 0;
 }
 
+// Split-BF16 tensor-core contraction: the row-exponent, split and epilogue
+// block functions run as in the kernels; the bulk copies are memcpy's with
+// the kernel's offsets into an exactly-sized stand-in for shared memory, and
+// each tcgen05.mma is modelled from its descriptors (operand element (m, k)
+// at start + (k/8) LBO + (m/8) SBO + 16 (m%8) + 2 (k%8)) with the FP32
+// accumulator rounded once per instruction.
+template <int W, int S>
+static int ozaki_run(const oz::Geom& g, const double* in, const double* M, double* out) {
+  using namespace oz;
+  std::vector<int> eA((size_t)g.mtiles * BM);
+  for (int64_t row = 0; row < (int64_t)g.mtiles * BM; ++row)
+    eA[row] = exp_from_field(rowexp_partial(in, g, row, 0, 1));
+  const size_t at_elems = (size_t)S * g.mtiles * g.nkb * A_ELEMS;
+  uint16_t* At = (uint16_t*)malloc(at_elems * 2);
+  for (size_t i = 0; i < at_elems; ++i) At[i] = 0x7FC0;  // BF16 NaN: unwritten shows
+  for (int64_t t = 0; t < (int64_t)g.mtiles * g.nkb * 4 * BM; ++t) split_thread<W, S>(in, eA.data(), At, g, t);
+  const size_t bt_elems = matrix_tile_elems(g.N, S);
+  uint16_t* Bt = (uint16_t*)malloc(bt_elems * 2);
+  int* eB = (int*)malloc(sizeof(int) * (size_t)g.ntiles * BN);
+  split_matrix_host<W, S>(M, g.N, Bt, eB);
+  const size_t stage_bytes = (size_t)S * (A_BYTES + B_BYTES);
+  uint8_t* smem = (uint8_t*)malloc(STAGES * stage_bytes);
+  std::vector<float> acc((size_t)NACC * BM * BN);
+  const uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
+  if (((idesc >> 17) & 63) * 8 != BN || ((idesc >> 24) & 31) * 16 != BM) return 5;
+  auto bf = [](const uint8_t* p) {
+    uint16_t h;
+    memcpy(&h, p, 2);
+    uint32_t u = (uint32_t)h << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+  };
+  for (int mt = 0; mt < g.mtiles; ++mt)
+    for (int nt = 0; nt < g.ntiles; ++nt) {
+      uint32_t inited = 0;
+      for (int kb = 0; kb < g.nkb; ++kb) {
+        const int st = kb % STAGES;
+        uint8_t* sbase = smem + st * stage_bytes;
+        for (int s = 0; s < S; ++s) {
+          memcpy(sbase + (size_t)s * A_BYTES, At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS,
+                 A_BYTES);
+          memcpy(sbase + (size_t)S * A_BYTES + (size_t)s * B_BYTES,
+                 Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * B_ELEMS, B_BYTES);
+        }
+        for (int ks = 0; ks < BK / 16; ++ks)
+          for (int s = 0; s < S; ++s)
+            for (int t = 0; t + s < S; ++t) {
+              const uint32_t a_off = (uint32_t)(st * stage_bytes + s * A_BYTES + ks * 2 * LBO_A);
+              const uint32_t b_off = (uint32_t)(st * stage_bytes + S * A_BYTES + t * B_BYTES + ks * 2 * LBO_B);
+              const uint64_t ad = tc::sdesc_interleave(a_off, LBO_A, SBO);
+              const uint64_t bd = tc::sdesc_interleave(b_off, LBO_B, SBO);
+              auto field = [](uint64_t d, int sh) { return (uint32_t)(((d >> sh) & 0x3FFF) << 4); };
+              const uint32_t as = field(ad, 0), al = field(ad, 16), asb = field(ad, 32);
+              const uint32_t bs = field(bd, 0), bl = field(bd, 16), bsb = field(bd, 32);
+              const int a = s + t < NACC - 1 ? s + t : NACC - 1;
+              for (int m = 0; m < BM; ++m)
+                for (int n = 0; n < BN; ++n) {
+                  double sum = 0;
+                  for (int k = 0; k < 16; ++k) {
+                    const uint32_t pa = as + (k >> 3) * al + (m >> 3) * asb + (m & 7) * 16 + (k & 7) * 2;
+                    const uint32_t pb = bs + (k >> 3) * bl + (n >> 3) * bsb + (n & 7) * 16 + (k & 7) * 2;
+                    if (pa + 2 > STAGES * stage_bytes || pb + 2 > STAGES * stage_bytes) return 6;
+                    sum += (double)bf(smem + pa) * (double)bf(smem + pb);
+                  }
+                  float& d = acc[((size_t)a * BM + m) * BN + n];
+                  d = (float)(((inited >> a) & 1 ? (double)d : 0.0) + sum);
+                }
+              inited |= 1u << a;
+            }
+      }
+      for (int m = 0; m < BM; ++m) {
+        const int64_t row = (int64_t)mt * BM + m;
+        if (row >= g.nrows) continue;
+        for (int n = 0; n < BN; ++n) {
+          const int col = nt * BN + n;
+          if (col >= g.N) continue;
+          uint32_t gb[NACC];
+          for (int a = 0; a < NACC; ++a) memcpy(&gb[a], &acc[((size_t)a * BM + m) * BN + n], 4);
+          out[row_offset(g, row, col)] = combine_groups(gb, eA[row] - 2 * W + eB[col]);
+        }
+      }
+    }
+  free(At);
+  free(Bt);
+  free(eB);
+  free(smem);
+  return 0;
+}
+
+// emu ozaki N nlines inner cplx W in.bin M.bin out.bin
+static int ozaki(int argc, char** argv) {
+  if (argc < 10) return 2;
+  const int N = atoi(argv[2]);
+  const long long nlines = atoll(argv[3]), inner = atoll(argv[4]);
+  const int cplx = atoi(argv[5]), W = atoi(argv[6]);
+  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx);
+  const size_t cnt = (size_t)nlines * N * (1 + cplx);
+  double* in = read_exact(argv[7], cnt);
+  double* M = read_exact(argv[8], (size_t)N * N);
+  double* out = (double*)malloc(sizeof(double) * cnt);
+  for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
+  const int rc = W == 7 ? ozaki_run<7, 7>(g, in, M, out) : ozaki_run<6, 7>(g, in, M, out);
+  if (rc) return rc;
+  write_exact(argv[9], out, cnt);
+  free(in);
+  free(M);
+  free(out);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   std::string mode = argv[1];
   if (mode == "xform") return xform(argc, argv);
+  if (mode == "ozaki") return ozaki(argc, argv);
   if (mode == "lkcheck") {
     // lkcheck: every (line, index) pair of the loop decompositions is visited
     // exactly once for the thread counts the kernels launch with
