@@ -117,7 +117,7 @@ struct sgpu_legendre_plan {
   double* d_mass;    // LU'd mass bands (reciprocal diagonal), forward transform
   double* d_nodes;   // x, w (2N)
   std::vector<double> x, w;
-  oz::Matrix tc_scalar, tc_back;  // mixed form: split Ms, Mb
+  oz::Matrix tc_scalar, tc_forward, tc_back;  // mixed form: split Ms (7 and 8 digits), Mb
 };
 
 extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int basis, int form) {
@@ -127,8 +127,7 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
   if (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SB) return SGPU_ERR_ARG;
   if (form != SGPU_PLAIN_F64 && form != SGPU_MIXED_DF) return SGPU_ERR_UNSUPPORTED;
   if (form == SGPU_MIXED_DF) {
-    int W, S;
-    if (oz::pick_digits(N, &W, &S) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
+    if (oz::pick_digits(N) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
   }
   if (basis == SGPU_BASIS_SD && N < 4) return SGPU_ERR_ARG;
   if (basis == SGPU_BASIS_SB && N < 8) return SGPU_ERR_ARG;
@@ -226,10 +225,15 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
     return SGPU_ERR_CUDA;
   }
   if (form == SGPU_MIXED_DF) {
-    int st = oz::matrix_create(Ms.data(), N, &p->tc_scalar);
-    if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, &p->tc_back);
+    // the forward transform divides the scalar product by the mass matrix,
+    // which magnifies its normwise error ~N-fold in the high modes: it uses
+    // the 8-digit split
+    int st = oz::matrix_create(Ms.data(), N, 0, &p->tc_scalar);
+    if (st == SGPU_OK) st = oz::matrix_create(Ms.data(), N, 1, &p->tc_forward);
+    if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, 0, &p->tc_back);
     if (st != SGPU_OK) {
       oz::matrix_destroy(&p->tc_scalar);
+      oz::matrix_destroy(&p->tc_forward);
       oz::matrix_destroy(&p->tc_back);
       cudaFree(dev);
       delete p;
@@ -244,6 +248,7 @@ extern "C" int sgpu_legendre_plan_destroy(sgpu_legendre_plan* p) {
   if (!p) return SGPU_OK;
   cudaFree(p->d_scalar);
   oz::matrix_destroy(&p->tc_scalar);
+  oz::matrix_destroy(&p->tc_forward);
   oz::matrix_destroy(&p->tc_back);
   delete p;
   return SGPU_OK;
@@ -376,7 +381,7 @@ static int legendre_run(const sgpu_legendre_plan* p, int direction, const void* 
   if (nlines == 0) return SGPU_OK;
   const int cplx = data_kind == SGPU_COMPLEX;
   if (p->form == SGPU_MIXED_DF) {
-    const oz::Matrix& M = direction == 2 ? p->tc_back : p->tc_scalar;
+    const oz::Matrix& M = direction == 2 ? p->tc_back : (direction == 1 ? p->tc_forward : p->tc_scalar);
     const int st = oz::contract(M, (const double*)in, (double*)out, nlines, inner, cplx, work, work_bytes, stream);
     if (st != SGPU_OK) return st;
   } else {
@@ -400,9 +405,14 @@ extern "C" int sgpu_legendre_workspace_size(const sgpu_legendre_plan* p, int64_t
                                             int data_kind, size_t* bytes) {
   if (!p || !bytes || outer < 0 || inner < 1) return SGPU_ERR_ARG;
   if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
-  *bytes = p->form == SGPU_MIXED_DF
-               ? oz::workspace_bytes(p->tc_scalar, outer * inner, inner, data_kind == SGPU_COMPLEX)
-               : 0;
+  if (p->form != SGPU_MIXED_DF) {
+    *bytes = 0;
+    return SGPU_OK;
+  }
+  const int c = data_kind == SGPU_COMPLEX;
+  const size_t a = oz::workspace_bytes(p->tc_scalar, outer * inner, inner, c);
+  const size_t b = oz::workspace_bytes(p->tc_forward, outer * inner, inner, c);
+  *bytes = a > b ? a : b;
   return SGPU_OK;
 }
 

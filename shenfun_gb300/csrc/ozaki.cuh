@@ -40,17 +40,31 @@ namespace sgpu {
 namespace oz {
 
 const int BM = 128;       // rows (lines) per tile = MMA M
-const int BN = 96;        // output columns per tile = MMA N (NACC * BN <= 512 TMEM columns)
 const int BK = 32;        // K per pipeline stage
 const int STAGES = 2;
-const int NACC = 5;       // accumulators: digit groups 0..3 exact, >= 4 combined
+const int W = 7;          // bits per digit
 const int A_ELEMS = BM * BK;            // 4096 bf16 = 8 KB per A slice block
-const int B_ELEMS = BN * BK;            // 3072 bf16 = 6 KB per B slice block
 const int A_BYTES = A_ELEMS * 2;
-const int B_BYTES = B_ELEMS * 2;
 const int LBO_A = BM * 16;              // K-direction core-matrix stride (bytes)
-const int LBO_B = BN * 16;
 const int SBO = 128;                    // row-direction core-matrix stride (bytes)
+
+// A digit configuration: S digits per operand, products with s + t <= S - 1,
+// NACC FP32 accumulators (groups 0..NACC-2 separately, the rest combined) and
+// BN output columns per tile (NACC * BN <= 512 TMEM columns).
+template <int S_, int NACC_, int BN_>
+struct Cfg {
+  static const int S = S_, NACC = NACC_, BN = BN_;
+  static const int B_ELEMS = BN * BK, B_BYTES = B_ELEMS * 2;
+  static const int LBO_B = BN * 16;
+  static const int NPROD = S * (S + 1) / 2;
+  static_assert(NACC * BN <= 512, "accumulators exceed TMEM");
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "MMA N");
+};
+// 7 digits (48 bits), 28 products, groups 0..3 exact: normwise ~1e-13
+typedef Cfg<7, 5, 96> CfgStd;
+// 8 digits (55 bits), 36 products, groups 0..4 exact: ~1e-15, for outputs that
+// a later step divides by small numbers (the forward transform's mass solve)
+typedef Cfg<8, 6, 80> CfgAcc;
 
 // index of element (row r, k in the K block) inside a block of `rows` rows:
 // [k / 8][r / 8][r % 8][k % 8]
@@ -79,8 +93,13 @@ SGPU_HD void split_digits(double x, int e, uint16_t (&out)[S]) {
   int64_t X = 0;
   if (field != 0) {
     const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1075 + e - W * S - field;  // >= 54 - W*S > 0 since |x| < 2^{e-1}
-    if (sh < 64) X = (int64_t)((m + (1ull << (sh - 1))) >> sh);
+    // X = round(|x| 2^{WS-e}) = round(m 2^{-sh}); sh >= 54 - W*S since
+    // |x| < 2^{e-1} (>= 12 for 6 digits, >= -2 for 8), and X < 2^{WS-1}
+    const int sh = 1075 + e - W * S - field;
+    if (sh <= 0)
+      X = (int64_t)(m << (-sh));
+    else if (sh < 64)
+      X = (int64_t)((m + (1ull << (sh - 1))) >> sh);
   }
   const bool neg = (b >> 63) != 0;
 #pragma unroll
@@ -162,8 +181,9 @@ SGPU_HD double fixed_to_double(int64_t T, int E) {
 }
 
 // one output element from the NACC FP32 accumulators (bit patterns) of the
-// digit groups; E = eA + eB - 2W (|G| <= 2^24 each, so the 2^-36 fixed
-// point stays below 2^63)
+// digit groups; E = eA + eB - 2W.  |G_g| <= (g+1) 2^{2W-2} K, so for
+// K <= 1024 the 2^-36 fixed-point sum stays below 21 * 2^58 < 2^63.
+template <int NACC>
 SGPU_HD double combine_groups(const uint32_t (&gb)[NACC], int E) {
   int64_t T = 0;
   for (int i = 0; i < NACC; ++i) T += f32_fixed(gb[i], 36);
@@ -195,7 +215,7 @@ inline size_t a_split_bytes(const Geom& g, int S) {
   return (size_t)S * g.mtiles * g.nkb * A_BYTES + (size_t)g.mtiles * BM * sizeof(int);
 }
 
-inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx) {
+inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx, int BN) {
   Geom g;
   g.N = N;
   g.inner = inner;
@@ -221,7 +241,7 @@ SGPU_HD uint32_t rowexp_partial(const double* in, const Geom& g, int64_t row, in
 
 // split thread t: (row rr of tile mt, 8-wide chunk kc of K) -> S 16-byte
 // stores, one per slice block.  t < mtiles * nkb * 4 * BM.
-template <int W, int S>
+template <int S>
 SGPU_HD void split_thread(const double* in, const int* eA, uint16_t* At, const Geom& g, int64_t t) {
   const int64_t nk = (int64_t)g.nkb * 4;
   const int rr = (int)(t & (BM - 1));
@@ -247,9 +267,10 @@ SGPU_HD void split_thread(const double* in, const int* eA, uint16_t* At, const G
 }
 
 // host: split a fixed N x N matrix M (out = in . M, so output column n is
-// M[:, n]) into tiled slices [S][ntiles][nkb][8 KB] and per-column exponents
-template <int W, int S>
+// M[:, n]) into tiled slices [S][ntiles][nkb][BN x BK] and per-column exponents
+template <class C>
 void split_matrix_host(const double* M, int N, uint16_t* tiles, int* ex) {
+  const int S = C::S, BN = C::BN, B_ELEMS = C::B_ELEMS;
   const int nkb = (N + BK - 1) / BK, ntiles = (N + BN - 1) / BN;
   memset(tiles, 0, sizeof(uint16_t) * (size_t)S * ntiles * nkb * B_ELEMS);
   memset(ex, 0, sizeof(int) * (size_t)ntiles * BN);
@@ -262,16 +283,17 @@ void split_matrix_host(const double* M, int N, uint16_t* tiles, int* ex) {
     ex[n] = exp_from_field(mf);
     const int nt = n / BN, r = n % BN;
     for (int k = 0; k < N; ++k) {
-      uint16_t d[S];
-      split_digits<W, S>(M[(size_t)k * N + n], ex[n], d);
+      uint16_t d[C::S];
+      split_digits<W, C::S>(M[(size_t)k * N + n], ex[n], d);
       for (int s = 0; s < S; ++s)
         tiles[(((size_t)s * ntiles + nt) * nkb + k / BK) * B_ELEMS + tile_index(BN, r, k % BK)] = d[s];
     }
   }
 }
 
-inline size_t matrix_tile_elems(int N, int S) {
-  return (size_t)S * ((N + BN - 1) / BN) * ((N + BK - 1) / BK) * B_ELEMS;
+template <class C>
+inline size_t matrix_tile_elems(int N) {
+  return (size_t)C::S * ((N + C::BN - 1) / C::BN) * ((N + BK - 1) / BK) * C::B_ELEMS;
 }
 
 }  // namespace oz

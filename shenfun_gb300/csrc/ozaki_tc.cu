@@ -3,9 +3,9 @@
 //   k_oz_rowexp   one warp per row: the row's power-of-two scale
 //   k_oz_split    one thread per (row, 8-wide K chunk): S digit slices written
 //                 pre-tiled (16-byte stores, coalesced along rows)
-//   k_oz_gemm     one CTA per 128 x 96 output tile: a producer thread streams
+//   k_oz_gemm     one CTA per 128 x BN output tile: a producer thread streams
 //                 2S slice blocks per K stage with bulk copies, one thread
-//                 issues tcgen05.mma for the S(S+1)/2 slice products into five
+//                 issues tcgen05.mma for the S(S+1)/2 slice products into NACC
 //                 TMEM accumulators, and all four warps run the integer
 //                 epilogue (TMEM -> registers -> FP64 bits -> global).
 // The split matrix operand (B) is built once on the host with the same digit
@@ -32,34 +32,36 @@ __global__ void __launch_bounds__(256) k_oz_rowexp(const double* __restrict__ in
   if ((threadIdx.x & 31) == 0) eA[warp] = exp_from_field(mf);
 }
 
-template <int W, int S>
+template <int S>
 __global__ void __launch_bounds__(256) k_oz_split(const double* __restrict__ in, const int* __restrict__ eA,
                                                   uint16_t* __restrict__ At, Geom g) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)g.mtiles * g.nkb * 4 * BM) return;
-  split_thread<W, S>(in, eA, At, g, t);
+  split_thread<S>(in, eA, At, g, t);
 }
 
 // shared memory: STAGES x (S blocks of A, S blocks of B), then the barriers
-template <int S>
+template <class C>
 struct GemmSmem {
-  static const size_t stage_bytes = (size_t)S * (A_BYTES + B_BYTES);
+  static const size_t stage_bytes = (size_t)C::S * (A_BYTES + C::B_BYTES);
   static const size_t bar_off = STAGES * stage_bytes;
   // barriers + alignment slack, rounded up to the 227 KB per-CTA maximum so
   // that every descriptor-addressed operand read stays inside the allocation
   static const size_t need = bar_off + 256 + 1024;
   static const size_t bytes = need < 232448 ? 232448 : need;
 };
-static_assert(GemmSmem<7>::need <= 232448, "stages exceed shared memory");
+static_assert(GemmSmem<CfgStd>::need <= 232448, "stages exceed shared memory");
+static_assert(GemmSmem<CfgAcc>::need <= 232448, "stages exceed shared memory");
 
-template <int W, int S>
+template <class C>
 __global__ void __launch_bounds__(128, 1)
     k_oz_gemm(const uint16_t* __restrict__ At, const int* __restrict__ eA, const uint16_t* __restrict__ Bt,
               const int* __restrict__ eB, double* __restrict__ out, Geom g) {
+  constexpr int S = C::S, NACC = C::NACC, BN = C::BN;
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte aligned base
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + GemmSmem<S>::bar_off);
+  uint64_t* full = (uint64_t*)(smem + GemmSmem<C>::bar_off);
   uint64_t* empty = full + STAGES;
   uint64_t* accf = empty + STAGES;
   uint32_t* tmem_holder = (uint32_t*)(accf + 1);
@@ -84,9 +86,9 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t tmem = *tmem_holder;
   bool ok = true;
 
-  auto sA = [&](int st, int s) { return smem + (size_t)st * GemmSmem<S>::stage_bytes + (size_t)s * A_BYTES; };
+  auto sA = [&](int st, int s) { return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)s * A_BYTES; };
   auto sB = [&](int st, int s) {
-    return smem + (size_t)st * GemmSmem<S>::stage_bytes + (size_t)S * A_BYTES + (size_t)s * B_BYTES;
+    return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)S * A_BYTES + (size_t)s * C::B_BYTES;
   };
 
   if (warp == 0 && lane == 0) {
@@ -99,10 +101,11 @@ __global__ void __launch_bounds__(128, 1)
         ok = false;
         break;
       }
-      tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (A_BYTES + B_BYTES)));
+      tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (A_BYTES + C::B_BYTES)));
       for (int s = 0; s < S; ++s) {
         tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS, A_BYTES, &full[st]);
-        tc::bulk_g2s(sB(st, s), Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * B_ELEMS, B_BYTES, &full[st]);
+        tc::bulk_g2s(sB(st, s), Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS, C::B_BYTES,
+                     &full[st]);
       }
     }
     // drain: every copy issued must have landed before the CTA may exit
@@ -129,7 +132,8 @@ __global__ void __launch_bounds__(128, 1)
           const uint64_t ad = tc::sdesc_interleave(tc::smem_u32(sA(st, s)) + ks * 2 * LBO_A, LBO_A, SBO);
 #pragma unroll
           for (int t = 0; t + s < S; ++t) {
-            const uint64_t bd = tc::sdesc_interleave(tc::smem_u32(sB(st, t)) + ks * 2 * LBO_B, LBO_B, SBO);
+            const uint64_t bd =
+                tc::sdesc_interleave(tc::smem_u32(sB(st, t)) + ks * 2 * C::LBO_B, C::LBO_B, SBO);
             const int acc = s + t < NACC - 1 ? s + t : NACC - 1;
             tc::mma_f16(tmem + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
             inited |= 1u << acc;
@@ -163,7 +167,7 @@ __global__ void __launch_bounds__(128, 1)
           uint32_t gb[NACC];
 #pragma unroll
           for (int q = 0; q < NACC; ++q) gb[q] = a[q][j];
-          out[row_offset(g, row, col)] = combine_groups(gb, erow + eB[col]);
+          out[row_offset(g, row, col)] = combine_groups<NACC>(gb, erow + eB[col]);
         }
       }
     }
@@ -181,18 +185,13 @@ __global__ void __launch_bounds__(128, 1)
 namespace sgpu {
 namespace oz {
 
-int pick_digits(int K, int* W, int* S) {
-  *W = 7;
-  *S = 7;
-  return K <= 1365 ? SGPU_OK : SGPU_ERR_UNSUPPORTED;
-}
+int pick_digits(int K) { return K >= 1 && K <= 1024 ? SGPU_OK : SGPU_ERR_UNSUPPORTED; }
 
-int matrix_create(const double* M, int N, Matrix* out) {
-  out->N = N;
-  if (pick_digits(N, &out->W, &out->S) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
-  std::vector<uint16_t> tiles(matrix_tile_elems(N, out->S));
-  std::vector<int> ex((size_t)((N + BN - 1) / BN) * BN);
-  split_matrix_host<7, 7>(M, N, tiles.data(), ex.data());
+template <class C>
+static int matrix_create_cfg(const double* M, int N, Matrix* out) {
+  std::vector<uint16_t> tiles(matrix_tile_elems<C>(N));
+  std::vector<int> ex((size_t)((N + C::BN - 1) / C::BN) * C::BN);
+  split_matrix_host<C>(M, N, tiles.data(), ex.data());
   const size_t tb = tiles.size() * sizeof(uint16_t), eb = ex.size() * sizeof(int);
   void* dev = nullptr;
   if (cudaMalloc(&dev, tb + eb) != cudaSuccess) {
@@ -211,43 +210,55 @@ int matrix_create(const double* M, int N, Matrix* out) {
   return SGPU_OK;
 }
 
+int matrix_create(const double* M, int N, int accurate, Matrix* out) {
+  if (pick_digits(N) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
+  out->N = N;
+  out->accurate = accurate ? 1 : 0;
+  out->S = accurate ? CfgAcc::S : CfgStd::S;
+  return accurate ? matrix_create_cfg<CfgAcc>(M, N, out) : matrix_create_cfg<CfgStd>(M, N, out);
+}
+
 void matrix_destroy(Matrix* m) {
   if (m && m->tiles) cudaFree(m->tiles);
   if (m) m->tiles = nullptr;
 }
 
 size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx) {
-  const Geom g = make_geom(m.N, nlines, inner, cplx);
+  const Geom g = make_geom(m.N, nlines, inner, cplx, m.accurate ? CfgAcc::BN : CfgStd::BN);
   return a_split_bytes(g, m.S);
 }
 
-template <int W, int S>
+template <class C>
 static int run(const Matrix& m, const Geom& g, const double* in, double* out, void* work, cudaStream_t stream) {
   static bool attr_set = false;  // benign race: every caller sets the same value
   if (!attr_set) {
-    if (cudaFuncSetAttribute(k_oz_gemm<W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)GemmSmem<S>::bytes) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_oz_gemm<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)GemmSmem<C>::bytes) != cudaSuccess) {
+      cudaGetLastError();
       return SGPU_ERR_CUDA;
+    }
     attr_set = true;
   }
   uint16_t* At = (uint16_t*)work;
-  int* eA = (int*)((char*)work + (size_t)S * g.mtiles * g.nkb * A_BYTES);
+  int* eA = (int*)((char*)work + (size_t)C::S * g.mtiles * g.nkb * A_BYTES);
   const int64_t nrow_pad = (int64_t)g.mtiles * BM;
   k_oz_rowexp<<<(unsigned)((nrow_pad * 32 + 255) / 256), 256, 0, stream>>>(in, eA, g);
   const int64_t nsplit = nrow_pad * g.nkb * 4;
-  k_oz_split<W, S><<<(unsigned)((nsplit + 255) / 256), 256, 0, stream>>>(in, eA, At, g);
+  k_oz_split<C::S><<<(unsigned)((nsplit + 255) / 256), 256, 0, stream>>>(in, eA, At, g);
   dim3 grid((unsigned)g.mtiles, (unsigned)g.ntiles);
-  k_oz_gemm<W, S><<<grid, 128, GemmSmem<S>::bytes, stream>>>(At, eA, m.tiles, m.exps, out, g);
+  k_oz_gemm<C><<<grid, 128, GemmSmem<C>::bytes, stream>>>(At, eA, m.tiles, m.exps, out, g);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
 int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int64_t inner, int cplx,
              void* work, size_t work_bytes, cudaStream_t stream) {
   if (nlines == 0) return SGPU_OK;
-  const Geom g = make_geom(m.N, nlines, inner, cplx);
-  if (g.mtiles > 0x7fffffff || work_bytes < a_split_bytes(g, m.S) || ((uintptr_t)work & 255)) return SGPU_ERR_ARG;
-  if (m.W != 7 || m.S != 7) return SGPU_ERR_UNSUPPORTED;
-  return run<7, 7>(m, g, in, out, work, stream);
+  if (!m.tiles) return SGPU_ERR_ARG;
+  const Geom g = make_geom(m.N, nlines, inner, cplx, m.accurate ? CfgAcc::BN : CfgStd::BN);
+  // grid.x and the split kernel's block count stay below 2^31
+  if ((int64_t)g.mtiles * BM * g.nkb * 4 / 256 > 0x7fffffff) return SGPU_ERR_ARG;
+  if (work_bytes < a_split_bytes(g, m.S) || ((uintptr_t)work & 255)) return SGPU_ERR_ARG;
+  return m.accurate ? run<CfgAcc>(m, g, in, out, work, stream) : run<CfgStd>(m, g, in, out, work, stream);
 }
 
 }  // namespace oz

@@ -12,16 +12,16 @@ namespace oz {
 // a fixed N x N matrix M (row-major, out(l, n) = sum_k in(l, k) M[k][n]),
 // split into BF16 digit slices and tiled on the device
 struct Matrix {
-  int N = 0, W = 0, S = 0;
+  int N = 0, S = 0;
+  int accurate = 0;           // 0: 7 digits (~1e-13 normwise), 1: 8 digits (~1e-15)
   uint16_t* tiles = nullptr;  // device: slices, then per-column exponents
   int* exps = nullptr;
 };
 
-// digit width W and count S for contraction length K (exact FP32 sums of the
-// leading three digit groups need 3 * 2^{2W-2} * K <= 2^24); UNSUPPORTED for
-// K beyond that
-int pick_digits(int K, int* W, int* S);
-int matrix_create(const double* M_host, int N, Matrix* out);
+// OK when the contraction length K keeps the FP32 sums of the exact digit
+// groups below 2^24 (K <= 1024), else UNSUPPORTED
+int pick_digits(int K);
+int matrix_create(const double* M_host, int N, int accurate, Matrix* out);
 void matrix_destroy(Matrix* m);
 // device scratch one contraction of `nlines` lines needs (256-byte aligned)
 size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx);

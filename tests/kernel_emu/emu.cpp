@@ -11,7 +11,7 @@
 //   emu hsolve N outer inner data_kind b.bin fac.bin out.bin   (fac = d0|d1|d2|L)
 //   emu hmatvec N outer inner data_kind v.bin alfa.bin beta.bin out.bin
 //   emu tdma|pdma n outer inner data_kind raw.bin u.bin out.bin (LU then solve)
-//   emu ozaki  N nlines inner cplx W in.bin M.bin out.bin     (split-BF16 contraction)
+//   emu ozaki  N nlines inner cplx accurate in.bin M.bin out.bin (split-BF16 contraction)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -108,20 +108,21 @@ static int xform(int argc, char** argv) {
 // each tcgen05.mma is modelled from its descriptors (operand element (m, k)
 // at start + (k/8) LBO + (m/8) SBO + 16 (m%8) + 2 (k%8)) with the FP32
 // accumulator rounded once per instruction.
-template <int W, int S>
+template <class C>
 static int ozaki_run(const oz::Geom& g, const double* in, const double* M, double* out) {
   using namespace oz;
+  const int S = C::S, NACC = C::NACC, BN = C::BN, B_BYTES = C::B_BYTES, LBO_B = C::LBO_B;
   std::vector<int> eA((size_t)g.mtiles * BM);
   for (int64_t row = 0; row < (int64_t)g.mtiles * BM; ++row)
     eA[row] = exp_from_field(rowexp_partial(in, g, row, 0, 1));
   const size_t at_elems = (size_t)S * g.mtiles * g.nkb * A_ELEMS;
   uint16_t* At = (uint16_t*)malloc(at_elems * 2);
   for (size_t i = 0; i < at_elems; ++i) At[i] = 0x7FC0;  // BF16 NaN: unwritten shows
-  for (int64_t t = 0; t < (int64_t)g.mtiles * g.nkb * 4 * BM; ++t) split_thread<W, S>(in, eA.data(), At, g, t);
-  const size_t bt_elems = matrix_tile_elems(g.N, S);
+  for (int64_t t = 0; t < (int64_t)g.mtiles * g.nkb * 4 * BM; ++t) split_thread<C::S>(in, eA.data(), At, g, t);
+  const size_t bt_elems = matrix_tile_elems<C>(g.N);
   uint16_t* Bt = (uint16_t*)malloc(bt_elems * 2);
   int* eB = (int*)malloc(sizeof(int) * (size_t)g.ntiles * BN);
-  split_matrix_host<W, S>(M, g.N, Bt, eB);
+  split_matrix_host<C>(M, g.N, Bt, eB);
   const size_t stage_bytes = (size_t)S * (A_BYTES + B_BYTES);
   uint8_t* smem = (uint8_t*)malloc(STAGES * stage_bytes);
   std::vector<float> acc((size_t)NACC * BM * BN);
@@ -145,7 +146,7 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
           memcpy(sbase + (size_t)s * A_BYTES, At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS,
                  A_BYTES);
           memcpy(sbase + (size_t)S * A_BYTES + (size_t)s * B_BYTES,
-                 Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * B_ELEMS, B_BYTES);
+                 Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS, B_BYTES);
         }
         for (int ks = 0; ks < BK / 16; ++ks)
           for (int s = 0; s < S; ++s)
@@ -179,9 +180,9 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
         for (int n = 0; n < BN; ++n) {
           const int col = nt * BN + n;
           if (col >= g.N) continue;
-          uint32_t gb[NACC];
+          uint32_t gb[C::NACC];
           for (int a = 0; a < NACC; ++a) memcpy(&gb[a], &acc[((size_t)a * BM + m) * BN + n], 4);
-          out[row_offset(g, row, col)] = combine_groups(gb, eA[row] - 2 * W + eB[col]);
+          out[row_offset(g, row, col)] = combine_groups<C::NACC>(gb, eA[row] - 2 * W + eB[col]);
         }
       }
     }
@@ -192,19 +193,19 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
   return 0;
 }
 
-// emu ozaki N nlines inner cplx W in.bin M.bin out.bin
+// emu ozaki N nlines inner cplx accurate in.bin M.bin out.bin
 static int ozaki(int argc, char** argv) {
   if (argc < 10) return 2;
   const int N = atoi(argv[2]);
   const long long nlines = atoll(argv[3]), inner = atoll(argv[4]);
-  const int cplx = atoi(argv[5]), W = atoi(argv[6]);
-  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx);
+  const int cplx = atoi(argv[5]), accurate = atoi(argv[6]);
+  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx, accurate ? oz::CfgAcc::BN : oz::CfgStd::BN);
   const size_t cnt = (size_t)nlines * N * (1 + cplx);
   double* in = read_exact(argv[7], cnt);
   double* M = read_exact(argv[8], (size_t)N * N);
   double* out = (double*)malloc(sizeof(double) * cnt);
   for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
-  const int rc = W == 7 ? ozaki_run<7, 7>(g, in, M, out) : ozaki_run<6, 7>(g, in, M, out);
+  const int rc = accurate ? ozaki_run<oz::CfgAcc>(g, in, M, out) : ozaki_run<oz::CfgStd>(g, in, M, out);
   if (rc) return rc;
   write_exact(argv[9], out, cnt);
   free(in);
