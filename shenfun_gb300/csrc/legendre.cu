@@ -108,6 +108,58 @@ void stencil(int basis, int N, std::vector<ld_t>& K2, std::vector<ld_t>& K4) {
   }
 }
 
+// Forward-transform matrix of the mixed form: F = Ms B^{-T}, so that
+// forward(f) = f . F in one contraction (scalar product and mass solve
+// together).  B_kl = sum_m K_km h_m K_lm (k, l < dim) is the mass matrix of
+// the basis (stencil K, h_m = 2 / (2m + 1); legendre/matrices.py:110-192 give
+// the same bands); F[j][k] = (B^{-1} Ms[j, :dim])_k, built in long double
+// with a banded LU (half-bandwidth 2 or 4, B is symmetric positive
+// definite).  Columns k >= dim are zero, as the forward transform leaves them.
+void forward_matrix(int N, int dim, const std::vector<ld_t>& K2, const std::vector<ld_t>& K4,
+                    const std::vector<ld_t>& MsL, std::vector<double>& F) {
+  const int bw = dim == N ? 0 : (dim == N - 2 ? 2 : 4);
+  std::vector<ld_t> h(N);
+  for (int m = 0; m < N; ++m) h[m] = 2.0L / (2 * m + 1);
+  // row k of K: entries at k, k+2, k+4
+  auto kent = [&](int k, int m) -> ld_t {
+    if (m == k) return 1;
+    if (m == k + 2) return K2[k];
+    if (m == k + 4) return K4[k];
+    return 0;
+  };
+  const int W = 2 * bw + 1;
+  std::vector<ld_t> A((size_t)dim * W, 0);  // A[k][bw + (l - k)]
+  for (int k = 0; k < dim; ++k)
+    for (int l = k - bw; l <= k + bw; ++l) {
+      if (l < 0 || l >= dim) continue;
+      ld_t v = 0;
+      for (int m = (k > l ? k : l); m <= (k < l ? k : l) + 4 && m < N; ++m) v += kent(k, m) * h[m] * kent(l, m);
+      A[(size_t)k * W + bw + (l - k)] = v;
+    }
+  // banded LU without pivoting: L unit lower (stored below), U upper
+  for (int k = 0; k < dim; ++k) {
+    const ld_t piv = A[(size_t)k * W + bw];
+    for (int i = k + 1; i <= k + bw && i < dim; ++i) {
+      const ld_t f = A[(size_t)i * W + bw + (k - i)] / piv;
+      A[(size_t)i * W + bw + (k - i)] = f;
+      for (int l = k + 1; l <= k + bw && l < dim; ++l) A[(size_t)i * W + bw + (l - i)] -= f * A[(size_t)k * W + bw + (l - k)];
+    }
+  }
+  F.assign((size_t)N * N, 0.0);
+  std::vector<ld_t> y(dim);
+  for (int j = 0; j < N; ++j) {
+    for (int k = 0; k < dim; ++k) y[k] = MsL[(size_t)j * N + k];
+    for (int i = 0; i < dim; ++i)
+      for (int k = i - bw; k < i; ++k)
+        if (k >= 0) y[i] -= A[(size_t)i * W + bw + (k - i)] * y[k];
+    for (int i = dim - 1; i >= 0; --i) {
+      for (int l = i + 1; l <= i + bw && l < dim; ++l) y[i] -= A[(size_t)i * W + bw + (l - i)] * y[l];
+      y[i] /= A[(size_t)i * W + bw];
+    }
+    for (int k = 0; k < dim; ++k) F[(size_t)j * N + k] = (double)y[k];
+  }
+}
+
 }  // namespace
 
 struct sgpu_legendre_plan {
@@ -117,7 +169,7 @@ struct sgpu_legendre_plan {
   double* d_mass;    // LU'd mass bands (reciprocal diagonal), forward transform
   double* d_nodes;   // x, w (2N)
   std::vector<double> x, w;
-  oz::Matrix tc_scalar, tc_forward, tc_back;  // mixed form: split Ms (7 and 8 digits), Mb
+  oz::Matrix tc_scalar, tc_forward, tc_back;  // mixed form: split Ms, Ms B^{-T}, Mb
 };
 
 extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int basis, int form) {
@@ -146,12 +198,14 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
   const int dim = N - nb;
   // Ms[j][k] = w_j (V_jk + K2_k V_j,k+2 + K4_k V_j,k+4)
   std::vector<double> Ms((size_t)N * N), Mb((size_t)N * N, 0.0);
+  std::vector<ld_t> MsL(form == SGPU_MIXED_DF ? (size_t)N * N : 0);
   for (int j = 0; j < N; ++j)
     for (int k = 0; k < N; ++k) {
       ld_t v = V[(size_t)j * N + k];
       if (k + 2 < N) v += K2[k] * V[(size_t)j * N + k + 2];
       if (k + 4 < N) v += K4[k] * V[(size_t)j * N + k + 4];
       Ms[(size_t)j * N + k] = (double)((ld_t)p->w[j] * v);
+      if (!MsL.empty()) MsL[(size_t)j * N + k] = (ld_t)p->w[j] * v;
     }
   // Mb[k][j] = V_jk + K2_k V_j,k+2 + K4_k V_j,k+4 for k < dim (rows k >= dim zero)
   for (int k = 0; k < dim; ++k)
@@ -225,12 +279,14 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
     return SGPU_ERR_CUDA;
   }
   if (form == SGPU_MIXED_DF) {
-    // the forward transform divides the scalar product by the mass matrix,
-    // which magnifies its normwise error ~N-fold in the high modes: it uses
-    // the 8-digit split
-    int st = oz::matrix_create(Ms.data(), N, 0, &p->tc_scalar);
-    if (st == SGPU_OK) st = oz::matrix_create(Ms.data(), N, 1, &p->tc_forward);
-    if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, 0, &p->tc_back);
+    // the forward transform contracts with F = Ms B^{-T} directly: a scalar
+    // product followed by the mass solve would magnify the scalar product's
+    // normwise error ~N-fold in the high modes
+    std::vector<double> F;
+    forward_matrix(N, dim, K2, K4, MsL, F);
+    int st = oz::matrix_create(Ms.data(), N, &p->tc_scalar);
+    if (st == SGPU_OK) st = oz::matrix_create(F.data(), N, &p->tc_forward);
+    if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, &p->tc_back);
     if (st != SGPU_OK) {
       oz::matrix_destroy(&p->tc_scalar);
       oz::matrix_destroy(&p->tc_forward);
@@ -391,7 +447,7 @@ static int legendre_run(const sgpu_legendre_plan* p, int direction, const void* 
     const double* M = direction == 2 ? p->d_back : p->d_scalar;
     k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, nrows, inner, cplx);
   }
-  if (direction == 1) {
+  if (direction == 1 && p->form != SGPU_MIXED_DF) {
     const unsigned nb = (unsigned)((nlines + 127) / 128);
     if (cplx)
       k_legendre_mass<cd><<<nb, 128, 0, stream>>>((cd*)out, p->d_mass, p->N, p->basis, nlines, inner);
@@ -409,10 +465,7 @@ extern "C" int sgpu_legendre_workspace_size(const sgpu_legendre_plan* p, int64_t
     *bytes = 0;
     return SGPU_OK;
   }
-  const int c = data_kind == SGPU_COMPLEX;
-  const size_t a = oz::workspace_bytes(p->tc_scalar, outer * inner, inner, c);
-  const size_t b = oz::workspace_bytes(p->tc_forward, outer * inner, inner, c);
-  *bytes = a > b ? a : b;
+  *bytes = oz::workspace_bytes(p->tc_scalar, outer * inner, inner, data_kind == SGPU_COMPLEX);
   return SGPU_OK;
 }
 

@@ -62,9 +62,6 @@ struct Cfg {
 };
 // 7 digits (48 bits), 28 products, groups 0..3 exact: normwise ~1e-13
 typedef Cfg<7, 5, 96> CfgStd;
-// 8 digits (55 bits), 36 products, groups 0..4 exact: ~1e-15, for outputs that
-// a later step divides by small numbers (the forward transform's mass solve)
-typedef Cfg<8, 6, 80> CfgAcc;
 
 // index of element (row r, k in the K block) inside a block of `rows` rows:
 // [k / 8][r / 8][r % 8][k % 8]
@@ -94,7 +91,7 @@ SGPU_HD void split_digits(double x, int e, uint16_t (&out)[S]) {
   if (field != 0) {
     const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     // X = round(|x| 2^{WS-e}) = round(m 2^{-sh}); sh >= 54 - W*S since
-    // |x| < 2^{e-1} (>= 12 for 6 digits, >= -2 for 8), and X < 2^{WS-1}
+    // |x| < 2^{e-1} (>= 5 for 7 digits; <= 0 only above 7), X < 2^{WS-1}
     const int sh = 1075 + e - W * S - field;
     if (sh <= 0)
       X = (int64_t)(m << (-sh));

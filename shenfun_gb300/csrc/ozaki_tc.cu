@@ -51,7 +51,6 @@ struct GemmSmem {
   static const size_t bytes = need < 232448 ? 232448 : need;
 };
 static_assert(GemmSmem<CfgStd>::need <= 232448, "stages exceed shared memory");
-static_assert(GemmSmem<CfgAcc>::need <= 232448, "stages exceed shared memory");
 
 template <class C>
 __global__ void __launch_bounds__(128, 1)
@@ -210,12 +209,11 @@ static int matrix_create_cfg(const double* M, int N, Matrix* out) {
   return SGPU_OK;
 }
 
-int matrix_create(const double* M, int N, int accurate, Matrix* out) {
+int matrix_create(const double* M, int N, Matrix* out) {
   if (pick_digits(N) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
   out->N = N;
-  out->accurate = accurate ? 1 : 0;
-  out->S = accurate ? CfgAcc::S : CfgStd::S;
-  return accurate ? matrix_create_cfg<CfgAcc>(M, N, out) : matrix_create_cfg<CfgStd>(M, N, out);
+  out->S = CfgStd::S;
+  return matrix_create_cfg<CfgStd>(M, N, out);
 }
 
 void matrix_destroy(Matrix* m) {
@@ -224,7 +222,7 @@ void matrix_destroy(Matrix* m) {
 }
 
 size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx) {
-  const Geom g = make_geom(m.N, nlines, inner, cplx, m.accurate ? CfgAcc::BN : CfgStd::BN);
+  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN);
   return a_split_bytes(g, m.S);
 }
 
@@ -254,11 +252,11 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
              void* work, size_t work_bytes, cudaStream_t stream) {
   if (nlines == 0) return SGPU_OK;
   if (!m.tiles) return SGPU_ERR_ARG;
-  const Geom g = make_geom(m.N, nlines, inner, cplx, m.accurate ? CfgAcc::BN : CfgStd::BN);
+  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN);
   // grid.x and the split kernel's block count stay below 2^31
   if ((int64_t)g.mtiles * BM * g.nkb * 4 / 256 > 0x7fffffff) return SGPU_ERR_ARG;
   if (work_bytes < a_split_bytes(g, m.S) || ((uintptr_t)work & 255)) return SGPU_ERR_ARG;
-  return m.accurate ? run<CfgAcc>(m, g, in, out, work, stream) : run<CfgStd>(m, g, in, out, work, stream);
+  return run<CfgStd>(m, g, in, out, work, stream);
 }
 
 }  // namespace oz
