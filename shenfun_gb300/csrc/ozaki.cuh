@@ -81,37 +81,46 @@ SGPU_HD uint32_t exp_field(double x) {
 }
 
 // balanced digits of x (|x| < 2^{e-1}) at W*S bits: BF16 bit patterns of
-// d_s 2^{-W s}.  Integer arithmetic only.
+// d_s 2^{-W s}.  Integer arithmetic (and exact FP32 adds) only: the W-bit
+// fields of the fixed-point magnitude X are read off with shifts, then made
+// balanced from the least significant end (a field >= 2^{W-1} becomes
+// field - 2^W with a carry into the next one), which gives the unique
+// representation with d_s in [-2^{W-1}, 2^{W-1}) for s >= 1.
 template <int W, int S>
 SGPU_HD void split_digits(double x, int e, uint16_t (&out)[S]) {
+  static_assert(W * S <= 52, "digits beyond the FP64 mantissa");
   uint64_t b;
   memcpy(&b, &x, 8);
   const int field = (int)((b >> 52) & 0x7ff);
-  int64_t X = 0;
+  uint64_t X = 0;
   if (field != 0) {
     const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    // X = round(|x| 2^{WS-e}) = round(m 2^{-sh}); sh >= 54 - W*S since
-    // |x| < 2^{e-1} (>= 5 for 7 digits; <= 0 only above 7), X < 2^{WS-1}
+    // X = round(|x| 2^{WS-e}) = round(m 2^{-sh}); sh >= 54 - W*S > 0 since
+    // |x| < 2^{e-1}, and X < 2^{WS-1}
     const int sh = 1075 + e - W * S - field;
-    if (sh <= 0)
-      X = (int64_t)(m << (-sh));
-    else if (sh < 64)
-      X = (int64_t)((m + (1ull << (sh - 1))) >> sh);
+    if (sh < 64) X = (m + (1ull << (sh - 1))) >> sh;
   }
-  const bool neg = (b >> 63) != 0;
+  int d[S];
+  int carry = 0;
+#pragma unroll
+  for (int s = S - 1; s >= 0; --s) {
+    int u = (int)((uint32_t)(X >> (W * (S - 1 - s))) & ((1u << W) - 1)) + carry;
+    if (s > 0) {
+      carry = u >= (1 << (W - 1)) ? 1 : 0;
+      u -= carry << W;
+    }
+    d[s] = u;
+  }
+  const uint32_t sign = (uint32_t)(b >> 63);
 #pragma unroll
   for (int s = 0; s < S; ++s) {
-    const int shs = W * (S - 1 - s);
-    int64_t d;
-    if (s < S - 1) {
-      d = (X + ((int64_t)1 << (shs - 1))) >> shs;
-      X -= d * ((int64_t)1 << shs);
-    } else {
-      d = X;
-    }
-    if (neg) d = -d;
-    // d 2^{-W s} as a float (exact), then its top 16 bits are the BF16 value
-    float f = (float)d;
+    const int v = sign ? -d[s] : d[s];
+    // exact float of v (|v| <= 2^W) by the 1.5 * 2^23 bias, scaled by 2^{-W s};
+    // its top 16 bits are the BF16 value
+    const uint32_t biased = 0x4B400000u + (uint32_t)v;
+    float f;
+    memcpy(&f, &biased, 4);
+    f -= 12582912.0f;
     const uint32_t pb = (uint32_t)(127 - W * s) << 23;  // 2^{-W s}
     float p;
     memcpy(&p, &pb, 4);
@@ -236,30 +245,33 @@ SGPU_HD uint32_t rowexp_partial(const double* in, const Geom& g, int64_t row, in
   return mf;
 }
 
-// split thread t: (row rr of tile mt, 8-wide chunk kc of K) -> S 16-byte
-// stores, one per slice block.  t < mtiles * nkb * 4 * BM.
+// split block (mt, kb): the 128 x 32 input block of row tile mt and K block
+// kb -> S slice blocks of 8 KB.  Phase 1 reads the inputs (consecutive
+// threads take consecutive elements of a line when lines are contiguous,
+// consecutive lines otherwise, so global reads coalesce either way) and writes
+// the digits to shared memory in the tiled order; phase 2 copies the S blocks
+// out with 16-byte stores.  smem: S * A_BYTES bytes, 16-byte aligned.
 template <int S>
-SGPU_HD void split_thread(const double* in, const int* eA, uint16_t* At, const Geom& g, int64_t t) {
-  const int64_t nk = (int64_t)g.nkb * 4;
-  const int rr = (int)(t & (BM - 1));
-  const int64_t rest = t >> 7;
-  const int kc = (int)(rest % nk);
-  const int mt = (int)(rest / nk);
-  const int kb = kc >> 2, kg = kc & 3;
-  const int64_t row = (int64_t)mt * BM + rr;
-  const int k0 = kb * BK + kg * 8;
-  const int e = eA[row];
-  uint16_t dig[8][S];
-  for (int q = 0; q < 8; ++q) {
-    const int k = k0 + q;
-    const double x = (row < g.nrows && k < g.N) ? in[row_offset(g, row, k)] : 0.0;
-    split_digits<W, S>(x, e, dig[q]);
+SGPU_HD void split_block(const double* in, const int* eA, uint16_t* At, const Geom& g, int mt, int kb,
+                         void* smem, int tid, int nth) {
+  uint16_t* sm = (uint16_t*)smem;
+  for (int idx = tid; idx < BM * BK; idx += nth) {
+    const int r = g.inner == 1 ? idx / BK : idx % BM;
+    const int k = g.inner == 1 ? idx % BK : idx / BM;
+    const int64_t row = (int64_t)mt * BM + r;
+    const int kk = kb * BK + k;
+    const double x = (row < g.nrows && kk < g.N) ? in[row_offset(g, row, kk)] : 0.0;
+    uint16_t d[S];
+    split_digits<W, S>(x, eA[row], d);
+    const int ti = tile_index(BM, r, k);
+    for (int s = 0; s < S; ++s) sm[s * A_ELEMS + ti] = d[s];
   }
-  for (int s = 0; s < S; ++s) {
-    uint32_t v[4];
-    for (int q = 0; q < 4; ++q) v[q] = (uint32_t)dig[2 * q][s] | ((uint32_t)dig[2 * q + 1][s] << 16);
-    uint16_t* dst = At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + tile_index(BM, rr, kg * 8);
-    memcpy(dst, v, 16);
+  SGPU_SYNC();
+  const int nvec = S * A_BYTES / 16;
+  for (int v = tid; v < nvec; v += nth) {
+    const int s = v / (A_BYTES / 16), off = v % (A_BYTES / 16);
+    uint16_t* dst = At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + off * 8;
+    memcpy(dst, sm + (size_t)s * A_ELEMS + off * 8, 16);
   }
 }
 

@@ -1,8 +1,8 @@
 // Split-BF16 tensor-core contraction along lines (the mixed form of the
 // Legendre Vandermonde transforms).  Kernels:
 //   k_oz_rowexp   one warp per row: the row's power-of-two scale
-//   k_oz_split    one thread per (row, 8-wide K chunk): S digit slices written
-//                 pre-tiled (16-byte stores, coalesced along rows)
+//   k_oz_split    one CTA per (128-row tile, 32-wide K block): S digit slices
+//                 staged in shared memory, written out pre-tiled (16-byte stores)
 //   k_oz_gemm     one CTA per 128 x BN output tile: a producer thread streams
 //                 2S slice blocks per K stage with bulk copies, one thread
 //                 issues tcgen05.mma for the S(S+1)/2 slice products into NACC
@@ -35,9 +35,9 @@ __global__ void __launch_bounds__(256) k_oz_rowexp(const double* __restrict__ in
 template <int S>
 __global__ void __launch_bounds__(256) k_oz_split(const double* __restrict__ in, const int* __restrict__ eA,
                                                   uint16_t* __restrict__ At, Geom g) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)g.mtiles * g.nkb * 4 * BM) return;
-  split_thread<S>(in, eA, At, g, t);
+  extern __shared__ __align__(16) unsigned char split_smem[];
+  const int mt = (int)(blockIdx.x / (unsigned)g.nkb), kb = (int)(blockIdx.x % (unsigned)g.nkb);
+  split_block<S>(in, eA, At, g, mt, kb, split_smem, (int)threadIdx.x, (int)blockDim.x);
 }
 
 // shared memory: STAGES x (S blocks of A, S blocks of B), then the barriers
@@ -65,7 +65,9 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t* accf = empty + STAGES;
   uint32_t* tmem_holder = (uint32_t*)(accf + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int mt = blockIdx.x, nt = blockIdx.y;
+  // output-column tiles fastest: the CTAs that share a row tile run together
+  // and read its slices from DRAM once
+  const int nt = (int)(blockIdx.x % (unsigned)g.ntiles), mt = (int)(blockIdx.x / (unsigned)g.ntiles);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
@@ -144,9 +146,11 @@ __global__ void __launch_bounds__(128, 1)
     tc::mma_commit(accf);  // accumulators final (also after an early exit)
   }
 
-  // epilogue: warp w owns TMEM lanes 32w..32w+31 = tile rows
+  // epilogue: warp w owns TMEM lanes 32w..32w+31 = tile rows.  The wait for
+  // the accumulators sleeps between probes so that the idle warps leave the
+  // issue slots to the producer and MMA threads.
   __syncwarp();
-  if (!tc::mbar_wait(accf, 0)) ok = false;
+  if (!tc::mbar_wait_sleep(accf, 0)) ok = false;
   __syncwarp();
   tc::fence_after_sync();
   const int64_t row = (int64_t)mt * BM + warp * 32 + lane;
@@ -241,10 +245,9 @@ static int run(const Matrix& m, const Geom& g, const double* in, double* out, vo
   int* eA = (int*)((char*)work + (size_t)C::S * g.mtiles * g.nkb * A_BYTES);
   const int64_t nrow_pad = (int64_t)g.mtiles * BM;
   k_oz_rowexp<<<(unsigned)((nrow_pad * 32 + 255) / 256), 256, 0, stream>>>(in, eA, g);
-  const int64_t nsplit = nrow_pad * g.nkb * 4;
-  k_oz_split<C::S><<<(unsigned)((nsplit + 255) / 256), 256, 0, stream>>>(in, eA, At, g);
-  dim3 grid((unsigned)g.mtiles, (unsigned)g.ntiles);
-  k_oz_gemm<C><<<grid, 128, GemmSmem<C>::bytes, stream>>>(At, eA, m.tiles, m.exps, out, g);
+  k_oz_split<C::S><<<(unsigned)((int64_t)g.mtiles * g.nkb), 256, C::S * A_BYTES, stream>>>(in, eA, At, g);
+  k_oz_gemm<C><<<(unsigned)((int64_t)g.mtiles * g.ntiles), 128, GemmSmem<C>::bytes, stream>>>(At, eA, m.tiles,
+                                                                                               m.exps, out, g);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
@@ -253,8 +256,9 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
   if (nlines == 0) return SGPU_OK;
   if (!m.tiles) return SGPU_ERR_ARG;
   const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN);
-  // grid.x and the split kernel's block count stay below 2^31
-  if ((int64_t)g.mtiles * BM * g.nkb * 4 / 256 > 0x7fffffff) return SGPU_ERR_ARG;
+  // one-dimensional grids: tiles x K blocks stay below 2^31
+  if ((int64_t)g.mtiles * (g.nkb > g.ntiles ? g.nkb : g.ntiles) > 0x7fffffff || (int64_t)g.mtiles * 16 > 0x7fffffff)
+    return SGPU_ERR_ARG;
   if (work_bytes < a_split_bytes(g, m.S) || ((uintptr_t)work & 255)) return SGPU_ERR_ARG;
   return run<CfgStd>(m, g, in, out, work, stream);
 }

@@ -67,6 +67,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
   return false;
 }
 
+// the same bound for waits that may take long (a whole main loop): probes
+// spaced by __nanosleep
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity,
+                                                uint64_t limit_ns = 1000000000ull) {
+  if (mbar_test(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t it = 0; it < (1u << 24); ++it) {
+    __nanosleep(256);
+    if (mbar_test(bar, parity)) return true;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  }
+  return false;
+}
+
 // ---- bulk copy global -> shared (16-byte aligned, size a multiple of 16) -----
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile(

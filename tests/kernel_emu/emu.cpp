@@ -118,7 +118,12 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
   const size_t at_elems = (size_t)S * g.mtiles * g.nkb * A_ELEMS;
   uint16_t* At = (uint16_t*)malloc(at_elems * 2);
   for (size_t i = 0; i < at_elems; ++i) At[i] = 0x7FC0;  // BF16 NaN: unwritten shows
-  for (int64_t t = 0; t < (int64_t)g.mtiles * g.nkb * 4 * BM; ++t) split_thread<C::S>(in, eA.data(), At, g, t);
+  {
+    void* ssm = malloc((size_t)S * A_BYTES);
+    for (int mt = 0; mt < g.mtiles; ++mt)
+      for (int kb = 0; kb < g.nkb; ++kb) split_block<C::S>(in, eA.data(), At, g, mt, kb, ssm, 0, 1);
+    free(ssm);
+  }
   const size_t bt_elems = matrix_tile_elems<C>(g.N);
   uint16_t* Bt = (uint16_t*)malloc(bt_elems * 2);
   int* eB = (int*)malloc(sizeof(int) * (size_t)g.ntiles * BN);
