@@ -53,7 +53,11 @@ extern "C" int sgpu_leggauss(int N, double* x, double* w) {
       pp = N * (z * p1 - p0) / (z * z - 1);
       ld_t dz = p1 / pp;
       z -= dz;
-      if (fabsl(dz) < 1e-19L) {
+      // Newton converges quadratically from Tricomi's guess: once the step
+      // is below 1e-15 the next one would be below 1e-30, beyond the long
+      // double format on every host (a fixed 1e-19 test can stall at the
+      // x86 80-bit format's resolution for up to the iteration cap)
+      if (fabsl(dz) < 1e-15L) {
         // refresh the derivative at the converged root
         p0 = 1;
         p1 = z;

@@ -235,7 +235,9 @@ static int run(const Matrix& m, const Geom& g, const double* in, double* out, vo
   static bool attr_set = false;  // benign race: every caller sets the same value
   if (!attr_set) {
     if (cudaFuncSetAttribute(k_oz_gemm<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)GemmSmem<C>::bytes) != cudaSuccess) {
+                             (int)GemmSmem<C>::bytes) != cudaSuccess ||
+        cudaFuncSetAttribute(k_oz_split<C::S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             C::S * A_BYTES) != cudaSuccess) {
       cudaGetLastError();
       return SGPU_ERR_CUDA;
     }
