@@ -186,14 +186,32 @@ SGPU_HD double fixed_to_double(int64_t T, int E) {
   return r;
 }
 
-// one output element from the NACC FP32 accumulators (bit patterns) of the
-// digit groups; E = eA + eB - 2W.  |G_g| <= (g+1) 2^{2W-2} K, so for
-// K <= 1024 the 2^-36 fixed-point sum stays below 21 * 2^58 < 2^63.
+// FP32 -> int32, round to nearest (exact for the integer-valued sums)
+SGPU_HD int32_t f2i_rn(float v) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rn(v);
+#else
+  return (int32_t)lrintf(v);
+#endif
+}
+
+// one output element from the five FP32 accumulators (bit patterns) of digit
+// groups 0..3 and >= 4; E = eA + eB - 2W.  G_g 2^{Wg} (g <= 3) are integers
+// below 2^24 in magnitude (exact sums), G4 2^33 is below 2^31; the int64 sum
+// T = sum_g G_g 2^{33} is exact up to the rounding of G4 at 2^-33, and T 2^{E-33}
+// is assembled as FP64 bits.
 template <int NACC>
 SGPU_HD double combine_groups(const uint32_t (&gb)[NACC], int E) {
-  int64_t T = 0;
-  for (int i = 0; i < NACC; ++i) T += f32_fixed(gb[i], 36);
-  return fixed_to_double(T, E - 36);
+  static_assert(NACC == 5 && W == 7, "the combination assumes 7-bit digits and five accumulators");
+  float g[NACC];
+  for (int i = 0; i < NACC; ++i) memcpy(&g[i], &gb[i], 4);
+  const int32_t i0 = f2i_rn(g[0]);
+  const int32_t i1 = f2i_rn(g[1] * 128.0f);
+  const int32_t i2 = f2i_rn(g[2] * 16384.0f);
+  const int32_t i3 = f2i_rn(g[3] * 2097152.0f);
+  const int32_t i4 = f2i_rn(g[4] * 8589934592.0f);  // 2^33
+  const int64_t T = ((((int64_t)i0 * 128 + i1) * 128 + i2) * 128 + i3) * 4096 + i4;
+  return fixed_to_double(T, E - 33);
 }
 
 // geometry of one contraction over lines of a (outer, N, inner) array:

@@ -52,8 +52,13 @@ struct GemmSmem {
 };
 static_assert(GemmSmem<CfgStd>::need <= 232448, "stages exceed shared memory");
 
+// 16 warps: warp 0 lane 0 produces, warp 1 lane 0 issues MMAs; in the
+// epilogue warp w reads TMEM lane quarter w % 4 (the hardware ties a warp to
+// the lanes 32 (w % 4) .. +31) and column quarter w / 4
+const int GEMM_THREADS = 512;
+
 template <class C>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_oz_gemm(const uint16_t* __restrict__ At, const int* __restrict__ eA, const uint16_t* __restrict__ Bt,
               const int* __restrict__ eB, double* __restrict__ out, Geom g) {
   constexpr int S = C::S, NACC = C::NACC, BN = C::BN;
@@ -146,31 +151,38 @@ __global__ void __launch_bounds__(128, 1)
     tc::mma_commit(accf);  // accumulators final (also after an early exit)
   }
 
-  // epilogue: warp w owns TMEM lanes 32w..32w+31 = tile rows.  The wait for
-  // the accumulators sleeps between probes so that the idle warps leave the
+  // epilogue: warp w owns TMEM lanes 32 (w % 4) .. +31 = tile rows, and
+  // columns [(w / 4) BN / 4, (w / 4 + 1) BN / 4).  The wait for the
+  // accumulators sleeps between probes so that the idle warps leave the
   // issue slots to the producer and MMA threads.
+  static_assert(BN % 32 == 0, "column quarters of 8-column chunks");
+  constexpr int CQ = BN / 4;
   __syncwarp();
   if (!tc::mbar_wait_sleep(accf, 0)) ok = false;
   __syncwarp();
   tc::fence_after_sync();
-  const int64_t row = (int64_t)mt * BM + warp * 32 + lane;
+  const int quarter = warp & 3, part = warp >> 2;
+  const int64_t row = (int64_t)mt * BM + quarter * 32 + lane;
   const bool row_ok = row < g.nrows;
   const int erow = eA[row] - 2 * W;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-  for (int c0 = 0; c0 < BN; c0 += 16) {
-    uint32_t a[NACC][16];
+  // element (row, col) of the output is out[obase + col * ostride]
+  const int64_t obase = row_offset(g, row_ok ? row : 0, 0);
+  const int64_t ostride = g.inner * (g.cplx ? 2 : 1);
+  const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+  for (int c0 = part * CQ; c0 < (part + 1) * CQ; c0 += 8) {
+    uint32_t a[NACC][8];
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) tc::tmem_ld16(tmem + lane_base + (uint32_t)(q * BN + c0), a[q]);
+    for (int q = 0; q < NACC; ++q) tc::tmem_ld8(tmem + lane_base + (uint32_t)(q * BN + c0), a[q]);
     tc::tmem_ld_wait();
     if (row_ok) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
+      for (int j = 0; j < 8; ++j) {
         const int col = nt * BN + c0 + j;
         if (col < g.N) {
           uint32_t gb[NACC];
 #pragma unroll
           for (int q = 0; q < NACC; ++q) gb[q] = a[q][j];
-          out[row_offset(g, row, col)] = combine_groups<NACC>(gb, erow + eB[col]);
+          out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eB[col]);
         }
       }
     }
@@ -248,8 +260,8 @@ static int run(const Matrix& m, const Geom& g, const double* in, double* out, vo
   const int64_t nrow_pad = (int64_t)g.mtiles * BM;
   k_oz_rowexp<<<(unsigned)((nrow_pad * 32 + 255) / 256), 256, 0, stream>>>(in, eA, g);
   k_oz_split<C::S><<<(unsigned)((int64_t)g.mtiles * g.nkb), 256, C::S * A_BYTES, stream>>>(in, eA, At, g);
-  k_oz_gemm<C><<<(unsigned)((int64_t)g.mtiles * g.ntiles), 128, GemmSmem<C>::bytes, stream>>>(At, eA, m.tiles,
-                                                                                               m.exps, out, g);
+  k_oz_gemm<C><<<(unsigned)((int64_t)g.mtiles * g.ntiles), GEMM_THREADS, GemmSmem<C>::bytes, stream>>>(
+      At, eA, m.tiles, m.exps, out, g);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
