@@ -98,6 +98,16 @@ int sgpu_plan_destroy(sgpu_plan* plan);
  * the Chebyshev/DCT kinds (real or complex lines); Fourier kinds fix it. */
 int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
                       int64_t inner, int data_kind, double scale, cudaStream_t stream);
+/* In the mixed form the Chebyshev kinds with 16 <= n <= 1024 run as a
+ * split-BF16 contraction on the tensor cores, which needs device scratch:
+ * sgpu_plan_workspace_size gives its size (0 for every other plan) and
+ * sgpu_plan_execute_ws takes it from the caller (256-byte aligned);
+ * sgpu_plan_execute takes it from cudaMallocAsync on `stream` for the call. */
+int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, int64_t inner, int data_kind,
+                             size_t* bytes);
+int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
+                         int64_t inner, int data_kind, double scale, void* work, size_t work_bytes,
+                         cudaStream_t stream);
 
 /* ---- banded solvers (optimization/cython/la.pyx) ------------------------
  * TDMA: offsets (-2, 0, 2); data is (3, n): data[0,:-2] = ld, data[1] = d,

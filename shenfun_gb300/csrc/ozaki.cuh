@@ -264,25 +264,40 @@ SGPU_HD uint32_t rowexp_partial(const double* in, const Geom& g, int64_t row, in
 }
 
 // split block (mt, kb): the 128 x 32 input block of row tile mt and K block
-// kb -> S slice blocks of 8 KB.  Phase 1 reads the inputs (consecutive
-// threads take consecutive elements of a line when lines are contiguous,
-// consecutive lines otherwise, so global reads coalesce either way) and writes
-// the digits to shared memory in the tiled order; phase 2 copies the S blocks
+// kb -> S slice blocks of 8 KB.  Phase 1: each work item is one row and eight
+// consecutive k (one 16-byte core-matrix row per slice); it loads its eight
+// inputs first (independent loads in flight), splits them and stores 16 bytes
+// per slice to shared memory in the tiled order.  Items are numbered so that
+// global reads coalesce: along k for contiguous lines (four items cover a
+// 256-byte line segment), along lines otherwise.  Phase 2 copies the S blocks
 // out with 16-byte stores.  smem: S * A_BYTES bytes, 16-byte aligned.
 template <int S>
 SGPU_HD void split_block(const double* in, const int* eA, uint16_t* At, const Geom& g, int mt, int kb,
                          void* smem, int tid, int nth) {
   uint16_t* sm = (uint16_t*)smem;
-  for (int idx = tid; idx < BM * BK; idx += nth) {
-    const int r = g.inner == 1 ? idx / BK : idx % BM;
-    const int k = g.inner == 1 ? idx % BK : idx / BM;
+  const int nitem = BM * (BK / 8);
+  for (int it = tid; it < nitem; it += nth) {
+    const int r = g.inner == 1 ? it / (BK / 8) : it % BM;
+    const int kc = g.inner == 1 ? it % (BK / 8) : it / BM;
     const int64_t row = (int64_t)mt * BM + r;
-    const int kk = kb * BK + k;
-    const double x = (row < g.nrows && kk < g.N) ? in[row_offset(g, row, kk)] : 0.0;
-    uint16_t d[S];
-    split_digits<W, S>(x, eA[row], d);
-    const int ti = tile_index(BM, r, k);
-    for (int s = 0; s < S; ++s) sm[s * A_ELEMS + ti] = d[s];
+    const int k0 = kb * BK + kc * 8;
+    double x[8];
+    if (row < g.nrows) {
+      const int64_t base = row_offset(g, row, 0);
+      const int64_t st = g.inner * (g.cplx ? 2 : 1);
+      for (int q = 0; q < 8; ++q) x[q] = k0 + q < g.N ? in[base + (int64_t)(k0 + q) * st] : 0.0;
+    } else {
+      for (int q = 0; q < 8; ++q) x[q] = 0.0;
+    }
+    const int e = eA[row];
+    uint16_t d[8][S];
+    for (int q = 0; q < 8; ++q) split_digits<W, S>(x[q], e, d[q]);
+    const int ti = tile_index(BM, r, kc * 8);
+    for (int s = 0; s < S; ++s) {
+      uint32_t v[4];
+      for (int q = 0; q < 4; ++q) v[q] = (uint32_t)d[2 * q][s] | ((uint32_t)d[2 * q + 1][s] << 16);
+      memcpy(sm + (size_t)s * A_ELEMS + ti, v, 16);
+    }
   }
   SGPU_SYNC();
   const int nvec = S * A_BYTES / 16;

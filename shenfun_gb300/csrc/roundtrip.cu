@@ -29,6 +29,15 @@ struct sgpu_legendre_plan;
 extern "C" {
 int sgpu_plan_create(sgpu_plan** plan, int kind, int n, int basis, int form);
 int sgpu_plan_destroy(sgpu_plan* plan);
+int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, int64_t inner, int data_kind,
+                             size_t* bytes);
+int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64_t outer, int64_t inner,
+                         int data_kind, double scale, void* work, size_t work_bytes, cudaStream_t stream);
+int sgpu_legendre_workspace_size(const sgpu_legendre_plan* plan, int64_t outer, int64_t inner,
+                                 int data_kind, size_t* bytes);
+int sgpu_legendre_execute_ws(const sgpu_legendre_plan* plan, int direction, const void* in, void* out,
+                             int64_t outer, int64_t inner, int data_kind, void* work, size_t work_bytes,
+                             cudaStream_t stream);
 int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
                       int64_t inner, int data_kind, double scale, cudaStream_t stream);
 int sgpu_legendre_plan_create(sgpu_legendre_plan** plan, int N, int basis, int form);
@@ -180,8 +189,8 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
   p->nsys = ndim == 2 ? (nr / 2 + 1) : N[0] * (nr / 2 + 1);
   p->nphys = (ndim == 2 ? N[0] : N[0] * N[1]) * Nd;
   p->nspec = p->nsys * Nd;
-  // Fourier plans use the requested arithmetic; the Dirichlet axis too when
-  // it is Chebyshev (Legendre contractions are FP64 here)
+  // every plan uses the requested arithmetic (mixed: double-float Fourier
+  // transforms, tensor-core contractions along the Dirichlet axis)
   int st = SGPU_OK;
   if (ndim == 3) {
     st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fx_f, SGPU_XF_C2C_FWD, (int)N[0], 0, form);
@@ -193,7 +202,10 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
     st |= (ordered ? cached_plan : sgpu_plan_create)(&p->d_s, SGPU_XF_CHEB_SCALAR, (int)Nd, SGPU_BASIS_SD, form);
     st |= (ordered ? cached_plan : sgpu_plan_create)(&p->d_b, SGPU_XF_CHEB_BACKWARD, (int)Nd, SGPU_BASIS_SD, form);
   } else {
-    st |= (ordered ? cached_leg_plan : sgpu_legendre_plan_create)(&p->leg, (int)Nd, SGPU_BASIS_SD, SGPU_PLAIN_F64);
+    // the mixed form contracts on the tensor cores where the plan supports N
+    int lform = form;
+    if (lform == SGPU_MIXED_DF && Nd > 1024) lform = SGPU_PLAIN_F64;
+    st |= (ordered ? cached_leg_plan : sgpu_legendre_plan_create)(&p->leg, (int)Nd, SGPU_BASIS_SD, lform);
   }
   if (st != SGPU_OK) {
     destroy_all(p);
@@ -281,25 +293,43 @@ extern "C" int sgpu_helmholtz_shape(const sgpu_helmholtz_problem* p, int64_t* ph
   return SGPU_OK;
 }
 
+// scratch layout: wr (real, physical size) | wc (complex, spectral size) |
+// wt (the Dirichlet-axis contraction's split input in the tensor-core form)
+static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static size_t split_bytes(const sgpu_helmholtz_problem* p) {
+  const int64_t nlines_d = p->nphys / p->N[p->ndim - 1];
+  size_t a = 0, b = 0;
+  if (p->family == SGPU_FAMILY_CHEBYSHEV) {
+    sgpu_plan_workspace_size(p->d_s, nlines_d, 1, SGPU_REAL, &a);
+    sgpu_plan_workspace_size(p->d_b, nlines_d, 1, SGPU_REAL, &b);
+  } else {
+    sgpu_legendre_workspace_size(p->leg, nlines_d, 1, SGPU_REAL, &a);
+  }
+  return a > b ? a : b;
+}
+
 extern "C" int sgpu_helmholtz_workspace_size(const sgpu_helmholtz_problem* p, size_t* bytes) {
   if (!p || !bytes) return SGPU_ERR_ARG;
-  const size_t r = ((size_t)p->nphys * 8 + 255) & ~(size_t)255;
-  *bytes = r + (size_t)p->nspec * 16;
+  *bytes = round256((size_t)p->nphys * 8) + round256((size_t)p->nspec * 16) + split_bytes(p);
   return SGPU_OK;
 }
 
-// the step itself, given scratch arrays wr (real, physical size) and wc
-// (complex, spectral size)
-static int helmholtz_run(const sgpu_helmholtz_problem* p, const double* f, double* u, double* wr,
-                         double* wc, cudaStream_t s) {
+// the step itself on a scratch area laid out as above
+static int helmholtz_run(const sgpu_helmholtz_problem* p, const double* f, double* u, void* work,
+                         cudaStream_t s) {
   const int64_t Nd = p->N[p->ndim - 1];
   const int64_t nlines_d = p->nphys / Nd;  // physical lines along the last axis
+  double* wr = (double*)work;
+  double* wc = (double*)((unsigned char*)work + round256((size_t)p->nphys * 8));
+  void* wt = (unsigned char*)wc + round256((size_t)p->nspec * 16);
+  const size_t wtb = split_bytes(p);
   int st = SGPU_OK;
   // 1. scalar product along the Dirichlet axis (real data)
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    st |= sgpu_plan_execute(p->d_s, f, wr, nlines_d, 1, SGPU_REAL, 1.0, s);
+    st |= sgpu_plan_execute_ws(p->d_s, f, wr, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s);
   else
-    st |= sgpu_legendre_execute(p->leg, 0, f, wr, nlines_d, 1, SGPU_REAL, s);
+    st |= sgpu_legendre_execute_ws(p->leg, 0, f, wr, nlines_d, 1, SGPU_REAL, wt, wtb, s);
   if (p->ndim == 2) {
     const int64_t N0 = p->N[0];
     st |= sgpu_plan_execute(p->fr_f, wr, wc, 1, Nd, SGPU_REAL, 1.0 / N0, s);
@@ -322,9 +352,9 @@ static int helmholtz_run(const sgpu_helmholtz_problem* p, const double* f, doubl
     st |= sgpu_plan_execute(p->fr_b, wc, wr, N0, Nd, SGPU_COMPLEX, 1.0, s);
   }
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    st |= sgpu_plan_execute(p->d_b, wr, u, nlines_d, 1, SGPU_REAL, 1.0, s);
+    st |= sgpu_plan_execute_ws(p->d_b, wr, u, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s);
   else
-    st |= sgpu_legendre_execute(p->leg, 2, wr, u, nlines_d, 1, SGPU_REAL, s);
+    st |= sgpu_legendre_execute_ws(p->leg, 2, wr, u, nlines_d, 1, SGPU_REAL, wt, wtb, s);
   return st == SGPU_OK ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
@@ -335,10 +365,7 @@ extern "C" int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* p, const doubl
   sgpu_helmholtz_workspace_size(p, &need);
   if (work_bytes < need) return SGPU_ERR_ARG;
   if (((uintptr_t)work & 255) != 0) return SGPU_ERR_ARG;
-  const size_t r = ((size_t)p->nphys * 8 + 255) & ~(size_t)255;
-  double* wr = (double*)work;
-  double* wc = (double*)((unsigned char*)work + r);
-  return helmholtz_run(p, f, u, wr, wc, stream);
+  return helmholtz_run(p, f, u, work, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -404,8 +431,5 @@ extern "C" int sgpu_helmholtz_solve_noalloc(const sgpu_helmholtz_problem* p, con
     }
     base = g_noalloc_addr[dev];
   }
-  const size_t r = ((size_t)p->nphys * 8 + 255) & ~(size_t)255;
-  double* wr = (double*)base;
-  double* wc = (double*)((unsigned char*)base + r);
-  return helmholtz_run(p, f, u, wr, wc, stream);
+  return helmholtz_run(p, f, u, base, stream);
 }

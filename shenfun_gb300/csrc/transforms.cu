@@ -1,9 +1,19 @@
 // Transform plans (C ABI: sgpu_plan_*); the kernels are in xf_*.cu.
+//
+// In the mixed form the Chebyshev kinds (scalar product, forward, backward
+// of a basis) run as a dense line contraction on the tensor cores
+// (ozaki_tc.cu) instead of the double-float FFT: the operator is linear in
+// the line, so its N x N matrix is the FP64 block program applied to the
+// identity on the host, and one split-BF16 contraction applies it (about 48
+// bits; the forward matrix includes the mass solve, so its error is not
+// magnified by it).  On GB300 the O(N^2) contraction on the tensor cores
+// beats the O(N log N) transform on the FP32/FP64 pipes for N up to ~1000.
 #include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
 
+#include "ozaki_tc.h"
 #include "plan_host.cuh"
 #include "xf_kernels.cuh"
 
@@ -12,11 +22,64 @@ using namespace sgpu;
 struct sgpu_plan {
   LinePlan lp;
   void* dev_tables;  // one allocation holding every device table
+  bool tensor = false;
+  oz::Matrix tc;     // tensor form: the line operator, split
 };
+
+namespace {
+
+bool tensor_kind(int kind, int n, int form) {
+  return form == SGPU_MIXED_DF && n >= 16 && oz::pick_digits(n) == SGPU_OK &&
+         (kind == SGPU_XF_CHEB_SCALAR || kind == SGPU_XF_CHEB_FORWARD || kind == SGPU_XF_CHEB_BACKWARD);
+}
+
+// M[j][k] = output k of the FP64 transform of the unit line e_j (n x n)
+int operator_matrix(int kind, int n, int basis, std::vector<double>& M) {
+  LinePlan p;
+  HostTables T;
+  const int st = build_plan_host(kind, n, basis, SGPU_PLAIN_F64, p, T);
+  if (st != SGPU_OK) return st;
+  if (p.n_in != n || p.n_out != n) return SGPU_ERR_UNSUPPORTED;
+  size_t off[SGPU_NTAB];
+  std::vector<unsigned char> img(table_layout(T, off), 0);
+  table_image(T, off, img.data());
+  bind_tables(p, T, off, img.data());
+  std::vector<double> I((size_t)n * n, 0.0);
+  for (int j = 0; j < n; ++j) I[(size_t)j * n + j] = 1.0;
+  M.assign((size_t)n * n, 0.0);
+  std::vector<unsigned char> smem(p.smem + 16);
+  const int lpb = lines_per_block(p, 0);
+  for (int64_t b = 0; b < (n + lpb - 1) / lpb; ++b)
+    prog_dispatch<double>(p, I.data(), M.data(), 0, n, 1, 1.0, b, smem.data(), 0, 1);
+  return SGPU_OK;
+}
+
+}  // namespace
 
 extern "C" int sgpu_plan_create(sgpu_plan** out, int kind, int n, int basis, int form) {
   if (!out) return SGPU_ERR_ARG;
   *out = nullptr;
+  if (tensor_kind(kind, n, form)) {
+    std::vector<double> M;
+    int st = operator_matrix(kind, n, basis, M);
+    if (st != SGPU_OK) return st;
+    sgpu_plan* plan = new (std::nothrow) sgpu_plan;
+    if (!plan) return SGPU_ERR_NOMEM;
+    st = oz::matrix_create(M.data(), n, &plan->tc);
+    if (st != SGPU_OK) {
+      delete plan;
+      return st;
+    }
+    std::memset(&plan->lp, 0, sizeof(plan->lp));
+    plan->lp.kind = kind;
+    plan->lp.basis = basis;
+    plan->lp.form = form;
+    plan->lp.n = plan->lp.n_in = plan->lp.n_out = n;
+    plan->dev_tables = nullptr;
+    plan->tensor = true;
+    *out = plan;
+    return SGPU_OK;
+  }
   LinePlan p;
   HostTables T;
   int st = build_plan_host(kind, n, basis, form, p, T);
@@ -50,15 +113,27 @@ extern "C" int sgpu_plan_create(sgpu_plan** out, int kind, int n, int basis, int
 extern "C" int sgpu_plan_destroy(sgpu_plan* plan) {
   if (!plan) return SGPU_OK;
   if (plan->dev_tables) cudaFree(plan->dev_tables);
+  oz::matrix_destroy(&plan->tc);
   delete plan;
   return SGPU_OK;
 }
 
-extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
-                                 int64_t inner, int data_kind, double scale, cudaStream_t stream) {
+extern "C" int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, int64_t inner, int data_kind,
+                                        size_t* bytes) {
+  if (!plan || !bytes || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
+  *bytes = plan->tensor ? oz::workspace_bytes(plan->tc, outer * inner, inner, data_kind == SGPU_COMPLEX) : 0;
+  return SGPU_OK;
+}
+
+static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t outer, int64_t inner,
+                    int data_kind, double scale, void* work, size_t work_bytes, cudaStream_t stream) {
   if (!plan || !in || !out) return SGPU_ERR_ARG;
   if (outer < 0 || inner < 1) return SGPU_ERR_ARG;
   if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
+  if (plan->tensor)  // in place is fine: the contraction reads the split copy of the input
+    return oz::contract(plan->tc, (const double*)in, (double*)out, outer * inner, inner,
+                        data_kind == SGPU_COMPLEX, work, work_bytes, stream);
   const LinePlan& p = plan->lp;
   if (in == out && p.n_in != p.n_out) return SGPU_ERR_ARG;
   const int64_t nlines = outer * inner;
@@ -77,4 +152,29 @@ extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* ou
                    : xf_launch_cheb_df(G, p, src, dst, dc, nlines, inner, scale, nb, stream);
   return fourier ? xf_launch_fourier_f64(G, p, src, dst, dc, nlines, inner, scale, nb, stream)
                  : xf_launch_cheb_f64(G, p, src, dst, dc, nlines, inner, scale, nb, stream);
+}
+
+extern "C" int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
+                                    int64_t inner, int data_kind, double scale, void* work, size_t work_bytes,
+                                    cudaStream_t stream) {
+  return plan_run(plan, in, out, outer, inner, data_kind, scale, work, work_bytes, stream);
+}
+
+// without a caller workspace the tensor form takes its scratch from the
+// stream-ordered allocator for the duration of the call
+extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
+                                 int64_t inner, int data_kind, double scale, cudaStream_t stream) {
+  if (!plan || !plan->tensor || outer * inner == 0)
+    return plan_run(plan, in, out, outer, inner, data_kind, scale, nullptr, 0, stream);
+  size_t nb = 0;
+  int st = sgpu_plan_workspace_size(plan, outer, inner, data_kind, &nb);
+  if (st != SGPU_OK) return st;
+  void* work = nullptr;
+  if (cudaMallocAsync(&work, nb, stream) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_NOMEM;
+  }
+  st = plan_run(plan, in, out, outer, inner, data_kind, scale, work, nb, stream);
+  cudaFreeAsync(work, stream);
+  return st;
 }

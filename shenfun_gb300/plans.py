@@ -7,6 +7,8 @@ chebyshev/bases.py:407-469, fourier/bases.py:218-279): built once per
 """
 import ctypes
 
+import torch
+
 from . import _lib
 from .device import ptr, stream_handle, view3, data_kind
 
@@ -34,8 +36,17 @@ class LinePlan:
         o2, n_out, i2 = view3(tuple(out.shape), axis)
         if (outer, inner) != (o2, i2):
             raise _lib.SgpuError(_lib.ERR_ARG, "input/output shapes differ off the axis")
-        _lib.call("sgpu_plan_execute", self._h, ptr(inp), ptr(out), outer, inner,
-                  data_kind(inp), float(scale), stream_handle(stream))
+        kind = data_kind(inp)
+        nb = ctypes.c_size_t()
+        _lib.call("sgpu_plan_workspace_size", self._h, outer, inner, kind, ctypes.byref(nb))
+        work = None
+        if nb.value:
+            # tensor-core form: scratch for the split input from torch's
+            # caching allocator (512-byte aligned, reused across calls)
+            work = torch.empty(nb.value, dtype=torch.uint8, device=inp.device)
+        _lib.call("sgpu_plan_execute_ws", self._h, ptr(inp), ptr(out), outer, inner, kind,
+                  float(scale), work.data_ptr() if work is not None else None, nb.value,
+                  stream_handle(stream))
         return out
 
 

@@ -98,3 +98,31 @@ def test_mixed_limits(L):
     from shenfun_gb300 import _lib
     with pytest.raises(_lib.SgpuError):
         L.get_plan(1100, _lib.BASIS_SD, _lib.MIXED_DF)
+
+
+@pytest.mark.parametrize("n", [16, 17, 64, 129, 257])
+@pytest.mark.parametrize("basis", ["T", "SD", "SB"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_chebyshev_mixed_tensor(L, n, basis, cplx):
+    """The mixed form's Chebyshev scalar product / forward / backward run as
+    tensor-core contractions with the FP64 transform's matrix: within 1e-10
+    of the oracle, on contiguous and strided axes, 300+ lines."""
+    from shenfun_gb300 import _lib
+    from shenfun_gb300.spaces import ChebyshevOrthogonal, ChebyshevShenDirichlet, ChebyshevShenBiharmonic
+    V = {"T": ChebyshevOrthogonal, "SD": ChebyshevShenDirichlet, "SB": ChebyshevShenBiharmonic}[basis](n)
+    V.form = _lib.MIXED_DF
+    rng = np.random.default_rng(n)
+    for shape, axis in (((100, 3, n), 2), ((3, n, 41), 1)):
+        x = rng.standard_normal(shape)
+        if cplx:
+            x = x + 1j * rng.standard_normal(shape)
+        assert rel(V.scalar_product(dev(x), axis=axis), S.cheb_scalar_product(x, basis, axis)) < TOL
+        fw = V.forward(dev(x), axis=axis)
+        assert rel(fw, S.cheb_forward(x, basis, axis)) < TOL
+        fwn = fw.cpu().numpy()
+        assert rel(V.backward(fw, axis=axis), S.cheb_backward(fwn, basis, axis)) < TOL
+        # in place (the contraction reads its split copy of the input)
+        y = dev(x).clone()
+        V.scalar_product(y, y, axis=axis)
+        assert rel(y, S.cheb_scalar_product(x, basis, axis)) < TOL
+    assert timeouts() == 0
