@@ -40,8 +40,8 @@ namespace sgpu {
 namespace oz {
 
 const int BM = 128;       // rows (lines) per tile = MMA M
-const int BK = 32;        // K per pipeline stage
-const int STAGES = 2;
+const int BK = 32;        // K per split block (the pre-tiled layout)
+const int STAGES = 4;     // pipeline stages of 16 K each (half a split block)
 const int W = 7;          // bits per digit
 const int A_ELEMS = BM * BK;            // 4096 bf16 = 8 KB per A slice block
 const int A_BYTES = A_ELEMS * 2;

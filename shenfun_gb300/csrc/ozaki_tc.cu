@@ -40,10 +40,12 @@ __global__ void __launch_bounds__(256) k_oz_split(const double* __restrict__ in,
   split_block<S>(in, eA, At, g, mt, kb, split_smem, (int)threadIdx.x, (int)blockDim.x);
 }
 
-// shared memory: STAGES x (S blocks of A, S blocks of B), then the barriers
+// shared memory: STAGES x (S half blocks of A, S half blocks of B), then the
+// barriers.  A stage is one MMA K step (16): the first or second half of a
+// split block ([kgroup 4][rowgroup][8][8]: kgroups 0-1 or 2-3, contiguous).
 template <class C>
 struct GemmSmem {
-  static const size_t stage_bytes = (size_t)C::S * (A_BYTES + C::B_BYTES);
+  static const size_t stage_bytes = (size_t)C::S * (A_BYTES + C::B_BYTES) / 2;
   static const size_t bar_off = STAGES * stage_bytes;
   // barriers + alignment slack, rounded up to the 227 KB per-CTA maximum so
   // that every descriptor-addressed operand read stays inside the allocation
@@ -92,29 +94,35 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   const uint32_t tmem = *tmem_holder;
   bool ok = true;
 
-  auto sA = [&](int st, int s) { return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)s * A_BYTES; };
+  constexpr int AH = A_BYTES / 2, BH = C::B_BYTES / 2;  // half blocks
+  auto sA = [&](int st, int s) { return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)s * AH; };
   auto sB = [&](int st, int s) {
-    return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)S * A_BYTES + (size_t)s * C::B_BYTES;
+    return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)S * AH + (size_t)s * BH;
   };
+  const int nsteps = 2 * g.nkb;  // K steps of 16
 
   if (warp == 0 && lane == 0) {
-    // producer: stream the slice blocks of both operands through the stages
-    int kb = 0;
-    for (; kb < g.nkb; ++kb) {
-      const int st = kb % STAGES;
-      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (kb >= STAGES && !tc::mbar_wait(&empty[st], ph ^ 1u)) {
+    // producer: stream the slice half blocks of both operands through the stages
+    int ks = 0;
+    for (; ks < nsteps; ++ks) {
+      const int st = ks % STAGES;
+      const uint32_t ph = (uint32_t)(ks / STAGES) & 1u;
+      if (ks >= STAGES && !tc::mbar_wait(&empty[st], ph ^ 1u)) {
         ok = false;
         break;
       }
-      tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (A_BYTES + C::B_BYTES)));
+      const int kb = ks >> 1, hf = ks & 1;
+      tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (AH + BH)));
       for (int s = 0; s < S; ++s) {
-        tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS, A_BYTES, &full[st]);
-        tc::bulk_g2s(sB(st, s), Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS, C::B_BYTES,
+        tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2),
+                     AH, &full[st]);
+        tc::bulk_g2s(sB(st, s),
+                     Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2), BH,
                      &full[st]);
       }
     }
     // drain: every copy issued must have landed before the CTA may exit
+    const int kb = ks;
     for (int q = kb - STAGES; q < kb; ++q) {
       if (q < 0) continue;
       if (!tc::mbar_wait(&full[q % STAGES], (uint32_t)(q / STAGES) & 1u)) ok = false;
@@ -123,27 +131,23 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     // MMA issuer
     const uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
     uint32_t inited = 0;
-    for (int kb = 0; kb < g.nkb; ++kb) {
-      const int st = kb % STAGES;
-      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+    for (int ks = 0; ks < nsteps; ++ks) {
+      const int st = ks % STAGES;
+      const uint32_t ph = (uint32_t)(ks / STAGES) & 1u;
       if (!tc::mbar_wait(&full[st], ph)) {
         ok = false;
         break;
       }
       tc::fence_after_sync();
 #pragma unroll
-      for (int ks = 0; ks < BK / 16; ++ks) {
+      for (int s = 0; s < S; ++s) {
+        const uint64_t ad = tc::sdesc_interleave(tc::smem_u32(sA(st, s)), LBO_A, SBO);
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const uint64_t ad = tc::sdesc_interleave(tc::smem_u32(sA(st, s)) + ks * 2 * LBO_A, LBO_A, SBO);
-#pragma unroll
-          for (int t = 0; t + s < S; ++t) {
-            const uint64_t bd =
-                tc::sdesc_interleave(tc::smem_u32(sB(st, t)) + ks * 2 * C::LBO_B, C::LBO_B, SBO);
-            const int acc = s + t < NACC - 1 ? s + t : NACC - 1;
-            tc::mma_f16(tmem + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
-            inited |= 1u << acc;
-          }
+        for (int t = 0; t + s < S; ++t) {
+          const uint64_t bd = tc::sdesc_interleave(tc::smem_u32(sB(st, t)), C::LBO_B, SBO);
+          const int acc = s + t < NACC - 1 ? s + t : NACC - 1;
+          tc::mma_f16(tmem + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
+          inited |= 1u << acc;
         }
       }
       tc::mma_commit(&empty[st]);  // frees the stage once these MMAs have read it

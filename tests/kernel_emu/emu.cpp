@@ -128,7 +128,8 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
   uint16_t* Bt = (uint16_t*)malloc(bt_elems * 2);
   int* eB = (int*)malloc(sizeof(int) * (size_t)g.ntiles * BN);
   split_matrix_host<C>(M, g.N, Bt, eB);
-  const size_t stage_bytes = (size_t)S * (A_BYTES + B_BYTES);
+  const size_t AH = A_BYTES / 2, BH = B_BYTES / 2;
+  const size_t stage_bytes = (size_t)S * (AH + BH);
   uint8_t* smem = (uint8_t*)malloc(STAGES * stage_bytes);
   std::vector<float> acc((size_t)NACC * BM * BN);
   const uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
@@ -144,40 +145,39 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
   for (int mt = 0; mt < g.mtiles; ++mt)
     for (int nt = 0; nt < g.ntiles; ++nt) {
       uint32_t inited = 0;
-      for (int kb = 0; kb < g.nkb; ++kb) {
-        const int st = kb % STAGES;
+      for (int ks = 0; ks < 2 * g.nkb; ++ks) {
+        const int st = ks % STAGES, kb = ks >> 1, hf = ks & 1;
         uint8_t* sbase = smem + st * stage_bytes;
         for (int s = 0; s < S; ++s) {
-          memcpy(sbase + (size_t)s * A_BYTES, At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS,
-                 A_BYTES);
-          memcpy(sbase + (size_t)S * A_BYTES + (size_t)s * B_BYTES,
-                 Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS, B_BYTES);
+          memcpy(sbase + (size_t)s * AH,
+                 At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2), AH);
+          memcpy(sbase + (size_t)S * AH + (size_t)s * BH,
+                 Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2), BH);
         }
-        for (int ks = 0; ks < BK / 16; ++ks)
-          for (int s = 0; s < S; ++s)
-            for (int t = 0; t + s < S; ++t) {
-              const uint32_t a_off = (uint32_t)(st * stage_bytes + s * A_BYTES + ks * 2 * LBO_A);
-              const uint32_t b_off = (uint32_t)(st * stage_bytes + S * A_BYTES + t * B_BYTES + ks * 2 * LBO_B);
-              const uint64_t ad = tc::sdesc_interleave(a_off, LBO_A, SBO);
-              const uint64_t bd = tc::sdesc_interleave(b_off, LBO_B, SBO);
-              auto field = [](uint64_t d, int sh) { return (uint32_t)(((d >> sh) & 0x3FFF) << 4); };
-              const uint32_t as = field(ad, 0), al = field(ad, 16), asb = field(ad, 32);
-              const uint32_t bs = field(bd, 0), bl = field(bd, 16), bsb = field(bd, 32);
-              const int a = s + t < NACC - 1 ? s + t : NACC - 1;
-              for (int m = 0; m < BM; ++m)
-                for (int n = 0; n < BN; ++n) {
-                  double sum = 0;
-                  for (int k = 0; k < 16; ++k) {
-                    const uint32_t pa = as + (k >> 3) * al + (m >> 3) * asb + (m & 7) * 16 + (k & 7) * 2;
-                    const uint32_t pb = bs + (k >> 3) * bl + (n >> 3) * bsb + (n & 7) * 16 + (k & 7) * 2;
-                    if (pa + 2 > STAGES * stage_bytes || pb + 2 > STAGES * stage_bytes) return 6;
-                    sum += (double)bf(smem + pa) * (double)bf(smem + pb);
-                  }
-                  float& d = acc[((size_t)a * BM + m) * BN + n];
-                  d = (float)(((inited >> a) & 1 ? (double)d : 0.0) + sum);
+        for (int s = 0; s < S; ++s)
+          for (int t = 0; t + s < S; ++t) {
+            const uint32_t a_off = (uint32_t)(st * stage_bytes + s * AH);
+            const uint32_t b_off = (uint32_t)(st * stage_bytes + S * AH + t * BH);
+            const uint64_t ad = tc::sdesc_interleave(a_off, LBO_A, SBO);
+            const uint64_t bd = tc::sdesc_interleave(b_off, LBO_B, SBO);
+            auto field = [](uint64_t d, int sh) { return (uint32_t)(((d >> sh) & 0x3FFF) << 4); };
+            const uint32_t as = field(ad, 0), al = field(ad, 16), asb = field(ad, 32);
+            const uint32_t bs = field(bd, 0), bl = field(bd, 16), bsb = field(bd, 32);
+            const int a = s + t < NACC - 1 ? s + t : NACC - 1;
+            for (int m = 0; m < BM; ++m)
+              for (int n = 0; n < BN; ++n) {
+                double sum = 0;
+                for (int k = 0; k < 16; ++k) {
+                  const uint32_t pa = as + (k >> 3) * al + (m >> 3) * asb + (m & 7) * 16 + (k & 7) * 2;
+                  const uint32_t pb = bs + (k >> 3) * bl + (n >> 3) * bsb + (n & 7) * 16 + (k & 7) * 2;
+                  if (pa + 2 > STAGES * stage_bytes || pb + 2 > STAGES * stage_bytes) return 6;
+                  sum += (double)bf(smem + pa) * (double)bf(smem + pb);
                 }
-              inited |= 1u << a;
-            }
+                float& d = acc[((size_t)a * BM + m) * BN + n];
+                d = (float)(((inited >> a) & 1 ? (double)d : 0.0) + sum);
+              }
+            inited |= 1u << a;
+          }
       }
       for (int m = 0; m < BM; ++m) {
         const int64_t row = (int64_t)mt * BM + m;
