@@ -228,23 +228,27 @@ def stage_times(torch, run, flush, st, reps=5):
     return out
 
 
-def serving_leg(torch, rates=(300.0, None), nreq=200, seed=5):
+def serving_leg(torch, nreq=200, seed=5, form="mixed"):
     """Serving stream: mixed 2D/3D Fourier x Chebyshev/Legendre Dirichlet
     Helmholtz requests, N per axis log-uniform in [32, 512] (grids above 2^24
-    points redrawn), c log-uniform in [0.1, 1e4], Poisson arrivals at each
-    rate (None = all at once: saturation).  Latency = completion - arrival."""
+    points redrawn), c log-uniform in [0.1, 1e4].  First all requests at once
+    (saturation throughput C), then Poisson arrivals at 0.5 C: latency =
+    completion - arrival, under load but below saturation."""
     from shenfun_gb300 import serving as SV
     out = []
-    for rate in rates:
+    rate = None
+    for _ in range(2):
         stream = SV.make_stream(nreq, seed=seed, rate=rate)
-        ex = SV.GpuExecutor(nstreams=4, cache_budget=8 << 30, keep_results=False)
+        ex = SV.GpuExecutor(nstreams=4, cache_budget=8 << 30, keep_results=False, form=form)
         fin, elapsed = SV.run_stream(stream, ex, max_slots=8, mem_budget=24 << 30)
         torch.cuda.synchronize()
         lat = np.array([r.latency for r in fin if r.state == SV.DONE])
-        out.append({"rate_req_per_s": rate, "requests": nreq, "completed": int(len(lat)),
-                    "solves_per_s": len(lat) / elapsed, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-                    "p99_ms": 1e3 * float(np.percentile(lat, 99)),
-                    "cache_hits": ex.hits, "cache_misses": ex.misses})
+        res = {"rate_req_per_s": rate, "requests": nreq, "completed": int(len(lat)), "form": form,
+               "solves_per_s": len(lat) / elapsed, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+               "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+               "cache_hits": ex.hits, "cache_misses": ex.misses}
+        out.append(res)
+        rate = 0.5 * res["solves_per_s"]
     return out
 
 

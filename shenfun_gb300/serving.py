@@ -63,13 +63,16 @@ def array_bytes(N):
 
 def request_bytes(N):
     """Device bytes one in-flight request holds: RHS + solution + scratch
-    (real physical array + complex spectral array)."""
+    (real physical array + complex spectral array + the mixed form's split
+    copy of the physical array, 14 bytes per padded point, bounded by 16 per
+    point with the padding of the last axis to a multiple of 32)."""
     spec = list(N)
     spec[-2 if len(N) == 3 else 0] = spec[-2 if len(N) == 3 else 0] // 2 + 1
     nspec = 1
     for v in spec:
         nspec *= v
-    return 3 * array_bytes(N) + 16 * nspec + 512
+    npad = array_bytes(N[:-1]) // 8 * (-(-N[-1] // 32) * 32)
+    return 3 * array_bytes(N) + 16 * nspec + 16 * npad + 1024
 
 
 def factor_bytes(N, family):
@@ -180,7 +183,7 @@ class GpuExecutor:
     """Runs requests on a pool of CUDA streams with a device-resident,
     byte-budgeted LRU cache of factorised problems."""
 
-    def __init__(self, nstreams=4, cache_budget=4 << 30, form="plain", keep_results=True):
+    def __init__(self, nstreams=4, cache_budget=4 << 30, form="mixed", keep_results=True):
         import torch
         from .problem import HelmholtzProblem
         self.torch = torch

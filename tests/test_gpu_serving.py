@@ -68,11 +68,12 @@ def test_serving_mix_equals_alone(sg):
         assert a[i].state == SV.DONE and m[i].state == SV.DONE, (a[i].error, m[i].error)
         # identical kernels on private buffers: bit-for-bit equal
         assert torch.equal(a[i].result, m[i].result), i
-    # and correct: a sample against the oracle
+    # and correct: a sample against the oracle (the executor's default is the
+    # mixed form, bound 1e-10)
     for i in range(0, 24, 6):
         N, fam, c, _, seed = stream[i]
         f = np.random.default_rng(seed).standard_normal(N)
-        assert rel(m[i].result.numpy(), oracle_roundtrip(f, N, fam, c)) < 1e-12
+        assert rel(m[i].result.numpy(), oracle_roundtrip(f, N, fam, c)) < 1e-10
 
 
 @pytest.mark.parametrize("N,family", [((16, 12, 24), "chebyshev"), ((24, 31), "legendre")])
