@@ -268,8 +268,8 @@ SGPU_HD uint32_t rowexp_partial(const double* in, const Geom& g, int64_t row, in
 // consecutive k (one 16-byte core-matrix row per slice); it loads its eight
 // inputs first (independent loads in flight), splits them and stores 16 bytes
 // per slice to shared memory in the tiled order.  Items are numbered so that
-// global reads coalesce: along k for contiguous lines (four items cover a
-// 256-byte line segment), along lines otherwise.  Phase 2 copies the S blocks
+// global reads coalesce: a warp covers whole 256-byte line segments for
+// contiguous lines, consecutive lines otherwise.  Phase 2 copies the S blocks
 // out with 16-byte stores.  smem: S * A_BYTES bytes, 16-byte aligned.
 template <int S>
 SGPU_HD void split_block(const double* in, const int* eA, uint16_t* At, const Geom& g, int mt, int kb,
@@ -277,8 +277,11 @@ SGPU_HD void split_block(const double* in, const int* eA, uint16_t* At, const Ge
   uint16_t* sm = (uint16_t*)smem;
   const int nitem = BM * (BK / 8);
   for (int it = tid; it < nitem; it += nth) {
-    const int r = g.inner == 1 ? it / (BK / 8) : it % BM;
-    const int kc = g.inner == 1 ? it % (BK / 8) : it / BM;
+    // contiguous lines: a warp takes 8 rows x 4 chunks (each row's 256 bytes
+    // read together), lanes 8j..8j+7 on 8 different rows so that their
+    // 16-byte shared stores hit different banks
+    const int r = g.inner == 1 ? 8 * (it >> 5) + (it & 7) : it % BM;
+    const int kc = g.inner == 1 ? (it >> 3) & 3 : it / BM;
     const int64_t row = (int64_t)mt * BM + r;
     const int k0 = kb * BK + kc * 8;
     double x[8];
@@ -292,19 +295,23 @@ SGPU_HD void split_block(const double* in, const int* eA, uint16_t* At, const Ge
     const int e = eA[row];
     uint16_t d[8][S];
     for (int q = 0; q < 8; ++q) split_digits<W, S>(x[q], e, d[q]);
-    const int ti = tile_index(BM, r, kc * 8);
+    const int ti = tile_index(BM, r, kc * 8);  // a multiple of 8 elements: 16-byte aligned
     for (int s = 0; s < S; ++s) {
-      uint32_t v[4];
-      for (int q = 0; q < 4; ++q) v[q] = (uint32_t)d[2 * q][s] | ((uint32_t)d[2 * q + 1][s] << 16);
-      memcpy(sm + (size_t)s * A_ELEMS + ti, v, 16);
+      uint4 v;
+      v.x = (uint32_t)d[0][s] | ((uint32_t)d[1][s] << 16);
+      v.y = (uint32_t)d[2][s] | ((uint32_t)d[3][s] << 16);
+      v.z = (uint32_t)d[4][s] | ((uint32_t)d[5][s] << 16);
+      v.w = (uint32_t)d[6][s] | ((uint32_t)d[7][s] << 16);
+      *reinterpret_cast<uint4*>(sm + (size_t)s * A_ELEMS + ti) = v;
     }
   }
   SGPU_SYNC();
   const int nvec = S * A_BYTES / 16;
+  const uint4* src = reinterpret_cast<const uint4*>(sm);
   for (int v = tid; v < nvec; v += nth) {
     const int s = v / (A_BYTES / 16), off = v % (A_BYTES / 16);
-    uint16_t* dst = At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + off * 8;
-    memcpy(dst, sm + (size_t)s * A_ELEMS + off * 8, 16);
+    uint4* dst = reinterpret_cast<uint4*>(At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS) + off;
+    *dst = src[v];
   }
 }
 

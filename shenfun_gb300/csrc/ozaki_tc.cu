@@ -49,7 +49,7 @@ struct GemmSmem {
   static const size_t bar_off = STAGES * stage_bytes;
   // barriers + alignment slack, rounded up to the 227 KB per-CTA maximum so
   // that every descriptor-addressed operand read stays inside the allocation
-  static const size_t need = bar_off + 256 + 1024;
+  static const size_t need = bar_off + 1024 + 1024;  // barriers, column exponents, slack
   static const size_t bytes = need < 232448 ? 232448 : need;
 };
 static_assert(GemmSmem<CfgStd>::need <= 232448, "stages exceed shared memory");
@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   uint64_t* empty = full + STAGES;
   uint64_t* accf = empty + STAGES;
   uint32_t* tmem_holder = (uint32_t*)(accf + 1);
+  int* eBs = (int*)(smem + GemmSmem<C>::bar_off + 256);  // this tile's column exponents
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // output-column tiles fastest: the CTAs that share a row tile run together
   // and read its slices from DRAM once
@@ -88,6 +89,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc::tmem_alloc(tmem_holder, 512);
     tc::tmem_relinquish();
   }
+  for (int c = threadIdx.x; c < BN; c += blockDim.x) eBs[c] = eB[nt * BN + c];  // padded to ntiles * BN
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           uint32_t gb[NACC];
 #pragma unroll
           for (int q = 0; q < NACC; ++q) gb[q] = a[q][j];
-          out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eB[col]);
+          out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eBs[c0 + j]);
         }
       }
     }

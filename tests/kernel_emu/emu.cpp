@@ -121,7 +121,10 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
   {
     void* ssm = malloc((size_t)S * A_BYTES);
     for (int mt = 0; mt < g.mtiles; ++mt)
-      for (int kb = 0; kb < g.nkb; ++kb) split_block<C::S>(in, eA.data(), At, g, mt, kb, ssm, 0, 1);
+      for (int kb = 0; kb < g.nkb; ++kb) {
+        for (size_t i = 0; i < (size_t)S * A_ELEMS; ++i) ((uint16_t*)ssm)[i] = 0x7FC0;  // BF16 NaN
+        split_block<C::S>(in, eA.data(), At, g, mt, kb, ssm, 0, 1);
+      }
     free(ssm);
   }
   const size_t bt_elems = matrix_tile_elems<C>(g.N);
