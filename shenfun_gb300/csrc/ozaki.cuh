@@ -51,17 +51,19 @@ const int SBO = 128;                    // row-direction core-matrix stride (byt
 // A digit configuration: S digits per operand, products with s + t <= S - 1,
 // NACC FP32 accumulators (groups 0..NACC-2 separately, the rest combined) and
 // BN output columns per tile (NACC * BN <= 512 TMEM columns).
+// Two accumulator sets (2 NACC BN <= 512 TMEM columns) let the epilogue of
+// one tile overlap the main loop of the next.
 template <int S_, int NACC_, int BN_>
 struct Cfg {
   static const int S = S_, NACC = NACC_, BN = BN_;
   static const int B_ELEMS = BN * BK, B_BYTES = B_ELEMS * 2;
   static const int LBO_B = BN * 16;
   static const int NPROD = S * (S + 1) / 2;
-  static_assert(NACC * BN <= 512, "accumulators exceed TMEM");
+  static_assert(2 * NACC * BN <= 512, "two accumulator sets exceed TMEM");
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "MMA N");
 };
 // 7 digits (48 bits), 28 products, groups 0..3 exact: normwise ~1e-13
-typedef Cfg<7, 5, 96> CfgStd;
+typedef Cfg<7, 5, 48> CfgStd;
 
 // index of element (row r, k in the K block) inside a block of `rows` rows:
 // [k / 8][r / 8][r % 8][k % 8]

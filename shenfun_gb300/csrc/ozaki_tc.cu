@@ -3,11 +3,13 @@
 //   k_oz_rowexp   one warp per row: the row's power-of-two scale
 //   k_oz_split    one CTA per (128-row tile, 32-wide K block): S digit slices
 //                 staged in shared memory, written out pre-tiled (16-byte stores)
-//   k_oz_gemm     one CTA per 128 x BN output tile: a producer thread streams
-//                 2S slice blocks per K stage with bulk copies, one thread
-//                 issues tcgen05.mma for the S(S+1)/2 slice products into NACC
-//                 TMEM accumulators, and all four warps run the integer
-//                 epilogue (TMEM -> registers -> FP64 bits -> global).
+//   k_oz_gemm     persistent, one CTA per SM over 128 x BN output tiles: a
+//                 producer thread streams 2S slice half blocks per K step with
+//                 bulk copies, one thread issues tcgen05.mma for the S(S+1)/2
+//                 slice products into NACC TMEM accumulators (two sets, so
+//                 that the next tile's MMAs overlap this tile's epilogue), and
+//                 twelve warps run the integer epilogue (TMEM -> registers ->
+//                 FP64 bits -> global).
 // The split matrix operand (B) is built once on the host with the same digit
 // code and uploaded with the plan.
 #include <cstdio>
@@ -49,47 +51,55 @@ struct GemmSmem {
   static const size_t bar_off = STAGES * stage_bytes;
   // barriers + alignment slack, rounded up to the 227 KB per-CTA maximum so
   // that every descriptor-addressed operand read stays inside the allocation
-  static const size_t need = bar_off + 1024 + 1024;  // barriers, column exponents, slack
+  static const size_t need = bar_off + 1024 + 1024;
   static const size_t bytes = need < 232448 ? 232448 : need;
 };
 static_assert(GemmSmem<CfgStd>::need <= 232448, "stages exceed shared memory");
 
-// 16 warps: warp 0 lane 0 produces, warp 1 lane 0 issues MMAs; in the
-// epilogue warp w reads TMEM lane quarter w % 4 (the hardware ties a warp to
-// the lanes 32 (w % 4) .. +31) and column quarter w / 4
+// Persistent kernel, one CTA per SM, 16 warps.  Warp 0 lane 0 streams the
+// operands' half blocks through the STAGES-deep ring for every tile this CTA
+// owns (tiles blockIdx.x, blockIdx.x + gridDim.x, ...; output-column tiles
+// fastest so that concurrent CTAs share row tiles in L2); warp 1 lane 0
+// issues the MMAs of tile i into accumulator set i % 2; warps 4..15 run the
+// epilogue of tile i (warp w reads TMEM lane quarter w % 4 - the hardware
+// ties a warp to lanes 32 (w % 4) .. +31 - and 16 of the BN = 48 columns)
+// while the MMAs of tile i + 1 fill the other set.
 const int GEMM_THREADS = 512;
+const int EPI_WARPS = 12;
 
 template <class C>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_oz_gemm(const uint16_t* __restrict__ At, const int* __restrict__ eA, const uint16_t* __restrict__ Bt,
               const int* __restrict__ eB, double* __restrict__ out, Geom g) {
   constexpr int S = C::S, NACC = C::NACC, BN = C::BN;
+  static_assert(BN == 3 * 16, "three epilogue warps of 16 columns per lane quarter");
   extern __shared__ uint8_t smem_raw[];
-  // 1024-byte aligned base
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + GemmSmem<C>::bar_off);
-  uint64_t* empty = full + STAGES;
-  uint64_t* accf = empty + STAGES;
-  uint32_t* tmem_holder = (uint32_t*)(accf + 1);
-  int* eBs = (int*)(smem + GemmSmem<C>::bar_off + 256);  // this tile's column exponents
+  uint64_t* full = (uint64_t*)(smem + GemmSmem<C>::bar_off);  // [STAGES]
+  uint64_t* empty = full + STAGES;                              // [STAGES]
+  uint64_t* tfull = empty + STAGES;                             // [2] accumulators ready
+  uint64_t* tempty = tfull + 2;                                 // [2] accumulators read out
+  uint64_t* mdone = tempty + 2;                                 // every MMA finished
+  uint32_t* tmem_holder = (uint32_t*)(mdone + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // output-column tiles fastest: the CTAs that share a row tile run together
-  // and read its slices from DRAM once
-  const int nt = (int)(blockIdx.x % (unsigned)g.ntiles), mt = (int)(blockIdx.x / (unsigned)g.ntiles);
+  const int64_t ntile = (int64_t)g.mtiles * g.ntiles;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&empty[i], 1);
     }
-    tc::mbar_init(accf, 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&tfull[i], 1);
+      tc::mbar_init(&tempty[i], EPI_WARPS);
+    }
+    tc::mbar_init(mdone, 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) {
     tc::tmem_alloc(tmem_holder, 512);
     tc::tmem_relinquish();
   }
-  for (int c = threadIdx.x; c < BN; c += blockDim.x) eBs[c] = eB[nt * BN + c];  // padded to ntiles * BN
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -101,99 +111,122 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   auto sB = [&](int st, int s) {
     return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)S * AH + (size_t)s * BH;
   };
-  const int nsteps = 2 * g.nkb;  // K steps of 16
+  const int nsteps = 2 * g.nkb;  // K steps of 16 per tile
 
   if (warp == 0 && lane == 0) {
-    // producer: stream the slice half blocks of both operands through the stages
-    int ks = 0;
-    for (; ks < nsteps; ++ks) {
-      const int st = ks % STAGES;
-      const uint32_t ph = (uint32_t)(ks / STAGES) & 1u;
-      if (ks >= STAGES && !tc::mbar_wait(&empty[st], ph ^ 1u)) {
-        ok = false;
-        break;
-      }
-      const int kb = ks >> 1, hf = ks & 1;
-      tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (AH + BH)));
-      for (int s = 0; s < S; ++s) {
-        tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2),
-                     AH, &full[st]);
-        tc::bulk_g2s(sB(st, s),
-                     Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2), BH,
-                     &full[st]);
+    // producer
+    int64_t q = 0;  // ring position over all tiles
+    for (int64_t t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
+      const int nt = (int)(t % g.ntiles), mt = (int)(t / g.ntiles);
+      for (int ks = 0; ks < nsteps; ++ks, ++q) {
+        const int st = (int)(q % STAGES);
+        const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
+        if (q >= STAGES && !tc::mbar_wait(&empty[st], ph ^ 1u)) {
+          ok = false;
+          break;
+        }
+        const int kb = ks >> 1, hf = ks & 1;
+        tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (AH + BH)));
+        for (int s = 0; s < S; ++s) {
+          tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2),
+                       AH, &full[st]);
+          tc::bulk_g2s(sB(st, s),
+                       Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2),
+                       BH, &full[st]);
+        }
       }
     }
     // drain: every copy issued must have landed before the CTA may exit
-    const int kb = ks;
-    for (int q = kb - STAGES; q < kb; ++q) {
-      if (q < 0) continue;
-      if (!tc::mbar_wait(&full[q % STAGES], (uint32_t)(q / STAGES) & 1u)) ok = false;
+    for (int64_t r = q - STAGES; r < q; ++r) {
+      if (r < 0) continue;
+      if (!tc::mbar_wait(&full[r % STAGES], (uint32_t)(r / STAGES) & 1u)) ok = false;
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
     const uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
-    uint32_t inited = 0;
-    for (int ks = 0; ks < nsteps; ++ks) {
-      const int st = ks % STAGES;
-      const uint32_t ph = (uint32_t)(ks / STAGES) & 1u;
-      if (!tc::mbar_wait(&full[st], ph)) {
+    int64_t q = 0;
+    int64_t i = 0;  // local tile count
+    for (int64_t t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++i) {
+      const int b = (int)(i & 1);
+      const int64_t use = i >> 1;  // uses of set b before this one
+      if (use >= 1 && !tc::mbar_wait(&tempty[b], (uint32_t)(use - 1) & 1u)) {
         ok = false;
         break;
       }
       tc::fence_after_sync();
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const uint64_t ad = tc::sdesc_interleave(tc::smem_u32(sA(st, s)), LBO_A, SBO);
-#pragma unroll
-        for (int t = 0; t + s < S; ++t) {
-          const uint64_t bd = tc::sdesc_interleave(tc::smem_u32(sB(st, t)), C::LBO_B, SBO);
-          const int acc = s + t < NACC - 1 ? s + t : NACC - 1;
-          tc::mma_f16(tmem + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
-          inited |= 1u << acc;
+      const uint32_t dbase = tmem + (uint32_t)(b * NACC * BN);
+      uint32_t inited = 0;
+      for (int ks = 0; ks < nsteps; ++ks, ++q) {
+        const int st = (int)(q % STAGES);
+        const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
+        if (!tc::mbar_wait(&full[st], ph)) {
+          ok = false;
+          break;
         }
-      }
-      tc::mma_commit(&empty[st]);  // frees the stage once these MMAs have read it
-    }
-    tc::mma_commit(accf);  // accumulators final (also after an early exit)
-  }
-
-  // epilogue: warp w owns TMEM lanes 32 (w % 4) .. +31 = tile rows, and
-  // columns [(w / 4) BN / 4, (w / 4 + 1) BN / 4).  The wait for the
-  // accumulators sleeps between probes so that the idle warps leave the
-  // issue slots to the producer and MMA threads.
-  static_assert(BN % 32 == 0, "column quarters of 8-column chunks");
-  constexpr int CQ = BN / 4;
-  __syncwarp();
-  if (!tc::mbar_wait_sleep(accf, 0)) ok = false;
-  __syncwarp();
-  tc::fence_after_sync();
-  const int quarter = warp & 3, part = warp >> 2;
-  const int64_t row = (int64_t)mt * BM + quarter * 32 + lane;
-  const bool row_ok = row < g.nrows;
-  const int erow = eA[row] - 2 * W;
-  // element (row, col) of the output is out[obase + col * ostride]
-  const int64_t obase = row_offset(g, row_ok ? row : 0, 0);
-  const int64_t ostride = g.inner * (g.cplx ? 2 : 1);
-  const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-  for (int c0 = part * CQ; c0 < (part + 1) * CQ; c0 += 8) {
-    uint32_t a[NACC][8];
+        tc::fence_after_sync();
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) tc::tmem_ld8(tmem + lane_base + (uint32_t)(q * BN + c0), a[q]);
-    tc::tmem_ld_wait();
-    if (row_ok) {
+        for (int s = 0; s < S; ++s) {
+          const uint64_t ad = tc::sdesc_interleave(tc::smem_u32(sA(st, s)), LBO_A, SBO);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int col = nt * BN + c0 + j;
-        if (col < g.N) {
-          uint32_t gb[NACC];
-#pragma unroll
-          for (int q = 0; q < NACC; ++q) gb[q] = a[q][j];
-          out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eBs[c0 + j]);
+          for (int tt = 0; tt + s < S; ++tt) {
+            const uint64_t bd = tc::sdesc_interleave(tc::smem_u32(sB(st, tt)), C::LBO_B, SBO);
+            const int acc = s + tt < NACC - 1 ? s + tt : NACC - 1;
+            tc::mma_f16(dbase + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
+            inited |= 1u << acc;
+          }
         }
+        tc::mma_commit(&empty[st]);  // frees the stage once these MMAs have read it
+      }
+      tc::mma_commit(&tfull[b]);  // set b final (also after an early exit)
+    }
+    tc::mma_commit(mdone);
+  } else if (warp >= 4) {
+    // epilogue
+    const int quarter = warp & 3, part = (warp >> 2) - 1;  // part 0..2: columns 16 part .. +15
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    const int64_t ostride = g.inner * (g.cplx ? 2 : 1);
+    int64_t i = 0;
+    for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x, ++i) {
+      const int nt = (int)(t % g.ntiles), mt = (int)(t / g.ntiles);
+      const int b = (int)(i & 1);
+      // a warp-uniform outcome keeps the .sync.aligned loads below convergent
+      const bool got = __all_sync(0xffffffffu, tc::mbar_wait_sleep(&tfull[b], (uint32_t)(i >> 1) & 1u));
+      if (!got) ok = false;
+      tc::fence_after_sync();
+      uint32_t a[2][NACC][8];
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int qq = 0; qq < NACC; ++qq)
+          tc::tmem_ld8(tmem + lane_base + (uint32_t)(b * NACC * BN + qq * BN + part * 16 + h * 8), a[h][qq]);
+      tc::tmem_ld_wait();
+      // the set may be refilled as soon as every epilogue warp has read it
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tempty[b]);
+      if (!ok) break;
+      const int64_t row = (int64_t)mt * BM + quarter * 32 + lane;
+      if (row < g.nrows) {
+        const int erow = eA[row] - 2 * W;
+        const int64_t obase = row_offset(g, row, 0);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int col = nt * BN + part * 16 + h * 8 + j;
+            if (col < g.N) {
+              uint32_t gb[NACC];
+#pragma unroll
+              for (int qq = 0; qq < NACC; ++qq) gb[qq] = a[h][qq][j];
+              out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eB[col]);
+            }
+          }
       }
     }
-    __syncwarp();
   }
+  // every MMA must have completed before TMEM is released
+  __syncwarp();
+  if (warp == 0 && !tc::mbar_wait_sleep(mdone, 0)) ok = false;
   tc::fence_before_sync();
   __syncthreads();
   if (!ok && lane == 0) atomicAdd(&g_oz_timeouts, 1u);
@@ -266,8 +299,15 @@ static int run(const Matrix& m, const Geom& g, const double* in, double* out, vo
   const int64_t nrow_pad = (int64_t)g.mtiles * BM;
   k_oz_rowexp<<<(unsigned)((nrow_pad * 32 + 255) / 256), 256, 0, stream>>>(in, eA, g);
   k_oz_split<C::S><<<(unsigned)((int64_t)g.mtiles * g.nkb), 256, C::S * A_BYTES, stream>>>(in, eA, At, g);
-  k_oz_gemm<C><<<(unsigned)((int64_t)g.mtiles * g.ntiles), GEMM_THREADS, GemmSmem<C>::bytes, stream>>>(
-      At, eA, m.tiles, m.exps, out, g);
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      nsm = 148;
+  }
+  const int64_t ntile = (int64_t)g.mtiles * g.ntiles;
+  const unsigned nctas = (unsigned)(ntile < nsm ? ntile : nsm);
+  k_oz_gemm<C><<<nctas, GEMM_THREADS, GemmSmem<C>::bytes, stream>>>(At, eA, m.tiles, m.exps, out, g);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
