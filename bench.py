@@ -8,9 +8,11 @@ batched Helmholtz solve (33,024 band systems, one per (kx, ky)) -> backward
 transform.  The factorisation is set-up work (done once, as in shenfun).
 
 Two arithmetic forms are measured on the same input: the plain form (all
-FP64) and the mixed ("chosen") form (double-float arithmetic on the FP32
-pipes, FP64 in and out).  ``value`` is the mixed form's throughput when its
-error against the FP64 oracle is within 1e-10, else the plain form's.
+FP64) and the mixed ("chosen") form (FP64 in and out: the Fourier axes in
+double-float arithmetic on the FP32 pipes, the Chebyshev axis as split-BF16
+contractions on the tensor cores, the banded solve in FP64).  ``value`` is the
+mixed form's throughput when its error against the FP64 oracle is within
+1e-10, else the plain form's.
 
 Prints one JSON line.  ``--impl reference`` times the reference's CPU path
 (its compiled Cython Helmholtz kernels when built in oracle/_ref, transforms

@@ -51,19 +51,24 @@ const int SBO = 128;                    // row-direction core-matrix stride (byt
 // A digit configuration: S digits per operand, products with s + t <= S - 1,
 // NACC FP32 accumulators (groups 0..NACC-2 separately, the rest combined) and
 // BN output columns per tile (NACC * BN <= 512 TMEM columns).
-// Two accumulator sets (2 NACC BN <= 512 TMEM columns) let the epilogue of
-// one tile overlap the main loop of the next.
+// NBUF accumulator sets: with two (2 NACC BN <= 512 TMEM columns) the
+// epilogue of one tile overlaps the main loop of the next; with one the
+// producer still prefetches the next tile's operands during the epilogue.
+// Wider tiles read the A operand from shared memory less often per flop
+// (measured on the channel grid's z axis: BN = 96 with one set beat BN = 48
+// with two).
 template <int S_, int NACC_, int BN_>
 struct Cfg {
   static const int S = S_, NACC = NACC_, BN = BN_;
+  static const int NBUF = 2 * NACC * BN <= 512 ? 2 : 1;
   static const int B_ELEMS = BN * BK, B_BYTES = B_ELEMS * 2;
   static const int LBO_B = BN * 16;
   static const int NPROD = S * (S + 1) / 2;
-  static_assert(2 * NACC * BN <= 512, "two accumulator sets exceed TMEM");
+  static_assert(NACC * BN <= 512, "accumulators exceed TMEM");
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "MMA N");
 };
 // 7 digits (48 bits), 28 products, groups 0..3 exact: normwise ~1e-13
-typedef Cfg<7, 5, 48> CfgStd;
+typedef Cfg<7, 5, 96> CfgStd;
 
 // index of element (row r, k in the K block) inside a block of `rows` rows:
 // [k / 8][r / 8][r % 8][k % 8]
@@ -221,7 +226,8 @@ SGPU_HD double combine_groups(const uint32_t (&gb)[NACC], int E) {
 struct Geom {
   int64_t nrows;   // rows of A (lines x (1 + cplx))
   int64_t inner;
-  int N;           // line length (= K = Nout)
+  int N;           // line length (= Nout, and the K extent of the tiles)
+  int K;           // leading input entries the matrix uses (its other rows are zero)
   int cplx;
   int nkb;         // K blocks of BK (K padded with zeros)
   int mtiles;      // row tiles of BM
@@ -241,9 +247,10 @@ inline size_t a_split_bytes(const Geom& g, int S) {
   return (size_t)S * g.mtiles * g.nkb * A_BYTES + (size_t)g.mtiles * BM * sizeof(int);
 }
 
-inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx, int BN) {
+inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx, int BN, int K) {
   Geom g;
   g.N = N;
+  g.K = K;
   g.inner = inner;
   g.cplx = cplx;
   g.nrows = nlines * (1 + cplx);
@@ -254,11 +261,13 @@ inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx, int BN) {
 }
 
 // largest exponent field of row `row` over the lanes' strided share
-// (lane, lane + nlane, ...); rows past nrows give 0
+// (lane, lane + nlane, ...) of the K entries the matrix uses (entries it
+// ignores, such as the boundary dofs a backward transform skips, must not
+// set the scale); rows past nrows give 0
 SGPU_HD uint32_t rowexp_partial(const double* in, const Geom& g, int64_t row, int lane, int nlane) {
   uint32_t mf = 0;
   if (row < g.nrows)
-    for (int j = lane; j < g.N; j += nlane) {
+    for (int j = lane; j < g.K; j += nlane) {
       const uint32_t f = exp_field(in[row_offset(g, row, j)]);
       mf = f > mf ? f : mf;
     }
@@ -290,7 +299,7 @@ SGPU_HD void split_block(const double* in, const int* eA, uint16_t* At, const Ge
     if (row < g.nrows) {
       const int64_t base = row_offset(g, row, 0);
       const int64_t st = g.inner * (g.cplx ? 2 : 1);
-      for (int q = 0; q < 8; ++q) x[q] = k0 + q < g.N ? in[base + (int64_t)(k0 + q) * st] : 0.0;
+      for (int q = 0; q < 8; ++q) x[q] = k0 + q < g.K ? in[base + (int64_t)(k0 + q) * st] : 0.0;
     } else {
       for (int q = 0; q < 8; ++q) x[q] = 0.0;
     }

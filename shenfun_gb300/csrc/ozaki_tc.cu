@@ -60,10 +60,11 @@ static_assert(GemmSmem<CfgStd>::need <= 232448, "stages exceed shared memory");
 // operands' half blocks through the STAGES-deep ring for every tile this CTA
 // owns (tiles blockIdx.x, blockIdx.x + gridDim.x, ...; output-column tiles
 // fastest so that concurrent CTAs share row tiles in L2); warp 1 lane 0
-// issues the MMAs of tile i into accumulator set i % 2; warps 4..15 run the
-// epilogue of tile i (warp w reads TMEM lane quarter w % 4 - the hardware
-// ties a warp to lanes 32 (w % 4) .. +31 - and 16 of the BN = 48 columns)
-// while the MMAs of tile i + 1 fill the other set.
+// issues the MMAs of tile i into accumulator set i % NBUF; warps 4..15 run
+// the epilogue of tile i (warp w reads TMEM lane quarter w % 4 - the hardware
+// ties a warp to lanes 32 (w % 4) .. +31 - and a third of the BN columns),
+// while the MMAs of tile i + 1 fill the other set (NBUF = 2) or the producer
+// prefetches its operands (NBUF = 1).
 const int GEMM_THREADS = 512;
 const int EPI_WARPS = 12;
 
@@ -71,8 +72,9 @@ template <class C>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_oz_gemm(const uint16_t* __restrict__ At, const int* __restrict__ eA, const uint16_t* __restrict__ Bt,
               const int* __restrict__ eB, double* __restrict__ out, Geom g) {
-  constexpr int S = C::S, NACC = C::NACC, BN = C::BN;
-  static_assert(BN == 3 * 16, "three epilogue warps of 16 columns per lane quarter");
+  constexpr int S = C::S, NACC = C::NACC, BN = C::BN, NBUF = C::NBUF;
+  constexpr int CW = BN / 3;  // columns per epilogue warp
+  static_assert(CW % 8 == 0, "three epilogue warps of whole 8-column chunks per lane quarter");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + GemmSmem<C>::bar_off);  // [STAGES]
@@ -147,8 +149,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     int64_t q = 0;
     int64_t i = 0;  // local tile count
     for (int64_t t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++i) {
-      const int b = (int)(i & 1);
-      const int64_t use = i >> 1;  // uses of set b before this one
+      const int b = (int)(i % NBUF);
+      const int64_t use = i / NBUF;  // uses of set b before this one
       if (use >= 1 && !tc::mbar_wait(&tempty[b], (uint32_t)(use - 1) & 1u)) {
         ok = false;
         break;
@@ -182,46 +184,47 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc::mma_commit(mdone);
   } else if (warp >= 4) {
     // epilogue
-    const int quarter = warp & 3, part = (warp >> 2) - 1;  // part 0..2: columns 16 part .. +15
+    const int quarter = warp & 3, part = (warp >> 2) - 1;  // part 0..2: columns CW part .. +CW-1
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const int64_t ostride = g.inner * (g.cplx ? 2 : 1);
     int64_t i = 0;
     for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x, ++i) {
       const int nt = (int)(t % g.ntiles), mt = (int)(t / g.ntiles);
-      const int b = (int)(i & 1);
+      const int b = (int)(i % NBUF);
       // a warp-uniform outcome keeps the .sync.aligned loads below convergent
-      const bool got = __all_sync(0xffffffffu, tc::mbar_wait_sleep(&tfull[b], (uint32_t)(i >> 1) & 1u));
+      const bool got =
+          __all_sync(0xffffffffu, tc::mbar_wait_sleep(&tfull[b], (uint32_t)(i / NBUF) & 1u));
       if (!got) ok = false;
       tc::fence_after_sync();
-      uint32_t a[2][NACC][8];
-#pragma unroll
-      for (int h = 0; h < 2; ++h)
+      const int64_t row = (int64_t)mt * BM + quarter * 32 + lane;
+      const bool row_ok = row < g.nrows;
+      const int erow = eA[row] - 2 * W;
+      const int64_t obase = row_offset(g, row_ok ? row : 0, 0);
+      for (int h = 0; h < CW / 8 && ok; ++h) {
+        uint32_t a[NACC][8];
 #pragma unroll
         for (int qq = 0; qq < NACC; ++qq)
-          tc::tmem_ld8(tmem + lane_base + (uint32_t)(b * NACC * BN + qq * BN + part * 16 + h * 8), a[h][qq]);
-      tc::tmem_ld_wait();
-      // the set may be refilled as soon as every epilogue warp has read it
+          tc::tmem_ld8(tmem + lane_base + (uint32_t)(b * NACC * BN + qq * BN + part * CW + h * 8), a[qq]);
+        tc::tmem_ld_wait();
+        if (row_ok) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int col = nt * BN + part * CW + h * 8 + j;
+            if (col < g.N) {
+              uint32_t gb[NACC];
+#pragma unroll
+              for (int qq = 0; qq < NACC; ++qq) gb[qq] = a[qq][j];
+              out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eB[col]);
+            }
+          }
+        }
+        __syncwarp();
+      }
+      // the set may be refilled once every epilogue warp has read it
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&tempty[b]);
       if (!ok) break;
-      const int64_t row = (int64_t)mt * BM + quarter * 32 + lane;
-      if (row < g.nrows) {
-        const int erow = eA[row] - 2 * W;
-        const int64_t obase = row_offset(g, row, 0);
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int col = nt * BN + part * 16 + h * 8 + j;
-            if (col < g.N) {
-              uint32_t gb[NACC];
-#pragma unroll
-              for (int qq = 0; qq < NACC; ++qq) gb[qq] = a[h][qq][j];
-              out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eB[col]);
-            }
-          }
-      }
     }
   }
   // every MMA must have completed before TMEM is released
@@ -268,6 +271,10 @@ int matrix_create(const double* M, int N, Matrix* out) {
   if (pick_digits(N) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
   out->N = N;
   out->S = CfgStd::S;
+  out->K = 0;
+  for (int k = 0; k < N; ++k)
+    for (int n = 0; n < N; ++n)
+      if (M[(size_t)k * N + n] != 0.0) out->K = k + 1;
   return matrix_create_cfg<CfgStd>(M, N, out);
 }
 
@@ -277,7 +284,7 @@ void matrix_destroy(Matrix* m) {
 }
 
 size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx) {
-  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN);
+  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN, m.K);
   return a_split_bytes(g, m.S);
 }
 
@@ -315,7 +322,7 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
              void* work, size_t work_bytes, cudaStream_t stream) {
   if (nlines == 0) return SGPU_OK;
   if (!m.tiles) return SGPU_ERR_ARG;
-  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN);
+  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN, m.K);
   // one-dimensional grids: tiles x K blocks stay below 2^31
   if ((int64_t)g.mtiles * (g.nkb > g.ntiles ? g.nkb : g.ntiles) > 0x7fffffff || (int64_t)g.mtiles * 16 > 0x7fffffff)
     return SGPU_ERR_ARG;

@@ -13,6 +13,7 @@ namespace oz {
 // split into BF16 digit slices and tiled on the device
 struct Matrix {
   int N = 0, S = 0;
+  int K = 0;                  // 1 + the last nonzero row: input entries the contraction reads
   uint16_t* tiles = nullptr;  // device: slices, then per-column exponents
   int* exps = nullptr;
 };

@@ -207,10 +207,14 @@ static int ozaki(int argc, char** argv) {
   const int N = atoi(argv[2]);
   const long long nlines = atoll(argv[3]), inner = atoll(argv[4]);
   const int cplx = atoi(argv[5]);
-  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx, oz::CfgStd::BN);
   const size_t cnt = (size_t)nlines * N * (1 + cplx);
   double* in = read_exact(argv[6], cnt);
   double* M = read_exact(argv[7], (size_t)N * N);
+  int K = 0;  // as the library: 1 + the last nonzero row of M
+  for (int k = 0; k < N; ++k)
+    for (int n = 0; n < N; ++n)
+      if (M[(size_t)k * N + n] != 0.0) K = k + 1;
+  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx, oz::CfgStd::BN, K);
   double* out = (double*)malloc(sizeof(double) * cnt);
   for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
   const int rc = ozaki_run<oz::CfgStd>(g, in, M, out);

@@ -310,3 +310,17 @@ def test_ozaki_contraction(emu, N, nlines, inner, cplx):
     assert np.abs(res - ref).max() / scale < 5e-13
     # and the all-zero line stays exactly zero
     assert np.all(res[0, :, 0] == 0)
+
+
+def test_ozaki_ignored_tail_rows(emu):
+    """A matrix whose last rows are zero (a backward transform ignores the
+    boundary dofs) must not let large values there set the line's scale."""
+    N, nlines = 53, 40
+    r = np.random.default_rng(5)
+    x = r.standard_normal((nlines, N)) * 1e-4
+    x[:, -2:] = 1e6  # ignored entries, far larger than the used ones
+    M = r.standard_normal((N, N))
+    M[-2:, :] = 0
+    res = run(emu, ["ozaki", N, nlines, 1, 0], [x, M], x.size).reshape(x.shape)
+    ref = x[:, :-2] @ M[:-2, :]
+    assert np.abs(res - ref).max() / np.abs(ref).max() < 5e-13
