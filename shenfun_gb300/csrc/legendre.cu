@@ -288,9 +288,9 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
     // normwise error ~N-fold in the high modes
     std::vector<double> F;
     forward_matrix(N, dim, K2, K4, MsL, F);
-    int st = oz::matrix_create(Ms.data(), N, &p->tc_scalar);
-    if (st == SGPU_OK) st = oz::matrix_create(F.data(), N, &p->tc_forward);
-    if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, &p->tc_back);
+    int st = oz::matrix_create(Ms.data(), N, 0, &p->tc_scalar);
+    if (st == SGPU_OK) st = oz::matrix_create(F.data(), N, 0, &p->tc_forward);
+    if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, 0, &p->tc_back);
     if (st != SGPU_OK) {
       oz::matrix_destroy(&p->tc_scalar);
       oz::matrix_destroy(&p->tc_forward);

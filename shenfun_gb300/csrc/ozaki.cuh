@@ -69,6 +69,11 @@ struct Cfg {
 };
 // 7 digits (48 bits), 28 products, groups 0..3 exact: normwise ~1e-13
 typedef Cfg<7, 5, 96> CfgStd;
+// 8 digits (55 bits), 36 products, groups 0..4 exact: normwise ~1e-15, for
+// contractions whose result a later step amplifies (the Chebyshev Dirichlet
+// Helmholtz recurrence magnifies input perturbations up to ~4000x at large
+// shifts, so its mixed form needs FP64-level transforms)
+typedef Cfg<8, 6, 80> CfgPrec;
 
 // index of element (row r, k in the K block) inside a block of `rows` rows:
 // [k / 8][r / 8][r % 8][k % 8]
@@ -95,17 +100,20 @@ SGPU_HD uint32_t exp_field(double x) {
 // representation with d_s in [-2^{W-1}, 2^{W-1}) for s >= 1.
 template <int W, int S>
 SGPU_HD void split_digits(double x, int e, uint16_t (&out)[S]) {
-  static_assert(W * S <= 52, "digits beyond the FP64 mantissa");
+  static_assert(W * S <= 60, "fixed point beyond 64 bits");
   uint64_t b;
   memcpy(&b, &x, 8);
   const int field = (int)((b >> 52) & 0x7ff);
   uint64_t X = 0;
   if (field != 0) {
     const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    // X = round(|x| 2^{WS-e}) = round(m 2^{-sh}); sh >= 54 - W*S > 0 since
-    // |x| < 2^{e-1}, and X < 2^{WS-1}
+    // X = round(|x| 2^{WS-e}) = round(m 2^{-sh}); sh >= 54 - W*S since
+    // |x| < 2^{e-1} (> 0 for 7 digits, >= -2 for 8), and X < 2^{WS-1}
     const int sh = 1075 + e - W * S - field;
-    if (sh < 64) X = (m + (1ull << (sh - 1))) >> sh;
+    if (sh <= 0)
+      X = m << (-sh);
+    else if (sh < 64)
+      X = (m + (1ull << (sh - 1))) >> sh;
   }
   int d[S];
   int carry = 0;
@@ -202,23 +210,31 @@ SGPU_HD int32_t f2i_rn(float v) {
 #endif
 }
 
-// one output element from the five FP32 accumulators (bit patterns) of digit
-// groups 0..3 and >= 4; E = eA + eB - 2W.  G_g 2^{Wg} (g <= 3) are integers
-// below 2^24 in magnitude (exact sums), G4 2^33 is below 2^31; the int64 sum
-// T = sum_g G_g 2^{33} is exact up to the rounding of G4 at 2^-33, and T 2^{E-33}
-// is assembled as FP64 bits.
+// one output element from the NACC FP32 accumulators (bit patterns) of digit
+// groups 0..NACC-2 (exact: G_g 2^{Wg} are integers below 2^24 in magnitude)
+// and >= NACC-1 (rounded); E = eA + eB - 2W.  The groups are added in 64-bit
+// fixed point T = sum_g G_g 2^F (F = 33 for five accumulators, 36 for six,
+// both keeping |T| < 2^63 for K <= 1024 and resolving the last exact group),
+// and T 2^{E-F} is assembled as FP64 bits.
 template <int NACC>
 SGPU_HD double combine_groups(const uint32_t (&gb)[NACC], int E) {
-  static_assert(NACC == 5 && W == 7, "the combination assumes 7-bit digits and five accumulators");
+  static_assert((NACC == 5 || NACC == 6) && W == 7, "five or six accumulators of 7-bit digits");
+  constexpr int F = NACC == 5 ? 33 : 36;
   float g[NACC];
   for (int i = 0; i < NACC; ++i) memcpy(&g[i], &gb[i], 4);
-  const int32_t i0 = f2i_rn(g[0]);
-  const int32_t i1 = f2i_rn(g[1] * 128.0f);
-  const int32_t i2 = f2i_rn(g[2] * 16384.0f);
-  const int32_t i3 = f2i_rn(g[3] * 2097152.0f);
-  const int32_t i4 = f2i_rn(g[4] * 8589934592.0f);  // 2^33
-  const int64_t T = ((((int64_t)i0 * 128 + i1) * 128 + i2) * 128 + i3) * 4096 + i4;
-  return fixed_to_double(T, E - 33);
+  int64_t T = f2i_rn(g[0]);
+  float sc = 1.0f;
+  for (int i = 1; i < NACC - 1; ++i) {
+    sc *= 128.0f;
+    T = T * 128 + f2i_rn(g[i] * sc);
+  }
+  // the rounded group at 2^-F: T so far is in units of 2^{-7 (NACC-2)}
+  constexpr int rest = F - 7 * (NACC - 2);
+  const uint32_t fb = (uint32_t)(127 + F) << 23;  // 2^F
+  float pF;
+  memcpy(&pF, &fb, 4);
+  T = T * ((int64_t)1 << rest) + f2i_rn(g[NACC - 1] * pF);
+  return fixed_to_double(T, E - F);
 }
 
 // geometry of one contraction over lines of a (outer, N, inner) array:

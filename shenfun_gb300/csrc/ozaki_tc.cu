@@ -55,6 +55,7 @@ struct GemmSmem {
   static const size_t bytes = need < 232448 ? 232448 : need;
 };
 static_assert(GemmSmem<CfgStd>::need <= 232448, "stages exceed shared memory");
+static_assert(GemmSmem<CfgPrec>::need <= 232448, "stages exceed shared memory");
 
 // Persistent kernel, one CTA per SM, 16 warps.  Warp 0 lane 0 streams the
 // operands' half blocks through the STAGES-deep ring for every tile this CTA
@@ -73,8 +74,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_oz_gemm(const uint16_t* __restrict__ At, const int* __restrict__ eA, const uint16_t* __restrict__ Bt,
               const int* __restrict__ eB, double* __restrict__ out, Geom g) {
   constexpr int S = C::S, NACC = C::NACC, BN = C::BN, NBUF = C::NBUF;
-  constexpr int CW = BN / 3;  // columns per epilogue warp
-  static_assert(CW % 8 == 0, "three epilogue warps of whole 8-column chunks per lane quarter");
+  static_assert(BN % 8 == 0, "8-column epilogue chunks");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + GemmSmem<C>::bar_off);  // [STAGES]
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc::mma_commit(mdone);
   } else if (warp >= 4) {
     // epilogue
-    const int quarter = warp & 3, part = (warp >> 2) - 1;  // part 0..2: columns CW part .. +CW-1
+    const int quarter = warp & 3, part = (warp >> 2) - 1;  // part 0..2: 8-column chunks part, part + 3, ...
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const int64_t ostride = g.inner * (g.cplx ? 2 : 1);
     int64_t i = 0;
@@ -200,16 +200,16 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       const bool row_ok = row < g.nrows;
       const int erow = eA[row] - 2 * W;
       const int64_t obase = row_offset(g, row_ok ? row : 0, 0);
-      for (int h = 0; h < CW / 8 && ok; ++h) {
+      for (int ch = part; ch < BN / 8 && ok; ch += 3) {
         uint32_t a[NACC][8];
 #pragma unroll
         for (int qq = 0; qq < NACC; ++qq)
-          tc::tmem_ld8(tmem + lane_base + (uint32_t)(b * NACC * BN + qq * BN + part * CW + h * 8), a[qq]);
+          tc::tmem_ld8(tmem + lane_base + (uint32_t)(b * NACC * BN + qq * BN + ch * 8), a[qq]);
         tc::tmem_ld_wait();
         if (row_ok) {
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            const int col = nt * BN + part * CW + h * 8 + j;
+            const int col = nt * BN + ch * 8 + j;
             if (col < g.N) {
               uint32_t gb[NACC];
 #pragma unroll
@@ -267,15 +267,16 @@ static int matrix_create_cfg(const double* M, int N, Matrix* out) {
   return SGPU_OK;
 }
 
-int matrix_create(const double* M, int N, Matrix* out) {
+int matrix_create(const double* M, int N, int precise, Matrix* out) {
   if (pick_digits(N) != SGPU_OK) return SGPU_ERR_UNSUPPORTED;
   out->N = N;
-  out->S = CfgStd::S;
+  out->precise = precise ? 1 : 0;
+  out->S = precise ? CfgPrec::S : CfgStd::S;
   out->K = 0;
   for (int k = 0; k < N; ++k)
     for (int n = 0; n < N; ++n)
       if (M[(size_t)k * N + n] != 0.0) out->K = k + 1;
-  return matrix_create_cfg<CfgStd>(M, N, out);
+  return precise ? matrix_create_cfg<CfgPrec>(M, N, out) : matrix_create_cfg<CfgStd>(M, N, out);
 }
 
 void matrix_destroy(Matrix* m) {
@@ -284,7 +285,7 @@ void matrix_destroy(Matrix* m) {
 }
 
 size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx) {
-  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN, m.K);
+  const Geom g = make_geom(m.N, nlines, inner, cplx, m.precise ? CfgPrec::BN : CfgStd::BN, m.K);
   return a_split_bytes(g, m.S);
 }
 
@@ -322,12 +323,12 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
              void* work, size_t work_bytes, cudaStream_t stream) {
   if (nlines == 0) return SGPU_OK;
   if (!m.tiles) return SGPU_ERR_ARG;
-  const Geom g = make_geom(m.N, nlines, inner, cplx, CfgStd::BN, m.K);
+  const Geom g = make_geom(m.N, nlines, inner, cplx, m.precise ? CfgPrec::BN : CfgStd::BN, m.K);
   // one-dimensional grids: tiles x K blocks stay below 2^31
   if ((int64_t)g.mtiles * (g.nkb > g.ntiles ? g.nkb : g.ntiles) > 0x7fffffff || (int64_t)g.mtiles * 16 > 0x7fffffff)
     return SGPU_ERR_ARG;
   if (work_bytes < a_split_bytes(g, m.S) || ((uintptr_t)work & 255)) return SGPU_ERR_ARG;
-  return run<CfgStd>(m, g, in, out, work, stream);
+  return m.precise ? run<CfgPrec>(m, g, in, out, work, stream) : run<CfgStd>(m, g, in, out, work, stream);
 }
 
 }  // namespace oz

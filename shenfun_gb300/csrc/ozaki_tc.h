@@ -14,6 +14,7 @@ namespace oz {
 struct Matrix {
   int N = 0, S = 0;
   int K = 0;                  // 1 + the last nonzero row: input entries the contraction reads
+  int precise = 0;            // 0: 7 digits (~1e-13 normwise), 1: 8 digits (~1e-15)
   uint16_t* tiles = nullptr;  // device: slices, then per-column exponents
   int* exps = nullptr;
 };
@@ -21,7 +22,7 @@ struct Matrix {
 // OK when the contraction length K keeps the FP32 sums of the exact digit
 // groups below 2^24 (K <= 1024), else UNSUPPORTED
 int pick_digits(int K);
-int matrix_create(const double* M_host, int N, Matrix* out);
+int matrix_create(const double* M_host, int N, int precise, Matrix* out);
 void matrix_destroy(Matrix* m);
 // device scratch one contraction of `nlines` lines needs (256-byte aligned)
 size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx);

@@ -11,7 +11,7 @@
 //   emu hsolve N outer inner data_kind b.bin fac.bin out.bin   (fac = d0|d1|d2|L)
 //   emu hmatvec N outer inner data_kind v.bin alfa.bin beta.bin out.bin
 //   emu tdma|pdma n outer inner data_kind raw.bin u.bin out.bin (LU then solve)
-//   emu ozaki  N nlines inner cplx in.bin M.bin out.bin       (split-BF16 contraction)
+//   emu ozaki  N nlines inner cplx precise in.bin M.bin out.bin (split-BF16 contraction)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -201,25 +201,25 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
   return 0;
 }
 
-// emu ozaki N nlines inner cplx in.bin M.bin out.bin
+// emu ozaki N nlines inner cplx precise in.bin M.bin out.bin
 static int ozaki(int argc, char** argv) {
-  if (argc < 9) return 2;
+  if (argc < 10) return 2;
   const int N = atoi(argv[2]);
   const long long nlines = atoll(argv[3]), inner = atoll(argv[4]);
-  const int cplx = atoi(argv[5]);
+  const int cplx = atoi(argv[5]), precise = atoi(argv[6]);
   const size_t cnt = (size_t)nlines * N * (1 + cplx);
-  double* in = read_exact(argv[6], cnt);
-  double* M = read_exact(argv[7], (size_t)N * N);
+  double* in = read_exact(argv[7], cnt);
+  double* M = read_exact(argv[8], (size_t)N * N);
   int K = 0;  // as the library: 1 + the last nonzero row of M
   for (int k = 0; k < N; ++k)
     for (int n = 0; n < N; ++n)
       if (M[(size_t)k * N + n] != 0.0) K = k + 1;
-  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx, oz::CfgStd::BN, K);
+  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx, precise ? oz::CfgPrec::BN : oz::CfgStd::BN, K);
   double* out = (double*)malloc(sizeof(double) * cnt);
   for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
-  const int rc = ozaki_run<oz::CfgStd>(g, in, M, out);
+  const int rc = precise ? ozaki_run<oz::CfgPrec>(g, in, M, out) : ozaki_run<oz::CfgStd>(g, in, M, out);
   if (rc) return rc;
-  write_exact(argv[8], out, cnt);
+  write_exact(argv[9], out, cnt);
   free(in);
   free(M);
   free(out);
