@@ -73,7 +73,7 @@ def build(verbose=False, force=False, extra_flags=()):
     with ThreadPoolExecutor(max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [exe, "-shared", "-o", tmp] + objs + ARCH + ["-cudart", "static"]
+    cmd = [exe, "-shared", "-o", tmp] + objs + ARCH + ["-cudart", "static", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -15,9 +15,11 @@
 // Plain form: FP64 tiled GEMM (k_line_gemm_f64).  Mixed form: the same
 // matrices split into BF16 digit slices and contracted on the tensor cores
 // (ozaki_tc.cu), about 48 bits, for N <= 1024.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "ozaki_tc.h"
@@ -27,6 +29,27 @@ using namespace sgpu;
 
 typedef long double ld_t;
 
+namespace {
+// run body(i) for i in [0, n) on up to 16 host threads (independent
+// iterations only): the plan's long-double set-up is O(N^2) and, on hosts
+// where long double is a software format, worth spreading
+template <class F>
+void parallel_for(int n, F body) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nth = std::min(n, (int)std::max(1u, std::min(hw ? hw : 1u, 16u)));
+  if (nth <= 1 || n < 64) {
+    for (int i = 0; i < n; ++i) body(i);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nth; ++t)
+    pool.emplace_back([=]() {
+      for (int i = t; i < n; i += nth) body(i);
+    });
+  for (auto& th : pool) th.join();
+}
+}  // namespace
+
 // Gauss-Legendre nodes (ascending) and weights: Newton iteration on P_N from
 // Tricomi's asymptotic initial guesses, P_N and P_N' by the three-term
 // recurrence in long double (Golub & Welsch 1969 give the same rule; the
@@ -34,7 +57,7 @@ typedef long double ld_t;
 extern "C" int sgpu_leggauss(int N, double* x, double* w) {
   if (N < 1 || !x || !w) return SGPU_ERR_ARG;
   const ld_t pi = 3.141592653589793238462643383279502884L;
-  for (int i = 0; i < (N + 1) / 2; ++i) {
+  parallel_for((N + 1) / 2, [=](int i) {
     // i-th largest root
     ld_t th = pi * (4.0L * (i + 1) - 1) / (4.0L * N + 2);
     ld_t z = cosl(th) * (1 - (N - 1.0L) / (8.0L * N * N * N));
@@ -74,7 +97,7 @@ extern "C" int sgpu_leggauss(int N, double* x, double* w) {
     x[N - 1 - i] = (double)z;
     x[i] = (double)(-z);
     w[i] = w[N - 1 - i] = (double)wt;
-  }
+  });
   if (N % 2 == 1) x[N / 2] = 0.0;
   return SGPU_OK;
 }
@@ -84,17 +107,18 @@ namespace {
 // V_jk = L_k(x_j) in long double, x from the FP64 nodes
 void vandermonde(int N, const double* x, std::vector<ld_t>& V) {
   V.assign((size_t)N * N, 0);
-  for (int j = 0; j < N; ++j) {
+  ld_t* v = V.data();
+  parallel_for(N, [=](int j) {
     ld_t z = x[j], p0 = 1, p1 = z;
-    V[(size_t)j * N + 0] = 1;
-    if (N > 1) V[(size_t)j * N + 1] = z;
+    v[(size_t)j * N + 0] = 1;
+    if (N > 1) v[(size_t)j * N + 1] = z;
     for (int k = 2; k < N; ++k) {
       ld_t p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
-      V[(size_t)j * N + k] = p2;
+      v[(size_t)j * N + k] = p2;
       p0 = p1;
       p1 = p2;
     }
-  }
+  });
 }
 
 // stencil K[k][m] (row k, offset m = 0, 2, 4) of the Legendre bases
@@ -150,9 +174,13 @@ void forward_matrix(int N, int dim, const std::vector<ld_t>& K2, const std::vect
     }
   }
   F.assign((size_t)N * N, 0.0);
-  std::vector<ld_t> y(dim);
-  for (int j = 0; j < N; ++j) {
-    for (int k = 0; k < dim; ++k) y[k] = MsL[(size_t)j * N + k];
+  double* Fp = F.data();
+  const ld_t* Ap = A.data();
+  const ld_t* Msp = MsL.data();
+  parallel_for(N, [=](int j) {
+    std::vector<ld_t> y(dim);
+    const ld_t* A = Ap;
+    for (int k = 0; k < dim; ++k) y[k] = Msp[(size_t)j * N + k];
     for (int i = 0; i < dim; ++i)
       for (int k = i - bw; k < i; ++k)
         if (k >= 0) y[i] -= A[(size_t)i * W + bw + (k - i)] * y[k];
@@ -160,8 +188,8 @@ void forward_matrix(int N, int dim, const std::vector<ld_t>& K2, const std::vect
       for (int l = i + 1; l <= i + bw && l < dim; ++l) y[i] -= A[(size_t)i * W + bw + (l - i)] * y[l];
       y[i] /= A[(size_t)i * W + bw];
     }
-    for (int k = 0; k < dim; ++k) F[(size_t)j * N + k] = (double)y[k];
-  }
+    for (int k = 0; k < dim; ++k) Fp[(size_t)j * N + k] = (double)y[k];
+  });
 }
 
 }  // namespace
@@ -203,22 +231,26 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
   // Ms[j][k] = w_j (V_jk + K2_k V_j,k+2 + K4_k V_j,k+4)
   std::vector<double> Ms((size_t)N * N), Mb((size_t)N * N, 0.0);
   std::vector<ld_t> MsL(form == SGPU_MIXED_DF ? (size_t)N * N : 0);
-  for (int j = 0; j < N; ++j)
-    for (int k = 0; k < N; ++k) {
-      ld_t v = V[(size_t)j * N + k];
-      if (k + 2 < N) v += K2[k] * V[(size_t)j * N + k + 2];
-      if (k + 4 < N) v += K4[k] * V[(size_t)j * N + k + 4];
-      Ms[(size_t)j * N + k] = (double)((ld_t)p->w[j] * v);
-      if (!MsL.empty()) MsL[(size_t)j * N + k] = (ld_t)p->w[j] * v;
-    }
-  // Mb[k][j] = V_jk + K2_k V_j,k+2 + K4_k V_j,k+4 for k < dim (rows k >= dim zero)
-  for (int k = 0; k < dim; ++k)
-    for (int j = 0; j < N; ++j) {
-      ld_t v = V[(size_t)j * N + k];
-      if (k + 2 < N) v += K2[k] * V[(size_t)j * N + k + 2];
-      if (k + 4 < N) v += K4[k] * V[(size_t)j * N + k + 4];
-      Mb[(size_t)k * N + j] = (double)v;
-    }
+  {
+    const ld_t* Vp = V.data();
+    const ld_t* K2p = K2.data();
+    const ld_t* K4p = K4.data();
+    const double* wp = p->w.data();
+    double* Msp = Ms.data();
+    double* Mbp = Mb.data();
+    ld_t* MsLp = MsL.empty() ? nullptr : MsL.data();
+    parallel_for(N, [=](int j) {
+      for (int k = 0; k < N; ++k) {
+        ld_t v = Vp[(size_t)j * N + k];
+        if (k + 2 < N) v += K2p[k] * Vp[(size_t)j * N + k + 2];
+        if (k + 4 < N) v += K4p[k] * Vp[(size_t)j * N + k + 4];
+        Msp[(size_t)j * N + k] = (double)((ld_t)wp[j] * v);
+        if (MsLp) MsLp[(size_t)j * N + k] = (ld_t)wp[j] * v;
+        // Mb[k][j] = V_jk + K2_k V_j,k+2 + K4_k V_j,k+4 for k < dim (rows k >= dim zero)
+        if (k < dim) Mbp[(size_t)k * N + j] = (double)v;
+      }
+    });
+  }
   // mass matrix (legendre/matrices.py:121-135, :179-192) LU'd with TDMA/PDMA_LU
   std::vector<double> mass;
   std::vector<ld_t> h(N);

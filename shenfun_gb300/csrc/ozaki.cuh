@@ -342,29 +342,34 @@ SGPU_HD void split_block(const double* in, const int* eA, uint16_t* At, const Ge
   }
 }
 
-// host: split a fixed N x N matrix M (out = in . M, so output column n is
-// M[:, n]) into tiled slices [S][ntiles][nkb][BN x BK] and per-column exponents
+// host: split column n of a fixed N x N matrix M (out = in . M, so output
+// column n is M[:, n]) into the tiled slices [S][ntiles][nkb][BN x BK] and its
+// exponent; the tiles start zeroed
 template <class C>
-void split_matrix_host(const double* M, int N, uint16_t* tiles, int* ex) {
+void split_matrix_column(const double* M, int N, int n, uint16_t* tiles, int* ex) {
   const int S = C::S, BN = C::BN, B_ELEMS = C::B_ELEMS;
   const int nkb = (N + BK - 1) / BK, ntiles = (N + BN - 1) / BN;
-  memset(tiles, 0, sizeof(uint16_t) * (size_t)S * ntiles * nkb * B_ELEMS);
-  memset(ex, 0, sizeof(int) * (size_t)ntiles * BN);
-  for (int n = 0; n < N; ++n) {
-    uint32_t mf = 0;
-    for (int k = 0; k < N; ++k) {
-      const uint32_t f = exp_field(M[(size_t)k * N + n]);
-      mf = f > mf ? f : mf;
-    }
-    ex[n] = exp_from_field(mf);
-    const int nt = n / BN, r = n % BN;
-    for (int k = 0; k < N; ++k) {
-      uint16_t d[C::S];
-      split_digits<W, C::S>(M[(size_t)k * N + n], ex[n], d);
-      for (int s = 0; s < S; ++s)
-        tiles[(((size_t)s * ntiles + nt) * nkb + k / BK) * B_ELEMS + tile_index(BN, r, k % BK)] = d[s];
-    }
+  uint32_t mf = 0;
+  for (int k = 0; k < N; ++k) {
+    const uint32_t f = exp_field(M[(size_t)k * N + n]);
+    mf = f > mf ? f : mf;
   }
+  ex[n] = exp_from_field(mf);
+  const int nt = n / BN, r = n % BN;
+  for (int k = 0; k < N; ++k) {
+    uint16_t d[C::S];
+    split_digits<W, C::S>(M[(size_t)k * N + n], ex[n], d);
+    for (int s = 0; s < S; ++s)
+      tiles[(((size_t)s * ntiles + nt) * nkb + k / BK) * B_ELEMS + tile_index(BN, r, k % BK)] = d[s];
+  }
+}
+
+template <class C>
+void split_matrix_host(const double* M, int N, uint16_t* tiles, int* ex) {
+  const int nkb = (N + BK - 1) / BK, ntiles = (N + C::BN - 1) / C::BN;
+  memset(tiles, 0, sizeof(uint16_t) * (size_t)C::S * ntiles * nkb * C::B_ELEMS);
+  memset(ex, 0, sizeof(int) * (size_t)ntiles * C::BN);
+  for (int n = 0; n < N; ++n) split_matrix_column<C>(M, N, n, tiles, ex);
 }
 
 template <class C>

@@ -12,8 +12,10 @@
 //                 FP64 bits -> global).
 // The split matrix operand (B) is built once on the host with the same digit
 // code and uploaded with the plan.
+#include <algorithm>
 #include <cstdio>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "ozaki.cuh"
@@ -248,7 +250,16 @@ template <class C>
 static int matrix_create_cfg(const double* M, int N, Matrix* out) {
   std::vector<uint16_t> tiles(matrix_tile_elems<C>(N));
   std::vector<int> ex((size_t)((N + C::BN - 1) / C::BN) * C::BN);
-  split_matrix_host<C>(M, N, tiles.data(), ex.data());
+  // columns split independently: spread them over the host's cores (the
+  // plan's set-up cost grows as N^2 x digits)
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nth = (int)std::max(1u, std::min(hw ? hw : 1u, 16u));
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nth; ++t)
+    pool.emplace_back([&, t]() {
+      for (int n = t; n < N; n += nth) split_matrix_column<C>(M, N, n, tiles.data(), ex.data());
+    });
+  for (auto& th : pool) th.join();
   const size_t tb = tiles.size() * sizeof(uint16_t), eb = ex.size() * sizeof(int);
   void* dev = nullptr;
   if (cudaMalloc(&dev, tb + eb) != cudaSuccess) {
