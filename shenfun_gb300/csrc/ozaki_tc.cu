@@ -6,10 +6,10 @@
 //   k_oz_gemm     persistent, one CTA per SM over 128 x BN output tiles: a
 //                 producer thread streams 2S slice half blocks per K step with
 //                 bulk copies, one thread issues tcgen05.mma for the S(S+1)/2
-//                 slice products into NACC TMEM accumulators (two sets, so
-//                 that the next tile's MMAs overlap this tile's epilogue), and
-//                 twelve warps run the integer epilogue (TMEM -> registers ->
-//                 FP64 bits -> global).
+//                 slice products into NACC TMEM accumulators (two sets where
+//                 TMEM holds them, so that the next tile's MMAs overlap this
+//                 tile's epilogue), and twelve warps run the integer epilogue
+//                 (TMEM -> registers -> FP64 bits -> global).
 // The split matrix operand (B) is built once on the host with the same digit
 // code and uploaded with the plan.
 #include <algorithm>
