@@ -307,6 +307,52 @@ def legendre_leg(torch, flush, st, N=512, lines=16384, reps=5):
     return out
 
 
+def imex_leg(torch, steps=10):
+    """IMEX time stepping on the channel grid (the caller of the path,
+    utilities/integrators.py:702-900): IMEXRK443 for u_t = nu lap(u) + u^2,
+    nu = 1e-3, dt = 1e-3, mixed form; the nonlinear term through the
+    transforms (backward, square, scalar product) at every stage, then the
+    stage's Helmholtz solve.  Per step: eager launches vs one CUDA-graph
+    replay."""
+    import shenfun_gb300 as sg
+    from shenfun_gb300 import integrators as I
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(NX, "F", dtype="D"), sg.FunctionSpace(NY, "F", dtype="d"),
+                                     sg.FunctionSpace(NZ, "C", bc=(0, 0))), form="mixed")
+    v = sg.TestFunction(T)
+    work = sg.Array(T)
+
+    def N(u_hat, out):
+        T.backward(u_hat.v, work.v)
+        work.v.mul_(work.v)
+        T.scalar_product(work.v, out)
+
+    a = sg.Array(T)
+    a.v.copy_(0.1 * torch.randn(a.shape, dtype=torch.float64, device="cuda"))
+    u_hat = a.forward()
+    sol = I.IMEXRK443(v, u_hat, lambda u: 1e-3 * sg.div(sg.grad(u)), N, 1e-3)
+    sol.assemble()
+    st = torch.cuda.current_stream()
+    out = {"scheme": "IMEXRK443", "stages": 4, "workload": "channel grid, mixed form, N = u^2"}
+    for mode in ("eager", "graph"):
+        if mode == "graph":
+            sol.capture_step(warmup=2)
+            fn = sol.replay
+        else:
+            fn = sol.step
+            fn()
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            fn()
+        e1.record(st)
+        e1.synchronize()
+        out[f"ms_per_step_{mode}"] = e0.elapsed_time(e1) / steps
+    out["finite"] = bool(torch.isfinite(u_hat.v).all().item())
+    return out
+
+
 CASES = {
     # one transform of the channel grid, for profiler captures:  name -> (kind, form)
     "r2c-plain": ("r2c", "plain"), "r2c-mixed": ("r2c", "mixed"),
@@ -468,10 +514,11 @@ def main():
     b.synchronize()
     e2e_val = ws * e2e_steps / (a.elapsed_time(b) / 1e3)
 
-    serving = legendre = None
+    serving = legendre = imex = None
     if rank == 0 and not args.no_extra:
         serving = serving_leg(torch)
         legendre = legendre_leg(torch, flush, st)
+        imex = imex_leg(torch)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -504,6 +551,7 @@ def main():
             "clocks": clk.summary(),
             "serving": serving,
             "legendre": legendre,
+            "imex": imex,
         }
         print(json.dumps(out))
     if dist is not None:

@@ -18,6 +18,7 @@ from .spaces import FunctionSpace, TensorProductSpace, R2C, C2C  # noqa: F401
 from .forms import (Array, Function, TestFunction, TrialFunction, inner, project,  # noqa: F401
                     div, grad, Dx, TPMatrix)
 from . import la, chebyshev  # noqa: F401
+from .integrators import PDEIMEXRK, IMEXRK011, IMEXRK111, IMEXRK222, IMEXRK443  # noqa: F401
 
 comm = None  # single GPU, single process: no MPI communicator
 

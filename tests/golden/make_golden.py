@@ -286,12 +286,43 @@ def legendre():
     put("legendre", p2d_fj=fj, p2d_fhat=f_hat, p2d_uhat=u_hat, p2d_uq=u_hat.backward())
 
 
+# --------------------------------------------------------------------------
+# IMEX Runge-Kutta time stepping of u_t = nu lap(u) + f (utilities/integrators.py:702-900)
+# on C2C x R2C x ShenDirichlet, with a fixed spectral forcing f_hat as the
+# "nonlinear" term; three steps of each scheme from the same start.  Own rng,
+# so that the other fixtures keep their draws.
+def imex():
+    from shenfun.utilities.integrators import IMEXRK111, IMEXRK222, IMEXRK443
+    r = np.random.default_rng(31)
+    T = TensorProductSpace(comm, (FunctionSpace(8, "F", dtype="D"), FunctionSpace(8, "F", dtype="d"),
+                                  FunctionSpace(17, "C", bc=(0, 0))))
+    nu, dt = 0.05, 0.01
+    a = Array(T)
+    a[:] = r.standard_normal(a.shape)
+    u_hat0 = a.forward()
+    a[:] = r.standard_normal(a.shape)
+    f_hat = a.forward()
+    d = {"u_hat0": u_hat0.copy(), "f_hat": f_hat.copy(), "nu": nu, "dt": dt}
+    for cls in (IMEXRK111, IMEXRK222, IMEXRK443):
+        u_hat = Function(T)
+        u_hat[:] = u_hat0
+        sol = cls(TestFunction(T), u_hat, lambda u: nu * div(grad(u)), f_hat, dt)
+        sol.assemble()
+        for step in range(3):
+            for rk in range(sol.steps()):
+                sol.compute_rhs(rk)
+                sol.solve_step(rk)
+            d[f"{cls.__name__}_step{step}"] = u_hat.copy()
+    put("imex", **d)
+
+
+GROUPS = {"cheb_1d": cheb_1d, "fourier_1d": fourier_1d, "banded": banded, "helmholtz": helmholtz,
+          "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex}
+
 if __name__ == "__main__":
-    cheb_1d()
-    fourier_1d()
-    banded()
-    helmholtz()
-    roundtrips()
-    biharmonic()
-    legendre()
+    # no arguments: every group (the shared rng makes the earlier groups depend
+    # on their order); with names: only those groups (those with their own rng
+    # reproduce exactly)
+    for name in (sys.argv[1:] or list(GROUPS)):
+        GROUPS[name]()
     save()

@@ -138,3 +138,16 @@ def test_legendre_poisson2d(golden):
     fs, shp = P._systems(d["p2d_fhat"], 1)
     us = la.leg_helmholtz_solve(fs, np.ones(fs.shape[0]), beta.reshape(-1))
     assert rel(np.moveaxis(us.reshape(shp), -1, 1), d["p2d_uhat"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["IMEXRK111", "IMEXRK222", "IMEXRK443"])
+def test_imex_oracle(golden, name):
+    """IMEX Runge-Kutta steps of u_t = nu lap(u) + f on C2C x R2C x SD
+    (utilities/integrators.py:702-900) against the reference's own run."""
+    from oracle import imex
+    d = golden("imex")
+    bases = [("fourier", "C2C", 8), ("fourier", "R2C", 8), ("chebyshev", "SD", 17)]
+    out = imex.imex_run(d["u_hat0"], d["f_hat"], float(d["nu"]), float(d["dt"]), name, 3, bases, 2)
+    for step in range(3):
+        ref = d[f"{name}_step{step}"]
+        assert np.abs(out[step] - ref).max() / np.abs(ref).max() < 1e-13
