@@ -109,6 +109,19 @@ int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64
                          int64_t inner, int data_kind, double scale, void* work, size_t work_bytes,
                          cudaStream_t stream);
 
+/* ---- padded (3/2-rule dealiased) Fourier transforms ---------------------
+ * FourierBase._padding_backward / _truncation_forward (fourier/bases.py:409-435
+ * R2C, :570-598 C2C) on complex (outer, n, inner) arrays: pad N spectral
+ * coefficients (N/2+1 for R2C) to M (M/2+1), or truncate M back to N, with the
+ * reference's handling of an even N's Nyquist coefficient.  kind is
+ * SGPU_XF_R2C/C2R or SGPU_XF_C2C_FWD/BWD; in and out must not alias.  A padded
+ * backward transform is pad + the length-M plan; a padded forward one is the
+ * length-M plan with scale 1/M + truncate. */
+int sgpu_fourier_pad(const void* in, void* out, int64_t outer, int N, int M, int64_t inner, int kind,
+                     cudaStream_t stream);
+int sgpu_fourier_truncate(const void* in, void* out, int64_t outer, int N, int M, int64_t inner, int kind,
+                          cudaStream_t stream);
+
 /* ---- banded solvers (optimization/cython/la.pyx) ------------------------
  * TDMA: offsets (-2, 0, 2); data is (3, n): data[0,:-2] = ld, data[1] = d,
  * data[2,2:] = ud (la.py:331-393).  PDMA: offsets (-4..4) in (5, n) rows

@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import require_cuda
+from .device import require_cuda, ptr, stream_handle, view3
 from .plans import get_plan
 
 
@@ -74,20 +74,73 @@ class SpectralBase:
 
 # ---------------------------------------------------------------------------
 class FourierBase(SpectralBase):
-    """fourier/bases.py:44-279."""
+    """fourier/bases.py:44-279.  With ``padding_factor`` > 1 the physical
+    grid has M = floor(padding_factor N) points: backward pads the N
+    coefficients (sgpu_fourier_pad) and runs the length-M inverse transform,
+    forward / scalar_product run the length-M transform scaled by 1/M and
+    truncate (sgpu_fourier_truncate) - the 3/2-rule dealiasing of
+    fourier/bases.py:409-435, 570-598."""
 
     family_name = "fourier"
 
-    def __init__(self, N, dtype, domain=(0.0, 2 * np.pi)):
+    def __init__(self, N, dtype, domain=(0.0, 2 * np.pi), padding_factor=1):
         SpectralBase.__init__(self, N, dtype)
         self.domain = Domain(domain)
+        self.padding_factor = padding_factor
+
+    @property
+    def M(self):
+        """points of the (padded) physical grid"""
+        return int(np.floor(self.padding_factor * self.N))
+
+    @property
+    def padded(self):
+        return self.M != self.N
+
+    def get_dealiased(self, padding_factor=1.5, **kw):
+        b = copy.copy(self)
+        b.padding_factor = padding_factor
+        return b
+
+    def _spectral_len(self, n):
+        return n
+
+    def _fwd(self, kind, input_array, output_array, axis):
+        """forward / scalar product, padded or not"""
+        require_cuda()
+        ax = self.axis if axis is None else axis
+        out = self._out(input_array, True, output_array, ax)
+        if not self.padded:
+            return get_plan(kind, self.N, form=self.form)(input_array, out, ax, 1.0 / self.N)
+        shape = list(input_array.shape)
+        shape[ax % len(shape)] = self._spectral_len(self.M)
+        work = torch.empty(shape, dtype=torch.complex128, device=input_array.device)
+        get_plan(kind, self.M, form=self.form)(input_array, work, ax, 1.0 / self.M)
+        outer, _, inner = view3(tuple(work.shape), ax)
+        _lib.call("sgpu_fourier_truncate", ptr(work), ptr(out), outer, self.N, self.M, inner, kind,
+                  stream_handle())
+        return out
+
+    def _bwd(self, kind, input_array, output_array, axis):
+        require_cuda()
+        ax = self.axis if axis is None else axis
+        out = self._out(input_array, False, output_array, ax)
+        if not self.padded:
+            return get_plan(kind, self.N, form=self.form)(input_array, out, ax, 1.0)
+        shape = list(input_array.shape)
+        shape[ax % len(shape)] = self._spectral_len(self.M)
+        work = torch.empty(shape, dtype=torch.complex128, device=input_array.device)
+        outer, _, inner = view3(tuple(input_array.shape), ax)
+        _lib.call("sgpu_fourier_pad", ptr(input_array), ptr(work), outer, self.N, self.M, inner, kind,
+                  stream_handle())
+        return get_plan(kind, self.M, form=self.form)(work, out, ax, 1.0)
 
     def domain_factor(self):
         a, b = self.domain
         return 2 * np.pi / (b - a)
 
     def points_and_weights(self, N=None, map_true_domain=False, **kw):
-        N = self.N if N is None else N
+        N = self.M if N is None else N
         points = np.arange(N, dtype=float) * 2 * np.pi / N
         if map_true_domain:
             points = points / self.domain_factor() + self.domain[0]
@@ -107,11 +160,14 @@ class FourierBase(SpectralBase):
 class R2C(FourierBase):
     """Real-to-complex Fourier space (fourier/bases.py:282-475)."""
 
-    def __init__(self, N, domain=(0.0, 2 * np.pi), **kw):
-        FourierBase.__init__(self, N, float, domain)
+    def __init__(self, N, domain=(0.0, 2 * np.pi), padding_factor=1, **kw):
+        FourierBase.__init__(self, N, float, domain, padding_factor)
 
     def shape(self, forward_output=True):
-        return self.N // 2 + 1 if forward_output else self.N
+        return self.N // 2 + 1 if forward_output else self.M
+
+    def _spectral_len(self, n):
+        return n // 2 + 1
 
     def wavenumbers(self, bcast=False, scaled=False, eliminate_highest_freq=False):
         k = np.fft.rfftfreq(self.N, 1.0 / self.N).astype(int)
@@ -127,25 +183,22 @@ class R2C(FourierBase):
         return torch.complex128 if forward_output else torch.float64
 
     def scalar_product(self, input_array, output_array=None, axis=None):
-        require_cuda()
-        ax = self.axis if axis is None else axis
-        out = self._out(input_array, True, output_array, ax)
-        return get_plan(_lib.XF_R2C, self.N, form=self.form)(input_array, out, ax, 1.0 / self.N)
+        return self._fwd(_lib.XF_R2C, input_array, output_array, axis)
 
     forward = scalar_product
 
     def backward(self, input_array, output_array=None, axis=None):
-        require_cuda()
-        ax = self.axis if axis is None else axis
-        out = self._out(input_array, False, output_array, ax)
-        return get_plan(_lib.XF_C2R, self.N, form=self.form)(input_array, out, ax, 1.0)
+        return self._bwd(_lib.XF_C2R, input_array, output_array, axis)
 
 
 class C2C(FourierBase):
     """Complex-to-complex Fourier space (fourier/bases.py:478-641)."""
 
-    def __init__(self, N, domain=(0.0, 2 * np.pi), **kw):
-        FourierBase.__init__(self, N, complex, domain)
+    def __init__(self, N, domain=(0.0, 2 * np.pi), padding_factor=1, **kw):
+        FourierBase.__init__(self, N, complex, domain, padding_factor)
+
+    def shape(self, forward_output=True):
+        return self.N if forward_output else self.M
 
     def wavenumbers(self, bcast=False, scaled=False, eliminate_highest_freq=False):
         k = np.fft.fftfreq(self.N, 1.0 / self.N).astype(int)
@@ -158,18 +211,12 @@ class C2C(FourierBase):
         return "C2C"
 
     def scalar_product(self, input_array, output_array=None, axis=None):
-        require_cuda()
-        ax = self.axis if axis is None else axis
-        out = self._out(input_array, True, output_array, ax)
-        return get_plan(_lib.XF_C2C_FWD, self.N, form=self.form)(input_array, out, ax, 1.0 / self.N)
+        return self._fwd(_lib.XF_C2C_FWD, input_array, output_array, axis)
 
     forward = scalar_product
 
     def backward(self, input_array, output_array=None, axis=None):
-        require_cuda()
-        ax = self.axis if axis is None else axis
-        out = self._out(input_array, False, output_array, ax)
-        return get_plan(_lib.XF_C2C_BWD, self.N, form=self.form)(input_array, out, ax, 1.0)
+        return self._bwd(_lib.XF_C2C_BWD, input_array, output_array, axis)
 
 
 # ---------------------------------------------------------------------------
@@ -282,9 +329,10 @@ def FunctionSpace(N, family="Fourier", bc=None, dtype="d", quad=None, domain=Non
     fam = family.lower()
     if fam in ("f", "fourier"):
         dom = domain if domain is not None else (0.0, 2 * np.pi)
+        pf = kw.get("padding_factor", 1)
         if np.dtype(dtype).char in "FDG":
-            return C2C(N, domain=dom)
-        return R2C(N, domain=dom)
+            return C2C(N, domain=dom, padding_factor=pf)
+        return R2C(N, domain=dom, padding_factor=pf)
     nb = 0 if bc is None else len(bc)
     if bc is not None and any(v != 0 for v in bc):
         raise NotImplementedError("only homogeneous boundary conditions are on the GPU path")
@@ -374,6 +422,24 @@ class TensorProductSpace:
         self.backward = _Chain(self, "backward")
         self.scalar_product = _Chain(self, "scalar_product")
         self._work = {}
+
+    def get_dealiased(self, padding_factor=1.5, dealias_direct=False, **kw):
+        """The space with padded Fourier axes (3/2-rule dealiasing,
+        tensorproductspace.py:543): one factor for every axis or a tuple.
+        Polynomial axes keep factor 1 (padding them is not on the GPU path)."""
+        if dealias_direct:
+            raise NotImplementedError("dealias_direct (2/3-rule truncation) is not on the GPU path")
+        nd = len(self.bases)
+        fac = tuple(padding_factor) if isinstance(padding_factor, (tuple, list)) else (padding_factor,) * nd
+        bases = []
+        for b, f in zip(self.bases, fac):
+            if isinstance(b, FourierBase):
+                bases.append(b.get_dealiased(f))
+            elif f == 1:
+                bases.append(copy.copy(b))
+            else:
+                raise NotImplementedError("padding along polynomial axes")
+        return TensorProductSpace(self.comm, bases, axes=self.axes, dtype=self._dtype, form=self.form)
 
     # -- meta ----------------------------------------------------------------
     def __len__(self):

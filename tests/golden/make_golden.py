@@ -316,8 +316,39 @@ def imex():
     put("imex", **d)
 
 
+# --------------------------------------------------------------------------
+# Padded (3/2-rule) transforms on the Fourier axes (TensorProductSpace.get_dealiased,
+# tensorproductspace.py:543; fourier/bases.py:409-435, 570-598): backward of
+# spectral data onto the padded grid, forward of padded-grid data, for even
+# and odd Fourier lengths.  Own rng.
+def dealias():
+    r = np.random.default_rng(43)
+    d = {}
+    for (Nx, Ny, Nz) in ((8, 8, 17), (9, 7, 12)):
+        T = TensorProductSpace(comm, (FunctionSpace(Nx, "F", dtype="D"), FunctionSpace(Ny, "F", dtype="d"),
+                                      FunctionSpace(Nz, "C", bc=(0, 0))))
+        TD = T.get_dealiased((1.5, 1.5, 1))
+        a = Array(T)
+        a[:] = r.standard_normal(a.shape)
+        u_hat = a.forward()
+        up = Array(TD)
+        up = TD.backward(u_hat, up)
+        b = Array(TD)
+        b[:] = r.standard_normal(b.shape)
+        fh = Function(TD)
+        fh = TD.forward(b, fh)
+        sh = Function(TD)
+        sh = TD.scalar_product(b, sh)
+        tag = f"{Nx}x{Ny}x{Nz}"
+        d.update({f"{tag}_u_hat": u_hat.copy(), f"{tag}_padded_backward": up.copy(),
+                  f"{tag}_padded_in": b.copy(), f"{tag}_padded_forward": fh.copy(),
+                  f"{tag}_padded_scalar": sh.copy()})
+    put("dealias", **d)
+
+
 GROUPS = {"cheb_1d": cheb_1d, "fourier_1d": fourier_1d, "banded": banded, "helmholtz": helmholtz,
-          "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex}
+          "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex,
+          "dealias": dealias}
 
 if __name__ == "__main__":
     # no arguments: every group (the shared rng makes the earlier groups depend

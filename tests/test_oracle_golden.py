@@ -151,3 +151,21 @@ def test_imex_oracle(golden, name):
     for step in range(3):
         ref = d[f"{name}_step{step}"]
         assert np.abs(out[step] - ref).max() / np.abs(ref).max() < 1e-13
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 17), (9, 7, 12)])
+def test_dealias_oracle(golden, shape):
+    """Padded (3/2-rule) Fourier transforms (get_dealiased((1.5, 1.5, 1)))
+    against the reference: backward onto the padded grid, forward and scalar
+    product from it, even and odd Fourier lengths."""
+    from oracle import dealias as D
+    d = golden("dealias")
+    tag = "%dx%dx%d" % shape
+    bases = [("fourier", "C2C", shape[0]), ("fourier", "R2C", shape[1]), ("chebyshev", "SD", shape[2])]
+    fac = (1.5, 1.5, 1)
+    up = D.padded_backward(d[f"{tag}_u_hat"], bases, fac)
+    assert np.abs(up - d[f"{tag}_padded_backward"]).max() < 1e-13 * np.abs(up).max()
+    fh = D.padded_forward(d[f"{tag}_padded_in"], bases, fac)
+    assert np.abs(fh - d[f"{tag}_padded_forward"]).max() < 1e-13 * np.abs(fh).max()
+    sh = D.padded_forward(d[f"{tag}_padded_in"], bases, fac, scalar=True)
+    assert np.abs(sh - d[f"{tag}_padded_scalar"]).max() < 1e-13 * np.abs(sh).max()
