@@ -52,8 +52,8 @@ class _HelmholtzForm:
                 alfa = alfa + m.scale
             else:
                 beta = beta + m.scale
-        self.alfa = torch.as_tensor(np.ascontiguousarray(np.broadcast_to(alfa, shape)), device="cuda")
-        self.beta = torch.as_tensor(np.ascontiguousarray(np.broadcast_to(beta, shape)), device="cuda")
+        self.alfa = torch.as_tensor(np.array(np.broadcast_to(alfa, shape), dtype=float), device="cuda")
+        self.beta = torch.as_tensor(np.array(np.broadcast_to(beta, shape), dtype=float), device="cuda")
         self.axis = ax
 
     def __call__(self, v, c):
