@@ -131,6 +131,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_total_ms(tot_ms, dist=None, device="cpu"):
+    """Replicas only (every rank solves its own copy, no data-path
+    collective): the job's time is the slowest rank's."""
+    if dist is None:
+        return float(tot_ms)
+    import torch
+    t = torch.tensor([float(tot_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def agree(obj, dist=None):
+    """Rank 0's decision on every rank (the error check runs on rank 0)."""
+    if dist is None:
+        return obj
+    box = [obj]
+    dist.broadcast_object_list(box, src=0)
+    return box[0]
+
+
 def setup_dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -453,11 +473,7 @@ def main():
                 run.step()
             barrier()
             ts_ms = time_steps_gpu(torch, run.step, args.steps, flush, st)
-            tot_ms = float(ts_ms.sum())
-            if dist is not None:
-                t = torch.tensor([tot_ms], device=dev)
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-                tot_ms = float(t.item())
+            tot_ms = replica_total_ms(float(ts_ms.sum()), dist, dev)
             err = None
             if ref is not None:
                 got = run.uq.v.cpu().numpy()
@@ -467,8 +483,8 @@ def main():
                              "p99_ms": float(np.percentile(ts_ms, 99)),
                              "rel_err_vs_oracle": err,
                              "achieved_roundtrip_GBs": ROUNDTRIP_BYTES / (tot_ms / args.steps / 1e3) / 1e9}
-    chosen = "mixed" if (results["mixed"]["rel_err_vs_oracle"] is not None and
-                         results["mixed"]["rel_err_vs_oracle"] <= MIXED_TOL) else "plain"
+    chosen = agree("mixed" if (results["mixed"]["rel_err_vs_oracle"] is not None and
+                               results["mixed"]["rel_err_vs_oracle"] <= MIXED_TOL) else "plain", dist)
     run = runs[chosen]
     for name in runs:
         results[name]["stage_ms"] = stage_times(torch, runs[name], flush, st)
