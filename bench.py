@@ -327,6 +327,83 @@ def legendre_leg(torch, flush, st, N=512, lines=16384, reps=5):
     return out
 
 
+def biharmonic_leg(torch, flush, st, steps=10):
+    """Fourier 128 (C2C) x Fourier 128 (R2C) x Chebyshev ShenBiharmonic 129:
+    scalar product of a random RHS (seed 0) -> biharmonic solve (8,320
+    banded + rank-2 semiseparable systems) -> backward, both forms, L2
+    flushed before every step; error of each form against the plain one."""
+    import shenfun_gb300 as sg
+    Nx, Ny, Nz = 128, 128, 129
+    f = np.random.default_rng(0).standard_normal((Nx, Ny, Nz))
+    out = {"workload": "Fourier 128 (C2C) x Fourier 128 (R2C) x Chebyshev ShenBiharmonic 129, RHS N(0,1) seed 0"}
+    ref = None
+    for form in ("plain", "mixed"):
+        T = sg.TensorProductSpace(None, (sg.FunctionSpace(Nx, "F", dtype="D"), sg.FunctionSpace(Ny, "F", dtype="d"),
+                                         sg.FunctionSpace(Nz, "C", bc=(0, 0, 0, 0))), form=form)
+        u, v = sg.TrialFunction(T), sg.TestFunction(T)
+        H = sg.chebyshev.la.Biharmonic(sg.inner(v, sg.div(sg.grad(sg.div(sg.grad(u))))))
+        fj = sg.Array(T, buffer=f)
+        f_hat, u_hat, uq = sg.Function(T), sg.Function(T), sg.Array(T)
+
+        def step():
+            sg.inner(v, fj, output_array=f_hat)
+            H(f_hat, u_hat)
+            T.backward(u_hat.v, uq.v)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        ms = float(np.mean(time_steps_gpu(torch, step, steps, flush, st)))
+        res = {"ms_per_step": ms, "solves_per_s": 1e3 / ms}
+        if ref is None:
+            ref = uq.v.clone()
+        else:
+            res["rel_err_vs_plain"] = float(((uq.v - ref).abs().max() / ref.abs().max()).item())
+        out[form] = res
+    return out
+
+
+def latency_leg(torch, reps=200):
+    """Small 2D Poisson on Fourier 64 x Chebyshev ShenDirichlet 64 (33
+    systems): per-solve latency of the round trip, eager and as one CUDA-graph
+    replay (inputs resident, no L2 flush: a latency figure)."""
+    import shenfun_gb300 as sg
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(64, "F", dtype="d"), sg.FunctionSpace(64, "C", bc=(0, 0))),
+                              axes=(1, 0))
+    u, v = sg.TrialFunction(T), sg.TestFunction(T)
+    H = sg.chebyshev.la.Helmholtz(*sg.inner(v, -sg.div(sg.grad(u))))
+    fj = sg.Array(T, buffer=np.random.default_rng(0).standard_normal((64, 64)))
+    f_hat, u_hat, uq = sg.Function(T), sg.Function(T), sg.Array(T)
+
+    def step():
+        sg.inner(v, fj, output_array=f_hat)
+        H(f_hat, u_hat)
+        T.backward(u_hat.v, uq.v)
+
+    out = {"workload": "2D Poisson, Fourier 64 x Chebyshev ShenDirichlet 64"}
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            step()
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+    st = torch.cuda.current_stream()
+    for mode, fn in (("eager", step), ("graph", g.replay)):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        e1.synchronize()
+        out[f"us_per_solve_{mode}"] = 1e3 * e0.elapsed_time(e1) / reps
+    return out
+
+
 def imex_leg(torch, steps=10):
     """IMEX time stepping on the channel grid (the caller of the path,
     utilities/integrators.py:702-900): IMEXRK443 for u_t = nu lap(u) + u^2,
@@ -530,11 +607,13 @@ def main():
     b.synchronize()
     e2e_val = ws * e2e_steps / (a.elapsed_time(b) / 1e3)
 
-    serving = legendre = imex = None
+    serving = legendre = imex = biharmonic = latency = None
     if rank == 0 and not args.no_extra:
         serving = serving_leg(torch)
         legendre = legendre_leg(torch, flush, st)
         imex = imex_leg(torch)
+        biharmonic = biharmonic_leg(torch, flush, st)
+        latency = latency_leg(torch)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -568,6 +647,8 @@ def main():
             "serving": serving,
             "legendre": legendre,
             "imex": imex,
+            "biharmonic": biharmonic,
+            "small_2d_latency": latency,
         }
         print(json.dumps(out))
     if dist is not None:
