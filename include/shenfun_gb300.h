@@ -51,6 +51,8 @@ extern "C" {
 #define SGPU_BASIS_ORTHO 0  /* T_k (Chebyshev) / L_k (Legendre)        */
 #define SGPU_BASIS_SD 1     /* ShenDirichlet  phi_k = P_k - P_{k+2}    */
 #define SGPU_BASIS_SB 2     /* ShenBiharmonic (chebyshev/bases.py:1249) */
+#define SGPU_BASIS_SN 3     /* ShenNeumann phi_k = T_k - (k/(k+2))^2 T_{k+2}
+                               (chebyshev/bases.py:863-937), Chebyshev only */
 
 /* transform kinds */
 #define SGPU_XF_R2C 1        /* rfft along axis, n -> n/2+1 (FFTW r2c)             */
@@ -138,11 +140,13 @@ int sgpu_PDMA_LU(double* data, int64_t n, cudaStream_t stream);
 int sgpu_PDMA_Solve(void* u, const double* data, int64_t outer, int64_t n, int64_t inner,
                     int data_kind, cudaStream_t stream);
 
-/* ---- Chebyshev Dirichlet Helmholtz (chebyshev/la.py:131-351) -------------
+/* ---- Chebyshev Dirichlet / Neumann Helmholtz (chebyshev/la.py:131-351) ----
  * (alfa A + beta B) u = b with A = ASDSD, B = BSDSD of a ShenDirichlet space
+ * (neumann = 0) or A = ASNSN, B = BSNSN of a ShenNeumann space (neumann = 1)
  * of N modes, one system per (outer, inner) index.  Factor arrays d0, d1, d2,
- * L have the reference's layout (outer, N, inner).  neumann != 0 (ShenNeumann)
- * returns SGPU_ERR_UNSUPPORTED.
+ * L have the reference's layout (outer, N, inner).  The Neumann branch
+ * follows la.pyx:735-751 and 907-912: columns j >= 1 scaled by 1/j^2, a pure
+ * stiffness system (|beta| < 1e-8) solved with u_0 = 0.
  */
 /* la.pyx:708 LU_Helmholtz(A, B, As, Bs, neumann, d0, d1, d2, L, axis) */
 int sgpu_LU_Helmholtz(int64_t N, const double* alfa, const double* beta, int neumann,
@@ -157,6 +161,23 @@ int sgpu_Solve_Helmholtz(const void* b, void* u, int neumann, const double* d0,
 int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa, const double* beta,
                           int64_t outer, int64_t N, int64_t inner, int data_kind,
                           cudaStream_t stream);
+/* Matvec.pyx:769 Helmholtz_Neumann_matvec(v, b, alfa, beta, A, B, axis):
+ * b = (alfa ASNSN + beta BSNSN) v on the N-2 dofs, the two tail entries zero */
+int sgpu_Helmholtz_Neumann_matvec(const void* v, void* b, const double* alfa,
+                                  const double* beta, int64_t outer, int64_t N, int64_t inner,
+                                  int data_kind, cudaStream_t stream);
+
+/* ---- Chebyshev Poisson solvers along one axis ------------------------------
+ * la.pyx:614 Poisson_Solve_ADD(A, b, u, axis) / chebyshev/la.py:11 ADDSolver:
+ * scale * ASDSD u = b on the N-2 dofs of a ShenDirichlet axis (N modes);
+ * the two boundary dofs of u are set to 0.  b may alias u. */
+int sgpu_Poisson_Solve_ADD(const void* b, void* u, double scale, int64_t outer, int64_t N,
+                           int64_t inner, int data_kind, cudaStream_t stream);
+/* chebyshev/la.py:74 ANNSolver.__call__(b, u, axis, constraints=((0, u0),)):
+ * scale * ASNSN u = b on a ShenNeumann axis; u_0 = u0 (the constraint),
+ * boundary dofs 0.  b may alias u. */
+int sgpu_Poisson_Solve_ANN(const void* b, void* u, double scale, double u0, int64_t outer,
+                           int64_t N, int64_t inner, int data_kind, cudaStream_t stream);
 
 /* ---- Helmholtz factorisation cache (no reference counterpart as a separate
  * call: it is LU_Helmholtz's result (la.pyx:717-763) stored for the GPU) ---
@@ -164,12 +185,13 @@ int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa, const doub
  * [q][k][system] for q = (multiplier L, 1/d0, d1, d2): consecutive systems are
  * contiguous.  form SGPU_PLAIN_F64 stores FP64, SGPU_MIXED_DF double-float
  * pairs.  The LU is computed in FP64 in the reference's order either way. */
-int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int64_t outer,
-                          int64_t inner, int form, void* fac, cudaStream_t stream);
+int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int neumann,
+                          int64_t outer, int64_t inner, int form, void* fac, cudaStream_t stream);
 /* Solve_Helmholtz (la.pyx:845-947) from the cache: b, u in the (outer, N,
- * inner) layout; one thread per (system, parity); b may alias u. */
-int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int64_t outer,
-                                int64_t N, int64_t inner, int data_kind, int form,
+ * inner) layout; one thread per (system, parity); b may alias u.  neumann
+ * must match the factorisation. */
+int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int neumann,
+                                int64_t outer, int64_t N, int64_t inner, int data_kind, int form,
                                 cudaStream_t stream);
 
 /* ---- per-wavenumber systems: banded + rank-2 upper semiseparable ----------

@@ -114,36 +114,72 @@ def cheb_sd_stiffness(N):
             4: -4 * np.pi * (k[:N - 6] + 1)}
 
 
-def helmholtz_lu(N, alfa, beta):
+def cheb_sn_stiffness(N):
+    """ASNSN diagonals 0, 2, 4 as the reference evaluates them
+    (chebyshev/matrices.py:1110-1122): a_kk = -2 pi k^2 (k+1)/(k+2),
+    a_{k,k+i} = -4 pi (k+i)^2 (k+1)/(k+2)^2."""
+    k = np.arange(N - 2, dtype=float)
+
+    def key(i):
+        if i == 0:
+            return -2 * np.pi * k ** 2 * (k + 1) / (k + 2)
+        return -4 * np.pi * (k[:-i] + i) ** 2 * (k[:-i] + 1) / (k[:-i] + 2) ** 2
+    return {0: key(0), 2: key(2), 4: key(4)}
+
+
+def helmholtz_lu(N, alfa, beta, neumann=False):
     """LU of alfa*A + beta*B for many systems (LU_Helmholtz_1D, la.pyx:717-763).
 
     alfa, beta: arrays of shape (S,).  Returns d0, d1, d2, L of shape (S, N)
     (the reference's factor arrays have the basis length N; entries beyond the
-    N-2 dofs stay zero).
+    N-2 dofs stay zero).  neumann: A = ASNSN, B = BSNSN with the Neumann
+    branch (la.pyx:735-751): columns j >= 1 divided by j^2, and for
+    |beta| < 1e-8 the singular row 0 replaced by a_00 = 1/alfa, b_00 = 0.
     """
     alfa = np.asarray(alfa, float).reshape(-1)
     beta = np.asarray(beta, float).reshape(-1)
     S = max(alfa.size, beta.size)
     alfa = np.broadcast_to(alfa, (S,))
     beta = np.broadcast_to(beta, (S,))
-    A = cheb_sd_stiffness(N)
-    B = spectral.mass_bands("chebyshev", "SD", N)
-    A0, A2, A4 = A[0], A[2], A[4]
-    Bm2, B0, B2 = B[-2], B[0], B[2]
     M = N - 2
+    if neumann:
+        A = cheb_sn_stiffness(N)
+        B = spectral.mass_bands("chebyshev", "SN", N)
+        i2 = np.arange(M, dtype=float) ** 2
+        A0 = np.tile(A[0], (S, 1))
+        B0 = np.tile(B[0], (S, 1))
+        sing = np.abs(beta) < 1e-8
+        A0[sing, 0] = 1.0 / alfa[sing]
+        B0[sing, 0] = 0.0
+        A0[:, 1:] /= i2[1:]
+        B0[:, 1:] /= i2[1:]
+        A2 = A[2] / i2[2:]
+        B2 = B[2] / i2[2:M]
+        A4 = A[4] / i2[4:]
+        Bm2 = B[-2].copy()
+        Bm2[1:] /= i2[1:M - 2]
+        A0c = lambda i: A0[:, i]  # noqa: E731
+        B0c = lambda i: B0[:, i]  # noqa: E731
+    else:
+        A = cheb_sd_stiffness(N)
+        B = spectral.mass_bands("chebyshev", "SD", N)
+        A2, A4 = A[2], A[4]
+        Bm2, B2 = B[-2], B[2]
+        A0c = lambda i: A[0][i]  # noqa: E731
+        B0c = lambda i: B[0][i]  # noqa: E731
     d0 = np.zeros((S, N))
     d1 = np.zeros((S, N))
     d2 = np.zeros((S, N))
     L = np.zeros((S, N))
-    d0[:, 0] = alfa * A0[0] + beta * B0[0]
-    d0[:, 1] = alfa * A0[1] + beta * B0[1]
+    d0[:, 0] = alfa * A0c(0) + beta * B0c(0)
+    d0[:, 1] = alfa * A0c(1) + beta * B0c(1)
     d1[:, 0] = alfa * A2[0] + beta * B2[0]
     d1[:, 1] = alfa * A2[1] + beta * B2[1]
     d2[:, 0] = alfa * A4[0]
     d2[:, 1] = alfa * A4[1]
     for i in range(2, M):
         L[:, i - 2] = beta * Bm2[i - 2] / d0[:, i - 2]
-        d0[:, i] = alfa * A0[i] + beta * B0[i] - L[:, i - 2] * d1[:, i - 2]
+        d0[:, i] = alfa * A0c(i) + beta * B0c(i) - L[:, i - 2] * d1[:, i - 2]
         if i < M - 2:
             d1[:, i] = alfa * A2[i] + beta * B2[i] - L[:, i - 2] * d2[:, i - 2]
         if i < M - 4:
@@ -151,10 +187,12 @@ def helmholtz_lu(N, alfa, beta):
     return d0, d1, d2, L
 
 
-def helmholtz_solve(f, d0, d1, d2, L):
+def helmholtz_solve(f, d0, d1, d2, L, neumann=False):
     """Solve_Helmholtz_1D_ptr (la.pyx:871-912) for systems along the last axis.
 
     f: (S, N) (complex or real); d*: (S, N).  Returns u (S, N), tail zeros.
+    neumann: the unknowns are w_j = j^2 u_j; u_0 = 0 where d0[0] == 1 to 1e-8
+    (la.pyx:907-912).
     """
     S, Nb = d0.shape
     N = Nb - 2
@@ -179,6 +217,10 @@ def helmholtz_solve(f, d0, d1, d2, L):
             so = so + u[:, i + 4]
             ui = ui - d2[:, i] * so
         u[:, i] = ui / d0[:, i]
+    if neumann:
+        u[(d0[:, 0] - 1.0) ** 2 < 1e-16, 0] = 0.0
+        for i in range(1, N):
+            u[:, i] /= i * i
     return u
 
 
@@ -290,4 +332,92 @@ def leg_helmholtz_solve(f, alfa, beta):
         data[2, 2:] = bet[s] * B[2]
         tdma_lu(data)
         u[s, :M] = tdma_solve(f[s, :M], data)
+    return u
+
+
+# ---------------------------------------------------------------------------
+# Chebyshev ShenNeumann matrices and the Poisson solvers
+def cheb_sn_dense(N):
+    """Dense ASNSN and BSNSN (chebyshev/matrices.py:1096-1122, :377-401) of
+    the N-2 dofs: a_kj = -4 pi j^2 (k+1)/(k+2)^2 for j = k+2, k+4, ..."""
+    M = N - 2
+    k = np.arange(M, dtype=float)
+    A = np.zeros((M, M))
+    A[k.astype(int), k.astype(int)] = -2 * np.pi * k ** 2 * (k + 1) / (k + 2)
+    for i in range(M):
+        for j in range(i + 2, M, 2):
+            A[i, j] = -4 * np.pi * j ** 2 * (i + 1) / (i + 2) ** 2
+    Bb = spectral.mass_bands("chebyshev", "SN", N)
+    B = np.diag(Bb[0]) + np.diag(Bb[2], 2) + np.diag(Bb[-2], -2)
+    return A, B
+
+
+def helmholtz_neumann_matvec(v, alfa, beta):
+    """b = (alfa ASNSN + beta BSNSN) v along the last axis, tail entries zero:
+    the definition Helmholtz_Neumann_matvec (Matvec.pyx:722-800) evaluates
+    (it does not run under numpy 2, so the dense product stands in)."""
+    S, Nb = v.shape
+    A, B = cheb_sn_dense(Nb)
+    alf = np.broadcast_to(np.asarray(alfa, float).reshape(-1), (S,))
+    bet = np.broadcast_to(np.asarray(beta, float).reshape(-1), (S,))
+    b = np.zeros_like(v)
+    b[:, :Nb - 2] = alf[:, None] * (v[:, :Nb - 2] @ A.T) + bet[:, None] * (v[:, :Nb - 2] @ B.T)
+    return b
+
+
+def add_solve(b, A0, A2, scale, axis=0):
+    """Poisson_Solve_ADD_1D_ptr (la.pyx:671-706) along axis: d = A[0],
+    d1 = A[2] (one value per row), N = len(d) dofs; boundary dofs 0
+    (ADDSolver.solve sets them, chebyshev/la.py:19-71)."""
+    u = np.array(b, copy=True)
+    uv, bv = _mv(u, axis), _mv(np.asarray(b), axis)
+    N = len(A0)
+    d, d1 = np.asarray(A0, float), np.broadcast_to(np.asarray(A2, float), (N - 2,))
+    se = np.zeros(uv.shape[1:], dtype=u.dtype)
+    so = np.zeros(uv.shape[1:], dtype=u.dtype)
+    uv[N - 1] = bv[N - 1] / d[N - 1]
+    uv[N - 2] = bv[N - 2] / d[N - 2]
+    for k in range(N - 3, -1, -1):
+        if k % 2 == 0:
+            se = se + uv[k + 2]
+            uv[k] = bv[k] - d1[k] * se
+        else:
+            so = so + uv[k + 2]
+            uv[k] = bv[k] - d1[k] * so
+        uv[k] /= d[k]
+    if not abs(scale - 1) < 1e-8:
+        uv[:N] /= scale
+    uv[N:] = 0
+    return u
+
+
+def ann_solve(b, A0, A2, scale, axis=0, u0=0.0):
+    """ANNSolver.__call__ (chebyshev/la.py:77-128) along axis: columns scaled
+    by 1/j^2, back substitution for k = N-3 .. 1, u = w / j^2 / scale, the
+    constraint u_0 = u0, boundary dofs 0."""
+    u = np.array(b, copy=True)
+    uv, bv = _mv(u, axis), _mv(np.asarray(b), axis)
+    M = len(A0)
+    j2 = np.arange(M, dtype=float) ** 2
+    j2[0] = 1
+    j2 = 1.0 / j2
+    d = np.asarray(A0, float) * j2
+    d1 = np.asarray(A2, float) * j2[2:]
+    se = np.zeros(uv.shape[1:], dtype=u.dtype)
+    so = np.zeros(uv.shape[1:], dtype=u.dtype)
+    us = uv[:M]
+    us[-1] = bv[M - 1] / d[-1]
+    us[-2] = bv[M - 2] / d[-2]
+    for k in range(M - 3, 0, -1):
+        if k % 2 == 0:
+            se = se + us[k + 2]
+            us[k] = bv[k] - d1[k] * se
+        else:
+            so = so + us[k + 2]
+            us[k] = bv[k] - d1[k] * so
+        us[k] /= d[k]
+    us *= j2.reshape((M,) + (1,) * (us.ndim - 1))
+    uv /= scale
+    uv[0] = u0
+    uv[M:] = 0
     return u

@@ -74,6 +74,10 @@ def stencil(family, basis, N):
     if basis == "SD":
         # chebyshev/bases.py:546 {0: 1, 2: -1}; legendre/bases.py:374 (unscaled)
         return {0: np.ones(N), 2: -np.ones(N - 2)}
+    if basis == "SN" and family == "chebyshev":
+        # chebyshev/bases.py:937 {0: 1, 2: -(n/(n+2))**2}; the array diagonal
+        # has N-2 entries, all kept (rows k >= N-2 do not exist in it)
+        return {0: np.ones(N), 2: -(k[:N - 2] / (k[:N - 2] + 2)) ** 2}
     if basis == "SB" and family == "chebyshev":
         # chebyshev/bases.py:1249 {0: 1, 2: -(2n+4)/(n+3), 4: (n+1)/(n+3)}
         d = {0: np.ones(N), 2: -(2 * k[:N - 2] + 4) / (k[:N - 2] + 3),
@@ -90,7 +94,7 @@ def stencil(family, basis, N):
 
 
 def num_bcs(basis):
-    return {"T": 0, "L": 0, "SD": 2, "SB": 4}[basis]
+    return {"T": 0, "L": 0, "SD": 2, "SN": 2, "SB": 4}[basis]
 
 
 def apply_stencil(c, K, axis=-1):
@@ -139,6 +143,15 @@ def mass_bands(family, basis, N):
     if family == "chebyshev" and basis == "SD":
         h = cheb_norm_sq(N)
         return {-2: np.full(N - 4, -h[1]), 0: h[:-2] + h[2:], 2: np.full(N - 4, -h[1])}
+    if family == "chebyshev" and basis == "SN":
+        # BSNSNmat (chebyshev/matrices.py:377-401): alpha = (k/(k+2))^2,
+        # {0: h + alpha^2 h_{k+2}, +-2: -alpha h_{k+2}}
+        h = cheb_norm_sq(N)
+        k = np.arange(N, dtype=float)
+        alpha = (k / (k + 2)) ** 2
+        d = {0: h[:-2] + alpha[:-2] ** 2 * h[2:], 2: -alpha[:N - 4] * h[2:N - 2]}
+        d[-2] = d[2].copy()
+        return d
     if family == "legendre" and basis == "SD":
         d0 = leg_norm_sq(N)
         return {0: d0[:-2] + d0[2:], -2: -d0[2:-2], 2: -d0[2:-2]}

@@ -1,2 +1,2 @@
 """``shenfun.chebyshev.la`` counterpart: tailored Chebyshev solvers."""
-from ..la import Helmholtz, Biharmonic  # noqa: F401
+from ..la import Helmholtz, Biharmonic, ADDSolver, ANNSolver  # noqa: F401

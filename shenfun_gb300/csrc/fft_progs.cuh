@@ -83,7 +83,7 @@ SGPU_HD R stencil_coef(const LinePlan& p, int off, int k) {
 }
 
 SGPU_HD int basis_nbcs(int basis) {
-  return basis == SGPU_BASIS_SD ? 2 : (basis == SGPU_BASIS_SB ? 4 : 0);
+  return (basis == SGPU_BASIS_SD || basis == SGPU_BASIS_SN) ? 2 : (basis == SGPU_BASIS_SB ? 4 : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -332,9 +332,9 @@ SGPU_HD void prog_dct2(const LinePlan& p, const double* in, double* out, int in_
       Cx<R> acc = y[k];
       if (p.basis == SGPU_BASIS_SD) {
         if (k + 2 < n) acc = acc - y[k + 2];
-      } else if (p.basis == SGPU_BASIS_SB) {
+      } else if (p.basis == SGPU_BASIS_SB || p.basis == SGPU_BASIS_SN) {
         if (k + 2 < n) acc = acc + scale(y[k + 2], stencil_coef<R>(p, 2, k));
-        if (k + 4 < n) acc = acc + scale(y[k + 4], stencil_coef<R>(p, 4, k));
+        if (p.basis == SGPU_BASIS_SB && k + 4 < n) acc = acc + scale(y[k + 4], stencil_coef<R>(p, 4, k));
       }
       s.B[(size_t)c * p.ld + k] = acc;
     }
@@ -410,7 +410,8 @@ SGPU_HD void prog_dct3(const LinePlan& p, const double* in, double* out, int in_
         if (k - 2 >= 0 && k - 2 < dim) acc = acc - u[k - 2];
       } else {
         if (k - 2 >= 0 && k - 2 < dim) acc = acc + scale(u[k - 2], stencil_coef<R>(p, 2, k - 2));
-        if (k - 4 >= 0 && k - 4 < dim) acc = acc + scale(u[k - 4], stencil_coef<R>(p, 4, k - 4));
+        if (p.basis == SGPU_BASIS_SB && k - 4 >= 0 && k - 4 < dim)
+          acc = acc + scale(u[k - 4], stencil_coef<R>(p, 4, k - 4));
       }
       s.B[(size_t)c * p.ld + k] = acc;
     }

@@ -107,7 +107,7 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   if (form != SGPU_PLAIN_F64 && form != SGPU_MIXED_DF) return SGPU_ERR_UNSUPPORTED;
   const bool cheb = kind >= SGPU_XF_DCT2;
   const bool composite = kind >= SGPU_XF_CHEB_SCALAR;
-  if (composite && (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SB)) return SGPU_ERR_ARG;
+  if (composite && (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SN)) return SGPU_ERR_ARG;
   if (composite && n < 2 + 2 * basis_nbcs(basis)) return SGPU_ERR_ARG;
   std::memset(&p, 0, sizeof(p));
   p.form = form;
@@ -208,6 +208,17 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
       T.sten_f[n + k] = ld_to_df((k + 1.0L) / (k + 3.0L));
     }
   }
+  if (p.basis == SGPU_BASIS_SN) {
+    // K2(k) = -(k/(k+2))^2 for k < n-2 (chebyshev/bases.py:937), no K4
+    sten.assign(2 * (size_t)n, 0.0);
+    T.sten_f.assign(2 * (size_t)n, df());
+    for (int k = 0; k < n - 2; ++k) {
+      const double r = k / (k + 2.0);
+      const ld_t rl = (ld_t)k / (k + 2.0L);
+      sten[k] = -(r * r);
+      T.sten_f[k] = ld_to_df(-(rl * rl));
+    }
+  }
   if (kind == SGPU_XF_CHEB_FORWARD) {
     // Chebyshev mass matrices (chebyshev/matrices.py:238-246, :515-528), LU'd
     // as la.pyx:213-252 do, diagonal row replaced by its reciprocal.
@@ -217,14 +228,27 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
     if (p.basis == SGPU_BASIS_ORTHO) {
       mass.resize(n);
       for (int k = 0; k < n; ++k) mass[k] = 1.0 / h[k];
-    } else if (p.basis == SGPU_BASIS_SD) {
+    } else if (p.basis == SGPU_BASIS_SD || p.basis == SGPU_BASIS_SN) {
+      // SN: BSNSN (chebyshev/matrices.py:377-401), b_kk = h_k + K2(k)^2 h_{k+2},
+      // b_{k,k+2} = b_{k+2,k} = K2(k) h_{k+2}
       const int dim = n - 2;
       mass.assign(3 * (size_t)dim, 0.0);
       double* ldg = &mass[0];
       double* d = &mass[dim];
       double* ud = &mass[2 * dim + 2];
-      for (int k = 0; k < dim; ++k) d[k] = h[k] + h[k + 2];
-      for (int k = 0; k < dim - 2; ++k) ldg[k] = ud[k] = -h[1];
+      if (p.basis == SGPU_BASIS_SD) {
+        for (int k = 0; k < dim; ++k) d[k] = h[k] + h[k + 2];
+        for (int k = 0; k < dim - 2; ++k) ldg[k] = ud[k] = -h[1];
+      } else {
+        for (int k = 0; k < dim; ++k) {
+          const double al = (k / (k + 2.0)) * (k / (k + 2.0));
+          d[k] = h[k] + al * al * h[k + 2];
+        }
+        for (int k = 0; k < dim - 2; ++k) {
+          const double al = (k / (k + 2.0)) * (k / (k + 2.0));
+          ldg[k] = ud[k] = -al * h[k + 2];
+        }
+      }
       for (int i = 2; i < dim; ++i) {
         ldg[i - 2] = ldg[i - 2] / d[i - 2];
         d[i] = d[i] - ldg[i - 2] * ud[i - 2];

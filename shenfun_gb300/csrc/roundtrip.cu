@@ -45,10 +45,10 @@ int sgpu_legendre_plan_destroy(sgpu_legendre_plan* plan);
 int sgpu_legendre_execute(const sgpu_legendre_plan* plan, int direction, const void* in,
                           void* out, int64_t outer, int64_t inner, int data_kind,
                           cudaStream_t stream);
-int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int64_t outer,
-                          int64_t inner, int form, void* fac, cudaStream_t stream);
-int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int64_t outer,
-                                int64_t N, int64_t inner, int data_kind, int form,
+int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int neumann,
+                          int64_t outer, int64_t inner, int form, void* fac, cudaStream_t stream);
+int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int neumann,
+                                int64_t outer, int64_t N, int64_t inner, int data_kind, int form,
                                 cudaStream_t stream);
 int sgpu_band_sep_factor(int n, int nterms, int gen_term, const double* bands,
                          const double* gens, const double* coef, int64_t nsys, double* fac,
@@ -243,7 +243,7 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
   cudaMemcpyAsync(p->alfa, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
   cudaMemcpyAsync(p->beta, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
   if (family == SGPU_FAMILY_CHEBYSHEV) {
-    st = sgpu_helmholtz_factor(Nd, p->alfa, p->beta, p->nsys, 1, SGPU_PLAIN_F64, p->fac, stream);
+    st = sgpu_helmholtz_factor(Nd, p->alfa, p->beta, 0, p->nsys, 1, SGPU_PLAIN_F64, p->fac, stream);
   } else {
     // terms: (phi''_j, phi_k) = -(4k+6) diagonal with coefficient alfa, and the
     // mass matrix B (legendre/matrices.py:121-135) with coefficient beta
@@ -340,7 +340,7 @@ static int helmholtz_run(const sgpu_helmholtz_problem* p, const double* f, doubl
   }
   // 2. one banded system per wavenumber, in place on the spectral array
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    st |= sgpu_helmholtz_solve_cached(wc, wc, p->fac, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s);
+    st |= sgpu_helmholtz_solve_cached(wc, wc, p->fac, 0, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s);
   else
     st |= sgpu_band_sep_solve(wc, wc, p->fac, nullptr, (int)(Nd - 2), p->nsys, Nd, 1, SGPU_COMPLEX, s);
   // 3. backward

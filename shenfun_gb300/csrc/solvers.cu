@@ -30,18 +30,39 @@ __global__ void k_pdma_solve(T* u, const double* data, int64_t n, int64_t inner,
   if (s < nsys) pdma_solve_prog<T>(u, data, n, inner, s);
 }
 
-__global__ void k_helmholtz_lu(int64_t N, const double* alfa, const double* beta, double* d0,
-                               double* d1, double* d2, double* L, int64_t inner, int64_t nsys) {
+__global__ void k_helmholtz_lu(int64_t N, const double* alfa, const double* beta, int neumann,
+                               double* d0, double* d1, double* d2, double* L, int64_t inner,
+                               int64_t nsys) {
   int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < nsys) helmholtz_lu_prog(N, alfa, beta, d0, d1, d2, L, inner, s);
+  if (s < nsys) helmholtz_lu_prog(N, alfa, beta, neumann, d0, d1, d2, L, inner, s);
 }
 
 template <class T>
-__global__ void k_helmholtz_solve(const T* b, T* u, const double* d0, const double* d1,
+__global__ void k_helmholtz_solve(const T* b, T* u, int neumann, const double* d0, const double* d1,
                                   const double* d2, const double* L, int64_t N, int64_t inner,
                                   int64_t nsys) {
   int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < nsys) helmholtz_solve_prog<T>(b, u, d0, d1, d2, L, N, inner, s);
+  if (s < nsys) helmholtz_solve_prog<T>(b, u, neumann, d0, d1, d2, L, N, inner, s);
+}
+
+template <class T>
+__global__ void k_helmholtz_neumann_matvec(const T* v, T* b, const double* alfa, const double* beta,
+                                           int64_t N, int64_t inner, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) helmholtz_neumann_matvec_prog<T>(v, b, alfa, beta, N, inner, s);
+}
+
+template <class T>
+__global__ void k_poisson_add(const T* b, T* u, double scale, int64_t N, int64_t inner, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) poisson_add_prog<T>(b, u, scale, N, inner, s);
+}
+
+template <class T>
+__global__ void k_poisson_ann(const T* b, T* u, double scale, double c0, int64_t N, int64_t inner,
+                              int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) poisson_ann_prog<T>(b, u, scale, c0, N, inner, s);
 }
 
 template <class T>
@@ -94,12 +115,12 @@ extern "C" int sgpu_PDMA_Solve(void* u, const double* data, int64_t outer, int64
 extern "C" int sgpu_LU_Helmholtz(int64_t N, const double* alfa, const double* beta, int neumann,
                                  double* d0, double* d1, double* d2, double* L, int64_t outer,
                                  int64_t inner, cudaStream_t stream) {
-  if (neumann) return SGPU_ERR_UNSUPPORTED;
-  if (!alfa || !beta || !d0 || !d1 || !d2 || !L || N < 8 || outer < 0 || inner < 1)
+  if (!alfa || !beta || !d0 || !d1 || !d2 || !L || N < 8 || outer < 0 || inner < 1 ||
+      (neumann != 0 && neumann != 1))
     return SGPU_ERR_ARG;
   const int64_t nsys = outer * inner;
   if (nsys == 0) return SGPU_OK;
-  k_helmholtz_lu<<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, d0, d1, d2, L, inner, nsys);
+  k_helmholtz_lu<<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, neumann, d0, d1, d2, L, inner, nsys);
   return finish();
 }
 
@@ -107,16 +128,17 @@ extern "C" int sgpu_Solve_Helmholtz(const void* b, void* u, int neumann, const d
                                     const double* d1, const double* d2, const double* L,
                                     int64_t outer, int64_t N, int64_t inner, int data_kind,
                                     cudaStream_t stream) {
-  if (neumann) return SGPU_ERR_UNSUPPORTED;
-  if (!b || !u || !d0 || !d1 || !d2 || !L || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  if (!b || !u || !d0 || !d1 || !d2 || !L || N < 8 || outer < 0 || inner < 1 ||
+      (neumann != 0 && neumann != 1))
+    return SGPU_ERR_ARG;
   const int64_t nsys = outer * inner;
   if (nsys == 0) return SGPU_OK;
   if (data_kind == SGPU_COMPLEX)
-    k_helmholtz_solve<cd><<<nblk(nsys), kThreads, 0, stream>>>((const cd*)b, (cd*)u, d0, d1, d2, L,
-                                                               N, inner, nsys);
+    k_helmholtz_solve<cd><<<nblk(nsys), kThreads, 0, stream>>>((const cd*)b, (cd*)u, neumann, d0, d1,
+                                                               d2, L, N, inner, nsys);
   else if (data_kind == SGPU_REAL)
     k_helmholtz_solve<double><<<nblk(nsys), kThreads, 0, stream>>>(
-        (const double*)b, (double*)u, d0, d1, d2, L, N, inner, nsys);
+        (const double*)b, (double*)u, neumann, d0, d1, d2, L, N, inner, nsys);
   else
     return SGPU_ERR_ARG;
   return finish();
@@ -140,51 +162,104 @@ extern "C" int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa,
   return finish();
 }
 
-// ---- factorisation cache + cached solve (both forms) -----------------------
-template <class R>
-__global__ void k_helmholtz_factor(int64_t N, const double* alfa, const double* beta, R* fac,
-                                   int64_t nsys) {
-  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < nsys) helmholtz_factor_prog<R>(N, alfa, beta, fac, nsys, s);
-}
-
-template <class R, class T>
-__global__ void k_helmholtz_cached(const T* b, T* u, const R* fac, int64_t N, int64_t inner,
-                                   int64_t nsys) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < 2 * nsys) helmholtz_cached_solve_prog<R, T>(b, u, fac, N, inner, nsys, t >> 1, (int)(t & 1));
-}
-
-extern "C" int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta,
-                                     int64_t outer, int64_t inner, int form, void* fac,
-                                     cudaStream_t stream) {
-  if (!alfa || !beta || !fac || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+extern "C" int sgpu_Helmholtz_Neumann_matvec(const void* v, void* b, const double* alfa,
+                                             const double* beta, int64_t outer, int64_t N,
+                                             int64_t inner, int data_kind, cudaStream_t stream) {
+  if (!v || !b || !alfa || !beta || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  if (v == b) return SGPU_ERR_ARG;
   const int64_t nsys = outer * inner;
   if (nsys == 0) return SGPU_OK;
-  if (form == SGPU_PLAIN_F64)
-    k_helmholtz_factor<double><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, (double*)fac, nsys);
-  else if (form == SGPU_MIXED_DF)
-    k_helmholtz_factor<df><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, (df*)fac, nsys);
+  if (data_kind == SGPU_COMPLEX)
+    k_helmholtz_neumann_matvec<cd><<<nblk(nsys), kThreads, 0, stream>>>((const cd*)v, (cd*)b, alfa,
+                                                                        beta, N, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_helmholtz_neumann_matvec<double><<<nblk(nsys), kThreads, 0, stream>>>(
+        (const double*)v, (double*)b, alfa, beta, N, inner, nsys);
   else
     return SGPU_ERR_ARG;
   return finish();
 }
 
-extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int64_t outer,
-                                           int64_t N, int64_t inner, int data_kind, int form,
-                                           cudaStream_t stream) {
-  if (!b || !u || !fac || N < 8 || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+extern "C" int sgpu_Poisson_Solve_ADD(const void* b, void* u, double scale, int64_t outer, int64_t N,
+                                      int64_t inner, int data_kind, cudaStream_t stream) {
+  if (!b || !u || N < 5 || outer < 0 || inner < 1 || !(scale != 0.0)) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_poisson_add<cd><<<nblk(nsys), kThreads, 0, stream>>>((const cd*)b, (cd*)u, scale, N, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_poisson_add<double><<<nblk(nsys), kThreads, 0, stream>>>((const double*)b, (double*)u, scale, N,
+                                                              inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+extern "C" int sgpu_Poisson_Solve_ANN(const void* b, void* u, double scale, double u0, int64_t outer,
+                                      int64_t N, int64_t inner, int data_kind, cudaStream_t stream) {
+  if (!b || !u || N < 5 || outer < 0 || inner < 1 || !(scale != 0.0)) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_poisson_ann<cd><<<nblk(nsys), kThreads, 0, stream>>>((const cd*)b, (cd*)u, scale, u0, N, inner,
+                                                           nsys);
+  else if (data_kind == SGPU_REAL)
+    k_poisson_ann<double><<<nblk(nsys), kThreads, 0, stream>>>((const double*)b, (double*)u, scale, u0,
+                                                              N, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+// ---- factorisation cache + cached solve (both forms) -----------------------
+template <class R>
+__global__ void k_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int neumann,
+                                   R* fac, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) helmholtz_factor_prog<R>(N, alfa, beta, neumann, fac, nsys, s);
+}
+
+template <class R, class T>
+__global__ void k_helmholtz_cached(const T* b, T* u, const R* fac, int neumann, int64_t N,
+                                   int64_t inner, int64_t nsys) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 2 * nsys)
+    helmholtz_cached_solve_prog<R, T>(b, u, fac, neumann, N, inner, nsys, t >> 1, (int)(t & 1));
+}
+
+extern "C" int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int neumann,
+                                     int64_t outer, int64_t inner, int form, void* fac,
+                                     cudaStream_t stream) {
+  if (!alfa || !beta || !fac || N < 8 || outer < 0 || inner < 1 || (neumann != 0 && neumann != 1))
+    return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (form == SGPU_PLAIN_F64)
+    k_helmholtz_factor<double><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, neumann, (double*)fac, nsys);
+  else if (form == SGPU_MIXED_DF)
+    k_helmholtz_factor<df><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, neumann, (df*)fac, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int neumann,
+                                           int64_t outer, int64_t N, int64_t inner, int data_kind,
+                                           int form, cudaStream_t stream) {
+  if (!b || !u || !fac || N < 8 || outer < 0 || inner < 1 || (neumann != 0 && neumann != 1))
+    return SGPU_ERR_ARG;
   const int64_t nsys = outer * inner;
   if (nsys == 0) return SGPU_OK;
   const unsigned nb = nblk(2 * nsys);
+  const int nm = neumann;
   if (form == SGPU_PLAIN_F64 && data_kind == SGPU_COMPLEX)
-    k_helmholtz_cached<double, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (const double*)fac, N, inner, nsys);
+    k_helmholtz_cached<double, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (const double*)fac, nm, N, inner, nsys);
   else if (form == SGPU_PLAIN_F64 && data_kind == SGPU_REAL)
-    k_helmholtz_cached<double, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (const double*)fac, N, inner, nsys);
+    k_helmholtz_cached<double, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (const double*)fac, nm, N, inner, nsys);
   else if (form == SGPU_MIXED_DF && data_kind == SGPU_COMPLEX)
-    k_helmholtz_cached<df, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (const df*)fac, N, inner, nsys);
+    k_helmholtz_cached<df, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (const df*)fac, nm, N, inner, nsys);
   else if (form == SGPU_MIXED_DF && data_kind == SGPU_REAL)
-    k_helmholtz_cached<df, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (const df*)fac, N, inner, nsys);
+    k_helmholtz_cached<df, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (const df*)fac, nm, N, inner, nsys);
   else
     return SGPU_ERR_ARG;
   return finish();

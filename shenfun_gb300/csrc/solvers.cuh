@@ -15,6 +15,10 @@ SGPU_HD double mulr(double a, double s) { return a * s; }
 SGPU_HD cd mulr(cd a, double s) { return scale(a, s); }
 SGPU_HD double zero_of(double) { return 0.0; }
 SGPU_HD cd zero_of(cd) { return cx<double>(0.0, 0.0); }
+SGPU_HD double divr(double a, double s) { return a / s; }
+SGPU_HD cd divr(cd a, double s) { return cx<double>(a.re / s, a.im / s); }
+SGPU_HD double real_of(double, double c) { return c; }
+SGPU_HD cd real_of(cd, double c) { return cx<double>(c, 0.0); }
 
 // strided line view: element k of system s
 template <class T>
@@ -95,7 +99,7 @@ SGPU_HD void pdma_solve_prog(T* u_all, const double* data, int64_t n, int64_t in
     u[k] = mulr(u[k] - mulr(u[k + 2], e[k]) - mulr(u[k + 4], f[k]), 1.0 / d[k]);
 }
 
-// ---- Chebyshev Dirichlet Helmholtz ---------------------------------------
+// ---- Chebyshev Dirichlet / Neumann Helmholtz -------------------------------
 // ASDSD / BSDSD coefficients in the reference's evaluation order
 // (chebyshev/matrices.py:1061-1079, :238-246).
 SGPU_HD double hA0(int64_t k) { return ((-2.0 * 3.141592653589793) * (k + 1.0)) * (k + 2.0); }
@@ -103,34 +107,92 @@ SGPU_HD double hA2(int64_t k) { return (-4.0 * 3.141592653589793) * (k + 1.0); }
 SGPU_HD double hB0(int64_t k) { return k == 0 ? 3.141592653589793 + 1.5707963267948966 : 3.141592653589793; }
 SGPU_HD double hB2() { return -1.5707963267948966; }
 
+// ShenNeumann phi_k = T_k - (k/(k+2))^2 T_{k+2} (chebyshev/bases.py:863-937):
+// A = ASNSN (chebyshev/matrices.py:1096-1122), a_kk = -2 pi k^2 (k+1)/(k+2),
+// a_kj = -4 pi j^2 (k+1)/(k+2)^2 for j = k+2, k+4, ...; B = BSNSN
+// (chebyshev/matrices.py:377-401), b_kk = h_k + (k/(k+2))^4 h_{k+2},
+// b_{k,k+2} = b_{k+2,k} = -(k/(k+2))^2 h_{k+2}, h_0 = pi, h_k = pi/2.  The
+// Neumann branch of LU_Helmholtz_1D (la.pyx:735-751) divides column j >= 1 of
+// both matrices by j^2: every strictly-upper row of the scaled A is then one
+// constant, -4 pi (k+1)/(k+2)^2, and the Dirichlet recurrences solve for
+// w_j = j^2 u_j.  For a pure stiffness system (|beta| < 1e-8) the singular
+// row 0 gets a_00 = 1/alfa, b_00 = 0, and the solve sets u_0 = 0.
+SGPU_HD double sn_h(int64_t k) { return k == 0 ? 3.141592653589793 : 1.5707963267948966; }
+SGPU_HD double sn_K2sq(int64_t k) {
+  const double r = k / (k + 2.0);
+  return r * r;
+}
+SGPU_HD double sn_col(int64_t j) { return (double)j * (double)j; }
+
+// Row i of the (column-scaled) matrices: A(i,i), A(i,i+2), A(i,i+4),
+// B(i,i), B(i,i+2), B(i+2,i).
+struct HelmRow {
+  double A0, A2, A4, B0, B2, Bm2;
+};
+
+SGPU_HD HelmRow helm_row(int64_t i, int neumann) {
+  HelmRow r;
+  if (!neumann) {
+    r.A0 = hA0(i);
+    r.A2 = hA2(i);
+    r.A4 = hA2(i);
+    r.B0 = hB0(i);
+    r.B2 = hB2();
+    r.Bm2 = hB2();
+    return r;
+  }
+  const double k = (double)i, m4pi = -4.0 * 3.141592653589793;
+  const double a2 = ((m4pi * ((k + 2) * (k + 2))) * (k + 1)) / ((k + 2) * (k + 2));
+  const double a4 = ((m4pi * ((k + 4) * (k + 4))) * (k + 1)) / ((k + 2) * (k + 2));
+  const double al = sn_K2sq(i);
+  r.A0 = i == 0 ? 0.0 : ((((-2.0 * 3.141592653589793) * (k * k)) * (k + 1)) / (k + 2)) / sn_col(i);
+  r.A2 = a2 / sn_col(i + 2);
+  r.A4 = a4 / sn_col(i + 4);
+  r.B0 = sn_h(i) + (al * al) * sn_h(i + 2);
+  if (i >= 1) r.B0 /= sn_col(i);
+  r.B2 = (-al * sn_h(i + 2)) / sn_col(i + 2);
+  r.Bm2 = i >= 1 ? (-al * sn_h(i + 2)) / sn_col(i) : 0.0;
+  return r;
+}
+
+// the pure-stiffness test of the Neumann branch (la.pyx:736, 908)
+SGPU_HD bool sn_singular(double beta) { return beta < 1e-8 && beta > -1e-8; }
+SGPU_HD bool sn_zero_mode(double d00) { return (d00 - 1.0) * (d00 - 1.0) < 1e-16; }
+
 // LU_Helmholtz_1D (la.pyx:717-763); N = number of basis functions, the
 // factor lines have N entries with the last two untouched.
-SGPU_HD void helmholtz_lu_prog(int64_t N, const double* alfa, const double* beta, double* d0_all,
-                               double* d1_all, double* d2_all, double* L_all, int64_t inner,
-                               int64_t s) {
+SGPU_HD void helmholtz_lu_prog(int64_t N, const double* alfa, const double* beta, int neumann,
+                               double* d0_all, double* d1_all, double* d2_all, double* L_all,
+                               int64_t inner, int64_t s) {
   const int64_t b0 = sys_base(s, N, inner);
   Line<double> d0{d0_all + b0, inner}, d1{d1_all + b0, inner}, d2{d2_all + b0, inner},
       L{L_all + b0, inner};
   const double a = alfa[s], b = beta[s];
   const int64_t M = N - 2;
-  d0[0] = a * hA0(0) + b * hB0(0);
-  d0[1] = a * hA0(1) + b * hB0(1);
-  d1[0] = a * hA2(0) + b * hB2();
-  d1[1] = a * hA2(1) + b * hB2();
-  d2[0] = a * hA2(0);
-  d2[1] = a * hA2(1);
+  HelmRow r0 = helm_row(0, neumann), r1 = helm_row(1, neumann);
+  if (neumann && sn_singular(b)) {
+    r0.A0 = 1.0 / a;
+    r0.B0 = 0.0;
+  }
+  d0[0] = a * r0.A0 + b * r0.B0;
+  d0[1] = a * r1.A0 + b * r1.B0;
+  d1[0] = a * r0.A2 + b * r0.B2;
+  d1[1] = a * r1.A2 + b * r1.B2;
+  d2[0] = a * r0.A4;
+  d2[1] = a * r1.A4;
   for (int64_t i = 2; i < M; ++i) {
-    double l = b * hB2() / d0[i - 2];
+    const HelmRow r = helm_row(i, neumann);
+    double l = b * helm_row(i - 2, neumann).Bm2 / d0[i - 2];
     L[i - 2] = l;
-    d0[i] = a * hA0(i) + b * hB0(i) - l * d1[i - 2];
-    if (i < M - 2) d1[i] = a * hA2(i) + b * hB2() - l * d2[i - 2];
-    if (i < M - 4) d2[i] = a * hA2(i) - l * d2[i - 2];
+    d0[i] = a * r.A0 + b * r.B0 - l * d1[i - 2];
+    if (i < M - 2) d1[i] = a * r.A2 + b * r.B2 - l * d2[i - 2];
+    if (i < M - 4) d2[i] = a * r.A4 - l * d2[i - 2];
   }
 }
 
 // Solve_Helmholtz_1D_ptr (la.pyx:871-912).  y is kept in u.
 template <class T>
-SGPU_HD void helmholtz_solve_prog(const T* b_all, T* u_all, const double* d0_all,
+SGPU_HD void helmholtz_solve_prog(const T* b_all, T* u_all, int neumann, const double* d0_all,
                                   const double* d1_all, const double* d2_all, const double* L_all,
                                   int64_t Nb, int64_t inner, int64_t s) {
   const int64_t b0 = sys_base(s, Nb, inner);
@@ -178,6 +240,102 @@ SGPU_HD void helmholtz_solve_prog(const T* b_all, T* u_all, const double* d0_all
     up2 = t2;
     up4 = t4;
   }
+  if (neumann) {
+    // back from w_j = j^2 u_j (la.pyx:907-912)
+    if (sn_zero_mode(d0[0])) u[0] = zero_of(T());
+    for (int64_t i = 1; i < N; ++i) u[i] = divr(u[i], sn_col(i));
+  }
+}
+
+// Helmholtz_Neumann_matvec (Matvec.pyx:722-800): b = (alfa A + beta B) v with
+// A = ASNSN, B = BSNSN on the N-2 dofs, tail zero.  Row k needs
+// S_k = sum_{j = k+2, k+4, ...} j^2 v_j, kept per parity while k descends.
+template <class T>
+SGPU_HD void helmholtz_neumann_matvec_prog(const T* v_all, T* b_all, const double* alfa,
+                                           const double* beta, int64_t Nb, int64_t inner,
+                                           int64_t s) {
+  const int64_t b0 = sys_base(s, Nb, inner);
+  Line<const T> v{v_all + b0, inner};
+  Line<T> b{b_all + b0, inner};
+  const int64_t M = Nb - 2;
+  const double alf = alfa[s], bet = beta[s];
+  const double pi = 3.141592653589793;
+  T S[2] = {zero_of(T()), zero_of(T())};
+  for (int64_t k = M - 1; k >= 0; --k) {
+    const double kk = (double)k;
+    const double akk = ((((-2.0 * pi) * (kk * kk)) * (kk + 1)) / (kk + 2));
+    const double bkk = sn_h(k) + (sn_K2sq(k) * sn_K2sq(k)) * sn_h(k + 2);
+    T acc = mulr(v[k], alf * akk + bet * bkk);
+    if (k + 2 < M) {
+      S[k & 1] = S[k & 1] + mulr(v[k + 2], sn_col(k + 2));
+      acc = acc + mulr(v[k + 2], bet * (-sn_K2sq(k) * sn_h(k + 2)));
+      acc = acc + mulr(S[k & 1], alf * (((-4.0 * pi) * (kk + 1)) / ((kk + 2) * (kk + 2))));
+    }
+    if (k >= 2) acc = acc + mulr(v[k - 2], bet * (-sn_K2sq(k - 2) * sn_h(k)));
+    b[k] = acc;
+  }
+  b[M] = zero_of(T());
+  b[M + 1] = zero_of(T());
+}
+
+// Poisson_Solve_ADD_1D_ptr (la.pyx:671-706): A u = b with A = scale * ASDSD,
+// upper triangular, back substitution with one running sum per parity; the
+// two boundary dofs are set to zero (homogeneous boundary values).
+template <class T>
+SGPU_HD void poisson_add_prog(const T* b_all, T* u_all, double scale, int64_t Nb, int64_t inner,
+                              int64_t s) {
+  const int64_t b0 = sys_base(s, Nb, inner);
+  Line<const T> b{b_all + b0, inner};
+  Line<T> u{u_all + b0, inner};
+  const int64_t N = Nb - 2;
+  T S[2] = {zero_of(T()), zero_of(T())};
+  T up[2] = {zero_of(T()), zero_of(T())};  // last u of each parity
+  for (int64_t k = N - 1; k >= 0; --k) {
+    T uk = b[k];
+    if (k <= N - 3) {
+      S[k & 1] = S[k & 1] + up[k & 1];
+      uk = uk - mulr(S[k & 1], hA2(k));
+    }
+    uk = divr(uk, hA0(k));
+    up[k & 1] = uk;
+    u[k] = uk;
+  }
+  if (!(scale - 1.0 < 1e-8 && scale - 1.0 > -1e-8))
+    for (int64_t k = 0; k < N; ++k) u[k] = divr(u[k], scale);
+  u[N] = zero_of(T());
+  u[N + 1] = zero_of(T());
+}
+
+// ANNSolver.__call__ (chebyshev/la.py:77-128): A u = b with A = scale * ASNSN,
+// columns scaled by 1/j^2 (j >= 1), back substitution for k = N-1 .. 1 with
+// one running sum per parity, u_k = w_k / k^2, then u /= scale and the
+// constraint u_0 = c0; boundary dofs zero.
+template <class T>
+SGPU_HD void poisson_ann_prog(const T* b_all, T* u_all, double scale, double c0, int64_t Nb,
+                              int64_t inner, int64_t s) {
+  const int64_t b0 = sys_base(s, Nb, inner);
+  Line<const T> b{b_all + b0, inner};
+  Line<T> u{u_all + b0, inner};
+  const int64_t N = Nb - 2;
+  const double pi = 3.141592653589793;
+  T S[2] = {zero_of(T()), zero_of(T())};
+  T up[2] = {zero_of(T()), zero_of(T())};
+  for (int64_t k = N - 1; k >= 1; --k) {
+    const double kk = (double)k;
+    const double d = ((((-2.0 * pi) * (kk * kk)) * (kk + 1)) / (kk + 2)) * (1.0 / sn_col(k));
+    T wk = b[k];
+    if (k <= N - 3) {
+      const double d1 = ((-4.0 * pi) * (kk + 1)) * (1.0 / sn_col(k + 2));
+      S[k & 1] = S[k & 1] + up[k & 1];
+      wk = wk - mulr(S[k & 1], d1);
+    }
+    wk = divr(wk, d);
+    up[k & 1] = wk;
+    u[k] = divr(mulr(wk, 1.0 / sn_col(k)), scale);
+  }
+  u[0] = real_of(T(), c0);
+  u[N] = zero_of(T());
+  u[N + 1] = zero_of(T());
 }
 
 // Helmholtz_matvec_ptr (Matvec.pyx:656-695): b = (alfa A + beta B) v, tail zero.
@@ -379,8 +537,8 @@ template <>
 SGPU_HD df store_cast<df>(double x) { return df_from_double(x); }
 
 template <class R>
-SGPU_HD void helmholtz_factor_prog(int64_t N, const double* alfa, const double* beta, R* fac,
-                                   int64_t nsys, int64_t s) {
+SGPU_HD void helmholtz_factor_prog(int64_t N, const double* alfa, const double* beta, int neumann,
+                                   R* fac, int64_t nsys, int64_t s) {
   const int64_t M = N - 2;
   const double a = alfa[s], b = beta[s];
   R* FL = fac;
@@ -388,24 +546,35 @@ SGPU_HD void helmholtz_factor_prog(int64_t N, const double* alfa, const double* 
   R* F1 = fac + 2 * M * nsys;
   R* F2 = fac + 3 * M * nsys;
   double d0m2 = 0, d1m2 = 0, d2m2 = 0, d0m1 = 0, d1m1 = 0, d2m1 = 0;  // rows i-2, i-1
+  double bm2m2 = 0, bm2m1 = 0;  // B(i, i-2) of rows i-2, i-1 (column-scaled)
   for (int64_t i = 0; i < M; ++i) {
+    HelmRow r = helm_row(i, neumann);
+    if (i == 0 && neumann && sn_singular(b)) {
+      r.A0 = 1.0 / a;
+      r.B0 = 0.0;
+    }
     double l = 0, d0, d1 = 0, d2 = 0;
     if (i < 2) {
-      d0 = a * hA0(i) + b * hB0(i);
-      d1 = a * hA2(i) + b * hB2();
-      d2 = a * hA2(i);
+      d0 = a * r.A0 + b * r.B0;
+      d1 = a * r.A2 + b * r.B2;
+      d2 = a * r.A4;
     } else {
-      l = b * hB2() / d0m2;
-      d0 = a * hA0(i) + b * hB0(i) - l * d1m2;
-      if (i < M - 2) d1 = a * hA2(i) + b * hB2() - l * d2m2;
-      if (i < M - 4) d2 = a * hA2(i) - l * d2m2;
+      l = b * bm2m2 / d0m2;
+      d0 = a * r.A0 + b * r.B0 - l * d1m2;
+      if (i < M - 2) d1 = a * r.A2 + b * r.B2 - l * d2m2;
+      if (i < M - 4) d2 = a * r.A4 - l * d2m2;
     }
     FL[i * nsys + s] = store_cast<R>(l);
-    FD[i * nsys + s] = store_cast<R>(1.0 / d0);
+    // a Neumann zero mode is solved as u_0 = 0 (la.pyx:907-909): a zero
+    // reciprocal pivot gives exactly that
+    const bool zero_mode = neumann && i == 0 && sn_zero_mode(d0);
+    FD[i * nsys + s] = store_cast<R>(zero_mode ? 0.0 : 1.0 / d0);
     F1[i * nsys + s] = store_cast<R>(d1);
     F2[i * nsys + s] = store_cast<R>(d2);
     d0m2 = d0m1; d1m2 = d1m1; d2m2 = d2m1;
     d0m1 = d0; d1m1 = d1; d2m1 = d2;
+    bm2m2 = bm2m1;
+    bm2m1 = r.Bm2;
   }
 }
 
@@ -439,8 +608,9 @@ SGPU_HD R fac_at(const R* fac, int64_t q, int64_t k, int64_t M, int64_t nsys, in
 }
 
 template <class R, class T>
-SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac, int64_t Nb,
-                                         int64_t inner, int64_t nsys, int64_t s, int par) {
+SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac, int neumann,
+                                         int64_t Nb, int64_t inner, int64_t nsys, int64_t s,
+                                         int par) {
   typedef ElemOps<R, T> E;
   typedef typename E::V V;
   const int64_t M = Nb - 2;
@@ -470,7 +640,8 @@ SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac,
       ui = ui - E::mul(S, fac_at(fac, 3, i, M, nsys, s));
     }
     ui = E::mul(ui, fac_at(fac, 1, i, M, nsys, s));
-    E::store(u + i * inner, ui);
+    // Neumann: the recurrences run on w_i = i^2 u_i
+    E::store(u + i * inner, (neumann && i >= 1) ? E::mul(ui, from_f64<R>(1.0 / sn_col(i))) : ui);
     pend = up2;
     up2 = ui;
     have2 = true;

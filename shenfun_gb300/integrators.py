@@ -7,8 +7,8 @@ reference's form: one implicit solve per stage with the matrix of
 right-hand sides assembled from the stored nonlinear and linear terms, the
 Nyquist modes of the Fourier axes masked out of every right-hand side.
 
-Supported here: a tensor-product space with one Chebyshev ShenDirichlet axis
-and Fourier axes, L of Helmholtz type (a combination of ``div(grad(u))`` and
+Supported here: a tensor-product space with one Chebyshev ShenDirichlet or
+ShenNeumann axis and Fourier axes, L of Helmholtz type (a combination of ``div(grad(u))`` and
 ``u``, e.g. ``lambda u: nu*div(grad(u))``), so that every linear form is a
 ``sgpu_Helmholtz_matvec`` call and every solve a cached Helmholtz solve.  The
 nonlinear term N is a spectral ``Function`` (a forcing: its linear form is
@@ -33,14 +33,16 @@ __all__ = ["PDEIMEXRK", "IMEXRK011", "IMEXRK111", "IMEXRK222", "IMEXRK443"]
 
 
 class _HelmholtzForm:
-    """c = (alfa A + beta B) v along the Chebyshev ShenDirichlet axis: the
-    linear form ``inner(v, L(u))`` of an L of Helmholtz type, from its
-    TPMatrix list (A = ASDSDmat of the second derivative, B = BSDSDmat)."""
+    """c = (alfa A + beta B) v along the Chebyshev ShenDirichlet (or
+    ShenNeumann) axis: the linear form ``inner(v, L(u))`` of an L of Helmholtz
+    type, from its TPMatrix list (A = ASDSDmat / ASNSNmat of the second
+    derivative, B = BSDSDmat / BSNSNmat)."""
 
     def __init__(self, mats, T):
         mats = list(mats)
         keys = {m.get_key() for m in mats}
-        if not keys <= {"ASDSDmat", "BSDSDmat"}:
+        self.neumann = keys <= {"ASNSNmat", "BSNSNmat"}
+        if not (keys <= {"ASDSDmat", "BSDSDmat"} or self.neumann):
             raise NotImplementedError(f"linear operator with matrices {sorted(keys)}")
         ax = mats[0].axis
         shape = list(T.shape(True))
@@ -48,7 +50,7 @@ class _HelmholtzForm:
         alfa = np.zeros(shape)
         beta = np.zeros(shape)
         for m in mats:
-            if m.get_key() == "ASDSDmat":
+            if m.get_key() in ("ASDSDmat", "ASNSNmat"):
                 alfa = alfa + m.scale
             else:
                 beta = beta + m.scale
@@ -60,7 +62,8 @@ class _HelmholtzForm:
         """c = operator(v); rows past the basis dimension are zero."""
         c.zero_()
         outer, n, inner_ = view3(tuple(v.shape), self.axis)
-        _lib.call("sgpu_Helmholtz_matvec", ptr(v), ptr(c), ptr(self.alfa), ptr(self.beta), outer, n, inner_,
+        entry = "sgpu_Helmholtz_Neumann_matvec" if self.neumann else "sgpu_Helmholtz_matvec"
+        _lib.call(entry, ptr(v), ptr(c), ptr(self.alfa), ptr(self.beta), outer, n, inner_,
                   data_kind(v), stream_handle())
         return c
 

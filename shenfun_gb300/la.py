@@ -100,8 +100,10 @@ def _sum_mats(mats):
 
 # ---------------------------------------------------------------------------
 class Helmholtz:
-    """Chebyshev Dirichlet Helmholtz solver (chebyshev/la.py:131-351):
+    """Chebyshev Dirichlet / Neumann Helmholtz solver (chebyshev/la.py:131-351):
     (alfa A + beta B) u = b along one axis, one system per Fourier wavenumber.
+    A, B are ASDSD, BSDSD (ShenDirichlet) or ASNSN, BSNSN (ShenNeumann: the
+    Neumann branch, la.pyx:735-751, 907-912).
 
     Accepts the two TPMatrix objects of ``inner(v, -div(grad(u)) + c*u)`` (or
     ``(A, B, alfa, beta)`` with SpectralMatrix A, B and scalars/arrays).
@@ -111,9 +113,12 @@ class Helmholtz:
         require_cuda()
         if len(args) == 1:
             args = tuple(args[0])
+        keys = {a.get_key() for a in args[:2]}
+        self.neumann = bool(keys & {"ASNSNmat", "BSNSNmat"})
+        akey, bkey = ("ASNSNmat", "BSNSNmat") if self.neumann else ("ASDSDmat", "BSDSDmat")
         if len(args) == 2 and all(isinstance(a, TPMatrix) for a in args):
             by = {a.get_key(): a for a in args}
-            A, B = by["ASDSDmat"], by["BSDSDmat"]
+            A, B = by[akey], by[bkey]
             self.T = A.space
             self.axis = A.axis
             alfa, beta = A.scale, B.scale
@@ -146,16 +151,16 @@ class Helmholtz:
         if outer * inner != self.alfa.numel():
             raise _lib.SgpuError(_lib.ERR_ARG, "scale arrays do not match the systems")
         self._outer, self._inner = outer, inner
-        _lib.call("sgpu_LU_Helmholtz", self.N, ptr(self.alfa), ptr(self.beta), 0, ptr(self.u0),
-                  ptr(self.u1), ptr(self.u2), ptr(self.L), outer, inner, stream_handle())
+        _lib.call("sgpu_LU_Helmholtz", self.N, ptr(self.alfa), ptr(self.beta), int(self.neumann),
+                  ptr(self.u0), ptr(self.u1), ptr(self.u2), ptr(self.L), outer, inner, stream_handle())
         # factorisation cache used by __call__: reciprocal pivots, interleaved
         # [q][k][system] layout, FP64 (plain) or double-float pairs (mixed)
         self.form = _lib.FORMS[form] if form is not None else (
             self.T.form if self.T is not None else _lib.PLAIN_F64)
         nsys = outer * inner
         self._fac = torch.empty(4 * (self.N - 2) * nsys, dtype=torch.float64, device="cuda")
-        _lib.call("sgpu_helmholtz_factor", self.N, ptr(self.alfa), ptr(self.beta), outer, inner,
-                  self.form, ptr(self._fac), stream_handle())
+        _lib.call("sgpu_helmholtz_factor", self.N, ptr(self.alfa), ptr(self.beta), int(self.neumann),
+                  outer, inner, self.form, ptr(self._fac), stream_handle())
 
     def __call__(self, b, u=None, constraints=()):
         b = _raw(b)
@@ -165,8 +170,8 @@ class Helmholtz:
         outer, n, inner = view3(tuple(b.shape), self.axis)
         if n != self.N or (outer, inner) != (self._outer, self._inner):
             raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
-        _lib.call("sgpu_helmholtz_solve_cached", ptr(b), ptr(ur), ptr(self._fac), outer, n, inner,
-                  data_kind(b), self.form, stream_handle())
+        _lib.call("sgpu_helmholtz_solve_cached", ptr(b), ptr(ur), ptr(self._fac), int(self.neumann),
+                  outer, n, inner, data_kind(b), self.form, stream_handle())
         if constraints:
             idx = [0] * ur.dim()
             ur[tuple(idx)] = constraints[0][1]
@@ -177,23 +182,26 @@ class Helmholtz:
         (Solve_Helmholtz, la.pyx:845) instead of the cache."""
         b, ur = _raw(b), _raw(u)
         outer, n, inner = view3(tuple(b.shape), self.axis)
-        _lib.call("sgpu_Solve_Helmholtz", ptr(b), ptr(ur), 0, ptr(self.u0), ptr(self.u1),
-                  ptr(self.u2), ptr(self.L), outer, n, inner, data_kind(b), stream_handle())
+        _lib.call("sgpu_Solve_Helmholtz", ptr(b), ptr(ur), int(self.neumann), ptr(self.u0),
+                  ptr(self.u1), ptr(self.u2), ptr(self.L), outer, n, inner, data_kind(b),
+                  stream_handle())
         return u
 
     def matvec(self, v, c):
         v, cr = _raw(v), _raw(c)
         outer, n, inner = view3(tuple(v.shape), self.axis)
-        _lib.call("sgpu_Helmholtz_matvec", ptr(v), ptr(cr), ptr(self.alfa), ptr(self.beta),
-                  outer, n, inner, data_kind(v), stream_handle())
+        entry = "sgpu_Helmholtz_Neumann_matvec" if self.neumann else "sgpu_Helmholtz_matvec"
+        _lib.call(entry, ptr(v), ptr(cr), ptr(self.alfa), ptr(self.beta), outer, n, inner,
+                  data_kind(v), stream_handle())
         return c
 
 
 class SolverGeneric1ND:
     """One non-periodic axis, one banded system per Fourier wavenumber
     (la.py:1183-1434).  Dispatches on the basis of the non-periodic axis:
-    Chebyshev ShenDirichlet -> the Helmholtz kernels (the reference falls back
-    to a sparse LU per wavenumber there, la.py:1299-1364)."""
+    Chebyshev ShenDirichlet / ShenNeumann -> the Helmholtz kernels (the
+    reference falls back to a sparse LU per wavenumber there,
+    la.py:1299-1364)."""
 
     def __init__(self, mats):
         mats = list(mats)
@@ -202,15 +210,16 @@ class SolverGeneric1ND:
         base = T.bases[ax]
         keys = {m.get_key() for m in mats}
         self.T, self.axis = T, ax
-        if base.family() == "chebyshev" and base.short_name() == "SD" and keys <= {"ASDSDmat", "BSDSDmat"}:
+        sn = base.short_name()
+        if base.family() == "chebyshev" and sn in ("SD", "SN") and keys <= {f"A{sn}{sn}mat", f"B{sn}{sn}mat"}:
             by = {m.get_key(): m for m in mats}
             shape = list(T.shape(True))
             shape[ax] = 1
-            A = by.get("ASDSDmat")
-            B = by.get("BSDSDmat")
+            A = by.get(f"A{sn}{sn}mat")
+            B = by.get(f"B{sn}{sn}mat")
             alfa = A.scale if A is not None else np.zeros(shape)
             beta = B.scale if B is not None else np.zeros(shape)
-            self._impl = Helmholtz(_tp("ASDSDmat", alfa, T, ax), _tp("BSDSDmat", beta, T, ax))
+            self._impl = Helmholtz(_tp(f"A{sn}{sn}mat", alfa, T, ax), _tp(f"B{sn}{sn}mat", beta, T, ax))
         else:
             self._impl = BandSepSolver(mats)
 
@@ -276,8 +285,65 @@ class Biharmonic(BandSepSolver):
 
 def _tp(key, scale, T, ax):
     from .matrices import galerkin_matrix
-    order = {"ASDSDmat": 2, "BSDSDmat": 0}[key]
+    order = {"ASDSDmat": 2, "BSDSDmat": 0, "ASNSNmat": 2, "BSNSNmat": 0}[key]
     return TPMatrix(galerkin_matrix(T.bases[ax], order), np.asarray(scale, dtype=float), T, ax)
+
+
+class _PoissonSolver:
+    """scale * A u = b along one axis for a single Chebyshev stiffness matrix
+    (SparseMatrixSolver.__call__, la.py:199-270)."""
+
+    key = None
+    entry = None
+
+    def __init__(self, mats):
+        require_cuda()
+        mats = mats if isinstance(mats, (list, tuple)) else [mats]
+        if len(mats) != 1 or mats[0].get_key() != self.key:
+            raise ValueError(f"{type(self).__name__} takes one {self.key}")
+        self.mat = mats[0]
+        sc = self.mat.scale
+        if isinstance(self.mat, TPMatrix) or not np.isscalar(sc) and np.size(sc) != 1:
+            raise NotImplementedError("a scalar-scaled 1D stiffness matrix")
+        self.scale = float(np.asarray(sc).reshape(-1)[0]) * getattr(self.mat, "sign", 1)
+        self.N = self.mat.shape[0] + 2
+
+    def _run(self, b, u, axis, extra=()):
+        b = _raw(b)
+        if u is None:
+            u = b
+        ur = _raw(u)
+        outer, n, inner = view3(tuple(b.shape), axis)
+        if n != self.N or tuple(ur.shape) != tuple(b.shape):
+            raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
+        _lib.call(self.entry, ptr(b), ptr(ur), self.scale, *extra, outer, n, inner, data_kind(b),
+                  stream_handle())
+        return u
+
+
+class ADDSolver(_PoissonSolver):
+    """Chebyshev ShenDirichlet Poisson solve, A = ASDSD (chebyshev/la.py:11-71,
+    Poisson_Solve_ADD la.pyx:614-706): back substitution with running sums."""
+
+    key = "ASDSDmat"
+    entry = "sgpu_Poisson_Solve_ADD"
+
+    def __call__(self, b, u=None, axis=0, constraints=()):
+        return self._run(b, u, axis)
+
+
+class ANNSolver(_PoissonSolver):
+    """Chebyshev ShenNeumann Poisson solve, A = ASNSN (chebyshev/la.py:74-128):
+    the mean mode is fixed by the constraint u_0 = value (default 0)."""
+
+    key = "ASNSNmat"
+    entry = "sgpu_Poisson_Solve_ANN"
+
+    def __call__(self, b, u=None, axis=0, constraints=((0, 0),)):
+        cons = tuple(constraints)
+        if len(cons) != 1 or cons[0][0] != 0:
+            raise NotImplementedError("one constraint on row 0")
+        return self._run(b, u, axis, (float(cons[0][1]),))
 
 
 Solver = SolverGeneric1ND

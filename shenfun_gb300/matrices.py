@@ -8,6 +8,7 @@ solvers (which copy what they need to the device).
                            A = ASDSD (chebyshev/matrices.py:1061-1079)
   Chebyshev ShenBiharmonic: B = BSBSB (:515-528), A = ASBSB (:1008-1017),
                             S = SSBSB (:1444-1458)
+  Chebyshev ShenNeumann: B = BSNSN (:377-401), A = ASNSN (:1096-1122)
   Legendre ShenDirichlet: B = BSDSD (legendre/matrices.py:121-135),
                           A = ASDSD (legendre/matrices.py:285-292)
   Legendre ShenBiharmonic: B = BSBSB (legendre/matrices.py:179-192)
@@ -70,6 +71,24 @@ def cheb_sd_A(N, space=None):
          4: -4 * np.pi * (k[:N - 6] + 1)}
     return SpectralMatrix("ASDSDmat", d, (N - 2, N - 2), space, space,
                           upper_rows=lambda i, j: -4 * np.pi * (i + 1))
+
+
+def cheb_sn_B(N, space=None):
+    h = cheb_norm_sq(N)
+    k = np.arange(N, dtype=float)
+    al = (k / (k + 2)) ** 2
+    d = {0: h[:-2] + al[:-2] ** 2 * h[2:], 2: -al[:N - 4] * h[2:N - 2]}
+    d[-2] = d[2].copy()
+    return SpectralMatrix("BSNSNmat", d, (N - 2, N - 2), space, space)
+
+
+def cheb_sn_A(N, space=None):
+    k = np.arange(N - 2, dtype=float)
+    d = {0: -2 * np.pi * k ** 2 * (k + 1) / (k + 2),
+         2: -4 * np.pi * (k[:-2] + 2) ** 2 * (k[:-2] + 1) / (k[:-2] + 2) ** 2,
+         4: -4 * np.pi * (k[:-4] + 4) ** 2 * (k[:-4] + 1) / (k[:-4] + 2) ** 2}
+    return SpectralMatrix("ASNSNmat", d, (N - 2, N - 2), space, space,
+                          upper_rows=lambda i, j: -4 * np.pi * j ** 2 * (i + 1) / (i + 2) ** 2)
 
 
 def cheb_sb_stencil(N):
@@ -137,6 +156,7 @@ def galerkin_matrix(space, order):
         ("chebyshev", "SD", 0): cheb_sd_B, ("chebyshev", "SD", 2): cheb_sd_A,
         ("chebyshev", "SB", 0): cheb_sb_B, ("chebyshev", "SB", 2): cheb_sb_A,
         ("chebyshev", "SB", 4): cheb_sb_S,
+        ("chebyshev", "SN", 0): cheb_sn_B, ("chebyshev", "SN", 2): cheb_sn_A,
         ("legendre", "SD", 0): leg_sd_B,
         ("legendre", "SB", 0): leg_sb_B,
     }

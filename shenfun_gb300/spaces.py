@@ -304,6 +304,24 @@ class ChebyshevShenDirichlet(ChebyshevBase):
         return "Dirichlet"
 
 
+class ChebyshevShenNeumann(ChebyshevBase):
+    """phi_k = T_k - (k/(k+2))^2 T_{k+2} (chebyshev/bases.py:863-945):
+    u'(-1) = u'(1) = 0."""
+
+    basis_id = _lib.BASIS_SN
+
+    def num_bcs(self):
+        return 2
+
+    @staticmethod
+    def short_name():
+        return "SN"
+
+    @staticmethod
+    def boundary_condition():
+        return "Neumann"
+
+
 class ChebyshevShenBiharmonic(ChebyshevBase):
     """phi_k = T_k - 2(k+2)/(k+3) T_{k+2} + (k+1)/(k+3) T_{k+4}
     (chebyshev/bases.py:1175-1258)."""
@@ -323,6 +341,24 @@ class ChebyshevShenBiharmonic(ChebyshevBase):
 
 
 # ---------------------------------------------------------------------------
+def _bc_kinds(bc):
+    """(ordered condition names, values) of a boundary-condition argument:
+    a tuple of Dirichlet values (2: left/right, 4: biharmonic) or the
+    reference's dict form {'left': {'D': a, 'N': b}, 'right': {...}}
+    (spectralbase.py BoundaryConditions, forms/arguments.py:155-188)."""
+    if bc is None:
+        return "", ()
+    if isinstance(bc, dict):
+        names, vals = [], []
+        for side, tag in (("left", "L"), ("right", "R")):
+            for key, v in (bc.get(side) or {}).items():
+                names.append(tag + key)
+                vals.append(v)
+        return "".join(names), tuple(vals)
+    vals = tuple(bc)
+    return {0: "", 2: "LDRD", 4: "LDLNRDRN"}.get(len(vals), "?"), vals
+
+
 def FunctionSpace(N, family="Fourier", bc=None, dtype="d", quad=None, domain=None, **kw):
     """Pick the 1D space from family and boundary conditions
     (forms/arguments.py:30-418; bc tuples of zeros only - homogeneous)."""
@@ -333,12 +369,18 @@ def FunctionSpace(N, family="Fourier", bc=None, dtype="d", quad=None, domain=Non
         if np.dtype(dtype).char in "FDG":
             return C2C(N, domain=dom, padding_factor=pf)
         return R2C(N, domain=dom, padding_factor=pf)
-    nb = 0 if bc is None else len(bc)
-    if bc is not None and any(v != 0 for v in bc):
+    kinds, vals = _bc_kinds(bc)
+    nb = len(vals)
+    if any(v != 0 for v in vals):
         raise NotImplementedError("only homogeneous boundary conditions are on the GPU path")
     dom = domain if domain is not None else (-1.0, 1.0)
+    basis = kw.get("basis")
     if fam in ("c", "chebyshev"):
         q = quad or "GC"
+        if basis == "ShenNeumann" or kinds == "LNRN":
+            return ChebyshevShenNeumann(N, quad=q, domain=dom)
+        if basis not in (None, "ShenDirichlet", "ShenBiharmonic", "Orthogonal") or kinds not in ("", "LDRD", "LDLNRDRN"):
+            raise NotImplementedError(f"Chebyshev basis {basis or kinds!r}")
         if nb == 0:
             return ChebyshevOrthogonal(N, quad=q, domain=dom)
         if nb == 2:

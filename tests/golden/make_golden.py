@@ -346,9 +346,88 @@ def dealias():
     put("dealias", **d)
 
 
+# --------------------------------------------------------------------------
+# Chebyshev ShenNeumann and the Poisson solvers: SN transforms
+# (chebyshev/bases.py:863-945), the Neumann branch of LU_Helmholtz /
+# Solve_Helmholtz (la.pyx:733-751, 907-912) with Helmholtz_Neumann_matvec
+# (Matvec.pyx:722-800), ADDSolver (chebyshev/la.py:11-71, la.pyx:614-706) and
+# ANNSolver (chebyshev/la.py:74-128).  Own rng, so the group reproduces alone.
+def neumann():
+    g = np.random.default_rng(59)
+    d = {}
+    bcN = {"left": {"N": 0}, "right": {"N": 0}}
+    for N in (8, 9, 16, 17, 33):
+        V = FunctionSpace(N, "C", bc=bcN)
+        assert V.short_name() == "SN"
+        f = g.standard_normal(N)
+        d[f"sn{N}_f"] = f
+        d[f"sn{N}_sp"] = V.scalar_product(f.copy(), np.zeros(N)).copy()
+        d[f"sn{N}_fw"] = V.forward(f.copy(), np.zeros(N)).copy()
+        uh = np.zeros(N)
+        uh[:N - 2] = g.standard_normal(N - 2)
+        d[f"sn{N}_uh"] = uh
+        d[f"sn{N}_bw"] = V.backward(uh.copy(), np.zeros(N)).copy()
+    for (Nx, Ny, Nz, c) in ((6, 4, 16, 0.0), (4, 6, 17, 50.0), (8, 8, 33, 1000.0)):
+        F0 = FunctionSpace(Nx, "F", dtype="D")
+        F1 = FunctionSpace(Ny, "F", dtype="d")
+        SN = FunctionSpace(Nz, "C", bc=bcN)
+        T = TensorProductSpace(comm, (F0, F1, SN))
+        u, v = TrialFunction(T), TestFunction(T)
+        mats = inner(v, -div(grad(u)) + c * u)
+        H = chebyshev.la.Helmholtz(*mats)
+        assert H.neumann
+        fh = Function(T)
+        fh[:] = g.standard_normal(fh.shape) + 1j * g.standard_normal(fh.shape)
+        fh[..., -2:] = 0
+        uh = H(fh.copy(), Function(T))
+        key = f"h{Nx}x{Ny}x{Nz}"
+        d.update({key + "_c": c, key + "_alfa": H.alfa, key + "_beta": H.beta,
+                  key + "_d0": H.u0, key + "_d1": H.u1, key + "_d2": H.u2, key + "_L": H.L,
+                  key + "_f": fh, key + "_u": uh})
+    # Helmholtz_Neumann_matvec does not run under numpy 2 (its 1/j2 lands in
+    # an integer array, Matvec.pyx:785-788): record the reference's own
+    # ASNSN / BSNSN matrices instead, the matvec's definition
+    for N in (16, 17):
+        SN = FunctionSpace(N, "C", bc=bcN)
+        A = inner(TestFunction(SN), div(grad(TrialFunction(SN))))
+        B = inner(TestFunction(SN), TrialFunction(SN))
+        d.update({f"snA{N}": A.diags("csr").toarray(), f"snB{N}": B.diags("csr").toarray()})
+    # Poisson solvers along one axis
+    for N in (16, 17, 32):
+        SD = FunctionSpace(N, "C", bc=(0, 0))
+        A = inner(TestFunction(SD), div(grad(TrialFunction(SD))))
+        sol = chebyshev.la.ADDSolver(A)
+        b = Function(SD)
+        b[:] = g.standard_normal(N)
+        b[-2:] = 0
+        x = sol(b.copy(), Function(SD))
+        d.update({f"add{N}_b": b, f"add{N}_u": x, f"add{N}_scale": A.scale,
+                  f"add{N}_A0": np.asarray(A[0]), f"add{N}_A2": np.broadcast_to(A[2], (N - 4,)).copy()})
+        SN = FunctionSpace(N, "C", bc=bcN)
+        A = inner(TestFunction(SN), -div(grad(TrialFunction(SN))))
+        sol = chebyshev.la.ANNSolver(A)
+        b = Function(SN)
+        b[:] = g.standard_normal(N)
+        b[-2:] = 0
+        x = sol(b.copy(), Function(SN))
+        d.update({f"ann{N}_b": b, f"ann{N}_u": x, f"ann{N}_scale": A.scale,
+                  f"ann{N}_A0": np.asarray(A[0]), f"ann{N}_A2": np.asarray(A[2])})
+    # ADD on a 2D array along either axis (the compiled kernel, la.pyx:614-629)
+    from shenfun.optimization.cython import la as cla
+    SD = FunctionSpace(20, "C", bc=(0, 0))
+    A = inner(TestFunction(SD), div(grad(TrialFunction(SD))))
+    for ax in (0, 1):
+        shape = (20, 5) if ax == 0 else (5, 20)
+        b = g.standard_normal(shape) + 1j * g.standard_normal(shape)
+        u = np.zeros_like(b)
+        cla.Poisson_Solve_ADD(A, b.copy(), u, ax)
+        d.update({f"add2d{ax}_b": b, f"add2d{ax}_u": u})
+    put("neumann", **d)
+
+
 GROUPS = {"cheb_1d": cheb_1d, "fourier_1d": fourier_1d, "banded": banded, "helmholtz": helmholtz,
           "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex,
-          "dealias": dealias}
+          "dealias": dealias, "neumann": neumann}
 
 if __name__ == "__main__":
     # no arguments: every group (the shared rng makes the earlier groups depend

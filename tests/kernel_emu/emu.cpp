@@ -10,6 +10,9 @@
 //   emu hlu    N outer inner alfa.bin beta.bin out.bin        (d0|d1|d2|L)
 //   emu hsolve N outer inner data_kind b.bin fac.bin out.bin   (fac = d0|d1|d2|L)
 //   emu hmatvec N outer inner data_kind v.bin alfa.bin beta.bin out.bin
+//   emu nlu|nsolve|ncached ...   the same with the Neumann branch (ShenNeumann)
+//   emu nmatvec N outer inner data_kind v.bin alfa.bin beta.bin out.bin
+//   emu padd|pann N outer inner data_kind scale b.bin out.bin   (Poisson ADD / ANN)
 //   emu tdma|pdma n outer inner data_kind raw.bin u.bin out.bin (LU then solve)
 //   emu ozaki  N nlines inner cplx precise in.bin M.bin out.bin (split-BF16 contraction)
 #include <cmath>
@@ -229,6 +232,11 @@ static int ozaki(int argc, char** argv) {
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   std::string mode = argv[1];
+  int nm = 0;  // Neumann branch of the Helmholtz programs
+  if (mode == "nlu" || mode == "nsolve" || mode == "ncached") {
+    nm = 1;
+    mode = "h" + mode.substr(1);
+  }
   if (mode == "xform") return xform(argc, argv);
   if (mode == "ozaki") return ozaki(argc, argv);
   if (mode == "lkcheck") {
@@ -281,7 +289,7 @@ int main(int argc, char** argv) {
     size_t cnt = (size_t)outer * N * inner;
     double* all = (double*)calloc(4 * cnt, sizeof(double));
     for (int i = 0; i < 4; ++i) f[i] = all + i * cnt;
-    for (long long s = 0; s < ns; ++s) helmholtz_lu_prog(N, a, b, f[0], f[1], f[2], f[3], inner, s);
+    for (long long s = 0; s < ns; ++s) helmholtz_lu_prog(N, a, b, nm, f[0], f[1], f[2], f[3], inner, s);
     write_exact(argv[7], all, 4 * cnt);
     return 0;
   }
@@ -296,10 +304,10 @@ int main(int argc, char** argv) {
     for (size_t i = 0; i < cnt * w; ++i) u[i] = 0.0;
     for (long long s = 0; s < outer * inner; ++s) {
       if (dk)
-        helmholtz_solve_prog<cd>((const cd*)b, (cd*)u, fac, fac + cnt, fac + 2 * cnt, fac + 3 * cnt,
+        helmholtz_solve_prog<cd>((const cd*)b, (cd*)u, nm, fac, fac + cnt, fac + 2 * cnt, fac + 3 * cnt,
                                  N, inner, s);
       else
-        helmholtz_solve_prog<double>(b, u, fac, fac + cnt, fac + 2 * cnt, fac + 3 * cnt, N, inner, s);
+        helmholtz_solve_prog<double>(b, u, nm, fac, fac + cnt, fac + 2 * cnt, fac + 3 * cnt, N, inner, s);
     }
     write_exact(argv[8], u, cnt * w);
     return 0;
@@ -317,16 +325,16 @@ int main(int argc, char** argv) {
     for (size_t i = 0; i < cnt; ++i) u[i] = 0.0;
     void* fac = malloc(8 * 4 * (size_t)M * ns);
     for (long long s = 0; s < ns; ++s) {
-      if (form) helmholtz_factor_prog<df>(N, a, be, (df*)fac, ns, s);
-      else helmholtz_factor_prog<double>(N, a, be, (double*)fac, ns, s);
+      if (form) helmholtz_factor_prog<df>(N, a, be, nm, (df*)fac, ns, s);
+      else helmholtz_factor_prog<double>(N, a, be, nm, (double*)fac, ns, s);
     }
     for (long long t = 0; t < 2 * ns; ++t) {
       long long s = t >> 1;
       int par = (int)(t & 1);
-      if (form && dk) helmholtz_cached_solve_prog<df, cd>((const cd*)b, (cd*)u, (const df*)fac, N, inner, ns, s, par);
-      else if (form) helmholtz_cached_solve_prog<df, double>(b, u, (const df*)fac, N, inner, ns, s, par);
-      else if (dk) helmholtz_cached_solve_prog<double, cd>((const cd*)b, (cd*)u, (const double*)fac, N, inner, ns, s, par);
-      else helmholtz_cached_solve_prog<double, double>(b, u, (const double*)fac, N, inner, ns, s, par);
+      if (form && dk) helmholtz_cached_solve_prog<df, cd>((const cd*)b, (cd*)u, (const df*)fac, nm, N, inner, ns, s, par);
+      else if (form) helmholtz_cached_solve_prog<df, double>(b, u, (const df*)fac, nm, N, inner, ns, s, par);
+      else if (dk) helmholtz_cached_solve_prog<double, cd>((const cd*)b, (cd*)u, (const double*)fac, nm, N, inner, ns, s, par);
+      else helmholtz_cached_solve_prog<double, double>(b, u, (const double*)fac, nm, N, inner, ns, s, par);
     }
     write_exact(argv[10], u, cnt);
     return 0;
@@ -354,6 +362,42 @@ int main(int argc, char** argv) {
       else band_sep_solve_prog<double>(b, u, fac, g, n, Nb, 1, nsys, ch);
     }
     write_exact(argv[12], u, cnt);
+    return 0;
+  }
+  if (mode == "nmatvec") {
+    long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]);
+    size_t cnt = (size_t)outer * N * inner * (dk ? 2 : 1);
+    double* v = read_exact(argv[6], cnt);
+    double* a = read_exact(argv[7], outer * inner);
+    double* be = read_exact(argv[8], outer * inner);
+    double* out = (double*)malloc(sizeof(double) * cnt);
+    for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
+    for (long long s = 0; s < outer * inner; ++s) {
+      if (dk) helmholtz_neumann_matvec_prog<cd>((const cd*)v, (cd*)out, a, be, N, inner, s);
+      else helmholtz_neumann_matvec_prog<double>(v, out, a, be, N, inner, s);
+    }
+    write_exact(argv[9], out, cnt);
+    return 0;
+  }
+  if (mode == "padd" || mode == "pann") {
+    long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]);
+    double scale = atof(argv[6]);
+    size_t cnt = (size_t)outer * N * inner * (dk ? 2 : 1);
+    double* b = read_exact(argv[7], cnt);
+    double* u = (double*)malloc(sizeof(double) * cnt);
+    for (size_t i = 0; i < cnt; ++i) u[i] = std::numeric_limits<double>::quiet_NaN();
+    for (long long s = 0; s < outer * inner; ++s) {
+      if (mode == "padd") {
+        if (dk) poisson_add_prog<cd>((const cd*)b, (cd*)u, scale, N, inner, s);
+        else poisson_add_prog<double>(b, u, scale, N, inner, s);
+      } else {
+        if (dk) poisson_ann_prog<cd>((const cd*)b, (cd*)u, scale, 0.0, N, inner, s);
+        else poisson_ann_prog<double>(b, u, scale, 0.0, N, inner, s);
+      }
+    }
+    write_exact(argv[8], u, cnt);
     return 0;
   }
   if (mode == "hmatvec") {

@@ -48,7 +48,14 @@ def test_argument_checks_without_device(lib):
     assert lib.sgpu_plan_create(ctypes.byref(h), _lib.XF_CHEB_SCALAR, 16, 7, 0) == _lib.ERR_ARG
     assert lib.sgpu_plan_create(ctypes.byref(h), _lib.XF_R2C, 16, 0, 5) == _lib.ERR_UNSUPPORTED
     assert lib.sgpu_LU_Helmholtz(16, None, None, 1, None, None, None, None, 1, 1, None) == \
-        _lib.ERR_UNSUPPORTED
+        _lib.ERR_ARG
+    # neumann must be 0 or 1; Poisson solves need a nonzero scale
+    buf = (ctypes.c_double * 64)()
+    assert lib.sgpu_LU_Helmholtz(16, buf, buf, 2, buf, buf, buf, buf, 1, 1, None) == _lib.ERR_ARG
+    assert lib.sgpu_Poisson_Solve_ADD(buf, buf, ctypes.c_double(0.0), 1, 16, 1, 0, None) == _lib.ERR_ARG
+    assert lib.sgpu_Poisson_Solve_ANN(buf, buf, ctypes.c_double(1.0), ctypes.c_double(0.0), 1, 4, 1, 0,
+                                      None) == _lib.ERR_ARG
+    assert lib.sgpu_plan_create(ctypes.byref(h), _lib.XF_CHEB_SCALAR, 16, 4, 0) == _lib.ERR_ARG
     assert lib.sgpu_Solve_Helmholtz(None, None, 0, None, None, None, None, 1, 16, 1, 1, None) == \
         _lib.ERR_ARG
     assert lib.sgpu_TDMA_Solve(None, None, 1, 16, 1, 0, None) == _lib.ERR_ARG

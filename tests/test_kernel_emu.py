@@ -24,7 +24,7 @@ CSRC = os.path.join(REPO, "shenfun_gb300", "csrc")
 
 # transform kinds / bases (include/shenfun_gb300.h)
 R2C, C2R, C2C_FWD, C2C_BWD, DCT2, DCT3, CHEB_SCALAR, CHEB_FORWARD, CHEB_BACKWARD = range(1, 10)
-BASIS = {"T": 0, "SD": 1, "SB": 2}
+BASIS = {"T": 0, "SD": 1, "SB": 2, "SN": 3}
 
 
 def _emu_stamp():
@@ -133,7 +133,7 @@ def test_raw_dct(emu, n, cplx):
 
 
 @pytest.mark.parametrize("n", [12, 16, 17, 33, 64, 129, 257])
-@pytest.mark.parametrize("basis", ["T", "SD", "SB"])
+@pytest.mark.parametrize("basis", ["T", "SD", "SB", "SN"])
 @pytest.mark.parametrize("layout", ["last", "middle"])
 @pytest.mark.parametrize("cplx", [False, True])
 def test_chebyshev(emu, n, basis, layout, cplx):
@@ -252,7 +252,7 @@ def test_df_fourier(emu, n):
 
 
 @pytest.mark.parametrize("n", [16, 17, 64, 129, 257])
-@pytest.mark.parametrize("basis", ["T", "SD", "SB"])
+@pytest.mark.parametrize("basis", ["T", "SD", "SB", "SN"])
 @pytest.mark.parametrize("cplx", [False, True])
 def test_df_chebyshev(emu, n, basis, cplx):
     x = rng.standard_normal((3, 2, n))
@@ -327,3 +327,59 @@ def test_ozaki_ignored_tail_rows(emu):
     res = run(emu, ["ozaki", N, nlines, 1, 0, 0], [x, M], x.size).reshape(x.shape)
     ref = x[:, :-2] @ M[:-2, :]
     assert np.abs(res - ref).max() / np.abs(ref).max() < 5e-13
+
+
+# --------------------------------------------------------------------------
+# Chebyshev ShenNeumann: Helmholtz Neumann branch, Neumann matvec, Poisson
+# ADD / ANN solves (la.pyx:735-751, 907-912; chebyshev/la.py:11-128)
+@pytest.mark.parametrize("N,outer,inner", [(8, 1, 3), (17, 4, 1), (33, 2, 5), (257, 2, 3)])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_helmholtz_neumann(emu, N, outer, inner, cplx):
+    ns = outer * inner
+    alfa = -np.ones(ns)
+    beta = rng.uniform(0.5, 2000.0, ns)
+    beta[0] = 0.0  # the pure-stiffness (zero-mode) system
+    fac = run(emu, ["nlu", N, outer, inner], [alfa, beta], 4 * outer * N * inner)
+    fac = fac.reshape(4, outer, N, inner)
+    d0, d1, d2, L = la.helmholtz_lu(N, alfa, beta, neumann=True)
+    to_sys = lambda a: np.moveaxis(a, 1, -1).reshape(ns, N)  # noqa: E731
+    for got, ref in zip(fac, (d0, d1, d2, L)):
+        assert rel(to_sys(got), ref) < 1e-14
+    f = rng.standard_normal((outer, N, inner))
+    if cplx:
+        f = f + 1j * rng.standard_normal((outer, N, inner))
+    cnt = outer * N * inner * (2 if cplx else 1)
+    uref = la.helmholtz_solve(to_sys(f), d0, d1, d2, L, neumann=True)
+    u = run(emu, ["nsolve", N, outer, inner, int(cplx)], [f, fac], cnt)
+    u = (u.view(np.complex128) if cplx else u).reshape(outer, N, inner)
+    assert rel(to_sys(u)[:, :N - 2], uref[:, :N - 2]) < 1e-13
+    for form in (0, 1):
+        uc = run(emu, ["ncached", N, outer, inner, int(cplx), form], [alfa, beta, f], cnt)
+        uc = (uc.view(np.complex128) if cplx else uc).reshape(outer, N, inner)
+        assert rel(to_sys(uc)[:, :N - 2], uref[:, :N - 2]) < (1e-13 if form == 0 else 1e-12)
+    mv = run(emu, ["nmatvec", N, outer, inner, int(cplx)], [u, alfa, beta], cnt)
+    mv = (mv.view(np.complex128) if cplx else mv).reshape(outer, N, inner)
+    ref = la.helmholtz_neumann_matvec(to_sys(u), alfa, beta)
+    assert rel(to_sys(mv), ref) < 1e-13
+    # the matvec undoes the solve on the dofs of the regular systems
+    assert rel(to_sys(mv)[1:, :N - 2], to_sys(f)[1:, :N - 2]) < 1e-11
+
+
+@pytest.mark.parametrize("N,outer,inner", [(8, 1, 1), (17, 3, 2), (32, 2, 5), (257, 1, 3)])
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("which", ["padd", "pann"])
+def test_poisson(emu, N, outer, inner, cplx, which):
+    b = rng.standard_normal((outer, N, inner))
+    if cplx:
+        b = b + 1j * rng.standard_normal(b.shape)
+    scale = -1.0
+    cnt = outer * N * inner * (2 if cplx else 1)
+    u = run(emu, [which, N, outer, inner, int(cplx), repr(scale)], [b], cnt)
+    u = (u.view(np.complex128) if cplx else u).reshape(outer, N, inner)
+    if which == "padd":
+        A = la.cheb_sd_stiffness(N)
+        ref = la.add_solve(b, A[0], -4 * np.pi * (np.arange(N - 4) + 1.0), scale, axis=1)
+    else:
+        A = la.cheb_sn_stiffness(N)
+        ref = la.ann_solve(b, A[0], A[2], scale, axis=1)
+    assert rel(u, ref) < 1e-13

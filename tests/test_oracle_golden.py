@@ -169,3 +169,61 @@ def test_dealias_oracle(golden, shape):
     assert np.abs(fh - d[f"{tag}_padded_forward"]).max() < 1e-13 * np.abs(fh).max()
     sh = D.padded_forward(d[f"{tag}_padded_in"], bases, fac, scalar=True)
     assert np.abs(sh - d[f"{tag}_padded_scalar"]).max() < 1e-13 * np.abs(sh).max()
+
+
+# --------------------------------------------------------------------------
+# Chebyshev ShenNeumann and the Poisson solvers (neumann.npz)
+@pytest.mark.parametrize("N", [8, 9, 16, 17, 33])
+def test_shen_neumann_1d(golden, N):
+    d = golden("neumann")
+    f = d[f"sn{N}_f"]
+    assert rel(S.cheb_scalar_product(f, "SN"), d[f"sn{N}_sp"]) < TOL
+    assert rel(S.cheb_forward(f, "SN"), d[f"sn{N}_fw"]) < TOL
+    assert rel(S.cheb_backward(d[f"sn{N}_uh"], "SN"), d[f"sn{N}_bw"]) < TOL
+
+
+@pytest.mark.parametrize("N", [16, 17])
+def test_shen_neumann_matrices(golden, N):
+    A, B = la.cheb_sn_dense(N)
+    d = golden("neumann")
+    assert rel(A, d[f"snA{N}"]) < TOL
+    assert rel(B, d[f"snB{N}"]) < TOL
+
+
+@pytest.mark.parametrize("key", ["h6x4x16", "h4x6x17", "h8x8x33"])
+def test_helmholtz_neumann(golden, key):
+    d = golden("neumann")
+    f = d[key + "_f"]
+    N = f.shape[-1]
+    sys = f.shape[:-1] + (1,)
+    alfa = np.broadcast_to(d[key + "_alfa"], sys).reshape(-1)
+    beta = np.broadcast_to(d[key + "_beta"], sys).reshape(-1)
+    fac = la.helmholtz_lu(N, alfa, beta, neumann=True)
+    for got, name in zip(fac, ("_d0", "_d1", "_d2", "_L")):
+        assert np.array_equal(got, d[key + name].reshape(-1, N))  # bit-exact LU
+    u = la.helmholtz_solve(f.reshape(-1, N), *fac, neumann=True)
+    assert rel(u, d[key + "_u"].reshape(-1, N)) < TOL
+    # the definition of the matvec undoes the solve (zero mode excluded)
+    mv = la.helmholtz_neumann_matvec(u, alfa, beta)
+    reg = np.abs(beta) >= 1e-8
+    assert rel(mv[reg, :N - 2], f.reshape(-1, N)[reg, :N - 2]) < 1e-11
+
+
+@pytest.mark.parametrize("N", [16, 17, 32])
+def test_poisson_add_ann(golden, N):
+    d = golden("neumann")
+    u = la.add_solve(d[f"add{N}_b"], d[f"add{N}_A0"], d[f"add{N}_A2"], float(d[f"add{N}_scale"]))
+    assert rel(u, d[f"add{N}_u"]) < TOL
+    u = la.ann_solve(d[f"ann{N}_b"], d[f"ann{N}_A0"], d[f"ann{N}_A2"], float(d[f"ann{N}_scale"]))
+    assert rel(u, d[f"ann{N}_u"]) < TOL
+
+
+@pytest.mark.parametrize("axis", [0, 1])
+def test_poisson_add_2d(golden, axis):
+    d = golden("neumann")
+    A = la.cheb_sd_stiffness(20)
+    u = la.add_solve(d[f"add2d{axis}_b"], A[0], A[2], 1.0, axis=axis)
+    ref = d[f"add2d{axis}_u"]
+    sl = [slice(None)] * 2
+    sl[axis] = slice(0, 18)  # the compiled kernel writes the dofs only
+    assert rel(u[tuple(sl)], ref[tuple(sl)]) < TOL
