@@ -53,6 +53,13 @@ extern "C" {
 #define SGPU_BASIS_SB 2     /* ShenBiharmonic (chebyshev/bases.py:1249) */
 #define SGPU_BASIS_SN 3     /* ShenNeumann phi_k = T_k - (k/(k+2))^2 T_{k+2}
                                (chebyshev/bases.py:863-937), Chebyshev only */
+/* flag OR'ed into SGPU_BASIS_SD / SGPU_BASIS_SN: non-homogeneous boundary
+ * values.  A SGPU_XF_CHEB_BACKWARD plan then adds the boundary functions of
+ * the last two coefficients (the boundary dofs) of every line, SD
+ * (T0 -/+ T1)/2 and SN T1/2 -/+ T2/8 (BoundaryValues._add_to_orthogonal,
+ * tensorproductspace.py:2072-2089); the other kinds ignore the flag (the
+ * forward lift is sgpu_bc_apply). */
+#define SGPU_BASIS_BC 0x10
 
 /* transform kinds */
 #define SGPU_XF_R2C 1        /* rfft along axis, n -> n/2+1 (FFTW r2c)             */
@@ -166,6 +173,20 @@ int sgpu_Helmholtz_matvec(const void* v, void* b, const double* alfa, const doub
 int sgpu_Helmholtz_Neumann_matvec(const void* v, void* b, const double* alfa,
                                   const double* beta, int64_t outer, int64_t N, int64_t inner,
                                   int data_kind, cudaStream_t stream);
+
+/* ---- non-homogeneous boundary values (tensorproductspace.py:1909-2128) ----
+ * For every line of u (outer, N, inner) along a Chebyshev SD / SN axis, with
+ * boundary values g0, g1 = g[o][0|1][i] (g has u's element type):
+ *   u[k] -= (alfa_s CA[k][0] + beta_s CB[k][0]) g0 + (... [1]) g1, k < N-2,
+ * CA, CB row-major (N-2) x 2 (either may be NULL; alfa / beta NULL mean 1),
+ * s = o * inner + i; then, if set_dofs, u[N-2] = g0, u[N-1] = g1.
+ * The forward lift (BoundaryValues._add_mass_rhs followed by the mass solve)
+ * is CA = B^-1 B_bc; the Helmholtz right-hand side (the boundary matrices of
+ * chebyshev.la.Helmholtz.__call__) is CA = A_bc, CB = B_bc with the solver's
+ * scales. */
+int sgpu_bc_apply(void* u, const double* CA, const double* alfa, const double* CB,
+                  const double* beta, const void* g, int64_t outer, int64_t N, int64_t inner,
+                  int set_dofs, int data_kind, cudaStream_t stream);
 
 /* ---- Chebyshev Poisson solvers along one axis ------------------------------
  * la.pyx:614 Poisson_Solve_ADD(A, b, u, axis) / chebyshev/la.py:11 ADDSolver:

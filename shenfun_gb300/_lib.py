@@ -15,6 +15,7 @@ OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_NONFINITE, ERR_ZERO_PIVOT
     ERR_SCRATCH_LIMIT = range(9)
 REAL, COMPLEX = 0, 1
 BASIS_ORTHO, BASIS_SD, BASIS_SB, BASIS_SN = 0, 1, 2, 3
+BASIS_BC = 0x10  # flag: non-homogeneous boundary values
 XF_R2C, XF_C2R, XF_C2C_FWD, XF_C2C_BWD, XF_DCT2, XF_DCT3, XF_CHEB_SCALAR, XF_CHEB_FORWARD, \
     XF_CHEB_BACKWARD = range(1, 10)
 PLAIN_F64, MIXED_DF = 0, 1
@@ -55,6 +56,7 @@ SIGNATURES = {
     "sgpu_Solve_Helmholtz": (_int, [_vp, _vp, _int, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
     "sgpu_Helmholtz_matvec": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
     "sgpu_Helmholtz_Neumann_matvec": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_bc_apply": (_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp]),
     "sgpu_Poisson_Solve_ADD": (_int, [_vp, _vp, _dbl, _i64, _i64, _i64, _int, _vp]),
     "sgpu_Poisson_Solve_ANN": (_int, [_vp, _vp, _dbl, _dbl, _i64, _i64, _i64, _int, _vp]),
     "sgpu_helmholtz_factor": (_int, [_i64, _vp, _vp, _int, _i64, _i64, _int, _vp, _vp]),

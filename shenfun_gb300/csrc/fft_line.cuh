@@ -50,6 +50,8 @@ struct LinePlan {
   const Cx<df>* post_f;
   const df* sten_f;
   int form;          // SGPU_PLAIN_F64 or SGPU_MIXED_DF
+  int bcfun;         // Chebyshev backward: add the boundary functions of the
+                     // two boundary dofs (non-homogeneous SD / SN)
 };
 
 // typed table access: FP64 tables for R = double, df tables for R = df

@@ -413,6 +413,18 @@ SGPU_HD void prog_dct3(const LinePlan& p, const double* in, double* out, int in_
         if (p.basis == SGPU_BASIS_SB && k - 4 >= 0 && k - 4 < dim)
           acc = acc + scale(u[k - 4], stencil_coef<R>(p, 4, k - 4));
       }
+      if (p.bcfun) {
+        // boundary functions of the dofs u_dim, u_dim+1 (BoundaryValues.
+        // _add_to_orthogonal, tensorproductspace.py:2072-2089): SD
+        // (T0 -+ T1)/2, SN T1/2 -+ T2/8 (the reference's bc stencils)
+        const Cx<R> g0 = u[dim], g1 = u[dim + 1];
+        const int kb = p.basis == SGPU_BASIS_SD ? 0 : 1;
+        if (k == kb) acc = acc + (scale(g0, R(0.5)) + scale(g1, R(0.5)));
+        if (k == kb + 1) {
+          const R w = p.basis == SGPU_BASIS_SD ? R(0.5) : R(0.125);
+          acc = acc + (scale(g1, w) - scale(g0, w));
+        }
+      }
       s.B[(size_t)c * p.ld + k] = acc;
     }
     SGPU_SYNC();

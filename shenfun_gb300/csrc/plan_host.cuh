@@ -107,12 +107,16 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   if (form != SGPU_PLAIN_F64 && form != SGPU_MIXED_DF) return SGPU_ERR_UNSUPPORTED;
   const bool cheb = kind >= SGPU_XF_DCT2;
   const bool composite = kind >= SGPU_XF_CHEB_SCALAR;
+  const int bcflag = basis & SGPU_BASIS_BC;
+  basis &= ~SGPU_BASIS_BC;
   if (composite && (basis < SGPU_BASIS_ORTHO || basis > SGPU_BASIS_SN)) return SGPU_ERR_ARG;
+  if (bcflag && !(composite && (basis == SGPU_BASIS_SD || basis == SGPU_BASIS_SN))) return SGPU_ERR_ARG;
   if (composite && n < 2 + 2 * basis_nbcs(basis)) return SGPU_ERR_ARG;
   std::memset(&p, 0, sizeof(p));
   p.form = form;
   p.kind = kind;
   p.basis = composite ? basis : SGPU_BASIS_ORTHO;
+  p.bcfun = (bcflag && kind == SGPU_XF_CHEB_BACKWARD) ? 1 : 0;
   p.n = n;
   p.n_in = (kind == SGPU_XF_C2R) ? n / 2 + 1 : n;
   p.n_out = (kind == SGPU_XF_R2C) ? n / 2 + 1 : n;

@@ -372,6 +372,42 @@ SGPU_HD void helmholtz_matvec_prog(const T* v_all, T* b_all, const double* alfa,
   b[M + 1] = zero_of(T());
 }
 
+// ---- non-homogeneous boundary values (sgpu_bc_apply) -----------------------
+// Line s of u: u[k] -= (alfa_s CA[k][0] + beta_s CB[k][0]) g0 + (...[1]) g1
+// for the dofs k < N-2 (tables row-major (N-2) x 2, NULL = absent, NULL
+// scales = 1), then optionally the boundary dofs u[N-2], u[N-1] = g0, g1.
+// g holds the two values of every line as g[o][0|1][i].
+SGPU_HD bool is_zero(double a) { return a == 0.0; }
+SGPU_HD bool is_zero(cd a) { return a.re == 0.0 && a.im == 0.0; }
+
+template <class T>
+SGPU_HD void bc_apply_prog(T* u, const double* CA, const double* alfa, const double* CB,
+                           const double* beta, const T* g, int64_t N, int64_t inner, int64_t s,
+                           int set_dofs) {
+  const int64_t o = s / inner, i = s - o * inner;
+  const T g0 = g[(o * 2) * inner + i], g1 = g[(o * 2 + 1) * inner + i];
+  Line<T> line{u + sys_base(s, N, inner), inner};
+  const int64_t dim = N - 2;
+  if (set_dofs) {
+    line[dim] = g0;
+    line[dim + 1] = g1;
+  }
+  if (!(CA || CB) || (is_zero(g0) && is_zero(g1))) return;
+  const double a = alfa ? alfa[s] : 1.0, b = beta ? beta[s] : 1.0;
+  for (int64_t k = 0; k < dim; ++k) {
+    double c0 = 0.0, c1 = 0.0;
+    if (CA) {
+      c0 = a * CA[2 * k];
+      c1 = a * CA[2 * k + 1];
+    }
+    if (CB) {
+      c0 += b * CB[2 * k];
+      c1 += b * CB[2 * k + 1];
+    }
+    if (c0 != 0.0 || c1 != 0.0) line[k] = line[k] - (mulr(g0, c0) + mulr(g1, c1));
+  }
+}
+
 // ---- banded + rank-2 upper semiseparable systems ---------------------------
 // One system per Fourier wavenumber: M = sum_t c_t M_t over up to 3 terms,
 // where every M_t has even offsets in {-4, -2, 0, 2, 4} and at most one term

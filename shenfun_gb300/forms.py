@@ -98,6 +98,17 @@ class Function(_ShenfunArray):
             a.forward(obj)
         return obj
 
+    def set_boundary_dofs(self):
+        """Boundary dofs of a non-homogeneous Chebyshev axis set to their
+        final values (BoundaryValues.set_boundary_dofs(u, final=True),
+        tensorproductspace.py:2108-2128)."""
+        T = self._space
+        bases = T.bases if isinstance(T, TensorProductSpace) else (T,)
+        for ax, b in enumerate(bases):
+            if getattr(b, "has_nonhomogeneous_bcs", False):
+                b._apply_bcs(self.v, ax, lift=False)
+        return self
+
     def backward(self, output_array=None, kind=None, mesh=None):
         if output_array is None:
             output_array = Array(self._space)

@@ -158,6 +158,10 @@ class Helmholtz:
         self.form = _lib.FORMS[form] if form is not None else (
             self.T.form if self.T is not None else _lib.PLAIN_F64)
         nsys = outer * inner
+        # boundary matrices of a non-homogeneous trial space (extract_bc_matrices,
+        # chebyshev/la.py:222-231): subtracted from the right-hand side
+        base = self.T.bases[self.axis] if self.T is not None else None
+        self._bcbase = base if getattr(base, "has_nonhomogeneous_bcs", False) else None
         self._fac = torch.empty(4 * (self.N - 2) * nsys, dtype=torch.float64, device="cuda")
         _lib.call("sgpu_helmholtz_factor", self.N, ptr(self.alfa), ptr(self.beta), int(self.neumann),
                   outer, inner, self.form, ptr(self._fac), stream_handle())
@@ -170,8 +174,19 @@ class Helmholtz:
         outer, n, inner = view3(tuple(b.shape), self.axis)
         if n != self.N or (outer, inner) != (self._outer, self._inner):
             raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
+        bb = self._bcbase
+        if bb is not None:
+            # u.set_boundary_dofs(); b -= bc_mat.matvec(u) (chebyshev/la.py:302-306)
+            g = bb.bc_lines(tuple(b.shape), self.axis, [a for a in range(b.dim()) if a != self.axis],
+                            b.dtype)
+            _lib.call("sgpu_bc_apply", ptr(b), ptr(bb._bc_table("A")), ptr(self.alfa),
+                      ptr(bb._bc_table("B")), ptr(self.beta), ptr(g), outer, n, inner, 0,
+                      data_kind(b), stream_handle())
         _lib.call("sgpu_helmholtz_solve_cached", ptr(b), ptr(ur), ptr(self._fac), int(self.neumann),
                   outer, n, inner, data_kind(b), self.form, stream_handle())
+        if bb is not None:
+            _lib.call("sgpu_bc_apply", ptr(ur), None, None, None, None, ptr(g), outer, n, inner, 1,
+                      data_kind(ur), stream_handle())
         if constraints:
             idx = [0] * ur.dim()
             ur[tuple(idx)] = constraints[0][1]

@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import require_cuda, ptr, stream_handle, view3
+from .device import require_cuda, ptr, stream_handle, view3, data_kind
 from .plans import get_plan
 
 
@@ -231,12 +231,99 @@ class ChebyshevBase(SpectralBase):
     family_name = "chebyshev"
     basis_id = _lib.BASIS_ORTHO
     quad = "GC"
+    bc_values = None  # constant boundary values (left, right) of SD / SN
 
-    def __init__(self, N, quad="GC", domain=(-1.0, 1.0), dtype=float, **kw):
+    def __init__(self, N, quad="GC", domain=(-1.0, 1.0), dtype=float, bc=None, **kw):
         if quad != "GC":
             raise NotImplementedError("only Gauss-Chebyshev quadrature is on the GPU path")
         SpectralBase.__init__(self, N, dtype)
         self.domain = Domain(domain)
+        if bc is not None:
+            vals = tuple(float(v) for v in bc)
+            if any(vals):
+                if self.basis_id not in (_lib.BASIS_SD, _lib.BASIS_SN) or len(vals) != 2:
+                    raise NotImplementedError("non-homogeneous values on ShenDirichlet / ShenNeumann only")
+                self.bc_values = vals
+        self._bc_tables = {}
+
+    @property
+    def has_nonhomogeneous_bcs(self):
+        return self.bc_values is not None
+
+    def _plan_basis(self, kind):
+        if kind == _lib.XF_CHEB_BACKWARD and self.has_nonhomogeneous_bcs:
+            return self.basis_id | _lib.BASIS_BC
+        return self.basis_id
+
+    # -- non-homogeneous boundary values (tensorproductspace.py:1909-2128) ---
+    def bc_matrices(self):
+        """(A_bc, B_bc): (phi''_{N-2+i}, phi_k)_w and (phi_{N-2+i}, phi_k)_w
+        for the dofs k, (N-2) x 2, of the boundary basis SD (T0 -+ T1)/2,
+        SN T1/2 -+ T2/8 (BCGeneric, spectralbase.py:1702-1790)."""
+        N = self.N
+        h = np.full(N, np.pi / 2)
+        h[0] = np.pi
+        A = np.zeros((N - 2, 2))
+        B = np.zeros((N - 2, 2))
+        if self.basis_id == _lib.BASIS_SD:
+            B[0] = [h[0] / 2, h[0] / 2]
+            B[1] = [-h[1] / 2, h[1] / 2]
+        else:
+            B[1] = [h[1] / 2, h[1] / 2]
+            B[2] = [-h[2] / 8, h[2] / 8]
+            A[0] = [-h[0] / 2, h[0] / 2]
+        return A, B
+
+    def _bc_table(self, name):
+        t = self._bc_tables.get(name)
+        if t is None:
+            A, B = self.bc_matrices()
+            if name == "lift":
+                # B^{-1} B_bc: the forward transform's correction of the dofs
+                from .la import TDMA
+                from .matrices import galerkin_matrix
+                rhs = torch.as_tensor(B, device="cuda").contiguous()
+                t = TDMA(galerkin_matrix(self, 0))(rhs, axis=0)
+            else:
+                t = torch.as_tensor(A if name == "A" else B, device="cuda").contiguous()
+            self._bc_tables[name] = t
+        return t
+
+    def bc_lines(self, shape, axis, spectral_axes, dtype):
+        """Boundary values of every line of an array of `shape` (the axis
+        holds the two values): the constants, on the zero-mode lines of the
+        Fourier axes in spectral space (set_tensor_bcs,
+        tensorproductspace.py:1928-2036)."""
+        key = ("g", tuple(shape), axis, tuple(sorted(spectral_axes)), dtype)
+        g = self._bc_tables.get(key)
+        if g is None:
+            gs = list(shape)
+            gs[axis] = 2
+            g = torch.zeros(gs, dtype=dtype, device="cuda")
+            idx = [slice(None)] * len(gs)
+            for a in spectral_axes:
+                idx[a] = slice(0, 1)
+            for i in range(2):
+                idx[axis] = i
+                g[tuple(idx)] = self.bc_values[i]
+            self._bc_tables[key] = g
+        return g
+
+    def _spectral_axes_before(self):
+        T = self.tensorproductspace
+        if T is None:
+            return []
+        order = list(reversed(T.axes))
+        return order[:order.index(self.axis)]
+
+    def _apply_bcs(self, arr, axis, lift):
+        ax = (self.axis if axis is None else axis) % arr.dim()
+        g = self.bc_lines(tuple(arr.shape), ax, self._spectral_axes_before() if lift else
+                          [a for a in range(arr.dim()) if a != ax], arr.dtype)
+        outer, n, inner = view3(tuple(arr.shape), ax)
+        _lib.call("sgpu_bc_apply", ptr(arr), ptr(self._bc_table("lift")) if lift else None, None, None,
+                  None, ptr(g), outer, n, inner, 1, data_kind(arr), stream_handle())
+        return arr
 
     def domain_factor(self):
         a, b = self.domain
@@ -263,13 +350,18 @@ class ChebyshevBase(SpectralBase):
             raise NotImplementedError("only the reference domain [-1, 1] is on the GPU path")
         ax = self.axis if axis is None else axis
         out = self._out(input_array, True, output_array, ax)
-        return get_plan(kind, self.N, self.basis_id, self.form)(input_array, out, ax)
+        return get_plan(kind, self.N, self._plan_basis(kind), self.form)(input_array, out, ax)
 
     def scalar_product(self, input_array, output_array=None, axis=None):
         return self._run(_lib.XF_CHEB_SCALAR, input_array, output_array, axis)
 
     def forward(self, input_array, output_array=None, axis=None):
-        return self._run(_lib.XF_CHEB_FORWARD, input_array, output_array, axis)
+        out = self._run(_lib.XF_CHEB_FORWARD, input_array, output_array, axis)
+        if self.has_nonhomogeneous_bcs:
+            # _add_mass_rhs + mass solve (spectralbase.py:255-259) by linearity:
+            # dofs -= B^{-1} B_bc g, boundary dofs = g
+            self._apply_bcs(out, axis, lift=True)
+        return out
 
     def backward(self, input_array, output_array=None, axis=None):
         return self._run(_lib.XF_CHEB_BACKWARD, input_array, output_array, axis)
@@ -371,23 +463,25 @@ def FunctionSpace(N, family="Fourier", bc=None, dtype="d", quad=None, domain=Non
         return R2C(N, domain=dom, padding_factor=pf)
     kinds, vals = _bc_kinds(bc)
     nb = len(vals)
-    if any(v != 0 for v in vals):
-        raise NotImplementedError("only homogeneous boundary conditions are on the GPU path")
+    if any(v != 0 for v in vals) and kinds not in ("LDRD", "LNRN"):
+        raise NotImplementedError("non-homogeneous values on ShenDirichlet / ShenNeumann only")
     dom = domain if domain is not None else (-1.0, 1.0)
     basis = kw.get("basis")
     if fam in ("c", "chebyshev"):
         q = quad or "GC"
         if basis == "ShenNeumann" or kinds == "LNRN":
-            return ChebyshevShenNeumann(N, quad=q, domain=dom)
+            return ChebyshevShenNeumann(N, quad=q, domain=dom, bc=vals or None)
         if basis not in (None, "ShenDirichlet", "ShenBiharmonic", "Orthogonal") or kinds not in ("", "LDRD", "LDLNRDRN"):
             raise NotImplementedError(f"Chebyshev basis {basis or kinds!r}")
         if nb == 0:
             return ChebyshevOrthogonal(N, quad=q, domain=dom)
         if nb == 2:
-            return ChebyshevShenDirichlet(N, quad=q, domain=dom)
+            return ChebyshevShenDirichlet(N, quad=q, domain=dom, bc=vals)
         if nb == 4:
             return ChebyshevShenBiharmonic(N, quad=q, domain=dom)
     if fam in ("l", "legendre"):
+        if any(v != 0 for v in vals):
+            raise NotImplementedError("non-homogeneous values on a Legendre space")
         from . import legendre
         return legendre.space(N, nb, quad=quad or "LG", domain=dom)
     raise NotImplementedError(f"family {family!r} with {nb} boundary conditions")

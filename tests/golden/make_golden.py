@@ -425,9 +425,68 @@ def neumann():
     put("neumann", **d)
 
 
+# --------------------------------------------------------------------------
+# Non-homogeneous boundary values on a Chebyshev axis (constants): the
+# boundary basis (utilities get_bc_basis via BCGeneric, spectralbase.py:
+# 1702-1790), BoundaryValues (tensorproductspace.py:1909-2106: set_tensor_bcs,
+# _add_to_orthogonal, _add_mass_rhs, set_boundary_dofs) and the Helmholtz
+# solve with boundary matrices (chebyshev/la.py:222-317).  Own rng.
+def nonhomog():
+    g = np.random.default_rng(67)
+    d = {}
+    cases = {"SD": (1.5, -0.5), "SN": {"left": {"N": 0.7}, "right": {"N": -0.3}}}
+    for tag, bc in cases.items():
+        for N in (12, 17):
+            V = FunctionSpace(N, "C", bc=bc)
+            assert V.short_name() == tag and V.has_nonhomogeneous_bcs
+            f = g.standard_normal(N)
+            d[f"{tag}{N}_f"] = f
+            d[f"{tag}{N}_sp"] = V.scalar_product(f.copy(), np.zeros(N)).copy()
+            d[f"{tag}{N}_fw"] = V.forward(f.copy(), np.zeros(N)).copy()
+            uh = Function(V)
+            uh[:N - 2] = g.standard_normal(N - 2)
+            uh.set_boundary_dofs()
+            d[f"{tag}{N}_uh"] = np.array(uh)
+            d[f"{tag}{N}_bw"] = V.backward(np.array(uh), np.zeros(N)).copy()
+    # channel grids: Fourier x Fourier x Chebyshev with constant wall values,
+    # and a 2D grid with the Chebyshev axis first
+    for tag, bc in cases.items():
+        for shape, order in (((8, 6, 17), "last"), ((16, 6), "first")):
+            if order == "last":
+                Nx, Ny, Nz = shape
+                bases = (FunctionSpace(Nx, "F", dtype="D"), FunctionSpace(Ny, "F", dtype="d"),
+                         FunctionSpace(Nz, "C", bc=bc))
+            else:
+                Nz, Ny = shape
+                bases = (FunctionSpace(Nz, "C", bc=bc), FunctionSpace(Ny, "F", dtype="d"))
+            T = TensorProductSpace(comm, bases)
+            key = f"{tag}_" + "x".join(str(n) for n in shape)
+            fa = Array(T)
+            fa[:] = g.standard_normal(fa.shape)
+            d[key + "_f"] = np.array(fa)
+            d[key + "_fw"] = np.array(fa.forward(Function(T)))
+            d[key + "_sp"] = np.array(inner(TestFunction(T), fa))
+            uh = Function(T)
+            uh[:] = g.standard_normal(uh.shape) + 1j * g.standard_normal(uh.shape)
+            uh.set_boundary_dofs()
+            d[key + "_uh"] = np.array(uh)
+            d[key + "_bw"] = np.array(uh.backward(Array(T)))
+            u, v = TrialFunction(T), TestFunction(T)
+            c = 5.0
+            mats = inner(v, -div(grad(u)) + c * u)
+            H = chebyshev.la.Helmholtz(*mats)
+            fh = inner(v, fa)
+            x = H(fh.copy(), Function(T))
+            d[key + "_rhs"] = np.array(fh)
+            d[key + "_sol"] = np.array(x)
+            d[key + "_solx"] = np.array(x.backward(Array(T)))
+    put("nonhomog", **d)
+
+
 GROUPS = {"cheb_1d": cheb_1d, "fourier_1d": fourier_1d, "banded": banded, "helmholtz": helmholtz,
           "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex,
-          "dealias": dealias, "neumann": neumann}
+          "dealias": dealias, "neumann": neumann,
+          "nonhomog": nonhomog}
 
 if __name__ == "__main__":
     # no arguments: every group (the shared rng makes the earlier groups depend

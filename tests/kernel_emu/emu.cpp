@@ -380,6 +380,30 @@ int main(int argc, char** argv) {
     write_exact(argv[9], out, cnt);
     return 0;
   }
+  if (mode == "bcapply") {
+    // bcapply N outer inner data_kind set_dofs tables u.bin CA.bin alfa.bin CB.bin beta.bin g.bin out.bin
+    // tables: bit 0 CA+alfa present, bit 1 CB+beta present
+    long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]), set = atoi(argv[6]), tab = atoi(argv[7]);
+    long long ns = outer * inner;
+    size_t w = dk ? 2 : 1, cnt = (size_t)outer * N * inner * w;
+    double* u = read_exact(argv[8], cnt);
+    double* CA = read_exact(argv[9], 2 * (size_t)(N - 2));
+    double* al = read_exact(argv[10], ns);
+    double* CB = read_exact(argv[11], 2 * (size_t)(N - 2));
+    double* be = read_exact(argv[12], ns);
+    double* g = read_exact(argv[13], (size_t)outer * 2 * inner * w);
+    const double* ca = (tab & 1) ? CA : nullptr;
+    const double* cb = (tab & 2) ? CB : nullptr;
+    for (long long s = 0; s < ns; ++s) {
+      if (dk) bc_apply_prog<cd>((cd*)u, ca, (tab & 1) ? al : nullptr, cb, (tab & 2) ? be : nullptr,
+                                (const cd*)g, N, inner, s, set);
+      else bc_apply_prog<double>(u, ca, (tab & 1) ? al : nullptr, cb, (tab & 2) ? be : nullptr, g, N,
+                                 inner, s, set);
+    }
+    write_exact(argv[14], u, cnt);
+    return 0;
+  }
   if (mode == "padd" || mode == "pann") {
     long long N = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
     int dk = atoi(argv[5]);

@@ -383,3 +383,58 @@ def test_poisson(emu, N, outer, inner, cplx, which):
         A = la.cheb_sn_stiffness(N)
         ref = la.ann_solve(b, A[0], A[2], scale, axis=1)
     assert rel(u, ref) < 1e-13
+
+
+# --------------------------------------------------------------------------
+# non-homogeneous boundary values: the backward flag (boundary functions in
+# to_ortho) and the dof correction / boundary dofs program
+@pytest.mark.parametrize("basis", ["SD", "SN"])
+@pytest.mark.parametrize("n", [12, 17, 64, 257])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_backward_boundary_functions(emu, basis, n, cplx):
+    from oracle import bcs as BC
+    x = rng.standard_normal((3, n, 4))
+    if cplx:
+        x = x + 1j * rng.standard_normal(x.shape)
+    flagged = BASIS[basis] | 0x10
+    got = xform(emu, CHEB_BACKWARD, n, flagged, x, 1, cplx)
+    assert rel(got, BC.backward_1d(x, basis, axis=1)) < 1e-13
+    got_df = xform_df(emu, CHEB_BACKWARD, n, flagged, x, 1, cplx)
+    assert rel(got_df, BC.backward_1d(x, basis, axis=1)) < DF_TOL
+    # scalar product / forward plans ignore the flag
+    f = rng.standard_normal((3, n, 4))
+    assert rel(xform(emu, CHEB_FORWARD, n, flagged, f, 1, False), S.cheb_forward(f, basis, 1)) < 1e-12
+
+
+@pytest.mark.parametrize("N,outer,inner", [(12, 1, 1), (17, 3, 4), (33, 2, 1)])
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("tables,set_dofs", [(0, 1), (1, 0), (2, 1), (3, 1)])
+def test_bc_apply(emu, N, outer, inner, cplx, tables, set_dofs):
+    u = rng.standard_normal((outer, N, inner))
+    g = rng.standard_normal((outer, 2, inner))
+    g[:, :, 0] = 0.0  # lines with zero boundary values are left alone
+    if cplx:
+        u = u + 1j * rng.standard_normal(u.shape)
+        g = g + 1j * rng.standard_normal(g.shape)
+        g[:, :, 0] = 0.0
+    CA = rng.standard_normal((N - 2, 2))
+    CB = rng.standard_normal((N - 2, 2))
+    al = rng.standard_normal(outer * inner)
+    be = rng.standard_normal(outer * inner)
+    cnt = u.size * (2 if cplx else 1)
+    got = run(emu, ["bcapply", N, outer, inner, int(cplx), set_dofs, tables], [u, CA, al, CB, be, g], cnt)
+    got = (got.view(np.complex128) if cplx else got).reshape(u.shape)
+    ref = u.copy()
+    for o in range(outer):
+        for i in range(inner):
+            s = o * inner + i
+            C = np.zeros((N - 2, 2))
+            if tables & 1:
+                C += al[s] * CA
+            if tables & 2:
+                C += be[s] * CB
+            if np.any(g[o, :, i] != 0):
+                ref[o, :N - 2, i] -= C @ g[o, :, i]
+            if set_dofs:
+                ref[o, N - 2:, i] = g[o, :, i]
+    assert rel(got, ref) < 1e-14

@@ -227,3 +227,41 @@ def test_poisson_add_2d(golden, axis):
     sl = [slice(None)] * 2
     sl[axis] = slice(0, 18)  # the compiled kernel writes the dofs only
     assert rel(u[tuple(sl)], ref[tuple(sl)]) < TOL
+
+
+# --------------------------------------------------------------------------
+# non-homogeneous boundary values (nonhomog.npz)
+BCV = {"SD": (1.5, -0.5), "SN": (0.7, -0.3)}
+
+
+def _nh_bases(tag, shape):
+    if len(shape) == 3:
+        return [("fourier", "C2C", shape[0]), ("fourier", "R2C", shape[1]), ("chebyshev", tag, shape[2])], 2
+    return [("chebyshev", tag, shape[0]), ("fourier", "R2C", shape[1])], 0
+
+
+@pytest.mark.parametrize("tag", ["SD", "SN"])
+@pytest.mark.parametrize("N", [12, 17])
+def test_nonhomog_1d(golden, tag, N):
+    from oracle import bcs as BC
+    d = golden("nonhomog")
+    f = d[f"{tag}{N}_f"]
+    assert rel(S.cheb_scalar_product(f, tag), d[f"{tag}{N}_sp"]) < TOL
+    assert rel(BC.forward_1d(f, tag, np.array(BCV[tag])), d[f"{tag}{N}_fw"]) < TOL
+    assert rel(BC.backward_1d(d[f"{tag}{N}_uh"], tag), d[f"{tag}{N}_bw"]) < TOL
+
+
+@pytest.mark.parametrize("tag", ["SD", "SN"])
+@pytest.mark.parametrize("shape", [(8, 6, 17), (16, 6)])
+def test_nonhomog_tensor(golden, tag, shape):
+    from oracle import bcs as BC
+    d = golden("nonhomog")
+    key = tag + "_" + "x".join(str(n) for n in shape)
+    bases, ax = _nh_bases(tag, shape)
+    f = d[key + "_f"]
+    assert rel(BC.tp_forward(f, bases, BCV[tag], ax), d[key + "_fw"]) < TOL
+    assert rel(P.scalar_product(f, bases), d[key + "_sp"]) < TOL
+    assert rel(BC.tp_backward(d[key + "_uh"], bases, ax), d[key + "_bw"]) < TOL
+    sol = BC.helmholtz_bc_solve(d[key + "_rhs"], bases, 5.0, ax, BCV[tag])
+    assert rel(sol, d[key + "_sol"]) < TOL
+    assert rel(BC.tp_backward(sol, bases, ax), d[key + "_solx"]) < TOL
