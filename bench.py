@@ -363,6 +363,91 @@ def biharmonic_leg(torch, flush, st, steps=10):
     return out
 
 
+def neumann_leg(torch, flush, st, steps=10):
+    """The Chebyshev boundary-condition row on the channel grid's sizes:
+    Fourier 256 (C2C) x Fourier 256 (R2C) x Chebyshev ShenNeumann 257 with
+    alpha = k^2 + 1000 (the headline's shift; the Neumann branch of the
+    Helmholtz kernels) in both forms, and ShenDirichlet with wall values
+    u(-1) = 1, u(1) = -1 in the mixed form (the boundary-function backward
+    and the Helmholtz boundary matrices): scalar product -> solve -> backward
+    of a random RHS (seed 0), L2 flushed before every step."""
+    import shenfun_gb300 as sg
+    f = np.random.default_rng(0).standard_normal((NX, NY, NZ))
+    out = {"workload": f"Fourier {NX} (C2C) x Fourier {NY} (R2C) x Chebyshev {NZ}, alpha = k^2 + 1000, "
+                       "RHS N(0,1) seed 0", "solve_factors": "FP64 (both forms, as the headline)"}
+    cases = (("neumann_plain", {"left": {"N": 0}, "right": {"N": 0}}, "plain"),
+             ("neumann_mixed", {"left": {"N": 0}, "right": {"N": 0}}, "mixed"),
+             ("dirichlet_walls_mixed", (1.0, -1.0), "mixed"))
+    ref = None
+    for name, bc, form in cases:
+        T = sg.TensorProductSpace(None, (sg.FunctionSpace(NX, "F", dtype="D"), sg.FunctionSpace(NY, "F", dtype="d"),
+                                         sg.FunctionSpace(NZ, "C", bc=bc)), form=form)
+        u, v = sg.TrialFunction(T), sg.TestFunction(T)
+        H = sg.chebyshev.la.Helmholtz(*sg.inner(v, -sg.div(sg.grad(u)) + C_SHIFT * u), form="plain")
+        fj = sg.Array(T, buffer=f)
+        f_hat, u_hat, uq = sg.Function(T), sg.Function(T), sg.Array(T)
+
+        def step():
+            sg.inner(v, fj, output_array=f_hat)
+            H(f_hat, u_hat)
+            T.backward(u_hat.v, uq.v)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        ms = float(np.mean(time_steps_gpu(torch, step, steps, flush, st)))
+        res = {"ms_per_step": ms, "solves_per_s": 1e3 / ms}
+        if name == "neumann_plain":
+            ref = uq.v.clone()
+        elif name == "neumann_mixed":
+            res["rel_err_vs_plain"] = float(((uq.v - ref).abs().max() / ref.abs().max()).item())
+        out[name] = res
+        del T, H, fj, f_hat, u_hat, uq
+    return out
+
+
+def dealias_leg(torch, flush, st, steps=10):
+    """The 3/2-rule dealiased nonlinear term on the channel grid: padded
+    backward (Fourier axes 256 -> 384, sgpu_fourier_pad + length-384
+    transforms), pointwise square, padded forward (length-384 transforms +
+    sgpu_fourier_truncate), Chebyshev ShenDirichlet 257 unpadded, both forms,
+    L2 flushed before every step."""
+    import shenfun_gb300 as sg
+    out = {"workload": f"u_hat -> u^2 (3/2 rule) on Fourier {NX} x Fourier {NY} x Chebyshev {NZ}, "
+                       "padded grid 384 x 384 x 257"}
+    rng = np.random.default_rng(0)
+    shape = (NX, NY // 2 + 1, NZ)
+    u0 = torch.as_tensor(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    u0[:, :, NZ - 2:] = 0
+    ref = None
+    for form in ("plain", "mixed"):
+        T = sg.TensorProductSpace(None, (sg.FunctionSpace(NX, "F", dtype="D"), sg.FunctionSpace(NY, "F", dtype="d"),
+                                         sg.FunctionSpace(NZ, "C", bc=(0, 0))), form=form)
+        TP = T.get_dealiased((1.5, 1.5, 1))
+        uh = sg.Function(T)
+        uh.v.copy_(u0)
+        up = sg.Array(TP)
+        wh = sg.Function(T)
+
+        def step():
+            TP.backward(uh.v, up.v)
+            up.v.mul_(up.v)
+            TP.forward(up.v, wh.v)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        ms = float(np.mean(time_steps_gpu(torch, step, steps, flush, st)))
+        res = {"ms_per_step": ms}
+        if ref is None:
+            ref = wh.v.clone()
+        else:
+            res["rel_err_vs_plain"] = float(((wh.v - ref).abs().max() / ref.abs().max()).item())
+        out[form] = res
+        del T, TP, uh, up, wh
+    return out
+
+
 def latency_leg(torch, reps=200):
     """Small 2D Poisson on Fourier 64 x Chebyshev ShenDirichlet 64 (33
     systems): per-solve latency of the round trip, eager and as one CUDA-graph
@@ -607,13 +692,15 @@ def main():
     b.synchronize()
     e2e_val = ws * e2e_steps / (a.elapsed_time(b) / 1e3)
 
-    serving = legendre = imex = biharmonic = latency = None
+    serving = legendre = imex = biharmonic = latency = neumann = dealias = None
     if rank == 0 and not args.no_extra:
         serving = serving_leg(torch)
         legendre = legendre_leg(torch, flush, st)
         imex = imex_leg(torch)
         biharmonic = biharmonic_leg(torch, flush, st)
         latency = latency_leg(torch)
+        neumann = neumann_leg(torch, flush, st)
+        dealias = dealias_leg(torch, flush, st)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -649,6 +736,8 @@ def main():
             "imex": imex,
             "biharmonic": biharmonic,
             "small_2d_latency": latency,
+            "boundary_conditions": neumann,
+            "dealias": dealias,
         }
         print(json.dumps(out))
     if dist is not None:
