@@ -696,6 +696,8 @@ def main():
     if rank == 0 and not args.no_extra:
         serving = serving_leg(torch)
         legendre = legendre_leg(torch, flush, st)
+        # beyond one exact K chunk (1024): two chunk launches per contraction
+        legendre["N2048"] = legendre_leg(torch, flush, st, N=2048, lines=4096, reps=3)
         imex = imex_leg(torch)
         biharmonic = biharmonic_leg(torch, flush, st)
         latency = latency_leg(torch)

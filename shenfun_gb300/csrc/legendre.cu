@@ -14,7 +14,12 @@
 // The matrices are built on the host in long double and stored in FP64.
 // Plain form: FP64 tiled GEMM (k_line_gemm_f64).  Mixed form: the same
 // matrices split into BF16 digit slices and contracted on the tensor cores
-// (ozaki_tc.cu), about 48 bits, for N <= 1024.
+// (ozaki_tc.cu), about 48 bits, for N <= 8192 (above 1024 as one exact
+// contraction per K chunk of 1024, the chunks' results added in FP64).  The
+// reference's fast transform for large N (Hale & Townsend's DLT, legendre/
+// dlt.py:20-206: leg2cheb plus ~20 Taylor-term DCT/DSTs in FP64) does not
+// pay on this part at these lengths: FP64 runs at ~1 TFLOP/s against
+// ~0.6 PFLOP/s for the split-BF16 contraction.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

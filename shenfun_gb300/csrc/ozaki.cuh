@@ -16,7 +16,8 @@
 // G0 (s+t=0), G1, G2, G3 and G4 (s+t>=4).  Group g holds multiples of
 // 2^{-W g} of magnitude at most (g+1) 2^{2W-2} K units, below 2^24 for
 // g <= 3 when K <= 2^{26-2W}/4 (W=7: K <= 1024), so those FP32 sums are
-// exact; G4 carries terms below 2^{-4W} relative, where FP32 rounding is
+// exact (longer contractions run in chunks of 1024 whose FP64 results are
+// added); G4 carries terms below 2^{-4W} relative, where FP32 rounding is
 // harmless (a fourth exact group lowers the error ~50x against folding
 // s+t=3 into the rounded one).  The
 // epilogue adds the four in 64-bit fixed point with integer instructions and
@@ -248,7 +249,17 @@ struct Geom {
   int nkb;         // K blocks of BK (K padded with zeros)
   int mtiles;      // row tiles of BM
   int ntiles;      // output-column tiles of BN
+  // one GEMM launch sums the K blocks [kb0, kb1): at most KCHUNK_MAX blocks,
+  // so that its FP32 group sums stay exact; a launch with accum adds its
+  // FP64 result to the output of the previous chunks
+  int kb0, kb1, accum;
+  int kchunk;      // K blocks per launch (KCHUNK_MAX; smaller in tests)
 };
+
+// K blocks per GEMM launch: 1024 / BK (the exactness bound K <= 1024 above)
+constexpr int KCHUNK_MAX = 1024 / 32;
+// largest contraction length: K chunks of 1024, each exact, added in FP64
+constexpr int OZ_MAX_K = 8192;
 
 SGPU_HD int64_t row_offset(const Geom& g, int64_t row, int64_t j) {
   const int64_t l = g.cplx ? (row >> 1) : row;
@@ -273,8 +284,22 @@ inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx, int BN, in
   g.nkb = (N + BK - 1) / BK;
   g.mtiles = (int)((g.nrows + BM - 1) / BM);
   g.ntiles = (N + BN - 1) / BN;
+  g.kb0 = 0;
+  g.kb1 = g.nkb;
+  g.accum = 0;
+  g.kchunk = KCHUNK_MAX;
   return g;
 }
+
+// the launch of chunk c: K blocks [c kchunk, min(nkb, (c+1) kchunk))
+inline Geom chunk_geom(const Geom& g, int c) {
+  Geom h = g;
+  h.kb0 = c * g.kchunk;
+  h.kb1 = h.kb0 + g.kchunk < g.nkb ? h.kb0 + g.kchunk : g.nkb;
+  h.accum = c > 0;
+  return h;
+}
+inline int num_chunks(const Geom& g) { return (g.nkb + g.kchunk - 1) / g.kchunk; }
 
 // largest exponent field of row `row` over the lanes' strided share
 // (lane, lane + nlane, ...) of the K entries the matrix uses (entries it

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   auto sB = [&](int st, int s) {
     return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)S * AH + (size_t)s * BH;
   };
-  const int nsteps = 2 * g.nkb;  // K steps of 16 per tile
+  const int nsteps = 2 * (g.kb1 - g.kb0);  // K steps of 16 per tile (this launch's chunk)
 
   if (warp == 0 && lane == 0) {
     // producer
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           ok = false;
           break;
         }
-        const int kb = ks >> 1, hf = ks & 1;
+        const int kb = g.kb0 + (ks >> 1), hf = ks & 1;
         tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(S * (AH + BH)));
         for (int s = 0; s < S; ++s) {
           tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2),
@@ -216,7 +216,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
               uint32_t gb[NACC];
 #pragma unroll
               for (int qq = 0; qq < NACC; ++qq) gb[qq] = a[qq][j];
-              out[obase + (int64_t)col * ostride] = combine_groups<NACC>(gb, erow + eB[col]);
+              const double v = combine_groups<NACC>(gb, erow + eB[col]);
+              double* o = out + obase + (int64_t)col * ostride;
+              *o = g.accum ? *o + v : v;
             }
           }
         }
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 namespace sgpu {
 namespace oz {
 
-int pick_digits(int K) { return K >= 1 && K <= 1024 ? SGPU_OK : SGPU_ERR_UNSUPPORTED; }
+int pick_digits(int K) { return K >= 1 && K <= OZ_MAX_K ? SGPU_OK : SGPU_ERR_UNSUPPORTED; }
 
 template <class C>
 static int matrix_create_cfg(const double* M, int N, Matrix* out) {
@@ -326,7 +328,11 @@ static int run(const Matrix& m, const Geom& g, const double* in, double* out, vo
   }
   const int64_t ntile = (int64_t)g.mtiles * g.ntiles;
   const unsigned nctas = (unsigned)(ntile < nsm ? ntile : nsm);
-  k_oz_gemm<C><<<nctas, GEMM_THREADS, GemmSmem<C>::bytes, stream>>>(At, eA, m.tiles, m.exps, out, g);
+  // one launch per K chunk of at most 1024 (stream-ordered: a chunk adds to
+  // the previous chunks' output)
+  for (int c = 0; c < num_chunks(g); ++c)
+    k_oz_gemm<C><<<nctas, GEMM_THREADS, GemmSmem<C>::bytes, stream>>>(At, eA, m.tiles, m.exps, out,
+                                                                      chunk_geom(g, c));
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 

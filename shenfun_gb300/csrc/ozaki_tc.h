@@ -19,8 +19,9 @@ struct Matrix {
   int* exps = nullptr;
 };
 
-// OK when the contraction length K keeps the FP32 sums of the exact digit
-// groups below 2^24 (K <= 1024), else UNSUPPORTED
+// OK for contraction lengths 1 <= K <= 8192: each GEMM launch sums at most
+// 1024 of them (the FP32 sums of the exact digit groups stay below 2^24)
+// and longer contractions add the launches' FP64 results; else UNSUPPORTED
 int pick_digits(int K);
 int matrix_create(const double* M_host, int N, int precise, Matrix* out);
 void matrix_destroy(Matrix* m);

@@ -29,7 +29,9 @@ struct sgpu_plan {
 namespace {
 
 bool tensor_kind(int kind, int n, int form) {
-  return form == SGPU_MIXED_DF && n >= 16 && oz::pick_digits(n) == SGPU_OK &&
+  // Chebyshev lengths above 1024 stay on the double-float FFT line kernels:
+  // the dense contraction's n^2 cost overtakes them there
+  return form == SGPU_MIXED_DF && n >= 16 && n <= 1024 &&
          (kind == SGPU_XF_CHEB_SCALAR || kind == SGPU_XF_CHEB_FORWARD || kind == SGPU_XF_CHEB_BACKWARD);
 }
 

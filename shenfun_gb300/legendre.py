@@ -4,7 +4,8 @@
 Transforms are dense contractions (``sgpu_legendre_execute_ws``) with the
 Shen stencil folded into the matrix; the nodes and weights come from the
 library's host routine ``sgpu_leggauss``.  ``form='mixed'`` runs them on the
-tensor cores with BF16 digit slices (about 48 bits, N <= 1024).  ``kind='vandermonde'`` zeroes the tail rows of
+tensor cores with BF16 digit slices (about 48 bits, N <= 8192; above 1024 in
+exact K chunks of 1024 whose results are added).  ``kind='vandermonde'`` zeroes the tail rows of
 the composite scalar product (spectralbase.py:1466-1469); the default
 ('recursive', the reference's default for Legendre) keeps the orthogonal
 coefficients there, as the reference's stencil product does.

@@ -15,6 +15,7 @@
 //   emu padd|pann N outer inner data_kind scale b.bin out.bin   (Poisson ADD / ANN)
 //   emu tdma|pdma n outer inner data_kind raw.bin u.bin out.bin (LU then solve)
 //   emu ozaki  N nlines inner cplx precise in.bin M.bin out.bin (split-BF16 contraction)
+//   emu ozakic N nlines inner cplx precise kchunk in.bin M.bin out.bin  (K blocks per launch)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -148,11 +149,13 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
     memcpy(&f, &u, 4);
     return f;
   };
+  for (int c = 0; c < num_chunks(g); ++c)
   for (int mt = 0; mt < g.mtiles; ++mt)
     for (int nt = 0; nt < g.ntiles; ++nt) {
+      const Geom h = chunk_geom(g, c);  // one GEMM launch per K chunk
       uint32_t inited = 0;
-      for (int ks = 0; ks < 2 * g.nkb; ++ks) {
-        const int st = ks % STAGES, kb = ks >> 1, hf = ks & 1;
+      for (int ks = 0; ks < 2 * (h.kb1 - h.kb0); ++ks) {
+        const int st = ks % STAGES, kb = h.kb0 + (ks >> 1), hf = ks & 1;
         uint8_t* sbase = smem + st * stage_bytes;
         for (int s = 0; s < S; ++s) {
           memcpy(sbase + (size_t)s * AH,
@@ -193,7 +196,9 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
           if (col >= g.N) continue;
           uint32_t gb[C::NACC];
           for (int a = 0; a < NACC; ++a) memcpy(&gb[a], &acc[((size_t)a * BM + m) * BN + n], 4);
-          out[row_offset(g, row, col)] = combine_groups<C::NACC>(gb, eA[row] - 2 * W + eB[col]);
+          const double v = combine_groups<C::NACC>(gb, eA[row] - 2 * W + eB[col]);
+          double& o = out[row_offset(g, row, col)];
+          o = h.accum ? o + v : v;
         }
       }
     }
@@ -206,18 +211,22 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
 
 // emu ozaki N nlines inner cplx precise in.bin M.bin out.bin
 static int ozaki(int argc, char** argv) {
-  if (argc < 10) return 2;
+  // "ozakic" takes the K blocks per GEMM launch before the files
+  const int chunked = std::string(argv[1]) == "ozakic";
+  if (argc < 10 + chunked) return 2;
   const int N = atoi(argv[2]);
   const long long nlines = atoll(argv[3]), inner = atoll(argv[4]);
   const int cplx = atoi(argv[5]), precise = atoi(argv[6]);
   const size_t cnt = (size_t)nlines * N * (1 + cplx);
+  argv += chunked;
   double* in = read_exact(argv[7], cnt);
   double* M = read_exact(argv[8], (size_t)N * N);
   int K = 0;  // as the library: 1 + the last nonzero row of M
   for (int k = 0; k < N; ++k)
     for (int n = 0; n < N; ++n)
       if (M[(size_t)k * N + n] != 0.0) K = k + 1;
-  const oz::Geom g = oz::make_geom(N, nlines, inner, cplx, precise ? oz::CfgPrec::BN : oz::CfgStd::BN, K);
+  oz::Geom g = oz::make_geom(N, nlines, inner, cplx, precise ? oz::CfgPrec::BN : oz::CfgStd::BN, K);
+  if (chunked) g.kchunk = atoi(argv[6]);  // argv shifted by one: the chunk argument
   double* out = (double*)malloc(sizeof(double) * cnt);
   for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
   const int rc = precise ? ozaki_run<oz::CfgPrec>(g, in, M, out) : ozaki_run<oz::CfgStd>(g, in, M, out);
@@ -238,7 +247,7 @@ int main(int argc, char** argv) {
     mode = "h" + mode.substr(1);
   }
   if (mode == "xform") return xform(argc, argv);
-  if (mode == "ozaki") return ozaki(argc, argv);
+  if (mode == "ozaki" || mode == "ozakic") return ozaki(argc, argv);
   if (mode == "lkcheck") {
     // lkcheck: every (line, index) pair of the loop decompositions is visited
     // exactly once for the thread counts the kernels launch with

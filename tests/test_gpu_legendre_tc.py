@@ -74,7 +74,7 @@ def test_axis_mixed(L, N, basis, cplx):
     assert timeouts() == 0
 
 
-@pytest.mark.parametrize("N,lines", [(512, 4096), (1024, 1000)])
+@pytest.mark.parametrize("N,lines", [(512, 4096), (1024, 1000), (1100, 700), (2048, 500)])
 def test_mixed_vs_plain_large(L, N, lines):
     """cfg-size lines with k^-2-decaying coefficients: backward then forward
     in both forms; the mixed form within 1e-10 of the FP64 one, and the round
@@ -95,9 +95,27 @@ def test_mixed_vs_plain_large(L, N, lines):
 
 
 def test_mixed_limits(L):
+    """Above 1024 the contraction runs in exact K chunks of 1024 (one GEMM
+    launch each); lengths beyond 8192 are rejected."""
     from shenfun_gb300 import _lib
     with pytest.raises(_lib.SgpuError):
-        L.get_plan(1100, _lib.BASIS_SD, _lib.MIXED_DF)
+        L.get_plan(8200, _lib.BASIS_SD, _lib.MIXED_DF)
+
+
+def test_mixed_chunked_golden_oracle(L):
+    """N = 1500 (two K chunks): the mixed backward / scalar product against
+    the oracle's FP64 Vandermonde evaluation."""
+    N = 1500
+    rng = np.random.default_rng(3)
+    c = rng.uniform(-1, 1, (64, N)) * (np.arange(N) + 1.0) ** -2
+    c[:, -2:] = 0
+    V = space(L, "SD", N)
+    u = V.backward(dev(c), axis=1)
+    ref = S.leg_backward(c, "SD", axis=1, kind="vandermonde")
+    assert rel(u, ref) < TOL
+    f = rng.standard_normal((64, N))
+    assert rel(V.scalar_product(dev(f), axis=1), S.leg_scalar_product(f, "SD", axis=1)) < TOL
+    assert timeouts() == 0
 
 
 @pytest.mark.parametrize("n", [16, 17, 64, 129, 257])

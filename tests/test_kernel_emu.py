@@ -438,3 +438,21 @@ def test_bc_apply(emu, N, outer, inner, cplx, tables, set_dofs):
             if set_dofs:
                 ref[o, N - 2:, i] = g[o, :, i]
     assert rel(got, ref) < 1e-14
+
+
+@pytest.mark.parametrize("N,nlines,kchunk,precise", [(150, 70, 2, 0), (200, 40, 3, 1), (97, 50, 1, 0)])
+def test_ozaki_k_chunks(emu, N, nlines, kchunk, precise):
+    """Contractions longer than one exact K chunk run as one GEMM launch per
+    chunk, each adding its FP64 result to the previous ones (the GPU's chunk
+    is 1024; small chunks here exercise the same launch sequence)."""
+    r = np.random.default_rng(N)
+    x = r.uniform(-1, 1, (nlines, N, 1)) / (np.arange(N)[None, :, None] + 1.0)
+    M = r.standard_normal((N, N))
+    res = run(emu, ["ozakic", N, nlines, 1, 0, precise, kchunk], [x, M], x.size).reshape(x.shape)
+    ref = np.einsum("ojl,jk->okl", x, M)
+    scale = np.einsum("ojl,jk->okl", np.abs(x), np.abs(M)).max()
+    # the chunks' FP64 sums add a few ulps of the partial results
+    tol = 2e-14 if precise else 5e-13
+    assert np.abs(res - ref).max() / scale < tol
+    one = run(emu, ["ozaki", N, nlines, 1, 0, precise], [x, M], x.size).reshape(x.shape)
+    assert np.abs(res - one).max() / scale < tol
