@@ -205,7 +205,7 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
   } else {
     // the mixed form contracts on the tensor cores where the plan supports N
     int lform = form;
-    if (lform == SGPU_MIXED_DF && oz::pick_digits((int)Nd) != SGPU_OK) lform = SGPU_PLAIN_F64;
+    if (lform == SGPU_MIXED_DF && sgpu::oz::pick_digits((int)Nd) != SGPU_OK) lform = SGPU_PLAIN_F64;
     st |= (ordered ? cached_leg_plan : sgpu_legendre_plan_create)(&p->leg, (int)Nd, SGPU_BASIS_SD, lform);
   }
   if (st != SGPU_OK) {
