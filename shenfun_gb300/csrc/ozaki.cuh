@@ -58,14 +58,24 @@ const int SBO = 128;                    // row-direction core-matrix stride (byt
 // Wider tiles read the A operand from shared memory less often per flop
 // (measured on the channel grid's z axis: BN = 96 with one set beat BN = 48
 // with two).
-template <int S_, int NACC_, int BN_>
+// ATMEM: the A slices of a K step are copied once into TMEM (tcgen05.cp,
+// two buffers of S x 8 columns after the accumulators) and every digit
+// product reads A from there; only B is read from shared memory per MMA.
+// Measured on the channel grid's z pass: correct, but no faster per MMA
+// than both operands in shared memory (~120 cycles per 128 x N x 16 MMA
+// including the epilogue's share, N = 64 .. 96): the MMAs are bound by an
+// instruction cadence, not by operand reads, and the smaller N it needs
+// (TMEM budget) adds tiles.  Both configurations below keep A in shared
+// memory; the TMEM variant stays selectable and tested.
+template <int S_, int NACC_, int BN_, int ATMEM_ = 0>
 struct Cfg {
-  static const int S = S_, NACC = NACC_, BN = BN_;
-  static const int NBUF = 2 * NACC * BN <= 512 ? 2 : 1;
+  static const int S = S_, NACC = NACC_, BN = BN_, ATMEM = ATMEM_;
+  static const int ACOLS = ATMEM ? 2 * S * 8 : 0;  // TMEM columns of the A buffers
+  static const int NBUF = 2 * NACC * BN + ACOLS <= 512 ? 2 : 1;
   static const int B_ELEMS = BN * BK, B_BYTES = B_ELEMS * 2;
   static const int LBO_B = BN * 16;
   static const int NPROD = S * (S + 1) / 2;
-  static_assert(NACC * BN <= 512, "accumulators exceed TMEM");
+  static_assert(NACC * BN + ACOLS <= 512, "accumulators and A buffers exceed TMEM");
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "MMA N");
 };
 // 7 digits (48 bits), 28 products, groups 0..3 exact: normwise ~1e-13
@@ -75,6 +85,8 @@ typedef Cfg<7, 5, 96> CfgStd;
 // Helmholtz recurrence magnifies input perturbations up to ~4000x at large
 // shifts, so its mixed form needs FP64-level transforms)
 typedef Cfg<8, 6, 80> CfgPrec;
+// the TMEM-A variant of CfgPrec (BN = 64: 6 x 64 accumulator + 2 x 64 A columns)
+typedef Cfg<8, 6, 64, 1> CfgPrecTmemA;
 
 // index of element (row r, k in the K block) inside a block of `rows` rows:
 // [k / 8][r / 8][r % 8][k % 8]

@@ -120,11 +120,28 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   if (warp == 0 && lane == 0) {
     // producer
     int64_t q = 0;  // ring position over all tiles
+    // the A slices miss L2 on first touch (the matrix's B slices stay
+    // resident): prefetch them into L2 PF_STEPS K steps ahead, across the
+    // boundary into this CTA's next tile, so that the ring's bulk copies
+    // (STAGES steps deep) hit L2
+    constexpr int PF_STEPS = 8;
+    auto prefetch_a = [&](int64_t tt, int ks) {
+      const int mtp = (int)(tt / g.ntiles), kb = g.kb0 + (ks >> 1), hf = ks & 1;
+      for (int s = 0; s < S; ++s)
+        tc::bulk_prefetch_l2(At + (((int64_t)s * g.mtiles + mtp) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2),
+                             AH);
+    };
+    if (blockIdx.x < ntile)
+      for (int ks = 0; ks < PF_STEPS && ks < nsteps; ++ks) prefetch_a(blockIdx.x, ks);
     for (int64_t t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
       const int nt = (int)(t % g.ntiles), mt = (int)(t / g.ntiles);
       for (int ks = 0; ks < nsteps; ++ks, ++q) {
         const int st = (int)(q % STAGES);
         const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
+        if (ks + PF_STEPS < nsteps)
+          prefetch_a(t, ks + PF_STEPS);
+        else if (t + gridDim.x < ntile && ks + PF_STEPS - nsteps < nsteps)
+          prefetch_a(t + gridDim.x, ks + PF_STEPS - nsteps);
         if (q >= STAGES && !tc::mbar_wait(&empty[st], ph ^ 1u)) {
           ok = false;
           break;
@@ -167,7 +184,23 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           ok = false;
           break;
         }
+        if (C::ATMEM && q >= 2) {
+          // A buffer (q & 1) was last read by the MMAs of step q - 2: their
+          // commit completed that step's phase of its stage's empty barrier
+          const int64_t q2 = q - 2;
+          if (!tc::mbar_wait(&empty[q2 % STAGES], (uint32_t)(q2 / STAGES) & 1u)) {
+            ok = false;
+            break;
+          }
+        }
         tc::fence_after_sync();
+        const uint32_t abuf = tmem + (uint32_t)(NACC * BN + (q & 1) * S * 8);
+        if (C::ATMEM) {
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+            tc::tmem_cp_128x256b(abuf + (uint32_t)(s * 8),
+                                 tc::sdesc_interleave(tc::smem_u32(sA(st, s)), LBO_A, SBO));
+        }
 #pragma unroll
         for (int s = 0; s < S; ++s) {
           const uint64_t ad = tc::sdesc_interleave(tc::smem_u32(sA(st, s)), LBO_A, SBO);
@@ -175,11 +208,15 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           for (int tt = 0; tt + s < S; ++tt) {
             const uint64_t bd = tc::sdesc_interleave(tc::smem_u32(sB(st, tt)), C::LBO_B, SBO);
             const int acc = s + tt < NACC - 1 ? s + tt : NACC - 1;
-            tc::mma_f16(dbase + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
+            if (C::ATMEM)
+              tc::mma_f16_ts(dbase + (uint32_t)(acc * BN), abuf + (uint32_t)(s * 8), bd, idesc,
+                             (inited >> acc) & 1u);
+            else
+              tc::mma_f16(dbase + (uint32_t)(acc * BN), ad, bd, idesc, (inited >> acc) & 1u);
             inited |= 1u << acc;
           }
         }
-        tc::mma_commit(&empty[st]);  // frees the stage once these MMAs have read it
+        tc::mma_commit(&empty[st]);  // frees the stage once these MMAs (and copies) have read it
       }
       tc::mma_commit(&tfull[b]);  // set b final (also after an early exit)
     }

@@ -523,6 +523,9 @@ SGPU_HD void band_sep_factor_prog(const BandSepDesc& d, double* fac, int64_t nsy
 template <class T>
 SGPU_HD void band_sep_solve_prog(const T* b_all, T* u_all, const double* fac, const double* gens,
                                  int n, int64_t Nb, int64_t inner, int64_t nsys, int64_t chain) {
+  // rows prefetched PF at a time, as in the Helmholtz cached solve (the loads
+  // do not depend on the recurrence; each row is read before it is written)
+  constexpr int PF = 4;
   const int64_t s = chain >> 1;
   const int par = (int)(chain & 1);
   const int m = (n + 1) / 2;
@@ -531,31 +534,69 @@ SGPU_HD void band_sep_solve_prog(const T* b_all, T* u_all, const double* fac, co
   const T* f = b_all + base;
   T* u = u_all + base;
   auto F = [&](int q, int c) { return fac[((size_t)q * m + c) * nch + chain]; };
-  int top = -1;
+  const int cend = (n - par + 1) / 2;  // chain rows k = 2c + par < n
   T y1 = zero_of(T()), y2 = zero_of(T());  // y_{c-1}, y_{c-2}
-  for (int c = 0; c < m; ++c) {
-    const int k = 2 * c + par;
-    if (k >= n) break;
-    T y = f[k * inner] - mulr(y1, F(1, c)) - mulr(y2, F(0, c));
-    u[k * inner] = y;
-    y2 = y1;
-    y1 = y;
-    top = c;
+  for (int c0 = 0; c0 < cend; c0 += PF) {
+    T fv[PF];
+    double l1[PF], l0[PF];
+#pragma unroll
+    for (int j = 0; j < PF; ++j) {
+      const int c = c0 + j;
+      if (c < cend) {
+        fv[j] = f[(2 * c + par) * inner];
+        l1[j] = F(1, c);
+        l0[j] = F(0, c);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < PF; ++j) {
+      const int c = c0 + j;
+      if (c < cend) {
+        T y = fv[j] - mulr(y1, l1[j]) - mulr(y2, l0[j]);
+        u[(2 * c + par) * inner] = y;
+        y2 = y1;
+        y1 = y;
+      }
+    }
   }
   T sq = zero_of(T()), st = zero_of(T());  // sum_{j >= c+1} q_j u_j, t_j u_j
   T up1 = zero_of(T()), up2 = zero_of(T());
-  for (int c = top; c >= 0; --c) {
-    const int k = 2 * c + par;
-    T v = u[k * inner] - mulr(up1, F(3, c)) - mulr(up2, F(4, c));
-    if (gens) v = v - mulr(sq, F(5, c)) - mulr(st, F(6, c));
-    v = mulr(v, F(2, c));
-    u[k * inner] = v;
-    if (gens) {
-      sq = sq + mulr(v, gens[n + k]);
-      st = st + mulr(v, gens[3 * n + k]);
+  for (int c0 = cend - 1; c0 >= 0; c0 -= PF) {
+    T yv[PF];
+    double dv[PF], e1[PF], e2[PF], p5[PF], p6[PF], gq[PF], gt[PF];
+#pragma unroll
+    for (int j = 0; j < PF; ++j) {
+      const int c = c0 - j;
+      if (c >= 0) {
+        const int k = 2 * c + par;
+        yv[j] = u[k * inner];
+        dv[j] = F(2, c);
+        e1[j] = F(3, c);
+        e2[j] = F(4, c);
+        if (gens) {
+          p5[j] = F(5, c);
+          p6[j] = F(6, c);
+          gq[j] = gens[n + k];
+          gt[j] = gens[3 * n + k];
+        }
+      }
     }
-    up2 = up1;
-    up1 = v;
+#pragma unroll
+    for (int j = 0; j < PF; ++j) {
+      const int c = c0 - j;
+      if (c >= 0) {
+        T v = yv[j] - mulr(up1, e1[j]) - mulr(up2, e2[j]);
+        if (gens) v = v - mulr(sq, p5[j]) - mulr(st, p6[j]);
+        v = mulr(v, dv[j]);
+        u[(2 * c + par) * inner] = v;
+        if (gens) {
+          sq = sq + mulr(v, gq[j]);
+          st = st + mulr(v, gt[j]);
+        }
+        up2 = up1;
+        up1 = v;
+      }
+    }
   }
 }
 
@@ -643,6 +684,14 @@ SGPU_HD R fac_at(const R* fac, int64_t q, int64_t k, int64_t M, int64_t nsys, in
   return fac[(q * M + k) * nsys + s];
 }
 
+// Both sweeps prefetch SOLVE_PF rows of their chain into registers before
+// running the recurrence over them: the loads do not depend on the
+// recurrence, so a thread keeps SOLVE_PF requests in flight instead of one
+// (the solve is bound by memory latency, not bandwidth, with one thread per
+// chain).  Rows are read before they are written in both sweeps, so b may
+// alias u.
+constexpr int SOLVE_PF = 8;
+
 template <class R, class T>
 SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac, int neumann,
                                          int64_t Nb, int64_t inner, int64_t nsys, int64_t s,
@@ -654,33 +703,66 @@ SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac,
   const T* f = b_all + base;
   T* u = u_all + base;
   // forward sweep y_i = f_i - L_{i-2} y_{i-2} along the chain i = par, par+2, ...
+  // (row i stores the multiplier the reference keeps in L[i-2])
   V y = E::zero();
   int64_t top = par;
-  for (int64_t i = par; i < M; i += 2) {
-    V fi = E::load(f + i * inner);
-    // row i stores the multiplier the reference keeps in L[i-2]
-    if (i >= 2) fi = fi - E::mul(y, fac_at(fac, 0, i, M, nsys, s));
-    y = fi;
-    E::store(u + i * inner, y);
-    top = i;
+  for (int64_t i0 = par; i0 < M; i0 += 2 * SOLVE_PF) {
+    V fv[SOLVE_PF];
+    R lv[SOLVE_PF];
+#pragma unroll
+    for (int j = 0; j < SOLVE_PF; ++j) {
+      const int64_t i = i0 + 2 * j;
+      if (i < M) {
+        fv[j] = E::load(f + i * inner);
+        lv[j] = fac_at(fac, 0, i, M, nsys, s);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < SOLVE_PF; ++j) {
+      const int64_t i = i0 + 2 * j;
+      if (i < M) {
+        V fi = fv[j];
+        if (i >= 2) fi = fi - E::mul(y, lv[j]);
+        y = fi;
+        E::store(u + i * inner, y);
+        top = i;
+      }
+    }
   }
   // back substitution from the top of the chain
   V up2 = E::zero(), S = E::zero(), pend = E::zero();  // u_{i+2}; sum of u_{>=i+4}
   bool have2 = false;
-  for (int64_t i = top; i >= 0; i -= 2) {
-    V yi = E::load(u + i * inner);
-    V ui = yi;
-    if (have2) ui = ui - E::mul(up2, fac_at(fac, 2, i, M, nsys, s));
-    if (i <= M - 5) {
-      S = S + pend;
-      ui = ui - E::mul(S, fac_at(fac, 3, i, M, nsys, s));
+  for (int64_t i0 = top; i0 >= 0; i0 -= 2 * SOLVE_PF) {
+    V yv[SOLVE_PF];
+    R dv[SOLVE_PF], d1v[SOLVE_PF], d2v[SOLVE_PF];
+#pragma unroll
+    for (int j = 0; j < SOLVE_PF; ++j) {
+      const int64_t i = i0 - 2 * j;
+      if (i >= 0) {
+        yv[j] = E::load(u + i * inner);
+        dv[j] = fac_at(fac, 1, i, M, nsys, s);
+        d1v[j] = fac_at(fac, 2, i, M, nsys, s);
+        d2v[j] = fac_at(fac, 3, i, M, nsys, s);
+      }
     }
-    ui = E::mul(ui, fac_at(fac, 1, i, M, nsys, s));
-    // Neumann: the recurrences run on w_i = i^2 u_i
-    E::store(u + i * inner, (neumann && i >= 1) ? E::mul(ui, from_f64<R>(1.0 / sn_col(i))) : ui);
-    pend = up2;
-    up2 = ui;
-    have2 = true;
+#pragma unroll
+    for (int j = 0; j < SOLVE_PF; ++j) {
+      const int64_t i = i0 - 2 * j;
+      if (i >= 0) {
+        V ui = yv[j];
+        if (have2) ui = ui - E::mul(up2, d1v[j]);
+        if (i <= M - 5) {
+          S = S + pend;
+          ui = ui - E::mul(S, d2v[j]);
+        }
+        ui = E::mul(ui, dv[j]);
+        // Neumann: the recurrences run on w_i = i^2 u_i
+        E::store(u + i * inner, (neumann && i >= 1) ? E::mul(ui, from_f64<R>(1.0 / sn_col(i))) : ui);
+        pend = up2;
+        up2 = ui;
+        have2 = true;
+      }
+    }
   }
 }
 

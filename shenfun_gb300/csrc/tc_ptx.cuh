@@ -94,6 +94,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// L2 prefetch of a global range (a hint: no shared memory, no completion);
+// src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // ---- tcgen05 ----------------------------------------------------------------
 // allocate `ncols` TMEM columns (power of two >= 32); the base address is
 // written to shared memory.  Executed by one whole warp.
@@ -128,6 +134,27 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
       "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
       : "memory");
+}
+
+// D[tmem] (+)= A[tmem] * B[smem]: the A operand (128 rows x 16 elements)
+// read from TMEM lanes 0..127, 8 columns at a_tmem (two 16-bit elements per
+// 32-bit column, K order)
+__device__ __forceinline__ void mma_f16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                           uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// copy a 128-row x 256-bit tile (128 x 16 16-bit elements in the canonical
+// layout `sdesc` describes) from shared memory into TMEM lanes 0..127,
+// columns taddr.col .. +7 (row r -> lane r); issued by one thread and
+// executed before the same thread's later tcgen05.mma
+__device__ __forceinline__ void tmem_cp_128x256b(uint32_t taddr, uint64_t sdesc) {
+  asm volatile("tcgen05.cp.cta_group::1.128x256b [%0], %1;" ::"r"(taddr), "l"(sdesc) : "memory");
 }
 
 // arrive once on `bar` when every MMA issued so far by this thread has completed

@@ -149,12 +149,15 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
     memcpy(&f, &u, 4);
     return f;
   };
+  // ATMEM: TMEM buffers of the A slices, [buffer][slice][lane 128][16 elements]
+  std::vector<float> tA(C::ATMEM ? (size_t)2 * S * BM * 16 : 0, std::numeric_limits<float>::quiet_NaN());
+  int64_t qg = 0;  // the MMA thread's step counter (selects the A buffer)
   for (int c = 0; c < num_chunks(g); ++c)
   for (int mt = 0; mt < g.mtiles; ++mt)
     for (int nt = 0; nt < g.ntiles; ++nt) {
       const Geom h = chunk_geom(g, c);  // one GEMM launch per K chunk
       uint32_t inited = 0;
-      for (int ks = 0; ks < 2 * (h.kb1 - h.kb0); ++ks) {
+      for (int ks = 0; ks < 2 * (h.kb1 - h.kb0); ++ks, ++qg) {
         const int st = ks % STAGES, kb = h.kb0 + (ks >> 1), hf = ks & 1;
         uint8_t* sbase = smem + st * stage_bytes;
         for (int s = 0; s < S; ++s) {
@@ -162,6 +165,21 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
                  At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2), AH);
           memcpy(sbase + (size_t)S * AH + (size_t)s * BH,
                  Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2), BH);
+        }
+        const int buf = (int)(qg & 1);
+        if (C::ATMEM) {
+          // tcgen05.cp 128x256b of each slice from its descriptor: row m -> lane m
+          for (int s = 0; s < S; ++s) {
+            const uint64_t ad = tc::sdesc_interleave((uint32_t)(st * stage_bytes + s * AH), LBO_A, SBO);
+            auto field = [](uint64_t d, int sh) { return (uint32_t)(((d >> sh) & 0x3FFF) << 4); };
+            const uint32_t as = field(ad, 0), al = field(ad, 16), asb = field(ad, 32);
+            for (int m = 0; m < BM; ++m)
+              for (int k = 0; k < 16; ++k) {
+                const uint32_t pa = as + (k >> 3) * al + (m >> 3) * asb + (m & 7) * 16 + (k & 7) * 2;
+                if (pa + 2 > STAGES * stage_bytes) return 6;
+                tA[(((size_t)buf * S + s) * BM + m) * 16 + k] = bf(smem + pa);
+              }
+          }
         }
         for (int s = 0; s < S; ++s)
           for (int t = 0; t + s < S; ++t) {
@@ -180,7 +198,8 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
                   const uint32_t pa = as + (k >> 3) * al + (m >> 3) * asb + (m & 7) * 16 + (k & 7) * 2;
                   const uint32_t pb = bs + (k >> 3) * bl + (n >> 3) * bsb + (n & 7) * 16 + (k & 7) * 2;
                   if (pa + 2 > STAGES * stage_bytes || pb + 2 > STAGES * stage_bytes) return 6;
-                  sum += (double)bf(smem + pa) * (double)bf(smem + pb);
+                  const float av = C::ATMEM ? tA[(((size_t)buf * S + s) * BM + m) * 16 + k] : bf(smem + pa);
+                  sum += (double)av * (double)bf(smem + pb);
                 }
                 float& d = acc[((size_t)a * BM + m) * BN + n];
                 d = (float)(((inited >> a) & 1 ? (double)d : 0.0) + sum);
@@ -225,11 +244,15 @@ static int ozaki(int argc, char** argv) {
   for (int k = 0; k < N; ++k)
     for (int n = 0; n < N; ++n)
       if (M[(size_t)k * N + n] != 0.0) K = k + 1;
-  oz::Geom g = oz::make_geom(N, nlines, inner, cplx, precise ? oz::CfgPrec::BN : oz::CfgStd::BN, K);
+  // precise: 0 CfgStd, 1 CfgPrec, 2 CfgPrecTmemA (A slices through TMEM)
+  const int bn = precise == 2 ? oz::CfgPrecTmemA::BN : (precise ? oz::CfgPrec::BN : oz::CfgStd::BN);
+  oz::Geom g = oz::make_geom(N, nlines, inner, cplx, bn, K);
   if (chunked) g.kchunk = atoi(argv[6]);  // argv shifted by one: the chunk argument
   double* out = (double*)malloc(sizeof(double) * cnt);
   for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
-  const int rc = precise ? ozaki_run<oz::CfgPrec>(g, in, M, out) : ozaki_run<oz::CfgStd>(g, in, M, out);
+  const int rc = precise == 2 ? ozaki_run<oz::CfgPrecTmemA>(g, in, M, out)
+                 : precise   ? ozaki_run<oz::CfgPrec>(g, in, M, out)
+                             : ozaki_run<oz::CfgStd>(g, in, M, out);
   if (rc) return rc;
   write_exact(argv[9], out, cnt);
   free(in);

@@ -286,7 +286,8 @@ def test_helmholtz_cached(emu, N, outer, inner, cplx, form):
 @pytest.mark.parametrize("N,nlines,inner,cplx,precise", [(40, 130, 1, 0, 0), (130, 70, 1, 0, 0),
                                                          (33, 50, 5, 1, 0), (24, 300, 3, 0, 0),
                                                          (64, 129, 1, 1, 0), (100, 40, 2, 1, 0),
-                                                         (40, 130, 1, 0, 1), (90, 60, 3, 1, 1)])
+                                                         (40, 130, 1, 0, 1), (90, 60, 3, 1, 1),
+                                                         (90, 60, 3, 1, 2), (130, 70, 1, 0, 2)])
 def test_ozaki_contraction(emu, N, nlines, inner, cplx, precise):
     """Split-BF16 tensor-core contraction (row exponents, digit split, slice
     tiles, MMA operand addressing from the descriptors, integer epilogue)
