@@ -76,9 +76,12 @@ extern "C" {
 #define SGPU_PLAIN_F64 0   /* all FP64                                        */
 #define SGPU_MIXED_DF 1    /* the mixed form, FP64 in and out: double-float (FP32
                               pair, ~48-bit) arithmetic on the FP32 pipes for
-                              the FFT/DCT line transforms; BF16 digit slices on
-                              the tensor cores (~48-bit) for the Legendre
-                              contractions                                     */
+                              the Fourier line transforms and for Chebyshev
+                              lines outside 16..1024; BF16 digit slices on the
+                              tensor cores for the Chebyshev composite
+                              transforms of 16..1024 points (8 digits, ~1e-15
+                              normwise) and the Legendre contractions (7
+                              digits, ~1e-13; N <= 8192 in K chunks of 1024) */
 
 const char* sgpu_status_string(int status);
 int sgpu_version(void);
