@@ -25,12 +25,23 @@ inline int xf_group(int kind) {
 }
 
 #ifdef __CUDACC__
-// three CTAs per SM: the line programs are latency-bound (long scoreboard
-// and barrier stalls at two CTAs, 118 registers); capping registers at 80
-// costs a few hundred bytes of L1-cached spills and measured 20-25 % faster
-// Fourier passes on the channel grid in both forms
+// CTAs per SM: the line programs are latency-bound (long scoreboard and
+// barrier stalls at two CTAs, 118 registers); capping registers (80 for
+// three CTAs, 64 for four) costs a few hundred bytes of L1-cached spills and
+// measured 20-25 % faster Fourier passes on the channel grid; four CTAs
+// measured best for FP64, three for double-float
+template <class R>
+struct LineMinBlocks {
+  static const int value = 3;
+};
+template <>
+struct LineMinBlocks<double> {
+  static const int value = 4;
+};
+
 template <class R, int G>
-__global__ void __launch_bounds__(256, 3) sgpu_line_kernel(LinePlan p, const double* in, double* out,
+__global__ void __launch_bounds__(256, LineMinBlocks<R>::value) sgpu_line_kernel(LinePlan p, const double* in,
+                                                                                double* out,
                                                         int data_complex, int64_t nlines,
                                                         int64_t inner, double scl) {
   extern __shared__ __align__(16) unsigned char sgpu_smem[];
