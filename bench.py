@@ -541,6 +541,8 @@ CASES = {
     "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
     "solve-plain": ("solve", "plain"),
     "leg-plain": ("leg", "plain"), "leg-mixed": ("leg", "mixed"),
+    # the whole round-trip step (scalar product, solve, backward)
+    "step-plain": ("step", "plain"), "step-mixed": ("step", "mixed"),
 }
 
 
@@ -570,6 +572,10 @@ def run_case(name, reps=3):
         c = torch.randn(16384, 512, dtype=torch.float64, device="cuda")
         y = torch.empty_like(c)
         fn = lambda: V.backward(c, y, axis=1)  # noqa: E731
+    elif kind == "step":
+        import shenfun_gb300 as sg
+        run = FormRun(sg, form, x.cpu().numpy())
+        fn = run.step
     else:
         import shenfun_gb300 as sg
         run = FormRun(sg, form, x.cpu().numpy())
