@@ -64,12 +64,8 @@ int xf_launch_group(const LinePlan& p, const double* in, double* out, int dc, in
                     int64_t inner, double scl, unsigned nblocks, cudaStream_t stream) {
   static bool attr_set = false;  // benign race: every caller sets the same value
   if (!attr_set) {
-    // the whole carve-out as shared memory: the CTAs per SM are then set by
-    // registers, not by the L1 / shared split
     if (cudaFuncSetAttribute(sgpu_line_kernel<R, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024) != cudaSuccess ||
-        cudaFuncSetAttribute(sgpu_line_kernel<R, G>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             cudaSharedmemCarveoutMaxShared) != cudaSuccess) {
+                             220 * 1024) != cudaSuccess) {
       cudaGetLastError();
       return SGPU_ERR_CUDA;
     }
