@@ -235,6 +235,14 @@ int sgpu_band_sep_factor(int n, int nterms, int gen_term, const double* bands,
 int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double* gens, int n,
                         int64_t outer, int64_t Nb, int64_t inner, int data_kind,
                         cudaStream_t stream);
+/* Matvec.pyx:908 Biharmonic_matvec (and the product of every other system
+ * above): c = (sum_t coef[t][s] M_t) v per system, with the same description
+ * as sgpu_band_sep_factor; v, c in the (outer, Nb, inner) layout, entries
+ * k >= n zeroed; v must not alias c. */
+int sgpu_band_sep_matvec(const void* v, void* c, int n, int nterms, int gen_term,
+                         const double* bands, const double* gens, const double* coef,
+                         int64_t outer, int64_t Nb, int64_t inner, int data_kind,
+                         cudaStream_t stream);
 
 /* ---- Helmholtz problem: the whole hot-path step in one call ----------------
  * (-lap + c) u = f on 2D R2C(N0) x D(N1) or 3D C2C(N0) x R2C(N1) x D(N2), D a

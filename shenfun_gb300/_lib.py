@@ -62,6 +62,7 @@ SIGNATURES = {
     "sgpu_helmholtz_factor": (_int, [_i64, _vp, _vp, _int, _i64, _i64, _int, _vp, _vp]),
     "sgpu_helmholtz_solve_cached": (_int, [_vp, _vp, _vp, _int, _i64, _i64, _i64, _int, _int, _vp]),
     "sgpu_band_sep_factor": (_int, [_int, _int, _int, _vp, _vp, _vp, _i64, _vp, _vp]),
+    "sgpu_band_sep_matvec": (_int, [_vp, _vp, _int, _int, _int, _vp, _vp, _vp, _i64, _i64, _i64, _int, _vp]),
     "sgpu_band_sep_solve": (_int, [_vp, _vp, _vp, _vp, _int, _i64, _i64, _i64, _int, _vp]),
     "sgpu_helmholtz_create": (_int, [ctypes.POINTER(_vp), _int, _vp, _int, _dbl, _int]),
     "sgpu_helmholtz_create_on": (_int, [ctypes.POINTER(_vp), _int, _vp, _int, _dbl, _int, _vp]),

@@ -291,6 +291,33 @@ extern "C" int sgpu_band_sep_factor(int n, int nterms, int gen_term, const doubl
   return finish();
 }
 
+template <class T>
+__global__ void k_band_sep_matvec(BandSepDesc d, const T* v, T* c, int64_t Nb, int64_t inner, int64_t nsys) {
+  int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ch < 2 * nsys) band_sep_matvec_prog<T>(d, v, c, Nb, inner, nsys, ch);
+}
+
+extern "C" int sgpu_band_sep_matvec(const void* v, void* c, int n, int nterms, int gen_term,
+                                    const double* bands, const double* gens, const double* coef,
+                                    int64_t outer, int64_t Nb, int64_t inner, int data_kind,
+                                    cudaStream_t stream) {
+  if (!v || !c || v == c || n < 2 || Nb < n || nterms < 1 || nterms > 3 || gen_term >= nterms ||
+      !bands || !coef || outer < 0 || inner < 1)
+    return SGPU_ERR_ARG;
+  if ((gen_term >= 0) != (gens != nullptr)) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  BandSepDesc d{n, nterms, gen_term, bands, gens, coef};
+  if (data_kind == SGPU_COMPLEX)
+    k_band_sep_matvec<cd><<<nblk(2 * nsys), kThreads, 0, stream>>>(d, (const cd*)v, (cd*)c, Nb, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_band_sep_matvec<double><<<nblk(2 * nsys), kThreads, 0, stream>>>(d, (const double*)v, (double*)c, Nb,
+                                                                       inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
 extern "C" int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double* gens,
                                    int n, int64_t outer, int64_t Nb, int64_t inner, int data_kind,
                                    cudaStream_t stream) {

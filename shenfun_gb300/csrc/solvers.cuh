@@ -600,6 +600,47 @@ SGPU_HD void band_sep_solve_prog(const T* b_all, T* u_all, const double* fac, co
   }
 }
 
+// c = M v with M = sum_t coef_t M_t (the matrix the factor/solve above
+// inverts): the residual Biharmonic_matvec (Matvec.pyx:908-1010) computes for
+// Chebyshev ShenBiharmonic, and the same product for every other
+// per-wavenumber system here.  One thread per (system, parity) chain, rows
+// descending so that the semiseparable part is two running sums
+// sum_{j >= k+2} q_j v_j and t_j v_j.  Entries k >= n of each line are zeroed.
+template <class T>
+SGPU_HD void band_sep_matvec_prog(const BandSepDesc& d, const T* v_all, T* c_all, int64_t Nb,
+                                  int64_t inner, int64_t nsys, int64_t chain) {
+  const int64_t s = chain >> 1;
+  const int par = (int)(chain & 1);
+  const int n = d.n;
+  const int64_t base = sys_base(s, Nb, inner);
+  const T* v = v_all + base;
+  T* c = c_all + base;
+  const double cg = d.gen_term >= 0 ? d.coef[d.gen_term * nsys + s] : 0.0;
+  const double* gp = d.gens;
+  const double* gq = d.gens ? d.gens + n : nullptr;
+  const double* gr = d.gens ? d.gens + 2 * n : nullptr;
+  const double* gt = d.gens ? d.gens + 3 * n : nullptr;
+  T sq = zero_of(T()), st = zero_of(T());
+  int top = n - 1;
+  if ((top & 1) != par) --top;
+  for (int k = top; k >= 0; k -= 2) {
+    if (d.gens && k + 2 < n) {
+      const T vk2 = v[(k + 2) * inner];
+      sq = sq + mulr(vk2, gq[k + 2]);
+      st = st + mulr(vk2, gt[k + 2]);
+    }
+    T acc = zero_of(T());
+#pragma unroll
+    for (int o = 0; o < 5; ++o) {
+      const int j = k + 2 * o - 4;
+      if (j >= 0 && j < n) acc = acc + mulr(v[j * inner], bs_band(d, nsys, s, o, k));
+    }
+    if (d.gens) acc = acc + mulr(sq, cg * gp[k]) + mulr(st, cg * gr[k]);
+    c[k * inner] = acc;
+  }
+  for (int64_t k = n + par; k < Nb; k += 2) c[k * inner] = zero_of(T());
+}
+
 // ---- factorisation cache: interleaved, reciprocal-pivot layout -------------
 // fac[q][k][s] for q = 0..3 (L, 1/d0, d1, d2), k in [0, M), s a system:
 // consecutive systems are contiguous, so thread s reads row k coalesced.

@@ -290,6 +290,18 @@ class BandSepSolver:
                   data_kind(b), stream_handle())
         return u
 
+    def matvec(self, v, c):
+        """c = (sum_t scale_t M_t) v per wavenumber (Biharmonic.matvec,
+        chebyshev/la.py:552-558: the residual of the solve); v must not be c."""
+        v, cr = _raw(v), _raw(c)
+        outer, Nb, inner = view3(tuple(v.shape), self.axis)
+        if (outer, inner) != (self._outer, self._inner) or Nb != self.N:
+            raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
+        _lib.call("sgpu_band_sep_matvec", ptr(v), ptr(cr), self.n, self._coef.shape[0], self.gen_term,
+                  ptr(self._bands), ptr(self._gens) if self._gens is not None else None, ptr(self._coef),
+                  outer, Nb, inner, data_kind(v), stream_handle())
+        return c
+
 
 class Biharmonic(BandSepSolver):
     """Chebyshev ShenBiharmonic solver for a0 S + alfa A + beta B

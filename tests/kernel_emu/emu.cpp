@@ -373,6 +373,7 @@ int main(int argc, char** argv) {
   }
   if (mode == "bandsep") {
     // bandsep n nterms gen_term nsys Nb data_kind bands.bin gens.bin coef.bin b.bin out.bin
+    // (out: the solution, then the matvec of the solution)
     int n = atoi(argv[2]), nterms = atoi(argv[3]), gen = atoi(argv[4]);
     long long nsys = atoll(argv[5]), Nb = atoll(argv[6]);
     int dk = atoi(argv[7]);
@@ -393,7 +394,15 @@ int main(int argc, char** argv) {
       if (dk) band_sep_solve_prog<cd>((const cd*)b, (cd*)u, fac, g, n, Nb, 1, nsys, ch);
       else band_sep_solve_prog<double>(b, u, fac, g, n, Nb, 1, nsys, ch);
     }
-    write_exact(argv[12], u, cnt);
+    // then the matvec of the solution: out = [u | M u]
+    double* mv = (double*)malloc(sizeof(double) * 2 * cnt);
+    for (size_t i = 0; i < cnt; ++i) mv[i] = u[i];
+    for (size_t i = cnt; i < 2 * cnt; ++i) mv[i] = std::numeric_limits<double>::quiet_NaN();
+    for (long long ch = 0; ch < 2 * nsys; ++ch) {
+      if (dk) band_sep_matvec_prog<cd>(d, (const cd*)u, (cd*)(mv + cnt), Nb, 1, nsys, ch);
+      else band_sep_matvec_prog<double>(d, u, mv + cnt, Nb, 1, nsys, ch);
+    }
+    write_exact(argv[12], mv, 2 * cnt);
     return 0;
   }
   if (mode == "nmatvec") {

@@ -52,14 +52,20 @@ def _systems(emu, fam, name, N, orders, coefs, cplx):  # noqa: F811
     if cplx:
         f = f + 1j * rng.standard_normal(f.shape)
     cnt = nsys * N * (2 if cplx else 1)
-    u = run(emu, ["bandsep", n, len(orders), gen_term, nsys, N, int(cplx)],
-            [bands, gens, coefs, f], cnt)
-    u = (u.view(np.complex128) if cplx else u).reshape(nsys, N)
+    out = run(emu, ["bandsep", n, len(orders), gen_term, nsys, N, int(cplx)],
+              [bands, gens, coefs, f], 2 * cnt)
+    out = out.view(np.complex128) if cplx else out
+    u = out[:out.size // 2].reshape(nsys, N)
+    mv = out[out.size // 2:].reshape(nsys, N)
     for s in range(nsys):
         M = sum(coefs[t, s] * MX.band_sep_dense(*terms[t]) for t in range(len(orders)))
         ref = np.linalg.solve(M, f[s, :n])
         err = np.abs(u[s, :n] - ref).max() / np.abs(ref).max()
         assert err < 1e-11, (s, err)
+        # the matvec (Biharmonic_matvec's product) of the solution, and its tail
+        mref = M @ u[s, :n]
+        assert np.abs(mv[s, :n] - mref).max() <= 1e-13 * np.abs(mref).max() + 1e-300
+        assert np.all(mv[s, n:] == 0)
 
 
 @pytest.mark.parametrize("N", [16, 17, 33])

@@ -113,3 +113,32 @@ def test_cfg3_biharmonic_full_size(sg):
     ref = P.backward(P.biharmonic_solve(ref_fh, bases, 2), bases)
     assert rel(uq, ref) < 1e-10
     assert rel(uq, sg.Array(T, buffer=ue).v) < 1e-10
+
+
+@pytest.mark.parametrize("Nz", [16, 17, 65])
+def test_biharmonic_matvec(sg, Nz):
+    """Biharmonic.matvec (the residual Biharmonic_matvec, Matvec.pyx:908):
+    the product of the oracle's dense SSBSB / ASBSB / BSBSB per wavenumber
+    (scales 1, -2 k^2, k^4 of inner(v, div(grad(div(grad(u)))))), and it
+    undoes the solve on the dofs; also for a Legendre ShenDirichlet system."""
+    from oracle import la as OL
+    Nx, Ny = 8, 6
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(Nx, "F", dtype="D"), sg.FunctionSpace(Ny, "F", dtype="d"),
+                                     sg.FunctionSpace(Nz, "C", bc=(0, 0, 0, 0))))
+    u, v = sg.TrialFunction(T), sg.TestFunction(T)
+    H = sg.chebyshev.la.Biharmonic(sg.inner(v, sg.div(sg.grad(sg.div(sg.grad(u))))))
+    rng = np.random.default_rng(Nz)
+    shape = (Nx, Ny // 2 + 1, Nz)
+    w = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    w[..., Nz - 4:] = 0
+    c = H.matvec(dev(w), torch.zeros(shape, dtype=torch.complex128, device="cuda"))
+    Sm, Am, Bm = OL.cheb_sb_dense(Nz)
+    k2 = P.fourier_k2([("fourier", "C2C", Nx), ("fourier", "R2C", Ny), ("chebyshev", "SB", Nz)], 2)
+    k2 = np.broadcast_to(k2, (Nx, Ny // 2 + 1, 1)).reshape(-1)
+    ws = w.reshape(-1, Nz)[:, :Nz - 4]
+    ref = np.zeros_like(w.reshape(-1, Nz))
+    for s in range(ws.shape[0]):
+        ref[s, :Nz - 4] = (Sm - 2 * k2[s] * Am + k2[s] ** 2 * Bm) @ ws[s]
+    assert rel(c.reshape(-1, Nz), ref) < 1e-12
+    x = H(c, torch.zeros_like(c))
+    assert rel(x, w) < 1e-10
