@@ -226,6 +226,55 @@ class FormRun:
         return 11 if self.form == "mixed" else 7
 
 
+def e2e_pipelined(torch, sg, run0, form, f_np, f_host, steps, st):
+    """Solves/s through the public API with host buffers, two requests in
+    flight: request i copies its RHS in (pinned H2D, its own stream), runs the
+    round trip on the compute stream and copies its solution out (D2H, its own
+    stream), while request i-1's copy-out and request i+1's copy-in overlap
+    it.  Every step moves its full input and output across the host link."""
+    slots = [run0, FormRun(sg, form, f_np)]
+    u_hosts = [torch.empty((NX, NY, NZ), dtype=torch.float64).pin_memory() for _ in slots]
+    h2d, comp, d2h = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    ev = lambda: torch.cuda.Event()  # noqa: E731
+    h_done, c_done, d_done = [ev(), ev()], [ev(), ev()], [ev(), ev()]
+
+    def submit(i):
+        k = i % 2
+        sl = slots[k]
+        with torch.cuda.stream(h2d):
+            if i >= 2:
+                h2d.wait_event(c_done[k])  # the slot's previous round trip read its RHS
+            sl.fj.v.copy_(f_host, non_blocking=True)
+            h_done[k].record(h2d)
+        with torch.cuda.stream(comp):
+            comp.wait_event(h_done[k])
+            if i >= 2:
+                comp.wait_event(d_done[k])  # the slot's previous solution was copied out
+            sl.step()
+            c_done[k].record(comp)
+        with torch.cuda.stream(d2h):
+            d2h.wait_event(c_done[k])
+            u_hosts[k].copy_(sl.uq.v, non_blocking=True)
+            d_done[k].record(d2h)
+
+    for i in range(4):  # warm-up of both slots
+        submit(i)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for s_ in (h2d, comp, d2h):
+        s_.wait_stream(st)
+    for i in range(steps):
+        submit(i)
+    for s_ in (h2d, comp, d2h):
+        st.wait_stream(s_)
+    b.record(st)
+    b.synchronize()
+    # the last solution arrived on the host and equals the resident result
+    assert torch.equal(u_hosts[(steps - 1) % 2], slots[(steps - 1) % 2].uq.v.cpu())
+    return steps / (a.elapsed_time(b) / 1e3)
+
+
 def time_steps_gpu(torch, fn, steps, flush, st):
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(steps)]
@@ -696,7 +745,8 @@ def main():
         e2e_step()
     b.record(st)
     b.synchronize()
-    e2e_val = ws * e2e_steps / (a.elapsed_time(b) / 1e3)
+    e2e_serial = ws * e2e_steps / (a.elapsed_time(b) / 1e3)
+    e2e_val = e2e_pipelined(torch, sg, run, chosen, f_np, f_host, e2e_steps, st) * ws
 
     serving = legendre = imex = biharmonic = latency = neumann = dealias = None
     if rank == 0 and not args.no_extra:
@@ -736,7 +786,10 @@ def main():
                              frac=achieved / peak, traffic=traffic, peak_source=peak_kind),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "solves/s",
-                    "h2d_bytes_per_step": R_BYTES, "d2h_bytes_per_step": R_BYTES},
+                    "h2d_bytes_per_step": R_BYTES, "d2h_bytes_per_step": R_BYTES,
+                    "mode": "two requests in flight: H2D and D2H on their own streams overlap the "
+                            "other request's round trip",
+                    "sequential_value": e2e_serial},
             "gpu_launches": sum(runs[k].launches_per_step for k in runs) * args.steps,
             "clocks": clk.summary(),
             "serving": serving,
