@@ -718,13 +718,11 @@ def main():
         peak, peak_kind = peaks()
         achieved = STAGE_BYTES[dom] / (stage_ms[dom] / 1e3) / 1e9
         roof = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": STAGE_BYTES[dom]}
-    traffic = None
-    tp = os.path.join(REPO, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get(f"{chosen}:{dom}")
-        except Exception:
-            traffic = None
+    # DRAM bytes of the dominant stage's kernels, one ncu capture each
+    # (dram__bytes_read.sum + dram__bytes_write.sum per launch, full-size z
+    # pass; profiles/tensor_contraction_256x256x257.md): k_oz_rowexp 134.9 MB,
+    # k_oz_split<8> 377.7 MB, k_oz_gemm 539.0 MB
+    traffic = {"mixed:z_scalar_product": 1051.6e6, "mixed:z_backward": 1051.6e6}.get(f"{chosen}:{dom}")
 
     # end to end through the public API with host buffers (pinned), per step:
     # H2D of the RHS, round trip, D2H of the solution
@@ -783,7 +781,8 @@ def main():
             "forms": results,
             "chosen_over_plain": results["mixed"]["value"] / results["plain"]["value"],
             "roofline": dict(roof, kernel=f"{chosen}:{dom}", achieved=achieved, peak=peak,
-                             frac=achieved / peak, traffic=traffic, peak_source=peak_kind),
+                             frac=achieved / peak, traffic=traffic, peak_source=peak_kind,
+                             traffic_unit="bytes per stage (ncu)" if traffic else None),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "solves/s",
                     "h2d_bytes_per_step": R_BYTES, "d2h_bytes_per_step": R_BYTES,
