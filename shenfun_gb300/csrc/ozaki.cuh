@@ -258,7 +258,9 @@ struct Geom {
   int N;           // line length (= Nout, and the K extent of the tiles)
   int K;           // leading input entries the matrix uses (its other rows are zero)
   int cplx;
-  int nkb;         // K blocks of BK (K padded with zeros)
+  int nkb;         // K blocks of BK the contraction runs over: the K active
+                   // input entries, padded (the A slices hold these blocks)
+  int nkb_b;       // K blocks of the matrix tiles: all N rows, padded
   int mtiles;      // row tiles of BM
   int ntiles;      // output-column tiles of BN
   // one GEMM launch sums the K blocks [kb0, kb1): at most KCHUNK_MAX blocks,
@@ -293,7 +295,10 @@ inline Geom make_geom(int N, int64_t nlines, int64_t inner, int cplx, int BN, in
   g.inner = inner;
   g.cplx = cplx;
   g.nrows = nlines * (1 + cplx);
-  g.nkb = (N + BK - 1) / BK;
+  // rows >= K of the matrix are zero: their input entries need no slices and
+  // their K steps no MMAs (a backward transform skips the boundary dofs)
+  g.nkb = ((K > 0 ? K : 1) + BK - 1) / BK;
+  g.nkb_b = (N + BK - 1) / BK;
   g.mtiles = (int)((g.nrows + BM - 1) / BM);
   g.ntiles = (N + BN - 1) / BN;
   g.kb0 = 0;

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           tc::bulk_g2s(sA(st, s), At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2),
                        AH, &full[st]);
           tc::bulk_g2s(sB(st, s),
-                       Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2),
+                       Bt + (((int64_t)s * g.ntiles + nt) * g.nkb_b + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2),
                        BH, &full[st]);
         }
       }

@@ -164,7 +164,7 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
           memcpy(sbase + (size_t)s * AH,
                  At + (((int64_t)s * g.mtiles + mt) * g.nkb + kb) * A_ELEMS + hf * (A_ELEMS / 2), AH);
           memcpy(sbase + (size_t)S * AH + (size_t)s * BH,
-                 Bt + (((int64_t)s * g.ntiles + nt) * g.nkb + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2), BH);
+                 Bt + (((int64_t)s * g.ntiles + nt) * g.nkb_b + kb) * C::B_ELEMS + hf * (C::B_ELEMS / 2), BH);
         }
         const int buf = (int)(qg & 1);
         if (C::ATMEM) {
