@@ -134,6 +134,19 @@ int sgpu_fourier_pad(const void* in, void* out, int64_t outer, int N, int M, int
 int sgpu_fourier_truncate(const void* in, void* out, int64_t outer, int N, int M, int64_t inner, int kind,
                           cudaStream_t stream);
 
+/* ---- the other banded solvers of the dispatch list: DiagMA (offsets 0),
+ * TwoDMA (0, 2), ThreeDMA (0, 2, 4), FDMA (-2, 0, 2, 4), HeptaDMA
+ * (-4 .. 8) (la.py:291-800; la.pyx DiagMA/TwoDMA/ThreeDMA/FDMA/HeptaDMA
+ * _LU / _Solve) --------------------------------------------------------------
+ * data: ndiag rows of n in the reference's column-aligned (scipy DIA)
+ * layout, row r holding M[i][i + offsets[r]] at column i + offsets[r];
+ * offsets (host array) even, ascending, containing 0 and every even value
+ * between the first and the last.  LU in place without pivoting; the solve
+ * runs along the middle axis of u (outer, n, inner), in place. */
+int sgpu_banded_LU(double* data, int ndiag, const int* offsets, int64_t n, cudaStream_t stream);
+int sgpu_banded_Solve(void* u, const double* data, int ndiag, const int* offsets, int64_t outer,
+                      int64_t n, int64_t inner, int data_kind, cudaStream_t stream);
+
 /* ---- banded solvers (optimization/cython/la.pyx) ------------------------
  * TDMA: offsets (-2, 0, 2); data is (3, n): data[0,:-2] = ld, data[1] = d,
  * data[2,2:] = ud (la.py:331-393).  PDMA: offsets (-4..4) in (5, n) rows

@@ -421,3 +421,64 @@ def ann_solve(b, A0, A2, scale, axis=0, u0=0.0):
     uv[0] = u0
     uv[M:] = 0
     return u
+
+
+# ---------------------------------------------------------------------------
+# The other banded solvers: DiagMA, TwoDMA, ThreeDMA, FDMA, HeptaDMA
+# (la.py:291-800).  data in the reference's column-aligned DIA layout:
+# row r holds M[i][i + off[r]] at column i + off[r].
+def dia_dense(data, offsets):
+    n = data.shape[1]
+    M = np.zeros((n, n))
+    for r, o in enumerate(offsets):
+        for i in range(n):
+            if 0 <= i + o < n:
+                M[i, i + o] = data[r, i + o]
+    return M
+
+
+def threedma_effective(data):
+    """ThreeDMA.inner_solve reads its offset-4 coefficient of row i from the
+    offset-2 row's storage (u2 = data[1, 4:], la.py:686-689, la.pyx:569-580):
+    u2[i] = data[1, i + 4].  Returns the DIA data of the matrix it solves."""
+    eff = np.array(data, copy=True)
+    n = data.shape[1]
+    eff[2, 4:] = data[1, 4:n]
+    return eff
+
+
+def banded_lu(data, offsets):
+    """Doolittle LU without pivoting, in place in the DIA layout (the
+    reference's *_LU recurrences are this elimination for their bands)."""
+    n = data.shape[1]
+    row = {o: r for r, o in enumerate(offsets)}
+    for i in range(n):
+        piv = data[row[0], i]
+        for l in offsets:
+            if l >= 0 or i - l >= n:
+                continue
+            m = data[row[l], i] / piv
+            data[row[l], i] = m
+            for u in offsets:
+                if u <= 0 or i + u >= n:
+                    continue
+                data[row[u + l], i + u] -= m * data[row[u], i + u]
+    return data
+
+
+def banded_solve(u, data, offsets, axis=0):
+    """Forward then back substitution with the LU of banded_lu (*_Solve)."""
+    u = np.array(u, copy=True)
+    v = np.moveaxis(u, axis, 0)
+    n = data.shape[1]
+    for i in range(n):
+        for r, l in enumerate(offsets):
+            if l < 0 and i + l >= 0:
+                v[i] = v[i] - data[r, i + l] * v[i + l]
+    r0 = list(offsets).index(0)
+    for i in range(n - 1, -1, -1):
+        for r, o in enumerate(offsets):
+            if o > 0 and i + o < n:
+                v[i] = v[i] - data[r, i + o] * v[i + o]
+        v[i] = v[i] / data[r0, i]
+    return u

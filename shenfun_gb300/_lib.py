@@ -48,6 +48,8 @@ SIGNATURES = {
     "sgpu_plan_execute_ws": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp, ctypes.c_size_t, _vp]),
     "sgpu_fourier_pad": (_int, [_vp, _vp, _i64, _int, _int, _i64, _int, _vp]),
     "sgpu_fourier_truncate": (_int, [_vp, _vp, _i64, _int, _int, _i64, _int, _vp]),
+    "sgpu_banded_LU": (_int, [_vp, _int, _vp, _i64, _vp]),
+    "sgpu_banded_Solve": (_int, [_vp, _vp, _int, _vp, _i64, _i64, _i64, _int, _vp]),
     "sgpu_TDMA_LU": (_int, [_vp, _i64, _vp]),
     "sgpu_TDMA_Solve": (_int, [_vp, _vp, _i64, _i64, _i64, _int, _vp]),
     "sgpu_PDMA_LU": (_int, [_vp, _i64, _vp]),

@@ -72,6 +72,56 @@ __global__ void k_helmholtz_matvec(const T* v, T* b, const double* alfa, const d
   if (s < nsys) helmholtz_matvec_prog<T>(v, b, alfa, beta, N, inner, s);
 }
 
+__global__ void k_banded_lu(double* data, BandDesc b, int64_t n) { banded_lu_prog(data, b, n); }
+
+template <class T>
+__global__ void k_banded_solve(T* u, const double* data, BandDesc b, int64_t n, int64_t inner, int64_t nsys) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) banded_solve_prog<T>(u, data, b, n, inner, s);
+}
+
+namespace {
+// offsets: 1..9 even values, ascending, with 0 and every even value between
+// the first and the last (elimination fills in only inside the band)
+int band_desc(int ndiag, const int* offsets, int64_t n, BandDesc* b) {
+  if (!offsets || ndiag < 1 || ndiag > 9 || n < 1) return SGPU_ERR_ARG;
+  b->nd = ndiag;
+  for (int r = 0; r < ndiag; ++r) {
+    const int o = offsets[r];
+    if (o % 2 != 0 || (r > 0 && o != offsets[r - 1] + 2) || (o < 0 ? -o : o) >= n) return SGPU_ERR_ARG;
+    b->off[r] = o;
+  }
+  if (offsets[0] > 0 || offsets[ndiag - 1] < 0) return SGPU_ERR_ARG;
+  return SGPU_OK;
+}
+}  // namespace
+
+extern "C" int sgpu_banded_LU(double* data, int ndiag, const int* offsets, int64_t n, cudaStream_t stream) {
+  BandDesc b;
+  if (!data) return SGPU_ERR_ARG;
+  const int st = band_desc(ndiag, offsets, n, &b);
+  if (st != SGPU_OK) return st;
+  k_banded_lu<<<1, 1, 0, stream>>>(data, b, n);
+  return finish();
+}
+
+extern "C" int sgpu_banded_Solve(void* u, const double* data, int ndiag, const int* offsets, int64_t outer,
+                                 int64_t n, int64_t inner, int data_kind, cudaStream_t stream) {
+  BandDesc b;
+  if (!u || !data || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int st = band_desc(ndiag, offsets, n, &b);
+  if (st != SGPU_OK) return st;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  if (data_kind == SGPU_COMPLEX)
+    k_banded_solve<cd><<<nblk(nsys), kThreads, 0, stream>>>((cd*)u, data, b, n, inner, nsys);
+  else if (data_kind == SGPU_REAL)
+    k_banded_solve<double><<<nblk(nsys), kThreads, 0, stream>>>((double*)u, data, b, n, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
 extern "C" int sgpu_TDMA_LU(double* data, int64_t n, cudaStream_t stream) {
   if (!data || n < 3) return SGPU_ERR_ARG;
   k_tdma_lu<<<1, 1, 0, stream>>>(data, n);

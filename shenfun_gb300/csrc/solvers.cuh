@@ -99,6 +99,70 @@ SGPU_HD void pdma_solve_prog(T* u_all, const double* data, int64_t n, int64_t in
     u[k] = mulr(u[k] - mulr(u[k + 2], e[k]) - mulr(u[k + 4], f[k]), 1.0 / d[k]);
 }
 
+// ---- general banded LU / solve (DiagMA, TwoDMA, ThreeDMA, FDMA, HeptaDMA) --
+// The reference's other banded solvers (la.py:291-800, la.pyx) differ only in
+// their band offsets.  Storage is theirs (scipy DIA, column aligned): row r of
+// data holds offset off[r], M[i][i + off[r]] at data[r * n + i + off[r]].
+// The offsets are even, ascending, include 0 and every even offset between
+// the lowest and the highest, so elimination without pivoting fills in only
+// inside the band.  LU in place (Doolittle: the multipliers replace the lower
+// entries), then per line forward and back substitution.
+struct BandDesc {
+  int nd;
+  int off[9];
+};
+
+SGPU_HD int band_row(const BandDesc& b, int o) {
+  for (int r = 0; r < b.nd; ++r)
+    if (b.off[r] == o) return r;
+  return -1;
+}
+
+SGPU_HD void banded_lu_prog(double* data, const BandDesc& b, int64_t n) {
+  const int r0 = band_row(b, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    const double piv = data[r0 * n + i];
+    for (int rl = 0; rl < b.nd; ++rl) {
+      const int l = b.off[rl];
+      if (l >= 0) continue;
+      const int64_t k = i - l;  // row eliminated
+      if (k >= n) continue;
+      double& mk = data[rl * n + i];  // M[k][i] (offset l of row k, column i)
+      const double m = mk / piv;
+      mk = m;
+      for (int ru = 0; ru < b.nd; ++ru) {
+        const int u = b.off[ru];
+        if (u <= 0 || i + u >= n) continue;
+        const int rt = band_row(b, u + l);  // offset of (k, i + u)
+        data[(int64_t)rt * n + i + u] -= m * data[(int64_t)ru * n + i + u];
+      }
+    }
+  }
+}
+
+template <class T>
+SGPU_HD void banded_solve_prog(T* u_all, const double* data, const BandDesc& b, int64_t n,
+                               int64_t inner, int64_t s) {
+  Line<T> u{u_all + sys_base(s, n, inner), inner};
+  const int r0 = band_row(b, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    T y = u[i];
+    for (int r = 0; r < b.nd; ++r) {
+      const int l = b.off[r];
+      if (l < 0 && i + l >= 0) y = y - mulr(u[i + l], data[r * n + i + l]);  // row i's multiplier
+    }
+    u[i] = y;
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    T x = u[i];
+    for (int r = 0; r < b.nd; ++r) {
+      const int o = b.off[r];
+      if (o > 0 && i + o < n) x = x - mulr(u[i + o], data[r * n + i + o]);
+    }
+    u[i] = divr(x, data[r0 * n + i]);
+  }
+}
+
 // ---- Chebyshev Dirichlet / Neumann Helmholtz -------------------------------
 // ASDSD / BSDSD coefficients in the reference's evaluation order
 // (chebyshev/matrices.py:1061-1079, :238-246).

@@ -4,6 +4,8 @@ reference): TDMA, PDMA, SolverGeneric1ND and the Chebyshev Helmholtz solver.
 Factorisations happen once at construction (on the device) and are reused by
 every call, like the reference's ``perform_lu`` / ``LU_Helmholtz``.
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -86,6 +88,83 @@ class PDMA(_BandedSolver):
     offsets = (-4, -2, 0, 2, 4)
     lu_entry = "sgpu_PDMA_LU"
     solve_entry = "sgpu_PDMA_Solve"
+
+
+class _GeneralBanded:
+    """Banded solver for the reference's other band patterns (la.py:291-800):
+    LU once on the device (sgpu_banded_LU), solve per call (sgpu_banded_Solve)
+    along any axis, in place; the dofs are the first n entries along it."""
+
+    offsets = None
+
+    def __init__(self, mat):
+        require_cuda()
+        if isinstance(mat, list):
+            mat = mat[0] if len(mat) == 1 else _sum_mats(mat)
+        self.mat = mat
+        self.n = mat.shape[0]
+        data = self._prepare(_band_data(mat, self.offsets))
+        self._lu = torch.as_tensor(data, device="cuda").contiguous()
+        self._off = (ctypes.c_int * len(self.offsets))(*self.offsets)
+        _lib.call("sgpu_banded_LU", ptr(self._lu), len(self.offsets), self._off, self.n, stream_handle())
+
+    @staticmethod
+    def _prepare(data):
+        return data
+
+    def __call__(self, b, u=None, axis=0, constraints=()):
+        b = _raw(b)
+        if u is None:
+            u = b
+        else:
+            u = _raw(u)
+            if u.data_ptr() != b.data_ptr():
+                u.copy_(b)
+        outer, n, inner = view3(tuple(u.shape), axis)
+        if n != self.n:
+            sub = u.narrow(axis, 0, self.n).contiguous()
+            o2, _, i2 = view3(tuple(sub.shape), axis)
+            _lib.call("sgpu_banded_Solve", ptr(sub), ptr(self._lu), len(self.offsets), self._off, o2, self.n,
+                      i2, data_kind(sub), stream_handle())
+            u.narrow(axis, 0, self.n).copy_(sub)
+            return u
+        _lib.call("sgpu_banded_Solve", ptr(u), ptr(self._lu), len(self.offsets), self._off, outer, n, inner,
+                  data_kind(u), stream_handle())
+        return u
+
+
+class DiagMA(_GeneralBanded):
+    """Diagonal (la.py:291-328)."""
+    offsets = (0,)
+
+
+class TwoDMA(_GeneralBanded):
+    """Offsets 0, 2 (la.py:615-659)."""
+    offsets = (0, 2)
+
+
+class ThreeDMA(_GeneralBanded):
+    """Offsets 0, 2, 4 (la.py:661-709).  The reference's solve reads the
+    offset-4 coefficient of row i from the offset-2 diagonal's storage
+    (u2 = data[1, 4:], la.py:686-689 and la.pyx:569-580), i.e. it solves the
+    matrix whose offset-4 entries are M[i + 2][i + 4]; kept for parity."""
+    offsets = (0, 2, 4)
+
+    @staticmethod
+    def _prepare(data):
+        data = data.copy()
+        data[2, 4:] = data[1, 4:]
+        return data
+
+
+class FDMA(_GeneralBanded):
+    """Offsets -2, 0, 2, 4 (la.py:545-613)."""
+    offsets = (-2, 0, 2, 4)
+
+
+class HeptaDMA(_GeneralBanded):
+    """Offsets -4, -2, 0, 2, 4, 6, 8 (la.py:711-800)."""
+    offsets = (-4, -2, 0, 2, 4, 6, 8)
 
 
 def _sum_mats(mats):

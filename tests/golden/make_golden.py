@@ -483,10 +483,41 @@ def nonhomog():
     put("nonhomog", **d)
 
 
+# --------------------------------------------------------------------------
+# The other banded solvers of the kernel dispatch list: DiagMA, TwoDMA,
+# ThreeDMA, FDMA, HeptaDMA (la.py:291-800, la.pyx), on diagonally dominant
+# random bands, solved along each axis of a 2D array.  Own rng.
+def dma():
+    from shenfun.matrixbase import SparseMatrix
+    g = np.random.default_rng(73)
+    d = {}
+    kinds = {"DiagMA": (0,), "TwoDMA": (0, 2), "ThreeDMA": (0, 2, 4), "FDMA": (-2, 0, 2, 4),
+             "HeptaDMA": (-4, -2, 0, 2, 4, 6, 8)}
+    for name, offs in kinds.items():
+        for n in (12, 17):
+            diags = {}
+            for o in offs:
+                m = n - abs(o)
+                diags[o] = (4.0 + g.uniform(0, 1, m)) if o == 0 else g.uniform(-0.5, 0.5, m)
+            M = SparseMatrix(dict(diags), (n, n))
+            dense = M.diags("csr").toarray()
+            for ax, shape in ((0, (n,)), (0, (n, 3)), (1, (4, n))):
+                b = g.standard_normal(shape)
+                sol = getattr(la, name)(SparseMatrix(dict(diags), (n, n)))
+                try:
+                    u = sol(b.copy(), axis=ax)
+                except ValueError:
+                    continue  # the reference's DiagMA solve takes 1D right-hand sides only
+                key = f"{name}{n}_{len(shape)}d_ax{ax}"
+                d.update({key + "_b": b, key + "_u": np.array(u)})
+            d[f"{name}{n}_dense"] = dense
+    put("dma", **d)
+
+
 GROUPS = {"cheb_1d": cheb_1d, "fourier_1d": fourier_1d, "banded": banded, "helmholtz": helmholtz,
           "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex,
           "dealias": dealias, "neumann": neumann,
-          "nonhomog": nonhomog}
+          "nonhomog": nonhomog, "dma": dma}
 
 if __name__ == "__main__":
     # no arguments: every group (the shared rng makes the earlier groups depend

@@ -483,6 +483,27 @@ int main(int argc, char** argv) {
     write_exact(argv[9], out, cnt * w);
     return 0;
   }
+  if (mode == "banded") {
+    // banded n ndiag outer inner data_kind offsets.bin raw.bin u.bin out.bin (LU then solve)
+    long long n = atoll(argv[2]);
+    int nd = atoi(argv[3]);
+    long long outer = atoll(argv[4]), inner = atoll(argv[5]);
+    int dk = atoi(argv[6]);
+    double* offd = read_exact(argv[7], nd);
+    BandDesc b;
+    b.nd = nd;
+    for (int r = 0; r < nd; ++r) b.off[r] = (int)offd[r];
+    double* data = read_exact(argv[8], (size_t)nd * n);
+    size_t cnt = (size_t)outer * n * inner * (dk ? 2 : 1);
+    double* u = read_exact(argv[9], cnt);
+    banded_lu_prog(data, b, n);
+    for (long long s = 0; s < outer * inner; ++s) {
+      if (dk) banded_solve_prog<cd>((cd*)u, data, b, n, inner, s);
+      else banded_solve_prog<double>(u, data, b, n, inner, s);
+    }
+    write_exact(argv[10], u, cnt);
+    return 0;
+  }
   if (mode == "tdma" || mode == "pdma") {
     long long n = atoll(argv[2]), outer = atoll(argv[3]), inner = atoll(argv[4]);
     int dk = atoi(argv[5]);

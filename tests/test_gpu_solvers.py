@@ -142,3 +142,38 @@ def test_biharmonic_matvec(sg, Nz):
     assert rel(c.reshape(-1, Nz), ref) < 1e-12
     x = H(c, torch.zeros_like(c))
     assert rel(x, w) < 1e-10
+
+
+DMA_OFFSETS = {"DiagMA": (0,), "TwoDMA": (0, 2), "ThreeDMA": (0, 2, 4), "FDMA": (-2, 0, 2, 4),
+               "HeptaDMA": (-4, -2, 0, 2, 4, 6, 8)}
+
+
+@pytest.mark.parametrize("name", sorted(DMA_OFFSETS))
+@pytest.mark.parametrize("n", [12, 17])
+def test_banded_solvers_golden(sg, golden, name, n):
+    """The reference's other banded solvers through sgpu_banded_LU / _Solve:
+    every recorded right-hand side (1D, and 2D along either axis) against the
+    reference's own solution, and complex right-hand sides against the
+    oracle."""
+    from oracle import la as OL
+    from shenfun_gb300.matrices import SpectralMatrix
+    d = golden("dma")
+    D = d[f"{name}{n}_dense"]
+    offs = DMA_OFFSETS[name]
+    mat = SpectralMatrix(name, {o: np.diagonal(D, o).copy() for o in offs}, (n, n))
+    solver = getattr(sg.la, name)(mat)
+    keys = [k[:-2] for k in d if k.startswith(f"{name}{n}_") and k.endswith("_b")]
+    for key in keys:
+        u = solver(dev(d[key + "_b"]), axis=int(key[-1]))
+        assert rel(u, d[key + "_u"]) < 1e-12
+    rng = np.random.default_rng(n)
+    b = rng.standard_normal((3, n, 4)) + 1j * rng.standard_normal((3, n, 4))
+    data = np.zeros((len(offs), n))
+    for r, o in enumerate(offs):
+        for i in range(n):
+            if 0 <= i + o < n:
+                data[r, i + o] = D[i, i + o]
+    if name == "ThreeDMA":
+        data = OL.threedma_effective(data)
+    OL.banded_lu(data, offs)
+    assert rel(solver(dev(b), axis=1), OL.banded_solve(b, data, offs, axis=1)) < 1e-12

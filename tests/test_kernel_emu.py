@@ -460,3 +460,27 @@ def test_ozaki_k_chunks(emu, N, nlines, kchunk, precise):
     assert np.abs(res - ref).max() / scale < tol
     one = run(emu, ["ozaki", N, nlines, 1, 0, precise], [x, M], x.size).reshape(x.shape)
     assert np.abs(res - one).max() / scale < tol
+
+
+# --------------------------------------------------------------------------
+# the general banded LU / solve (DiagMA, TwoDMA, ThreeDMA, FDMA, HeptaDMA)
+@pytest.mark.parametrize("offsets", [(0,), (0, 2), (0, 2, 4), (-2, 0, 2, 4), (-4, -2, 0, 2, 4, 6, 8)])
+@pytest.mark.parametrize("n,outer,inner", [(12, 1, 3), (17, 4, 1), (33, 2, 5)])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_general_banded(emu, offsets, n, outer, inner, cplx):
+    raw = np.zeros((len(offsets), n))
+    for r, o in enumerate(offsets):
+        lo, hi = max(0, o), n + min(0, o)
+        raw[r, lo:hi] = (4.0 + rng.uniform(0, 1, hi - lo)) if o == 0 else rng.uniform(-0.5, 0.5, hi - lo)
+    u = rng.standard_normal((outer, n, inner))
+    if cplx:
+        u = u + 1j * rng.standard_normal(u.shape)
+    cnt = u.size * (2 if cplx else 1)
+    got = run(emu, ["banded", n, len(offsets), outer, inner, int(cplx)],
+              [np.array(offsets, dtype=float), raw, u], cnt)
+    got = (got.view(np.complex128) if cplx else got).reshape(u.shape)
+    data = raw.copy()
+    la.banded_lu(data, offsets)
+    assert rel(got, la.banded_solve(u, data, offsets, axis=1)) < 1e-14
+    ref = np.einsum("ij,ojk->oik", np.linalg.inv(la.dia_dense(raw, offsets)), u)
+    assert rel(got, ref) < 1e-12

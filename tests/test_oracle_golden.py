@@ -265,3 +265,35 @@ def test_nonhomog_tensor(golden, tag, shape):
     sol = BC.helmholtz_bc_solve(d[key + "_rhs"], bases, 5.0, ax, BCV[tag])
     assert rel(sol, d[key + "_sol"]) < TOL
     assert rel(BC.tp_backward(sol, bases, ax), d[key + "_solx"]) < TOL
+
+
+# --------------------------------------------------------------------------
+# DiagMA / TwoDMA / ThreeDMA / FDMA / HeptaDMA (dma.npz)
+DMA_OFFSETS = {"DiagMA": (0,), "TwoDMA": (0, 2), "ThreeDMA": (0, 2, 4), "FDMA": (-2, 0, 2, 4),
+               "HeptaDMA": (-4, -2, 0, 2, 4, 6, 8)}
+
+
+def dma_data(D, offsets):
+    n = D.shape[0]
+    data = np.zeros((len(offsets), n))
+    for r, o in enumerate(offsets):
+        for i in range(n):
+            if 0 <= i + o < n:
+                data[r, i + o] = D[i, i + o]
+    return data
+
+
+@pytest.mark.parametrize("name", sorted(DMA_OFFSETS))
+@pytest.mark.parametrize("n", [12, 17])
+def test_banded_solvers(golden, name, n):
+    d = golden("dma")
+    offs = DMA_OFFSETS[name]
+    keys = [k[:-2] for k in d if k.startswith(f"{name}{n}_") and k.endswith("_b")]
+    assert keys
+    for key in keys:
+        data = dma_data(d[f"{name}{n}_dense"], offs)
+        if name == "ThreeDMA":
+            data = la.threedma_effective(data)
+        la.banded_lu(data, offs)
+        u = la.banded_solve(d[key + "_b"], data, offs, axis=int(key[-1]))
+        assert rel(u, d[key + "_u"]) < TOL
