@@ -3,8 +3,8 @@
 // In the mixed form the Chebyshev kinds (scalar product, forward, backward
 // of a basis) run as a dense line contraction on the tensor cores
 // (ozaki_tc.cu) instead of the double-float FFT: the operator is linear in
-// the line, so its N x N matrix is the FP64 block program applied to the
-// identity on the host, and one split-BF16 contraction applies it (about 48
+// the line, so its N x N matrix is the FP64 line kernel applied to the
+// identity (on the device), and one split-BF16 contraction applies it (about 48
 // bits; the forward matrix includes the mass solve, so its error is not
 // magnified by it).  On GB300 the O(N^2) contraction on the tensor cores
 // beats the O(N log N) transform on the FP32/FP64 pipes for N up to ~1000.
@@ -35,25 +35,58 @@ bool tensor_kind(int kind, int n, int form) {
          (kind == SGPU_XF_CHEB_SCALAR || kind == SGPU_XF_CHEB_FORWARD || kind == SGPU_XF_CHEB_BACKWARD);
 }
 
-// M[j][k] = output k of the FP64 transform of the unit line e_j (n x n)
+__global__ void k_identity(double* I, int n) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)n * n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    I[t] = (t / n == t % n) ? 1.0 : 0.0;
+}
+
+// M[j][k] = output k of the FP64 transform of the unit line e_j (n x n): the
+// FP64 line kernel applied to the n x n identity on the device, on a private
+// non-blocking stream with stream-ordered scratch, so that building a plan
+// does not wait for work on the caller's streams (the same block program on
+// the host took 3-40 ms for n = 129-1024)
 int operator_matrix(int kind, int n, int basis, std::vector<double>& M) {
   LinePlan p;
   HostTables T;
-  const int st = build_plan_host(kind, n, basis, SGPU_PLAIN_F64, p, T);
+  int st = build_plan_host(kind, n, basis, SGPU_PLAIN_F64, p, T);
   if (st != SGPU_OK) return st;
   if (p.n_in != n || p.n_out != n) return SGPU_ERR_UNSUPPORTED;
   size_t off[SGPU_NTAB];
-  std::vector<unsigned char> img(table_layout(T, off), 0);
+  const size_t tb = table_layout(T, off);
+  std::vector<unsigned char> img(tb, 0);
   table_image(T, off, img.data());
-  bind_tables(p, T, off, img.data());
-  std::vector<double> I((size_t)n * n, 0.0);
-  for (int j = 0; j < n; ++j) I[(size_t)j * n + j] = 1.0;
-  M.assign((size_t)n * n, 0.0);
-  std::vector<unsigned char> smem(p.smem + 16);
-  const int lpb = lines_per_block(p, 0);
-  for (int64_t b = 0; b < (n + lpb - 1) / lpb; ++b)
-    prog_dispatch<double>(p, I.data(), M.data(), 0, n, 1, 1.0, b, smem.data(), 0, 1);
-  return SGPU_OK;
+  const size_t tbr = (tb + 255) & ~(size_t)255, mb = (size_t)n * n * sizeof(double);
+  cudaStream_t s;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_CUDA;
+  }
+  unsigned char* dev = nullptr;
+  st = SGPU_OK;
+  if (cudaMallocAsync((void**)&dev, tbr + 2 * mb, s) != cudaSuccess) {
+    st = SGPU_ERR_NOMEM;
+  } else {
+    double* I = (double*)(dev + tbr);
+    double* O = I + (size_t)n * n;
+    bind_tables(p, T, off, dev);
+    M.assign((size_t)n * n, 0.0);
+    const int lpb = lines_per_block(p, 0);
+    const unsigned nb = (unsigned)((n + lpb - 1) / lpb);
+    if (cudaMemcpyAsync(dev, img.data(), tb, cudaMemcpyHostToDevice, s) != cudaSuccess) st = SGPU_ERR_CUDA;
+    if (st == SGPU_OK) {
+      k_identity<<<(unsigned)(((int64_t)n * n + 255) / 256 < 4096 ? ((int64_t)n * n + 255) / 256 : 4096), 256, 0,
+                   s>>>(I, n);
+      st = xf_launch_cheb_f64(xf_group(p.kind), p, I, O, 0, n, 1, 1.0, nb, s);
+    }
+    if (st == SGPU_OK && cudaMemcpyAsync(M.data(), O, mb, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      st = SGPU_ERR_CUDA;
+    cudaFreeAsync(dev, s);
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess && st == SGPU_OK) st = SGPU_ERR_CUDA;
+  cudaStreamDestroy(s);
+  cudaGetLastError();
+  return st;
 }
 
 }  // namespace

@@ -231,6 +231,14 @@ class GpuExecutor:
         self.shrink_cache(self.cache_budget)
         return p
 
+    def prepare(self, f):
+        """Host input as page-locked memory, so that its copy to the device
+        is asynchronous on the request's stream (a pageable source makes the
+        copy wait on the host)."""
+        torch = self.torch
+        t = f if isinstance(f, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(f))
+        return t if t.is_pinned() else t.pin_memory()
+
     # -- execution ----------------------------------------------------------
     def launch(self, req):
         torch = self.torch
@@ -288,9 +296,10 @@ def run_stream(stream, executor, max_slots=8, mem_budget=8 << 30, poll_sleep=0.0
     finished requests and the elapsed seconds."""
     sched = Scheduler(executor, max_slots=max_slots, mem_budget=mem_budget)
     reqs = []
+    prepare = getattr(executor, "prepare", None)
     for i, (N, fam, c, t, seed) in enumerate(stream):
         f = np.random.default_rng(seed).standard_normal(N)
-        reqs.append(Request(i, N, fam, c, f, t))
+        reqs.append(Request(i, N, fam, c, prepare(f) if prepare else f, t))
     t0 = time.perf_counter()
     now = lambda: time.perf_counter() - t0  # noqa: E731
     nxt = 0
