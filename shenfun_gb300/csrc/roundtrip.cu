@@ -13,6 +13,7 @@
 // Creation builds the transform plans and factorises every system (device
 // allocations happen there); the solve allocates nothing: its two scratch
 // arrays come from the caller (sgpu_helmholtz_workspace_size).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -137,7 +138,39 @@ void destroy_all(sgpu_helmholtz_problem* p) {
   delete p;
 }
 
-int64_t fftfreq(int64_t i, int64_t n) { return i <= (n - 1) / 2 ? i : i - n; }
+SGPU_HD int64_t fftfreq(int64_t i, int64_t n) { return i <= (n - 1) / 2 ? i : i - n; }
+
+// per-wavenumber scales alfa = -1, beta = |k|^2 + c of a problem, written on
+// the device (a pageable host source would make the copy wait for the
+// stream's earlier work)
+__global__ void k_problem_scales(double* alfa, double* beta, int64_t nsys, int ndim, int64_t n0, int64_t nr,
+                                 double c) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nsys; s += (int64_t)gridDim.x * blockDim.x) {
+    double k2;
+    if (ndim == 2) {
+      k2 = (double)(s * s);
+    } else {
+      const int64_t ix = s / (nr / 2 + 1), iy = s % (nr / 2 + 1);
+      const double kx = (double)fftfreq(ix, n0);
+      k2 = kx * kx + (double)(iy * iy);
+    }
+    alfa[s] = -1.0;
+    beta[s] = k2 + c;
+  }
+}
+
+// Legendre ShenDirichlet terms (legendre/matrices.py:121-135, 285-292):
+// term 0 the stiffness diagonal -(4k+6), term 1 the mass matrix
+__global__ void k_legendre_terms(double* bands, int64_t n) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double hk = 2.0 / (2.0 * k + 1.0), hk2 = 2.0 / (2.0 * (k + 2) + 1.0);
+    for (int r = 0; r < 10; ++r) bands[r * n + k] = 0.0;
+    bands[(0 * 5 + 2) * n + k] = -(4.0 * k + 6.0);
+    bands[(1 * 5 + 2) * n + k] = hk + hk2;
+    if (k + 2 < n) bands[(1 * 5 + 3) * n + k] = -hk2;
+    if (k >= 2) bands[(1 * 5 + 1) * n + k] = -hk;
+  }
+}
 
 int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int family, double c,
                 int form, bool ordered, cudaStream_t stream);
@@ -212,19 +245,6 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
     destroy_all(p);
     return SGPU_ERR_UNSUPPORTED;
   }
-  // per-wavenumber scales: alfa = -1, beta = |k|^2 + c
-  std::vector<double> alfa(p->nsys, -1.0), beta(p->nsys);
-  for (int64_t s = 0; s < p->nsys; ++s) {
-    double k2;
-    if (ndim == 2) {
-      k2 = (double)(s * s);
-    } else {
-      const int64_t ix = s / (nr / 2 + 1), iy = s % (nr / 2 + 1);
-      const double kx = (double)fftfreq(ix, N[0]);
-      k2 = kx * kx + (double)(iy * iy);
-    }
-    beta[s] = k2 + c;
-  }
   const int64_t n = Nd - 2;
   const int64_t m = (n + 1) / 2;
   size_t nfac = family == SGPU_FAMILY_CHEBYSHEV ? (size_t)4 * n * p->nsys
@@ -241,8 +261,9 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
   p->alfa = p->dev;
   p->beta = p->alfa + p->nsys;
   p->fac = p->beta + p->nsys;
-  cudaMemcpyAsync(p->alfa, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
-  cudaMemcpyAsync(p->beta, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
+  // per-wavenumber scales alfa = -1, beta = |k|^2 + c
+  const unsigned sgrid = (unsigned)std::min<int64_t>((p->nsys + 255) / 256, 1024);
+  k_problem_scales<<<sgrid, 256, 0, stream>>>(p->alfa, p->beta, p->nsys, ndim, N[0], nr, c);
   if (family == SGPU_FAMILY_CHEBYSHEV) {
     st = sgpu_helmholtz_factor(Nd, p->alfa, p->beta, 0, p->nsys, 1, SGPU_PLAIN_F64, p->fac, stream);
   } else {
@@ -250,18 +271,8 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
     // mass matrix B (legendre/matrices.py:121-135) with coefficient beta
     p->bands = p->fac + nfac;
     p->coef = p->bands + nb;
-    std::vector<double> bands(nb, 0.0);
-    std::vector<double> h(Nd);
-    for (int64_t k = 0; k < Nd; ++k) h[k] = 2.0 / (2.0 * k + 1.0);
-    for (int64_t k = 0; k < n; ++k) {
-      bands[(0 * 5 + 2) * n + k] = -(4.0 * k + 6.0);
-      bands[(1 * 5 + 2) * n + k] = h[k] + h[k + 2];
-      if (k + 2 < n) bands[(1 * 5 + 3) * n + k] = -h[k + 2];
-      if (k >= 2) bands[(1 * 5 + 1) * n + k] = -h[k];
-    }
-    cudaMemcpyAsync(p->bands, bands.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(p->coef, alfa.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(p->coef + p->nsys, beta.data(), sizeof(double) * p->nsys, cudaMemcpyHostToDevice, stream);
+    k_legendre_terms<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, stream>>>(p->bands, n);
+    cudaMemcpyAsync(p->coef, p->alfa, sizeof(double) * 2 * p->nsys, cudaMemcpyDeviceToDevice, stream);
     st = sgpu_band_sep_factor((int)n, 2, -1, p->bands, nullptr, p->coef, p->nsys, p->fac, stream);
   }
   // plain creation waits for the factorisation; stream-ordered creation leaves
