@@ -4,6 +4,9 @@
 // and by the CPU index-check harness (which keeps them in host memory).
 #pragma once
 
+#include <algorithm>
+#include <thread>
+
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -179,19 +182,30 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
       wi[e] = sinl(a);
     }
     rk.resize(m);
-    for (int s = 0; s < m; ++s) {
-      ld_t sr = 0, si = 0;
-      int e = 0;  // q * s mod m
-      for (int q = 0; q < m; ++q) {
-        const ld_t c = wr[e], sn = wi[e];
-        sr += br[q] * c - bi[q] * sn;
-        si += br[q] * sn + bi[q] * c;
-        e += s;
-        if (e >= m) e -= m;
+    T.rk_f.resize(m);
+    // O(m^2) in long double (software quad precision on some hosts): the
+    // outputs s are independent, spread over the host's cores
+    auto rk_range = [&](int s0, int s1) {
+      for (int s = s0; s < s1; ++s) {
+        ld_t sr = 0, si = 0;
+        int e = 0;  // q * s mod m
+        for (int q = 0; q < m; ++q) {
+          const ld_t c = wr[e], sn = wi[e];
+          sr += br[q] * c - bi[q] * sn;
+          si += br[q] * sn + bi[q] * c;
+          e += s;
+          if (e >= m) e -= m;
+        }
+        rk[s] = cx<double>((double)(sr / m), (double)(si / m));
+        T.rk_f[s] = cx<df>(ld_to_df(sr / m), ld_to_df(si / m));
       }
-      rk[s] = cx<double>((double)(sr / m), (double)(si / m));
-      T.rk_f.push_back(cx<df>(ld_to_df(sr / m), ld_to_df(si / m)));
-    }
+    };
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nth = m >= 64 ? (int)std::min(hw ? hw : 1u, 16u) : 1;
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; ++t) pool.emplace_back(rk_range, (int)((int64_t)m * t / nth), (int)((int64_t)m * (t + 1) / nth));
+    rk_range(0, (int)((int64_t)m / nth));
+    for (auto& th : pool) th.join();
   }
   if (cheb) {
     post.resize(n);
