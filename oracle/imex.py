@@ -54,15 +54,20 @@ def imex_run(u_hat0, f_hat, nu, dt, name, nsteps, bases, axis):
     ks = np.moveaxis(np.broadcast_to(k2, k2.shape), axis, -1).reshape(-1)
     one = np.ones_like(ks)
 
+    # a ShenNeumann axis takes the Neumann branch of the Helmholtz LU / solve
+    # and the ASNSN / BSNSN product (la.pyx:735-751, 907-912)
+    nm = bases[axis][1] == "SN"
+    matvec = la.helmholtz_neumann_matvec if nm else la.helmholtz_matvec
+
     def mv(v, alfa, beta):
         vs, shp = P._systems(v, axis)
-        return np.moveaxis(la.helmholtz_matvec(vs, alfa, beta).reshape(shp), -1, axis)
+        return np.moveaxis(matvec(vs, alfa, beta).reshape(shp), -1, axis)
 
-    d = la.helmholtz_lu(N, -dt * a[1, 1] * nu * one, one + dt * a[1, 1] * nu * ks)
+    d = la.helmholtz_lu(N, -dt * a[1, 1] * nu * one, one + dt * a[1, 1] * nu * ks, neumann=nm)
 
     def solve(f):
         fs, shp = P._systems(f, axis)
-        return np.moveaxis(la.helmholtz_solve(fs, *d).reshape(shp), -1, axis)
+        return np.moveaxis(la.helmholtz_solve(fs, *d, neumann=nm).reshape(shp), -1, axis)
 
     mask = nyquist_mask(bases)
     u = u_hat0.copy()

@@ -107,3 +107,33 @@ def test_imex_nonlinear_graph(sg):
         res.append(u_hat.v.clone())
     assert torch.isfinite(res[0]).all()
     assert torch.equal(res[0], res[1])
+
+
+@pytest.mark.parametrize("name", ["IMEXRK111", "IMEXRK222", "IMEXRK443"])
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_imex_neumann_oracle(sg, name, form):
+    """The IMEX caller on a ShenNeumann axis (the Neumann Helmholtz branch for
+    every stage's solve, the Neumann matvec for the linear forms): three
+    steps against the oracle's scheme with the Neumann LU and product."""
+    from oracle import imex as OI
+    from shenfun_gb300 import integrators as I
+    nb = [("fourier", "C2C", 8), ("fourier", "R2C", 8), ("chebyshev", "SN", 17)]
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(8, "F", dtype="D"), sg.FunctionSpace(8, "F", dtype="d"),
+                                     sg.FunctionSpace(17, "C", bc={"left": {"N": 0}, "right": {"N": 0}})),
+                              form=form)
+    rng = np.random.default_rng(41)
+    shape = (8, 5, 17)
+    u0 = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    f0 = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    u0[..., -2:] = 0
+    f0[..., -2:] = 0
+    nu, dt = 0.1, 0.01
+    u_hat = sg.Function(T, buffer=u0)
+    sol = getattr(I, name)(sg.TestFunction(T), u_hat, lambda u: nu * sg.div(sg.grad(u)),
+                           sg.Function(T, buffer=f0), dt)
+    sol.assemble()
+    ref = OI.imex_run(u0, f0, nu, dt, name, 3, nb, 2)
+    tol = 1e-12 if form == "plain" else 1e-10
+    for step in range(3):
+        sol.step()
+        assert rel(u_hat, ref[step]) < tol, step
