@@ -318,6 +318,15 @@ inline Geom chunk_geom(const Geom& g, int c) {
 }
 inline int num_chunks(const Geom& g) { return (g.nkb + g.kchunk - 1) / g.kchunk; }
 
+// MMA K steps (16 wide) of one launch: the chunk's blocks, cut at the last
+// active entry K; at least one (a zero contraction still initialises the
+// accumulators)
+SGPU_HD int oz_steps(const Geom& g) {
+  const int kend = g.kb1 * BK < g.K ? g.kb1 * BK : g.K;
+  const int n = (kend - g.kb0 * BK + 15) / 16;
+  return n < 1 ? 1 : n;
+}
+
 // largest exponent field of row `row` over the lanes' strided share
 // (lane, lane + nlane, ...) of the K entries the matrix uses (entries it
 // ignores, such as the boundary dofs a backward transform skips, must not

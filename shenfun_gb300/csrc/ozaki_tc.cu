@@ -115,7 +115,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   auto sB = [&](int st, int s) {
     return smem + (size_t)st * GemmSmem<C>::stage_bytes + (size_t)S * AH + (size_t)s * BH;
   };
-  const int nsteps = 2 * (g.kb1 - g.kb0);  // K steps of 16 per tile (this launch's chunk)
+  // K steps of 16 per tile in this launch's chunk, up to the last active
+  // input entry (a 257-long contraction runs 17 steps, not 18)
+  const int nsteps = oz_steps(g);
 
   if (warp == 0 && lane == 0) {
     // producer

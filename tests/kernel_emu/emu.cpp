@@ -157,7 +157,7 @@ static int ozaki_run(const oz::Geom& g, const double* in, const double* M, doubl
     for (int nt = 0; nt < g.ntiles; ++nt) {
       const Geom h = chunk_geom(g, c);  // one GEMM launch per K chunk
       uint32_t inited = 0;
-      for (int ks = 0; ks < 2 * (h.kb1 - h.kb0); ++ks, ++qg) {
+      for (int ks = 0; ks < oz_steps(h); ++ks, ++qg) {
         const int st = ks % STAGES, kb = h.kb0 + (ks >> 1), hf = ks & 1;
         uint8_t* sbase = smem + st * stage_bytes;
         for (int s = 0; s < S; ++s) {
