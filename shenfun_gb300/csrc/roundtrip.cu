@@ -92,30 +92,44 @@ std::mutex g_plan_mutex;
 std::map<std::tuple<int, int, int, int>, sgpu_plan*> g_plans;
 std::map<std::tuple<int, int, int>, sgpu_legendre_plan*> g_leg_plans;
 
-int cached_plan(sgpu_plan** out, int kind, int n, int basis, int form) {
+// Plans are built outside the lock, so that callers on several threads build
+// plans of different lengths at the same time; two callers that build the
+// same plan keep the first one inserted.
+template <class Plan, class Key, class Make, class Destroy>
+int cached(std::map<Key, Plan*>& cache, const Key& key, Plan** out, Make make, Destroy destroy) {
+  {
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second;
+      return SGPU_OK;
+    }
+  }
+  Plan* mine = nullptr;
+  const int st = make(&mine);
+  if (st != SGPU_OK) return st;
   std::lock_guard<std::mutex> lock(g_plan_mutex);
-  auto key = std::make_tuple(kind, n, basis, form);
-  auto it = g_plans.find(key);
-  if (it != g_plans.end()) {
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    destroy(mine);
     *out = it->second;
     return SGPU_OK;
   }
-  int st = sgpu_plan_create(out, kind, n, basis, form);
-  if (st == SGPU_OK) g_plans[key] = *out;
-  return st;
+  cache[key] = mine;
+  *out = mine;
+  return SGPU_OK;
+}
+
+int cached_plan(sgpu_plan** out, int kind, int n, int basis, int form) {
+  return cached(g_plans, std::make_tuple(kind, n, basis, form), out,
+                [&](sgpu_plan** p) { return sgpu_plan_create(p, kind, n, basis, form); },
+                [](sgpu_plan* p) { sgpu_plan_destroy(p); });
 }
 
 int cached_leg_plan(sgpu_legendre_plan** out, int n, int basis, int form) {
-  std::lock_guard<std::mutex> lock(g_plan_mutex);
-  auto key = std::make_tuple(n, basis, form);
-  auto it = g_leg_plans.find(key);
-  if (it != g_leg_plans.end()) {
-    *out = it->second;
-    return SGPU_OK;
-  }
-  int st = sgpu_legendre_plan_create(out, n, basis, form);
-  if (st == SGPU_OK) g_leg_plans[key] = *out;
-  return st;
+  return cached(g_leg_plans, std::make_tuple(n, basis, form), out,
+                [&](sgpu_legendre_plan** p) { return sgpu_legendre_plan_create(p, n, basis, form); },
+                [](sgpu_legendre_plan* p) { sgpu_legendre_plan_destroy(p); });
 }
 
 void destroy_all(sgpu_helmholtz_problem* p) {

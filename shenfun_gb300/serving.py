@@ -183,7 +183,7 @@ class GpuExecutor:
     """Runs requests on a pool of CUDA streams with a device-resident,
     byte-budgeted LRU cache of factorised problems."""
 
-    def __init__(self, nstreams=4, cache_budget=4 << 30, form="mixed", keep_results=True):
+    def __init__(self, nstreams=4, cache_budget=4 << 30, form="mixed", keep_results=True, prep_workers=4):
         import torch
         from .problem import HelmholtzProblem
         self.torch = torch
@@ -196,6 +196,16 @@ class GpuExecutor:
         self.keep_results = keep_results
         self.hits = 0
         self.misses = 0
+        # problems of new keys are built on worker threads (plan tables and
+        # matrices are host work; the library releases the GIL), so that the
+        # loop keeps launching requests whose problems are cached
+        self.pool = None
+        if prep_workers > 0:
+            from concurrent.futures import ThreadPoolExecutor
+            self.pool = ThreadPoolExecutor(max_workers=prep_workers)
+        self.pending = {}   # key -> (future, creation stream)
+        self.waiting = {}   # request id -> request whose problem is being built
+        self.failed = []    # request ids whose problem could not be built
 
     # -- factorisation cache ---------------------------------------------
     def cache_bytes(self):
@@ -207,7 +217,8 @@ class GpuExecutor:
     def shrink_cache(self, room):
         while self.cache and self.cache_bytes() > max(0, min(room, self.cache_budget)):
             key, _ = next(iter(self.cache.items()))
-            if any(r.key == key for r, _, _ in self.inflight.values()):
+            if any(r.key == key for r, _, _ in self.inflight.values()) or \
+                    any(r.key == key for r in self.waiting.values()):
                 break  # still in use
             self.cache.popitem(last=False)
 
@@ -239,11 +250,60 @@ class GpuExecutor:
         t = f if isinstance(f, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(f))
         return t if t.is_pinned() else t.pin_memory()
 
+    def _cached(self, req, stream):
+        """The cached problem of `req` for use on `stream` (a hit)."""
+        self.cache.move_to_end(req.key)
+        p, _, ready = self.cache[req.key]
+        if ready is not None and ready[1] is not stream:
+            stream.wait_event(ready[0])
+        return p
+
+    def _collect(self):
+        """Move finished builds into the cache and start the requests that
+        wait for them; a failed build fails its waiting requests."""
+        for key, (fut, cs) in list(self.pending.items()):
+            if not fut.done():
+                continue
+            del self.pending[key]
+            err = fut.exception()
+            if err is None:
+                ev = self.torch.cuda.Event()
+                ev.record(cs)  # after the build's factorisation on its stream
+                self.cache[key] = (fut.result(), factor_bytes(key[0], key[1]), (ev, cs))
+                self.shrink_cache(self.cache_budget)
+            for rid, r in list(self.waiting.items()):
+                if r.key != key:
+                    continue
+                del self.waiting[rid]
+                if err is not None:
+                    r.state = FAILED
+                    r.error = repr(err)
+                    self.failed.append(rid)
+                else:
+                    s = self.streams[r.slot % len(self.streams)]
+                    try:
+                        self._start(r, self._cached(r, s), s)
+                    except Exception as e:  # launch failure: report, keep serving
+                        r.state = FAILED
+                        r.error = repr(e)
+                        self.failed.append(rid)
+
     # -- execution ----------------------------------------------------------
     def launch(self, req):
-        torch = self.torch
         s = self.streams[req.slot % len(self.streams)]
-        p = self.problem(req, s)
+        if self.pool is None or req.key in self.cache:
+            self._start(req, self.problem(req, s), s)
+            return
+        if req.key in self.pending:
+            self.hits += 1  # built once for every request of the key
+        else:
+            self.misses += 1
+            fut = self.pool.submit(self.Problem, req.N, req.family, req.c, self.form, stream=s)
+            self.pending[req.key] = (fut, s)
+        self.waiting[req.id] = req
+
+    def _start(self, req, p, s):
+        torch = self.torch
         with torch.cuda.stream(s):
             f_host = req.f if isinstance(req.f, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(req.f))
             d_f = torch.empty(p.phys_shape, dtype=torch.float64, device="cuda")
@@ -261,7 +321,8 @@ class GpuExecutor:
         req.result = out
 
     def poll(self):
-        done = []
+        self._collect()
+        done, self.failed = list(self.failed), []
         for rid, (req, ev, bufs) in list(self.inflight.items()):
             if ev.query():
                 done.append(rid)
