@@ -8,14 +8,16 @@ of several CUDA streams so that work from different requests overlaps on the
 device, and completions are detected with CUDA events and retired while new
 requests keep arriving.  Factorised problems are cached on the device, keyed
 by (grid, family, c, form), with least-recently-used eviction under a byte
-budget.  Results do not depend on what else is in flight: every request runs
+budget; a problem whose key is new is built on a worker thread while the
+loop keeps launching other requests, and every request of that key starts
+once it is ready.  Results do not depend on what else is in flight: every request runs
 its own deterministic kernels on its own buffers (no atomics, no shared
 scratch), which tests/test_gpu_serving.py checks bit for bit.
 
 Failure handling is host-side: a request larger than the whole memory budget
 is rejected with an error, a cancelled request is dropped before launch (or
-its result discarded after), and a request that raises during launch is
-marked failed without stopping the loop.
+its result discarded after), and a request that raises during launch, or
+whose problem fails to build, is marked failed without stopping the loop.
 """
 import collections
 import time
