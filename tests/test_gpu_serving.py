@@ -110,3 +110,30 @@ def test_serving_shared_keys_across_streams(sg):
     for r in mix:
         assert r.state == SV.DONE, r.error
         assert torch.equal(a[r.id].result, r.result), r.id
+
+
+def test_background_build_failure_fails_only_its_requests(sg):
+    """A problem the library refuses to build (Dirichlet axis shorter than 8)
+    fails, on its worker thread, the two requests of its key; the others
+    finish and equal their runs alone."""
+    from shenfun_gb300 import serving as SV
+    good = [((24, 20, 32), "chebyshev", 10.0), ((40, 48), "legendre", 2.0)]
+    bad = ((16, 4), "chebyshev", 1.0)
+    stream = []
+    for i in range(8):
+        N, fam, c = bad if i in (2, 5) else good[i % 2]
+        stream.append((N, fam, c, 0.0, 300 + i))
+    ex = SV.GpuExecutor(nstreams=4)
+    fin, _ = SV.run_stream(stream, ex, max_slots=4)
+    torch.cuda.synchronize()
+    by = {r.id: r for r in fin}
+    assert len(by) == 8
+    for i in range(8):
+        if i in (2, 5):
+            assert by[i].state == SV.FAILED and "SgpuError" in by[i].error
+        else:
+            assert by[i].state == SV.DONE, by[i].error
+    alone, _ = SV.run_stream([stream[i] for i in (0, 1)], SV.GpuExecutor(nstreams=1, prep_workers=0),
+                             max_slots=1)
+    for r in alone:
+        assert torch.equal(r.result, by[r.id].result)
