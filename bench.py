@@ -220,10 +220,10 @@ class FormRun:
         self.T.backward(self.u_hat.v, self.uq.v)
 
     # our kernels per step: plain 7 (three axes each way + the solve); mixed
-    # 11 (each Chebyshev pass is three: row scale, digit split, contraction)
+    # 9 (each Chebyshev pass is two: line scales, fused contraction)
     @property
     def launches_per_step(self):
-        return 11 if self.form == "mixed" else 7
+        return 9 if self.form == "mixed" else 7
 
 
 def e2e_pipelined(torch, sg, run0, form, f_np, f_host, steps, st):

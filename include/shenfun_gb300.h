@@ -120,6 +120,20 @@ int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, int64_t inner
 int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
                          int64_t inner, int data_kind, double scale, void* work, size_t work_bytes,
                          cudaStream_t stream);
+/* Mixed-form Chebyshev plans with 16 <= n whose operator uses at most 339
+ * input entries (n <= 339; backward transforms n <= 341) run contiguous lines
+ * (inner = 1) through a fused kernel that splits the lines into digits on
+ * the fly; its scratch is 4 bytes per line (the line scales).  For n > 130
+ * it does not run
+ * in place: sgpu_plan_execute_ws returns SGPU_ERR_ARG for in == out there,
+ * and sgpu_plan_execute goes through a stream-ordered temporary output. */
+/* Tile width of that kernel: 1 = 64-line tiles with one TMEM accumulator set,
+ * 2 = 32-line tiles with two (the next tile's MMAs overlap this tile's
+ * epilogue); 0 = the library's default (1).  SGPU_ERR_UNSUPPORTED for plans
+ * that do not use the fused kernel.  get returns 0 for them.  No counterpart
+ * in the reference (a tuning knob of this library's kernels). */
+int sgpu_plan_set_variant(sgpu_plan* plan, int variant);
+int sgpu_plan_get_variant(const sgpu_plan* plan, int* variant);
 
 /* ---- padded (3/2-rule dealiased) Fourier transforms ---------------------
  * FourierBase._padding_backward / _truncation_forward (fourier/bases.py:409-435

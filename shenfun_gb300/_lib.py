@@ -46,6 +46,8 @@ SIGNATURES = {
     "sgpu_plan_execute": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp]),
     "sgpu_plan_workspace_size": (_int, [_vp, _i64, _i64, _int, ctypes.POINTER(ctypes.c_size_t)]),
     "sgpu_plan_execute_ws": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp, ctypes.c_size_t, _vp]),
+    "sgpu_plan_set_variant": (_int, [_vp, _int]),
+    "sgpu_plan_get_variant": (_int, [_vp, ctypes.POINTER(_int)]),
     "sgpu_fourier_pad": (_int, [_vp, _vp, _i64, _int, _int, _i64, _int, _vp]),
     "sgpu_fourier_truncate": (_int, [_vp, _vp, _i64, _int, _int, _i64, _int, _vp]),
     "sgpu_banded_LU": (_int, [_vp, _int, _vp, _i64, _vp]),

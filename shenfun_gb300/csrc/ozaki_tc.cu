@@ -18,6 +18,7 @@
 #include <thread>
 #include <vector>
 
+#include "lc_fused.h"
 #include "ozaki.cuh"
 #include "ozaki_tc.h"
 
@@ -392,6 +393,16 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
 
 extern "C" int sgpu_wait_timeouts(unsigned int* count) {
   if (!count) return SGPU_ERR_ARG;
-  return cudaMemcpyFromSymbol(count, g_oz_timeouts, sizeof(unsigned int)) == cudaSuccess ? SGPU_OK
-                                                                                           : SGPU_ERR_CUDA;
+  unsigned int a = 0, b = 0;
+  if (cudaMemcpyFromSymbol(&a, g_oz_timeouts, sizeof(unsigned int)) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_CUDA;
+  }
+  const int st = sgpu::lc::read_timeouts(&b);
+  if (st != SGPU_OK) {
+    cudaGetLastError();
+    return st;
+  }
+  *count = a + b;
+  return SGPU_OK;
 }

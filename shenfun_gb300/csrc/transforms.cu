@@ -13,6 +13,7 @@
 #include <new>
 #include <vector>
 
+#include "lc_fused.h"
 #include "ozaki_tc.h"
 #include "plan_host.cuh"
 #include "xf_kernels.cuh"
@@ -23,7 +24,9 @@ struct sgpu_plan {
   LinePlan lp;
   void* dev_tables;  // one allocation holding every device table
   bool tensor = false;
-  oz::Matrix tc;     // tensor form: the line operator, split
+  oz::Matrix tc;     // tensor form: the line operator, split (any line layout)
+  bool fused = false;
+  lc::Matrix fm;     // the same operator for the fused contraction (contiguous lines)
 };
 
 namespace {
@@ -107,6 +110,17 @@ extern "C" int sgpu_plan_create(sgpu_plan** out, int kind, int n, int basis, int
       delete plan;
       return st;
     }
+    // contiguous lines take the fused contraction where it applies (no
+    // scratch, one pass over the data)
+    if (lc::supported(n, plan->tc.K)) {
+      st = lc::matrix_create(M.data(), n, plan->tc.K, &plan->fm);
+      if (st != SGPU_OK) {
+        oz::matrix_destroy(&plan->tc);
+        delete plan;
+        return st;
+      }
+      plan->fused = true;
+    }
     std::memset(&plan->lp, 0, sizeof(plan->lp));
     plan->lp.kind = kind;
     plan->lp.basis = basis;
@@ -151,6 +165,7 @@ extern "C" int sgpu_plan_destroy(sgpu_plan* plan) {
   if (!plan) return SGPU_OK;
   if (plan->dev_tables) cudaFree(plan->dev_tables);
   oz::matrix_destroy(&plan->tc);
+  lc::matrix_destroy(&plan->fm);
   delete plan;
   return SGPU_OK;
 }
@@ -159,7 +174,26 @@ extern "C" int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, in
                                         size_t* bytes) {
   if (!plan || !bytes || outer < 0 || inner < 1) return SGPU_ERR_ARG;
   if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
-  *bytes = plan->tensor ? oz::workspace_bytes(plan->tc, outer * inner, inner, data_kind == SGPU_COMPLEX) : 0;
+  if (!plan->tensor)
+    *bytes = 0;
+  else if (plan->fused && inner == 1)
+    *bytes = lc::workspace_bytes(plan->fm, outer, data_kind == SGPU_COMPLEX);
+  else
+    *bytes = oz::workspace_bytes(plan->tc, outer * inner, inner, data_kind == SGPU_COMPLEX);
+  return SGPU_OK;
+}
+
+
+extern "C" int sgpu_plan_set_variant(sgpu_plan* plan, int variant) {
+  if (!plan || variant < 0 || variant > 2) return SGPU_ERR_ARG;
+  if (!plan->fused) return variant == 0 ? SGPU_OK : SGPU_ERR_UNSUPPORTED;
+  plan->fm.variant = variant == 0 ? 1 : variant;
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_plan_get_variant(const sgpu_plan* plan, int* variant) {
+  if (!plan || !variant) return SGPU_ERR_ARG;
+  *variant = plan->fused ? plan->fm.variant : 0;
   return SGPU_OK;
 }
 
@@ -168,9 +202,19 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
   if (!plan || !in || !out) return SGPU_ERR_ARG;
   if (outer < 0 || inner < 1) return SGPU_ERR_ARG;
   if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
-  if (plan->tensor)  // in place is fine: the contraction reads the split copy of the input
+  if (plan->tensor) {
+    // contiguous lines: the fused kernel.  Its CTAs for different 128-output
+    // parts of a line do not wait for one another, so it runs in place only
+    // when one CTA covers every output (n <= 130); the split-copy kernels
+    // (strided lines) run in place by construction
+    if (plan->fused && inner == 1) {
+      if (in == out && plan->fm.MT > 1) return SGPU_ERR_ARG;
+      return lc::contract(plan->fm, (const double*)in, (double*)out, outer, data_kind == SGPU_COMPLEX, work,
+                          work_bytes, nullptr, 0, stream);
+    }
     return oz::contract(plan->tc, (const double*)in, (double*)out, outer * inner, inner,
                         data_kind == SGPU_COMPLEX, work, work_bytes, stream);
+  }
   const LinePlan& p = plan->lp;
   if (in == out && p.n_in != p.n_out) return SGPU_ERR_ARG;
   const int64_t nlines = outer * inner;
@@ -206,12 +250,21 @@ extern "C" int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* ou
   size_t nb = 0;
   int st = sgpu_plan_workspace_size(plan, outer, inner, data_kind, &nb);
   if (st != SGPU_OK) return st;
+  // the fused kernel on more than 128 outputs runs in place through a
+  // temporary output appended to the scratch
+  const bool tmp_out = plan->fused && inner == 1 && in == out && plan->fm.MT > 1;
+  const size_t ob = tmp_out ? (size_t)outer * plan->lp.n_out * (data_kind == SGPU_COMPLEX ? 16 : 8) : 0;
+  const size_t nb_r = (nb + 255) & ~(size_t)255;
   void* work = nullptr;
-  if (cudaMallocAsync(&work, nb, stream) != cudaSuccess) {
+  if (cudaMallocAsync(&work, nb_r + ob, stream) != cudaSuccess) {
     cudaGetLastError();
     return SGPU_ERR_NOMEM;
   }
-  st = plan_run(plan, in, out, outer, inner, data_kind, scale, work, nb, stream);
+  void* dst = tmp_out ? (void*)((char*)work + nb_r) : out;
+  st = plan_run(plan, in, dst, outer, inner, data_kind, scale, work, nb, stream);
+  if (st == SGPU_OK && tmp_out && cudaMemcpyAsync(out, dst, ob, cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+    st = SGPU_ERR_CUDA;
   cudaFreeAsync(work, stream);
+  cudaGetLastError();
   return st;
 }

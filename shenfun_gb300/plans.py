@@ -41,12 +41,19 @@ class LinePlan:
         _lib.call("sgpu_plan_workspace_size", self._h, outer, inner, kind, ctypes.byref(nb))
         work = None
         if nb.value:
-            # tensor-core form: scratch for the split input from torch's
-            # caching allocator (512-byte aligned, reused across calls)
+            # tensor-core form on strided lines: scratch for the split input
+            # from torch's caching allocator (512-byte aligned, reused)
             work = torch.empty(nb.value, dtype=torch.uint8, device=inp.device)
-        _lib.call("sgpu_plan_execute_ws", self._h, ptr(inp), ptr(out), outer, inner, kind,
+        dst = out
+        if (self.form == _lib.MIXED_DF and inner == 1 and n_in > 130 and inp.data_ptr() == out.data_ptr()
+                and self.kind in (_lib.XF_CHEB_SCALAR, _lib.XF_CHEB_FORWARD, _lib.XF_CHEB_BACKWARD)):
+            # the fused tensor-core kernel does not run in place for n > 130
+            dst = torch.empty_like(out)
+        _lib.call("sgpu_plan_execute_ws", self._h, ptr(inp), ptr(dst), outer, inner, kind,
                   float(scale), work.data_ptr() if work is not None else None, nb.value,
                   stream_handle(stream))
+        if dst is not out:
+            out.copy_(dst)
         return out
 
 

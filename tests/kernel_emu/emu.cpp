@@ -16,6 +16,7 @@
 //   emu tdma|pdma n outer inner data_kind raw.bin u.bin out.bin (LU then solve)
 //   emu ozaki  N nlines inner cplx precise in.bin M.bin out.bin (split-BF16 contraction)
 //   emu ozakic N nlines inner cplx precise kchunk in.bin M.bin out.bin  (K blocks per launch)
+//   emu lcf    N nlines cplx bn in.bin M.bin out.bin   (fused contraction, 64- or 32-line tiles)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -27,6 +28,7 @@
 #include "../../shenfun_gb300/csrc/plan_host.cuh"
 #include "../../shenfun_gb300/csrc/solvers.cuh"
 #include "../../shenfun_gb300/csrc/ozaki.cuh"
+#include "../../shenfun_gb300/csrc/lc_fused.cuh"
 
 using namespace sgpu;
 
@@ -261,6 +263,161 @@ static int ozaki(int argc, char** argv) {
   return 0;
 }
 
+// Fused split-BF16 contraction (lc_fused.cu): per tile, pass 1 (scales and
+// FP64 dot-product outputs) over every cluster rank's share of rows, pass 2
+// into a NaN-poisoned, exactly-sized B stage at the kernel's offsets for
+// every K step, the MMAs of every rank modelled from their descriptors and
+// instruction descriptors (operand element (m, k) at start + (k/8) LBO +
+// (m/8) SBO + 16 (m%8) + 2 (k%8), FP32 accumulator rounded once per MMA), and
+// the integer epilogue.
+template <class C>
+static int lcf_run(const lc::Geom& g, const double* in, const double* M, double* out) {
+  using namespace lc;
+  const int S = C::S, BN = C::BN;
+  std::vector<uint16_t> tiles(matrix_tile_elems<C>(g));
+  std::vector<int> em((size_t)g.MT * MROWS);
+  std::vector<double> xcol((size_t)(g.NX > 0 ? g.NX : 1) * g.K);
+  split_matrix_host<C>(M, g, tiles.data(), em.data(), xcol.data());
+  std::vector<uint8_t> bst(C::B_STAGE), ast(C::A_STAGE);
+  std::vector<int> e(BN);
+  std::vector<double> xo((size_t)BN * MAX_NX);
+  std::vector<float> D((size_t)g.MT * MROWS * S * BN);
+  auto bf = [](const uint8_t* p) {
+    uint16_t h;
+    memcpy(&h, p, 2);
+    uint32_t u = (uint32_t)h << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+  };
+  auto field = [](uint64_t d, int sh) { return (uint32_t)(((d >> sh) & 0x3FFF) << 4); };
+  const int ksd = kstride(g);
+  for (int64_t T = 0; T < g.tiles; ++T) {
+    const int64_t row0 = T * BN;
+    int covered = 0;
+    for (int r = 0; r < g.MT; ++r) {
+      int lo, hi;
+      row_share(BN, g.MT, r, lo, hi);
+      covered += hi - lo;
+      for (int jj = lo; jj < hi; ++jj) {
+        const int64_t row = row0 + jj;
+        uint32_t mf = 0;
+        double acc[MAX_NX] = {0.0, 0.0};
+        if (row < g.nrows)
+          for (int k = 0; k < g.K; ++k) {
+            const double x = in[row_base(g, row) + (int64_t)k * ksd];
+            mf = exp_field(x) > mf ? exp_field(x) : mf;
+            for (int c = 0; c < g.NX; ++c) acc[c] += x * xcol[(size_t)c * g.K + k];
+          }
+        e[jj] = exp_from_field(mf);
+        for (int c = 0; c < MAX_NX; ++c) xo[(size_t)jj * MAX_NX + c] = acc[c];
+      }
+    }
+    if (covered != BN) return 7;
+    for (int ks = 0; ks < g.nsteps; ++ks) {
+      for (size_t i = 0; i < bst.size(); i += 2) {
+        bst[i] = 0xC0;
+        bst[i + 1] = 0x7F;  // BF16 NaN: unwritten shows
+      }
+      for (int r = 0; r < g.MT; ++r) {
+        int lo, hi;
+        row_share(BN, g.MT, r, lo, hi);
+        for (int h = 0; h < 2; ++h)
+          for (int jj = lo; jj < hi; ++jj) {
+            const int64_t row = row0 + jj;
+            double x[8];
+            const int k0 = ks * KSTEP + h * 8;
+            for (int q = 0; q < 8; ++q)
+              x[q] = row < g.nrows && k0 + q < g.K ? in[row_base(g, row) + (int64_t)(k0 + q) * ksd] : 0.0;
+            uint4 dg[C::S];
+            split8<C>(x, e[jj], dg);
+            for (int t = 0; t < S; ++t) {
+              const uint32_t off = b_offset<C>(t, jj, h);
+              if (off + 16 > bst.size() || (off & 15)) return 8;
+              memcpy(bst.data() + off, &dg[t], 16);
+            }
+          }
+      }
+      for (int r = 0; r < g.MT; ++r) {
+        memcpy(ast.data(), tiles.data() + (((size_t)r * g.nsteps + ks) * S) * A_BLOCK, C::A_STAGE);
+        float* Dr = D.data() + (size_t)r * MROWS * S * BN;
+        for (int s = 0; s < S; ++s) {
+          const int rows = (S - s) * BN;
+          for (int c0 = 0; c0 < rows; c0 += 256) {
+            const int n = rows - c0 < 256 ? rows - c0 : 256;
+            const uint32_t idesc = tc::idesc_bf16_f32(MROWS, n);
+            if ((int)((idesc >> 17) & 63) * 8 != n || (int)((idesc >> 24) & 31) * 16 != MROWS) return 5;
+            const uint64_t ad = tc::sdesc_interleave((uint32_t)(s * A_BLOCK * 2), LBO_A, SBO);
+            const uint64_t bd = tc::sdesc_interleave((uint32_t)(c0 * 16), C::LBO_B, SBO);
+            const uint32_t as = field(ad, 0), al = field(ad, 16), asb = field(ad, 32);
+            const uint32_t bs = field(bd, 0), bl = field(bd, 16), bsb = field(bd, 32);
+            const int dcol = s * BN + c0;
+            if (dcol + n > S * BN) return 9;
+            for (int m = 0; m < MROWS; ++m)
+              for (int col = 0; col < n; ++col) {
+                double sum = 0;
+                for (int k = 0; k < 16; ++k) {
+                  const uint32_t pa = as + (k >> 3) * al + (m >> 3) * asb + (m & 7) * 16 + (k & 7) * 2;
+                  const uint32_t pb = bs + (k >> 3) * bl + (col >> 3) * bsb + (col & 7) * 16 + (k & 7) * 2;
+                  if (pa + 2 > ast.size() || pb + 2 > bst.size()) return 6;
+                  sum += (double)bf(ast.data() + pa) * (double)bf(bst.data() + pb);
+                }
+                float& d = Dr[(size_t)m * S * BN + dcol + col];
+                d = (float)((ks > 0 || s > 0 ? (double)d : 0.0) + sum);
+              }
+          }
+        }
+      }
+    }
+    for (int r = 0; r < g.MT; ++r)
+      for (int m = 0; m < MROWS; ++m) {
+        const int n = r * MROWS + m;
+        if (n >= g.Nmma) continue;
+        for (int jj = 0; jj < BN; ++jj) {
+          const int64_t row = row0 + jj;
+          if (row >= g.nrows) continue;
+          uint32_t gb[C::S];
+          for (int gg = 0; gg < S; ++gg)
+            memcpy(&gb[gg], &D[((size_t)r * MROWS + m) * S * BN + gg * BN + jj], 4);
+          out[row_base(g, row) + (int64_t)n * ksd] = combine<C>(gb, e[jj], em[n]);
+        }
+      }
+    for (int jj = 0; jj < BN; ++jj) {
+      const int64_t row = row0 + jj;
+      if (row >= g.nrows) continue;
+      for (int c = 0; c < g.NX; ++c) out[row_base(g, row) + (int64_t)(g.Nmma + c) * ksd] = xo[(size_t)jj * MAX_NX + c];
+    }
+  }
+  return 0;
+}
+
+// emu lcf N nlines cplx bn in.bin M.bin out.bin
+static int lcf(int argc, char** argv) {
+  if (argc < 9) return 2;
+  const int N = atoi(argv[2]);
+  const long long nlines = atoll(argv[3]);
+  const int cplx = atoi(argv[4]), bn = atoi(argv[5]);
+  const size_t cnt = (size_t)nlines * N * (1 + cplx);
+  argv += 1;
+  double* in = read_exact(argv[5], cnt);
+  double* M = read_exact(argv[6], (size_t)N * N);
+  int K = 0;
+  for (int k = 0; k < N; ++k)
+    for (int n = 0; n < N; ++n)
+      if (M[(size_t)k * N + n] != 0.0) K = k + 1;
+  if (!lc::supported_nk(N, K)) return 3;
+  double* out = (double*)malloc(sizeof(double) * cnt);
+  for (size_t i = 0; i < cnt; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
+  const int rc = bn == 32 ? lcf_run<lc::CfgNarrow>(lc::make_geom<lc::CfgNarrow>(N, K, nlines, cplx), in, M, out)
+                          : lcf_run<lc::CfgWide>(lc::make_geom<lc::CfgWide>(N, K, nlines, cplx), in, M, out);
+  if (rc) return rc;
+  write_exact(argv[7], out, cnt);
+  free(in);
+  free(M);
+  free(out);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   std::string mode = argv[1];
@@ -271,6 +428,7 @@ int main(int argc, char** argv) {
   }
   if (mode == "xform") return xform(argc, argv);
   if (mode == "ozaki" || mode == "ozakic") return ozaki(argc, argv);
+  if (mode == "lcf") return lcf(argc, argv);
   if (mode == "lkcheck") {
     // lkcheck: every (line, index) pair of the loop decompositions is visited
     // exactly once for the thread counts the kernels launch with
