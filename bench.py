@@ -65,11 +65,31 @@ def peaks(key="hbm_gbs", fallback=6800.0):
 
 
 # the mixed form's Chebyshev-axis passes are split-BF16 contractions on the
-# tensor cores: 36 digit products (8 digits, s + t <= 7) of a lines x NZ by
-# NZ x NZ product, 2 flops per multiply-add
-TC_PRODUCTS = 36
+# tensor cores: 28 digit products (7 digits, s + t <= 6) of a lines x NZ by
+# NZ x NZ product, 2 flops per multiply-add (the tensor pipe's work; the
+# roofline of the pass is still HBM bytes)
+TC_PRODUCTS = 28
 TC_FLOPS = TC_PRODUCTS * 2.0 * NX * NY * NZ * NZ
 TC_STAGES = ("z_scalar_product", "z_backward")
+# DRAM traffic per stage from the committed ncu summaries: a line
+# "dram_bytes_per_pass: <bytes>" in the profile of the stage's kernels
+TRAFFIC_PROFILES = {
+    "mixed:z_scalar_product": "profiles/fused_contraction_256x256x257.md",
+}
+
+
+def profiled_traffic(key):
+    """Per-pass DRAM bytes (read + write) recorded in the stage's committed
+    ncu summary, or None when the stage has none."""
+    import re
+    path = TRAFFIC_PROFILES.get(key)
+    if not path:
+        return None
+    try:
+        m = re.search(r"dram_bytes_per_pass:\s*([0-9]+)", open(os.path.join(REPO, path)).read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
 
 
 class ClockSampler:
@@ -707,22 +727,25 @@ def main():
         results[name]["stage_ms"] = stage_times(torch, runs[name], flush, st)
     stage_ms = results[chosen]["stage_ms"]
     dom = max(stage_ms, key=stage_ms.get)
+    # the roofline of every stage is HBM: algorithmic bytes (read + write of
+    # the arrays, the factor cache for the solve) over the stage time against
+    # the measured copy bandwidth.  The tensor-core passes also report the
+    # tensor pipe's share (digit-product flops over the BF16 peak) separately.
+    peak, peak_kind = peaks()
+    achieved = STAGE_BYTES[dom] / (stage_ms[dom] / 1e3) / 1e9
+    roof = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": STAGE_BYTES[dom]}
+    tensor_util = None
     if chosen == "mixed" and dom in TC_STAGES:
-        # tensor-bound: algorithmic BF16 flops of the contraction over the
-        # stage time (which also holds the split kernels: a lower bound)
-        peak, peak_kind = peaks("bf16_tflops", 1900.0)
-        achieved = TC_FLOPS / (stage_ms[dom] / 1e3) / 1e12
-        roof = {"bound": "tensor", "unit": "TFLOP/s", "algorithmic_flops": TC_FLOPS,
-                "note": "stage time includes the row-scale and digit-split kernels"}
-    else:
-        peak, peak_kind = peaks()
-        achieved = STAGE_BYTES[dom] / (stage_ms[dom] / 1e3) / 1e9
-        roof = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": STAGE_BYTES[dom]}
-    # DRAM bytes of the dominant stage's kernels, one ncu capture each
-    # (dram__bytes_read.sum + dram__bytes_write.sum per launch, full-size z
-    # pass; profiles/tensor_contraction_256x256x257.md): k_oz_rowexp 134.9 MB,
-    # k_oz_split<8> 377.7 MB, k_oz_gemm 539.0 MB
-    traffic = {"mixed:z_scalar_product": 1051.6e6, "mixed:z_backward": 1051.6e6}.get(f"{chosen}:{dom}")
+        tpeak, tpeak_kind = peaks("bf16_tflops", 1900.0)
+        tach = TC_FLOPS / (stage_ms[dom] / 1e3) / 1e12
+        tensor_util = {"achieved_tflops": tach, "peak_tflops": tpeak, "frac": tach / tpeak,
+                       "peak_source": tpeak_kind, "flops": TC_FLOPS,
+                       "note": "28 BF16 digit products per FP64 multiply-add; stage time includes the "
+                               "line-scale kernel"}
+    traffic = profiled_traffic(f"{chosen}:{dom}")
+    if traffic is None and chosen == "mixed" and dom == "z_backward":
+        traffic = profiled_traffic("mixed:z_scalar_product")  # the same kernels, one K step fewer
+    stage_frac = {k: STAGE_BYTES[k] / (v / 1e3) / 1e9 / peak for k, v in stage_ms.items()}
 
     # end to end through the public API with host buffers (pinned), per step:
     # H2D of the RHS, round trip, D2H of the solution
@@ -782,7 +805,8 @@ def main():
             "chosen_over_plain": results["mixed"]["value"] / results["plain"]["value"],
             "roofline": dict(roof, kernel=f"{chosen}:{dom}", achieved=achieved, peak=peak,
                              frac=achieved / peak, traffic=traffic, peak_source=peak_kind,
-                             traffic_unit="bytes per stage (ncu)" if traffic else None),
+                             traffic_unit="bytes per stage (ncu, committed profile)" if traffic else None,
+                             tensor_util=tensor_util, stage_hbm_frac=stage_frac),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "solves/s",
                     "h2d_bytes_per_step": R_BYTES, "d2h_bytes_per_step": R_BYTES,

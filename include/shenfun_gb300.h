@@ -346,6 +346,17 @@ int sgpu_legendre_execute_ws(const sgpu_legendre_plan* plan, int direction, cons
 /* number of bounded device-side waits of the tensor-core kernels that gave up
  * since load (0 unless a pipeline stalled; such a launch's output is invalid) */
 int sgpu_wait_timeouts(unsigned int* count);
+/* Synchronise `stream` and report whether any tensor-core launch since the
+ * previous call gave up a bounded wait: SGPU_ERR_TIMEOUT (its outputs are
+ * invalid), SGPU_OK, or SGPU_ERR_CUDA when the synchronisation itself
+ * failed.  The kernels never trap: a pipeline that stalls past its limit
+ * records the event, drains the work it issued and returns.  No counterpart
+ * in the reference (its kernels are synchronous CPU code). */
+int sgpu_last_error(cudaStream_t stream);
+/* Limit of each pipeline wait of the fused tensor-core contraction, in
+ * nanoseconds (0: the default, one second).  For tests that make a wait run
+ * out; process-wide. */
+int sgpu_set_wait_limit_ns(unsigned long long ns);
 
 #ifdef __cplusplus
 }

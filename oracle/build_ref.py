@@ -73,7 +73,9 @@ def compile_cpp(src_root, name):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default=os.environ.get("REFERENCE_ROOT", "/root/reference"))
+    ap.add_argument("--src", default=os.environ.get("REFERENCE_ROOT") or os.path.normpath(os.path.join(
+        os.path.dirname(os.path.dirname(OUT)), os.pardir, "reference")),
+        help="reference checkout (default: REFERENCE_ROOT, else a 'reference' checkout beside the repository)")
     ap.add_argument("--from-cpp", action="store_true",
                     help="skip Cython; compile existing oracle/_ref/*.cpp")
     ap.add_argument("--only", nargs="*", default=None)

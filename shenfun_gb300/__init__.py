@@ -13,7 +13,7 @@ The Python API mirrors shenfun's for this path::
     u = u_hat.backward()
 """
 from . import _lib  # noqa: F401
-from ._lib import SgpuError  # noqa: F401
+from ._lib import SgpuError, check_device  # noqa: F401
 from .spaces import FunctionSpace, TensorProductSpace, R2C, C2C  # noqa: F401
 from .forms import (Array, Function, TestFunction, TrialFunction, inner, project,  # noqa: F401
                     div, grad, Dx, TPMatrix)

@@ -47,6 +47,8 @@ SIGNATURES = {
     "sgpu_plan_workspace_size": (_int, [_vp, _i64, _i64, _int, ctypes.POINTER(ctypes.c_size_t)]),
     "sgpu_plan_execute_ws": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp, ctypes.c_size_t, _vp]),
     "sgpu_plan_set_variant": (_int, [_vp, _int]),
+    "sgpu_last_error": (_int, [_vp]),
+    "sgpu_set_wait_limit_ns": (_int, [ctypes.c_ulonglong]),
     "sgpu_plan_get_variant": (_int, [_vp, ctypes.POINTER(_int)]),
     "sgpu_fourier_pad": (_int, [_vp, _vp, _i64, _int, _int, _i64, _int, _vp]),
     "sgpu_fourier_truncate": (_int, [_vp, _vp, _i64, _int, _int, _i64, _int, _vp]),
@@ -117,3 +119,11 @@ def call(name, *args):
     if st != OK:
         raise SgpuError(st, name)
     return st
+
+
+def check_device(stream=None):
+    """Synchronise `stream` (a torch stream or None for the current one) and
+    raise SgpuError(ERR_TIMEOUT) when a tensor-core launch since the last
+    check gave up a bounded wait (its outputs are invalid)."""
+    from .device import stream_handle
+    call("sgpu_last_error", stream_handle(stream))

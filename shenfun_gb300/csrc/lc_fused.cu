@@ -30,6 +30,7 @@
 // error word, the roles leave their loops at uniform points, and the copies
 // and MMAs in flight are waited for before the CTA exits.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <new>
@@ -521,6 +522,10 @@ void matrix_destroy(Matrix* m) {
   if (m) m->tiles = nullptr;
 }
 
+// pipeline-wait limit of the fused kernel (0: one second); a test sets a
+// short one to make the waits run out
+std::atomic<unsigned long long> g_wait_limit_ns{0};
+
 int read_timeouts(unsigned int* count) {
   return cudaMemcpyFromSymbol(count, g_lc_timeouts, sizeof(unsigned int)) == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
@@ -536,6 +541,7 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
   if (nlines == 0) return SGPU_OK;
   if (!m.tiles || !in || !out || nlines < 0) return SGPU_ERR_ARG;
   if ((((uintptr_t)in) & 7) || (((uintptr_t)out) & 7)) return SGPU_ERR_ARG;
+  if (wait_ns == 0) wait_ns = g_wait_limit_ns.load(std::memory_order_relaxed);
   if (wait_ns == 0) wait_ns = 1000000000ull;
   return m.variant == 2 ? launch<CfgNarrow>(m, in, out, nlines, cplx, work, work_bytes, err, wait_ns, stream)
                         : launch<CfgWide>(m, in, out, nlines, cplx, work, work_bytes, err, wait_ns, stream);
@@ -543,3 +549,8 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
 
 }  // namespace lc
 }  // namespace sgpu
+
+extern "C" int sgpu_set_wait_limit_ns(unsigned long long ns) {
+  sgpu::lc::g_wait_limit_ns.store(ns, std::memory_order_relaxed);
+  return SGPU_OK;
+}

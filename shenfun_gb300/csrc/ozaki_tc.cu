@@ -13,7 +13,9 @@
 // The split matrix operand (B) is built once on the host with the same digit
 // code and uploaded with the plan.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
+#include <mutex>
 #include <new>
 #include <thread>
 #include <vector>
@@ -342,30 +344,45 @@ size_t workspace_bytes(const Matrix& m, int64_t nlines, int64_t inner, int cplx)
   return a_split_bytes(g, m.S);
 }
 
+// per-device launch state: the large dynamic shared memory attributes (set
+// once per device and configuration) and the SM count
+struct OzDevState {
+  std::once_flag attr[2];
+  int attr_rc[2] = {0, 0};
+  std::once_flag sm_once;
+  int nsm = 0;
+};
+static OzDevState g_oz_dev[64];
+
 template <class C>
 static int run(const Matrix& m, const Geom& g, const double* in, double* out, void* work, cudaStream_t stream) {
-  static bool attr_set = false;  // benign race: every caller sets the same value
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(k_oz_gemm<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)GemmSmem<C>::bytes) != cudaSuccess ||
-        cudaFuncSetAttribute(k_oz_split<C::S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             C::S * A_BYTES) != cudaSuccess) {
-      cudaGetLastError();
-      return SGPU_ERR_CUDA;
-    }
-    attr_set = true;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return SGPU_ERR_CUDA;
   }
+  OzDevState& ds = g_oz_dev[dev];
+  const int ci = m.precise ? 1 : 0;
+  std::call_once(ds.attr[ci], [&]() {
+    ds.attr_rc[ci] = (cudaFuncSetAttribute(k_oz_gemm<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)GemmSmem<C>::bytes) == cudaSuccess &&
+                      cudaFuncSetAttribute(k_oz_split<C::S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           C::S * A_BYTES) == cudaSuccess)
+                         ? 1
+                         : -1;
+    cudaGetLastError();
+  });
+  if (ds.attr_rc[ci] != 1) return SGPU_ERR_CUDA;
+  std::call_once(ds.sm_once, [&]() {
+    if (cudaDeviceGetAttribute(&ds.nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || ds.nsm <= 0) ds.nsm = 1;
+    cudaGetLastError();
+  });
+  const int nsm = ds.nsm;
   uint16_t* At = (uint16_t*)work;
   int* eA = (int*)((char*)work + (size_t)C::S * g.mtiles * g.nkb * A_BYTES);
   const int64_t nrow_pad = (int64_t)g.mtiles * BM;
   k_oz_rowexp<<<(unsigned)((nrow_pad * 32 + 255) / 256), 256, 0, stream>>>(in, eA, g);
   k_oz_split<C::S><<<(unsigned)((int64_t)g.mtiles * g.nkb), 256, C::S * A_BYTES, stream>>>(in, eA, At, g);
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      nsm = 148;
-  }
   const int64_t ntile = (int64_t)g.mtiles * g.ntiles;
   const unsigned nctas = (unsigned)(ntile < nsm ? ntile : nsm);
   // one launch per K chunk of at most 1024 (stream-ordered: a chunk adds to
@@ -405,4 +422,19 @@ extern "C" int sgpu_wait_timeouts(unsigned int* count) {
   }
   *count = a + b;
   return SGPU_OK;
+}
+
+// the timeout counters as last seen by sgpu_last_error (process-wide)
+static std::atomic<unsigned int> g_seen_timeouts{0};
+
+extern "C" int sgpu_last_error(cudaStream_t stream) {
+  if (cudaStreamSynchronize(stream) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_CUDA;
+  }
+  unsigned int now = 0;
+  const int st = sgpu_wait_timeouts(&now);
+  if (st != SGPU_OK) return st;
+  const unsigned int seen = g_seen_timeouts.exchange(now);
+  return now != seen ? SGPU_ERR_TIMEOUT : SGPU_OK;
 }

@@ -81,6 +81,7 @@ struct sgpu_helmholtz_problem {
   bool shared_plans = false;       // plans come from the process-wide cache
   bool stream_ordered = false;     // device memory from cudaMallocAsync
   cudaStream_t stream = 0;         // creation stream (stream-ordered problems)
+  int device = -1;                 // the device the problem's memory and plans live on
 };
 
 namespace {
@@ -222,8 +223,14 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
   for (int i = 0; i < ndim; ++i)
     if (N[i] < 2 || N[i] > (1 << 16)) return SGPU_ERR_ARG;
   if (N[ndim - 1] < 8) return SGPU_ERR_ARG;
+  int device = -1;
+  if (cudaGetDevice(&device) != cudaSuccess) {
+    cudaGetLastError();
+    return SGPU_ERR_CUDA;
+  }
   sgpu_helmholtz_problem* p = new (std::nothrow) sgpu_helmholtz_problem;
   if (!p) return SGPU_ERR_NOMEM;
+  p->device = device;
   p->ndim = ndim;
   p->family = family;
   p->form = form;
@@ -240,24 +247,27 @@ int create_impl(sgpu_helmholtz_problem** out, int ndim, const int64_t* N, int fa
   // every plan uses the requested arithmetic (mixed: double-float Fourier
   // transforms, tensor-core contractions along the Dirichlet axis)
   int st = SGPU_OK;
+  auto chk = [&](int r) {  // the first failure's status
+    if (st == SGPU_OK) st = r;
+  };
   if (ndim == 3) {
-    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fx_f, SGPU_XF_C2C_FWD, (int)N[0], 0, form);
-    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fx_b, SGPU_XF_C2C_BWD, (int)N[0], 0, form);
+    chk((ordered ? cached_plan : sgpu_plan_create)(&p->fx_f, SGPU_XF_C2C_FWD, (int)N[0], 0, form));
+    chk((ordered ? cached_plan : sgpu_plan_create)(&p->fx_b, SGPU_XF_C2C_BWD, (int)N[0], 0, form));
   }
-  st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fr_f, SGPU_XF_R2C, (int)nr, 0, form);
-  st |= (ordered ? cached_plan : sgpu_plan_create)(&p->fr_b, SGPU_XF_C2R, (int)nr, 0, form);
+  chk((ordered ? cached_plan : sgpu_plan_create)(&p->fr_f, SGPU_XF_R2C, (int)nr, 0, form));
+  chk((ordered ? cached_plan : sgpu_plan_create)(&p->fr_b, SGPU_XF_C2R, (int)nr, 0, form));
   if (family == SGPU_FAMILY_CHEBYSHEV) {
-    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->d_s, SGPU_XF_CHEB_SCALAR, (int)Nd, SGPU_BASIS_SD, form);
-    st |= (ordered ? cached_plan : sgpu_plan_create)(&p->d_b, SGPU_XF_CHEB_BACKWARD, (int)Nd, SGPU_BASIS_SD, form);
+    chk((ordered ? cached_plan : sgpu_plan_create)(&p->d_s, SGPU_XF_CHEB_SCALAR, (int)Nd, SGPU_BASIS_SD, form));
+    chk((ordered ? cached_plan : sgpu_plan_create)(&p->d_b, SGPU_XF_CHEB_BACKWARD, (int)Nd, SGPU_BASIS_SD, form));
   } else {
     // the mixed form contracts on the tensor cores where the plan supports N
     int lform = form;
     if (lform == SGPU_MIXED_DF && sgpu::oz::pick_digits((int)Nd) != SGPU_OK) lform = SGPU_PLAIN_F64;
-    st |= (ordered ? cached_leg_plan : sgpu_legendre_plan_create)(&p->leg, (int)Nd, SGPU_BASIS_SD, lform);
+    chk((ordered ? cached_leg_plan : sgpu_legendre_plan_create)(&p->leg, (int)Nd, SGPU_BASIS_SD, lform));
   }
   if (st != SGPU_OK) {
     destroy_all(p);
-    return SGPU_ERR_UNSUPPORTED;
+    return st;
   }
   const int64_t n = Nd - 2;
   const int64_t m = (n + 1) / 2;
@@ -350,43 +360,58 @@ static int helmholtz_run(const sgpu_helmholtz_problem* p, const double* f, doubl
   double* wc = (double*)((unsigned char*)work + round256((size_t)p->nphys * 8));
   void* wt = (unsigned char*)wc + round256((size_t)p->nspec * 16);
   const size_t wtb = split_bytes(p);
+  // the first failing call's status is the step's status
   int st = SGPU_OK;
+  auto chk = [&](int r) {
+    if (st == SGPU_OK) st = r;
+  };
   // 1. scalar product along the Dirichlet axis (real data)
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    st |= sgpu_plan_execute_ws(p->d_s, f, wr, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s);
+    chk(sgpu_plan_execute_ws(p->d_s, f, wr, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s));
   else
-    st |= sgpu_legendre_execute_ws(p->leg, 0, f, wr, nlines_d, 1, SGPU_REAL, wt, wtb, s);
+    chk(sgpu_legendre_execute_ws(p->leg, 0, f, wr, nlines_d, 1, SGPU_REAL, wt, wtb, s));
   if (p->ndim == 2) {
     const int64_t N0 = p->N[0];
-    st |= sgpu_plan_execute(p->fr_f, wr, wc, 1, Nd, SGPU_REAL, 1.0 / N0, s);
+    chk(sgpu_plan_execute(p->fr_f, wr, wc, 1, Nd, SGPU_REAL, 1.0 / N0, s));
   } else {
     const int64_t N0 = p->N[0], N1 = p->N[1], Nh = N1 / 2 + 1;
-    st |= sgpu_plan_execute(p->fr_f, wr, wc, N0, Nd, SGPU_REAL, 1.0 / N1, s);
-    st |= sgpu_plan_execute(p->fx_f, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0 / N0, s);
+    chk(sgpu_plan_execute(p->fr_f, wr, wc, N0, Nd, SGPU_REAL, 1.0 / N1, s));
+    chk(sgpu_plan_execute(p->fx_f, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0 / N0, s));
   }
   // 2. one banded system per wavenumber, in place on the spectral array
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    st |= sgpu_helmholtz_solve_cached(wc, wc, p->fac, 0, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s);
+    chk(sgpu_helmholtz_solve_cached(wc, wc, p->fac, 0, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s));
   else
-    st |= sgpu_band_sep_solve(wc, wc, p->fac, nullptr, (int)(Nd - 2), p->nsys, Nd, 1, SGPU_COMPLEX, s);
+    chk(sgpu_band_sep_solve(wc, wc, p->fac, nullptr, (int)(Nd - 2), p->nsys, Nd, 1, SGPU_COMPLEX, s));
   // 3. backward
   if (p->ndim == 2) {
-    st |= sgpu_plan_execute(p->fr_b, wc, wr, 1, Nd, SGPU_COMPLEX, 1.0, s);
+    chk(sgpu_plan_execute(p->fr_b, wc, wr, 1, Nd, SGPU_COMPLEX, 1.0, s));
   } else {
     const int64_t N0 = p->N[0], N1 = p->N[1], Nh = N1 / 2 + 1;
-    st |= sgpu_plan_execute(p->fx_b, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0, s);
-    st |= sgpu_plan_execute(p->fr_b, wc, wr, N0, Nd, SGPU_COMPLEX, 1.0, s);
+    chk(sgpu_plan_execute(p->fx_b, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0, s));
+    chk(sgpu_plan_execute(p->fr_b, wc, wr, N0, Nd, SGPU_COMPLEX, 1.0, s));
   }
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    st |= sgpu_plan_execute_ws(p->d_b, wr, u, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s);
+    chk(sgpu_plan_execute_ws(p->d_b, wr, u, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s));
   else
-    st |= sgpu_legendre_execute_ws(p->leg, 2, wr, u, nlines_d, 1, SGPU_REAL, wt, wtb, s);
-  return st == SGPU_OK ? SGPU_OK : SGPU_ERR_CUDA;
+    chk(sgpu_legendre_execute_ws(p->leg, 2, wr, u, nlines_d, 1, SGPU_REAL, wt, wtb, s));
+  return st;
+}
+
+// the current device must be the one the problem was created on
+static bool on_own_device(const sgpu_helmholtz_problem* p) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return dev == p->device;
 }
 
 extern "C" int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* p, const double* f, double* u,
                                     void* work, size_t work_bytes, cudaStream_t stream) {
   if (!p || !f || !u || !work) return SGPU_ERR_ARG;
+  if (!on_own_device(p)) return SGPU_ERR_ARG;
   size_t need = 0;
   sgpu_helmholtz_workspace_size(p, &need);
   if (work_bytes < need) return SGPU_ERR_ARG;
@@ -407,17 +432,24 @@ extern "C" int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* p, const doubl
 //
 // The array below is a fixed 64 MiB of device memory.  Every GPU that loads
 // the library holds it until the process exits, whether or not this entry
-// point is used.  Problems whose scratch (one real physical array plus one
-// complex spectral array, sgpu_helmholtz_workspace_size) exceeds 64 MiB are
-// rejected with SGPU_ERR_SCRATCH_LIMIT; e.g. 128 x 128 x 129 (34 MB) fits,
-// 256 x 256 x 65 (68 MB) does not.
+// point is used.  Problems whose scratch (sgpu_helmholtz_workspace_size: one
+// real physical array, one complex spectral array, and for the mixed form
+// the contraction's scratch along the Dirichlet axis) exceeds 64 MiB are
+// rejected with SGPU_ERR_SCRATCH_LIMIT.  The Chebyshev mixed form needs 4
+// bytes more per line than the plain form, so 128 x 128 x 129 fits both
+// (34 MB); the Legendre mixed form adds a digit copy of the physical array
+// (about 14 bytes per point), so compare sgpu_helmholtz_workspace_size with
+// 64 MiB for it; 256 x 256 x 65 (68 MB) fits neither.
 //
-// The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and remembers it; make that
-// first call before any stream capture.  All calls share the one array and it
-// keeps whatever the last call left in it; every call writes each scratch
-// element it reads before reading it, so nothing has to be cleared between
-// calls.  Calls whose execution overlaps on the GPU (different streams, or
+// The first call on a device (and after cudaDeviceReset, which replaces the
+// device's context and with it the array's address) looks up the array's
+// device address with cudaGetSymbolAddress, with that device current, and
+// remembers it per (device, context); make that first call before any
+// stream capture.  The problem must be used on the device it was created on
+// (SGPU_ERR_ARG otherwise).  All calls share the one array and it keeps
+// whatever the last call left in it; every call writes each scratch element
+// it reads before reading it, so nothing has to be cleared between calls.
+// Calls whose execution overlaps on the GPU (different streams, or
 // different host threads without ordering) race on the array and give wrong
 // results: serialise them.  Host code never passes the array's name to a
 // kernel (in host code it is a host-side stand-in, not a device address):
@@ -429,8 +461,34 @@ extern "C" int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* p, const doubl
 
 static __device__ __align__(256) unsigned char g_sgpu_noalloc_scratch[SGPU_NOALLOC_SCRATCH_BYTES];
 
-static std::mutex g_noalloc_mutex;
-static void* g_noalloc_addr[SGPU_NOALLOC_MAX_DEVICES] = {};
+namespace {
+struct NoallocEntry {
+  int dev = -1;
+  void* ctx = nullptr;
+  void* addr = nullptr;
+};
+std::mutex g_noalloc_mutex;
+NoallocEntry g_noalloc[SGPU_NOALLOC_MAX_DEVICES];
+
+// the current context of the calling thread (the runtime's primary context
+// of the current device), through the driver's cuCtxGetCurrent
+void* current_context() {
+  typedef int (*GetCurrent)(void**);
+  static GetCurrent fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, []() {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (GetCurrent)f;
+    cudaGetLastError();
+  });
+  void* ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
+}  // namespace
 
 extern "C" int sgpu_helmholtz_solve_noalloc(const sgpu_helmholtz_problem* p, const double* f,
                                             double* u, cudaStream_t stream) {
@@ -443,19 +501,24 @@ extern "C" int sgpu_helmholtz_solve_noalloc(const sgpu_helmholtz_problem* p, con
     cudaGetLastError();
     return SGPU_ERR_CUDA;
   }
+  if (dev != p->device) return SGPU_ERR_ARG;
   if (dev < 0 || dev >= SGPU_NOALLOC_MAX_DEVICES) return SGPU_ERR_UNSUPPORTED;
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[dev]) {
+    NoallocEntry& e = g_noalloc[dev];
+    void* ctx = current_context();
+    if (!e.addr || e.ctx != ctx) {
       void* addr = nullptr;
       if (cudaGetSymbolAddress(&addr, g_sgpu_noalloc_scratch) != cudaSuccess || !addr) {
         cudaGetLastError();
         return SGPU_ERR_CUDA;
       }
-      g_noalloc_addr[dev] = addr;
+      e.dev = dev;
+      e.ctx = ctx;
+      e.addr = addr;
     }
-    base = g_noalloc_addr[dev];
+    base = e.addr;
   }
   return helmholtz_run(p, f, u, base, stream);
 }

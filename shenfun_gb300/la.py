@@ -27,7 +27,10 @@ def _band_data(mat, offsets):
     for r, off in enumerate(offsets):
         d = mat.get(off, 0.0)
         d = np.broadcast_to(np.atleast_1d(np.asarray(d, dtype=float)), (n - abs(off),))
-        s = mat.scale if np.isscalar(mat.scale) else 1.0
+        if not np.isscalar(mat.scale) and np.asarray(mat.scale).size != 1:
+            # per-row scales belong to a TPMatrix's solver, not to one band
+            raise _lib.SgpuError(_lib.ERR_ARG, "banded solver: the matrix scale must be a scalar")
+        s = float(np.asarray(mat.scale).reshape(-1)[0]) if not np.isscalar(mat.scale) else mat.scale
         if off >= 0:
             data[r, off:] = d * s
         else:

@@ -5,7 +5,8 @@ the GPU machine).  Puts the single-process shims of ``refshim/`` on sys.path,
 maps ``shenfun.optimization.cython.*`` and ``shenfun.legendre.fastgl.fastgl_wrap``
 onto the reference's own Cython kernels compiled by ``oracle/build_ref.py`` into
 ``oracle/_ref/``, and imports shenfun from the reference checkout
-(``REFERENCE_ROOT``, default ``/root/reference``).
+(``REFERENCE_ROOT``, else a checkout named ``reference`` beside this
+repository).
 """
 import importlib.abc
 import importlib.machinery
@@ -16,7 +17,7 @@ import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("REFERENCE_ROOT") or os.path.normpath(os.path.join(REPO, os.pardir, "reference"))
 REF_BUILD = os.path.join(REPO, "oracle", "_ref")
 
 _MAP = {
