@@ -74,6 +74,8 @@ extern "C" {
 
 /* arithmetic form */
 #define SGPU_PLAIN_F64 0   /* all FP64                                        */
+#define SGPU_FP32_REFINED 2 /* banded solves only: FP32 factor cache and sweeps,
+                              FP64-level residual, iterative refinement */
 #define SGPU_MIXED_DF 1    /* the mixed form, FP64 in and out: double-float (FP32
                               pair, ~48-bit) arithmetic on the FP32 pipes for
                               the Fourier line transforms and for Chebyshev
@@ -238,12 +240,29 @@ int sgpu_Poisson_Solve_ANN(const void* b, void* u, double scale, double u0, int6
  * pairs.  The LU is computed in FP64 in the reference's order either way. */
 int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int neumann,
                           int64_t outer, int64_t inner, int form, void* fac, cudaStream_t stream);
+/* form SGPU_FP32_REFINED (Dirichlet only) stores the cache as FP32: 4 bytes
+ * per entry, the LU computed in FP64 and rounded once. */
 /* Solve_Helmholtz (la.pyx:845-947) from the cache: b, u in the (outer, N,
  * inner) layout; one thread per (system, parity); b may alias u.  neumann
  * must match the factorisation. */
 int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int neumann,
                                 int64_t outer, int64_t N, int64_t inner, int data_kind, int form,
                                 cudaStream_t stream);
+
+/* FP32 solve with iterative refinement (the chosen form of the benchmark spec's
+ * banded solves; no reference counterpart as a call: it returns the same
+ * solution as Solve_Helmholtz, la.pyx:845-947, to FP64 accuracy).  One
+ * thread per (system, parity) chain: u = A32^-1 b; repeat r = b - A u,
+ * d = A32^-1 r, u += d until max|d| <= tol max|u| or max_it corrections.
+ * fac32 from sgpu_helmholtz_factor(form = SGPU_FP32_REFINED); A = alfa ASDSD
+ * + beta BSDSD with the factorisation's scales; r is scratch of b's size;
+ * b, u, r distinct.  residual_form SGPU_PLAIN_F64 computes the residual in
+ * FP64, SGPU_MIXED_DF in double-float on the FP32 pipes.  iters (device, 2
+ * outer inner ints, may be NULL) receives each chain's correction count,
+ * chain 2 s + parity.  The two tail entries of u are not written. */
+int sgpu_helmholtz_solve_refined(const void* b, void* u, void* r, const void* fac32, const double* alfa,
+                                 const double* beta, int64_t outer, int64_t N, int64_t inner, int data_kind,
+                                 double tol, int max_it, int residual_form, int* iters, cudaStream_t stream);
 
 /* ---- per-wavenumber systems: banded + rank-2 upper semiseparable ----------
  * M_s = sum_t coef[t][s] M_t, offsets -4..4 (even) plus, for term gen_term,
@@ -262,6 +281,16 @@ int sgpu_band_sep_factor(int n, int nterms, int gen_term, const double* bands,
 int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double* gens, int n,
                         int64_t outer, int64_t Nb, int64_t inner, int data_kind,
                         cudaStream_t stream);
+/* The same systems with an FP32 factor cache (half the bytes; LU in FP64,
+ * rounded once) and FP32 sweeps refined by an FP64 residual (the matvec
+ * below), as sgpu_helmholtz_solve_refined: fac 7 * ((n+1)/2) * 2 * nsys
+ * floats; b, u, r distinct, r scratch of b's size; iters as there. */
+int sgpu_band_sep_factor32(int n, int nterms, int gen_term, const double* bands, const double* gens,
+                           const double* coef, int64_t nsys, float* fac, cudaStream_t stream);
+int sgpu_band_sep_solve_refined(const void* b, void* u, void* r, const float* fac32, int n, int nterms,
+                                int gen_term, const double* bands, const double* gens, const double* coef,
+                                int64_t outer, int64_t Nb, int64_t inner, int data_kind, double tol, int max_it,
+                                int* iters, cudaStream_t stream);
 /* Matvec.pyx:908 Biharmonic_matvec (and the product of every other system
  * above): c = (sum_t coef[t][s] M_t) v per system, with the same description
  * as sgpu_band_sep_factor; v, c in the (outer, Nb, inner) layout, entries

@@ -18,7 +18,7 @@ BASIS_ORTHO, BASIS_SD, BASIS_SB, BASIS_SN = 0, 1, 2, 3
 BASIS_BC = 0x10  # flag: non-homogeneous boundary values
 XF_R2C, XF_C2R, XF_C2C_FWD, XF_C2C_BWD, XF_DCT2, XF_DCT3, XF_CHEB_SCALAR, XF_CHEB_FORWARD, \
     XF_CHEB_BACKWARD = range(1, 10)
-PLAIN_F64, MIXED_DF = 0, 1
+PLAIN_F64, MIXED_DF, FP32_REFINED = 0, 1, 2
 FORMS = {"plain": PLAIN_F64, "mixed": MIXED_DF, PLAIN_F64: PLAIN_F64, MIXED_DF: MIXED_DF}
 
 
@@ -48,6 +48,11 @@ SIGNATURES = {
     "sgpu_plan_execute_ws": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp, ctypes.c_size_t, _vp]),
     "sgpu_plan_set_variant": (_int, [_vp, _int]),
     "sgpu_last_error": (_int, [_vp]),
+    "sgpu_helmholtz_solve_refined": (_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _dbl, _int, _int,
+                                            _vp, _vp]),
+    "sgpu_band_sep_factor32": (_int, [_int, _int, _int, _vp, _vp, _vp, _i64, _vp, _vp]),
+    "sgpu_band_sep_solve_refined": (_int, [_vp, _vp, _vp, _vp, _int, _int, _int, _vp, _vp, _vp, _i64, _i64, _i64,
+                                           _int, _dbl, _int, _vp, _vp]),
     "sgpu_set_wait_limit_ns": (_int, [ctypes.c_ulonglong]),
     "sgpu_plan_get_variant": (_int, [_vp, ctypes.POINTER(_int)]),
     "sgpu_fourier_pad": (_int, [_vp, _vp, _i64, _int, _int, _i64, _int, _vp]),

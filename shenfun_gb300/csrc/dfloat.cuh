@@ -178,6 +178,31 @@ SGPU_HD df from_f64<df>(double x) { return df_from_double(x); }
 SGPU_HD double to_f64(double x) { return x; }
 SGPU_HD double to_f64(df x) { return df_to_double(x); }
 
+// FP64 <-> FP32 with integer operations (the F2F conversions run on the
+// FP64 pipe): the FP32 value is the FP64 significand truncated to 24 bits
+// (|x| < 2^-120 flushes to zero, beyond FP32 range becomes +-inf), and the
+// widening is exact.  The refined solves use them around their FP32 sweeps.
+SGPU_HD float f32_from_f64(double x) {
+  const uint64_t b = d2u(x);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const int ef = e - 1023 + 127;
+  if (e == 0x7ff || ef >= 255) return u2f(sign | 0x7f800000u);
+  if (ef <= 6) return u2f(sign);
+  return u2f(sign | ((uint32_t)ef << 23) | (uint32_t)((b & 0xFFFFFFFFFFFFFull) >> 29));
+}
+SGPU_HD double f64_from_f32(float x) {
+  const uint32_t u = f2u(x);
+  const uint32_t sign = u & 0x80000000u;
+  const uint32_t ef = (u >> 23) & 0xff;
+  if (ef == 0) return u2d((uint64_t)sign << 32);
+  if (ef == 0xff) return u2d(((uint64_t)sign << 32) | 0x7ff0000000000000ull | ((uint64_t)(u & 0x7fffff) << 29));
+  return u2d(((uint64_t)sign << 32) | ((uint64_t)(ef - 127 + 1023) << 52) | ((uint64_t)(u & 0x7fffff) << 29));
+}
+template <>
+SGPU_HD float from_f64<float>(double x) { return f32_from_f64(x); }
+SGPU_HD double to_f64(float x) { return f64_from_f32(x); }
+
 // complex product specialisation for df (4 products, 2 sums)
 SGPU_HD Cx<df> operator*(Cx<df> a, Cx<df> b) {
   Cx<df> z;

@@ -277,6 +277,45 @@ __global__ void k_helmholtz_cached(const T* b, T* u, const R* fac, int neumann, 
     helmholtz_cached_solve_prog<R, T>(b, u, fac, neumann, N, inner, nsys, t >> 1, (int)(t & 1));
 }
 
+template <class R, class T>
+__global__ void k_helmholtz_refine(const T* b, T* u, T* r, const float* fac, const double* alfa, const double* beta,
+                                   int64_t N, int64_t inner, int64_t nsys, double tol, int max_it, int* iters) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 2 * nsys) {
+    const int it = helmholtz_refine_prog<R, T>(b, u, r, fac, alfa, beta, N, inner, nsys, t >> 1, (int)(t & 1), tol,
+                                               max_it);
+    if (iters) iters[t] = it;
+  }
+}
+
+extern "C" int sgpu_helmholtz_solve_refined(const void* b, void* u, void* r, const void* fac32, const double* alfa,
+                                            const double* beta, int64_t outer, int64_t N, int64_t inner,
+                                            int data_kind, double tol, int max_it, int residual_form, int* iters,
+                                            cudaStream_t stream) {
+  if (!b || !u || !r || !fac32 || !alfa || !beta || N < 8 || outer < 0 || inner < 1 || max_it < 0 || !(tol >= 0))
+    return SGPU_ERR_ARG;
+  if (b == u || b == r || u == r) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  const unsigned nb = nblk(2 * nsys);
+  const float* f32 = (const float*)fac32;
+  if (residual_form == SGPU_PLAIN_F64 && data_kind == SGPU_COMPLEX)
+    k_helmholtz_refine<double, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (cd*)r, f32, alfa, beta, N, inner,
+                                                               nsys, tol, max_it, iters);
+  else if (residual_form == SGPU_PLAIN_F64 && data_kind == SGPU_REAL)
+    k_helmholtz_refine<double, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (double*)r, f32, alfa,
+                                                                   beta, N, inner, nsys, tol, max_it, iters);
+  else if (residual_form == SGPU_MIXED_DF && data_kind == SGPU_COMPLEX)
+    k_helmholtz_refine<df, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (cd*)r, f32, alfa, beta, N, inner,
+                                                           nsys, tol, max_it, iters);
+  else if (residual_form == SGPU_MIXED_DF && data_kind == SGPU_REAL)
+    k_helmholtz_refine<df, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, (double*)r, f32, alfa,
+                                                               beta, N, inner, nsys, tol, max_it, iters);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
 extern "C" int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double* beta, int neumann,
                                      int64_t outer, int64_t inner, int form, void* fac,
                                      cudaStream_t stream) {
@@ -288,6 +327,8 @@ extern "C" int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double
     k_helmholtz_factor<double><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, neumann, (double*)fac, nsys);
   else if (form == SGPU_MIXED_DF)
     k_helmholtz_factor<df><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, neumann, (df*)fac, nsys);
+  else if (form == SGPU_FP32_REFINED && neumann == 0)
+    k_helmholtz_factor<float><<<nblk(nsys), kThreads, 0, stream>>>(N, alfa, beta, neumann, (float*)fac, nsys);
   else
     return SGPU_ERR_ARG;
   return finish();
@@ -316,9 +357,20 @@ extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* f
 }
 
 // ---- banded + semiseparable per-wavenumber systems --------------------------
-__global__ void k_band_sep_factor(BandSepDesc d, double* fac, int64_t nsys) {
+template <class F>
+__global__ void k_band_sep_factor(BandSepDesc d, F* fac, int64_t nsys) {
   int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (ch < 2 * nsys) band_sep_factor_prog(d, fac, nsys, ch);
+  if (ch < 2 * nsys) band_sep_factor_prog<F>(d, fac, nsys, ch);
+}
+
+template <class T>
+__global__ void k_band_sep_refine(BandSepDesc d, const T* b, T* u, T* r, const float* fac, int64_t Nb, int64_t inner,
+                                  int64_t nsys, double tol, int max_it, int* iters) {
+  int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ch < 2 * nsys) {
+    const int it = band_sep_refine_prog<T>(d, b, u, r, fac, Nb, inner, nsys, ch, tol, max_it);
+    if (iters) iters[ch] = it;
+  }
 }
 
 template <class T>
@@ -337,7 +389,41 @@ extern "C" int sgpu_band_sep_factor(int n, int nterms, int gen_term, const doubl
   if ((gen_term >= 0) != (gens != nullptr)) return SGPU_ERR_ARG;
   if (nsys == 0) return SGPU_OK;
   BandSepDesc d{n, nterms, gen_term, bands, gens, coef};
-  k_band_sep_factor<<<nblk(2 * nsys), kThreads, 0, stream>>>(d, fac, nsys);
+  k_band_sep_factor<double><<<nblk(2 * nsys), kThreads, 0, stream>>>(d, fac, nsys);
+  return finish();
+}
+
+extern "C" int sgpu_band_sep_factor32(int n, int nterms, int gen_term, const double* bands, const double* gens,
+                                      const double* coef, int64_t nsys, float* fac, cudaStream_t stream) {
+  if (n < 2 || nterms < 1 || nterms > 3 || gen_term >= nterms || !bands || !coef || !fac || nsys < 0)
+    return SGPU_ERR_ARG;
+  if ((gen_term >= 0) != (gens != nullptr)) return SGPU_ERR_ARG;
+  if (nsys == 0) return SGPU_OK;
+  BandSepDesc d{n, nterms, gen_term, bands, gens, coef};
+  k_band_sep_factor<float><<<nblk(2 * nsys), kThreads, 0, stream>>>(d, fac, nsys);
+  return finish();
+}
+
+extern "C" int sgpu_band_sep_solve_refined(const void* b, void* u, void* r, const float* fac32, int n, int nterms,
+                                           int gen_term, const double* bands, const double* gens, const double* coef,
+                                           int64_t outer, int64_t Nb, int64_t inner, int data_kind, double tol,
+                                           int max_it, int* iters, cudaStream_t stream) {
+  if (!b || !u || !r || !fac32 || n < 2 || Nb < n || nterms < 1 || nterms > 3 || gen_term >= nterms || !bands ||
+      !coef || outer < 0 || inner < 1 || max_it < 0 || !(tol >= 0))
+    return SGPU_ERR_ARG;
+  if ((gen_term >= 0) != (gens != nullptr)) return SGPU_ERR_ARG;
+  if (b == u || b == r || u == r) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  BandSepDesc d{n, nterms, gen_term, bands, gens, coef};
+  if (data_kind == SGPU_COMPLEX)
+    k_band_sep_refine<cd><<<nblk(2 * nsys), kThreads, 0, stream>>>(d, (const cd*)b, (cd*)u, (cd*)r, fac32, Nb, inner,
+                                                                   nsys, tol, max_it, iters);
+  else if (data_kind == SGPU_REAL)
+    k_band_sep_refine<double><<<nblk(2 * nsys), kThreads, 0, stream>>>(d, (const double*)b, (double*)u, (double*)r,
+                                                                       fac32, Nb, inner, nsys, tol, max_it, iters);
+  else
+    return SGPU_ERR_ARG;
   return finish();
 }
 

@@ -494,6 +494,18 @@ SGPU_HD void bc_apply_prog(T* u, const double* CA, const double* alfa, const dou
 // the same structure with running sums; the reference's generic path for
 // these systems is a sparse LU per wavenumber, la.py:1231-1364.)
 //
+template <class R>
+SGPU_HD R store_cast(double x);
+template <>
+SGPU_HD double store_cast<double>(double x) { return x; }
+template <>
+SGPU_HD df store_cast<df>(double x) { return df_from_double(x); }
+template <>
+SGPU_HD float store_cast<float>(double x) {
+  // round to nearest (a one-off cost of the factorisation)
+  return (float)x;
+}
+
 // Factor cache: fac[q][c][chain], q = L0, L1, 1/diag, corr1, corr2, P, R,
 // chain = 2 * system + parity, c < m = (n + 1) / 2.
 struct BandSepDesc {
@@ -512,7 +524,8 @@ SGPU_HD double bs_band(const BandSepDesc& d, int64_t nsys, int64_t s, int off_id
   return v;
 }
 
-SGPU_HD void band_sep_factor_prog(const BandSepDesc& d, double* fac, int64_t nsys, int64_t chain) {
+template <class F = double>
+SGPU_HD void band_sep_factor_prog(const BandSepDesc& d, F* fac, int64_t nsys, int64_t chain) {
   const int64_t s = chain >> 1;
   const int par = (int)(chain & 1);
   const int n = d.n;
@@ -568,18 +581,18 @@ SGPU_HD void band_sep_factor_prog(const BandSepDesc& d, double* fac, int64_t nsy
       r2[6] -= l0 * r0[6];
     }
     // multipliers belong to the rows they eliminate
-    if (c + 1 < m) fac[((size_t)1 * m + c + 1) * nch + chain] = l1;
-    if (c + 2 < m) fac[((size_t)0 * m + c + 2) * nch + chain] = l0;
+    if (c + 1 < m) fac[((size_t)1 * m + c + 1) * nch + chain] = store_cast<F>(l1);
+    if (c + 2 < m) fac[((size_t)0 * m + c + 2) * nch + chain] = store_cast<F>(l0);
     if (c == 0) {
-      fac[((size_t)1 * m + 0) * nch + chain] = 0.0;
-      fac[((size_t)0 * m + 0) * nch + chain] = 0.0;
-      if (m > 1) fac[((size_t)0 * m + 1) * nch + chain] = 0.0;
+      fac[((size_t)1 * m + 0) * nch + chain] = store_cast<F>(0.0);
+      fac[((size_t)0 * m + 0) * nch + chain] = store_cast<F>(0.0);
+      if (m > 1) fac[((size_t)0 * m + 1) * nch + chain] = store_cast<F>(0.0);
     }
-    fac[((size_t)2 * m + c) * nch + chain] = dinv;
-    fac[((size_t)3 * m + c) * nch + chain] = r0[3];
-    fac[((size_t)4 * m + c) * nch + chain] = r0[4];
-    fac[((size_t)5 * m + c) * nch + chain] = r0[5];
-    fac[((size_t)6 * m + c) * nch + chain] = r0[6];
+    fac[((size_t)2 * m + c) * nch + chain] = store_cast<F>(dinv);
+    fac[((size_t)3 * m + c) * nch + chain] = store_cast<F>(r0[3]);
+    fac[((size_t)4 * m + c) * nch + chain] = store_cast<F>(r0[4]);
+    fac[((size_t)5 * m + c) * nch + chain] = store_cast<F>(r0[5]);
+    fac[((size_t)6 * m + c) * nch + chain] = store_cast<F>(r0[6]);
     load_row(r0, c + 3);  // slot of row c becomes row c+3
   }
 }
@@ -711,13 +724,6 @@ SGPU_HD void band_sep_matvec_prog(const BandSepDesc& d, const T* v_all, T* c_all
 // Entries are FP64 (plain form) or double-float pairs (mixed form); both are
 // 8 bytes.  The LU itself is computed in FP64 in the reference's order
 // (la.pyx:717-763) and only then stored.
-template <class R>
-SGPU_HD R store_cast(double x);
-template <>
-SGPU_HD double store_cast<double>(double x) { return x; }
-template <>
-SGPU_HD df store_cast<df>(double x) { return df_from_double(x); }
-
 template <class R>
 SGPU_HD void helmholtz_factor_prog(int64_t N, const double* alfa, const double* beta, int neumann,
                                    R* fac, int64_t nsys, int64_t s) {
@@ -869,6 +875,149 @@ SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac,
       }
     }
   }
+}
+
+// ---- FP32 solves with FP64 iterative refinement ------------------------------
+// The chosen form of the banded solves: the factor cache is FP32 (half the
+// bytes of the FP64 one; the LU is still computed in FP64 and rounded once),
+// the sweeps run in FP32, and a residual in FP64-level arithmetic (R = double
+// on the FP64 pipe, or R = df, double-float on the FP32 pipes) drives the
+// correction: u = A32^-1 f; repeat r = f - A u, d = A32^-1 r, u += d until
+// max|d| <= tol max|u| (or max_it corrections).  One thread per (system,
+// parity) chain: the Chebyshev Dirichlet Helmholtz and ShenBiharmonic
+// systems decouple by parity, so the whole loop runs on the chain.
+
+// magnitude bound used by the stopping test (max of |re|, |im|)
+SGPU_HD double mag(double a) { return a < 0 ? -a : a; }
+SGPU_HD double mag(cd a) {
+  const double x = a.re < 0 ? -a.re : a.re, y = a.im < 0 ? -a.im : a.im;
+  return x > y ? x : y;
+}
+
+// r = f - (alfa A + beta B) u on the chain k = par, par+2, .. < M of a
+// ShenDirichlet Helmholtz line (the rows of helmholtz_matvec_prog), in
+// arithmetic R; rows descending so that sum_{j >= k+2} u_j is a running sum
+template <class R, class T>
+SGPU_HD void helmholtz_residual_chain(const T* f, const T* u, T* r, double alf, double bet, int64_t M,
+                                      int64_t inner, int par) {
+  typedef ElemOps<R, T> E;
+  typedef typename E::V V;
+  const double h = 1.5707963267948966;
+  int64_t top = M - 1;
+  if ((top & 1) != par) --top;
+  V S = E::zero();                  // sum of u_j, j >= k+2 on the chain
+  V up2 = E::zero(), uk = E::zero();
+  bool have = false;
+  if (top >= 0) uk = E::load(u + top * inner);
+  for (int64_t k = top; k >= 0; k -= 2) {
+    const V um2 = k >= 2 ? E::load(u + (k - 2) * inner) : E::zero();
+    V acc = E::mul(uk, from_f64<R>(hA0(k) * alf + hB0(k) * bet));
+    if (k >= 2) acc = acc - E::mul(um2, from_f64<R>(h * bet));
+    if (have) {
+      S = S + up2;
+      acc = acc - E::mul(up2, from_f64<R>(h * bet)) + E::mul(S, from_f64<R>(hA2(k) * alf));
+    }
+    E::store(r + k * inner, E::load(f + k * inner) - acc);
+    up2 = uk;
+    uk = um2;
+    have = true;
+  }
+}
+
+// u += d on the chain (FP64), returning max|d| and max|u| (after the update)
+template <class T>
+SGPU_HD void chain_update(T* u, const T* d, int64_t M, int64_t inner, int par, double& dmax, double& umax) {
+  dmax = 0.0;
+  umax = 0.0;
+  for (int64_t k = par; k < M; k += 2) {
+    const T dk = d[k * inner];
+    const T uk = u[k * inner] + dk;
+    u[k * inner] = uk;
+    const double a = mag(dk), b = mag(uk);
+    dmax = a > dmax ? a : dmax;
+    umax = b > umax ? b : umax;
+  }
+}
+
+// the whole refinement of one Helmholtz chain; returns the corrections applied
+template <class R, class T>
+SGPU_HD int helmholtz_refine_prog(const T* f_all, T* u_all, T* r_all, const float* fac32, const double* alfa,
+                                  const double* beta, int64_t Nb, int64_t inner, int64_t nsys, int64_t s,
+                                  int par, double tol, int max_it) {
+  const int64_t M = Nb - 2;
+  const int64_t base = sys_base(s, Nb, inner);
+  helmholtz_cached_solve_prog<float, T>(f_all, u_all, fac32, 0, Nb, inner, nsys, s, par);
+  int it = 0;
+  while (it < max_it) {
+    helmholtz_residual_chain<R, T>(f_all + base, u_all + base, r_all + base, alfa[s], beta[s], M, inner, par);
+    helmholtz_cached_solve_prog<float, T>(r_all, r_all, fac32, 0, Nb, inner, nsys, s, par);
+    double dmax, umax;
+    chain_update(u_all + base, r_all + base, M, inner, par, dmax, umax);
+    ++it;
+    if (dmax <= tol * umax) break;
+  }
+  return it;
+}
+
+// band_sep_solve_prog in arithmetic R from a factor cache of R entries (the
+// FP32 sweeps of the refined biharmonic / generic solves)
+template <class R, class T>
+SGPU_HD void band_sep_solve_gen(const T* b_all, T* u_all, const R* fac, const double* gens, int n, int64_t Nb,
+                                int64_t inner, int64_t nsys, int64_t chain) {
+  typedef ElemOps<R, T> E;
+  typedef typename E::V V;
+  const int64_t s = chain >> 1;
+  const int par = (int)(chain & 1);
+  const int m = (n + 1) / 2;
+  const int64_t nch = 2 * nsys;
+  const int64_t base = sys_base(s, Nb, inner);
+  const T* f = b_all + base;
+  T* u = u_all + base;
+  auto F = [&](int q, int c) { return fac[((size_t)q * m + c) * nch + chain]; };
+  const int cend = (n - par + 1) / 2;
+  V y1 = E::zero(), y2 = E::zero();
+  for (int c = 0; c < cend; ++c) {
+    const V y = E::load(f + (2 * c + par) * inner) - E::mul(y1, F(1, c)) - E::mul(y2, F(0, c));
+    E::store(u + (2 * c + par) * inner, y);
+    y2 = y1;
+    y1 = y;
+  }
+  V sq = E::zero(), st = E::zero(), up1 = E::zero(), up2 = E::zero();
+  for (int c = cend - 1; c >= 0; --c) {
+    const int k = 2 * c + par;
+    V v = E::load(u + k * inner) - E::mul(up1, F(3, c)) - E::mul(up2, F(4, c));
+    if (gens) v = v - E::mul(sq, F(5, c)) - E::mul(st, F(6, c));
+    v = E::mul(v, F(2, c));
+    E::store(u + k * inner, v);
+    if (gens) {
+      sq = sq + E::mul(v, from_f64<R>(gens[n + k]));
+      st = st + E::mul(v, from_f64<R>(gens[3 * n + k]));
+    }
+    up2 = up1;
+    up1 = v;
+  }
+}
+
+// the whole refinement of one banded + semiseparable chain (biharmonic,
+// Legendre, generic systems): FP32 sweeps, FP64 residual from the matvec
+template <class T>
+SGPU_HD int band_sep_refine_prog(const BandSepDesc& d, const T* f_all, T* u_all, T* r_all, const float* fac32,
+                                 int64_t Nb, int64_t inner, int64_t nsys, int64_t chain, double tol, int max_it) {
+  const int64_t s = chain >> 1;
+  const int par = (int)(chain & 1);
+  const int64_t base = sys_base(s, Nb, inner);
+  band_sep_solve_gen<float, T>(f_all, u_all, fac32, d.gens, d.n, Nb, inner, nsys, chain);
+  int it = 0;
+  while (it < max_it) {
+    band_sep_matvec_prog<T>(d, u_all, r_all, Nb, inner, nsys, chain);  // r = M u on the chain
+    for (int64_t k = par; k < d.n; k += 2) r_all[base + k * inner] = f_all[base + k * inner] - r_all[base + k * inner];
+    band_sep_solve_gen<float, T>(r_all, r_all, fac32, d.gens, d.n, Nb, inner, nsys, chain);
+    double dmax, umax;
+    chain_update(u_all + base, r_all + base, d.n, inner, par, dmax, umax);
+    ++it;
+    if (dmax <= tol * umax) break;
+  }
+  return it;
 }
 
 }  // namespace sgpu

@@ -189,9 +189,17 @@ class Helmholtz:
 
     Accepts the two TPMatrix objects of ``inner(v, -div(grad(u)) + c*u)`` (or
     ``(A, B, alfa, beta)`` with SpectralMatrix A, B and scalars/arrays).
+
+    ``form``: "plain" (FP64 factor cache and sweeps), "mixed" (double-float),
+    or "refined" (Dirichlet only): FP32 factor cache (half the bytes) and
+    FP32 sweeps refined by an FP64-level residual until the correction is
+    below ``tol`` of the solution (at most ``max_it`` corrections); the
+    residual runs in FP64 (``residual="fp64"``) or double-float on the FP32
+    pipes (``residual="df"``).  ``last_iterations`` then holds each
+    (system, parity) chain's correction count.
     """
 
-    def __init__(self, *args, form=None):
+    def __init__(self, *args, form=None, tol=1e-13, max_it=8, residual="fp64"):
         require_cuda()
         if len(args) == 1:
             args = tuple(args[0])
@@ -236,17 +244,26 @@ class Helmholtz:
         _lib.call("sgpu_LU_Helmholtz", self.N, ptr(self.alfa), ptr(self.beta), int(self.neumann),
                   ptr(self.u0), ptr(self.u1), ptr(self.u2), ptr(self.L), outer, inner, stream_handle())
         # factorisation cache used by __call__: reciprocal pivots, interleaved
-        # [q][k][system] layout, FP64 (plain) or double-float pairs (mixed)
-        self.form = _lib.FORMS[form] if form is not None else (
-            self.T.form if self.T is not None else _lib.PLAIN_F64)
+        # [q][k][system] layout, FP64 (plain), double-float pairs (mixed) or
+        # FP32 (refined)
+        self.refined = form == "refined"
+        if self.refined and self.neumann:
+            raise _lib.SgpuError(_lib.ERR_UNSUPPORTED, "refined solves: Dirichlet systems only")
+        self.tol, self.max_it = float(tol), int(max_it)
+        self.residual_form = {"fp64": _lib.PLAIN_F64, "df": _lib.MIXED_DF}[residual]
+        self.form = _lib.FP32_REFINED if self.refined else (_lib.FORMS[form] if form is not None else (
+            self.T.form if self.T is not None else _lib.PLAIN_F64))
+        self.last_iterations = None
+        self._r = None
         nsys = outer * inner
         # boundary matrices of a non-homogeneous trial space (extract_bc_matrices,
         # chebyshev/la.py:222-231): subtracted from the right-hand side
         base = self.T.bases[self.axis] if self.T is not None else None
         self._bcbase = base if getattr(base, "has_nonhomogeneous_bcs", False) else None
-        self._fac = torch.empty(4 * (self.N - 2) * nsys, dtype=torch.float64, device="cuda")
+        self._fac = torch.empty(4 * (self.N - 2) * nsys, dtype=torch.float32 if self.refined else torch.float64,
+                                device="cuda")
         _lib.call("sgpu_helmholtz_factor", self.N, ptr(self.alfa), ptr(self.beta), int(self.neumann),
-                  outer, inner, self.form, ptr(self._fac), stream_handle())
+                  outer, inner, self.form, self._fac.data_ptr(), stream_handle())
 
     def __call__(self, b, u=None, constraints=()):
         b = _raw(b)
@@ -264,8 +281,11 @@ class Helmholtz:
             _lib.call("sgpu_bc_apply", ptr(b), ptr(bb._bc_table("A")), ptr(self.alfa),
                       ptr(bb._bc_table("B")), ptr(self.beta), ptr(g), outer, n, inner, 0,
                       data_kind(b), stream_handle())
-        _lib.call("sgpu_helmholtz_solve_cached", ptr(b), ptr(ur), ptr(self._fac), int(self.neumann),
-                  outer, n, inner, data_kind(b), self.form, stream_handle())
+        if self.refined:
+            self._solve_refined(b, ur, outer, n, inner)
+        else:
+            _lib.call("sgpu_helmholtz_solve_cached", ptr(b), ptr(ur), ptr(self._fac), int(self.neumann),
+                      outer, n, inner, data_kind(b), self.form, stream_handle())
         if bb is not None:
             _lib.call("sgpu_bc_apply", ptr(ur), None, None, None, None, ptr(g), outer, n, inner, 1,
                       data_kind(ur), stream_handle())
@@ -273,6 +293,17 @@ class Helmholtz:
             idx = [0] * ur.dim()
             ur[tuple(idx)] = constraints[0][1]
         return u
+
+    def _solve_refined(self, b, ur, outer, n, inner):
+        if self._r is None or self._r.shape != b.shape or self._r.dtype != b.dtype:
+            self._r = torch.empty_like(b)
+            self.last_iterations = torch.zeros(2 * outer * inner, dtype=torch.int32, device="cuda")
+        src = b
+        if b.data_ptr() == ur.data_ptr():  # the refinement re-reads b: keep it
+            src = b.clone()
+        _lib.call("sgpu_helmholtz_solve_refined", ptr(src), ptr(ur), ptr(self._r), self._fac.data_ptr(),
+                  ptr(self.alfa), ptr(self.beta), outer, n, inner, data_kind(b), self.tol, self.max_it,
+                  self.residual_form, self.last_iterations.data_ptr(), stream_handle())
 
     def solve_reference_layout(self, b, u):
         """Solve through the reference-layout factors u0, u1, u2, L
@@ -328,9 +359,12 @@ class BandSepSolver:
     """Per-wavenumber systems sum_t scale_t M_t with banded + rank-2 upper
     semiseparable M_t, factorised once on the device (sgpu_band_sep_factor)
     and solved per call (sgpu_band_sep_solve).  Used for Legendre
-    ShenDirichlet / ShenBiharmonic and Chebyshev ShenBiharmonic."""
+    ShenDirichlet / ShenBiharmonic and Chebyshev ShenBiharmonic.
 
-    def __init__(self, mats):
+    ``form="refined"``: an FP32 factor cache and FP32 sweeps refined by the
+    FP64 residual of the matvec below, as Helmholtz(form="refined")."""
+
+    def __init__(self, mats, form="plain", tol=1e-13, max_it=8):
         from .matrices import band_sep_term
         require_cuda()
         mats = sorted(list(mats), key=lambda m: -m.pmat.order)
@@ -354,10 +388,15 @@ class BandSepSolver:
         self._gens = (torch.as_tensor(np.ascontiguousarray(terms[self.gen_term][1]), device="cuda")
                       if self.gen_term >= 0 else None)
         m = (self.n + 1) // 2
-        self._fac = torch.empty(7 * m * 2 * self.nsys, dtype=torch.float64, device="cuda")
-        _lib.call("sgpu_band_sep_factor", self.n, len(mats), self.gen_term, ptr(self._bands),
-                  ptr(self._gens) if self._gens is not None else None, ptr(self._coef),
-                  self.nsys, ptr(self._fac), stream_handle())
+        self.refined = form == "refined"
+        self.tol, self.max_it = float(tol), int(max_it)
+        self.last_iterations = None
+        self._r = None
+        self._fac = torch.empty(7 * m * 2 * self.nsys, dtype=torch.float32 if self.refined else torch.float64,
+                                device="cuda")
+        _lib.call("sgpu_band_sep_factor32" if self.refined else "sgpu_band_sep_factor", self.n, len(mats),
+                  self.gen_term, ptr(self._bands), ptr(self._gens) if self._gens is not None else None,
+                  ptr(self._coef), self.nsys, self._fac.data_ptr(), stream_handle())
 
     def __call__(self, b, u=None, constraints=()):
         b = _raw(b)
@@ -367,6 +406,16 @@ class BandSepSolver:
         outer, Nb, inner = view3(tuple(b.shape), self.axis)
         if (outer, inner) != (self._outer, self._inner) or Nb != self.N:
             raise _lib.SgpuError(_lib.ERR_ARG, "array shape does not match the solver")
+        if self.refined:
+            if self._r is None or self._r.shape != b.shape or self._r.dtype != b.dtype:
+                self._r = torch.empty_like(b)
+                self.last_iterations = torch.zeros(2 * self.nsys, dtype=torch.int32, device="cuda")
+            src = b.clone() if b.data_ptr() == ur.data_ptr() else b
+            _lib.call("sgpu_band_sep_solve_refined", ptr(src), ptr(ur), ptr(self._r), self._fac.data_ptr(),
+                      self.n, self._coef.shape[0], self.gen_term, ptr(self._bands),
+                      ptr(self._gens) if self._gens is not None else None, ptr(self._coef), outer, Nb, inner,
+                      data_kind(b), self.tol, self.max_it, self.last_iterations.data_ptr(), stream_handle())
+            return u
         _lib.call("sgpu_band_sep_solve", ptr(b), ptr(ur), ptr(self._fac),
                   ptr(self._gens) if self._gens is not None else None, self.n, outer, Nb, inner,
                   data_kind(b), stream_handle())

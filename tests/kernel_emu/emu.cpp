@@ -515,8 +515,26 @@ int main(int argc, char** argv) {
     for (size_t i = 0; i < cnt; ++i) u[i] = 0.0;
     void* fac = malloc(8 * 4 * (size_t)M * ns);
     for (long long s = 0; s < ns; ++s) {
-      if (form) helmholtz_factor_prog<df>(N, a, be, nm, (df*)fac, ns, s);
+      if (form >= 2) helmholtz_factor_prog<float>(N, a, be, nm, (float*)fac, ns, s);
+      else if (form) helmholtz_factor_prog<df>(N, a, be, nm, (df*)fac, ns, s);
       else helmholtz_factor_prog<double>(N, a, be, nm, (double*)fac, ns, s);
+    }
+    if (form >= 2) {
+      // FP32 sweeps refined by an FP64 (form 2) or double-float (form 3)
+      // residual; r is scratch of b's size
+      double* r = (double*)malloc(sizeof(double) * cnt);
+      for (size_t i = 0; i < cnt; ++i) r[i] = std::numeric_limits<double>::quiet_NaN();
+      for (long long t = 0; t < 2 * ns; ++t) {
+        long long s = t >> 1;
+        int par = (int)(t & 1);
+        if (form == 2 && dk) helmholtz_refine_prog<double, cd>((const cd*)b, (cd*)u, (cd*)r, (const float*)fac, a, be, N, inner, ns, s, par, 1e-14, 8);
+        else if (form == 2) helmholtz_refine_prog<double, double>(b, u, r, (const float*)fac, a, be, N, inner, ns, s, par, 1e-14, 8);
+        else if (dk) helmholtz_refine_prog<df, cd>((const cd*)b, (cd*)u, (cd*)r, (const float*)fac, a, be, N, inner, ns, s, par, 1e-14, 8);
+        else helmholtz_refine_prog<df, double>(b, u, r, (const float*)fac, a, be, N, inner, ns, s, par, 1e-14, 8);
+      }
+      free(r);
+      write_exact(argv[10], u, cnt);
+      return 0;
     }
     for (long long t = 0; t < 2 * ns; ++t) {
       long long s = t >> 1;

@@ -266,8 +266,10 @@ def test_df_chebyshev(emu, n, basis, cplx):
 
 @pytest.mark.parametrize("N,outer,inner", [(8, 1, 3), (17, 4, 1), (33, 2, 5), (257, 3, 2)])
 @pytest.mark.parametrize("cplx", [False, True])
-@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("form", [0, 1, 2, 3])
 def test_helmholtz_cached(emu, N, outer, inner, cplx, form):
+    """Cached solves: FP64 (form 0), double-float (1), FP32 sweeps refined by
+    an FP64 (2) or double-float (3) residual, against the oracle's FP64 LU."""
     ns = outer * inner
     alfa = -np.ones(ns)
     beta = rng.uniform(0.5, 2000.0, ns)
@@ -279,7 +281,7 @@ def test_helmholtz_cached(emu, N, outer, inner, cplx, form):
     u = (u.view(np.complex128) if cplx else u).reshape(outer, N, inner)
     to_sys = lambda a: np.moveaxis(a, 1, -1).reshape(ns, N)  # noqa: E731
     uref = la.helmholtz_solve(to_sys(f), *la.helmholtz_lu(N, alfa, beta))
-    tol = 1e-13 if form == 0 else 1e-12
+    tol = {0: 1e-13, 1: 1e-12, 2: 1e-12, 3: 1e-12}[form]
     assert rel(to_sys(u)[:, :N - 2], uref[:, :N - 2]) < tol
 
 
