@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 struct DevState {
   std::once_flag attr[2];
   int attr_rc[2] = {0, 0};
-  int nclusters[2][1] = {};  // resident CTAs per device and tile width
+  int nctas[2] = {};  // resident CTAs per device and tile width
 };
 const int MAX_DEV = 64;
 DevState g_dev[MAX_DEV];
@@ -433,7 +433,7 @@ int prepare(int dev, int& nctas) {
     cudaGetLastError();
   });
   if (d.attr_rc[ci] != 1) return SGPU_ERR_CUDA;
-  int n = __atomic_load_n(&d.nclusters[ci][0], __ATOMIC_ACQUIRE);
+  int n = __atomic_load_n(&d.nctas[ci], __ATOMIC_ACQUIRE);
   if (n <= 0) {
     int per_sm = 0, nsm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lc_fused<C>, THREADS, Smem<C>::bytes) != cudaSuccess ||
@@ -442,7 +442,7 @@ int prepare(int dev, int& nctas) {
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
     cudaGetLastError();
     n = per_sm * nsm;
-    __atomic_store_n(&d.nclusters[ci][0], n, __ATOMIC_RELEASE);
+    __atomic_store_n(&d.nctas[ci], n, __ATOMIC_RELEASE);
   }
   nctas = n;
   return SGPU_OK;

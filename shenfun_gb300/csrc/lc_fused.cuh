@@ -10,15 +10,15 @@
 //
 //   D[n][line] = sum_k Mt[n][k] X[line][k]
 //
-// MMA M = 128 output indices n (one tile per CTA of a cluster of MT CTAs:
-// CTA r owns outputs 128 r .. 128 r + 127), MMA N = lines, K = entries.  A
-// tile of BN lines is split once: each CTA of the cluster splits a share of
-// the tile's lines and writes their digits into every CTA's shared memory
-// (distributed shared memory), so all MT CTAs multiply the same line digits
-// by their own rows of the matrix.  The matrix digits (A operand) are split
-// on the host and streamed from L2 with bulk copies.  Outputs past the last
-// full 128-row tile (at most two: N = 257 has output 256 left over) are FP64
-// dot products computed while the lines are read for their scales.
+// MMA M = 128 output indices n (MT CTAs share a tile of lines: CTA r of the
+// group owns outputs 128 r .. 128 r + 127), MMA N = lines, K = entries.
+// Every CTA of a group splits the tile's lines into digits in its own shared
+// memory (the second read of the lines hits L2); all synchronisation stays
+// inside the CTA.  The matrix digits (A operand) are split on the host and
+// streamed from L2 with bulk copies.  Outputs past the last full 128-row tile
+// (at most two: N = 257 has output 256 left over) are FP64 dot products that
+// the digit threads accumulate while they read the lines, each CTA of the
+// group taking a share of the tile's lines.
 //
 // Digits.  Every line (and every matrix column) is scaled by a power of two
 // 2^e with all |x| < 2^e and cut to a P-bit fixed-point integer X < 2^P
@@ -64,7 +64,7 @@ const int KSTEP = 16;     // K per MMA (kind::f16)
 const int A_BLOCK = MROWS * KSTEP;  // elements of one matrix-digit block (4 KB)
 const int LBO_A = MROWS * 16;       // bytes between the two 8-wide K core-matrix columns of A
 const int SBO = 128;                // bytes between adjacent 8-row core matrices
-const int MAX_MT = 4;               // CTAs per cluster (outputs <= 512 + 2)
+const int MAX_MT = 4;               // CTAs per tile group (outputs <= 512 + 2)
 const int MAX_NX = 2;               // outputs computed as FP64 dot products
 
 template <int W_, int S_, int H_, int BN_>
@@ -375,7 +375,7 @@ struct Geom {
   int K;        // leading input entries the matrix uses
   int cplx;
   int nsteps;   // MMA K steps of 16 (K rounded up)
-  int MT;       // CTAs per cluster = 128-output tiles on the tensor cores
+  int MT;       // CTAs per tile group = 128-output tiles on the tensor cores
   int Nmma;     // outputs on the tensor cores (the rest: FP64 dot products)
   int NX;       // outputs as FP64 dot products (N - Nmma, at most 2)
   int64_t tiles;  // tiles of BN rows
@@ -385,12 +385,6 @@ SGPU_HD int64_t row_base(const Geom& g, int64_t row) {
   return g.cplx ? (row >> 1) * 2 * (int64_t)g.N + (row & 1) : row * (int64_t)g.N;
 }
 SGPU_HD int kstride(const Geom& g) { return g.cplx ? 2 : 1; }
-
-// the rows [lo, hi) of a tile that cluster rank r splits (contiguous shares)
-SGPU_HD void row_share(int BN, int MT, int r, int& lo, int& hi) {
-  lo = (BN * r) / MT;
-  hi = (BN * (r + 1)) / MT;
-}
 
 // outputs on the tensor cores: whole 128-row tiles, plus the last partial
 // tile unless at most two outputs spill past a multiple of 128

@@ -13,7 +13,7 @@ namespace lc {
 // K leading nonzero rows, split into BF16 digits for the tensor cores
 struct Matrix {
   int N = 0, K = 0;
-  int MT = 0;     // CTAs per cluster (128-output tiles)
+  int MT = 0;     // CTAs per tile group (128-output tiles)
   int Nmma = 0;   // outputs on the tensor cores
   int NX = 0;     // outputs as FP64 dot products
   uint16_t* tiles = nullptr;  // device: digit tiles | exponents | dot-product columns

@@ -294,36 +294,27 @@ static int lcf_run(const lc::Geom& g, const double* in, const double* M, double*
   const int ksd = kstride(g);
   for (int64_t T = 0; T < g.tiles; ++T) {
     const int64_t row0 = T * BN;
-    int covered = 0;
-    for (int r = 0; r < g.MT; ++r) {
-      int lo, hi;
-      row_share(BN, g.MT, r, lo, hi);
-      covered += hi - lo;
-      for (int jj = lo; jj < hi; ++jj) {
-        const int64_t row = row0 + jj;
-        uint32_t mf = 0;
-        double acc[MAX_NX] = {0.0, 0.0};
-        if (row < g.nrows)
-          for (int k = 0; k < g.K; ++k) {
-            const double x = in[row_base(g, row) + (int64_t)k * ksd];
-            mf = exp_field(x) > mf ? exp_field(x) : mf;
-            for (int c = 0; c < g.NX; ++c) acc[c] += x * xcol[(size_t)c * g.K + k];
-          }
-        e[jj] = exp_from_field(mf);
-        for (int c = 0; c < MAX_NX; ++c) xo[(size_t)jj * MAX_NX + c] = acc[c];
-      }
+    for (int jj = 0; jj < BN; ++jj) {
+      const int64_t row = row0 + jj;
+      uint32_t mf = 0;
+      double acc[MAX_NX] = {0.0, 0.0};
+      if (row < g.nrows)
+        for (int k = 0; k < g.K; ++k) {
+          const double x = in[row_base(g, row) + (int64_t)k * ksd];
+          mf = exp_field(x) > mf ? exp_field(x) : mf;
+          for (int c = 0; c < g.NX; ++c) acc[c] += x * xcol[(size_t)c * g.K + k];
+        }
+      e[jj] = exp_from_field(mf);
+      for (int c = 0; c < MAX_NX; ++c) xo[(size_t)jj * MAX_NX + c] = acc[c];
     }
-    if (covered != BN) return 7;
     for (int ks = 0; ks < g.nsteps; ++ks) {
       for (size_t i = 0; i < bst.size(); i += 2) {
         bst[i] = 0xC0;
         bst[i + 1] = 0x7F;  // BF16 NaN: unwritten shows
       }
-      for (int r = 0; r < g.MT; ++r) {
-        int lo, hi;
-        row_share(BN, g.MT, r, lo, hi);
+      {
         for (int h = 0; h < 2; ++h)
-          for (int jj = lo; jj < hi; ++jj) {
+          for (int jj = 0; jj < BN; ++jj) {
             const int64_t row = row0 + jj;
             double x[8];
             const int k0 = ks * KSTEP + h * 8;
