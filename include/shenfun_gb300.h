@@ -5,9 +5,11 @@
  * Conventions
  *  - Every pointer argument named in/out/u/b/d0/... is a DEVICE pointer to
  *    C-contiguous FP64 (or interleaved complex FP64) data.  The caller owns all
- *    memory; no entry point below allocates device memory except
- *    sgpu_plan_create (tables, once per plan) and sgpu_*_workspace queries
- *    return sizes the caller allocates.
+ *    memory.  Plan and problem creation allocate their tables once; the
+ *    sgpu_*_workspace_size queries return the scratch an execution needs, and
+ *    the *_ws / _noalloc entry points allocate nothing.  Entry points that
+ *    need scratch without taking it from the caller say so (stream-ordered
+ *    cudaMallocAsync on the call's stream).
  *  - An N-D array is handed over as a 3-D view (outer, n, inner) around the
  *    axis being transformed or solved: element (o, k, i) lives at
  *    o*n*inner + k*inner + i.  This covers every axis of a C-contiguous array
@@ -156,8 +158,8 @@ int sgpu_fourier_truncate(const void* in, void* out, int64_t outer, int N, int M
  * _LU / _Solve) --------------------------------------------------------------
  * data: ndiag rows of n in the reference's column-aligned (scipy DIA)
  * layout, row r holding M[i][i + offsets[r]] at column i + offsets[r];
- * offsets (host array) even, ascending, containing 0 and every even value
- * between the first and the last.  LU in place without pivoting; the solve
+ * offsets (host array) ascending, containing 0 and every even value between
+ * the first and the last, or every value (consecutive: TDMA_O's -1, 0, 1).  LU in place without pivoting; the solve
  * runs along the middle axis of u (outer, n, inner), in place. */
 int sgpu_banded_LU(double* data, int ndiag, const int* offsets, int64_t n, cudaStream_t stream);
 int sgpu_banded_Solve(void* u, const double* data, int ndiag, const int* offsets, int64_t outer,
@@ -386,6 +388,91 @@ int sgpu_last_error(cudaStream_t stream);
  * nanoseconds (0: the default, one second).  For tests that make a wait run
  * out; process-wide. */
 int sgpu_set_wait_limit_ns(unsigned long long ns);
+
+/* ---- reference-signature entry points (optimization/cython) ---------------
+ * The kernels shenfun's optimization modules export by name, on the
+ * reference's own argument arrays (device copies, same shapes and layouts),
+ * so that a shenfun optimization mode can forward to them unchanged.  An
+ * N-D array with the solve axis `axis` is (outer, N, inner) with outer and
+ * inner the products of the dimensions before and after it.
+ *
+ * Chebyshev biharmonic (chebyshev/la.py:354-558): the factor arrays u0, u1,
+ * u2, l0, l1, ak, bk have the reference's shape (2, outer, M, inner) (M per
+ * parity; the space has N - 4 = 2M dofs); alfa, beta hold one value per
+ * system (outer x inner, the scale arrays broadcast to the systems); the 11
+ * diagonals are the reference's sii, siu, siuu (SBB 0, +2, +4), ail, aii,
+ * aiu (ABB -2, 0, +2), bill, bil, bii, biu, biuu (BBB -4 .. +4) of lengths
+ * 2M, 2M-2, 2M-4, ...  M >= 5.  The reference's row elimination is O(M^2)
+ * per system; the LU here keeps each row's full upper part as two
+ * coefficients (O(M)), the same factors to rounding. */
+/* la.pyx:975 LU_Biharmonic(a0, alfa, beta, sii, siu, siuu, ail, aii, aiu, bill,
+ * bil, bii, biu, biuu, u0, u1, u2, l0, l1, axis) */
+int sgpu_LU_Biharmonic(double a0, const double* alfa, const double* beta, const double* sii,
+                       const double* siu, const double* siuu, const double* ail, const double* aii,
+                       const double* aiu, const double* bill, const double* bil, const double* bii,
+                       const double* biu, const double* biuu, double* u0, double* u1, double* u2,
+                       double* l0, double* l1, int64_t outer, int64_t M, int64_t inner, cudaStream_t stream);
+/* la.pyx:1195 Biharmonic_factor_pr(ak, bk, l0, l1, axis): rows 0 .. M-3 */
+int sgpu_Biharmonic_factor_pr(double* ak, double* bk, const double* l0, const double* l1, int64_t outer,
+                              int64_t M, int64_t inner, cudaStream_t stream);
+/* la.pyx:1235 Biharmonic_Solve(b, u, u0, u1, u2, l0, l1, ak, bk, a0, axis):
+ * b, u (outer, N, inner) with 2M <= N; entries 2M .. N-1 of u are left as
+ * they are; u may alias b */
+int sgpu_Biharmonic_Solve(const void* b, void* u, const double* u0, const double* u1, const double* u2,
+                          const double* l0, const double* l1, const double* ak, const double* bk, double a0,
+                          int64_t outer, int64_t N, int64_t inner, int64_t M, int data_kind,
+                          cudaStream_t stream);
+/* Matvec.pyx:908 Biharmonic_matvec(v, b, a0, alfa, beta, sii, ..., biuu, axis):
+ * b[0 .. M-1] = (a0 SBB + alfa ABB + beta BBB) v with M = len(sii) = N - 4 >= 10;
+ * v and b must not alias */
+int sgpu_Biharmonic_matvec(const void* v, void* b, double a0, const double* alfa, const double* beta,
+                           const double* sii, const double* siu, const double* siuu, const double* ail,
+                           const double* aii, const double* aiu, const double* bill, const double* bil,
+                           const double* bii, const double* biu, const double* biuu, int64_t outer, int64_t N,
+                           int64_t inner, int64_t M, int data_kind, cudaStream_t stream);
+
+/* the *_inner_solve kernels SolverGeneric1ND_solve_data dispatches to by name
+ * (la.pyx:307-325, 466-613), each reading the reference's LU'd data layout */
+#define SGPU_SOL_DIAGMA 0
+#define SGPU_SOL_TWODMA 1
+#define SGPU_SOL_THREEDMA 2 /* reads its +4 band from the +2 row, 4 columns on (la.pyx:569-584) */
+#define SGPU_SOL_TDMA 3
+#define SGPU_SOL_TDMA_O 4
+#define SGPU_SOL_PDMA 5
+#define SGPU_SOL_FDMA 6
+#define SGPU_SOL_HEPTADMA 7
+/* la.pyx:371 SolverGeneric1ND_solve_data(u, data, sol, naxes, is_zero_index):
+ * u (outer, N, inner) along the solve axis naxes, in place; data holds one
+ * (rows, cols) LU'd matrix per system, systems in (outer, inner) order (the
+ * reference's data[i, j]); the first cols entries of each line are solved;
+ * is_zero_index skips system 0 (solved separately by the caller). */
+int sgpu_SolverGeneric1ND_solve_data(void* u, const double* data, int sol, int is_zero_index, int64_t outer,
+                                     int64_t N, int64_t inner, int64_t rows, int64_t cols, int data_kind,
+                                     cudaStream_t stream);
+/* la.pyx DiagMA_Solve / TwoDMA_Solve / ThreeDMA_Solve / TDMA_O_Solve /
+ * FDMA_Solve / HeptaDMA_Solve(u, data, axis): one (rows, cols) LU'd matrix
+ * for every line */
+int sgpu_DMA_Solve(int sol, void* u, const double* data, int64_t rows, int64_t cols, int64_t outer, int64_t N,
+                   int64_t inner, int data_kind, cudaStream_t stream);
+
+/* Recursive Legendre transforms (transforms.pyx:175-216, called at
+ * spectralbase.py:485-491, 551-558): x the points, w the weights, a the DIA
+ * data (a_rows = 2 or 3 rows of a_cols >= N + 2) of the basis' recursion
+ * matrix.  The recurrence builds the point-by-degree matrix once (one thread
+ * per point, the reference's operation order), then an FP64 GEMM applies it
+ * to every line; the matrix (N x Nx doubles) lives in `work` when given
+ * (work_bytes >= 8 N Nx), else in cudaMallocAsync memory on `stream`.
+ * input and output must not alias. */
+/* scalar_product(input, output, x, w, axis, a): output[i] = sum_j P_i(x_j) w_j input[j],
+ * input and output of N entries along the axis */
+int sgpu_scalar_product(const void* input, void* output, const double* x, const double* w, const double* a,
+                        int a_rows, int64_t a_cols, int64_t outer, int64_t N, int64_t inner, int data_kind,
+                        void* work, size_t work_bytes, cudaStream_t stream);
+/* evaluate_expansion_all(input, output, x, axis, a): output[j] = sum_i P_i(x_j) input[i],
+ * N coefficients in, Nx points out */
+int sgpu_evaluate_expansion_all(const void* input, void* output, const double* x, const double* a, int a_rows,
+                                int64_t a_cols, int64_t outer, int64_t N, int64_t Nx, int64_t inner, int data_kind,
+                                void* work, size_t work_bytes, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -91,6 +91,15 @@ SIGNATURES = {
     "sgpu_legendre_workspace_size": (_int, [_vp, _i64, _i64, _int, ctypes.POINTER(ctypes.c_size_t)]),
     "sgpu_legendre_execute_ws": (_int, [_vp, _int, _vp, _vp, _i64, _i64, _int, _vp, ctypes.c_size_t, _vp]),
     "sgpu_wait_timeouts": (_int, [ctypes.POINTER(ctypes.c_uint)]),
+    "sgpu_LU_Biharmonic": (_int, [_dbl] + [_vp] * 18 + [_i64, _i64, _i64, _vp]),
+    "sgpu_Biharmonic_factor_pr": (_int, [_vp] * 4 + [_i64, _i64, _i64, _vp]),
+    "sgpu_Biharmonic_Solve": (_int, [_vp] * 9 + [_dbl, _i64, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_Biharmonic_matvec": (_int, [_vp, _vp, _dbl] + [_vp] * 13 + [_i64, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_SolverGeneric1ND_solve_data": (_int, [_vp, _vp, _int, _int, _i64, _i64, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_DMA_Solve": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_scalar_product": (_int, [_vp] * 5 + [_int, _i64, _i64, _i64, _i64, _int, _vp, ctypes.c_size_t, _vp]),
+    "sgpu_evaluate_expansion_all": (_int, [_vp] * 4 + [_int, _i64, _i64, _i64, _i64, _i64, _int, _vp,
+                                                       ctypes.c_size_t, _vp]),
 }
 
 

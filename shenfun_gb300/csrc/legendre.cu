@@ -360,15 +360,16 @@ extern "C" int sgpu_legendre_nodes(const sgpu_legendre_plan* p, double* x, doubl
 
 // ---------------------------------------------------------------------------
 // FP64 GEMM along lines: out(l, k) = sum_j in(l, j) M[j][k] for every line l
-// of a (outer, N, inner) array (complex lines: real and imaginary parts are
-// two rows).  64 x 64 output tiles, K steps of 16, 256 threads with 4 x 4
-// register blocks; rows are (line, part) pairs.
+// of an (outer, Nin, inner) input and (outer, Nout, inner) output (complex
+// lines: real and imaginary parts are two rows); M is Nin x Nout.  64 x 64
+// output tiles, K steps of 16, 256 threads with 4 x 4 register blocks; rows
+// are (line, part) pairs.
 namespace {
 const int TM = 64, TN = 64, TK = 16;
 }
 
 __global__ void __launch_bounds__(256) k_line_gemm_f64(const double* in, double* out, const double* M,
-                                                       int N, int64_t nrows, int64_t inner,
+                                                       int Nin, int Nout, int64_t nrows, int64_t inner,
                                                        int cplx) {
   __shared__ double As[TK][TM + 1];
   __shared__ double Bs[TK][TN + 1];
@@ -377,26 +378,26 @@ __global__ void __launch_bounds__(256) k_line_gemm_f64(const double* in, double*
   const int col0 = blockIdx.y * TN;
   const int tr = tid / 16, tc = tid % 16;  // 16 x 16 threads, 4 x 4 each
   double acc[4][4] = {};
-  // element (row, j): row = line * (1 + cplx) + part
-  auto off = [&](int64_t row, int64_t j) -> int64_t {
+  // element (row, j) of a line of length N: row = line * (1 + cplx) + part
+  auto off = [&](int64_t row, int64_t j, int N) -> int64_t {
     int64_t l = cplx ? (row >> 1) : row;
     int part = cplx ? (int)(row & 1) : 0;
     int64_t o = l / inner, i = l - o * inner;
     int64_t e = (o * N + j) * inner + i;
     return cplx ? 2 * e + part : e;
   };
-  for (int k0 = 0; k0 < N; k0 += TK) {
+  for (int k0 = 0; k0 < Nin; k0 += TK) {
     // A tile: TM rows x TK columns (4 per thread)
     for (int e = tid; e < TM * TK; e += 256) {
       int r = e / TK, kk = e % TK;
       int64_t row = row0 + r;
       int j = k0 + kk;
-      As[kk][r] = (row < nrows && j < N) ? in[off(row, j)] : 0.0;
+      As[kk][r] = (row < nrows && j < Nin) ? in[off(row, j, Nin)] : 0.0;
     }
     for (int e = tid; e < TK * TN; e += 256) {
       int kk = e / TN, c = e % TN;
       int j = k0 + kk, col = col0 + c;
-      Bs[kk][c] = (j < N && col < N) ? M[(size_t)j * N + col] : 0.0;
+      Bs[kk][c] = (j < Nin && col < Nout) ? M[(size_t)j * Nout + col] : 0.0;
     }
     __syncthreads();
 #pragma unroll
@@ -420,10 +421,21 @@ __global__ void __launch_bounds__(256) k_line_gemm_f64(const double* in, double*
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       int col = col0 + tc * 4 + q;
-      if (col < N) out[off(row, col)] = acc[i][q];
+      if (col < Nout) out[off(row, col, Nout)] = acc[i][q];
     }
   }
 }
+
+namespace sgpu {
+int line_gemm_f64(const double* in, double* out, const double* M, int Nin, int Nout, int64_t nrows,
+                  int64_t inner, int cplx, cudaStream_t stream) {
+  if (nrows == 0) return SGPU_OK;
+  if ((nrows + TM - 1) / TM > 0x7fffffff || Nin < 1 || Nout < 1) return SGPU_ERR_ARG;
+  dim3 grid((unsigned)((nrows + TM - 1) / TM), (unsigned)((Nout + TN - 1) / TN));
+  k_line_gemm_f64<<<grid, 256, 0, stream>>>(in, out, M, Nin, Nout, nrows, inner, cplx);
+  return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
+}
+}  // namespace sgpu
 
 // mass solve along lines after the scalar product (forward transform)
 template <class T>
@@ -486,7 +498,7 @@ static int legendre_run(const sgpu_legendre_plan* p, int direction, const void* 
     dim3 grid((unsigned)((nrows + TM - 1) / TM), (unsigned)((p->N + TN - 1) / TN));
     if ((nrows + TM - 1) / TM > 0x7fffffff) return SGPU_ERR_ARG;
     const double* M = direction == 2 ? p->d_back : p->d_scalar;
-    k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, nrows, inner, cplx);
+    k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, p->N, nrows, inner, cplx);
   }
   if (direction == 1 && p->form != SGPU_MIXED_DF) {
     const unsigned nb = (unsigned)((nlines + 127) / 128);

@@ -81,14 +81,18 @@ __global__ void k_banded_solve(T* u, const double* data, BandDesc b, int64_t n, 
 }
 
 namespace {
-// offsets: 1..9 even values, ascending, with 0 and every even value between
-// the first and the last (elimination fills in only inside the band)
+// offsets: 1..9 values, ascending, with 0 and every value between the first
+// and the last, all even (steps of 2) or consecutive (steps of 1, as
+// TDMA_O's -1, 0, 1): elimination fills in only inside the band
 int band_desc(int ndiag, const int* offsets, int64_t n, BandDesc* b) {
   if (!offsets || ndiag < 1 || ndiag > 9 || n < 1) return SGPU_ERR_ARG;
   b->nd = ndiag;
+  bool even = true;
+  for (int r = 0; r < ndiag; ++r) even = even && offsets[r] % 2 == 0;
+  const int step = even ? 2 : 1;
   for (int r = 0; r < ndiag; ++r) {
     const int o = offsets[r];
-    if (o % 2 != 0 || (r > 0 && o != offsets[r - 1] + 2) || (o < 0 ? -o : o) >= n) return SGPU_ERR_ARG;
+    if ((r > 0 && o != offsets[r - 1] + step) || (o < 0 ? -o : o) >= n) return SGPU_ERR_ARG;
     b->off[r] = o;
   }
   if (offsets[0] > 0 || offsets[ndiag - 1] < 0) return SGPU_ERR_ARG;

@@ -514,10 +514,140 @@ def dma():
     put("dma", **d)
 
 
+# --------------------------------------------------------------------------
+# The kernel dispatch boundary (optimization/__init__.py:37-84): every call
+# the reference's own classes make to its compiled kernels by name, recorded
+# with its arguments before and after (the kernels write in place).  The
+# replays in tests/test_optimization_mode.py and test_gpu_optimization_mode.py
+# feed the same arguments to the gb300 optimization module and to the oracle.
+# Own rng.
+OPT_NAMES = ("TDMA_LU", "TDMA_Solve", "PDMA_LU", "PDMA_Solve", "FDMA_LU", "FDMA_Solve", "TwoDMA_Solve",
+             "ThreeDMA_Solve", "DiagMA_Solve", "HeptaDMA_LU", "HeptaDMA_Solve", "TDMA_O_LU", "TDMA_O_Solve",
+             "SolverGeneric1ND_solve_data", "LU_Helmholtz", "Solve_Helmholtz", "Helmholtz_matvec",
+             "LU_Biharmonic", "Biharmonic_factor_pr", "Biharmonic_Solve", "Biharmonic_matvec")
+OPT_TRANSFORMS = ("scalar_product", "evaluate_expansion_all")
+
+
+def optmode():
+    import functools
+    import json
+    import shenfun.optimization as opt
+    from shenfun.matrixbase import SparseMatrix, SpectralMatrix
+    g = np.random.default_rng(4099)
+    cy = opt.cython
+    tr = sys.modules["shenfun.optimization.cython.transforms"]
+    calls = []
+    arrays = {}
+
+    def snap(a, key):
+        if isinstance(a, (bool, np.bool_)):
+            return {"t": "bool", "v": bool(a)}
+        if isinstance(a, (int, float, np.integer, np.floating)) and not isinstance(a, np.ndarray):
+            return {"t": "num", "v": float(a), "int": isinstance(a, (int, np.integer))}
+        if callable(a) and not isinstance(a, np.ndarray):
+            return {"t": "fn", "v": a.__name__}
+        if isinstance(a, (SparseMatrix, SpectralMatrix)) or (isinstance(a, dict)):
+            offs = sorted(int(k) for k in a.keys())
+            for o in offs:
+                arrays[f"{key}_d{o}"] = np.atleast_1d(np.asarray(a[o], dtype=float)).copy()
+            return {"t": "mat", "offsets": offs, "key": key}
+        arr = np.asarray(a)
+        if arr.ndim == 0:
+            return {"t": "num", "v": float(arr), "int": False}
+        arrays[key] = arr.copy()
+        return {"t": "arr", "key": key}
+
+    def recorder(name, fn):
+        @functools.wraps(fn)
+        def wrapped(*args):
+            i = len(calls)
+            spec = [snap(a, f"c{i:03d}_a{j}") for j, a in enumerate(args)]
+            before = [np.array(a, copy=True) if s["t"] == "arr" else None for a, s in zip(args, spec)]
+            r = fn(*args)
+            for a, s, b0 in zip(args, spec, before):
+                if s["t"] == "arr" and not np.array_equal(np.asarray(a), b0, equal_nan=True):
+                    s["out"] = s["key"] + "_out"
+                    arrays[s["out"]] = np.array(a, copy=True)
+            calls.append({"name": name, "args": spec})
+            return r
+        return wrapped
+
+    saved = {}
+    for n in OPT_NAMES:
+        saved[(cy, n)] = getattr(cy, n)
+        setattr(cy, n, recorder(n, getattr(cy, n)))
+    for n in OPT_TRANSFORMS:
+        saved[(tr, n)] = getattr(tr, n)
+        setattr(tr, n, recorder("transforms." + n, getattr(tr, n)))
+    try:
+        # banded solvers through the reference's own classes (la.py:291-800)
+        kinds = {"TDMA": (-2, 0, 2), "PDMA": (-4, -2, 0, 2, 4), "FDMA": (-2, 0, 2, 4), "TwoDMA": (0, 2),
+                 "ThreeDMA": (0, 2, 4), "HeptaDMA": (-4, -2, 0, 2, 4, 6, 8), "TDMA_O": (-1, 0, 1)}
+        for name, offs in kinds.items():
+            n = 14
+            diags = {o: (4.0 + g.uniform(0, 1, n - abs(o))) if o == 0 else g.uniform(-0.5, 0.5, n - abs(o))
+                     for o in offs}
+            for ax, shape in ((0, (n, 3)), (1, (4, n))):
+                sol = getattr(la, name)(SparseMatrix(dict(diags), (n, n)))
+                b = g.standard_normal(shape) + 1j * g.standard_normal(shape)
+                sol(b.copy(), axis=ax)
+        # the reference's DiagMA solve takes 1D right-hand sides only
+        n = 14
+        sol = la.DiagMA(SparseMatrix({0: 2.0 + g.uniform(0, 1, n)}, (n, n)))
+        sol(g.standard_normal(n) + 1j * g.standard_normal(n), axis=0)
+        # Chebyshev Dirichlet / Neumann Helmholtz (chebyshev/la.py:131-351)
+        for basis, bc in (("SD", (0, 0)), ("SN", {"left": ("N", 0), "right": ("N", 0)})):
+            F0 = FunctionSpace(6, "F", dtype="D")
+            F1 = FunctionSpace(6, "F", dtype="d")
+            C = FunctionSpace(16, "C", bc=bc)
+            T = TensorProductSpace(comm, (F0, F1, C))
+            u, v = TrialFunction(T), TestFunction(T)
+            mats = inner(v, -div(grad(u)) + 10 * u)
+            H = chebyshev.la.Helmholtz(*mats)
+            fh = Function(T, buffer=g.standard_normal(T.shape(True)) + 1j * g.standard_normal(T.shape(True)))
+            H(fh.copy(), Function(T))
+            if basis == "SD":
+                H.matvec(fh.copy(), Function(T))
+        # Chebyshev biharmonic (chebyshev/la.py:354-558), even N
+        F0 = FunctionSpace(6, "F", dtype="D")
+        F1 = FunctionSpace(6, "F", dtype="d")
+        SB = FunctionSpace(20, "C", bc=(0, 0, 0, 0))
+        T = TensorProductSpace(comm, (F0, F1, SB))
+        u, v = TrialFunction(T), TestFunction(T)
+        mats = inner(v, div(grad(div(grad(u)))) + 5 * div(grad(u)) + 3 * u)
+        Hb = chebyshev.la.Biharmonic(*mats)
+        fh = Function(T, buffer=g.standard_normal(T.shape(True)) + 1j * g.standard_normal(T.shape(True)))
+        Hb(fh.copy(), Function(T))
+        Hb.matvec(fh.copy(), Function(T))
+        # SolverGeneric1ND on Fourier x Legendre (la.py:1183-1434): one TDMA /
+        # PDMA per wavenumber through SolverGeneric1ND_solve_data
+        for bc in ((0, 0), (0, 0, 0, 0)):
+            F0 = FunctionSpace(6, "F", dtype="D")
+            L = FunctionSpace(18, "L", bc=bc)
+            T = TensorProductSpace(comm, (F0, L))
+            u, v = TrialFunction(T), TestFunction(T)
+            op = -div(grad(u)) + u if len(bc) == 2 else div(grad(div(grad(u)))) + u
+            S = la.SolverGeneric1ND(inner(v, op))
+            fh = Function(T, buffer=g.standard_normal(T.shape(True)) + 1j * g.standard_normal(T.shape(True)))
+            S(fh.copy(), Function(T))
+        # recursive Legendre transforms (spectralbase.py:485-491, 551-558)
+        for N, bc in ((12, None), (17, (0, 0))):
+            L = FunctionSpace(N, "L", bc=bc) if bc else FunctionSpace(N, "L")
+            fj = g.standard_normal(N)
+            L.scalar_product(fj, np.zeros(N), kind="recursive")
+            L.backward(g.standard_normal(N), np.zeros(N), kind="recursive")
+    finally:
+        for (mod, n), fn in saved.items():
+            setattr(mod, n, fn)
+    arrays["manifest"] = np.array(json.dumps(calls))
+    put("optmode", **arrays)
+    print("optmode:", len(calls), "calls:", sorted({c["name"] for c in calls}))
+
+
 GROUPS = {"cheb_1d": cheb_1d, "fourier_1d": fourier_1d, "banded": banded, "helmholtz": helmholtz,
           "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex,
           "dealias": dealias, "neumann": neumann,
-          "nonhomog": nonhomog, "dma": dma}
+          "nonhomog": nonhomog, "dma": dma, "optmode": optmode}
 
 if __name__ == "__main__":
     # no arguments: every group (the shared rng makes the earlier groups depend

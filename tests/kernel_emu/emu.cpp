@@ -29,6 +29,7 @@
 #include "../../shenfun_gb300/csrc/solvers.cuh"
 #include "../../shenfun_gb300/csrc/ozaki.cuh"
 #include "../../shenfun_gb300/csrc/lc_fused.cuh"
+#include "../../shenfun_gb300/csrc/ref_progs.cuh"
 
 using namespace sgpu;
 
@@ -669,6 +670,98 @@ int main(int argc, char** argv) {
       else banded_solve_prog<double>(u, data, b, n, inner, s);
     }
     write_exact(argv[10], u, cnt);
+    return 0;
+  }
+  if (mode == "bih") {
+    // bih outer M inner dk a0 alfa beta sii siu siuu ail aii aiu bill bil bii biu biuu f out
+    // (LU, factor_pr, solve; out = u0 u1 u2 l0 l1 ak bk u)
+    long long outer = atoll(argv[2]), M = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]);
+    double a0 = atof(argv[6]);
+    const long long nsys = outer * inner, n = 2 * M, N = n + 4;
+    const int w = dk ? 2 : 1;
+    double* alfa = read_exact(argv[7], nsys);
+    double* beta = read_exact(argv[8], nsys);
+    const int shorter[11] = {0, 2, 4, 2, 0, 2, 4, 2, 0, 2, 4};
+    double* dg[11];
+    for (int q = 0; q < 11; ++q) dg[q] = read_exact(argv[9 + q], n - shorter[q]);
+    ref::BihDiags d{dg[0], dg[1], dg[2], dg[3], dg[4], dg[5], dg[6], dg[7], dg[8], dg[9], dg[10]};
+    const size_t cnt = (size_t)outer * N * inner * w, fsz = (size_t)2 * nsys * M;
+    double* f = read_exact(argv[20], cnt);
+    double* fac = (double*)calloc(7 * fsz, sizeof(double));
+    double *u0 = fac, *u1 = fac + fsz, *u2 = fac + 2 * fsz, *l0 = fac + 3 * fsz, *l1 = fac + 4 * fsz,
+           *ak = fac + 5 * fsz, *bk = fac + 6 * fsz;
+    for (long long c = 0; c < 2 * nsys; ++c) ref::bih_lu_chain(c, nsys, d, a0, alfa, beta, u0, u1, u2, l0, l1, M, inner);
+    for (long long c = 0; c < 2 * nsys; ++c) ref::bih_factor_pr_chain(c, nsys, ak, bk, l0, l1, M, inner);
+    double* u = (double*)malloc(sizeof(double) * cnt);
+    memcpy(u, f, sizeof(double) * cnt);
+    for (long long c = 0; c < 2 * nsys; ++c) {
+      if (dk)
+        ref::bih_solve_chain<cd>(c, nsys, (const cd*)f, (cd*)u, u0, u1, u2, l0, l1, ak, bk, a0, N, M, inner);
+      else
+        ref::bih_solve_chain<double>(c, nsys, f, u, u0, u1, u2, l0, l1, ak, bk, a0, N, M, inner);
+    }
+    double* out = (double*)malloc(sizeof(double) * (7 * fsz + cnt));
+    memcpy(out, fac, sizeof(double) * 7 * fsz);
+    memcpy(out + 7 * fsz, u, sizeof(double) * cnt);
+    write_exact(argv[21], out, 7 * fsz + cnt);
+    return 0;
+  }
+  if (mode == "bihmv") {
+    // bihmv outer N inner dk a0 alfa beta sii .. biuu v out   (M = N - 4)
+    long long outer = atoll(argv[2]), N = atoll(argv[3]), inner = atoll(argv[4]);
+    int dk = atoi(argv[5]);
+    double a0 = atof(argv[6]);
+    const long long nsys = outer * inner, M = N - 4;
+    const int w = dk ? 2 : 1;
+    double* alfa = read_exact(argv[7], nsys);
+    double* beta = read_exact(argv[8], nsys);
+    const int shorter[11] = {0, 2, 4, 2, 0, 2, 4, 2, 0, 2, 4};
+    double* dg[11];
+    for (int q = 0; q < 11; ++q) dg[q] = read_exact(argv[9 + q], M - shorter[q]);
+    ref::BihDiags d{dg[0], dg[1], dg[2], dg[3], dg[4], dg[5], dg[6], dg[7], dg[8], dg[9], dg[10]};
+    const size_t cnt = (size_t)outer * N * inner * w;
+    double* v = read_exact(argv[20], cnt);
+    double* b = (double*)calloc(cnt, sizeof(double));
+    for (long long s2 = 0; s2 < nsys; ++s2) {
+      if (dk) ref::bih_matvec_sys<cd>(s2, (const cd*)v, (cd*)b, d, a0, alfa, beta, N, M, inner);
+      else ref::bih_matvec_sys<double>(s2, v, b, d, a0, alfa, beta, N, M, inner);
+    }
+    write_exact(argv[21], b, cnt);
+    return 0;
+  }
+  if (mode == "dma") {
+    // dma kind rows cols outer N inner dk per_system skip data u out
+    int kind = atoi(argv[2]);
+    long long rows = atoll(argv[3]), cols = atoll(argv[4]), outer = atoll(argv[5]), N = atoll(argv[6]),
+              inner = atoll(argv[7]);
+    int dk = atoi(argv[8]), per = atoi(argv[9]), skip = atoi(argv[10]);
+    const long long nsys = outer * inner;
+    if (rows < ref::dma_rows(kind) || cols < ref::dma_min_cols(kind) || cols > N) return 4;
+    double* data = read_exact(argv[11], (size_t)(per ? nsys : 1) * rows * cols);
+    const size_t cnt = (size_t)outer * N * inner * (dk ? 2 : 1);
+    double* u = read_exact(argv[12], cnt);
+    for (long long s2 = 0; s2 < nsys; ++s2) {
+      if (skip && s2 == 0) continue;
+      if (dk) ref::dma_solve_sys<cd>(s2, kind, (cd*)u, data, per ? rows * cols : 0, cols, N, inner);
+      else ref::dma_solve_sys<double>(s2, kind, u, data, per ? rows * cols : 0, cols, N, inner);
+    }
+    write_exact(argv[13], u, cnt);
+    return 0;
+  }
+  if (mode == "legrec") {
+    // legrec scalar n npts rows cols x w a out
+    int scalar = atoi(argv[2]);
+    long long n = atoll(argv[3]), npts = atoll(argv[4]);
+    int rows = atoi(argv[5]);
+    long long cols = atoll(argv[6]);
+    if (cols < n + 2 || (rows != 2 && rows != 3)) return 4;
+    double* x = read_exact(argv[7], npts);
+    double* wv = read_exact(argv[8], npts);
+    double* a = read_exact(argv[9], (size_t)rows * cols);
+    double* M = (double*)malloc(sizeof(double) * n * npts);
+    for (long long j = 0; j < npts; ++j) ref::legendre_matrix_point(j, scalar, x, wv, a, rows, cols, n, npts, M);
+    write_exact(argv[10], M, n * npts);
     return 0;
   }
   if (mode == "tdma" || mode == "pdma") {

@@ -528,3 +528,112 @@ def test_general_banded(emu, offsets, n, outer, inner, cplx):
     assert rel(got, la.banded_solve(u, data, offsets, axis=1)) < 1e-14
     ref = np.einsum("ij,ojk->oik", np.linalg.inv(la.dia_dense(raw, offsets)), u)
     assert rel(got, ref) < 1e-12
+
+
+# ---- reference-signature programs (ref_progs.cuh) ---------------------------
+from oracle import refabi as RA  # noqa: E402
+
+_BIH_SHORT = (0, 2, 4, 2, 0, 2, 4, 2, 0, 2, 4)
+
+
+def _bih_diags(g, n):
+    """Random diagonals with a dominant main diagonal, lengths n - short."""
+    out = []
+    for q, short in enumerate(_BIH_SHORT):
+        main = q in (0, 4, 8)
+        out.append((3.0 + g.uniform(0, 1, n - short)) if main else g.uniform(-0.5, 0.5, n - short))
+    return out
+
+
+@pytest.mark.parametrize("M,outer,inner,cplx", [(5, 2, 1, 0), (6, 1, 3, 1), (9, 3, 2, 1), (33, 2, 5, 0)])
+def test_biharmonic_reference_layout(emu, M, outer, inner, cplx):
+    g = np.random.default_rng(M * 7 + inner)
+    n, N = 2 * M, 2 * M + 4
+    diags = _bih_diags(g, n)
+    a0 = 1.0
+    alfa = g.uniform(-3, 3, outer * inner)
+    beta = g.uniform(0.5, 4, outer * inner)
+    shape = (outer, N, inner)
+    f = g.standard_normal(shape) + (1j * g.standard_normal(shape) if cplx else 0)
+    res = run(emu, ["bih", outer, M, inner, cplx, repr(a0)], [alfa, beta] + diags + [f],
+              7 * 2 * outer * inner * M + f.size * (2 if cplx else 1))
+    fsz = 2 * outer * M * inner
+    got = [res[q * fsz:(q + 1) * fsz].reshape(2, outer, M, inner) for q in range(7)]
+    u = res[7 * fsz:]
+    u = (u.view(np.complex128) if cplx else u).reshape(shape)
+    ref = [np.zeros((2, outer, M, inner)) for _ in range(7)]
+    RA.lu_biharmonic(a0, alfa.reshape(outer, 1, inner), beta.reshape(outer, 1, inner), *diags, *ref[:5], axis=1)
+    RA.biharmonic_factor_pr(ref[5], ref[6], ref[3], ref[4], axis=1)
+    for q in range(7):
+        assert rel(got[q], ref[q]) < 1e-13, q
+    uo = f.copy()
+    RA.biharmonic_solve(f, uo, *ref, a0, axis=1)
+    assert rel(u, uo) < 1e-12
+    assert np.array_equal(u[:, n:], f[:, n:])  # entries past the dofs untouched
+
+
+@pytest.mark.parametrize("N,outer,inner,cplx", [(14, 1, 1, 0), (20, 2, 3, 1), (37, 3, 1, 1)])
+def test_biharmonic_matvec_reference_layout(emu, N, outer, inner, cplx):
+    g = np.random.default_rng(N)
+    M = N - 4
+    diags = _bih_diags(g, M)
+    alfa = g.uniform(-3, 3, outer * inner)
+    beta = g.uniform(0.5, 4, outer * inner)
+    shape = (outer, N, inner)
+    v = g.standard_normal(shape) + (1j * g.standard_normal(shape) if cplx else 0)
+    res = run(emu, ["bihmv", outer, N, inner, cplx, repr(1.5)], [alfa, beta] + diags + [v], v.size * (2 if cplx else 1))
+    b = (res.view(np.complex128) if cplx else res).reshape(shape)
+    ref = np.zeros_like(v)
+    RA.biharmonic_matvec(v, ref, 1.5, alfa.reshape(outer, 1, inner), beta.reshape(outer, 1, inner), *diags, axis=1)
+    assert rel(b, ref) < 1e-13
+
+
+_DMA = {"DiagMA": (0, 1), "TwoDMA": (1, 2), "ThreeDMA": (2, 3), "TDMA": (3, 3), "TDMA_O": (4, 3), "PDMA": (5, 5),
+        "FDMA": (6, 4), "HeptaDMA": (7, 7)}
+
+
+@pytest.mark.parametrize("name", list(_DMA))
+@pytest.mark.parametrize("per,skip", [(0, 0), (1, 1)])
+def test_dma_solves_reference_layout(emu, name, per, skip):
+    kind, rows = _DMA[name]
+    g = np.random.default_rng(kind * 11 + per)
+    outer, N, inner, cols = 3, 15, 2, 13
+    nsys = outer * inner
+    data = g.uniform(-0.3, 0.3, (nsys if per else 1, rows, cols))
+    mid = {"DiagMA": 0, "TwoDMA": 0, "ThreeDMA": 0, "TDMA": 1, "TDMA_O": 1, "PDMA": 2, "FDMA": 1, "HeptaDMA": 2}[name]
+    data[:, mid] = 2.0 + g.uniform(0, 1, (data.shape[0], cols))
+    u = g.standard_normal((outer, N, inner)) + 1j * g.standard_normal((outer, N, inner))
+    res = run(emu, ["dma", kind, rows, cols, outer, N, inner, 1, per, skip], [data, u], u.size * 2)
+    got = res.view(np.complex128).reshape(u.shape)
+    ref = u.copy()
+    lines = np.moveaxis(ref, 1, -1).reshape(-1, N)
+    for s in range(nsys):
+        if skip and s == 0:
+            continue
+        line = lines[s].copy()
+        RA.inner_solve(name, line, data[s if per else 0])
+        lines[s] = line
+    ref = np.moveaxis(lines.reshape(outer, inner, N), -1, 1)
+    assert rel(got, ref) < 1e-13
+
+
+@pytest.mark.parametrize("n,npts,rows", [(12, 12, 2), (17, 17, 3), (9, 20, 2)])
+@pytest.mark.parametrize("scalar", [0, 1])
+def test_legendre_recursion_matrix(emu, n, npts, rows, scalar):
+    if scalar and n != npts:
+        pytest.skip("the scalar product takes as many points as degrees")
+    g = np.random.default_rng(n + npts)
+    x = np.sort(g.uniform(-1, 1, npts))
+    w = g.uniform(0.1, 1, npts)
+    cols = max(n, npts) + 3
+    k = np.arange(cols, dtype=float)
+    # the Legendre recursion x L_k = k/(2k+1) L_{k-1} + (k+1)/(2k+1) L_{k+1} in DIA rows
+    a = np.zeros((rows, cols))
+    a[0] = (k + 1) / (2 * k + 1)
+    a[-1] = k / (2 * k + 1)
+    if rows == 3:
+        a[1] = g.uniform(-0.1, 0.1, cols)
+    res = run(emu, ["legrec", scalar, n, npts, rows, cols], [x, w, a], n * npts)
+    P = RA.legendre_matrix(x, a, n)
+    ref = (P * w).T if scalar else P
+    assert rel(res.reshape(ref.shape), ref) < 1e-14
