@@ -474,6 +474,16 @@ int sgpu_evaluate_expansion_all(const void* input, void* output, const double* x
                                 int64_t a_cols, int64_t outer, int64_t N, int64_t Nx, int64_t inner, int data_kind,
                                 void* work, size_t work_bytes, cudaStream_t stream);
 
+/* A dense matrix along an axis: out(l, k) [+]= s_l sum_j in(l, j) M[j][k] for
+ * every line l = (o, i) of in (outer, Nin, inner) and out (outer, Nout,
+ * inner); M is Nin x Nout (row-major, device); line_scale (optional) holds one
+ * factor per line in (outer, inner) order, complex (re, im pairs) for complex
+ * data; accumulate adds to out.  FP64 tiled GEMM.  Serves the generic
+ * SparseMatrix solve (la.py:823-840) and projections of expressions
+ * (forms/project.py:124-199), whose operators are dense along the axis. */
+int sgpu_line_gemm(const void* in, void* out, const double* M, int64_t Nin, int64_t Nout, int64_t outer,
+                   int64_t inner, int data_kind, const double* line_scale, int accumulate, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -367,8 +367,9 @@ def helmholtz_neumann_matvec(v, alfa, beta):
 
 def add_solve(b, A0, A2, scale, axis=0):
     """Poisson_Solve_ADD_1D_ptr (la.pyx:671-706) along axis: d = A[0],
-    d1 = A[2] (one value per row), N = len(d) dofs; boundary dofs 0
-    (ADDSolver.solve sets them, chebyshev/la.py:19-71)."""
+    d1 = A[2] (one value per row), N = len(d) dofs; the boundary rows keep
+    b's values (ADDSolver.solve copies b into u, chebyshev/la.py:17-20; a
+    Function's set_boundary_dofs zeroes them afterwards)."""
     u = np.array(b, copy=True)
     uv, bv = _mv(u, axis), _mv(np.asarray(b), axis)
     N = len(A0)
@@ -387,7 +388,6 @@ def add_solve(b, A0, A2, scale, axis=0):
         uv[k] /= d[k]
     if not abs(scale - 1) < 1e-8:
         uv[:N] /= scale
-    uv[N:] = 0
     return u
 
 

@@ -97,6 +97,7 @@ SIGNATURES = {
     "sgpu_Biharmonic_matvec": (_int, [_vp, _vp, _dbl] + [_vp] * 13 + [_i64, _i64, _i64, _i64, _int, _vp]),
     "sgpu_SolverGeneric1ND_solve_data": (_int, [_vp, _vp, _int, _int, _i64, _i64, _i64, _i64, _i64, _int, _vp]),
     "sgpu_DMA_Solve": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_line_gemm": (_int, [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _int, _vp, _int, _vp]),
     "sgpu_scalar_product": (_int, [_vp] * 5 + [_int, _i64, _i64, _i64, _i64, _int, _vp, ctypes.c_size_t, _vp]),
     "sgpu_evaluate_expansion_all": (_int, [_vp] * 4 + [_int, _i64, _i64, _i64, _i64, _i64, _int, _vp,
                                                        ctypes.c_size_t, _vp]),

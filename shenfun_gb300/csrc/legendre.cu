@@ -368,9 +368,11 @@ namespace {
 const int TM = 64, TN = 64, TK = 16;
 }
 
+// lscale (optional): one factor per line (complex lines: a complex factor,
+// re/im pairs) multiplying the line's result; accumulate: out += result.
 __global__ void __launch_bounds__(256) k_line_gemm_f64(const double* in, double* out, const double* M,
                                                        int Nin, int Nout, int64_t nrows, int64_t inner,
-                                                       int cplx) {
+                                                       int cplx, const double* lscale, int accumulate) {
   __shared__ double As[TK][TM + 1];
   __shared__ double Bs[TK][TN + 1];
   const int tid = threadIdx.x;
@@ -414,6 +416,32 @@ __global__ void __launch_bounds__(256) k_line_gemm_f64(const double* in, double*
     }
     __syncthreads();
   }
+  if (lscale) {
+    // a thread's 4 rows start at an even row, so (re, im) of a complex line
+    // are rows (0, 1) or (2, 3) of its block
+    if (cplx) {
+#pragma unroll
+      for (int pr = 0; pr < 2; ++pr) {
+        const int64_t row = row0 + tr * 4 + 2 * pr;
+        if (row >= nrows) continue;
+        const double sr = lscale[row], si = lscale[row + 1];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double re = acc[2 * pr][q], im = acc[2 * pr + 1][q];
+          acc[2 * pr][q] = sr * re - si * im;
+          acc[2 * pr + 1][q] = sr * im + si * re;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int64_t row = row0 + tr * 4 + i;
+        if (row >= nrows) continue;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[i][q] *= lscale[row];
+      }
+    }
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     int64_t row = row0 + tr * 4 + i;
@@ -421,21 +449,35 @@ __global__ void __launch_bounds__(256) k_line_gemm_f64(const double* in, double*
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       int col = col0 + tc * 4 + q;
-      if (col < Nout) out[off(row, col, Nout)] = acc[i][q];
+      if (col < Nout) {
+        double* o = out + off(row, col, Nout);
+        *o = accumulate ? *o + acc[i][q] : acc[i][q];
+      }
     }
   }
 }
 
 namespace sgpu {
 int line_gemm_f64(const double* in, double* out, const double* M, int Nin, int Nout, int64_t nrows,
-                  int64_t inner, int cplx, cudaStream_t stream) {
+                  int64_t inner, int cplx, cudaStream_t stream, const double* lscale, int accumulate) {
   if (nrows == 0) return SGPU_OK;
   if ((nrows + TM - 1) / TM > 0x7fffffff || Nin < 1 || Nout < 1) return SGPU_ERR_ARG;
   dim3 grid((unsigned)((nrows + TM - 1) / TM), (unsigned)((Nout + TN - 1) / TN));
-  k_line_gemm_f64<<<grid, 256, 0, stream>>>(in, out, M, Nin, Nout, nrows, inner, cplx);
+  k_line_gemm_f64<<<grid, 256, 0, stream>>>(in, out, M, Nin, Nout, nrows, inner, cplx, lscale, accumulate);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 }  // namespace sgpu
+
+extern "C" int sgpu_line_gemm(const void* in, void* out, const double* M, int64_t Nin, int64_t Nout,
+                              int64_t outer, int64_t inner, int data_kind, const double* line_scale,
+                              int accumulate, cudaStream_t stream) {
+  if (!in || !out || !M || in == out || outer < 0 || inner < 1 || Nin < 1 || Nout < 1) return SGPU_ERR_ARG;
+  if (Nin > 0x7fffffff || Nout > 0x7fffffff) return SGPU_ERR_ARG;
+  if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
+  const int cplx = data_kind == SGPU_COMPLEX;
+  return sgpu::line_gemm_f64((const double*)in, (double*)out, M, (int)Nin, (int)Nout, outer * inner * (1 + cplx),
+                             inner, cplx, stream, line_scale, accumulate ? 1 : 0);
+}
 
 // mass solve along lines after the scalar product (forward transform)
 template <class T>
@@ -498,7 +540,8 @@ static int legendre_run(const sgpu_legendre_plan* p, int direction, const void* 
     dim3 grid((unsigned)((nrows + TM - 1) / TM), (unsigned)((p->N + TN - 1) / TN));
     if ((nrows + TM - 1) / TM > 0x7fffffff) return SGPU_ERR_ARG;
     const double* M = direction == 2 ? p->d_back : p->d_scalar;
-    k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, p->N, nrows, inner, cplx);
+    k_line_gemm_f64<<<grid, 256, 0, stream>>>((const double*)in, (double*)out, M, p->N, p->N, nrows, inner, cplx,
+                                              nullptr, 0);
   }
   if (direction == 1 && p->form != SGPU_MIXED_DF) {
     const unsigned nb = (unsigned)((nlines + 127) / 128);

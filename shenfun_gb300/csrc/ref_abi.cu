@@ -12,7 +12,7 @@ using namespace sgpu::ref;
 
 namespace sgpu {
 int line_gemm_f64(const double* in, double* out, const double* M, int Nin, int Nout, int64_t nrows,
-                  int64_t inner, int cplx, cudaStream_t stream);
+                  int64_t inner, int cplx, cudaStream_t stream, const double* lscale, int accumulate);
 }
 
 namespace {
@@ -193,7 +193,7 @@ int legendre_recursive(int scalar, const void* in, void* out, const double* x, c
   const int64_t nrows = outer * inner * (data_kind == SGPU_COMPLEX ? 2 : 1);
   if (st == SGPU_OK)
     st = line_gemm_f64((const double*)in, (double*)out, M, (int)Nin, (int)Nout, nrows, inner,
-                       data_kind == SGPU_COMPLEX, stream);
+                       data_kind == SGPU_COMPLEX, stream, nullptr, 0);
   if (own && cudaFreeAsync(M, stream) != cudaSuccess && st == SGPU_OK) st = SGPU_ERR_CUDA;
   return st;
 }

@@ -366,8 +366,10 @@ SGPU_HD void poisson_add_prog(const T* b_all, T* u_all, double scale, int64_t Nb
   }
   if (!(scale - 1.0 < 1e-8 && scale - 1.0 > -1e-8))
     for (int64_t k = 0; k < N; ++k) u[k] = divr(u[k], scale);
-  u[N] = zero_of(T());
-  u[N + 1] = zero_of(T());
+  // ADDSolver.solve copies b into u and the kernel solves the N - 2 dofs
+  // (chebyshev/la.py:17-20, la.pyx:671-706): the two boundary rows keep b's
+  u[N] = b[N];
+  u[N + 1] = b[N + 1];
 }
 
 // ANNSolver.__call__ (chebyshev/la.py:77-128): A u = b with A = scale * ASNSN,

@@ -2,16 +2,19 @@
 inner and project (forms/arguments.py, forms/inner.py, forms/project.py).
 
 Only what the hot path needs is provided: linear forms ``inner(v, Array)``
-(the scalar product transform) and bilinear forms built from constant
-multiples of derivatives of the trial function, which assemble into
-``TPMatrix`` objects with per-wavenumber scale arrays (the reference's
-``get_simplified_tpmatrices`` result, matrixbase.py:1648-1678).
+(the scalar product transform) and ``inner(v, expr)`` with ``expr`` a
+constant-coefficient combination of derivatives of a Function, bilinear forms
+built from constant multiples of derivatives of the trial function, which
+assemble into ``TPMatrix`` objects with per-wavenumber scale arrays (the
+reference's ``get_simplified_tpmatrices`` result, matrixbase.py:1648-1678),
+and ``project`` of Arrays, Functions and such expressions.
 """
 import numbers
 
 import numpy as np
 import torch
 
+from . import _lib
 from .spaces import TensorProductSpace, FourierBase, SpectralBase
 from . import matrices as M
 
@@ -130,6 +133,9 @@ class Expr:
 
     def __add__(self, other):
         other = _as_expr(other)
+        a, b = getattr(self.basis, "function", None), getattr(other.basis, "function", None)
+        if (a is None) != (b is None) or (a is not None and a.data_ptr() != b.data_ptr()):
+            raise NotImplementedError("a sum of expressions of different arguments")
         assert other.basis is self.basis or other.basis.space is self.basis.space
         return Expr(self.basis, self.terms + other.terms)
 
@@ -166,9 +172,20 @@ def TrialFunction(space):
     return BasisFunction(space, 1)
 
 
+class FunctionBasis(BasisFunction):
+    """A Function in a form: argument 2, the expansion it holds
+    (forms/arguments.py:1204-1230, Function as a BasisFunction)."""
+
+    def __init__(self, function):
+        self.function = function
+        BasisFunction.__init__(self, function.function_space(), 2)
+
+
 def _as_expr(e):
     if isinstance(e, Expr):
         return e
+    if isinstance(e, Function):
+        return FunctionBasis(e)
     raise TypeError(f"cannot use {type(e)} in a form")
 
 
@@ -246,7 +263,7 @@ def _bilinear(test, expr):
         for m, c in out.values():
             m.scale = c
             res.append(m)
-        return res
+        return res[0] if len(res) == 1 else res
     np_axes = T.get_nonperiodic_axes()
     if len(np_axes) != 1:
         raise NotImplementedError("exactly one non-periodic axis is on the GPU path")
@@ -274,12 +291,52 @@ def _bilinear(test, expr):
         if np.abs(sc.imag).max() > 0:
             raise NotImplementedError("odd derivatives along Fourier axes")
         out.append(TPMatrix(M.galerkin_matrix(base, order), np.ascontiguousarray(sc.real), T, ax))
-    return out
+    return out[0] if len(out) == 1 else out
+
+
+def _expr_apply(T, expr, solve, output_array=None):
+    """The linear form (phi_k, expr)_w of an expression of one Function uh
+    (forms/inner.py:483-497, the matvecs of the assembled matrices) or, with
+    ``solve``, its projection u = B^{-1} (phi_k, expr)_w (forms/project.py:
+    124-199), on the GPU: one line GEMM (sgpu_line_gemm, per-line scales,
+    accumulating) per derivative order along the line axis, with the host
+    operators of operators.expr_plan."""
+    from .device import ptr, stream_handle, view3, require_cuda
+    from .operators import expr_plan
+    require_cuda()
+    fb = expr.basis
+    src = fb.function.v
+    ax, out_shape, cplx, terms = expr_plan(T, fb.space, expr.terms, solve, src.is_complex())
+    dt = torch.complex128 if cplx else torch.float64
+    if src.dtype != dt:
+        src = src.to(dt)
+    src = src.contiguous()
+    if output_array is None:
+        output_array = Function(T)
+    out = torch.zeros(out_shape, dtype=dt, device=src.device)
+    o_in, n_in, i_in = view3(tuple(src.shape), ax)
+    o_out, n_out, i_out = view3(tuple(out.shape), ax)
+    if (o_in, i_in) != (o_out, i_out):
+        raise _lib.SgpuError(_lib.ERR_ARG, "the Function does not match the space off the line axis")
+    for Mat, scale in terms:
+        Md = torch.as_tensor(np.ascontiguousarray(Mat), device=src.device)
+        sd = torch.as_tensor(scale, device=src.device)
+        # Md, sd live on the current stream: the caching allocator reuses their
+        # memory only after this launch in stream order
+        _lib.call("sgpu_line_gemm", ptr(src), ptr(out), ptr(Md), n_in, n_out, o_in, i_in,
+                  _lib.COMPLEX if cplx else _lib.REAL, ptr(sd), 1, stream_handle())
+    dst = output_array.v if isinstance(output_array, _ShenfunArray) else output_array
+    dst.copy_(out if dst.is_complex() else out.real)
+    return output_array
 
 
 def inner(test, trial, output_array=None, kind=None):
     """Scalar product (linear form) or matrix assembly (bilinear form)
     (forms/inner.py:16-511)."""
+    if isinstance(test, BasisFunction) and isinstance(trial, (Function, FunctionBasis)) or (
+            isinstance(test, BasisFunction) and isinstance(trial, Expr) and
+            getattr(trial.basis, "argument", 1) == 2):
+        return _expr_apply(test.function_space(), _as_expr(trial), False, output_array)
     if isinstance(test, BasisFunction) and isinstance(trial, torch.Tensor):
         T = test.function_space()
         if output_array is None:
@@ -296,8 +353,15 @@ def inner(test, trial, output_array=None, kind=None):
 
 
 def project(uh, T, output_array=None):
-    """Projection of an Array on the space's mesh: the forward transform
-    (forms/project.py:117-122)."""
+    """Projection on T (forms/project.py:16-199): an Array on T's mesh is
+    forward transformed (:117-122); a Function or an expression of one
+    (derivatives with constant coefficients) is projected with the mass
+    solve, u = B^{-1} (v, uh) (:124-199), on the GPU."""
+    if isinstance(uh, (Function, Expr)):
+        expr = _as_expr(uh)
+        if getattr(expr.basis, "argument", None) != 2:
+            raise ValueError("project takes an Array, a Function or an expression of a Function")
+        return _expr_apply(T, expr, True, output_array)
     if output_array is None:
         output_array = Function(T)
     src = uh.v if isinstance(uh, _ShenfunArray) else uh

@@ -39,7 +39,7 @@ class _HelmholtzForm:
     derivative, B = BSDSDmat / BSNSNmat)."""
 
     def __init__(self, mats, T):
-        mats = list(mats)
+        mats = [mats] if isinstance(mats, TPMatrix) else list(mats)
         keys = {m.get_key() for m in mats}
         self.neumann = keys <= {"ASNSNmat", "BSNSNmat"}
         if not (keys <= {"ASDSDmat", "BSDSDmat"} or self.neumann):

@@ -11,7 +11,7 @@ import torch
 
 from . import _lib
 from .device import ptr, stream_handle, view3, data_kind, require_cuda
-from .forms import TPMatrix, _ShenfunArray
+from .forms import Function, TPMatrix, _ShenfunArray
 from .matrices import SpectralMatrix
 
 
@@ -38,7 +38,37 @@ def _band_data(mat, offsets):
     return data
 
 
-class _BandedSolver:
+def _as_list(mats):
+    """A form's matrices: inner() returns one matrix for a one-term form and a
+    list otherwise (forms/inner.py:497-499)."""
+    if isinstance(mats, (TPMatrix, SpectralMatrix)):
+        return [mats]
+    return list(mats)
+
+
+def _constraint_rows(b, axis, constraints):
+    """b[T.si[row]] = val for every constraint (la.py:124-129)."""
+    for row, val in constraints:
+        b.select(axis, int(row)).fill_(val)
+
+
+class _Constrained:
+    """Solvers factorise at construction; a call with constraints refactors
+    once from the matrix with those rows made identity rows
+    (SparseMatrixSolver.apply_constraints, la.py:77-130)."""
+
+    _cons = ()
+
+    def _check_constraints(self, constraints):
+        cons = tuple((int(r), v) for r, v in constraints)
+        if cons and tuple(r for r, _ in cons) != tuple(r for r, _ in self._cons):
+            from .matrices import constrained
+            self._factor(constrained(self.mat, cons))
+            self._cons = cons
+        return cons
+
+
+class _BandedSolver(_Constrained):
     offsets = None
     lu_entry = None
     solve_entry = None
@@ -49,12 +79,16 @@ class _BandedSolver:
             mat = mat[0] if len(mat) == 1 else _sum_mats(mat)
         self.mat = mat
         self.n = mat.shape[0]
+        self._factor(mat)
+
+    def _factor(self, mat):
         data = _band_data(mat, self.offsets)
         self._lu = torch.as_tensor(data, device="cuda").contiguous()
         _lib.call(self.lu_entry, ptr(self._lu), self.n, stream_handle())
 
     def __call__(self, b, u=None, axis=0, constraints=()):
         b = _raw(b)
+        _constraint_rows(b, axis, self._check_constraints(constraints))
         if u is None:
             u = b
         else:
@@ -93,7 +127,7 @@ class PDMA(_BandedSolver):
     solve_entry = "sgpu_PDMA_Solve"
 
 
-class _GeneralBanded:
+class _GeneralBanded(_Constrained):
     """Banded solver for the reference's other band patterns (la.py:291-800):
     LU once on the device (sgpu_banded_LU), solve per call (sgpu_banded_Solve)
     along any axis, in place; the dofs are the first n entries along it."""
@@ -106,6 +140,9 @@ class _GeneralBanded:
             mat = mat[0] if len(mat) == 1 else _sum_mats(mat)
         self.mat = mat
         self.n = mat.shape[0]
+        self._factor(mat)
+
+    def _factor(self, mat):
         data = self._prepare(_band_data(mat, self.offsets))
         self._lu = torch.as_tensor(data, device="cuda").contiguous()
         self._off = (ctypes.c_int * len(self.offsets))(*self.offsets)
@@ -117,6 +154,7 @@ class _GeneralBanded:
 
     def __call__(self, b, u=None, axis=0, constraints=()):
         b = _raw(b)
+        _constraint_rows(b, axis, self._check_constraints(constraints))
         if u is None:
             u = b
         else:
@@ -168,6 +206,53 @@ class FDMA(_GeneralBanded):
 class HeptaDMA(_GeneralBanded):
     """Offsets -4, -2, 0, 2, 4, 6, 8 (la.py:711-800)."""
     offsets = (-4, -2, 0, 2, 4, 6, 8)
+
+
+class TDMA_O(_GeneralBanded):
+    """Symmetric tridiagonal with offsets -1, 0, 1 (la.py:396-447)."""
+    offsets = (-1, 0, 1)
+
+
+class Solve(_Constrained):
+    """Generic solver for a matrix without a tailored band pattern
+    (la.py:823-840).  The reference factorises with scipy's splu and solves
+    on the host; here the (constrained) matrix is inverted once on the host in
+    FP64 and every solve applies the inverse along the axis with the FP64 line
+    GEMM on the GPU (sgpu_line_gemm); the dofs are the first n entries."""
+
+    def __init__(self, mats, format=None):
+        require_cuda()
+        if isinstance(mats, list):
+            mats = mats[0] if len(mats) == 1 else _sum_mats(mats)
+        self.mat = mats
+        self.n = mats.shape[0]
+        self._factor(mats)
+
+    def _factor(self, mat):
+        sc = np.asarray(mat.scale, dtype=float)
+        if sc.size != 1:
+            raise _lib.SgpuError(_lib.ERR_ARG, "Solve: the matrix scale must be a scalar")
+        dense = mat.todense() * float(sc.reshape(-1)[0])
+        inv = np.linalg.inv(dense)
+        # sgpu_line_gemm computes out(l, k) = sum_j in(l, j) M[j][k]
+        self._M = torch.as_tensor(np.ascontiguousarray(inv.T), device="cuda")
+
+    def __call__(self, b, u=None, axis=0, constraints=()):
+        b = _raw(b)
+        _constraint_rows(b, axis, self._check_constraints(constraints))
+        ur = b if u is None else _raw(u)
+        outer, N, inner = view3(tuple(b.shape), axis)
+        if N < self.n:
+            raise _lib.SgpuError(_lib.ERR_ARG, "array shorter than the matrix along axis")
+        src = b.narrow(axis, 0, self.n).contiguous()
+        if src.data_ptr() == b.data_ptr() and ur.data_ptr() == b.data_ptr():
+            src = src.clone()
+        dst = torch.empty_like(src)
+        o2, _, i2 = view3(tuple(src.shape), axis)
+        _lib.call("sgpu_line_gemm", ptr(src), ptr(dst), ptr(self._M), self.n, self.n, o2, i2, data_kind(src),
+                  None, 0, stream_handle())
+        ur.narrow(axis, 0, self.n).copy_(dst)
+        return b if u is None else u
 
 
 def _sum_mats(mats):
@@ -332,7 +417,7 @@ class SolverGeneric1ND:
     la.py:1299-1364)."""
 
     def __init__(self, mats):
-        mats = list(mats)
+        mats = _as_list(mats)
         T = mats[0].space
         ax = mats[0].axis
         base = T.bases[ax]
@@ -367,7 +452,7 @@ class BandSepSolver:
     def __init__(self, mats, form="plain", tol=1e-13, max_it=8):
         from .matrices import band_sep_term
         require_cuda()
-        mats = sorted(list(mats), key=lambda m: -m.pmat.order)
+        mats = sorted(_as_list(mats), key=lambda m: -m.pmat.order)
         T, ax = mats[0].space, mats[0].axis
         base = T.bases[ax]
         self.T, self.axis, self.N = T, ax, base.N
@@ -487,7 +572,11 @@ class ADDSolver(_PoissonSolver):
     entry = "sgpu_Poisson_Solve_ADD"
 
     def __call__(self, b, u=None, axis=0, constraints=()):
-        return self._run(b, u, axis)
+        out = self._run(b, u, axis)
+        if isinstance(out, Function) and not getattr(out.function_space(), "has_nonhomogeneous_bcs", False):
+            # u.set_boundary_dofs() of a homogeneous space (la.py:265-266)
+            _raw(out).narrow(axis, self.N - 2, 2).zero_()
+        return out
 
 
 class ANNSolver(_PoissonSolver):

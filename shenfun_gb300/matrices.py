@@ -30,9 +30,20 @@ class SpectralMatrix(dict):
         self.trialfunction = (trial, 0)
         self.upper_rows = upper_rows
         self.scale = 1.0
+        self.solver = None
+        self.constrained_rows = ()
 
     def get_key(self):
         return self.key
+
+    @property
+    def issymmetric(self):
+        offs = set(self.keys())
+        if any(-o not in offs for o in offs) or self.upper_rows is not None:
+            return False
+        n = self.shape[0]
+        return all(np.allclose(np.broadcast_to(np.atleast_1d(self[o]), (n - abs(o),)),
+                               np.broadcast_to(np.atleast_1d(self[-o]), (n - abs(o),))) for o in offs if o > 0)
 
     def todense(self):
         M = np.zeros(self.shape)
@@ -45,7 +56,70 @@ class SpectralMatrix(dict):
                 for j in range(i + 2, n, 2):
                     if j - i not in self:
                         M[i, j] = self.upper_rows(i, j)
+        for row in self.constrained_rows:
+            diag = M[row, row]
+            M[row, :] = 0.0
+            M[row, row] = diag
         return M
+
+    def get_solver(self):
+        """The solver class for this matrix (matrixbase.py:439-474): the
+        overrides of the Chebyshev / Legendre matrix classes
+        (chebyshev/matrices.py:248, 403, 530, 1081, 1124; legendre/matrices.py:
+        136, 191), else by band pattern, else the generic ``la.Solve``."""
+        from . import la
+        if np.all(np.asarray(self.scale) == 0):
+            return la.Solve
+        space = self.testfunction[0]
+        fam = space.family() if space is not None else None
+        over = {"chebyshev": {"BSDSDmat": la.TDMA, "BSNSNmat": la.TDMA, "BSBSBmat": la.PDMA,
+                              "ASDSDmat": la.ADDSolver, "ASNSNmat": la.ANNSolver},
+                "legendre": {"BSDSDmat": la.TDMA, "BSBSBmat": la.PDMA}}.get(fam, {})
+        if self.key in over:
+            return over[self.key]
+        if self.upper_rows is not None:
+            return la.Solve
+        keys = tuple(sorted(int(k) for k in self.keys()))
+        if keys == (-1, 0, 1) and self.issymmetric:
+            return la.TDMA_O
+        return {(0,): la.DiagMA, (0, 2): la.TwoDMA, (-2, 0, 2): la.TDMA, (0, 2, 4): la.ThreeDMA,
+                (-2, 0, 2, 4): la.FDMA, (-4, -2, 0, 2, 4): la.PDMA,
+                (-4, -2, 0, 2, 4, 6, 8): la.HeptaDMA}.get(keys, la.Solve)
+
+    def solve(self, b, u=None, axis=0, constraints=()):
+        """Solve self u = b along axis (matrixbase.py:410-437); the solver is
+        created on the first call and kept."""
+        if self.solver is None:
+            self.solver = self.get_solver()(self)
+        return self.solver(b, u=u, axis=axis, constraints=constraints)
+
+
+def constrained(mat, constraints):
+    """A copy of ``mat`` with the rows of ``constraints`` ((row, value)
+    pairs) made identity rows, as SparseMatrixSolver.apply_constraints does
+    for a SparseMatrix (la.py:77-130): the row's diagonal entry becomes
+    1/scale and its other stored entries 0 (a dense upper part too)."""
+    n = mat.shape[0]
+    d = {k: np.array(np.broadcast_to(np.atleast_1d(np.asarray(v, dtype=float)), (n - abs(k),)))
+         for k, v in mat.items()}
+    A = SpectralMatrix(mat.key, d, mat.shape, mat.testfunction[0], mat.trialfunction[0], mat.upper_rows)
+    A.scale = mat.scale
+    for attr in ("order", "sign"):
+        if hasattr(mat, attr):
+            setattr(A, attr, getattr(mat, attr))
+    sc = float(np.asarray(mat.scale).reshape(-1)[0])
+    rows = []
+    for row, _ in constraints:
+        row = int(row)
+        for key, v in A.items():
+            if key >= 0:
+                if row < n - key:
+                    v[row] = float(key == 0) / sc
+            elif 0 < row + key < n + key:
+                v[row + key] = 0.0
+        rows.append(row)
+    A.constrained_rows = tuple(rows)
+    return A
 
 
 def cheb_norm_sq(N):

@@ -644,10 +644,74 @@ def optmode():
     print("optmode:", len(calls), "calls:", sorted({c["name"] for c in calls}))
 
 
+# --------------------------------------------------------------------------
+# project of Functions and of expressions (forms/project.py:124-199), linear
+# forms of expressions (forms/inner.py:483-497), and SpectralMatrix.solve
+# through get_solver (matrixbase.py:410-474).  Own rng.
+def project_group():
+    from shenfun import project
+    g = np.random.default_rng(515)
+    d = {}
+
+    def fn(space, ndof):
+        uh = Function(space)
+        uh[:ndof] = g.standard_normal(ndof)
+        return uh
+
+    SD = FunctionSpace(14, "C", bc=(0, 0))
+    SB = FunctionSpace(16, "C", bc=(0, 0, 0, 0))
+    SN = FunctionSpace(14, "C", bc={"left": {"N": 0}, "right": {"N": 0}})
+    T14, T16 = FunctionSpace(14, "C"), FunctionSpace(16, "C")
+    u = fn(SD, 12)
+    d.update(sd_u=u, sd_dx_T=project(Dx(u, 0, 1), T14), sd_dxx_SD=project(Dx(u, 0, 2), SD),
+             sd_u_T=project(u, T14), sd_lap_T=project(div(grad(u)), T14),
+             sd_inner_dxx=inner(TestFunction(SD), Dx(u, 0, 2)), sd_inner_u_T=inner(TestFunction(T14), u))
+    ub = fn(SB, 12)
+    d.update(sb_u=ub, sb_d3_T=project(Dx(ub, 0, 3), T16), sb_lap_SB=project(div(grad(ub)), SB))
+    un = fn(SN, 12)
+    d.update(sn_u=un, sn_dx_T=project(Dx(un, 0, 1), T14))
+    LSD, L14 = FunctionSpace(14, "L", bc=(0, 0)), FunctionSpace(14, "L")
+    ul = fn(LSD, 12)
+    d.update(l_u=ul, l_dx_L=project(Dx(ul, 0, 1), L14), l_dxx_SD=project(Dx(ul, 0, 2), LSD))
+    F0 = FunctionSpace(6, "F", dtype="D")
+    F1 = FunctionSpace(8, "F", dtype="d")
+    T3 = TensorProductSpace(comm, (F0, F1, SD))
+    T3o = TensorProductSpace(comm, (F0, F1, T14))
+    u3 = Function(T3)
+    u3[..., :12] = g.standard_normal(u3[..., :12].shape) + 1j * g.standard_normal(u3[..., :12].shape)
+    d.update(t3_u=u3, t3_dz_T=project(Dx(u3, 2, 1), T3o), t3_lap=project(div(grad(u3)), T3),
+             t3_mix=project(Dx(u3, 0, 1) + 2 * Dx(u3, 1, 2), T3),
+             t3_inner_lap=inner(TestFunction(T3), div(grad(u3))))
+    FF = TensorProductSpace(comm, (F0, F1))
+    uf = Function(FF, buffer=g.standard_normal(FF.shape(True)) + 1j * g.standard_normal(FF.shape(True)))
+    d.update(ff_u=uf, ff_d=project(Dx(uf, 1, 1) - Dx(uf, 0, 2), FF))
+    # SpectralMatrix.solve through get_solver
+    for name, space in (("csd", SD), ("csb", SB), ("csn", SN), ("lsd", LSD)):
+        v, w = TestFunction(space), TrialFunction(space)
+        forms = {"B": inner(v, w), "A": inner(v, div(grad(w)))}
+        if name == "csb":
+            forms["S"] = inner(v, div(grad(div(grad(w)))))
+        for key, mat in forms.items():
+            N = space.N
+            for shape, ax in (((N,), 0), ((N, 3), 0), ((4, N), 1)):
+                b = g.standard_normal(shape) + 1j * g.standard_normal(shape)
+                cons = ((0, 0),) if (name == "csn" and key == "A") else ()
+                try:
+                    x = mat.solve(b.copy(), axis=ax, constraints=cons) if cons else mat.solve(b.copy(), axis=ax)
+                except Exception:
+                    continue
+                tag = f"ms_{name}{key}_{len(shape)}d{ax}"
+                d.update({tag + "_b": b, tag + "_x": np.array(x)})
+                d[tag + "_solver"] = np.array(type(mat.solver).__name__)
+                mat.solver = None
+    put("project", **d)
+
+
 GROUPS = {"cheb_1d": cheb_1d, "fourier_1d": fourier_1d, "banded": banded, "helmholtz": helmholtz,
           "roundtrips": roundtrips, "biharmonic": biharmonic, "legendre": legendre, "imex": imex,
           "dealias": dealias, "neumann": neumann,
-          "nonhomog": nonhomog, "dma": dma, "optmode": optmode}
+          "nonhomog": nonhomog, "dma": dma, "optmode": optmode,
+          "project": project_group}
 
 if __name__ == "__main__":
     # no arguments: every group (the shared rng makes the earlier groups depend
