@@ -131,11 +131,15 @@ int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64
  * it does not run
  * in place: sgpu_plan_execute_ws returns SGPU_ERR_ARG for in == out there,
  * and sgpu_plan_execute goes through a stream-ordered temporary output. */
-/* Tile width of that kernel: 1 = 64-line tiles with one TMEM accumulator set,
- * 2 = 32-line tiles with two (the next tile's MMAs overlap this tile's
- * epilogue); 0 = the library's default (1).  SGPU_ERR_UNSUPPORTED for plans
- * that do not use the fused kernel.  get returns 0 for them.  No counterpart
- * in the reference (a tuning knob of this library's kernels). */
+/* Kernel variant of a plan.  Fused-contraction plans: 1 = 64-line tiles with
+ * one TMEM accumulator set, 2 = 32-line tiles with two (the next tile's MMAs
+ * overlap this tile's epilogue).  Length-256 Fourier plans (R2C, C2R, C2C):
+ * 1 = the strided-pass kernel for axes with inner >= 16 (pass 1 and pass 2
+ * of a 16 x 16 register FFT reading and writing global memory directly, one
+ * shared-memory transpose), 2 = the generic line programs.  0 = the
+ * library's default (1).  SGPU_ERR_UNSUPPORTED for other plans; get returns
+ * 0 for them.  No counterpart in the reference (a tuning knob of this
+ * library's kernels). */
 int sgpu_plan_set_variant(sgpu_plan* plan, int variant);
 int sgpu_plan_get_variant(const sgpu_plan* plan, int* variant);
 

@@ -27,7 +27,13 @@ struct sgpu_plan {
   oz::Matrix tc;     // tensor form: the line operator, split (any line layout)
   bool fused = false;
   lc::Matrix fm;     // the same operator for the fused contraction (contiguous lines)
+  int fvariant = 1;  // length-256 Fourier plans: 1 strided-pass kernel, 2 generic line programs
 };
+
+namespace sgpu {
+int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines, int64_t inner, double scl,
+                cudaStream_t s);
+}
 
 namespace {
 
@@ -184,16 +190,30 @@ extern "C" int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, in
 }
 
 
+namespace {
+bool fourier256(const sgpu_plan* plan) {
+  const LinePlan& p = plan->lp;
+  return !plan->tensor && p.n == 256 && p.m == 256 && !p.rader &&
+         (p.kind == SGPU_XF_R2C || p.kind == SGPU_XF_C2R || p.kind == SGPU_XF_C2C_FWD || p.kind == SGPU_XF_C2C_BWD);
+}
+}  // namespace
+
 extern "C" int sgpu_plan_set_variant(sgpu_plan* plan, int variant) {
   if (!plan || variant < 0 || variant > 2) return SGPU_ERR_ARG;
-  if (!plan->fused) return variant == 0 ? SGPU_OK : SGPU_ERR_UNSUPPORTED;
-  plan->fm.variant = variant == 0 ? 1 : variant;
-  return SGPU_OK;
+  if (plan->fused) {
+    plan->fm.variant = variant == 0 ? 1 : variant;
+    return SGPU_OK;
+  }
+  if (fourier256(plan)) {
+    plan->fvariant = variant == 0 ? 1 : variant;
+    return SGPU_OK;
+  }
+  return variant == 0 ? SGPU_OK : SGPU_ERR_UNSUPPORTED;
 }
 
 extern "C" int sgpu_plan_get_variant(const sgpu_plan* plan, int* variant) {
   if (!plan || !variant) return SGPU_ERR_ARG;
-  *variant = plan->fused ? plan->fm.variant : 0;
+  *variant = plan->fused ? plan->fm.variant : (fourier256(plan) ? plan->fvariant : 0);
   return SGPU_OK;
 }
 
@@ -219,6 +239,10 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
   if (in == out && p.n_in != p.n_out) return SGPU_ERR_ARG;
   const int64_t nlines = outer * inner;
   if (nlines == 0) return SGPU_OK;
+  if (plan->fvariant == 1 && fourier256(plan) && inner >= 16) {
+    const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, stream);
+    if (st != SGPU_ERR_UNSUPPORTED) return st;
+  }
   const int lpb = lines_per_block(p, data_complex_for(p, data_kind));
   const int64_t nblocks = (nlines + lpb - 1) / lpb;
   if (nblocks > 0x7fffffffLL) return SGPU_ERR_ARG;

@@ -30,6 +30,18 @@ class LinePlan:
         except Exception:
             pass
 
+    @property
+    def variant(self):
+        """The plan's kernel variant (sgpu_plan_get_variant; 0 where the plan
+        has a single kernel)."""
+        v = ctypes.c_int()
+        _lib.call("sgpu_plan_get_variant", self._h, ctypes.byref(v))
+        return v.value
+
+    @variant.setter
+    def variant(self, v):
+        _lib.call("sgpu_plan_set_variant", self._h, int(v))
+
     def __call__(self, inp, out, axis, scale=1.0, stream=None):
         """Transform `inp` into `out` along `axis` (both C-contiguous CUDA tensors)."""
         outer, n_in, inner = view3(tuple(inp.shape), axis)

@@ -30,6 +30,7 @@
 #include "../../shenfun_gb300/csrc/ozaki.cuh"
 #include "../../shenfun_gb300/csrc/lc_fused.cuh"
 #include "../../shenfun_gb300/csrc/ref_progs.cuh"
+#include "../../shenfun_gb300/csrc/fft256.cuh"
 
 using namespace sgpu;
 
@@ -103,6 +104,76 @@ static int xform(int argc, char** argv) {
     free(smem);
   }
   write_exact(argv[10], out, nout);
+  free(in);
+  free(out);
+  free(img);
+  return 0;
+}
+
+// Strided length-256 Fourier passes (fft256.cuh): every thread of a CTA runs
+// each phase in turn, with the CTA's barriers between the phases.
+template <class R>
+static void f256_block(int kind, const LinePlan& p, const f256::Args& a, int64_t blk, Cx<R>* Z) {
+  using namespace f256;
+  for (int t = 0; t < NT; ++t) {
+    switch (kind) {
+      case C2C_FWD: pass1<R, C2C_FWD>(p, a, blk, Z, t); break;
+      case C2C_BWD: pass1<R, C2C_BWD>(p, a, blk, Z, t); break;
+      case R2C: pass1<R, R2C>(p, a, blk, Z, t); break;
+      default: pass1<R, C2R>(p, a, blk, Z, t); break;
+    }
+  }
+  static Cx<R> v[NT][16];
+  for (int t = 0; t < NT; ++t) pass2_dft<R>(Z, t, v[t]);
+  if (kind == R2C) {
+    for (int t = 0; t < NT; ++t) r2c_stash<R>(Z, t, v[t]);
+    for (int t = 0; t < NT; ++t) r2c_post<R>(a, blk, Z, t, NT);
+    return;
+  }
+  for (int t = 0; t < NT; ++t) {
+    switch (kind) {
+      case C2C_FWD: pass2_store<R, C2C_FWD>(a, blk, t, v[t]); break;
+      case C2C_BWD: pass2_store<R, C2C_BWD>(a, blk, t, v[t]); break;
+      default: pass2_store<R, C2R>(a, blk, t, v[t]); break;
+    }
+  }
+}
+
+static int f256_mode(int argc, char** argv) {
+  // f256 kind outer inner scl in out   (kind: SGPU_XF_*; form from SGPU_EMU_FORM)
+  if (argc < 8) return 2;
+  const int xk = atoi(argv[2]);
+  long long outer = atoll(argv[3]), inner = atoll(argv[4]);
+  double scl = atof(argv[5]);
+  const int form = getenv("SGPU_EMU_FORM") ? atoi(getenv("SGPU_EMU_FORM")) : SGPU_PLAIN_F64;
+  LinePlan p;
+  HostTables T;
+  if (build_plan_host(xk, 256, 0, form, p, T) != SGPU_OK) return 3;
+  size_t off[SGPU_NTAB];
+  unsigned char* img = (unsigned char*)malloc(table_layout(T, off));
+  table_image(T, off, img);
+  bind_tables(p, T, off, img);
+  int kind = xk == SGPU_XF_C2C_FWD ? f256::C2C_FWD : xk == SGPU_XF_C2C_BWD ? f256::C2C_BWD
+             : xk == SGPU_XF_R2C ? f256::R2C : f256::C2R;
+  const int in_c = kind != f256::R2C, out_c = kind != f256::C2R;
+  const size_t nin = (size_t)outer * p.n_in * inner * (in_c ? 2 : 1);
+  const size_t nout = (size_t)outer * p.n_out * inner * (out_c ? 2 : 1);
+  double* in = read_exact(argv[6], nin);
+  double* out = (double*)malloc(sizeof(double) * nout);
+  for (size_t i = 0; i < nout; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
+  f256::Args a{in, out, outer * inner, inner, scl};
+  const int64_t nt = f256::tiles(kind, a.nlines);
+  const size_t zb = form == SGPU_MIXED_DF ? f256::smem_bytes<df>() : f256::smem_bytes<double>();
+  void* Z = malloc(zb);
+  for (int64_t b = 0; b < nt; ++b) {
+    memset(Z, 0xff, zb);  // NaN patterns: unwritten entries show
+    if (form == SGPU_MIXED_DF)
+      f256_block<df>(kind, p, a, b, (Cx<df>*)Z);
+    else
+      f256_block<double>(kind, p, a, b, (Cx<double>*)Z);
+  }
+  write_exact(argv[7], out, nout);
+  free(Z);
   free(in);
   free(out);
   free(img);
@@ -419,6 +490,7 @@ int main(int argc, char** argv) {
     mode = "h" + mode.substr(1);
   }
   if (mode == "xform") return xform(argc, argv);
+  if (mode == "f256") return f256_mode(argc, argv);
   if (mode == "ozaki" || mode == "ozakic") return ozaki(argc, argv);
   if (mode == "lcf") return lcf(argc, argv);
   if (mode == "lkcheck") {

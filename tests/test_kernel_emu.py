@@ -637,3 +637,31 @@ def test_legendre_recursion_matrix(emu, n, npts, rows, scalar):
     P = RA.legendre_matrix(x, a, n)
     ref = (P * w).T if scalar else P
     assert rel(res.reshape(ref.shape), ref) < 1e-14
+
+
+# ---- strided length-256 Fourier passes (fft256.cuh) ---------------------------
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("kind,outer,inner", [(C2C_FWD, 1, 37), (C2C_BWD, 2, 20), (R2C, 3, 19), (R2C, 1, 33),
+                                              (C2R, 2, 17), (C2R, 1, 33)])
+def test_fft256_strided(emu, kind, outer, inner, form, monkeypatch):
+    monkeypatch.setenv("SGPU_EMU_FORM", str(form))
+    g = np.random.default_rng(kind * 100 + inner)
+    n = 256
+    if kind in (C2C_FWD, C2C_BWD):
+        x = g.standard_normal((outer, n, inner)) + 1j * g.standard_normal((outer, n, inner))
+        scl = 1.0 / n if kind == C2C_FWD else 1.0
+        res = run(emu, ["f256", kind, outer, inner, repr(scl)], [x], x.size * 2).view(np.complex128)
+        ref = S.c2c_forward(x, axis=1) if kind == C2C_FWD else S.c2c_backward(x, axis=1)
+        got = res.reshape(x.shape)
+    elif kind == R2C:
+        x = g.standard_normal((outer, n, inner))
+        res = run(emu, ["f256", kind, outer, inner, repr(1.0 / n)], [x], outer * 129 * inner * 2)
+        got = res.view(np.complex128).reshape(outer, 129, inner)
+        ref = S.r2c_forward(x, axis=1)
+    else:
+        y = g.standard_normal((outer, 129, inner)) + 1j * g.standard_normal((outer, 129, inner))
+        res = run(emu, ["f256", kind, outer, inner, repr(1.0)], [y], outer * n * inner)
+        got = res.reshape(outer, n, inner)
+        ref = S.r2c_backward(y, n, axis=1)
+    assert np.isfinite(got).all()
+    assert rel(got, ref) < 1e-13
