@@ -658,6 +658,8 @@ def imex_leg(torch, steps=10):
 CASES = {
     # one transform of the channel grid, for profiler captures:  name -> (kind, form)
     "r2c-plain": ("r2c", "plain"), "r2c-mixed": ("r2c", "mixed"),
+    "c2r-mixed": ("c2r", "mixed"), "c2c-plain": ("c2c", "plain"), "c2c-mixed": ("c2c", "mixed"),
+    "bih-plain": ("bih", "plain"), "pad-mixed": ("pad", "mixed"), "bc-mixed": ("bc", "mixed"),
     "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
     "solve-plain": ("solve", "plain"),
     "leg-plain": ("leg", "plain"), "leg-mixed": ("leg", "mixed"),
@@ -680,6 +682,44 @@ def run_case(name, reps=3):
         V.form = _lib.FORMS[form]
         y = torch.empty(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
         fn = lambda: V.forward(x, y, axis=1)  # noqa: E731
+    elif kind == "c2r":
+        V = R2C(NY)
+        V.form = _lib.FORMS[form]
+        c = torch.randn(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
+        fn = lambda: V.backward(c, x, axis=1)  # noqa: E731
+    elif kind == "c2c":
+        from shenfun_gb300.spaces import C2C
+        V = C2C(NX)
+        V.form = _lib.FORMS[form]
+        c = torch.randn(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
+        y = torch.empty_like(c)
+        fn = lambda: V.forward(c, y, axis=0)  # noqa: E731
+    elif kind == "bih":
+        # biharmonic solve of Fourier 128 x Fourier 128 x ShenBiharmonic 129
+        import shenfun_gb300 as sg
+        T = sg.TensorProductSpace(sg.comm, (sg.FunctionSpace(128, "F", dtype="D"),
+                                            sg.FunctionSpace(128, "F", dtype="d"),
+                                            sg.FunctionSpace(129, "C", bc=(0, 0, 0, 0))), form=form)
+        u, v = sg.TrialFunction(T), sg.TestFunction(T)
+        H = sg.chebyshev.la.Biharmonic(sg.inner(v, sg.div(sg.grad(sg.div(sg.grad(u))))))
+        b = sg.Function(T, buffer=np.random.default_rng(0).standard_normal(T.shape(True)))
+        uh = sg.Function(T)
+        fn = lambda: H(b, uh)  # noqa: E731
+    elif kind == "pad":
+        # 3/2-rule padded backward of the x axis: 256 -> 384 coefficients
+        import shenfun_gb300 as sg
+        F = sg.FunctionSpace(NX, "F", dtype="D").get_dealiased(1.5)
+        F.form = _lib.FORMS[form]
+        c = torch.randn(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
+        y = torch.empty(3 * NX // 2, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
+        fn = lambda: F.backward(c, y, axis=0)  # noqa: E731
+    elif kind == "bc":
+        # the forward transform of a Chebyshev axis with wall values 1, -1
+        import shenfun_gb300 as sg
+        V = sg.FunctionSpace(NZ, "C", bc=(1.0, -1.0))
+        V.form = _lib.FORMS[form]
+        y = torch.empty_like(x)
+        fn = lambda: V.forward(x, y, axis=2)  # noqa: E731
     elif kind == "cheb":
         V = ChebyshevShenDirichlet(NZ)
         V.form = _lib.FORMS[form]
