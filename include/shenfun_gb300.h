@@ -136,8 +136,9 @@ int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64
  * overlap this tile's epilogue).  Length-256 Fourier plans (R2C, C2R, C2C):
  * 1 = the strided-pass kernel for axes with inner >= 16 (pass 1 and pass 2
  * of a 16 x 16 register FFT reading and writing global memory directly, one
- * shared-memory transpose), 2 = the generic line programs.  0 = the
- * library's default (1).  SGPU_ERR_UNSUPPORTED for other plans; get returns
+ * shared-memory transpose) at its default occupancy (3 CTAs per SM in the
+ * mixed form, 2 in FP64), 2 = the generic line programs, 3 / 4 = the
+ * strided-pass kernel at 2 / 3 CTAs per SM.  0 = the library's default (1).  SGPU_ERR_UNSUPPORTED for other plans; get returns
  * 0 for them.  No counterpart in the reference (a tuning knob of this
  * library's kernels). */
 int sgpu_plan_set_variant(sgpu_plan* plan, int variant);

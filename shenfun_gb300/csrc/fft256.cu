@@ -1,15 +1,18 @@
 // Kernels of the strided length-256 Fourier passes (fft256.cuh has the
 // schedule), FP64 and double-float, and their launcher.
+#include <mutex>
+#include <type_traits>
+
 #include "fft256.cuh"
 
 namespace sgpu {
 namespace f256 {
 
-// CTAs per SM: 2 (128 registers a thread: the 16 complex values of a
-// thread's register DFT stay in registers) for double-float; FP64 values are
-// pairs of FP64 registers, so the same budget holds
-template <class R, int KIND>
-__global__ void __launch_bounds__(NT, 2) k_fft256(LinePlan p, Args a) {
+// CTAs per SM (MINB): 2 gives 128 registers a thread (the 16 complex values
+// of a thread's register DFT and the DFT's temporaries stay in registers),
+// 3 gives 85 registers and more warps to hide latency, at the cost of spills
+template <class R, int KIND, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_fft256(LinePlan p, Args a) {
   extern __shared__ __align__(16) unsigned char f256_smem[];
   Cx<R>* Z = (Cx<R>*)f256_smem;
   const int64_t blk = (int64_t)blockIdx.x;
@@ -28,28 +31,40 @@ __global__ void __launch_bounds__(NT, 2) k_fft256(LinePlan p, Args a) {
   }
 }
 
-template <class R, int KIND>
+// per device: the large dynamic shared memory of every instantiation, set
+// once ([arithmetic][kind][occupancy])
+struct DevAttr {
+  std::once_flag once[2][4][2];
+  int rc[2][4][2] = {};
+};
+const int MAX_DEV = 64;
+DevAttr g_dev[MAX_DEV];
+
+template <class R, int KIND, int MINB>
 int launch_kind(const LinePlan& p, const Args& a, unsigned nblocks, cudaStream_t s) {
-  static bool attr = false;  // benign race: every caller sets the same value
-  if (!attr) {
-    if (cudaFuncSetAttribute(k_fft256<R, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_bytes<R>()) != cudaSuccess) {
-      cudaGetLastError();
-      return SGPU_ERR_CUDA;
-    }
-    attr = true;
-  }
-  k_fft256<R, KIND><<<nblocks, NT, smem_bytes<R>(), s>>>(p, a);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) return SGPU_ERR_CUDA;
+  DevAttr& d = g_dev[dev];
+  const int ri = std::is_same<R, df>::value ? 1 : 0, mi = MINB == 3 ? 1 : 0;
+  std::call_once(d.once[ri][KIND][mi], [&]() {
+    d.rc[ri][KIND][mi] = cudaFuncSetAttribute(k_fft256<R, KIND, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem_bytes<R>()) == cudaSuccess
+                             ? 1
+                             : -1;
+    cudaGetLastError();
+  });
+  if (d.rc[ri][KIND][mi] != 1) return SGPU_ERR_CUDA;
+  k_fft256<R, KIND, MINB><<<nblocks, NT, smem_bytes<R>(), s>>>(p, a);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
-template <class R>
+template <class R, int MINB>
 int launch_r(int kind, const LinePlan& p, const Args& a, unsigned nb, cudaStream_t s) {
   switch (kind) {
-    case C2C_FWD: return launch_kind<R, C2C_FWD>(p, a, nb, s);
-    case C2C_BWD: return launch_kind<R, C2C_BWD>(p, a, nb, s);
-    case R2C: return launch_kind<R, R2C>(p, a, nb, s);
-    case C2R: return launch_kind<R, C2R>(p, a, nb, s);
+    case C2C_FWD: return launch_kind<R, C2C_FWD, MINB>(p, a, nb, s);
+    case C2C_BWD: return launch_kind<R, C2C_BWD, MINB>(p, a, nb, s);
+    case R2C: return launch_kind<R, R2C, MINB>(p, a, nb, s);
+    case C2R: return launch_kind<R, C2R, MINB>(p, a, nb, s);
   }
   return SGPU_ERR_ARG;
 }
@@ -57,9 +72,10 @@ int launch_r(int kind, const LinePlan& p, const Args& a, unsigned nb, cudaStream
 }  // namespace f256
 
 // The plan's length-256 Fourier pass along a strided axis, or
-// SGPU_ERR_UNSUPPORTED when the plan or layout does not qualify.
+// SGPU_ERR_UNSUPPORTED when the plan or layout does not qualify; ctas_per_sm
+// 2 or 3 picks the register budget (above).
 int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines, int64_t inner, double scl,
-                cudaStream_t s) {
+                int ctas_per_sm, cudaStream_t s) {
   using namespace f256;
   if (p.n != N || p.m != N || p.rader || inner < 16) return SGPU_ERR_UNSUPPORTED;
   int kind;
@@ -75,8 +91,11 @@ int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines
   if (nt == 0) return SGPU_OK;
   if (nt > 0x7fffffffLL) return SGPU_ERR_ARG;
   Args a{in, out, nlines, inner, scl};
-  return p.form == SGPU_MIXED_DF ? launch_r<df>(kind, p, a, (unsigned)nt, s)
-                                 : launch_r<double>(kind, p, a, (unsigned)nt, s);
+  if (ctas_per_sm == 3)
+    return p.form == SGPU_MIXED_DF ? launch_r<df, 3>(kind, p, a, (unsigned)nt, s)
+                                   : launch_r<double, 3>(kind, p, a, (unsigned)nt, s);
+  return p.form == SGPU_MIXED_DF ? launch_r<df, 2>(kind, p, a, (unsigned)nt, s)
+                                 : launch_r<double, 2>(kind, p, a, (unsigned)nt, s);
 }
 
 }  // namespace sgpu

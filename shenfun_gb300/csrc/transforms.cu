@@ -27,12 +27,14 @@ struct sgpu_plan {
   oz::Matrix tc;     // tensor form: the line operator, split (any line layout)
   bool fused = false;
   lc::Matrix fm;     // the same operator for the fused contraction (contiguous lines)
-  int fvariant = 1;  // length-256 Fourier plans: 1 strided-pass kernel, 2 generic line programs
+  int fvariant = 1;  // length-256 Fourier plans: 1 strided-pass kernel at its default occupancy
+                     // (3 CTAs per SM for double-float, 2 for FP64: measured best on the channel
+                     // grid), 2 generic line programs, 3 / 4 strided-pass kernel at 2 / 3 CTAs per SM
 };
 
 namespace sgpu {
 int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines, int64_t inner, double scl,
-                cudaStream_t s);
+                int ctas_per_sm, cudaStream_t s);
 }
 
 namespace {
@@ -199,8 +201,9 @@ bool fourier256(const sgpu_plan* plan) {
 }  // namespace
 
 extern "C" int sgpu_plan_set_variant(sgpu_plan* plan, int variant) {
-  if (!plan || variant < 0 || variant > 2) return SGPU_ERR_ARG;
+  if (!plan || variant < 0 || variant > 4) return SGPU_ERR_ARG;
   if (plan->fused) {
+    if (variant > 2) return SGPU_ERR_ARG;
     plan->fm.variant = variant == 0 ? 1 : variant;
     return SGPU_OK;
   }
@@ -239,8 +242,9 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
   if (in == out && p.n_in != p.n_out) return SGPU_ERR_ARG;
   const int64_t nlines = outer * inner;
   if (nlines == 0) return SGPU_OK;
-  if (plan->fvariant == 1 && fourier256(plan) && inner >= 16) {
-    const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, stream);
+  if (plan->fvariant != 2 && fourier256(plan) && inner >= 16) {
+    const int ctas = plan->fvariant == 3 ? 2 : plan->fvariant == 4 ? 3 : (p.form == SGPU_MIXED_DF ? 3 : 2);
+    const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, ctas, stream);
     if (st != SGPU_ERR_UNSUPPORTED) return st;
   }
   const int lpb = lines_per_block(p, data_complex_for(p, data_kind));
