@@ -124,6 +124,14 @@ int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, int64_t inner
 int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
                          int64_t inner, int data_kind, double scale, void* work, size_t work_bytes,
                          cudaStream_t stream);
+/* The same for a stack of independent arrays of pair_lines lines each
+ * (outer x inner = their total): real lines are transformed two at a time as
+ * one complex line, and here the pairs never cross a block of pair_lines
+ * lines, so every array of the stack gets the bits it gets alone
+ * (pair_lines = 0: one block, as sgpu_plan_execute_ws). */
+int sgpu_plan_execute_blocks(const sgpu_plan* plan, const void* in, void* out, int64_t outer, int64_t inner,
+                             int data_kind, double scale, void* work, size_t work_bytes, int64_t pair_lines,
+                             cudaStream_t stream);
 /* Mixed-form Chebyshev plans with 16 <= n whose operator uses at most 339
  * input entries (n <= 339; backward transforms n <= 341) run contiguous lines
  * (inner = 1) through a fused kernel that splits the lines into digits on
@@ -335,6 +343,27 @@ int sgpu_helmholtz_shape(const sgpu_helmholtz_problem* problem, int64_t* phys, i
 int sgpu_helmholtz_workspace_size(const sgpu_helmholtz_problem* problem, size_t* bytes);
 int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* problem, const double* f, double* u,
                          void* work, size_t work_bytes, cudaStream_t stream);
+/* Batched step for serving: K problems of one shape, family and form
+ * (different shifts c) solved together, their right-hand sides f and
+ * solutions u stacked as K physical arrays.  Every transform pass runs once
+ * over the stacked lines with `problem`'s plans, and one solve launch covers
+ * every member's systems, member k with the factor cache facs[k] (a device
+ * array of K pointers, each from sgpu_helmholtz_factor_ptr of a problem of
+ * that shape).  Scratch from sgpu_helmholtz_batch_workspace_size; allocates
+ * nothing, so a caller can capture it in a CUDA graph and replay it with new
+ * right-hand sides and a new factor table.  Results equal K single solves
+ * bit for bit.  No counterpart in the reference. */
+int sgpu_helmholtz_batch_workspace_size(const sgpu_helmholtz_problem* problem, int K, size_t* bytes);
+int sgpu_helmholtz_factor_ptr(const sgpu_helmholtz_problem* problem, const void** fac);
+int sgpu_helmholtz_solve_batch(const sgpu_helmholtz_problem* problem, int K, const void* const* facs,
+                               const double* f, double* u, void* work, size_t work_bytes, cudaStream_t stream);
+/* the batched solves under it: systems of member k at b + k nsys N (nsys =
+ * outer x inner per member) with factor cache facs[k] (device array) */
+int sgpu_helmholtz_solve_cached_batch(const void* b, void* u, const void* const* facs, int K, int neumann,
+                                      int64_t outer, int64_t N, int64_t inner, int data_kind, int form,
+                                      cudaStream_t stream);
+int sgpu_band_sep_solve_batch(const void* b, void* u, const double* const* facs, const double* gens, int K,
+                              int n, int64_t outer, int64_t Nb, int64_t inner, int data_kind, cudaStream_t stream);
 /* Same step without any scratch argument, for callers that cannot provide or
  * allocate device memory (a host program whose device memory belongs to
  * another allocator, an FFI caller that only has its input and output arrays,

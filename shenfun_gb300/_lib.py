@@ -47,6 +47,7 @@ SIGNATURES = {
     "sgpu_plan_workspace_size": (_int, [_vp, _i64, _i64, _int, ctypes.POINTER(ctypes.c_size_t)]),
     "sgpu_plan_execute_ws": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp, ctypes.c_size_t, _vp]),
     "sgpu_plan_set_variant": (_int, [_vp, _int]),
+    "sgpu_plan_execute_blocks": (_int, [_vp, _vp, _vp, _i64, _i64, _int, _dbl, _vp, ctypes.c_size_t, _i64, _vp]),
     "sgpu_last_error": (_int, [_vp]),
     "sgpu_helmholtz_solve_refined": (_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _int, _dbl, _int, _int,
                                             _vp, _vp]),
@@ -97,6 +98,11 @@ SIGNATURES = {
     "sgpu_Biharmonic_matvec": (_int, [_vp, _vp, _dbl] + [_vp] * 13 + [_i64, _i64, _i64, _i64, _int, _vp]),
     "sgpu_SolverGeneric1ND_solve_data": (_int, [_vp, _vp, _int, _int, _i64, _i64, _i64, _i64, _i64, _int, _vp]),
     "sgpu_DMA_Solve": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _int, _vp]),
+    "sgpu_helmholtz_batch_workspace_size": (_int, [_vp, _int, ctypes.POINTER(ctypes.c_size_t)]),
+    "sgpu_helmholtz_factor_ptr": (_int, [_vp, ctypes.POINTER(_vp)]),
+    "sgpu_helmholtz_solve_batch": (_int, [_vp, _int, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]),
+    "sgpu_helmholtz_solve_cached_batch": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64, _i64, _int, _int, _vp]),
+    "sgpu_band_sep_solve_batch": (_int, [_vp, _vp, _vp, _vp, _int, _int, _i64, _i64, _i64, _int, _vp]),
     "sgpu_line_gemm": (_int, [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _int, _vp, _int, _vp]),
     "sgpu_scalar_product": (_int, [_vp] * 5 + [_int, _i64, _i64, _i64, _i64, _int, _vp, ctypes.c_size_t, _vp]),
     "sgpu_evaluate_expansion_all": (_int, [_vp] * 4 + [_int, _i64, _i64, _i64, _i64, _i64, _int, _vp,

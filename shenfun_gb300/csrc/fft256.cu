@@ -87,10 +87,10 @@ int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines
     default: return SGPU_ERR_UNSUPPORTED;
   }
   if (in == out && (kind == R2C || kind == C2R)) return SGPU_ERR_ARG;
-  const int64_t nt = tiles(kind, nlines);
+  const int64_t nt = tiles(kind, nlines, p.pb);
   if (nt == 0) return SGPU_OK;
   if (nt > 0x7fffffffLL) return SGPU_ERR_ARG;
-  Args a{in, out, nlines, inner, scl};
+  Args a{in, out, nlines, inner, scl, p.pb};
   if (ctas_per_sm == 3)
     return p.form == SGPU_MIXED_DF ? launch_r<df, 3>(kind, p, a, (unsigned)nt, s)
                                    : launch_r<double, 3>(kind, p, a, (unsigned)nt, s);

@@ -55,7 +55,19 @@ struct Args {
   int64_t nlines;  // lines of the transform: complex lines (C2C) or real lines (R2C / C2R)
   int64_t inner;
   double scl;
+  int64_t pb;      // R2C / C2R: lines pair up only within blocks of pb lines (0: one block)
 };
+
+// R2C / C2R: the two real lines of complex slot C (pairs never cross a block
+// of pb lines); live flags for lines past a block or the array
+SGPU_HD void pair_lines(const Args& a, int64_t C, int64_t& lp, bool& lvp, bool& lvq) {
+  const int64_t B = a.pb > 0 ? a.pb : a.nlines;
+  const int64_t hp = (B + 1) / 2;
+  const int64_t b = C / hp, j = C - b * hp;
+  lp = b * B + 2 * j;
+  lvp = 2 * j < B && lp < a.nlines;
+  lvq = 2 * j + 1 < B && lp + 1 < a.nlines;
+}
 
 #ifdef __CUDA_ARCH__
 SGPU_HD double ldg(const double* p) { return __ldg(p); }
@@ -85,8 +97,10 @@ SGPU_HD void pass1(const LinePlan& p, const Args& a, int64_t blk, Cx<R>* Z, int 
       if (KIND == C2C_BWD) v[n1] = conj(v[n1]);
     }
   } else if (KIND == R2C) {
-    const int64_t lp = 2 * (blk * TL + line), lq = lp + 1;
-    const bool lvp = lp < a.nlines, lvq = lq < a.nlines;
+    int64_t lp;
+    bool lvp, lvq;
+    pair_lines(a, blk * TL + line, lp, lvp, lvq);
+    const int64_t lq = lp + 1;
     const double* sp = a.in + (lvp ? base_off(lp, N, a.inner) : 0);
     const double* sq = a.in + (lvq ? base_off(lq, N, a.inner) : 0);
 #pragma unroll
@@ -95,8 +109,10 @@ SGPU_HD void pass1(const LinePlan& p, const Args& a, int64_t blk, Cx<R>* Z, int 
       v[n1] = cx<R>(lvp ? from_f64<R>(ldg(sp + k)) : R(0.0), lvq ? from_f64<R>(ldg(sq + k)) : R(0.0));
     }
   } else {  // C2R: Z_j = P_j + i Q_j with the Hermitian extension, conjugated
-    const int64_t lp = 2 * (blk * TL + line), lq = lp + 1;
-    const bool lvp = lp < a.nlines, lvq = lq < a.nlines;
+    int64_t lp;
+    bool lvp, lvq;
+    pair_lines(a, blk * TL + line, lp, lvp, lvq);
+    const int64_t lq = lp + 1;
     const int nh = N / 2 + 1;
     const double* sp = a.in + 2 * (lvp ? base_off(lp, nh, a.inner) : 0);
     const double* sq = a.in + 2 * (lvq ? base_off(lq, nh, a.inner) : 0);
@@ -151,9 +167,11 @@ SGPU_HD void pass2_store(const Args& a, int64_t blk, int t, const Cx<R>* v) {
       d[1] = to_f64(KIND == C2C_BWD ? -(x.im * sc) : x.im * sc);
     }
   } else {  // C2R: conj(X) * scale -> real lines 2c (re) and 2c + 1 (im)
-    const int64_t lp = 2 * (blk * TL + line), lq = lp + 1;
-    double* dp = lp < a.nlines ? a.out + base_off(lp, N, a.inner) : nullptr;
-    double* dq = lq < a.nlines ? a.out + base_off(lq, N, a.inner) : nullptr;
+    int64_t lp;
+    bool lvp, lvq;
+    pair_lines(a, blk * TL + line, lp, lvp, lvq);
+    double* dp = lvp ? a.out + base_off(lp, N, a.inner) : nullptr;
+    double* dq = lvq ? a.out + base_off(lp + 1, N, a.inner) : nullptr;
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) {
       const int64_t k = (int64_t)(k1 + 16 * k2) * a.inner;
@@ -185,23 +203,30 @@ SGPU_HD void r2c_post(const Args& a, int64_t blk, const Cx<R>* W, int t, int nth
     const Cx<R> zc = conj(w[k == 0 ? 0 : N - k]);
     const Cx<R> P = scale(z + zc, h);
     const Cx<R> Q = scale(mul_mi(z - zc), h);
-    const int64_t lp = 2 * (blk * TL + line), lq = lp + 1;
-    if (lp < a.nlines) {
+    int64_t lp;
+    bool lvp, lvq;
+    pair_lines(a, blk * TL + line, lp, lvp, lvq);
+    if (lvp) {
       double* d = a.out + 2 * (base_off(lp, nh, a.inner) + (int64_t)k * a.inner);
       d[0] = to_f64(P.re);
       d[1] = to_f64(P.im);
     }
-    if (lq < a.nlines) {
-      double* d = a.out + 2 * (base_off(lq, nh, a.inner) + (int64_t)k * a.inner);
+    if (lvq) {
+      double* d = a.out + 2 * (base_off(lp + 1, nh, a.inner) + (int64_t)k * a.inner);
       d[0] = to_f64(Q.re);
       d[1] = to_f64(Q.im);
     }
   }
 }
 
-// tiles of a launch: complex lines / 16
-SGPU_HD int64_t tiles(int kind, int64_t nlines) {
-  const int64_t cl = (kind == R2C || kind == C2R) ? (nlines + 1) / 2 : nlines;
+// tiles of a launch: complex lines (slots of real line pairs) / 16
+SGPU_HD int64_t tiles(int kind, int64_t nlines, int64_t pb) {
+  int64_t cl = nlines;
+  if (kind == R2C || kind == C2R) {
+    const int64_t B = pb > 0 ? pb : nlines;
+    const int64_t full = B > 0 ? nlines / B : 0, r = nlines - full * B;
+    cl = full * ((B + 1) / 2) + (r + 1) / 2;
+  }
   return (cl + TL - 1) / TL;
 }
 

@@ -50,6 +50,10 @@ struct LinePlan {
   const Cx<df>* post_f;
   const df* sten_f;
   int form;          // SGPU_PLAIN_F64 or SGPU_MIXED_DF
+  int64_t pb;        // real data: lines pair up (one complex FFT per pair)
+                     // only within blocks of pb lines (0: one block of all
+                     // lines), so that a stack of independent arrays gives
+                     // each array's bits
   int bcfun;         // Chebyshev backward: add the boundary functions of the
                      // two boundary dofs (non-homogeneous SD / SN)
 };

@@ -64,6 +64,28 @@ SGPU_HD LK lk_rows(int L, int tid, int nth) {
   return m;
 }
 
+// Real data: slot t of a tile starting at real line l0 (= 2 x the tile's
+// first complex slot) holds real line pair_line(...): complex slot C pairs
+// lines 2j and 2j + 1 of block b (blocks of pb lines, pb = 0: one block), so
+// pairs never cross a block.  With one block this is line l0 + t.
+SGPU_HD int64_t pair_line(int64_t l0, int t, int64_t pb, int64_t nlines, bool& live) {
+  const int64_t B = pb > 0 ? pb : nlines;
+  const int64_t hp = (B + 1) / 2;
+  const int64_t C = l0 / 2 + (t >> 1);
+  const int64_t b = C / hp, j = C - b * hp;
+  const int64_t i = 2 * j + (t & 1);
+  live = i < B && b * B + i < nlines;
+  return b * B + i;
+}
+
+// complex slots (pairs of real lines) of nlines real lines in blocks of pb
+SGPU_HD int64_t pair_slots(int64_t nlines, int64_t pb) {
+  const int64_t B = pb > 0 ? pb : nlines;
+  if (B <= 0) return 0;
+  const int64_t full = nlines / B, r = nlines - full * B;
+  return full * ((B + 1) / 2) + (r + 1) / 2;
+}
+
 #define SGPU_FOR_LK(m, L, n, c, k)                  \
   for (int c = (m).c0; c < (L); c += (m).cstep)     \
     for (int k = (m).k0; k < (n); k += (m).kstep)
@@ -117,14 +139,16 @@ SGPU_HD size_t smem_bytes(int tlc, int ld) {
 // Load TL lines into X.  Real data: line pair (2c, 2c+1) -> complex line c
 // (re, im); complex data: line c -> complex line c.  Lines past the end of
 // the array read as zero.
+// paired: the tile's lines are the real-line pairs of its complex slots
+// (R2C, C2R, real DCTs), placed by pair_line; otherwise line l0 + t.
 template <class R>
-SGPU_HD void load_tile(const LinePlan& p, const void* in, int in_complex, int TL, int n_arr,
+SGPU_HD void load_tile(const LinePlan& p, const void* in, int in_complex, int paired, int TL, int n_arr,
                        int64_t l0, int64_t nlines, int64_t inner, Cx<R>* X, int tid, int nth) {
   if (inner == 1) {
     const LK m = lk_lines(TL, tid, nth);
     for (int t = m.c0; t < TL; t += m.cstep) {
-      const int64_t l = l0 + t;
-      const bool live = l < nlines;
+      bool live = l0 + t < nlines;
+      const int64_t l = paired ? pair_line(l0, t, p.pb, nlines, live) : l0 + t;
       if (in_complex) {
         const double* src = (const double*)in + 2 * (l * n_arr);
         Cx<R>* dst = X + (size_t)t * p.ld;
@@ -140,8 +164,8 @@ SGPU_HD void load_tile(const LinePlan& p, const void* in, int in_complex, int TL
   } else {
     const LK m = lk_rows(TL, tid, nth);
     for (int t = m.c0; t < TL; t += m.cstep) {
-      const int64_t l = l0 + t;
-      const bool live = l < nlines;
+      bool live = l0 + t < nlines;
+      const int64_t l = paired ? pair_line(l0, t, p.pb, nlines, live) : l0 + t;
       const int64_t base = live ? elem_off(l, 0, n_arr, inner) : 0;
       for (int k = m.k0; k < n_arr; k += m.kstep) {
         const int64_t off = base + (int64_t)k * inner;
@@ -161,14 +185,15 @@ SGPU_HD void load_tile(const LinePlan& p, const void* in, int in_complex, int TL
 
 // Store TL lines from Y (complex lines, or real line pairs packed re/im).
 template <class R>
-SGPU_HD void store_tile(const LinePlan& p, void* out, int out_complex, int TL, int n_arr,
+SGPU_HD void store_tile(const LinePlan& p, void* out, int out_complex, int paired, int TL, int n_arr,
                         int64_t l0, int64_t nlines, int64_t inner, const Cx<R>* Y, int tid,
                         int nth) {
   if (inner == 1) {
     const LK m = lk_lines(TL, tid, nth);
     for (int t = m.c0; t < TL; t += m.cstep) {
-      const int64_t l = l0 + t;
-      if (l >= nlines) continue;
+      bool live = l0 + t < nlines;
+      const int64_t l = paired ? pair_line(l0, t, p.pb, nlines, live) : l0 + t;
+      if (!live) continue;
       if (out_complex) {
         double* dst = (double*)out + 2 * (l * n_arr);
         const Cx<R>* src = Y + (size_t)t * p.ld;
@@ -186,8 +211,9 @@ SGPU_HD void store_tile(const LinePlan& p, void* out, int out_complex, int TL, i
   } else {
     const LK m = lk_rows(TL, tid, nth);
     for (int t = m.c0; t < TL; t += m.cstep) {
-      const int64_t l = l0 + t;
-      if (l >= nlines) continue;
+      bool live = l0 + t < nlines;
+      const int64_t l = paired ? pair_line(l0, t, p.pb, nlines, live) : l0 + t;
+      if (!live) continue;
       const int64_t base = elem_off(l, 0, n_arr, inner);
       for (int k = m.k0; k < n_arr; k += m.kstep) {
         const int64_t off = base + (int64_t)k * inner;
@@ -212,7 +238,7 @@ SGPU_HD void prog_r2c(const LinePlan& p, const double* in, double* out, int64_t 
                       int64_t inner, double scl, int64_t blk, void* smem, int tid, int nth) {
   Smem<R> s = carve<R>(p, smem);
   const int64_t l0 = blk * 2 * p.tlc;
-  load_tile<R>(p, in, 0, 2 * p.tlc, p.n_in, l0, nlines, inner, s.X, tid, nth);
+  load_tile<R>(p, in, 0, 1, 2 * p.tlc, p.n_in, l0, nlines, inner, s.X, tid, nth);
   dft_lines<R>(p, s.X, s.A, s.B, s.slot, p.tlc, tid, nth);
   // P_k = (Z_k + conj Z_{n-k}) / 2, Q_k = (Z_k - conj Z_{n-k}) / (2i)
   const int n = p.n, nh = n / 2 + 1;
@@ -225,7 +251,7 @@ SGPU_HD void prog_r2c(const LinePlan& p, const double* in, double* out, int64_t 
     s.A[(size_t)(2 * c + 1) * p.ld + k] = scale(mul_mi(z - zc), h);
   }
   SGPU_SYNC();
-  store_tile<R>(p, out, 1, 2 * p.tlc, p.n_out, l0, nlines, inner, s.A, tid, nth);
+  store_tile<R>(p, out, 1, 1, 2 * p.tlc, p.n_out, l0, nlines, inner, s.A, tid, nth);
 }
 
 // Fourier C2R: pairs of half spectra -> real lines (unnormalised), times scale.
@@ -234,7 +260,7 @@ SGPU_HD void prog_c2r(const LinePlan& p, const double* in, double* out, int64_t 
                       int64_t inner, double scl, int64_t blk, void* smem, int tid, int nth) {
   Smem<R> s = carve<R>(p, smem);
   const int64_t l0 = blk * 2 * p.tlc;
-  load_tile<R>(p, in, 1, 2 * p.tlc, p.n_in, l0, nlines, inner, s.A, tid, nth);
+  load_tile<R>(p, in, 1, 1, 2 * p.tlc, p.n_in, l0, nlines, inner, s.A, tid, nth);
   const int n = p.n, nh = n / 2 + 1;
   // Z_k = P_k + i Q_k with Hermitian extension; DC and (even n) Nyquist real;
   // conjugated for the inverse: IDFT(Z) = conj(DFT(conj Z))
@@ -264,7 +290,7 @@ SGPU_HD void prog_c2r(const LinePlan& p, const double* in, double* out, int64_t 
     s.X[(size_t)c * p.ld + k] = cx<R>(z.re * sc, -(z.im * sc));
   }
   SGPU_SYNC();
-  store_tile<R>(p, out, 0, 2 * p.tlc, p.n_out, l0, nlines, inner, s.X, tid, nth);
+  store_tile<R>(p, out, 0, 1, 2 * p.tlc, p.n_out, l0, nlines, inner, s.X, tid, nth);
 }
 
 // Fourier C2C forward / backward (unnormalised), times scale.
@@ -274,7 +300,7 @@ SGPU_HD void prog_c2c(const LinePlan& p, const double* in, double* out, int64_t 
   Smem<R> s = carve<R>(p, smem);
   const int64_t l0 = blk * p.tlc;
   const bool bwd = p.kind == SGPU_XF_C2C_BWD;
-  load_tile<R>(p, in, 1, p.tlc, p.n_in, l0, nlines, inner, s.X, tid, nth);
+  load_tile<R>(p, in, 1, 0, p.tlc, p.n_in, l0, nlines, inner, s.X, tid, nth);
   const int n = p.n;
   const LK m = lk_lines(p.tlc, tid, nth);
   if (bwd) {
@@ -288,7 +314,7 @@ SGPU_HD void prog_c2c(const LinePlan& p, const double* in, double* out, int64_t 
     s.X[(size_t)c * p.ld + k] = bwd ? cx<R>(z.re * sc, -(z.im * sc)) : scale(z, sc);
   }
   SGPU_SYNC();
-  store_tile<R>(p, out, 1, p.tlc, p.n_out, l0, nlines, inner, s.X, tid, nth);
+  store_tile<R>(p, out, 1, 0, p.tlc, p.n_out, l0, nlines, inner, s.X, tid, nth);
 }
 
 // Chebyshev forward kinds: DCT-II (REDFT10) and the GC scalar product with the
@@ -301,7 +327,7 @@ SGPU_HD void prog_dct2(const LinePlan& p, const double* in, double* out, int in_
   const int TL = in_complex ? p.tlc : 2 * p.tlc;
   const int64_t l0 = blk * TL;
   const int n = p.n, h = (n + 1) / 2;
-  load_tile<R>(p, in, in_complex, TL, n, l0, nlines, inner, s.A, tid, nth);
+  load_tile<R>(p, in, in_complex, !in_complex, TL, n, l0, nlines, inner, s.A, tid, nth);
   const LK m = lk_lines(p.tlc, tid, nth);
   // Makhoul reorder: v_j = x_{2j} (j < h), v_{n-1-j} = x_{2j+1}
   SGPU_FOR_LK(m, p.tlc, n, c, j) {
@@ -383,7 +409,7 @@ SGPU_HD void prog_dct2(const LinePlan& p, const double* in, double* out, int in_
     }
     SGPU_SYNC();
   }
-  store_tile<R>(p, out, in_complex, TL, n, l0, nlines, inner, Y, tid, nth);
+  store_tile<R>(p, out, in_complex, !in_complex, TL, n, l0, nlines, inner, Y, tid, nth);
 }
 
 // Chebyshev backward kinds: DCT-III (REDFT01) and the GC backward with the
@@ -396,7 +422,7 @@ SGPU_HD void prog_dct3(const LinePlan& p, const double* in, double* out, int in_
   const int TL = in_complex ? p.tlc : 2 * p.tlc;
   const int64_t l0 = blk * TL;
   const int n = p.n;
-  load_tile<R>(p, in, in_complex, TL, n, l0, nlines, inner, s.A, tid, nth);
+  load_tile<R>(p, in, in_complex, !in_complex, TL, n, l0, nlines, inner, s.A, tid, nth);
   const LK m = lk_lines(p.tlc, tid, nth);
   Cx<R>* C = s.A;
   if (p.kind == SGPU_XF_CHEB_BACKWARD && p.basis != SGPU_BASIS_ORTHO) {
@@ -462,7 +488,7 @@ SGPU_HD void prog_dct3(const LinePlan& p, const double* in, double* out, int in_
     s.A[(size_t)c * p.ld + i] = scale(z, sc);
   }
   SGPU_SYNC();
-  store_tile<R>(p, out, in_complex, TL, n, l0, nlines, inner, s.A, tid, nth);
+  store_tile<R>(p, out, in_complex, !in_complex, TL, n, l0, nlines, inner, s.A, tid, nth);
 }
 
 template <class R>

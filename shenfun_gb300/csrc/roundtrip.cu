@@ -42,6 +42,9 @@ int sgpu_legendre_execute_ws(const sgpu_legendre_plan* plan, int direction, cons
                              cudaStream_t stream);
 int sgpu_plan_execute(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
                       int64_t inner, int data_kind, double scale, cudaStream_t stream);
+int sgpu_plan_execute_blocks(const sgpu_plan* plan, const void* in, void* out, int64_t outer, int64_t inner,
+                             int data_kind, double scale, void* work, size_t work_bytes, int64_t pair_lines,
+                             cudaStream_t stream);
 int sgpu_legendre_plan_create(sgpu_legendre_plan** plan, int N, int basis, int form);
 int sgpu_legendre_plan_destroy(sgpu_legendre_plan* plan);
 int sgpu_legendre_execute(const sgpu_legendre_plan* plan, int direction, const void* in,
@@ -58,6 +61,11 @@ int sgpu_band_sep_factor(int n, int nterms, int gen_term, const double* bands,
 int sgpu_band_sep_solve(const void* b, void* u, const double* fac, const double* gens, int n,
                         int64_t outer, int64_t Nb, int64_t inner, int data_kind,
                         cudaStream_t stream);
+int sgpu_helmholtz_solve_cached_batch(const void* b, void* u, const void* const* facs, int K, int neumann,
+                                      int64_t outer, int64_t N, int64_t inner, int data_kind, int form,
+                                      cudaStream_t stream);
+int sgpu_band_sep_solve_batch(const void* b, void* u, const double* const* facs, const double* gens, int K, int n,
+                              int64_t outer, int64_t Nb, int64_t inner, int data_kind, cudaStream_t stream);
 }
 
 struct sgpu_helmholtz_problem {
@@ -333,8 +341,8 @@ extern "C" int sgpu_helmholtz_shape(const sgpu_helmholtz_problem* p, int64_t* ph
 // wt (the Dirichlet-axis contraction's split input in the tensor-core form)
 static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-static size_t split_bytes(const sgpu_helmholtz_problem* p) {
-  const int64_t nlines_d = p->nphys / p->N[p->ndim - 1];
+static size_t split_bytes(const sgpu_helmholtz_problem* p, int K = 1) {
+  const int64_t nlines_d = K * (p->nphys / p->N[p->ndim - 1]);
   size_t a = 0, b = 0;
   if (p->family == SGPU_FAMILY_CHEBYSHEV) {
     sgpu_plan_workspace_size(p->d_s, nlines_d, 1, SGPU_REAL, &a);
@@ -351,48 +359,57 @@ extern "C" int sgpu_helmholtz_workspace_size(const sgpu_helmholtz_problem* p, si
   return SGPU_OK;
 }
 
-// the step itself on a scratch area laid out as above
+// the step itself on a scratch area laid out as above, for K problems of p's
+// shape stacked along a leading axis (f, u: K physical arrays; work: the
+// scratch of the stacked arrays); facs (device, K pointers) gives each
+// member's factor cache, nullptr for K = 1 and p's own
 static int helmholtz_run(const sgpu_helmholtz_problem* p, const double* f, double* u, void* work,
-                         cudaStream_t s) {
+                         cudaStream_t s, int K = 1, const void* const* facs = nullptr) {
   const int64_t Nd = p->N[p->ndim - 1];
-  const int64_t nlines_d = p->nphys / Nd;  // physical lines along the last axis
+  const int64_t nlines_d = K * (p->nphys / Nd);  // physical lines along the last axis
   double* wr = (double*)work;
-  double* wc = (double*)((unsigned char*)work + round256((size_t)p->nphys * 8));
-  void* wt = (unsigned char*)wc + round256((size_t)p->nspec * 16);
-  const size_t wtb = split_bytes(p);
+  double* wc = (double*)((unsigned char*)work + round256((size_t)K * p->nphys * 8));
+  void* wt = (unsigned char*)wc + round256((size_t)K * p->nspec * 16);
+  const size_t wtb = split_bytes(p, K);
   // the first failing call's status is the step's status
   int st = SGPU_OK;
   auto chk = [&](int r) {
     if (st == SGPU_OK) st = r;
   };
+  // real lines pair up within each member only (bits independent of the batch)
+  const int64_t pl_d = nlines_d / K;
+  const int64_t pl_r = p->ndim == 2 ? Nd : p->N[0] * Nd;
   // 1. scalar product along the Dirichlet axis (real data)
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    chk(sgpu_plan_execute_ws(p->d_s, f, wr, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s));
+    chk(sgpu_plan_execute_blocks(p->d_s, f, wr, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, pl_d, s));
   else
     chk(sgpu_legendre_execute_ws(p->leg, 0, f, wr, nlines_d, 1, SGPU_REAL, wt, wtb, s));
   if (p->ndim == 2) {
     const int64_t N0 = p->N[0];
-    chk(sgpu_plan_execute(p->fr_f, wr, wc, 1, Nd, SGPU_REAL, 1.0 / N0, s));
+    chk(sgpu_plan_execute_blocks(p->fr_f, wr, wc, K, Nd, SGPU_REAL, 1.0 / N0, nullptr, 0, pl_r, s));
   } else {
     const int64_t N0 = p->N[0], N1 = p->N[1], Nh = N1 / 2 + 1;
-    chk(sgpu_plan_execute(p->fr_f, wr, wc, N0, Nd, SGPU_REAL, 1.0 / N1, s));
-    chk(sgpu_plan_execute(p->fx_f, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0 / N0, s));
+    chk(sgpu_plan_execute_blocks(p->fr_f, wr, wc, K * N0, Nd, SGPU_REAL, 1.0 / N1, nullptr, 0, pl_r, s));
+    chk(sgpu_plan_execute(p->fx_f, wc, wc, K, Nh * Nd, SGPU_COMPLEX, 1.0 / N0, s));
   }
   // 2. one banded system per wavenumber, in place on the spectral array
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    chk(sgpu_helmholtz_solve_cached(wc, wc, p->fac, 0, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s));
+    chk(facs ? sgpu_helmholtz_solve_cached_batch(wc, wc, facs, K, 0, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s)
+             : sgpu_helmholtz_solve_cached(wc, wc, p->fac, 0, p->nsys, Nd, 1, SGPU_COMPLEX, SGPU_PLAIN_F64, s));
   else
-    chk(sgpu_band_sep_solve(wc, wc, p->fac, nullptr, (int)(Nd - 2), p->nsys, Nd, 1, SGPU_COMPLEX, s));
+    chk(facs ? sgpu_band_sep_solve_batch(wc, wc, (const double* const*)facs, nullptr, K, (int)(Nd - 2), p->nsys, Nd,
+                                         1, SGPU_COMPLEX, s)
+             : sgpu_band_sep_solve(wc, wc, p->fac, nullptr, (int)(Nd - 2), p->nsys, Nd, 1, SGPU_COMPLEX, s));
   // 3. backward
   if (p->ndim == 2) {
-    chk(sgpu_plan_execute(p->fr_b, wc, wr, 1, Nd, SGPU_COMPLEX, 1.0, s));
+    chk(sgpu_plan_execute_blocks(p->fr_b, wc, wr, K, Nd, SGPU_COMPLEX, 1.0, nullptr, 0, pl_r, s));
   } else {
     const int64_t N0 = p->N[0], N1 = p->N[1], Nh = N1 / 2 + 1;
-    chk(sgpu_plan_execute(p->fx_b, wc, wc, 1, Nh * Nd, SGPU_COMPLEX, 1.0, s));
-    chk(sgpu_plan_execute(p->fr_b, wc, wr, N0, Nd, SGPU_COMPLEX, 1.0, s));
+    chk(sgpu_plan_execute(p->fx_b, wc, wc, K, Nh * Nd, SGPU_COMPLEX, 1.0, s));
+    chk(sgpu_plan_execute_blocks(p->fr_b, wc, wr, K * N0, Nd, SGPU_COMPLEX, 1.0, nullptr, 0, pl_r, s));
   }
   if (p->family == SGPU_FAMILY_CHEBYSHEV)
-    chk(sgpu_plan_execute_ws(p->d_b, wr, u, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, s));
+    chk(sgpu_plan_execute_blocks(p->d_b, wr, u, nlines_d, 1, SGPU_REAL, 1.0, wt, wtb, pl_d, s));
   else
     chk(sgpu_legendre_execute_ws(p->leg, 2, wr, u, nlines_d, 1, SGPU_REAL, wt, wtb, s));
   return st;
@@ -406,6 +423,29 @@ static bool on_own_device(const sgpu_helmholtz_problem* p) {
     return false;
   }
   return dev == p->device;
+}
+
+extern "C" int sgpu_helmholtz_batch_workspace_size(const sgpu_helmholtz_problem* p, int K, size_t* bytes) {
+  if (!p || !bytes || K < 1) return SGPU_ERR_ARG;
+  *bytes = round256((size_t)K * p->nphys * 8) + round256((size_t)K * p->nspec * 16) + split_bytes(p, K);
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_helmholtz_factor_ptr(const sgpu_helmholtz_problem* p, const void** fac) {
+  if (!p || !fac) return SGPU_ERR_ARG;
+  *fac = p->fac;
+  return SGPU_OK;
+}
+
+extern "C" int sgpu_helmholtz_solve_batch(const sgpu_helmholtz_problem* p, int K, const void* const* facs,
+                                          const double* f, double* u, void* work, size_t work_bytes,
+                                          cudaStream_t stream) {
+  if (!p || K < 1 || !facs || !f || !u || !work) return SGPU_ERR_ARG;
+  if (!on_own_device(p)) return SGPU_ERR_ARG;
+  size_t need = 0;
+  sgpu_helmholtz_batch_workspace_size(p, K, &need);
+  if (work_bytes < need || ((uintptr_t)work & 255) != 0) return SGPU_ERR_ARG;
+  return helmholtz_run(p, f, u, work, stream, K, facs);
 }
 
 extern "C" int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* p, const double* f, double* u,

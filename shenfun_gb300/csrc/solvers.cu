@@ -360,6 +360,45 @@ extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* f
   return finish();
 }
 
+// Batches of problems of one shape (serving): member k's systems are at
+// b + k nsys N with their own factor cache facs[k] (a device array of K
+// pointers); one thread per (system, parity) of every member.
+template <class R, class T>
+__global__ void k_helmholtz_cached_batch(const T* b, T* u, const void* const* facs, int neumann, int64_t N,
+                                         int64_t inner, int64_t nsys, int K) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * nsys * K) return;
+  const int64_t c = t >> 1;
+  const int k = (int)(c / nsys);
+  const int64_t s = c - (int64_t)k * nsys, off = (int64_t)k * nsys * N;
+  helmholtz_cached_solve_prog<R, T>(b + off, u + off, (const R*)facs[k], neumann, N, inner, nsys, s, (int)(t & 1));
+}
+
+extern "C" int sgpu_helmholtz_solve_cached_batch(const void* b, void* u, const void* const* facs, int K, int neumann,
+                                                 int64_t outer, int64_t N, int64_t inner, int data_kind, int form,
+                                                 cudaStream_t stream) {
+  if (!b || !u || !facs || K < 1 || N < 8 || outer < 0 || inner < 1 || (neumann != 0 && neumann != 1))
+    return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  const unsigned nb = nblk(2 * nsys * K);
+  if (form == SGPU_PLAIN_F64 && data_kind == SGPU_COMPLEX)
+    k_helmholtz_cached_batch<double, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, facs, neumann, N, inner,
+                                                                      nsys, K);
+  else if (form == SGPU_PLAIN_F64 && data_kind == SGPU_REAL)
+    k_helmholtz_cached_batch<double, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, facs, neumann,
+                                                                          N, inner, nsys, K);
+  else if (form == SGPU_MIXED_DF && data_kind == SGPU_COMPLEX)
+    k_helmholtz_cached_batch<df, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, facs, neumann, N, inner, nsys,
+                                                                  K);
+  else if (form == SGPU_MIXED_DF && data_kind == SGPU_REAL)
+    k_helmholtz_cached_batch<df, double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, facs, neumann, N,
+                                                                      inner, nsys, K);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
 // ---- banded + semiseparable per-wavenumber systems --------------------------
 template <class F>
 __global__ void k_band_sep_factor(BandSepDesc d, F* fac, int64_t nsys) {
@@ -468,6 +507,33 @@ extern "C" int sgpu_band_sep_solve(const void* b, void* u, const double* fac, co
     k_band_sep_solve<cd><<<nblk(2 * nsys), kThreads, 0, stream>>>((const cd*)b, (cd*)u, fac, gens, n, Nb, inner, nsys);
   else if (data_kind == SGPU_REAL)
     k_band_sep_solve<double><<<nblk(2 * nsys), kThreads, 0, stream>>>((const double*)b, (double*)u, fac, gens, n, Nb, inner, nsys);
+  else
+    return SGPU_ERR_ARG;
+  return finish();
+}
+
+template <class T>
+__global__ void k_band_sep_solve_batch(const T* b, T* u, const double* const* facs, const double* gens, int n,
+                                       int64_t Nb, int64_t inner, int64_t nsys, int K) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * nsys * K) return;
+  const int k = (int)(t / (2 * nsys));
+  const int64_t ch = t - (int64_t)k * 2 * nsys, off = (int64_t)k * nsys * Nb;
+  band_sep_solve_prog<T>(b + off, u + off, facs[k], gens, n, Nb, inner, nsys, ch);
+}
+
+extern "C" int sgpu_band_sep_solve_batch(const void* b, void* u, const double* const* facs, const double* gens, int K,
+                                         int n, int64_t outer, int64_t Nb, int64_t inner, int data_kind,
+                                         cudaStream_t stream) {
+  if (!b || !u || !facs || K < 1 || n < 2 || Nb < n || outer < 0 || inner < 1) return SGPU_ERR_ARG;
+  const int64_t nsys = outer * inner;
+  if (nsys == 0) return SGPU_OK;
+  const unsigned nb = nblk(2 * nsys * K);
+  if (data_kind == SGPU_COMPLEX)
+    k_band_sep_solve_batch<cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, facs, gens, n, Nb, inner, nsys, K);
+  else if (data_kind == SGPU_REAL)
+    k_band_sep_solve_batch<double><<<nb, kThreads, 0, stream>>>((const double*)b, (double*)u, facs, gens, n, Nb, inner,
+                                                                nsys, K);
   else
     return SGPU_ERR_ARG;
   return finish();

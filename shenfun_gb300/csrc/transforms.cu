@@ -221,7 +221,8 @@ extern "C" int sgpu_plan_get_variant(const sgpu_plan* plan, int* variant) {
 }
 
 static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t outer, int64_t inner,
-                    int data_kind, double scale, void* work, size_t work_bytes, cudaStream_t stream) {
+                    int data_kind, double scale, void* work, size_t work_bytes, cudaStream_t stream,
+                    int64_t pair_lines = 0) {
   if (!plan || !in || !out) return SGPU_ERR_ARG;
   if (outer < 0 || inner < 1) return SGPU_ERR_ARG;
   if (data_kind != SGPU_REAL && data_kind != SGPU_COMPLEX) return SGPU_ERR_ARG;
@@ -238,7 +239,8 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
     return oz::contract(plan->tc, (const double*)in, (double*)out, outer * inner, inner,
                         data_kind == SGPU_COMPLEX, work, work_bytes, stream);
   }
-  const LinePlan& p = plan->lp;
+  LinePlan p = plan->lp;  // per call: the pairing blocks of real lines
+  p.pb = pair_lines > 0 && pair_lines < outer * inner ? pair_lines : 0;
   if (in == out && p.n_in != p.n_out) return SGPU_ERR_ARG;
   const int64_t nlines = outer * inner;
   if (nlines == 0) return SGPU_OK;
@@ -247,8 +249,10 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
     const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, ctas, stream);
     if (st != SGPU_ERR_UNSUPPORTED) return st;
   }
-  const int lpb = lines_per_block(p, data_complex_for(p, data_kind));
-  const int64_t nblocks = (nlines + lpb - 1) / lpb;
+  const int dcx = data_complex_for(p, data_kind);
+  const int lpb = lines_per_block(p, dcx);
+  // real data: one CTA per tlc complex slots (pairs of real lines)
+  const int64_t nblocks = dcx ? (nlines + lpb - 1) / lpb : (pair_slots(nlines, p.pb) + p.tlc - 1) / p.tlc;
   if (nblocks > 0x7fffffffLL) return SGPU_ERR_ARG;
   const int dc = data_complex_for(p, data_kind);
   const int G = xf_group(p.kind);
@@ -261,6 +265,13 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
                    : xf_launch_cheb_df(G, p, src, dst, dc, nlines, inner, scale, nb, stream);
   return fourier ? xf_launch_fourier_f64(G, p, src, dst, dc, nlines, inner, scale, nb, stream)
                  : xf_launch_cheb_f64(G, p, src, dst, dc, nlines, inner, scale, nb, stream);
+}
+
+extern "C" int sgpu_plan_execute_blocks(const sgpu_plan* plan, const void* in, void* out, int64_t outer,
+                                        int64_t inner, int data_kind, double scale, void* work, size_t work_bytes,
+                                        int64_t pair_lines, cudaStream_t stream) {
+  if (pair_lines < 0) return SGPU_ERR_ARG;
+  return plan_run(plan, in, out, outer, inner, data_kind, scale, work, work_bytes, stream, pair_lines);
 }
 
 extern "C" int sgpu_plan_execute_ws(const sgpu_plan* plan, const void* in, void* out, int64_t outer,

@@ -79,3 +79,71 @@ class HelmholtzProblem:
         _lib.call("sgpu_helmholtz_solve", self._h, ptr(f), ptr(u), work.data_ptr(),
                   work.numel(), stream_handle(stream))
         return u
+
+
+class BatchRunner:
+    """K problems of one shape class (N, family, form), different shifts,
+    solved with one launch per stage (sgpu_helmholtz_solve_batch) on fixed
+    staging buffers, captured once as a CUDA graph and replayed: per batch
+    the members' right-hand sides are copied into the input slots, the
+    factor-pointer table is updated, the graph is replayed and the solutions
+    are read from the output slots.  The graph allocates nothing and reads
+    the table at replay time, so any K problems of the class (any shifts) can
+    share it."""
+
+    def __init__(self, proto, K, stream, graph=True):
+        self.proto = proto
+        self.K = int(K)
+        self.stream = stream
+        shape = (self.K,) + proto.phys_shape
+        with torch.cuda.stream(stream):
+            self.f = torch.zeros(shape, dtype=torch.float64, device="cuda")
+            self.u = torch.zeros(shape, dtype=torch.float64, device="cuda")
+            nb = ctypes.c_size_t()
+            _lib.call("sgpu_helmholtz_batch_workspace_size", proto._h, self.K, ctypes.byref(nb))
+            self.work = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device="cuda")
+            self.table = torch.zeros(self.K, dtype=torch.int64, device="cuda")
+        self.table_host = torch.zeros(self.K, dtype=torch.int64, pin_memory=True)
+        self.graph = None
+        if graph:
+            self._capture()
+
+    def _launch(self):
+        _lib.call("sgpu_helmholtz_solve_batch", self.proto._h, self.K, self.table.data_ptr(), self.f.data_ptr(),
+                  self.u.data_ptr(), self.work.data_ptr(), self.work.numel(), stream_handle(self.stream))
+
+    def _capture(self):
+        # the table must hold valid pointers while the warm-up launch runs
+        p = ctypes.c_void_p()
+        _lib.call("sgpu_helmholtz_factor_ptr", self.proto._h, ctypes.byref(p))
+        self.table_host.fill_(p.value)
+        with torch.cuda.stream(self.stream):
+            self.table.copy_(self.table_host, non_blocking=True)
+            self._launch()  # warm-up outside the capture (plan attributes, lazy state)
+        self.stream.synchronize()
+        g = torch.cuda.CUDAGraph()
+        # thread-local capture: worker threads keep creating problems
+        # (stream-ordered allocations) while this thread captures
+        with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+            self._launch()
+        self.graph = g
+
+    def run(self, problems):
+        """Queue the batch of `problems` (at most K, all of the class) whose
+        right-hand sides are already in self.f[:len(problems)]; the solutions
+        land in self.u.  Unused slots repeat the last member."""
+        ptrs = []
+        for p in problems:
+            q = ctypes.c_void_p()
+            _lib.call("sgpu_helmholtz_factor_ptr", p._h, ctypes.byref(q))
+            ptrs.append(q.value)
+        ptrs += [ptrs[-1]] * (self.K - len(ptrs))
+        # a fresh page-locked source per batch: the previous batch's copy may
+        # still be queued (torch's host allocator keeps it until that copy ran)
+        host = torch.tensor(ptrs, dtype=torch.int64).pin_memory()
+        with torch.cuda.stream(self.stream):
+            self.table.copy_(host, non_blocking=True)
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._launch()

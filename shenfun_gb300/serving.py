@@ -332,22 +332,209 @@ class GpuExecutor:
         return done
 
 
-def make_stream(n, seed=0, rate=None, nmin=32, nmax=512, max_points=2 ** 24, families=("chebyshev", "legendre")):
+class BatchExecutor(GpuExecutor):
+    """Continuous batching across requests: admitted requests wait per shape
+    class (grid, family); whenever a stream is free, the class with the
+    oldest waiting request is launched as one batch of up to ``max_batch``
+    requests (any shifts) through a CUDA graph of the batched step
+    (problem.BatchRunner: one launch per transform pass and one solve launch
+    for all members, each member with its own cached factorisation).  While
+    the streams are busy, arrivals accumulate into larger batches.  Graph
+    runners are cached per (class, batch size), batch sizes rounded up to a
+    power of two; a batch's members stay independent (per-line transforms,
+    per-system solves), so results are the same alone and in a batch."""
+
+    def __init__(self, nstreams=4, cache_budget=4 << 30, form="mixed", keep_results=True, prep_workers=4,
+                 max_batch=16, batch_bytes=1 << 30, graphs=True):
+        GpuExecutor.__init__(self, nstreams=nstreams, cache_budget=cache_budget, form=form,
+                             keep_results=keep_results, prep_workers=prep_workers)
+        self.max_batch = int(max_batch)
+        self.batch_bytes = int(batch_bytes)
+        self.graphs = graphs
+        self.ready = collections.OrderedDict()  # class -> deque of requests whose problem is cached
+        self.runners = collections.OrderedDict()  # (class, K) -> BatchRunner
+        self.busy = {}  # stream index -> batch id in flight
+        self.batches = 0
+        self.batch_sizes = collections.Counter()
+        self._bid = 0
+
+    @staticmethod
+    def _class(req):
+        return (req.N, req.family)
+
+    def cache_bytes(self):
+        return GpuExecutor.cache_bytes(self) + sum(r.bytes for r in self.runners.values())
+
+    def _kmax(self, req):
+        per = 3 * request_bytes(req.N)
+        return max(1, min(self.max_batch, self.batch_bytes // max(per, 1)))
+
+    def launch(self, req):
+        if req.key in self.cache:
+            self.hits += 1
+            self.ready.setdefault(self._class(req), collections.deque()).append(req)
+            self._flush()
+            return
+        if req.key in self.pending:
+            self.hits += 1
+        else:
+            self.misses += 1
+            s = self.streams[req.slot % len(self.streams)]
+            fut = self.pool.submit(self.Problem, req.N, req.family, req.c, self.form, stream=s) if self.pool else None
+            if fut is None:
+                p = self.Problem(req.N, req.family, req.c, self.form, stream=s)
+                ev = self.torch.cuda.Event()
+                ev.record(s)
+                self.cache[req.key] = (p, factor_bytes(req.N, req.family), (ev, s))
+                self.ready.setdefault(self._class(req), collections.deque()).append(req)
+                self._flush()
+                return
+            self.pending[req.key] = (fut, s)
+        self.waiting[req.id] = req
+
+    def _collect(self):
+        for key, (fut, cs) in list(self.pending.items()):
+            if not fut.done():
+                continue
+            del self.pending[key]
+            err = fut.exception()
+            if err is None:
+                ev = self.torch.cuda.Event()
+                ev.record(cs)
+                self.cache[key] = (fut.result(), factor_bytes(key[0], key[1]), (ev, cs))
+                self.shrink_cache(self.cache_budget)
+            for rid, r in list(self.waiting.items()):
+                if r.key != key:
+                    continue
+                del self.waiting[rid]
+                if err is not None:
+                    r.state = FAILED
+                    r.error = repr(err)
+                    self.failed.append(rid)
+                else:
+                    self.ready.setdefault(self._class(r), collections.deque()).append(r)
+
+    def _runner(self, cls, K, proto, si):
+        from .problem import BatchRunner
+        key = (cls, K, si)
+        r = self.runners.get(key)
+        if r is not None:
+            self.runners.move_to_end(key)
+            return r
+        r = BatchRunner(proto, K, self.streams[si], graph=self.graphs)
+        r.bytes = r.f.numel() * 16 + r.work.numel()
+        self.runners[key] = r
+        return r
+
+    def _flush(self):
+        torch = self.torch
+        while self.ready:
+            free = [i for i in range(len(self.streams)) if i not in self.busy]
+            if not free:
+                return
+            cls = next(iter(self.ready))
+            q = self.ready[cls]
+            if not q:
+                del self.ready[cls]
+                continue
+            si = free[0]
+            s = self.streams[si]
+            kmax = self._kmax(q[0])
+            reqs = [q.popleft() for _ in range(min(kmax, len(q)))]
+            if not q:
+                del self.ready[cls]
+            else:
+                self.ready.move_to_end(cls)
+            K = 1
+            while K < len(reqs):
+                K *= 2
+            K = min(K, kmax) if kmax >= len(reqs) else len(reqs)
+            try:
+                probs = [self._cached(r, s) for r in reqs]
+                run = self._runner(cls, K, probs[0], si)
+                with torch.cuda.stream(s):
+                    for k, r in enumerate(reqs):
+                        src = r.f if isinstance(r.f, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(r.f))
+                        run.f[k].copy_(src.reshape(run.f[k].shape), non_blocking=True)
+                    run.run(probs)
+                    outs = []
+                    for k, r in enumerate(reqs):
+                        out = torch.empty(run.u.shape[1:], dtype=torch.float64, pin_memory=True) \
+                            if self.keep_results else None
+                        if out is not None:
+                            out.copy_(run.u[k], non_blocking=True)
+                        r.result = out
+                        outs.append(out)
+                    ev = torch.cuda.Event()
+                    ev.record(s)
+            except Exception as e:  # launch failure: report, keep serving
+                for r in reqs:
+                    r.state = FAILED
+                    r.error = repr(e)
+                    self.failed.append(r.id)
+                continue
+            self._bid += 1
+            self.busy[si] = self._bid
+            self.inflight[("batch", self._bid)] = (reqs, ev, (outs, run, si))
+            self.batches += 1
+            self.batch_sizes[len(reqs)] += 1
+
+    def shrink_cache(self, room):
+        limit = max(0, min(room, self.cache_budget))
+        busy_keys = {r.key for reqs, _, _ in self.inflight.values() for r in reqs}
+        busy_keys |= {r.key for q in self.ready.values() for r in q}
+        busy_keys |= {r.key for r in self.waiting.values()}
+        busy_runners = {id(v[2][1]) for v in self.inflight.values()}
+        while self.runners and self.cache_bytes() > limit:
+            key, r = next(iter(self.runners.items()))
+            if id(r) in busy_runners:
+                break
+            self.runners.popitem(last=False)
+        while self.cache and self.cache_bytes() > limit:
+            key, _ = next(iter(self.cache.items()))
+            if key in busy_keys:
+                break  # still in use
+            self.cache.popitem(last=False)
+
+    def poll(self):
+        self._collect()
+        done, self.failed = list(self.failed), []
+        for bid, (reqs, ev, bufs) in list(self.inflight.items()):
+            if ev.query():
+                del self.inflight[bid]
+                self.busy.pop(bufs[2], None)
+                done.extend(r.id for r in reqs)
+        self._flush()
+        return done
+
+
+def make_stream(n, seed=0, rate=None, nmin=32, nmax=512, max_points=2 ** 24, families=("chebyshev", "legendre"),
+                sizes=None, shifts=None):
     """Synthetic request stream: dim in {2, 3} (50/50), N per axis log-uniform
     in [nmin, nmax], family uniform, shift c log-uniform in [0.1, 1e4],
     Poisson arrivals at `rate` requests/s (all at t = 0 when rate is None).
-    Grids with more than `max_points` points are redrawn (device memory)."""
+    Grids with more than `max_points` points are redrawn (device memory).
+    With `sizes` / `shifts` (sequences), N per axis and c are drawn
+    log-uniformly from those discrete values instead, so that keys repeat
+    (a serving population of fixed configurations with new right-hand
+    sides)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
     while len(out) < n:
         dim = 2 if rng.random() < 0.5 else 3
-        N = tuple(int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))) for _ in range(dim))
+        if sizes is not None:
+            N = tuple(int(sizes[int(rng.integers(len(sizes)))]) for _ in range(dim))
+        else:
+            N = tuple(int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))) for _ in range(dim))
         N = N[:-1] + (max(N[-1], 8),)
         if np.prod(N) > max_points:
             continue
         fam = families[int(rng.integers(len(families)))]
-        c = float(np.exp(rng.uniform(np.log(0.1), np.log(1e4))))
+        if shifts is not None:
+            c = float(shifts[int(rng.integers(len(shifts)))])
+        else:
+            c = float(np.exp(rng.uniform(np.log(0.1), np.log(1e4))))
         if rate:
             t += rng.exponential(1.0 / rate)
         out.append((N, fam, c, t, int(rng.integers(1 << 31))))

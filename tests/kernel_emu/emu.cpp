@@ -91,8 +91,9 @@ static int xform(int argc, char** argv) {
   double* out = (double*)malloc(sizeof(double) * (nout ? nout : 1));
   for (size_t i = 0; i < nout; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
   const long long nlines = outer * inner;
+  p.pb = getenv("SGPU_EMU_PB") ? atoll(getenv("SGPU_EMU_PB")) : 0;
   const int lpb = lines_per_block(p, dc);
-  const long long nblocks = (nlines + lpb - 1) / lpb;
+  const long long nblocks = dc ? (nlines + lpb - 1) / lpb : (pair_slots(nlines, p.pb) + p.tlc - 1) / p.tlc;
   const size_t nsm = p.smem / sizeof(double);
   for (long long b = 0; b < nblocks; ++b) {
     double* smem = (double*)malloc(p.smem);
@@ -161,8 +162,9 @@ static int f256_mode(int argc, char** argv) {
   double* in = read_exact(argv[6], nin);
   double* out = (double*)malloc(sizeof(double) * nout);
   for (size_t i = 0; i < nout; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
-  f256::Args a{in, out, outer * inner, inner, scl};
-  const int64_t nt = f256::tiles(kind, a.nlines);
+  const int64_t pbl = getenv("SGPU_EMU_PB") ? atoll(getenv("SGPU_EMU_PB")) : 0;
+  f256::Args a{in, out, outer * inner, inner, scl, pbl};
+  const int64_t nt = f256::tiles(kind, a.nlines, pbl);
   const size_t zb = form == SGPU_MIXED_DF ? f256::smem_bytes<df>() : f256::smem_bytes<double>();
   void* Z = malloc(zb);
   for (int64_t b = 0; b < nt; ++b) {

@@ -48,6 +48,8 @@ def test_fft256_variants_and_oracle(form, shape, axis):
         a = run(kind, f, xd, axis, 256, 1, scale)
         b = run(kind, f, xd, axis, 256, 2, scale)
         assert rel(a, b.cpu().numpy()) < tol
+        for v in (3, 4):  # the strided kernel at 2 and 3 CTAs per SM: the same arithmetic
+            assert torch.equal(run(kind, f, xd, axis, 256, v, scale), a)
         if small:
             ref = S.c2c_forward(xc, axis=axis) if kind == _lib.XF_C2C_FWD else S.c2c_backward(xc, axis=axis)
             assert rel(a, ref) < tol

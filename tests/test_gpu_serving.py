@@ -137,3 +137,46 @@ def test_background_build_failure_fails_only_its_requests(sg):
                              max_slots=1)
     for r in alone:
         assert torch.equal(r.result, by[r.id].result)
+
+
+@pytest.mark.parametrize("N,family", [((16, 12, 24), "chebyshev"), ((24, 31), "legendre"),
+                                      ((32, 33), "chebyshev"), ((8, 10, 20), "legendre")])
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_batched_step_equals_single_solves(sg, N, family, form):
+    """sgpu_helmholtz_solve_batch over K problems of one shape (different
+    shifts): the same bits as K single solves, eager and as a graph replay."""
+    from shenfun_gb300.problem import HelmholtzProblem, BatchRunner
+    shifts = [0.5, 3.0, 1000.0]
+    probs = [HelmholtzProblem(N, family, c, form) for c in shifts]
+    g = np.random.default_rng(9)
+    fs = [torch.as_tensor(g.standard_normal(N), device="cuda") for _ in shifts]
+    single = [p.solve(f) for p, f in zip(probs, fs)]
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    for graph in (False, True):
+        run = BatchRunner(probs[0], 4, s, graph=graph)  # one slot unused
+        with torch.cuda.stream(s):
+            for k, f in enumerate(fs):
+                run.f[k].copy_(f)
+            run.run(probs)
+        s.synchronize()
+        for k in range(len(shifts)):
+            assert torch.equal(run.u[k], single[k]), (graph, k)
+
+
+def test_batch_executor_mix_equals_alone(sg):
+    """The batching executor: requests batched per shape class through graph
+    replays give the bits of the same requests run alone, and repeated keys
+    hit the factorisation cache."""
+    from shenfun_gb300 import serving as SV
+    stream = SV.make_stream(40, seed=21, rate=None, sizes=(16, 24, 32), shifts=(0.5, 10.0, 1e3))
+    alone, _ = SV.run_stream(stream, SV.GpuExecutor(nstreams=1), max_slots=1)
+    ex = SV.BatchExecutor(nstreams=2, max_batch=8)
+    mix, _ = SV.run_stream(stream, ex, max_slots=64)
+    torch.cuda.synchronize()
+    a = {r.id: r for r in alone}
+    assert len(mix) == 40
+    for r in mix:
+        assert r.state == SV.DONE, r.error
+        assert torch.equal(a[r.id].result, r.result), r.id
+    assert ex.hits > 0 and max(ex.batch_sizes) > 1

@@ -665,3 +665,34 @@ def test_fft256_strided(emu, kind, outer, inner, form, monkeypatch):
         ref = S.r2c_backward(y, n, axis=1)
     assert np.isfinite(got).all()
     assert rel(got, ref) < 1e-13
+
+
+# ---- pairing blocks: a stack of arrays transformed at once gives each array's bits
+@pytest.mark.parametrize("kind,n,basis", [(R2C, 24, 0), (R2C, 256, 0), (C2R, 24, 0), (C2R, 256, 0),
+                                          (CHEB_SCALAR, 17, BASIS["SD"]), (CHEB_BACKWARD, 17, BASIS["SD"])])
+@pytest.mark.parametrize("inner", [1, 31])
+def test_pair_blocks_stack_equals_alone(emu, kind, n, basis, inner, monkeypatch):
+    g = np.random.default_rng(n + inner)
+    K, outer = 3, 3  # outer x inner lines per member: odd when inner is odd
+    if kind == C2R:
+        nin = n // 2 + 1
+        x = g.standard_normal((K * outer, nin, inner)) + 1j * g.standard_normal((K * outer, nin, inner))
+        n_out, cplx = n, True
+    else:
+        x = g.standard_normal((K * outer, n, inner))
+        n_out = n // 2 + 1 if kind == R2C else n
+        cplx = False
+    if n == 256 and inner >= 16 and kind in (R2C, C2R):
+        mode = ["f256", kind, K * outer, inner, repr(1.0)]
+        count_out = K * outer * n_out * inner * (2 if kind == R2C else 1)
+        runner = lambda arr, o: run(emu, ["f256", kind, o, inner, repr(1.0)], [arr],  # noqa: E731
+                                    o * n_out * inner * (2 if kind == R2C else 1))
+    else:
+        runner = lambda arr, o: xform(emu, kind, n, basis, arr, 1, cplx, 1.0, n_out).reshape(-1)  # noqa: E731
+    monkeypatch.setenv("SGPU_EMU_PB", str(outer * inner))
+    stacked = runner(x, K * outer)
+    monkeypatch.delenv("SGPU_EMU_PB")
+    per = stacked.size // K
+    for k in range(K):
+        alone = runner(x[k * outer:(k + 1) * outer], outer)
+        assert np.array_equal(stacked[k * per:(k + 1) * per], alone), k
