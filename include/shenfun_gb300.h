@@ -355,6 +355,12 @@ int sgpu_helmholtz_solve(const sgpu_helmholtz_problem* problem, const double* f,
  * bit for bit.  No counterpart in the reference. */
 int sgpu_helmholtz_batch_workspace_size(const sgpu_helmholtz_problem* problem, int K, size_t* bytes);
 int sgpu_helmholtz_factor_ptr(const sgpu_helmholtz_problem* problem, const void** fac);
+/* The transform plans of a problem's step, in order: Dirichlet-axis scalar
+ * product, R2C forward, C2C forward, C2C backward, C2R backward,
+ * Dirichlet-axis backward (null where the grid has no such pass or the family
+ * is Legendre), and each pass's (outer, inner) in lines[2 i], lines[2 i + 1];
+ * for tuning their kernel variants (sgpu_plan_set_variant). */
+int sgpu_helmholtz_plan_handles(const sgpu_helmholtz_problem* problem, sgpu_plan** plans, int64_t* lines);
 int sgpu_helmholtz_solve_batch(const sgpu_helmholtz_problem* problem, int K, const void* const* facs,
                                const double* f, double* u, void* work, size_t work_bytes, cudaStream_t stream);
 /* the batched solves under it: systems of member k at b + k nsys N (nsys =

@@ -100,6 +100,7 @@ SIGNATURES = {
     "sgpu_DMA_Solve": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _int, _vp]),
     "sgpu_helmholtz_batch_workspace_size": (_int, [_vp, _int, ctypes.POINTER(ctypes.c_size_t)]),
     "sgpu_helmholtz_factor_ptr": (_int, [_vp, ctypes.POINTER(_vp)]),
+    "sgpu_helmholtz_plan_handles": (_int, [_vp, _vp, _vp]),
     "sgpu_helmholtz_solve_batch": (_int, [_vp, _int, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]),
     "sgpu_helmholtz_solve_cached_batch": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64, _i64, _int, _int, _vp]),
     "sgpu_band_sep_solve_batch": (_int, [_vp, _vp, _vp, _vp, _int, _int, _i64, _i64, _i64, _int, _vp]),

@@ -431,6 +431,22 @@ extern "C" int sgpu_helmholtz_batch_workspace_size(const sgpu_helmholtz_problem*
   return SGPU_OK;
 }
 
+extern "C" int sgpu_helmholtz_plan_handles(const sgpu_helmholtz_problem* p, sgpu_plan** plans, int64_t* lines) {
+  if (!p || !plans || !lines) return SGPU_ERR_ARG;
+  const int64_t Nd = p->N[p->ndim - 1], nl = p->nphys / Nd;
+  sgpu_plan* h[6] = {p->d_s, p->fr_f, p->fx_f, p->fx_b, p->fr_b, p->d_b};
+  int64_t oi[12] = {nl, 1, 0, 0, 0, 0, 0, 0, 0, 0, nl, 1};
+  if (p->ndim == 2) {
+    oi[2] = 1, oi[3] = Nd, oi[8] = 1, oi[9] = Nd;
+  } else {
+    const int64_t Nh = p->N[1] / 2 + 1;
+    oi[2] = p->N[0], oi[3] = Nd, oi[4] = 1, oi[5] = Nh * Nd, oi[6] = 1, oi[7] = Nh * Nd, oi[8] = p->N[0], oi[9] = Nd;
+  }
+  for (int i = 0; i < 6; ++i) plans[i] = h[i];
+  for (int i = 0; i < 12; ++i) lines[i] = oi[i];
+  return SGPU_OK;
+}
+
 extern "C" int sgpu_helmholtz_factor_ptr(const sgpu_helmholtz_problem* p, const void** fac) {
   if (!p || !fac) return SGPU_ERR_ARG;
   *fac = p->fac;

@@ -49,6 +49,14 @@ class LinePlan:
         if (outer, inner) != (o2, i2):
             raise _lib.SgpuError(_lib.ERR_ARG, "input/output shapes differ off the axis")
         kind = data_kind(inp)
+        from . import autotune
+        if autotune.enabled():
+            lay = (outer, inner, kind)
+            tuned = self.__dict__.setdefault("_tuned", {})
+            if lay not in tuned:
+                tuned[lay] = autotune.apply(self, outer, inner, kind)
+            elif tuned[lay] is not None and self.variant != tuned[lay]:
+                self.variant = tuned[lay]
         nb = ctypes.c_size_t()
         _lib.call("sgpu_plan_workspace_size", self._h, outer, inner, kind, ctypes.byref(nb))
         work = None

@@ -345,12 +345,14 @@ class BatchExecutor(GpuExecutor):
     per-system solves), so results are the same alone and in a batch."""
 
     def __init__(self, nstreams=4, cache_budget=4 << 30, form="mixed", keep_results=True, prep_workers=4,
-                 max_batch=16, batch_bytes=1 << 30, graphs=True):
+                 max_batch=16, batch_bytes=1 << 30, graphs=True, tune=False):
         GpuExecutor.__init__(self, nstreams=nstreams, cache_budget=cache_budget, form=form,
                              keep_results=keep_results, prep_workers=prep_workers)
         self.max_batch = int(max_batch)
         self.batch_bytes = int(batch_bytes)
         self.graphs = graphs
+        self.tune = tune
+        self.tuned = {}  # class -> variants the autotuner picked for its plans
         self.ready = collections.OrderedDict()  # class -> deque of requests whose problem is cached
         self.runners = collections.OrderedDict()  # (class, K) -> BatchRunner
         self.busy = {}  # stream index -> batch id in flight
@@ -421,6 +423,10 @@ class BatchExecutor(GpuExecutor):
         if r is not None:
             self.runners.move_to_end(key)
             return r
+        if self.tune and cls not in self.tuned:
+            from . import autotune
+            self.streams[si].synchronize()
+            self.tuned[cls] = autotune.tune_problem(proto)  # before the graph captures the variants
         r = BatchRunner(proto, K, self.streams[si], graph=self.graphs)
         r.bytes = r.f.numel() * 16 + r.work.numel()
         self.runners[key] = r

@@ -1,0 +1,59 @@
+"""The autotuner on the GPU: it times the variants of real plans, records
+the fastest per layout, sets it on the plan, and a tuned problem gives the
+same results."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def tune_cache(tmp_path, monkeypatch):
+    from shenfun_gb300 import autotune
+    monkeypatch.setenv("SGPU_TUNE_CACHE", str(tmp_path / "tuning.json"))
+    monkeypatch.setattr(autotune, "_records", None)
+    return tmp_path / "tuning.json"
+
+
+def test_tune_fourier_and_fused_plans(tune_cache):
+    from shenfun_gb300 import _lib, autotune
+    from shenfun_gb300.plans import LinePlan
+    p = LinePlan(_lib.XF_C2C_FWD, 256, form=_lib.MIXED_DF)
+    v = autotune.tune_plan(p, 1, 129 * 40, _lib.COMPLEX)
+    assert v in (1, 2, 3, 4)
+    rec = autotune._load()[autotune.key(p, 1, 129 * 40, _lib.COMPLEX)]
+    assert set(rec["us"]) == {"1", "2", "3", "4"}
+    assert autotune.lookup(p, 1, 129 * 40, _lib.COMPLEX) == v
+    q = LinePlan(_lib.XF_CHEB_SCALAR, 257, basis=_lib.BASIS_SD, form=_lib.MIXED_DF)
+    assert autotune.tune_plan(q, 4096, 1, _lib.REAL) in (1, 2)
+    assert tune_cache.exists()
+
+
+def test_enabled_plans_apply_their_tuned_variant(tune_cache):
+    from shenfun_gb300 import _lib, autotune
+    from shenfun_gb300.plans import LinePlan
+    autotune.enable(True)
+    try:
+        p = LinePlan(_lib.XF_R2C, 256, form=_lib.MIXED_DF)
+        x = torch.randn(8, 256, 33, dtype=torch.float64, device="cuda")
+        y = torch.empty(8, 129, 33, dtype=torch.complex128, device="cuda")
+        p(x, y, 1, 1.0 / 256)
+        v = autotune.lookup(p, 8, 33, _lib.REAL)
+        assert v is not None and p.variant == v
+        ref = np.fft.rfft(x.cpu().numpy(), axis=1) / 256
+        assert np.abs(y.cpu().numpy() - ref).max() / np.abs(ref).max() < 1e-13
+    finally:
+        autotune.enable(False)
+
+
+def test_tune_problem_keeps_results(tune_cache):
+    from shenfun_gb300 import autotune
+    from shenfun_gb300.problem import HelmholtzProblem
+    f = torch.as_tensor(np.random.default_rng(2).standard_normal((256, 40, 33)), device="cuda")
+    p = HelmholtzProblem((256, 40, 33), "chebyshev", 10.0, "mixed")
+    u0 = p.solve(f).clone()
+    chosen = autotune.tune_problem(p)
+    assert {"c2c_fwd", "c2c_bwd", "dirichlet_scalar", "dirichlet_backward"} <= set(chosen)
+    u1 = p.solve(f)
+    assert float((u1 - u0).abs().max() / u0.abs().max()) < 1e-12
