@@ -338,28 +338,66 @@ def stage_times(torch, run, flush, st, reps=5):
     return out
 
 
-def serving_leg(torch, nreq=200, seed=5, form="mixed"):
-    """Serving stream: mixed 2D/3D Fourier x Chebyshev/Legendre Dirichlet
-    Helmholtz requests, N per axis log-uniform in [32, 512] (grids above 2^24
-    points redrawn), c log-uniform in [0.1, 1e4].  First all requests at once
-    (saturation throughput C), then Poisson arrivals at 0.5 C: latency =
-    completion - arrival, under load but below saturation."""
+SERVE_SIZES = (32, 64, 128, 256, 512)
+SERVE_SHIFTS = (0.1, 1.0, 10.0, 100.0, 1e3, 1e4)
+
+
+def serving_leg(torch, nreq=10000, seed=5, form="mixed", fractions=(0.75, 0.5, 0.25), cache_gb=64,
+                compare=2000):
+    """Serving stream of `nreq` mixed 2D/3D Fourier x Chebyshev/Legendre
+    Dirichlet Helmholtz requests: N per axis drawn log-uniformly from
+    {32, 64, 128, 256, 512} (3D grids above 2^24 points redrawn), c drawn
+    log-uniformly from {0.1, 1, 10, 100, 1e3, 1e4} (a population of fixed
+    configurations, so that factorisations repeat), family 50/50, RHS N(0, 1)
+    (two seeded arrays per grid shape, page-locked on the host; every request
+    copies its RHS to the device).  One batching executor (graphs of batched
+    steps, device factorisation cache of `cache_gb` GB, LRU) runs: all
+    requests at once on a cold cache, all at once warm (saturation
+    throughput C), then Poisson arrivals at each fraction of C (latency =
+    completion - arrival).  The per-request executor (no batching) runs the
+    first `compare` requests warm for comparison.  Solutions stay on the
+    device."""
+    import collections
     from shenfun_gb300 import serving as SV
-    out = []
-    rate = None
-    for _ in range(2):
-        stream = SV.make_stream(nreq, seed=seed, rate=rate)
-        ex = SV.GpuExecutor(nstreams=4, cache_budget=8 << 30, keep_results=False, form=form)
-        fin, elapsed = SV.run_stream(stream, ex, max_slots=8, mem_budget=24 << 30)
+    pool = SV.RhsPool(per_shape=2, seed=seed)
+    budget = (cache_gb + 32) << 30
+
+    def one(label, ex, rate, n):
+        stream = SV.make_stream(n, seed=seed, rate=rate, sizes=SERVE_SIZES, shifts=SERVE_SHIFTS)
+        h0, m0 = ex.hits, ex.misses
+        b0 = collections.Counter(getattr(ex, "batch_sizes", {}))
+        fin, elapsed = SV.run_stream(stream, ex, max_slots=256, mem_budget=budget, rhs=pool)
         torch.cuda.synchronize()
-        lat = np.array([r.latency for r in fin if r.state == SV.DONE])
-        res = {"rate_req_per_s": rate, "requests": nreq, "completed": int(len(lat)), "form": form,
-               "solves_per_s": len(lat) / elapsed, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-               "p99_ms": 1e3 * float(np.percentile(lat, 99)),
-               "cache_hits": ex.hits, "cache_misses": ex.misses}
-        out.append(res)
-        rate = 0.5 * res["solves_per_s"]
-    return out
+        done = [r for r in fin if r.state == SV.DONE]
+        lat = np.array([r.latency for r in done])
+        pts = sum(int(np.prod(r.N)) for r in done)
+        res = {"run": label, "rate_req_per_s": rate, "requests": n, "completed": len(done),
+               "failed": sum(r.state != SV.DONE for r in fin),
+               "solves_per_s": len(done) / elapsed, "grid_points_per_s": pts / elapsed,
+               "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+               "cache_hits": ex.hits - h0, "cache_misses": ex.misses - m0, "seconds": elapsed}
+        if hasattr(ex, "batch_sizes"):
+            bs = ex.batch_sizes - b0
+            nb = sum(bs.values())
+            res["batches"] = nb
+            res["mean_batch"] = sum(k * v for k, v in bs.items()) / max(nb, 1)
+            res["batch_size_hist"] = {str(k): v for k, v in sorted(bs.items())}
+        return res
+
+    ex = SV.BatchExecutor(nstreams=4, cache_budget=cache_gb << 30, keep_results=False, form=form)
+    runs = [one("all at once, cold cache", ex, None, nreq), one("all at once, warm (saturation)", ex, None, nreq)]
+    C = runs[-1]["solves_per_s"]
+    for fr in fractions:
+        runs.append(one(f"Poisson at {fr} x saturation", ex, fr * C, nreq))
+    if ex.pool is not None:
+        ex.pool.shutdown()
+    del ex
+    torch.cuda.empty_cache()
+    ex1 = SV.GpuExecutor(nstreams=4, cache_budget=cache_gb << 30, keep_results=False, form=form)
+    one("per-request executor, cold", ex1, None, compare)
+    runs.append(one("per-request executor (no batching), all at once, warm", ex1, None, compare))
+    return {"requests_per_run": nreq, "form": form, "sizes": list(SERVE_SIZES), "shifts": list(SERVE_SHIFTS),
+            "cache_budget_gb": cache_gb, "rhs_host_gb": pool.nbytes / 1e9, "runs": runs}
 
 
 def legendre_leg(torch, flush, st, N=512, lines=16384, reps=5):
@@ -403,19 +441,64 @@ def legendre_leg(torch, flush, st, N=512, lines=16384, reps=5):
     return out
 
 
+def legendre_cpu(N, lines_max=4096, budget_flop=3e8):
+    """The reference's recursive Legendre transforms (compiled transforms.pyx
+    when built, else the numpy restatement) on one host thread, on a sample
+    of lines sized to about budget_flop multiply-adds per direction."""
+    from oracle.cpu_baseline import LegendreLines, time_calls
+    n = int(max(64, min(lines_max, budget_flop // (N * N))))
+    L = LegendreLines(N, n)
+    tb = float(np.median(time_calls(L.backward, 2)))
+    tf = float(np.median(time_calls(L.forward, 2)))
+    return {"kind": L.kind, "cores": 1, "sample_lines": n,
+            "lines_per_s_backward": n / tb, "lines_per_s_forward": n / tf,
+            "gflops_fp64_backward": 2.0 * N * N * n / tb / 1e9}
+
+
+def legendre_sweep(torch, flush, st, Ns=(128, 256, 512, 1024), lines=(4096, 16384, 65536), reps=3):
+    """The batched Legendre configuration: N in Ns x lines per launch, both
+    forms (legendre_leg), and per N the reference's CPU transforms on a
+    sample (lines/s on one thread; GPU/CPU ratio at the largest line count)."""
+    out = []
+    for N in Ns:
+        cpu = legendre_cpu(N)
+        for L in lines:
+            r = legendre_leg(torch, flush, st, N=N, lines=L, reps=reps)
+            m = r["forms"]["mixed"]
+            r["lines_per_s_mixed"] = {"backward": L / (m["ms_backward"] * 1e-3),
+                                      "forward": L / (m["ms_forward"] * 1e-3)}
+            r["cpu_reference"] = cpu
+            r["gpu_mixed_over_cpu"] = {
+                "backward": r["lines_per_s_mixed"]["backward"] / cpu["lines_per_s_backward"],
+                "forward": r["lines_per_s_mixed"]["forward"] / cpu["lines_per_s_forward"]}
+            out.append(r)
+    return out
+
+
 def biharmonic_leg(torch, flush, st, steps=10):
-    """Fourier 128 (C2C) x Fourier 128 (R2C) x Chebyshev ShenBiharmonic 129:
-    scalar product of a random RHS (seed 0) -> biharmonic solve (8,320
-    banded + rank-2 semiseparable systems) -> backward, L2 flushed before
-    every step; forms plain (FP64), mixed (mixed transforms, FP64 direct
-    solve) and mixed-refined (mixed transforms, FP32 solve refined by the
-    FP64 residual); error of each form against the plain one, correction
-    counts of the refined solve."""
+    """Fourier 128 (C2C) x Fourier 128 (R2C) x Chebyshev ShenBiharmonic 129,
+    RHS f = lap^2 u of the manufactured u = sin(x) cos(y) (1 - z^2)^2
+    sampled on the quadrature grid: scalar product -> biharmonic solve
+    (8,320 banded + rank-2 semiseparable systems) -> backward, L2 flushed
+    before every step; forms plain (FP64), mixed (mixed transforms, FP64
+    direct solve) and mixed-refined (mixed transforms, FP32 solve refined by
+    the FP64 residual); error of each form against u and against the plain
+    form, correction counts of the refined solve.  The reference's CPU path
+    on the same grid beside it (its LU_Biharmonic leaves the last even row
+    unfactored when N - 4 is odd, as here, and its solve returns non-finite
+    values: the CPU figure is a timing only)."""
     import shenfun_gb300 as sg
     Nx, Ny, Nz = 128, 128, 129
-    f = np.random.default_rng(0).standard_normal((Nx, Ny, Nz))
-    out = {"workload": "Fourier 128 (C2C) x Fourier 128 (R2C) x Chebyshev ShenBiharmonic 129, RHS N(0,1) seed 0"}
+    x = 2 * np.pi * np.arange(Nx) / Nx
+    y = 2 * np.pi * np.arange(Ny) / Ny
+    z = np.cos(np.pi * (2 * np.arange(Nz) + 1) / (2 * Nz))
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    u_exact = np.sin(X) * np.cos(Y) * (1 - Z ** 2) ** 2
+    f = np.sin(X) * np.cos(Y) * (44 - 56 * Z ** 2 + 4 * Z ** 4)
+    out = {"workload": "Fourier 128 (C2C) x Fourier 128 (R2C) x Chebyshev ShenBiharmonic 129, "
+                       "RHS lap^2 u, u = sin(x)cos(y)(1-z^2)^2"}
     ref = None
+    ue = torch.as_tensor(u_exact, device="cuda")
     for form in ("plain", "mixed", "mixed-refined"):
         T = sg.TensorProductSpace(None, (sg.FunctionSpace(Nx, "F", dtype="D"), sg.FunctionSpace(Ny, "F", dtype="d"),
                                          sg.FunctionSpace(Nz, "C", bc=(0, 0, 0, 0))),
@@ -435,7 +518,8 @@ def biharmonic_leg(torch, flush, st, steps=10):
             step()
         torch.cuda.synchronize()
         ms = float(np.mean(time_steps_gpu(torch, step, steps, flush, st)))
-        res = {"ms_per_step": ms, "solves_per_s": 1e3 / ms}
+        res = {"ms_per_step": ms, "solves_per_s": 1e3 / ms,
+               "rel_err_vs_exact": float(((uq.v - ue).abs().max() / ue.abs().max()).item())}
         # the solve alone
         H(f_hat, u_hat)
         torch.cuda.synchronize()
@@ -448,6 +532,18 @@ def biharmonic_leg(torch, flush, st, steps=10):
             it = H.last_iterations.cpu().numpy()
             res["corrections"] = {"max": int(it.max()), "mean": float(it.mean())}
         out[form] = res
+    from oracle.cpu_baseline import BiharmonicRoundTrip, time_steps
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        rt = BiharmonicRoundTrip(Nx, Ny, Nz)
+        ts = time_steps(rt, f, 3, 1)
+        finite = bool(np.isfinite(rt.step(f)).all())
+    out["cpu_baseline"] = {"value": len(ts) / float(sum(ts)), "unit": "solves/s", "cores": 1, "kind": rt.kind,
+                           "sample": f"{len(ts)} full round trips on 1 host thread (scipy.fft for FFTW, "
+                                     f"reference LU_Biharmonic/Biharmonic_Solve), factorisation excluded "
+                                     f"({rt.setup_s:.2f} s)",
+                           "output_finite": finite}
     return out
 
 
@@ -569,15 +665,27 @@ def dealias_leg(torch, flush, st, steps=10):
 
 
 def latency_leg(torch, reps=200):
-    """Small 2D Poisson on Fourier 64 x Chebyshev ShenDirichlet 64 (33
-    systems): per-solve latency of the round trip, eager and as one CUDA-graph
-    replay (inputs resident, no L2 flush: a latency figure)."""
+    """2D Poisson on Fourier 64 (x, [0, 2 pi)) x Chebyshev ShenDirichlet 64
+    (y): manufactured u = sin(2x) (1 - y^2) cos(pi y / 2), f = -lap u on the
+    quadrature grid; per-solve latency of the round trip (33 systems), eager
+    and as one CUDA-graph replay (inputs resident, no L2 flush: a latency
+    figure), the error against u, and the reference's CPU path on the same
+    grid."""
     import shenfun_gb300 as sg
-    T = sg.TensorProductSpace(None, (sg.FunctionSpace(64, "F", dtype="d"), sg.FunctionSpace(64, "C", bc=(0, 0))),
+    Nx = Ny = 64
+    T = sg.TensorProductSpace(None, (sg.FunctionSpace(Nx, "F", dtype="d"), sg.FunctionSpace(Ny, "C", bc=(0, 0))),
                               axes=(1, 0))
     u, v = sg.TrialFunction(T), sg.TestFunction(T)
     H = sg.chebyshev.la.Helmholtz(*sg.inner(v, -sg.div(sg.grad(u))))
-    fj = sg.Array(T, buffer=np.random.default_rng(0).standard_normal((64, 64)))
+    x = 2 * np.pi * np.arange(Nx) / Nx
+    y = np.cos(np.pi * (2 * np.arange(Ny) + 1) / (2 * Ny))
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    cy, sy = np.cos(np.pi * Y / 2), np.sin(np.pi * Y / 2)
+    g = (1 - Y ** 2) * cy
+    gpp = -2 * cy + 2 * np.pi * Y * sy - (np.pi ** 2 / 4) * (1 - Y ** 2) * cy
+    u_exact = np.sin(2 * X) * g
+    f = np.sin(2 * X) * (4 * g - gpp)
+    fj = sg.Array(T, buffer=f)
     f_hat, u_hat, uq = sg.Function(T), sg.Function(T), sg.Array(T)
 
     def step():
@@ -585,18 +693,18 @@ def latency_leg(torch, reps=200):
         H(f_hat, u_hat)
         T.backward(u_hat.v, uq.v)
 
-    out = {"workload": "2D Poisson, Fourier 64 x Chebyshev ShenDirichlet 64"}
+    out = {"workload": "2D Poisson, Fourier 64 x Chebyshev ShenDirichlet 64, u = sin(2x)(1-y^2)cos(pi y/2)"}
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
         for _ in range(3):
             step()
     torch.cuda.current_stream().wait_stream(s)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
+    g_ = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_):
         step()
     st = torch.cuda.current_stream()
-    for mode, fn in (("eager", step), ("graph", g.replay)):
+    for mode, fn in (("eager", step), ("graph", g_.replay)):
         fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -606,6 +714,15 @@ def latency_leg(torch, reps=200):
         e1.record(st)
         e1.synchronize()
         out[f"us_per_solve_{mode}"] = 1e3 * e0.elapsed_time(e1) / reps
+    got = uq.v.cpu().numpy()
+    out["rel_err_vs_exact"] = float(np.abs(got - u_exact).max() / np.abs(u_exact).max())
+    from oracle.cpu_baseline import Poisson2D, time_calls
+    pz = Poisson2D(Nx, Ny)
+    ts = time_calls(lambda: pz.step(f), 50, 3)
+    out["cpu_baseline"] = {"us_per_solve": 1e6 * float(np.median(ts)), "cores": 1, "kind": pz.kind,
+                           "sample": "50 round trips on 1 host thread (scipy.fft for FFTW, reference "
+                                     "LU_Helmholtz/Solve_Helmholtz), median",
+                           "rel_err_vs_exact": float(np.abs(pz.step(f) - u_exact).max() / np.abs(u_exact).max())}
     return out
 
 
@@ -868,9 +985,9 @@ def main():
     serving = legendre = imex = biharmonic = latency = neumann = dealias = refinement = None
     if rank == 0 and not args.no_extra:
         serving = serving_leg(torch)
-        legendre = legendre_leg(torch, flush, st)
-        # beyond one exact K chunk (1024): two chunk launches per contraction
-        legendre["N2048"] = legendre_leg(torch, flush, st, N=2048, lines=4096, reps=3)
+        legendre = {"sweep": legendre_sweep(torch, flush, st),
+                    # beyond one exact K chunk (1024): two chunk launches per contraction
+                    "N2048": legendre_leg(torch, flush, st, N=2048, lines=4096, reps=3)}
         imex = imex_leg(torch)
         biharmonic = biharmonic_leg(torch, flush, st)
         refinement = refinement_leg(torch, flush, st, f_np)

@@ -100,7 +100,13 @@ def lu_biharmonic_oe(odd, a, b, c, sii, siu, siuu, ail, aii, aiu, bill, bil, bii
 
 def lu_biharmonic(a0, alfa, beta, sii, siu, siuu, ail, aii, aiu, bill, bil, bii, biu, biuu, u0, u1, u2, l0, l1,
                   axis=0):
-    """la.pyx:975 LU_Biharmonic: fills the (2, ..., M, ...) factor arrays in place."""
+    """la.pyx:975 LU_Biharmonic: fills the (2, ..., M, ...) factor arrays in place.
+
+    Rows per parity: the 1D kernel (la.pyx:991-1016) factors the length of
+    each parity's slice of sii; the 2D and 3D kernels (la.pyx:1651, 1950)
+    factor len(sii) // 2 rows for both parities.  With an odd number of dofs
+    the 2D/3D kernels therefore leave the last even row at zero (and the
+    reference's solve then divides by it), which this restatement keeps."""
     shape = u0.shape[1:]
     M = shape[axis]
     sys_shape = list(shape)
@@ -108,10 +114,14 @@ def lu_biharmonic(a0, alfa, beta, sii, siu, siuu, ail, aii, aiu, bill, bil, bii,
     b = np.broadcast_to(np.asarray(alfa, dtype=float), sys_shape).reshape(-1)
     c = np.broadcast_to(np.asarray(beta, dtype=float), sys_shape).reshape(-1)
     diags = (sii, siu, siuu, ail, aii, aiu, bill, bil, bii, biu, biuu)
+    nd = np.asarray(sii).shape[0]
     for odd in (0, 1):
-        res = lu_biharmonic_oe(odd, float(a0), b, c, *[np.asarray(d)[odd::2] for d in diags], M)
+        Mp = (nd - odd + 1) // 2 if len(shape) == 1 else nd // 2
+        res = lu_biharmonic_oe(odd, float(a0), b, c, *[np.asarray(d)[odd::2] for d in diags], Mp)
         for arr, r in zip((u0, u1, u2, l0, l1), res):
-            arr[odd] = _unsys(r, shape, axis)
+            full = np.zeros((M, r.shape[1]))
+            full[:Mp] = r
+            arr[odd] = _unsys(full, shape, axis)
 
 
 def biharmonic_factor_pr(ak, bk, l0, l1, axis=0):

@@ -54,6 +54,7 @@ class LinePlan:
             lay = (outer, inner, kind)
             tuned = self.__dict__.setdefault("_tuned", {})
             if lay not in tuned:
+                tuned[lay] = None  # the tuner's own calls of this plan run as set
                 tuned[lay] = autotune.apply(self, outer, inner, kind)
             elif tuned[lay] is not None and self.variant != tuned[lay]:
                 self.variant = tuned[lay]

@@ -84,14 +84,21 @@ class HelmholtzProblem:
 class BatchRunner:
     """K problems of one shape class (N, family, form), different shifts,
     solved with one launch per stage (sgpu_helmholtz_solve_batch) on fixed
-    staging buffers, captured once as a CUDA graph and replayed: per batch
-    the members' right-hand sides are copied into the input slots, the
+    staging buffers, captured as a CUDA graph and replayed: per batch the
+    members' right-hand sides are copied into the input slots, the
     factor-pointer table is updated, the graph is replayed and the solutions
     are read from the output slots.  The graph allocates nothing and reads
     the table at replay time, so any K problems of the class (any shifts) can
-    share it."""
+    share it.
 
-    def __init__(self, proto, K, stream, graph=True):
+    With ``capture_after=0`` the graph is captured at construction (after one
+    warm-up launch); with ``capture_after=n`` the first n batches run as
+    plain launches and the graph is captured at the next one, so that a
+    runner used once costs no capture.  Capture neither synchronises the
+    device nor touches torch's allocator (the capture of torch.cuda.graph
+    does both), so a serving loop can capture while other streams work."""
+
+    def __init__(self, proto, K, stream, graph=True, capture_after=0):
         self.proto = proto
         self.K = int(K)
         self.stream = stream
@@ -103,29 +110,39 @@ class BatchRunner:
             _lib.call("sgpu_helmholtz_batch_workspace_size", proto._h, self.K, ctypes.byref(nb))
             self.work = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device="cuda")
             self.table = torch.zeros(self.K, dtype=torch.int64, device="cuda")
-        self.table_host = torch.zeros(self.K, dtype=torch.int64, pin_memory=True)
         self.graph = None
-        if graph:
+        self.use_graph = bool(graph)
+        self.capture_after = int(capture_after)
+        self.runs = 0
+        if self.use_graph and self.capture_after == 0:
+            p = ctypes.c_void_p()
+            _lib.call("sgpu_helmholtz_factor_ptr", proto._h, ctypes.byref(p))
+            self._set_table([p.value] * self.K)  # valid pointers for the warm-up launch
+            with torch.cuda.stream(stream):
+                self._launch()  # warm-up outside the capture (plan attributes, lazy state)
             self._capture()
 
     def _launch(self):
         _lib.call("sgpu_helmholtz_solve_batch", self.proto._h, self.K, self.table.data_ptr(), self.f.data_ptr(),
                   self.u.data_ptr(), self.work.data_ptr(), self.work.numel(), stream_handle(self.stream))
 
-    def _capture(self):
-        # the table must hold valid pointers while the warm-up launch runs
-        p = ctypes.c_void_p()
-        _lib.call("sgpu_helmholtz_factor_ptr", self.proto._h, ctypes.byref(p))
-        self.table_host.fill_(p.value)
+    def _set_table(self, ptrs):
+        # a fresh page-locked source per batch: the previous batch's copy may
+        # still be queued (torch's host allocator keeps it until that copy ran)
+        host = torch.tensor(ptrs, dtype=torch.int64).pin_memory()
         with torch.cuda.stream(self.stream):
-            self.table.copy_(self.table_host, non_blocking=True)
-            self._launch()  # warm-up outside the capture (plan attributes, lazy state)
-        self.stream.synchronize()
+            self.table.copy_(host, non_blocking=True)
+
+    def _capture(self):
         g = torch.cuda.CUDAGraph()
-        # thread-local capture: worker threads keep creating problems
+        # thread-local capture mode: worker threads keep creating problems
         # (stream-ordered allocations) while this thread captures
-        with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-            self._launch()
+        with torch.cuda.stream(self.stream):
+            g.capture_begin(capture_error_mode="thread_local")
+            try:
+                self._launch()
+            finally:
+                g.capture_end()
         self.graph = g
 
     def run(self, problems):
@@ -138,12 +155,12 @@ class BatchRunner:
             _lib.call("sgpu_helmholtz_factor_ptr", p._h, ctypes.byref(q))
             ptrs.append(q.value)
         ptrs += [ptrs[-1]] * (self.K - len(ptrs))
-        # a fresh page-locked source per batch: the previous batch's copy may
-        # still be queued (torch's host allocator keeps it until that copy ran)
-        host = torch.tensor(ptrs, dtype=torch.int64).pin_memory()
+        self._set_table(ptrs)
+        if self.graph is None and self.use_graph and self.runs >= self.capture_after:
+            self._capture()
         with torch.cuda.stream(self.stream):
-            self.table.copy_(host, non_blocking=True)
             if self.graph is not None:
                 self.graph.replay()
             else:
                 self._launch()
+        self.runs += 1

@@ -427,7 +427,9 @@ class BatchExecutor(GpuExecutor):
             from . import autotune
             self.streams[si].synchronize()
             self.tuned[cls] = autotune.tune_problem(proto)  # before the graph captures the variants
-        r = BatchRunner(proto, K, self.streams[si], graph=self.graphs)
+        # a runner's first batch runs as plain launches, later ones replay
+        # the graph captured at its second batch
+        r = BatchRunner(proto, K, self.streams[si], graph=self.graphs, capture_after=1)
         r.bytes = r.f.numel() * 16 + r.work.numel()
         self.runners[key] = r
         return r
@@ -547,14 +549,47 @@ def make_stream(n, seed=0, rate=None, nmin=32, nmax=512, max_points=2 ** 24, fam
     return out
 
 
-def run_stream(stream, executor, max_slots=8, mem_budget=8 << 30, poll_sleep=0.0):
+class RhsPool:
+    """Right-hand sides of a synthetic stream: `per_shape` seeded N(0, 1)
+    arrays per grid shape, page-locked, made on first use and shared by the
+    requests of that shape (request i of a shape gets array i mod
+    `per_shape`), so that a stream of thousands of requests holds a bounded
+    amount of host memory."""
+
+    def __init__(self, per_shape=2, seed=0, pinned=True):
+        self.per_shape = int(per_shape)
+        self.seed = int(seed)
+        self.pinned = pinned
+        self.arrays = {}
+
+    def __call__(self, N, seed):
+        N = tuple(int(n) for n in N)
+        k = (N, int(seed) % self.per_shape)
+        a = self.arrays.get(k)
+        if a is None:
+            f = np.random.default_rng([self.seed, k[1]] + list(N)).standard_normal(N)
+            if self.pinned:
+                import torch
+                a = torch.from_numpy(f).pin_memory()
+            else:
+                a = f
+            self.arrays[k] = a
+        return a
+
+    @property
+    def nbytes(self):
+        return sum(int(a.nbytes) if hasattr(a, "nbytes") else a.numel() * 8 for a in self.arrays.values())
+
+
+def run_stream(stream, executor, max_slots=8, mem_budget=8 << 30, poll_sleep=0.0, rhs=None):
     """Drive a stream through the scheduler in wall-clock time; returns the
-    finished requests and the elapsed seconds."""
+    finished requests and the elapsed seconds.  `rhs(N, seed)` gives a
+    request's right-hand side (default: a fresh seeded N(0, 1) array)."""
     sched = Scheduler(executor, max_slots=max_slots, mem_budget=mem_budget)
     reqs = []
     prepare = getattr(executor, "prepare", None)
     for i, (N, fam, c, t, seed) in enumerate(stream):
-        f = np.random.default_rng(seed).standard_normal(N)
+        f = rhs(N, seed) if rhs is not None else np.random.default_rng(seed).standard_normal(N)
         reqs.append(Request(i, N, fam, c, prepare(f) if prepare else f, t))
     t0 = time.perf_counter()
     now = lambda: time.perf_counter() - t0  # noqa: E731
