@@ -342,7 +342,7 @@ SERVE_SIZES = (32, 64, 128, 256, 512)
 SERVE_SHIFTS = (0.1, 1.0, 10.0, 100.0, 1e3, 1e4)
 
 
-def serving_leg(torch, nreq=10000, seed=5, form="mixed", fractions=(0.75, 0.5, 0.25), cache_gb=64,
+def serving_leg(torch, nreq=10000, seed=5, form="mixed", fractions=(0.75, 0.5, 0.25), cache_gb=128,
                 compare=2000):
     """Serving stream of `nreq` mixed 2D/3D Fourier x Chebyshev/Legendre
     Dirichlet Helmholtz requests: N per axis drawn log-uniformly from
@@ -780,8 +780,11 @@ CASES = {
     "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
     "solve-plain": ("solve", "plain"),
     "leg-plain": ("leg", "plain"), "leg-mixed": ("leg", "mixed"),
+    "leg128-mixed": ("leg128", "mixed"),
     # the whole round-trip step (scalar product, solve, backward)
     "step-plain": ("step", "plain"), "step-mixed": ("step", "mixed"),
+    # the 2D Poisson round trip on Fourier 64 x Chebyshev ShenDirichlet 64
+    "poisson2d-plain": ("poisson2d", "plain"),
 }
 
 
@@ -849,10 +852,30 @@ def run_case(name, reps=3):
         c = torch.randn(16384, 512, dtype=torch.float64, device="cuda")
         y = torch.empty_like(c)
         fn = lambda: V.backward(c, y, axis=1)  # noqa: E731
+    elif kind == "leg128":
+        # Legendre ShenDirichlet N = 128 backward over 65,536 lines
+        from shenfun_gb300.legendre import LegendreShenDirichlet
+        V = LegendreShenDirichlet(128, form=form)
+        c = torch.randn(65536, 128, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(c)
+        fn = lambda: V.backward(c, y, axis=1)  # noqa: E731
     elif kind == "step":
         import shenfun_gb300 as sg
         run = FormRun(sg, form, x.cpu().numpy())
         fn = run.step
+    elif kind == "poisson2d":
+        import shenfun_gb300 as sg
+        T = sg.TensorProductSpace(None, (sg.FunctionSpace(64, "F", dtype="d"),
+                                         sg.FunctionSpace(64, "C", bc=(0, 0))), axes=(1, 0))
+        u, v = sg.TrialFunction(T), sg.TestFunction(T)
+        H = sg.chebyshev.la.Helmholtz(*sg.inner(v, -sg.div(sg.grad(u))))
+        fj = sg.Array(T, buffer=np.random.default_rng(0).standard_normal((64, 64)))
+        f_hat, u_hat, uq = sg.Function(T), sg.Function(T), sg.Array(T)
+
+        def fn():
+            sg.inner(v, fj, output_array=f_hat)
+            H(f_hat, u_hat)
+            T.backward(u_hat.v, uq.v)
     else:
         import shenfun_gb300 as sg
         run = FormRun(sg, form, x.cpu().numpy())

@@ -11,7 +11,8 @@
 // K is the stencil matrix with the reference's convention that the constant
 // entries of ShenDirichlet apply to every row (spectralbase.py:1504-1526), so
 // the scalar product keeps the orthogonal coefficients in the tail rows.
-// The matrices are built on the host in long double and stored in FP64.
+// The matrices are built on the host in double-double (ddouble.h) and
+// stored in FP64.
 // Plain form: FP64 tiled GEMM (k_line_gemm_f64).  Mixed form: the same
 // matrices split into BF16 digit slices and contracted on the tensor cores
 // (ozaki_tc.cu), about 48 bits, for N <= 8192 (above 1024 as one exact
@@ -27,17 +28,18 @@
 #include <thread>
 #include <vector>
 
+#include "ddouble.h"
 #include "ozaki_tc.h"
 #include "solvers.cuh"
 
 using namespace sgpu;
 
-typedef long double ld_t;
+using ddm::dd;
+using ddm::to_double;
 
 namespace {
 // run body(i) for i in [0, n) on up to 16 host threads (independent
-// iterations only): the plan's long-double set-up is O(N^2) and, on hosts
-// where long double is a software format, worth spreading
+// iterations only): the plan's double-double set-up is O(N^2)
 template <class F>
 void parallel_for(int n, F body) {
   const unsigned hw = std::thread::hardware_concurrency();
@@ -57,51 +59,56 @@ void parallel_for(int n, F body) {
 
 // Gauss-Legendre nodes (ascending) and weights: Newton iteration on P_N from
 // Tricomi's asymptotic initial guesses, P_N and P_N' by the three-term
-// recurrence in long double (Golub & Welsch 1969 give the same rule; the
-// reference uses Bogaert's 2014 iteration-free method, legendre/fastgl).
+// recurrence, first in FP64 and then two steps in double-double (Newton
+// doubles the correct digits per step); Golub & Welsch 1969 give the same
+// rule, the reference uses Bogaert's 2014 iteration-free method
+// (legendre/fastgl).
+namespace {
+// P_N(z) and P_{N-1}(z)
+template <class T>
+void legendre_pn(int N, const T& z, T& pn, T& pm) {
+  T p0 = T(1.0), p1 = z;
+  for (int k = 2; k <= N; ++k) {
+    T p2 = ((double)(2 * k - 1) * z * p1 - (double)(k - 1) * p0) / (double)k;
+    p0 = p1;
+    p1 = p2;
+  }
+  if (N == 1) {
+    p1 = z;
+    p0 = T(1.0);
+  }
+  pn = p1;
+  pm = p0;
+}
+}  // namespace
+
 extern "C" int sgpu_leggauss(int N, double* x, double* w) {
   if (N < 1 || !x || !w) return SGPU_ERR_ARG;
-  const ld_t pi = 3.141592653589793238462643383279502884L;
+  const double pi = 3.14159265358979323846;
   parallel_for((N + 1) / 2, [=](int i) {
     // i-th largest root
-    ld_t th = pi * (4.0L * (i + 1) - 1) / (4.0L * N + 2);
-    ld_t z = cosl(th) * (1 - (N - 1.0L) / (8.0L * N * N * N));
-    ld_t pp = 0;
+    const double th = pi * (4.0 * (i + 1) - 1) / (4.0 * N + 2);
+    double z = std::cos(th) * (1 - (N - 1.0) / (8.0 * N * N * N));
     for (int it = 0; it < 100; ++it) {
-      ld_t p0 = 1, p1 = z;
-      for (int k = 2; k <= N; ++k) {
-        ld_t p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
-        p0 = p1;
-        p1 = p2;
-      }
-      if (N == 1) {
-        p1 = z;
-        p0 = 1;
-      }
-      pp = N * (z * p1 - p0) / (z * z - 1);
-      ld_t dz = p1 / pp;
+      double pn, pm;
+      legendre_pn(N, z, pn, pm);
+      const double dz = pn / (N * (z * pn - pm) / (z * z - 1));
       z -= dz;
-      // Newton converges quadratically from Tricomi's guess: once the step
-      // is below 1e-15 the next one would be below 1e-30, beyond the long
-      // double format on every host (a fixed 1e-19 test can stall at the
-      // x86 80-bit format's resolution for up to the iteration cap)
-      if (fabsl(dz) < 1e-15L) {
-        // refresh the derivative at the converged root
-        p0 = 1;
-        p1 = z;
-        for (int k = 2; k <= N; ++k) {
-          ld_t p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
-          p0 = p1;
-          p1 = p2;
-        }
-        pp = N * (z * p1 - p0) / (z * z - 1);
-        break;
-      }
+      if (std::fabs(dz) < 1e-14) break;
     }
-    ld_t wt = 2 / ((1 - z * z) * pp * pp);
-    x[N - 1 - i] = (double)z;
-    x[i] = (double)(-z);
-    w[i] = w[N - 1 - i] = (double)wt;
+    dd zd(z), pn, pm;
+    for (int it = 0; it < 2; ++it) {
+      legendre_pn(N, zd, pn, pm);
+      const dd pp = (double)N * (zd * pn - pm) / (zd * zd - dd(1.0));
+      zd = zd - pn / pp;
+    }
+    // the derivative at the converged root
+    legendre_pn(N, zd, pn, pm);
+    const dd pp = (double)N * (zd * pn - pm) / (zd * zd - dd(1.0));
+    const dd wt = dd(2.0) / ((dd(1.0) - zd * zd) * pp * pp);
+    x[N - 1 - i] = to_double(zd);
+    x[i] = -to_double(zd);
+    w[i] = w[N - 1 - i] = to_double(wt);
   });
   if (N % 2 == 1) x[N / 2] = 0.0;
   return SGPU_OK;
@@ -109,16 +116,16 @@ extern "C" int sgpu_leggauss(int N, double* x, double* w) {
 
 namespace {
 
-// V_jk = L_k(x_j) in long double, x from the FP64 nodes
-void vandermonde(int N, const double* x, std::vector<ld_t>& V) {
-  V.assign((size_t)N * N, 0);
-  ld_t* v = V.data();
+// V_jk = L_k(x_j) in double-double, x from the FP64 nodes
+void vandermonde(int N, const double* x, std::vector<dd>& V) {
+  V.assign((size_t)N * N, dd());
+  dd* v = V.data();
   parallel_for(N, [=](int j) {
-    ld_t z = x[j], p0 = 1, p1 = z;
-    v[(size_t)j * N + 0] = 1;
+    dd z = x[j], p0 = 1.0, p1 = z;
+    v[(size_t)j * N + 0] = 1.0;
     if (N > 1) v[(size_t)j * N + 1] = z;
     for (int k = 2; k < N; ++k) {
-      ld_t p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+      dd p2 = ((double)(2 * k - 1) * z * p1 - (double)(k - 1) * p0) / (double)k;
       v[(size_t)j * N + k] = p2;
       p0 = p1;
       p1 = p2;
@@ -127,16 +134,16 @@ void vandermonde(int N, const double* x, std::vector<ld_t>& V) {
 }
 
 // stencil K[k][m] (row k, offset m = 0, 2, 4) of the Legendre bases
-void stencil(int basis, int N, std::vector<ld_t>& K2, std::vector<ld_t>& K4) {
-  K2.assign(N, 0);
-  K4.assign(N, 0);
+void stencil(int basis, int N, std::vector<dd>& K2, std::vector<dd>& K4) {
+  K2.assign(N, dd());
+  K4.assign(N, dd());
   if (basis == SGPU_BASIS_SD) {
-    for (int k = 0; k < N - 2; ++k) K2[k] = -1;  // constant: every row
+    for (int k = 0; k < N - 2; ++k) K2[k] = -1.0;  // constant: every row
   } else if (basis == SGPU_BASIS_SB) {
     // legendre/bases.py:564 {0: 1, 2: -(4n+10)/(2n+7), 4: (2n+3)/(2n+7)}, zero for k >= N-4
     for (int k = 0; k < N - 4; ++k) {
-      K2[k] = -(4.0L * k + 10) / (2.0L * k + 7);
-      K4[k] = (2.0L * k + 3) / (2.0L * k + 7);
+      K2[k] = -(dd(4.0 * k + 10) / (2.0 * k + 7));
+      K4[k] = dd(2.0 * k + 3) / (2.0 * k + 7);
     }
   }
 }
@@ -145,46 +152,46 @@ void stencil(int basis, int N, std::vector<ld_t>& K2, std::vector<ld_t>& K4) {
 // forward(f) = f . F in one contraction (scalar product and mass solve
 // together).  B_kl = sum_m K_km h_m K_lm (k, l < dim) is the mass matrix of
 // the basis (stencil K, h_m = 2 / (2m + 1); legendre/matrices.py:110-192 give
-// the same bands); F[j][k] = (B^{-1} Ms[j, :dim])_k, built in long double
+// the same bands); F[j][k] = (B^{-1} Ms[j, :dim])_k, built in double-double
 // with a banded LU (half-bandwidth 2 or 4, B is symmetric positive
 // definite).  Columns k >= dim are zero, as the forward transform leaves them.
-void forward_matrix(int N, int dim, const std::vector<ld_t>& K2, const std::vector<ld_t>& K4,
-                    const std::vector<ld_t>& MsL, std::vector<double>& F) {
+void forward_matrix(int N, int dim, const std::vector<dd>& K2, const std::vector<dd>& K4,
+                    const std::vector<dd>& MsL, std::vector<double>& F) {
   const int bw = dim == N ? 0 : (dim == N - 2 ? 2 : 4);
-  std::vector<ld_t> h(N);
-  for (int m = 0; m < N; ++m) h[m] = 2.0L / (2 * m + 1);
+  std::vector<dd> h(N);
+  for (int m = 0; m < N; ++m) h[m] = dd(2.0) / (double)(2 * m + 1);
   // row k of K: entries at k, k+2, k+4
-  auto kent = [&](int k, int m) -> ld_t {
-    if (m == k) return 1;
+  auto kent = [&](int k, int m) -> dd {
+    if (m == k) return 1.0;
     if (m == k + 2) return K2[k];
     if (m == k + 4) return K4[k];
-    return 0;
+    return 0.0;
   };
   const int W = 2 * bw + 1;
-  std::vector<ld_t> A((size_t)dim * W, 0);  // A[k][bw + (l - k)]
+  std::vector<dd> A((size_t)dim * W, dd());  // A[k][bw + (l - k)]
   for (int k = 0; k < dim; ++k)
     for (int l = k - bw; l <= k + bw; ++l) {
       if (l < 0 || l >= dim) continue;
-      ld_t v = 0;
+      dd v = 0.0;
       for (int m = (k > l ? k : l); m <= (k < l ? k : l) + 4 && m < N; ++m) v += kent(k, m) * h[m] * kent(l, m);
       A[(size_t)k * W + bw + (l - k)] = v;
     }
   // banded LU without pivoting: L unit lower (stored below), U upper
   for (int k = 0; k < dim; ++k) {
-    const ld_t piv = A[(size_t)k * W + bw];
+    const dd piv = A[(size_t)k * W + bw];
     for (int i = k + 1; i <= k + bw && i < dim; ++i) {
-      const ld_t f = A[(size_t)i * W + bw + (k - i)] / piv;
+      const dd f = A[(size_t)i * W + bw + (k - i)] / piv;
       A[(size_t)i * W + bw + (k - i)] = f;
       for (int l = k + 1; l <= k + bw && l < dim; ++l) A[(size_t)i * W + bw + (l - i)] -= f * A[(size_t)k * W + bw + (l - k)];
     }
   }
   F.assign((size_t)N * N, 0.0);
   double* Fp = F.data();
-  const ld_t* Ap = A.data();
-  const ld_t* Msp = MsL.data();
+  const dd* Ap = A.data();
+  const dd* Msp = MsL.data();
   parallel_for(N, [=](int j) {
-    std::vector<ld_t> y(dim);
-    const ld_t* A = Ap;
+    std::vector<dd> y(dim);
+    const dd* A = Ap;
     for (int k = 0; k < dim; ++k) y[k] = Msp[(size_t)j * N + k];
     for (int i = 0; i < dim; ++i)
       for (int k = i - bw; k < i; ++k)
@@ -193,7 +200,7 @@ void forward_matrix(int N, int dim, const std::vector<ld_t>& K2, const std::vect
       for (int l = i + 1; l <= i + bw && l < dim; ++l) y[i] -= A[(size_t)i * W + bw + (l - i)] * y[l];
       y[i] /= A[(size_t)i * W + bw];
     }
-    for (int k = 0; k < dim; ++k) Fp[(size_t)j * N + k] = (double)y[k];
+    for (int k = 0; k < dim; ++k) Fp[(size_t)j * N + k] = to_double(y[k]);
   });
 }
 
@@ -228,48 +235,49 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
   p->x.resize(N);
   p->w.resize(N);
   sgpu_leggauss(N, p->x.data(), p->w.data());
-  std::vector<ld_t> V, K2, K4;
+  std::vector<dd> V, K2, K4;
   vandermonde(N, p->x.data(), V);
   stencil(basis, N, K2, K4);
   const int nb = basis == SGPU_BASIS_SD ? 2 : (basis == SGPU_BASIS_SB ? 4 : 0);
   const int dim = N - nb;
   // Ms[j][k] = w_j (V_jk + K2_k V_j,k+2 + K4_k V_j,k+4)
   std::vector<double> Ms((size_t)N * N), Mb((size_t)N * N, 0.0);
-  std::vector<ld_t> MsL(form == SGPU_MIXED_DF ? (size_t)N * N : 0);
+  std::vector<dd> MsL(form == SGPU_MIXED_DF ? (size_t)N * N : 0);
   {
-    const ld_t* Vp = V.data();
-    const ld_t* K2p = K2.data();
-    const ld_t* K4p = K4.data();
+    const dd* Vp = V.data();
+    const dd* K2p = K2.data();
+    const dd* K4p = K4.data();
     const double* wp = p->w.data();
     double* Msp = Ms.data();
     double* Mbp = Mb.data();
-    ld_t* MsLp = MsL.empty() ? nullptr : MsL.data();
+    dd* MsLp = MsL.empty() ? nullptr : MsL.data();
     parallel_for(N, [=](int j) {
       for (int k = 0; k < N; ++k) {
-        ld_t v = Vp[(size_t)j * N + k];
+        dd v = Vp[(size_t)j * N + k];
         if (k + 2 < N) v += K2p[k] * Vp[(size_t)j * N + k + 2];
         if (k + 4 < N) v += K4p[k] * Vp[(size_t)j * N + k + 4];
-        Msp[(size_t)j * N + k] = (double)((ld_t)wp[j] * v);
-        if (MsLp) MsLp[(size_t)j * N + k] = (ld_t)wp[j] * v;
+        const dd wv = wp[j] * v;
+        Msp[(size_t)j * N + k] = to_double(wv);
+        if (MsLp) MsLp[(size_t)j * N + k] = wv;
         // Mb[k][j] = V_jk + K2_k V_j,k+2 + K4_k V_j,k+4 for k < dim (rows k >= dim zero)
-        if (k < dim) Mbp[(size_t)k * N + j] = (double)v;
+        if (k < dim) Mbp[(size_t)k * N + j] = to_double(v);
       }
     });
   }
   // mass matrix (legendre/matrices.py:121-135, :179-192) LU'd with TDMA/PDMA_LU
   std::vector<double> mass;
-  std::vector<ld_t> h(N);
-  for (int k = 0; k < N; ++k) h[k] = 2.0L / (2 * k + 1);
+  std::vector<dd> h(N);
+  for (int k = 0; k < N; ++k) h[k] = dd(2.0) / (double)(2 * k + 1);
   if (nb == 0) {
     mass.resize(N);
-    for (int k = 0; k < N; ++k) mass[k] = (double)(1 / h[k]);
+    for (int k = 0; k < N; ++k) mass[k] = to_double(dd(1.0) / h[k]);
   } else if (nb == 2) {
     mass.assign(3 * (size_t)dim, 0.0);
     double* ld = &mass[0];
     double* d = &mass[dim];
     double* ud = &mass[2 * dim + 2];
-    for (int k = 0; k < dim; ++k) d[k] = (double)(h[k] + h[k + 2]);
-    for (int k = 0; k < dim - 2; ++k) ld[k] = ud[k] = (double)(-h[k + 2]);
+    for (int k = 0; k < dim; ++k) d[k] = to_double(h[k] + h[k + 2]);
+    for (int k = 0; k < dim - 2; ++k) ld[k] = ud[k] = -to_double(h[k + 2]);
     tdma_lu_prog(mass.data(), dim);
     for (int k = 0; k < dim; ++k) d[k] = 1.0 / d[k];
   } else {
@@ -279,19 +287,20 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
     double* d = &mass[2 * dim];
     double* e = &mass[3 * dim + 2];
     double* f = &mass[4 * dim + 4];
+    // the integer factors below are exact in FP64 (|i| < 2^20)
     for (int i = 0; i < dim; ++i) {
-      ld_t I = i;
-      d[i] = (double)((-4 * I - 10) * (-4 * I - 10) * h[i + 2] / ((2 * I + 7) * (2 * I + 7)) +
-                      (2 * I + 3) * (2 * I + 3) * h[i + 4] / ((2 * I + 7) * (2 * I + 7)) + h[i]);
+      const double I = i;
+      d[i] = to_double(((-4 * I - 10) * (-4 * I - 10)) * h[i + 2] / ((2 * I + 7) * (2 * I + 7)) +
+                       ((2 * I + 3) * (2 * I + 3)) * h[i + 4] / ((2 * I + 7) * (2 * I + 7)) + h[i]);
     }
     for (int i = 0; i < dim - 2; ++i) {
-      ld_t I = i;
-      b[i] = e[i] = (double)((-4 * I - 18) * (2 * I + 3) * h[i + 4] / ((2 * I + 7) * (2 * I + 11)) +
-                             (-4 * I - 10) * h[i + 2] / (2 * I + 7));
+      const double I = i;
+      b[i] = e[i] = to_double(((-4 * I - 18) * (2 * I + 3)) * h[i + 4] / ((2 * I + 7) * (2 * I + 11)) +
+                              (-4 * I - 10) * h[i + 2] / (2 * I + 7));
     }
     for (int i = 0; i < dim - 4; ++i) {
-      ld_t I = i;
-      a[i] = f[i] = (double)((2 * I + 3) * h[i + 4] / (2 * I + 7));
+      const double I = i;
+      a[i] = f[i] = to_double((2 * I + 3) * h[i + 4] / (2 * I + 7));
     }
     pdma_lu_prog(mass.data(), dim);
     for (int k = 0; k < dim; ++k) d[k] = 1.0 / d[k];

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ddouble.h"
 #include "fft_line.cuh"
 
 namespace sgpu {
@@ -23,17 +24,17 @@ struct HostTables {
   std::vector<df> sten_f;
 };
 
-// long double -> double-float pair (hi = nearest float, lo = nearest float of the rest)
-inline df ld_to_df(long double x) {
-  float h = (float)x;
-  float l = (float)(x - (long double)h);
-  return df(h, l);
+// double-double -> double-float pair (hi = the float nearest to the FP64
+// rounding, lo = the float nearest to the rest)
+inline df dd_to_df(const ddm::dd& x) {
+  const float h = (float)x.hi;
+  const ddm::dd r = x - ddm::dd((double)h);
+  return df(h, (float)(r.hi + r.lo));
 }
 
 namespace planhost {
 
-typedef long double ld_t;
-const ld_t kPi = 3.141592653589793238462643383279502884L;
+using ddm::dd;
 
 bool is_prime(int n) {
   if (n < 2) return false;
@@ -154,9 +155,10 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   tw.resize(m);
   T.tw_f.resize(m);
   for (int e = 0; e < m; ++e) {
-    ld_t a = -2 * kPi * (ld_t)e / (ld_t)m;
-    tw[e] = cx<double>((double)cosl(a), (double)sinl(a));
-    T.tw_f[e] = cx<df>(ld_to_df(cosl(a)), ld_to_df(sinl(a)));
+    dd c, s;  // exp(-2 pi i e / m)
+    ddm::sincos_2pi_frac(-e, m, c, s);
+    tw[e] = cx<double>(ddm::to_double(c), ddm::to_double(s));
+    T.tw_f[e] = cx<df>(dd_to_df(c), dd_to_df(s));
   }
   if (p.rader) {
     const int g = primitive_root(n);
@@ -168,36 +170,30 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
       rout[q] = powmod(ginv, q, n);
     }
     // rk = DFT_m(b) / m with b_q = exp(-2 pi i ginv^q / n)
-    std::vector<ld_t> br(m), bi(m);
-    for (int q = 0; q < m; ++q) {
-      ld_t a = -2 * kPi * (ld_t)rout[q] / (ld_t)n;
-      br[q] = cosl(a);
-      bi[q] = sinl(a);
-    }
-    // m-th roots of unity once (long double), indexed by q s mod m
-    std::vector<ld_t> wr(m), wi(m);
-    for (int e = 0; e < m; ++e) {
-      const ld_t a = -2 * kPi * (ld_t)e / (ld_t)m;
-      wr[e] = cosl(a);
-      wi[e] = sinl(a);
-    }
+    std::vector<dd> br(m), bi(m);
+    for (int q = 0; q < m; ++q) ddm::sincos_2pi_frac(-(int64_t)rout[q], n, br[q], bi[q]);
+    // m-th roots of unity once (double-double), indexed by q s mod m
+    std::vector<dd> wr(m), wi(m);
+    for (int e = 0; e < m; ++e) ddm::sincos_2pi_frac(-e, m, wr[e], wi[e]);
     rk.resize(m);
     T.rk_f.resize(m);
-    // O(m^2) in long double (software quad precision on some hosts): the
-    // outputs s are independent, spread over the host's cores
+    // O(m^2) in double-double: the outputs s are independent, spread over
+    // the host's cores
     auto rk_range = [&](int s0, int s1) {
       for (int s = s0; s < s1; ++s) {
-        ld_t sr = 0, si = 0;
+        dd sr, si;
         int e = 0;  // q * s mod m
         for (int q = 0; q < m; ++q) {
-          const ld_t c = wr[e], sn = wi[e];
+          const dd& c = wr[e];
+          const dd& sn = wi[e];
           sr += br[q] * c - bi[q] * sn;
           si += br[q] * sn + bi[q] * c;
           e += s;
           if (e >= m) e -= m;
         }
-        rk[s] = cx<double>((double)(sr / m), (double)(si / m));
-        T.rk_f[s] = cx<df>(ld_to_df(sr / m), ld_to_df(si / m));
+        const dd rr = sr / (double)m, ri = si / (double)m;
+        rk[s] = cx<double>(ddm::to_double(rr), ddm::to_double(ri));
+        T.rk_f[s] = cx<df>(dd_to_df(rr), dd_to_df(ri));
       }
     };
     const unsigned hw = std::thread::hardware_concurrency();
@@ -210,9 +206,10 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   if (cheb) {
     post.resize(n);
     for (int k = 0; k < n; ++k) {
-      ld_t a = -kPi * (ld_t)k / (ld_t)(2 * n);
-      post[k] = cx<double>((double)cosl(a), (double)sinl(a));
-      T.post_f.push_back(cx<df>(ld_to_df(cosl(a)), ld_to_df(sinl(a))));
+      dd c, s;  // exp(-i pi k / (2 n)) = exp(-2 pi i k / (4 n))
+      ddm::sincos_2pi_frac(-k, 4 * (int64_t)n, c, s);
+      post[k] = cx<double>(ddm::to_double(c), ddm::to_double(s));
+      T.post_f.push_back(cx<df>(dd_to_df(c), dd_to_df(s)));
     }
   }
   if (p.basis == SGPU_BASIS_SB) {
@@ -222,8 +219,8 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
     for (int k = 0; k < n - 4; ++k) {
       sten[k] = -(2.0 * k + 4) / (k + 3.0);
       sten[n + k] = (k + 1.0) / (k + 3.0);
-      T.sten_f[k] = ld_to_df(-(2.0L * k + 4) / (k + 3.0L));
-      T.sten_f[n + k] = ld_to_df((k + 1.0L) / (k + 3.0L));
+      T.sten_f[k] = dd_to_df(-(dd(2.0 * k + 4) / (k + 3.0)));
+      T.sten_f[n + k] = dd_to_df(dd(k + 1.0) / (k + 3.0));
     }
   }
   if (p.basis == SGPU_BASIS_SN) {
@@ -232,9 +229,9 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
     T.sten_f.assign(2 * (size_t)n, df());
     for (int k = 0; k < n - 2; ++k) {
       const double r = k / (k + 2.0);
-      const ld_t rl = (ld_t)k / (k + 2.0L);
+      const dd rl = dd((double)k) / (k + 2.0);
       sten[k] = -(r * r);
-      T.sten_f[k] = ld_to_df(-(rl * rl));
+      T.sten_f[k] = dd_to_df(-(rl * rl));
     }
   }
   if (kind == SGPU_XF_CHEB_FORWARD) {

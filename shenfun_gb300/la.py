@@ -522,8 +522,11 @@ class BandSepSolver:
 class Biharmonic(BandSepSolver):
     """Chebyshev ShenBiharmonic solver for a0 S + alfa A + beta B
     (chebyshev/la.py:354-558): the same structured per-wavenumber LU, valid for
-    even and odd N (the reference's tailored kernel assumes equal even/odd
-    lengths, la.pyx:1356-1362; its odd-N path is a sparse LU per wavenumber)."""
+    even and odd N.  The reference's 2D/3D kernels assume equal even/odd
+    lengths: with N - 4 odd its LU factors len(sii) // 2 rows per parity
+    (la.pyx:1651, 1950) and its solve divides by the unfactored last even row
+    (la.pyx:1356-1362), so its output is non-finite there (checked against
+    the unmodified reference at N = 21 and 33)."""
 
 
 def _tp(key, scale, T, ax):

@@ -46,6 +46,17 @@ class HelmholtzProblem:
         _lib.call("sgpu_helmholtz_workspace_size", self._h, ctypes.byref(nb))
         self.workspace_bytes = int(nb.value)
         self._work = None
+        self._fac = None
+
+    @property
+    def factor_ptr(self):
+        """Device address of the problem's factor block (what a batched
+        step's pointer table holds for this member)."""
+        if self._fac is None:
+            q = ctypes.c_void_p()
+            _lib.call("sgpu_helmholtz_factor_ptr", self._h, ctypes.byref(q))
+            self._fac = q.value
+        return self._fac
 
     def __del__(self):
         try:
@@ -115,9 +126,7 @@ class BatchRunner:
         self.capture_after = int(capture_after)
         self.runs = 0
         if self.use_graph and self.capture_after == 0:
-            p = ctypes.c_void_p()
-            _lib.call("sgpu_helmholtz_factor_ptr", proto._h, ctypes.byref(p))
-            self._set_table([p.value] * self.K)  # valid pointers for the warm-up launch
+            self._set_table([proto.factor_ptr] * self.K)  # valid pointers for the warm-up launch
             with torch.cuda.stream(stream):
                 self._launch()  # warm-up outside the capture (plan attributes, lazy state)
             self._capture()
@@ -149,11 +158,7 @@ class BatchRunner:
         """Queue the batch of `problems` (at most K, all of the class) whose
         right-hand sides are already in self.f[:len(problems)]; the solutions
         land in self.u.  Unused slots repeat the last member."""
-        ptrs = []
-        for p in problems:
-            q = ctypes.c_void_p()
-            _lib.call("sgpu_helmholtz_factor_ptr", p._h, ctypes.byref(q))
-            ptrs.append(q.value)
+        ptrs = [p.factor_ptr for p in problems]
         ptrs += [ptrs[-1]] * (self.K - len(ptrs))
         self._set_table(ptrs)
         if self.graph is None and self.use_graph and self.runs >= self.capture_after:

@@ -192,6 +192,7 @@ class GpuExecutor:
         self.Problem = HelmholtzProblem
         self.streams = [torch.cuda.Stream() for _ in range(nstreams)]
         self.cache = collections.OrderedDict()
+        self._cbytes = 0  # bytes of the cached problems, kept with every insertion and eviction
         self.cache_budget = int(cache_budget)
         self.form = form
         self.inflight = {}
@@ -211,7 +212,18 @@ class GpuExecutor:
 
     # -- factorisation cache ---------------------------------------------
     def cache_bytes(self):
-        return sum(ent[1] for ent in self.cache.values())
+        return self._cbytes
+
+    def _cache_put(self, key, p, nbytes, ready):
+        old = self.cache.get(key)
+        if old is not None:
+            self._cbytes -= old[1]
+        self.cache[key] = (p, nbytes, ready)
+        self._cbytes += nbytes
+
+    def _cache_evict_oldest(self):
+        _, ent = self.cache.popitem(last=False)
+        self._cbytes -= ent[1]
 
     def factor_cost(self, req):
         return 0 if req.key in self.cache else factor_bytes(req.N, req.family)
@@ -222,7 +234,7 @@ class GpuExecutor:
             if any(r.key == key for r, _, _ in self.inflight.values()) or \
                     any(r.key == key for r in self.waiting.values()):
                 break  # still in use
-            self.cache.popitem(last=False)
+            self._cache_evict_oldest()
 
     def problem(self, req, stream):
         """Cached problem for `req`, ready for use on `stream`.  A miss is
@@ -240,7 +252,7 @@ class GpuExecutor:
         p = self.Problem(req.N, req.family, req.c, self.form, stream=stream)
         ev = self.torch.cuda.Event()
         ev.record(stream)
-        self.cache[req.key] = (p, factor_bytes(req.N, req.family), (ev, stream))
+        self._cache_put(req.key, p, factor_bytes(req.N, req.family), (ev, stream))
         self.shrink_cache(self.cache_budget)
         return p
 
@@ -255,9 +267,12 @@ class GpuExecutor:
     def _cached(self, req, stream):
         """The cached problem of `req` for use on `stream` (a hit)."""
         self.cache.move_to_end(req.key)
-        p, _, ready = self.cache[req.key]
+        p, nb, ready = self.cache[req.key]
         if ready is not None and ready[1] is not stream:
-            stream.wait_event(ready[0])
+            if ready[0].query():
+                self.cache[req.key] = (p, nb, None)  # factorised: no later request needs to wait
+            else:
+                stream.wait_event(ready[0])
         return p
 
     def _collect(self):
@@ -271,7 +286,7 @@ class GpuExecutor:
             if err is None:
                 ev = self.torch.cuda.Event()
                 ev.record(cs)  # after the build's factorisation on its stream
-                self.cache[key] = (fut.result(), factor_bytes(key[0], key[1]), (ev, cs))
+                self._cache_put(key, fut.result(), factor_bytes(key[0], key[1]), (ev, cs))
                 self.shrink_cache(self.cache_budget)
             for rid, r in list(self.waiting.items()):
                 if r.key != key:
@@ -354,7 +369,8 @@ class BatchExecutor(GpuExecutor):
         self.tune = tune
         self.tuned = {}  # class -> variants the autotuner picked for its plans
         self.ready = collections.OrderedDict()  # class -> deque of requests whose problem is cached
-        self.runners = collections.OrderedDict()  # (class, K) -> BatchRunner
+        self.runners = collections.OrderedDict()  # (class, K, stream index) -> BatchRunner
+        self._rbytes = 0  # bytes of the runners' staging buffers
         self.busy = {}  # stream index -> batch id in flight
         self.batches = 0
         self.batch_sizes = collections.Counter()
@@ -365,7 +381,7 @@ class BatchExecutor(GpuExecutor):
         return (req.N, req.family)
 
     def cache_bytes(self):
-        return GpuExecutor.cache_bytes(self) + sum(r.bytes for r in self.runners.values())
+        return self._cbytes + self._rbytes
 
     def _kmax(self, req):
         per = 3 * request_bytes(req.N)
@@ -387,7 +403,7 @@ class BatchExecutor(GpuExecutor):
                 p = self.Problem(req.N, req.family, req.c, self.form, stream=s)
                 ev = self.torch.cuda.Event()
                 ev.record(s)
-                self.cache[req.key] = (p, factor_bytes(req.N, req.family), (ev, s))
+                self._cache_put(req.key, p, factor_bytes(req.N, req.family), (ev, s))
                 self.ready.setdefault(self._class(req), collections.deque()).append(req)
                 self._flush()
                 return
@@ -403,7 +419,7 @@ class BatchExecutor(GpuExecutor):
             if err is None:
                 ev = self.torch.cuda.Event()
                 ev.record(cs)
-                self.cache[key] = (fut.result(), factor_bytes(key[0], key[1]), (ev, cs))
+                self._cache_put(key, fut.result(), factor_bytes(key[0], key[1]), (ev, cs))
                 self.shrink_cache(self.cache_budget)
             for rid, r in list(self.waiting.items()):
                 if r.key != key:
@@ -432,6 +448,7 @@ class BatchExecutor(GpuExecutor):
         r = BatchRunner(proto, K, self.streams[si], graph=self.graphs, capture_after=1)
         r.bytes = r.f.numel() * 16 + r.work.numel()
         self.runners[key] = r
+        self._rbytes += r.bytes
         return r
 
     def _flush(self):
@@ -489,6 +506,8 @@ class BatchExecutor(GpuExecutor):
 
     def shrink_cache(self, room):
         limit = max(0, min(room, self.cache_budget))
+        if self.cache_bytes() <= limit:
+            return
         busy_keys = {r.key for reqs, _, _ in self.inflight.values() for r in reqs}
         busy_keys |= {r.key for q in self.ready.values() for r in q}
         busy_keys |= {r.key for r in self.waiting.values()}
@@ -498,11 +517,12 @@ class BatchExecutor(GpuExecutor):
             if id(r) in busy_runners:
                 break
             self.runners.popitem(last=False)
+            self._rbytes -= r.bytes
         while self.cache and self.cache_bytes() > limit:
             key, _ = next(iter(self.cache.items()))
             if key in busy_keys:
                 break  # still in use
-            self.cache.popitem(last=False)
+            self._cache_evict_oldest()
 
     def poll(self):
         self._collect()

@@ -17,6 +17,8 @@
 //   emu ozaki  N nlines inner cplx precise in.bin M.bin out.bin (split-BF16 contraction)
 //   emu ozakic N nlines inner cplx precise kchunk in.bin M.bin out.bin  (K blocks per launch)
 //   emu lcf    N nlines cplx bn in.bin M.bin out.bin   (fused contraction, 64- or 32-line tiles)
+//   emu tables kind n basis out.bin   (plan tables: tw, rk, post as FP64 pairs, then the
+//                                      double-float tw_f, rk_f, post_f as (hi, lo) per part)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -490,6 +492,27 @@ int main(int argc, char** argv) {
   if (mode == "nlu" || mode == "nsolve" || mode == "ncached") {
     nm = 1;
     mode = "h" + mode.substr(1);
+  }
+  if (mode == "tables") {
+    if (argc < 6) return 2;
+    LinePlan p;
+    HostTables T;
+    if (build_plan_host(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), SGPU_MIXED_DF, p, T) != SGPU_OK) return 3;
+    std::vector<double> o;
+    for (auto* v : {&T.tw, &T.rk, &T.post})
+      for (const cd& c : *v) {
+        o.push_back(c.re);
+        o.push_back(c.im);
+      }
+    for (auto* v : {&T.tw_f, &T.rk_f, &T.post_f})
+      for (const Cx<df>& c : *v) {
+        o.push_back(c.re.hi);
+        o.push_back(c.re.lo);
+        o.push_back(c.im.hi);
+        o.push_back(c.im.lo);
+      }
+    write_exact(argv[5], o.data(), o.size());
+    return 0;
   }
   if (mode == "xform") return xform(argc, argv);
   if (mode == "f256") return f256_mode(argc, argv);

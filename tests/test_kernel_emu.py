@@ -696,3 +696,56 @@ def test_pair_blocks_stack_equals_alone(emu, kind, n, basis, inner, monkeypatch)
     for k in range(K):
         alone = runner(x[k * outer:(k + 1) * outer], outer)
         assert np.array_equal(stacked[k * per:(k + 1) * per], alone), k
+
+
+# ---------------------------------------------------------------------------
+# plan tables built in double-double: every FP64 twiddle is the correctly
+# rounded value of its exact expression (mpmath at 60 digits), and every
+# double-float pair carries the value to ~2^-48
+@pytest.mark.parametrize("kind,n,basis", [(C2C_FWD, 256, 0), (C2C_FWD, 257, 0), (R2C, 96, 0),
+                                          (CHEB_SCALAR, 65, 1), (C2C_FWD, 31, 0)])
+def test_plan_tables_correctly_rounded(emu, kind, n, basis):
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 60
+    rader = n >= 11 and all(n % d for d in range(2, int(n ** 0.5) + 1))
+    m = n - 1 if rader else n
+    cheb = kind >= DCT2
+    nrk = m if rader else 0
+    npost = n if cheb else 0
+    cnt = 2 * (m + nrk + npost) + 4 * (m + nrk + npost)
+    with tempfile.TemporaryDirectory() as td:
+        outp = os.path.join(td, "t.bin")
+        env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0:abort_on_error=1")
+        r = subprocess.run([emu, "tables", str(kind), str(n), str(basis), outp], capture_output=True,
+                           text=True, env=env)
+        assert r.returncode == 0, r.stderr[-2000:]
+        o = np.fromfile(outp, dtype=np.float64)
+    assert o.size == cnt
+    exact = []
+    for e in range(m):  # exp(-2 pi i e / m)
+        a = -2 * mpmath.pi * e / m
+        exact.append((mpmath.cos(a), mpmath.sin(a)))
+    if rader:
+        g = next(g for g in range(2, n) if all(pow(g, (n - 1) // q, n) != 1 for q in range(2, n)
+                                                if (n - 1) % q == 0 and all(q % d for d in range(2, q))))
+        ginv = pow(g, n - 2, n)
+        b = [mpmath.exp(-2j * mpmath.pi * pow(ginv, q, n) / n) for q in range(m)]
+        for s in range(m):
+            v = mpmath.fsum(b[q] * mpmath.exp(-2j * mpmath.pi * q * s / m) for q in range(m)) / m
+            exact.append((mpmath.re(v), mpmath.im(v)))
+    if cheb:
+        for k in range(n):
+            a = -mpmath.pi * k / (2 * n)
+            exact.append((mpmath.cos(a), mpmath.sin(a)))
+    fp = o[:2 * len(exact)].reshape(-1, 2)
+    pairs = o[2 * len(exact):].reshape(-1, 4)
+    for i, (cr, ci) in enumerate(exact):
+        for j, ex in enumerate((cr, ci)):
+            got = fp[i, j]
+            rounded = float(ex)  # mpmath rounds to nearest
+            # (an exact zero of the Rader spectrum comes out of a 256-term
+            # double-double sum as ~1e-33: absolute slack 1e-30)
+            assert got == rounded or abs(mpmath.mpf(got) - ex) <= abs(mpmath.mpf(rounded) - ex) * (1 + 1e-9) + 1e-30, \
+                (i, j, got, rounded)
+            hi, lo = pairs[i, 2 * j], pairs[i, 2 * j + 1]
+            assert abs(mpmath.mpf(hi) + mpmath.mpf(lo) - ex) <= 2.0 ** -47 * max(abs(ex), 2.0 ** -20)
