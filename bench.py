@@ -776,6 +776,8 @@ CASES = {
     # one transform of the channel grid, for profiler captures:  name -> (kind, form)
     "r2c-plain": ("r2c", "plain"), "r2c-mixed": ("r2c", "mixed"),
     "c2r-mixed": ("c2r", "mixed"), "c2c-plain": ("c2c", "plain"), "c2c-mixed": ("c2c", "mixed"),
+    # the mixed form's length-256 passes in 64-bit fixed point (plan variant 5)
+    "c2c-fixed": ("c2c", "fixed"), "r2c-fixed": ("r2c", "fixed"), "c2r-fixed": ("c2r", "fixed"),
     "bih-plain": ("bih", "plain"), "pad-mixed": ("pad", "mixed"), "bc-mixed": ("bc", "mixed"),
     "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
     "solve-plain": ("solve", "plain"),
@@ -796,8 +798,24 @@ def run_case(name, reps=3):
     from shenfun_gb300 import _lib
     from shenfun_gb300.spaces import R2C, ChebyshevShenDirichlet
     kind, form = CASES[name]
+    fixed = form == "fixed"
+    if fixed:
+        form = "mixed"
     x = torch.randn(NX, NY, NZ, dtype=torch.float64, device="cuda")
-    if kind == "r2c":
+    if kind in ("r2c", "c2r", "c2c") and fixed:
+        from shenfun_gb300.plans import LinePlan
+        xk = {"r2c": _lib.XF_R2C, "c2r": _lib.XF_C2R, "c2c": _lib.XF_C2C_FWD}[kind]
+        P = LinePlan(xk, 256, form=_lib.MIXED_DF)
+        P.variant = 5
+        c = torch.randn(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
+        y = torch.empty_like(c)
+        if kind == "r2c":
+            fn = lambda: P(x, y, 1, 1.0 / NY)  # noqa: E731
+        elif kind == "c2r":
+            fn = lambda: P(c, x, 1, 1.0)  # noqa: E731
+        else:
+            fn = lambda: P(c, y, 0, 1.0 / NX)  # noqa: E731
+    elif kind == "r2c":
         V = R2C(NY)
         V.form = _lib.FORMS[form]
         y = torch.empty(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")

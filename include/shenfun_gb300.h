@@ -144,9 +144,14 @@ int sgpu_plan_execute_blocks(const sgpu_plan* plan, const void* in, void* out, i
  * overlap this tile's epilogue).  Length-256 Fourier plans (R2C, C2R, C2C):
  * 1 = the strided-pass kernel for axes with inner >= 16 (pass 1 and pass 2
  * of a 16 x 16 register FFT reading and writing global memory directly, one
- * shared-memory transpose) at its default occupancy (3 CTAs per SM in the
- * mixed form, 2 in FP64), 2 = the generic line programs, 3 / 4 = the
- * strided-pass kernel at 2 / 3 CTAs per SM.  0 = the library's default (1).  SGPU_ERR_UNSUPPORTED for other plans; get returns
+ * shared-memory transpose) in its default arithmetic and occupancy (FP64 at
+ * 2 CTAs per SM; the mixed form in 64-bit fixed point, C2C at 2 CTAs per SM
+ * and R2C / C2R at 3), 2 = the generic line programs, 3 / 4 = the
+ * strided-pass kernel at 2 / 3 CTAs per SM in FP64 (plain form) or
+ * double-float (mixed form), 5 / 6 = the mixed form in 64-bit fixed point
+ * at 2 / 3 CTAs per SM (SGPU_ERR_UNSUPPORTED for the plain form; complex
+ * arrays that are not 16-byte aligned run the generic programs).  0 = the
+ * library's default (1).  SGPU_ERR_UNSUPPORTED for other plans; get returns
  * 0 for them.  No counterpart in the reference (a tuning knob of this
  * library's kernels). */
 int sgpu_plan_set_variant(sgpu_plan* plan, int variant);

@@ -3,7 +3,8 @@
 Several plans have more than one kernel for the same result
 (``sgpu_plan_set_variant``): the fused Chebyshev contraction runs 64- or
 32-line tiles, the length-256 Fourier passes run the strided register-FFT
-kernel at two or three CTAs per SM or the generic line programs.  Which is
+kernel at two or three CTAs per SM (the mixed form in double-float or in
+64-bit fixed point) or the generic line programs.  Which is
 fastest depends on the layout and the size.  ``tune_plan`` times every
 variant of a plan on the call's own layout (CUDA events, the median of a few
 repetitions after warm-up), checks that the candidates agree with the
@@ -78,7 +79,7 @@ def _save():
 def candidates(kind, n, form, inner):
     """Variants that exist for this plan and layout (the default first)."""
     if kind in FOURIER and n == 256 and inner >= 16:
-        return [1, 2, 3, 4]
+        return [1, 2, 3, 4, 5, 6] if form == _lib.MIXED_DF else [1, 2, 3, 4]
     if form == _lib.MIXED_DF and kind in CHEB_TENSOR and inner == 1 and 16 <= n <= 341:
         return [1, 2]
     return []

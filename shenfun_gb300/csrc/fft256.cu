@@ -4,6 +4,7 @@
 #include <type_traits>
 
 #include "fft256.cuh"
+#include "fft256_fx.cuh"
 
 namespace sgpu {
 namespace f256 {
@@ -31,11 +32,41 @@ __global__ void __launch_bounds__(NT, MINB) k_fft256(LinePlan p, Args a) {
   }
 }
 
+// the mixed form in 64-bit fixed point (fft256_fx.cuh)
+template <int KIND, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_fft256_fx(LinePlan p, Args a, FxScale s) {
+  extern __shared__ __align__(16) unsigned char f256_smem[];
+  const FxShared sh = fx_shared(f256_smem);
+  const int t = (int)threadIdx.x;
+  const int64_t blk = (int64_t)blockIdx.x;
+  Cq v[16];
+  if (KIND == C2C_FWD || KIND == C2C_BWD) {
+    fx_c2c_pass1<KIND>(p, a, blk, sh, t);
+    __syncthreads();
+    const int E = fx_c2c_pass2(sh, t, v);
+    fx_c2c_store<KIND>(a, t, v, E, sh, s);
+    return;
+  }
+  fx_load<KIND>(a, blk, t, sh);
+  __syncthreads();
+  fx_pass1<KIND>(p, a, sh, t);
+  __syncthreads();
+  fx_pass2_dft(sh.Z, t, v);
+  if (KIND == R2C) {
+    __syncthreads();
+    fx_r2c_stash(sh.Z, t, v);
+    __syncthreads();
+    fx_r2c_post(a, sh, t, NT, s);
+  } else {
+    fx_c2r_store(a, t, v, sh, s);
+  }
+}
+
 // per device: the large dynamic shared memory of every instantiation, set
-// once ([arithmetic][kind][occupancy])
+// once ([arithmetic: FP64, double-float, fixed point][kind][occupancy])
 struct DevAttr {
-  std::once_flag once[2][4][2];
-  int rc[2][4][2] = {};
+  std::once_flag once[3][4][2];
+  int rc[3][4][2] = {};
 };
 const int MAX_DEV = 64;
 DevAttr g_dev[MAX_DEV];
@@ -58,6 +89,35 @@ int launch_kind(const LinePlan& p, const Args& a, unsigned nblocks, cudaStream_t
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
+template <int KIND, int MINB>
+int launch_fx(const LinePlan& p, const Args& a, const FxScale& sc, unsigned nblocks, cudaStream_t s) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) return SGPU_ERR_CUDA;
+  DevAttr& d = g_dev[dev];
+  const int mi = MINB == 3 ? 1 : 0;
+  std::call_once(d.once[2][KIND][mi], [&]() {
+    d.rc[2][KIND][mi] = cudaFuncSetAttribute(k_fft256_fx<KIND, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fx_smem_bytes()) == cudaSuccess
+                            ? 1
+                            : -1;
+    cudaGetLastError();
+  });
+  if (d.rc[2][KIND][mi] != 1) return SGPU_ERR_CUDA;
+  k_fft256_fx<KIND, MINB><<<nblocks, NT, fx_smem_bytes(), s>>>(p, a, sc);
+  return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
+}
+
+template <int MINB>
+int launch_fx_kind(int kind, const LinePlan& p, const Args& a, const FxScale& sc, unsigned nb, cudaStream_t s) {
+  switch (kind) {
+    case C2C_FWD: return launch_fx<C2C_FWD, MINB>(p, a, sc, nb, s);
+    case C2C_BWD: return launch_fx<C2C_BWD, MINB>(p, a, sc, nb, s);
+    case R2C: return launch_fx<R2C, MINB>(p, a, sc, nb, s);
+    case C2R: return launch_fx<C2R, MINB>(p, a, sc, nb, s);
+  }
+  return SGPU_ERR_ARG;
+}
+
 template <class R, int MINB>
 int launch_r(int kind, const LinePlan& p, const Args& a, unsigned nb, cudaStream_t s) {
   switch (kind) {
@@ -73,9 +133,11 @@ int launch_r(int kind, const LinePlan& p, const Args& a, unsigned nb, cudaStream
 
 // The plan's length-256 Fourier pass along a strided axis, or
 // SGPU_ERR_UNSUPPORTED when the plan or layout does not qualify; ctas_per_sm
-// 2 or 3 picks the register budget (above).
+// 2 or 3 picks the register budget (above); fixed: the mixed form in 64-bit
+// fixed point instead of double-float (SGPU_ERR_UNSUPPORTED for the plain
+// form, whose arithmetic is FP64).
 int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines, int64_t inner, double scl,
-                int ctas_per_sm, cudaStream_t s) {
+                int ctas_per_sm, int fixed, cudaStream_t s) {
   using namespace f256;
   if (p.n != N || p.m != N || p.rader || inner < 16) return SGPU_ERR_UNSUPPORTED;
   int kind;
@@ -91,6 +153,16 @@ int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines
   if (nt == 0) return SGPU_OK;
   if (nt > 0x7fffffffLL) return SGPU_ERR_ARG;
   Args a{in, out, nlines, inner, scl, p.pb};
+  if (fixed) {
+    if (p.form != SGPU_MIXED_DF || !p.tw_q) return SGPU_ERR_UNSUPPORTED;
+    // complex entries move as 16-byte loads and stores: complex arrays must
+    // be 16-byte aligned (else the caller runs the generic programs)
+    const bool cin = kind != R2C, cout = kind != C2R;
+    if ((cin && ((uintptr_t)in & 15)) || (cout && ((uintptr_t)out & 15))) return SGPU_ERR_UNSUPPORTED;
+    const FxScale sc = fx_scale(scl);
+    return ctas_per_sm == 3 ? launch_fx_kind<3>(kind, p, a, sc, (unsigned)nt, s)
+                            : launch_fx_kind<2>(kind, p, a, sc, (unsigned)nt, s);
+  }
   if (ctas_per_sm == 3)
     return p.form == SGPU_MIXED_DF ? launch_r<df, 3>(kind, p, a, (unsigned)nt, s)
                                    : launch_r<double, 3>(kind, p, a, (unsigned)nt, s);

@@ -49,6 +49,10 @@ struct LinePlan {
   const Cx<df>* rk_f;
   const Cx<df>* post_f;
   const df* sten_f;
+  // m = 256: exp(-2 pi i e / 256) in Q0.62, each part split as h 2^31 + l
+  // (tw_q[4 e .. 4 e + 3] = re h, re l, im h, im l; +1 saturates, the
+  // fixed-point passes never use it)
+  const int* tw_q;
   int form;          // SGPU_PLAIN_F64 or SGPU_MIXED_DF
   int64_t pb;        // real data: lines pair up (one complex FFT per pair)
                      // only within blocks of pb lines (0: one block of all

@@ -22,7 +22,26 @@ struct HostTables {
   std::vector<double> mass, sten;
   std::vector<Cx<df>> tw_f, rk_f, post_f;
   std::vector<df> sten_f;
+  std::vector<int> tw_q;
 };
+
+// round(x 2^62) of a double-double |x| <= 1, split as h 2^31 + l with
+// l in [0, 2^31) (+1, whose h does not fit, saturates)
+inline void dd_to_q62(const ddm::dd& x, int* out) {
+  const double two62 = 4611686018427387904.0;
+  const double hv = x.hi * two62;  // exact: a power-of-two scaling
+  long long q;
+  if (hv >= two62) {
+    q = (1LL << 62) - 1;
+  } else {
+    // hv is an integer when |x.hi| >= 2^-9 (53-bit significand scaled by
+    // 2^62); the fraction and the low part add their rounded value
+    const double hf = std::floor(hv);
+    q = (long long)hf + (long long)std::llround((hv - hf) + x.lo * two62);
+  }
+  out[0] = (int)(q >> 31);
+  out[1] = (int)(q & 0x7FFFFFFFLL);
+}
 
 // double-double -> double-float pair (hi = the float nearest to the FP64
 // rounding, lo = the float nearest to the rest)
@@ -154,11 +173,16 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
   std::vector<double>& sten = T.sten;
   tw.resize(m);
   T.tw_f.resize(m);
+  if (m == 256) T.tw_q.resize(4 * (size_t)m);
   for (int e = 0; e < m; ++e) {
     dd c, s;  // exp(-2 pi i e / m)
     ddm::sincos_2pi_frac(-e, m, c, s);
     tw[e] = cx<double>(ddm::to_double(c), ddm::to_double(s));
     T.tw_f[e] = cx<df>(dd_to_df(c), dd_to_df(s));
+    if (m == 256) {
+      dd_to_q62(c, &T.tw_q[4 * (size_t)e]);
+      dd_to_q62(s, &T.tw_q[4 * (size_t)e + 2]);
+    }
   }
   if (p.rader) {
     const int g = primitive_root(n);
@@ -311,7 +335,7 @@ inline int build_plan_host(int kind, int n, int basis, int form, LinePlan& p, Ho
 
 // Point a plan's table pointers into one contiguous table image at `base`
 // (device or host); `off` receives the byte layout.  Returns total bytes.
-#define SGPU_NTAB 11
+#define SGPU_NTAB 12
 inline size_t table_layout(const HostTables& T, size_t off[SGPU_NTAB]) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t sizes[SGPU_NTAB] = {
@@ -320,7 +344,7 @@ inline size_t table_layout(const HostTables& T, size_t off[SGPU_NTAB]) {
       sizeof(cd) * T.post.size(),     sizeof(double) * T.mass.size(),
       sizeof(double) * T.sten.size(), sizeof(Cx<df>) * T.tw_f.size(),
       sizeof(Cx<df>) * T.rk_f.size(), sizeof(Cx<df>) * T.post_f.size(),
-      sizeof(df) * T.sten_f.size()};
+      sizeof(df) * T.sten_f.size(),   sizeof(int) * T.tw_q.size()};
   size_t sz = 0;
   for (int i = 0; i < SGPU_NTAB; ++i) {
     off[i] = sz;
@@ -344,6 +368,7 @@ inline void table_image(const HostTables& T, const size_t off[SGPU_NTAB], unsign
   cp(8, T.rk_f.data(), sizeof(Cx<df>) * T.rk_f.size());
   cp(9, T.post_f.data(), sizeof(Cx<df>) * T.post_f.size());
   cp(10, T.sten_f.data(), sizeof(df) * T.sten_f.size());
+  cp(11, T.tw_q.data(), sizeof(int) * T.tw_q.size());
 }
 
 inline void bind_tables(LinePlan& p, const HostTables& T, const size_t off[SGPU_NTAB],
@@ -359,6 +384,7 @@ inline void bind_tables(LinePlan& p, const HostTables& T, const size_t off[SGPU_
   p.rk_f = T.rk_f.empty() ? nullptr : (const Cx<df>*)(b + off[8]);
   p.post_f = T.post_f.empty() ? nullptr : (const Cx<df>*)(b + off[9]);
   p.sten_f = T.sten_f.empty() ? nullptr : (const df*)(b + off[10]);
+  p.tw_q = T.tw_q.empty() ? nullptr : (const int*)(b + off[11]);
 }
 
 }  // namespace sgpu

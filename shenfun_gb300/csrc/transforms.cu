@@ -27,14 +27,14 @@ struct sgpu_plan {
   oz::Matrix tc;     // tensor form: the line operator, split (any line layout)
   bool fused = false;
   lc::Matrix fm;     // the same operator for the fused contraction (contiguous lines)
-  int fvariant = 1;  // length-256 Fourier plans: 1 strided-pass kernel at its default occupancy
+  int fvariant = 1;  // length-256 Fourier plans: 1 strided-pass kernel, its default arithmetic and occupancy
                      // (3 CTAs per SM for double-float, 2 for FP64: measured best on the channel
                      // grid), 2 generic line programs, 3 / 4 strided-pass kernel at 2 / 3 CTAs per SM
 };
 
 namespace sgpu {
 int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines, int64_t inner, double scl,
-                int ctas_per_sm, cudaStream_t s);
+                int ctas_per_sm, int fixed, cudaStream_t s);
 }
 
 namespace {
@@ -201,13 +201,14 @@ bool fourier256(const sgpu_plan* plan) {
 }  // namespace
 
 extern "C" int sgpu_plan_set_variant(sgpu_plan* plan, int variant) {
-  if (!plan || variant < 0 || variant > 4) return SGPU_ERR_ARG;
+  if (!plan || variant < 0 || variant > 6) return SGPU_ERR_ARG;
   if (plan->fused) {
     if (variant > 2) return SGPU_ERR_ARG;
     plan->fm.variant = variant == 0 ? 1 : variant;
     return SGPU_OK;
   }
   if (fourier256(plan)) {
+    if (variant >= 5 && plan->lp.form != SGPU_MIXED_DF) return SGPU_ERR_UNSUPPORTED;
     plan->fvariant = variant == 0 ? 1 : variant;
     return SGPU_OK;
   }
@@ -245,8 +246,14 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
   const int64_t nlines = outer * inner;
   if (nlines == 0) return SGPU_OK;
   if (plan->fvariant != 2 && fourier256(plan) && inner >= 16) {
-    const int ctas = plan->fvariant == 3 ? 2 : plan->fvariant == 4 ? 3 : (p.form == SGPU_MIXED_DF ? 3 : 2);
-    const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, ctas, stream);
+    // variant 1: plain FP64 at 2 CTAs per SM; the mixed form in fixed point,
+    // C2C at 2 CTAs per SM (its 3-CTA register budget spills), R2C / C2R at 3
+    const int fv = plan->fvariant;
+    const bool mixed = p.form == SGPU_MIXED_DF;
+    const bool c2c = p.kind == SGPU_XF_C2C_FWD || p.kind == SGPU_XF_C2C_BWD;
+    const int ctas = (fv == 3 || fv == 5) ? 2 : (fv == 4 || fv == 6) ? 3 : (mixed && !c2c ? 3 : 2);
+    const int fixed = (fv >= 5 || (fv == 1 && mixed)) ? 1 : 0;
+    const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, ctas, fixed, stream);
     if (st != SGPU_ERR_UNSUPPORTED) return st;
   }
   const int dcx = data_complex_for(p, data_kind);

@@ -33,6 +33,7 @@
 #include "../../shenfun_gb300/csrc/lc_fused.cuh"
 #include "../../shenfun_gb300/csrc/ref_progs.cuh"
 #include "../../shenfun_gb300/csrc/fft256.cuh"
+#include "../../shenfun_gb300/csrc/fft256_fx.cuh"
 
 using namespace sgpu;
 
@@ -142,6 +143,32 @@ static void f256_block(int kind, const LinePlan& p, const f256::Args& a, int64_t
   }
 }
 
+// the fixed-point form of the same passes (fft256_fx.cuh)
+template <int KIND>
+static void f256_block_fx(const LinePlan& p, const f256::Args& a, int64_t blk, unsigned char* smem,
+                          const f256::FxScale& s) {
+  using namespace f256;
+  const FxShared sh = fx_shared(smem);
+  static Cq v[NT][16];
+  if (KIND == C2C_FWD || KIND == C2C_BWD) {
+    for (int t = 0; t < NT; ++t) fx_c2c_pass1<KIND>(p, a, blk, sh, t);
+    for (int t = 0; t < NT; ++t) {
+      const int E = fx_c2c_pass2(sh, t, v[t]);
+      fx_c2c_store<KIND>(a, t, v[t], E, sh, s);
+    }
+    return;
+  }
+  for (int t = 0; t < NT; ++t) fx_load<KIND>(a, blk, t, sh);
+  for (int t = 0; t < NT; ++t) fx_pass1<KIND>(p, a, sh, t);
+  for (int t = 0; t < NT; ++t) fx_pass2_dft(sh.Z, t, v[t]);
+  if (KIND == R2C) {
+    for (int t = 0; t < NT; ++t) fx_r2c_stash(sh.Z, t, v[t]);
+    for (int t = 0; t < NT; ++t) fx_r2c_post(a, sh, t, NT, s);
+    return;
+  }
+  for (int t = 0; t < NT; ++t) fx_c2r_store(a, t, v[t], sh, s);
+}
+
 static int f256_mode(int argc, char** argv) {
   // f256 kind outer inner scl in out   (kind: SGPU_XF_*; form from SGPU_EMU_FORM)
   if (argc < 8) return 2;
@@ -167,11 +194,22 @@ static int f256_mode(int argc, char** argv) {
   const int64_t pbl = getenv("SGPU_EMU_PB") ? atoll(getenv("SGPU_EMU_PB")) : 0;
   f256::Args a{in, out, outer * inner, inner, scl, pbl};
   const int64_t nt = f256::tiles(kind, a.nlines, pbl);
-  const size_t zb = form == SGPU_MIXED_DF ? f256::smem_bytes<df>() : f256::smem_bytes<double>();
+  const bool fx = getenv("SGPU_EMU_FX") && atoi(getenv("SGPU_EMU_FX")) && form == SGPU_MIXED_DF;
+  const size_t zb = fx ? f256::fx_smem_bytes()
+                       : (form == SGPU_MIXED_DF ? f256::smem_bytes<df>() : f256::smem_bytes<double>());
   void* Z = malloc(zb);
+  const f256::FxScale fs = f256::fx_scale(scl);
   for (int64_t b = 0; b < nt; ++b) {
     memset(Z, 0xff, zb);  // NaN patterns: unwritten entries show
-    if (form == SGPU_MIXED_DF)
+    if (fx) {
+      unsigned char* sm = (unsigned char*)Z;
+      switch (kind) {
+        case f256::C2C_FWD: f256_block_fx<f256::C2C_FWD>(p, a, b, sm, fs); break;
+        case f256::C2C_BWD: f256_block_fx<f256::C2C_BWD>(p, a, b, sm, fs); break;
+        case f256::R2C: f256_block_fx<f256::R2C>(p, a, b, sm, fs); break;
+        default: f256_block_fx<f256::C2R>(p, a, b, sm, fs); break;
+      }
+    } else if (form == SGPU_MIXED_DF)
       f256_block<df>(kind, p, a, b, (Cx<df>*)Z);
     else
       f256_block<double>(kind, p, a, b, (Cx<double>*)Z);

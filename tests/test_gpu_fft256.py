@@ -1,6 +1,7 @@
 """The strided length-256 Fourier kernel (variant 1 of length-256 Fourier
-plans) against the generic line programs (variant 2) and the oracle, on the
-channel grid's layouts and on ragged ones, in both arithmetic forms."""
+plans: FP64, or the mixed form in 64-bit fixed point) against the generic
+line programs (variant 2), the double-float kernels (variants 3 / 4) and the
+oracle, on the channel grid's layouts and on ragged ones."""
 import numpy as np
 import pytest
 import torch
@@ -48,8 +49,15 @@ def test_fft256_variants_and_oracle(form, shape, axis):
         a = run(kind, f, xd, axis, 256, 1, scale)
         b = run(kind, f, xd, axis, 256, 2, scale)
         assert rel(a, b.cpu().numpy()) < tol
-        for v in (3, 4):  # the strided kernel at 2 and 3 CTAs per SM: the same arithmetic
+        # the strided kernel at 2 and 3 CTAs per SM: the same arithmetic (the
+        # mixed form's default is the fixed-point pair 5 / 6, FP64's is 3 / 4)
+        pair = (5, 6) if form == "mixed" else (3, 4)
+        for v in pair:
             assert torch.equal(run(kind, f, xd, axis, 256, v, scale), a)
+        if form == "mixed":
+            d3 = run(kind, f, xd, axis, 256, 3, scale)
+            assert torch.equal(run(kind, f, xd, axis, 256, 4, scale), d3)
+            assert rel(d3, b.cpu().numpy()) < tol
         if small:
             ref = S.c2c_forward(xc, axis=axis) if kind == _lib.XF_C2C_FWD else S.c2c_backward(xc, axis=axis)
             assert rel(a, ref) < tol
@@ -77,3 +85,52 @@ def test_fft256_in_place_c2c():
         x = torch.as_tensor(xc, device="cuda")
         p(x, x, 0, 1.0 / 256)
         assert rel(x, S.c2c_forward(xc, axis=0)) < 2e-13
+
+
+@pytest.mark.parametrize("shape,axis", SHAPES, ids=[f"{s}-ax{a}" for s, a in SHAPES])
+def test_fft256_fixed_point_variants(shape, axis):
+    """Variants 5 and 6 (the mixed form in 64-bit fixed point, 2 and 3 CTAs
+    per SM): the same bits at both occupancies, every line to ~1e-15 of its
+    own largest entry with line magnitudes spread over 2^-200 .. 2^200, and
+    R2C -> C2R returns the input."""
+    from shenfun_gb300 import _lib
+    f = _lib.MIXED_DF
+    g = np.random.default_rng(sum(shape) + 3 * axis)
+    small = int(np.prod(shape)) <= 2_000_000
+    mshape = [1] * len(shape)
+    for d in range(len(shape)):
+        if d != axis:
+            mshape[d] = shape[d]
+    mag = np.exp2(g.integers(-200, 200, mshape).astype(float))
+
+    def line_rel(a, ref):
+        a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else a
+        err = np.abs(a - ref).max(axis=axis)
+        sc = np.abs(ref).max(axis=axis)
+        return float((err / np.where(sc > 0, sc, 1.0)).max())
+
+    xc = (g.standard_normal(shape) + 1j * g.standard_normal(shape)) * mag
+    xd = torch.as_tensor(xc, device="cuda")
+    for kind, scale in ((_lib.XF_C2C_FWD, 1.0 / 256), (_lib.XF_C2C_BWD, 1.0)):
+        a = run(kind, f, xd, axis, 256, 5, scale)
+        assert torch.equal(run(kind, f, xd, axis, 256, 6, scale), a)
+        if small:
+            ref = S.c2c_forward(xc, axis=axis) if kind == _lib.XF_C2C_FWD else S.c2c_backward(xc, axis=axis)
+            assert line_rel(a, ref) < 4e-15
+    xr = g.standard_normal(shape) * mag
+    xrd = torch.as_tensor(xr, device="cuda")
+    a = run(_lib.XF_R2C, f, xrd, axis, 129, 5, 1.0 / 256)
+    assert torch.equal(run(_lib.XF_R2C, f, xrd, axis, 129, 6, 1.0 / 256), a)
+    if small:
+        assert line_rel(a, S.r2c_forward(xr, axis=axis)) < 4e-15
+    c1 = run(_lib.XF_C2R, f, a, axis, 256, 5, 1.0)
+    assert torch.equal(run(_lib.XF_C2R, f, a, axis, 256, 6, 1.0), c1)
+    assert line_rel(c1, xr) < 1e-14
+
+
+def test_fft256_fixed_point_is_mixed_only():
+    from shenfun_gb300 import _lib
+    from shenfun_gb300.plans import LinePlan
+    p = LinePlan(_lib.XF_C2C_FWD, 256, form=_lib.PLAIN_F64)
+    with pytest.raises(_lib.SgpuError):
+        p.variant = 5

@@ -667,11 +667,88 @@ def test_fft256_strided(emu, kind, outer, inner, form, monkeypatch):
     assert rel(got, ref) < 1e-13
 
 
+# ---- the same passes in 64-bit fixed point (fft256_fx.cuh) ------------------------
+def _line_rel(got, ref, axis=1):
+    """max over lines of the line's error / the line's largest entry"""
+    err = np.abs(got - ref).max(axis=axis)
+    scale = np.abs(ref).max(axis=axis)
+    return float((err / np.where(scale > 0, scale, 1.0)).max())
+
+
+@pytest.mark.parametrize("kind,outer,inner", [(C2C_FWD, 1, 37), (C2C_BWD, 2, 20), (R2C, 3, 19), (R2C, 1, 33),
+                                              (C2R, 2, 17), (C2R, 1, 33)])
+def test_fft256_fixed_point(emu, kind, outer, inner, monkeypatch):
+    """Every line (every real line of a pair) to ~2^-53 of its own largest
+    entry, with line magnitudes spread over 2^-300 .. 2^300 so that paired
+    lines differ by many orders of magnitude."""
+    monkeypatch.setenv("SGPU_EMU_FORM", "1")
+    monkeypatch.setenv("SGPU_EMU_FX", "1")
+    g = np.random.default_rng(kind * 100 + inner + 7)
+    n = 256
+    mag = np.exp2(g.integers(-300, 300, (outer, 1, inner)).astype(float))
+    if kind in (C2C_FWD, C2C_BWD):
+        x = (g.standard_normal((outer, n, inner)) + 1j * g.standard_normal((outer, n, inner))) * mag
+        scl = 1.0 / n if kind == C2C_FWD else 1.0
+        res = run(emu, ["f256", kind, outer, inner, repr(scl)], [x], x.size * 2).view(np.complex128)
+        ref = S.c2c_forward(x, axis=1) if kind == C2C_FWD else S.c2c_backward(x, axis=1)
+        got = res.reshape(x.shape)
+    elif kind == R2C:
+        x = g.standard_normal((outer, n, inner)) * mag
+        res = run(emu, ["f256", kind, outer, inner, repr(1.0 / n)], [x], outer * 129 * inner * 2)
+        got = res.view(np.complex128).reshape(outer, 129, inner)
+        ref = S.r2c_forward(x, axis=1)
+    else:
+        y = (g.standard_normal((outer, 129, inner)) + 1j * g.standard_normal((outer, 129, inner))) * mag
+        res = run(emu, ["f256", kind, outer, inner, repr(1.0)], [y], outer * n * inner)
+        got = res.reshape(outer, n, inner)
+        ref = S.r2c_backward(y, n, axis=1)
+    assert np.isfinite(got).all()
+    assert _line_rel(got, ref) < 4e-15
+
+
+@pytest.mark.parametrize("kind", [C2C_FWD, R2C, C2R])
+def test_fft256_fixed_point_nan_scale_and_zero_lines(emu, kind, monkeypatch):
+    """A line holding NaN comes out NaN (its pair partner does not), a zero
+    line stays zero, and a scale that is not a power of two applies."""
+    monkeypatch.setenv("SGPU_EMU_FORM", "1")
+    monkeypatch.setenv("SGPU_EMU_FX", "1")
+    g = np.random.default_rng(kind)
+    n, outer, inner = 256, 1, 18
+    scl = 0.3
+    if kind == C2C_FWD:
+        x = g.standard_normal((outer, n, inner)) + 1j * g.standard_normal((outer, n, inner))
+        x[0, 5, 3] = np.nan
+        x[0, :, 4] = 0
+        got = run(emu, ["f256", kind, outer, inner, repr(scl)], [x], x.size * 2).view(np.complex128)
+        got = got.reshape(x.shape)
+        ref = S.c2c_forward(x, axis=1) * n * scl
+    elif kind == R2C:
+        x = g.standard_normal((outer, n, inner))
+        x[0, 7, 2] = np.inf
+        x[0, :, 5] = 0
+        got = run(emu, ["f256", kind, outer, inner, repr(scl)], [x], outer * 129 * inner * 2)
+        got = got.view(np.complex128).reshape(outer, 129, inner)
+        ref = S.r2c_forward(x, axis=1) * n * scl
+    else:
+        x = g.standard_normal((outer, 129, inner)) + 1j * g.standard_normal((outer, 129, inner))
+        x[0, 9, 2] = np.nan
+        x[0, :, 5] = 0
+        got = run(emu, ["f256", kind, outer, inner, repr(scl)], [x], outer * n * inner).reshape(outer, n, inner)
+        ref = S.r2c_backward(x, n, axis=1) * scl
+    bad = 3 if kind == C2C_FWD else 2
+    assert np.isnan(got[0, :, bad]).all()
+    ok = [i for i in range(inner) if i != bad]
+    assert np.isfinite(got[0][:, ok]).all()
+    assert np.all(got[0, :, 4 if kind == C2C_FWD else 5] == 0)
+    assert _line_rel(got[:, :, ok], ref[:, :, ok]) < 4e-15
+
+
 # ---- pairing blocks: a stack of arrays transformed at once gives each array's bits
 @pytest.mark.parametrize("kind,n,basis", [(R2C, 24, 0), (R2C, 256, 0), (C2R, 24, 0), (C2R, 256, 0),
                                           (CHEB_SCALAR, 17, BASIS["SD"]), (CHEB_BACKWARD, 17, BASIS["SD"])])
 @pytest.mark.parametrize("inner", [1, 31])
-def test_pair_blocks_stack_equals_alone(emu, kind, n, basis, inner, monkeypatch):
+@pytest.mark.parametrize("fx_form", [0, 1])
+def test_pair_blocks_stack_equals_alone(emu, kind, n, basis, inner, fx_form, monkeypatch):
     g = np.random.default_rng(n + inner)
     K, outer = 3, 3  # outer x inner lines per member: odd when inner is odd
     if kind == C2R:
@@ -689,6 +766,9 @@ def test_pair_blocks_stack_equals_alone(emu, kind, n, basis, inner, monkeypatch)
                                     o * n_out * inner * (2 if kind == R2C else 1))
     else:
         runner = lambda arr, o: xform(emu, kind, n, basis, arr, 1, cplx, 1.0, n_out).reshape(-1)  # noqa: E731
+    if n == 256 and inner >= 16 and kind in (R2C, C2R):
+        monkeypatch.setenv("SGPU_EMU_FORM", str(fx_form))
+        monkeypatch.setenv("SGPU_EMU_FX", "1" if fx_form else "0")
     monkeypatch.setenv("SGPU_EMU_PB", str(outer * inner))
     stacked = runner(x, K * outer)
     monkeypatch.delenv("SGPU_EMU_PB")
