@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "ddouble.h"
+#include "lc_fused.h"
 #include "ozaki_tc.h"
 #include "solvers.cuh"
 
@@ -214,6 +215,10 @@ struct sgpu_legendre_plan {
   double* d_nodes;   // x, w (2N)
   std::vector<double> x, w;
   oz::Matrix tc_scalar, tc_forward, tc_back;  // mixed form: split Ms, Ms B^{-T}, Mb
+  // mixed form, contiguous lines, N <= 339: the same three operators for the
+  // fused contraction (the digit split inside the GEMM kernel, 54 bits)
+  lc::Matrix fc[3];
+  bool fused = false;
 };
 
 extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int basis, int form) {
@@ -337,10 +342,19 @@ extern "C" int sgpu_legendre_plan_create(sgpu_legendre_plan** out, int N, int ba
     int st = oz::matrix_create(Ms.data(), N, 0, &p->tc_scalar);
     if (st == SGPU_OK) st = oz::matrix_create(F.data(), N, 0, &p->tc_forward);
     if (st == SGPU_OK) st = oz::matrix_create(Mb.data(), N, 0, &p->tc_back);
+    // contiguous lines: the fused contraction where it applies (all three
+    // directions, so one scratch size serves every call)
+    const oz::Matrix* tcs[3] = {&p->tc_scalar, &p->tc_forward, &p->tc_back};
+    const double* hm[3] = {Ms.data(), F.data(), Mb.data()};
+    if (st == SGPU_OK && lc::supported(N, tcs[0]->K) && lc::supported(N, tcs[1]->K) && lc::supported(N, tcs[2]->K)) {
+      for (int d = 0; d < 3 && st == SGPU_OK; ++d) st = lc::matrix_create(hm[d], N, tcs[d]->K, &p->fc[d]);
+      p->fused = st == SGPU_OK;
+    }
     if (st != SGPU_OK) {
       oz::matrix_destroy(&p->tc_scalar);
       oz::matrix_destroy(&p->tc_forward);
       oz::matrix_destroy(&p->tc_back);
+      for (int d = 0; d < 3; ++d) lc::matrix_destroy(&p->fc[d]);
       cudaFree(dev);
       delete p;
       return st;
@@ -356,6 +370,7 @@ extern "C" int sgpu_legendre_plan_destroy(sgpu_legendre_plan* p) {
   oz::matrix_destroy(&p->tc_scalar);
   oz::matrix_destroy(&p->tc_forward);
   oz::matrix_destroy(&p->tc_back);
+  for (int d = 0; d < 3; ++d) lc::matrix_destroy(&p->fc[d]);
   delete p;
   return SGPU_OK;
 }
@@ -540,7 +555,11 @@ static int legendre_run(const sgpu_legendre_plan* p, int direction, const void* 
   const int64_t nlines = outer * inner;
   if (nlines == 0) return SGPU_OK;
   const int cplx = data_kind == SGPU_COMPLEX;
-  if (p->form == SGPU_MIXED_DF) {
+  if (p->form == SGPU_MIXED_DF && p->fused && inner == 1) {
+    const int st = lc::contract(p->fc[direction], (const double*)in, (double*)out, nlines, cplx, work, work_bytes,
+                                nullptr, 0, stream);
+    if (st != SGPU_OK) return st;
+  } else if (p->form == SGPU_MIXED_DF) {
     const oz::Matrix& M = direction == 2 ? p->tc_back : (direction == 1 ? p->tc_forward : p->tc_scalar);
     const int st = oz::contract(M, (const double*)in, (double*)out, nlines, inner, cplx, work, work_bytes, stream);
     if (st != SGPU_OK) return st;
@@ -570,7 +589,9 @@ extern "C" int sgpu_legendre_workspace_size(const sgpu_legendre_plan* p, int64_t
     *bytes = 0;
     return SGPU_OK;
   }
-  *bytes = oz::workspace_bytes(p->tc_scalar, outer * inner, inner, data_kind == SGPU_COMPLEX);
+  *bytes = p->fused && inner == 1
+               ? lc::workspace_bytes(p->fc[0], outer, data_kind == SGPU_COMPLEX)
+               : oz::workspace_bytes(p->tc_scalar, outer * inner, inner, data_kind == SGPU_COMPLEX);
   return SGPU_OK;
 }
 
