@@ -144,9 +144,10 @@ int sgpu_plan_execute_blocks(const sgpu_plan* plan, const void* in, void* out, i
  * overlap this tile's epilogue).  Length-256 Fourier plans (R2C, C2R, C2C):
  * 1 = the strided-pass kernel for axes with inner >= 16 (pass 1 and pass 2
  * of a 16 x 16 register FFT reading and writing global memory directly, one
- * shared-memory transpose) in its default arithmetic and occupancy (FP64 at
- * 2 CTAs per SM; the mixed form in 64-bit fixed point, C2C at 2 CTAs per SM
- * and R2C / C2R at 3), 2 = the generic line programs, 3 / 4 = the
+ * shared-memory transpose) in its default arithmetic and occupancy (FP64,
+ * or the mixed form in 64-bit fixed point, at 2 CTAs per SM; fixed-point
+ * R2C / C2R transform each real line as a half-length complex FFT), 2 = the
+ * generic line programs, 3 / 4 = the
  * strided-pass kernel at 2 / 3 CTAs per SM in FP64 (plain form) or
  * double-float (mixed form), 5 / 6 = the mixed form in 64-bit fixed point
  * at 2 / 3 CTAs per SM (SGPU_ERR_UNSUPPORTED for the plain form; complex

@@ -36,29 +36,37 @@ __global__ void __launch_bounds__(NT, MINB) k_fft256(LinePlan p, Args a) {
 template <int KIND, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_fft256_fx(LinePlan p, Args a, FxScale s) {
   extern __shared__ __align__(16) unsigned char f256_smem[];
-  const FxShared sh = fx_shared(f256_smem);
   const int t = (int)threadIdx.x;
   const int64_t blk = (int64_t)blockIdx.x;
-  Cq v[16];
   if (KIND == C2C_FWD || KIND == C2C_BWD) {
+    const FxShared sh = fx_shared(f256_smem);
+    Cq v[16];
     fx_c2c_pass1<KIND>(p, a, blk, sh, t);
     __syncthreads();
     const int E = fx_c2c_pass2(sh, t, v);
     fx_c2c_store<KIND>(a, t, v, E, sh, s);
     return;
   }
-  fx_load<KIND>(a, blk, t, sh);
+  const FxHalf sh = fxh_shared(f256_smem);
+  if (KIND == R2C)
+    fxh_r2c_pass1(p, a, blk, sh, t);
+  else
+    fxh_c2r_pass1(p, a, blk, sh, t);
   __syncthreads();
-  fx_pass1<KIND>(p, a, sh, t);
-  __syncthreads();
-  fx_pass2_dft(sh.Z, t, v);
+  // pass 2: two (line, k1) items per thread
+  Cq v[2][8];
+  int E[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) E[j] = fxh_pass2(sh, (t + NT * j) & 31, (t + NT * j) >> 5, v[j]);
   if (KIND == R2C) {
     __syncthreads();
-    fx_r2c_stash(sh.Z, t, v);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) fxh_r2c_stash(sh, (t + NT * j) & 31, (t + NT * j) >> 5, v[j], E[j]);
     __syncthreads();
-    fx_r2c_post(a, sh, t, NT, s);
+    fxh_r2c_post(p, a, sh, t, NT, s);
   } else {
-    fx_c2r_store(a, t, v, sh, s);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) fxh_c2r_store(a, sh, (t + NT * j) & 31, (t + NT * j) >> 5, v[j], E[j], s);
   }
 }
 
@@ -95,15 +103,16 @@ int launch_fx(const LinePlan& p, const Args& a, const FxScale& sc, unsigned nblo
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) return SGPU_ERR_CUDA;
   DevAttr& d = g_dev[dev];
   const int mi = MINB == 3 ? 1 : 0;
+  const size_t smem = (KIND == R2C || KIND == C2R) ? fxh_smem_bytes() : fx_smem_bytes();
   std::call_once(d.once[2][KIND][mi], [&]() {
     d.rc[2][KIND][mi] = cudaFuncSetAttribute(k_fft256_fx<KIND, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)fx_smem_bytes()) == cudaSuccess
+                                             (int)smem) == cudaSuccess
                             ? 1
                             : -1;
     cudaGetLastError();
   });
   if (d.rc[2][KIND][mi] != 1) return SGPU_ERR_CUDA;
-  k_fft256_fx<KIND, MINB><<<nblocks, NT, fx_smem_bytes(), s>>>(p, a, sc);
+  k_fft256_fx<KIND, MINB><<<nblocks, NT, smem, s>>>(p, a, sc);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }
 
@@ -160,8 +169,10 @@ int f256_launch(const LinePlan& p, const double* in, double* out, int64_t nlines
     const bool cin = kind != R2C, cout = kind != C2R;
     if ((cin && ((uintptr_t)in & 15)) || (cout && ((uintptr_t)out & 15))) return SGPU_ERR_UNSUPPORTED;
     const FxScale sc = fx_scale(scl);
-    return ctas_per_sm == 3 ? launch_fx_kind<3>(kind, p, a, sc, (unsigned)nt, s)
-                            : launch_fx_kind<2>(kind, p, a, sc, (unsigned)nt, s);
+    const int64_t nx = fx_tiles(kind, nlines);  // R2C / C2R: 32 real lines per CTA, no pairs
+    if (nx > 0x7fffffffLL) return SGPU_ERR_ARG;
+    return ctas_per_sm == 3 ? launch_fx_kind<3>(kind, p, a, sc, (unsigned)nx, s)
+                            : launch_fx_kind<2>(kind, p, a, sc, (unsigned)nx, s);
   }
   if (ctas_per_sm == 3)
     return p.form == SGPU_MIXED_DF ? launch_r<df, 3>(kind, p, a, (unsigned)nt, s)

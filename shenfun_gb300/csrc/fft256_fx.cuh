@@ -18,14 +18,15 @@
 // normwise accuracy of an FP64 FFT - at 2 integer instructions per addition
 // instead of ~11 FP32 instructions for a double-float addition.
 //
-// Lines of a complex pair (R2C: z = p + i q; C2R: z = conj(P + i Q)) keep
-// separate scales 2^Sp and 2^Sq: the DFT is linear, so the pair's transform
-// is 2^Sp DFT(p) + i 2^Sq DFT(q) on one integer grid, and each line is
-// unscaled on its own at the end.  The scales need the line's maximum
-// exponent before any value is converted: each thread reduces the exponents
-// of its 16 values, the 16 threads of a line meet in shared memory (one
-// barrier), and the values are then loaded again (from L1 or L2) and
-// converted: held in registers across the barrier they would spill.
+// Grids.  C2C: thread (line, n2) converts its 16 values on its own grid
+// (its largest exponent) before the first DFT; pass 2 aligns the 16 threads'
+// results to the line's grid by rounding shifts.  R2C / C2R transform each
+// real line alone as a half-length complex FFT (z_n = x_2n + i x_2n+1, 128
+// points: DFT16 x DFT8 four-step, 32 lines per CTA) with the same per-thread
+// grids, so no line shares a grid with another and no exponent pass or
+// barrier comes before the first DFT.  R2C separates the even / odd spectra
+// after the FFT (X_k = E_k + W^k O_k from Z_k and Z_{128-k}), C2R combines
+// them before it (Z_k = X_k + conj X_{128-k} + i W^-k (X_k - conj X_{128-k})).
 //
 // A line holding Inf or NaN comes out as NaN (an FP64 transform spreads it
 // over the line the same way); subnormal inputs count as zero, and outputs
@@ -182,29 +183,23 @@ SGPU_HD long long q_shr(long long X, int d) {
   return (X + ((1LL << sft) >> 1)) >> sft;
 }
 
-// shared memory beyond the exchange buffer: per (line, n2) the local
-// maximum exponents of the line's values (R2C / C2R: of p and of q), per
-// line their maximum, then per line the element offsets of its first
-// entries in the input and the output (R2C / C2R: of p and of q; -1 for
-// lines past the array or block)
-const int EX = TL * 16;
+// C2C shared memory: the exchange buffer, per (line, n2) the pass-1 grid
+// exponents, per line its exponent and output offset (-1 past the array)
 SGPU_HD size_t fx_smem_bytes() {
-  return sizeof(Cq) * (size_t)TL * LDZ + sizeof(int) * (2 * EX + 2 * TL) + sizeof(long long) * 4 * TL;
+  return sizeof(Cq) * (size_t)TL * LDZ + sizeof(int) * (16 * TL + TL) + sizeof(long long) * TL + 8;
 }
 struct FxShared {
   Cq* Z;
-  int* Ez;          // [2][TL][16]
-  int* El;          // [2][TL]: written in pass 1, read after its barrier
-  long long* Lin;   // [2 TL]: p (or the complex line), q
-  long long* Lout;  // [2 TL]
+  int* Ez;          // [TL][16]
+  int* El;          // [TL]
+  long long* Lout;  // [TL]
 };
 SGPU_HD FxShared fx_shared(unsigned char* base) {
   FxShared f;
   f.Z = (Cq*)base;
   f.Ez = (int*)(base + sizeof(Cq) * (size_t)TL * LDZ);
-  f.El = f.Ez + 2 * EX;
-  f.Lin = (long long*)(f.El + 2 * TL);
-  f.Lout = f.Lin + 2 * TL;
+  f.El = f.Ez + 16 * TL;
+  f.Lout = (long long*)(f.El + TL);  // 17 TL = 272 ints: 8-byte aligned
   return f;
 }
 
@@ -214,135 +209,6 @@ SGPU_HD int line_exp(const int* Ez, int line) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) E = Ez[line * 16 + i] > E ? Ez[line * 16 + i] : E;
   return E;
-}
-
-// -- phase A: the maximum exponents of the thread's inputs and (threads
-// n2 = 0) the line offsets --------------------------------------------------
-template <int KIND>
-SGPU_HD void fx_load(const Args& a, int64_t blk, int t, const FxShared& sh) {
-  const int line = t & 15, n2 = t >> 4;
-  int ep = 0, eq = 0;
-  if (KIND == C2C_FWD || KIND == C2C_BWD) {
-    // C2C needs no common exponent before its first DFT (fx_c2c_pass1)
-  } else {
-    int64_t lp;
-    bool lvp, lvq;
-    pair_lines(a, blk * TL + line, lp, lvp, lvq);
-    const int nh = N / 2 + 1;
-    const int64_t n_in = KIND == R2C ? N : nh, n_out = KIND == R2C ? nh : N;
-    if (n2 == 0) {
-      sh.Lin[line] = lvp ? base_off(lp, n_in, a.inner) : -1;
-      sh.Lin[TL + line] = lvq ? base_off(lp + 1, n_in, a.inner) : -1;
-      sh.Lout[line] = lvp ? base_off(lp, n_out, a.inner) : -1;
-      sh.Lout[TL + line] = lvq ? base_off(lp + 1, n_out, a.inner) : -1;
-    }
-    if (KIND == R2C) {
-      const double* sp = a.in + (lvp ? base_off(lp, N, a.inner) : 0);
-      const double* sq = a.in + (lvq ? base_off(lp + 1, N, a.inner) : 0);
-#pragma unroll
-      for (int n1 = 0; n1 < 16; ++n1) {
-        const int64_t k = (int64_t)(16 * n1 + n2) * a.inner;
-        const int e0 = lvp ? bexp(ldg(sp + k)) : 0, e1 = lvq ? bexp(ldg(sq + k)) : 0;
-        ep = e0 > ep ? e0 : ep;
-        eq = e1 > eq ? e1 : eq;
-      }
-    } else {  // C2R: exponents only (the values are loaded again in pass 1)
-      const double* sp = a.in + 2 * (lvp ? base_off(lp, nh, a.inner) : 0);
-      const double* sq = a.in + 2 * (lvq ? base_off(lp + 1, nh, a.inner) : 0);
-#pragma unroll
-      for (int n1 = 0; n1 < 16; ++n1) {
-        const int j = 16 * n1 + n2;
-        if (j > N / 2) continue;  // the conjugate half repeats entries 1..127
-        const int64_t k = (int64_t)j * a.inner;
-        const bool edge = j == 0 || j == N / 2;
-        if (lvp) {
-          double re, im;
-          ldg2(sp + 2 * k, re, im);
-          const int e0 = bexp(re), e1 = edge ? 0 : bexp(im);
-          ep = e0 > ep ? e0 : ep;
-          ep = e1 > ep ? e1 : ep;
-        }
-        if (lvq) {
-          double re, im;
-          ldg2(sq + 2 * k, re, im);
-          const int e0 = bexp(re), e1 = edge ? 0 : bexp(im);
-          eq = e0 > eq ? e0 : eq;
-          eq = e1 > eq ? e1 : eq;
-        }
-      }
-    }
-  }
-  sh.Ez[line * 16 + n2] = ep;
-  sh.Ez[EX + line * 16 + n2] = eq;
-}
-
-// -- pass 1: convert on the line grid, 16-point DFT, twiddle, Z[line][k1][n2]
-template <int KIND>
-SGPU_HD void fx_pass1(const LinePlan& p, const Args& a, const FxShared& sh, int t) {
-  const int line = t & 15, n2 = t >> 4;
-  Cq v[16];
-  if (KIND == C2C_FWD || KIND == C2C_BWD) {
-    return;  // fx_c2c_pass1
-  } else if (KIND == R2C) {
-    const int Ep = line_exp(sh.Ez, line) + 1, Eq = line_exp(sh.Ez + EX, line) + 1;
-    if (n2 == 0) {
-      sh.El[line] = Ep - 1;
-      sh.El[TL + line] = Eq - 1;
-    }
-    const long long bp = sh.Lin[line], bq = sh.Lin[TL + line];
-    const double* sp = a.in + (bp >= 0 ? bp : 0);
-    const double* sq = a.in + (bq >= 0 ? bq : 0);
-#pragma unroll
-    for (int n1 = 0; n1 < 16; ++n1) {
-      const int64_t k = (int64_t)(16 * n1 + n2) * a.inner;
-      v[n1] = cq(bp >= 0 ? fx_from_f64(ldg(sp + k), Ep) : 0, bq >= 0 ? fx_from_f64(ldg(sq + k), Eq) : 0);
-    }
-  } else {  // C2R: z_j = conj(P_j + i Q_j), Hermitian extension, P and Q on their own grids
-    const int Ep = line_exp(sh.Ez, line) + 1, Eq = line_exp(sh.Ez + EX, line) + 1;
-    if (n2 == 0) {
-      sh.El[line] = Ep - 1;
-      sh.El[TL + line] = Eq - 1;
-    }
-    const long long bp = sh.Lin[line], bq = sh.Lin[TL + line];
-    const double* sp = a.in + 2 * (bp >= 0 ? bp : 0);
-    const double* sq = a.in + 2 * (bq >= 0 ? bq : 0);
-#pragma unroll
-    for (int n1 = 0; n1 < 16; ++n1) {
-      const int j = 16 * n1 + n2;
-      const bool up = j > N / 2;
-      const int64_t k = (int64_t)(up ? N - j : j) * a.inner;
-      const bool edge = j == 0 || j == N / 2;
-      long long pr = 0, pi = 0, qr = 0, qi = 0;
-      if (bp >= 0) {
-        double re, im;
-        ldg2(sp + 2 * k, re, im);
-        pr = fx_from_f64(re, Ep);
-        pi = edge ? 0 : fx_from_f64(im, Ep);
-      }
-      if (bq >= 0) {
-        double re, im;
-        ldg2(sq + 2 * k, re, im);
-        qr = fx_from_f64(re, Eq);
-        qi = edge ? 0 : fx_from_f64(im, Eq);
-      }
-      if (up) {
-        pi = -pi;
-        qi = -qi;
-      }
-      // P + i Q = (pr - qi) + i (pi + qr), conjugated
-      v[n1] = cq(pr - qi, -(pi + qr));
-    }
-  }
-  q_dft16(v);
-  Cq* z = sh.Z + (size_t)line * LDZ + n2;
-  z[0] = v[0];
-  const int* tw = p.tw_q;
-#pragma unroll
-  for (int k1 = 1; k1 < 16; ++k1) {
-    const int e = n2 * k1;
-    const Tw wr{tw[4 * e], tw[4 * e + 1]}, wi{tw[4 * e + 2], tw[4 * e + 3]};
-    z[k1 * 17] = e == 0 ? v[k1] : q_mul(v[k1], wr, wi);
-  }
 }
 
 // output scaling: value = X 2^(sx + Eh - 1076) (sm: a remaining FP64
@@ -432,65 +298,214 @@ SGPU_HD void fx_c2c_store(const Args& a, int t, const Cq* v, int Eh, const FxSha
   }
 }
 
-// -- pass 2: thread (line, k1); X[k1 + 16 k2] in v[k2] ----------------------
-SGPU_HD void fx_pass2_dft(const Cq* Z, int t, Cq* v) {
-  const int line = t & 15, k1 = t >> 4;
-  const Cq* z = Z + (size_t)line * LDZ + k1 * 17;
-#pragma unroll
-  for (int n2 = 0; n2 < 16; ++n2) v[n2] = z[n2];
-  q_dft16(v);
+// -- R2C / C2R: one real line as a 128-point complex FFT ------------------
+const int TH = 32;    // real lines per CTA
+const int MH = 128;   // complex FFT length
+const int LDH = 129;  // shared-memory line stride (odd in 16-byte units)
+
+struct FxHalf {
+  Cq* Z;            // [TH][LDH]: entry (k1, n2) of pass 1 at k1 * 8 + n2; spectrum k after pass 2
+  int* Ez;          // [TH][8]: pass-1 grid exponents
+  int* El;          // [TH]: line exponents
+  long long* Lout;  // [TH]: output offset of each line (-1 past the array)
+};
+SGPU_HD size_t fxh_smem_bytes() {
+  return sizeof(Cq) * (size_t)TH * LDH + sizeof(int) * (8 * TH + TH) + sizeof(long long) * TH + 8;
+}
+SGPU_HD FxHalf fxh_shared(unsigned char* base) {
+  FxHalf f;
+  f.Z = (Cq*)base;
+  f.Ez = (int*)(base + sizeof(Cq) * (size_t)TH * LDH);
+  f.El = f.Ez + 8 * TH;
+  // 8-byte aligned: the int arrays hold 9 TH = 288 entries
+  f.Lout = (long long*)(f.El + TH);
+  return f;
 }
 
-// C2R: conj(X) -> real lines 2c (re) and 2c + 1 (im)
-SGPU_HD void fx_c2r_store(const Args& a, int t, const Cq* v, const FxShared& sh, const FxScale& s) {
-  const int line = t & 15, k1 = t >> 4;
-  const double qnan = u2d(0x7ff8000000000000ull);
-  const long long bp = sh.Lout[line], bq = sh.Lout[TL + line];
-  const int Ep = sh.El[line], Eq = sh.El[TL + line];
-  double* dp = bp >= 0 ? a.out + bp : nullptr;
-  double* dq = bq >= 0 ? a.out + bq : nullptr;
+// 8-point forward DFT in place, natural order (2 x 4: n = 4 n1 + n2, k = k1 + 2 k2)
+SGPU_HD void q_dft8(Cq* v) {
+  Cq a[4][2];
 #pragma unroll
-  for (int k2 = 0; k2 < 16; ++k2) {
-    const int64_t k = (int64_t)(k1 + 16 * k2) * a.inner;
-    if (dp) dp[k] = Ep == 0x7ff ? qnan : fx_out(v[k2].re, Ep + 1, s);
-    if (dq) dq[k] = Eq == 0x7ff ? qnan : fx_out(-v[k2].im, Eq + 1, s);
+  for (int n2 = 0; n2 < 4; ++n2) {
+    const Cq t0 = v[n2], t1 = v[4 + n2];
+    a[n2][0] = t0 + t1;
+    a[n2][1] = q_mul_w16(t0 - t1, 2 * n2);  // W_8^{n2}
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 2; ++k1) {
+    Cq t[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+    q_dft4(t);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 2 * k2] = t[k2];
   }
 }
 
-// R2C, after the pass-2 DFTs: W[line][k] = X[k] in shared memory (reusing Z
-// behind a barrier), then P_k = (Z_k + conj Z_{N-k}) / 2 on p's grid and
-// Q_k = -i (Z_k - conj Z_{N-k}) / 2 on q's (the halving folds into the
-// exponent: the grids were 2^(1076 - E - 1), so E - 1 + 1)
-SGPU_HD void fx_r2c_stash(Cq* W, int t, const Cq* v) {
-  const int line = t & 15, k1 = t >> 4;
-  Cq* w = W + (size_t)line * LDZ;
+SGPU_HD Tw tw_re(const LinePlan& p, int e) { return Tw{p.tw_q[4 * e], p.tw_q[4 * e + 1]}; }
+SGPU_HD Tw tw_im(const LinePlan& p, int e) { return Tw{p.tw_q[4 * e + 2], p.tw_q[4 * e + 3]}; }
+
+// pass-1 tail shared by R2C and C2R: 16-point DFT over n1, twiddle
+// W_128^{n2 k1} (= W_256^{2 n2 k1}), Z[line][k1][n2]
+SGPU_HD void fxh_store_pass1(const LinePlan& p, const FxHalf& sh, int line, int n2, Cq* v) {
+  q_dft16(v);
+  Cq* z = sh.Z + (size_t)line * LDH + n2;
+  z[0] = v[0];
 #pragma unroll
-  for (int k2 = 0; k2 < 16; ++k2) w[k1 + 16 * k2] = v[k2];
+  for (int k1 = 1; k1 < 16; ++k1) {
+    const int e = 2 * n2 * k1;
+    z[k1 * 8] = e == 0 ? v[k1] : q_mul(v[k1], tw_re(p, e), tw_im(p, e));
+  }
 }
 
-SGPU_HD void fx_r2c_post(const Args& a, const FxShared& sh, int t, int nth, const FxScale& s) {
+// R2C pass 1: thread t = (n2 << 5) | line loads x[16 n1 + 2 n2] and
+// x[16 n1 + 2 n2 + 1] (z_{8 n1 + n2}) of its line, on its own grid
+SGPU_HD void fxh_r2c_pass1(const LinePlan& p, const Args& a, int64_t blk, const FxHalf& sh, int t) {
+  const int line = t & 31, n2 = t >> 5;
+  const int64_t l = blk * TH + line;
+  const bool live = l < a.nlines;
+  const int64_t bi = live ? base_off(l, N, a.inner) : 0;
+  if (n2 == 0) sh.Lout[line] = live ? base_off(l, N / 2 + 1, a.inner) : -1;
+  const double* src = a.in + bi;
+  double x[32];
+  int et = 0;
+#pragma unroll
+  for (int n1 = 0; n1 < 16; ++n1) {
+    const int64_t k = (int64_t)(16 * n1 + 2 * n2) * a.inner;
+    x[2 * n1] = live ? ldg(src + k) : 0.0;
+    x[2 * n1 + 1] = live ? ldg(src + k + a.inner) : 0.0;
+    const int e0 = bexp(x[2 * n1]), e1 = bexp(x[2 * n1 + 1]);
+    et = e0 > et ? e0 : et;
+    et = e1 > et ? e1 : et;
+  }
+  Cq v[16];
+#pragma unroll
+  for (int n1 = 0; n1 < 16; ++n1) v[n1] = cq(fx_from_f64(x[2 * n1], et + 1), fx_from_f64(x[2 * n1 + 1], et + 1));
+  sh.Ez[line * 8 + n2] = et;
+  fxh_store_pass1(p, sh, line, n2, v);
+}
+
+// C2R pass 1: Z'_k = X_k + conj X_{128-k} + i W^-k (X_k - conj X_{128-k})
+// for k = 8 n1 + n2 (the imaginary parts of X_0 and X_128 are ignored, as
+// an FP64 C2R does), conjugated for the inverse DFT; the inputs are read
+// once for the thread's exponent and again (L1) to convert
+SGPU_HD void fxh_c2r_pass1(const LinePlan& p, const Args& a, int64_t blk, const FxHalf& sh, int t) {
+  const int line = t & 31, n2 = t >> 5;
+  const int nh = N / 2 + 1;
+  const int64_t l = blk * TH + line;
+  const bool live = l < a.nlines;
+  const int64_t bi = live ? base_off(l, nh, a.inner) : 0;
+  if (n2 == 0) sh.Lout[line] = live ? base_off(l, N, a.inner) : -1;
+  const double* src = a.in + 2 * bi;
+  int et = 0;
+  if (live) {
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) {
+      const int k = 8 * n1 + n2, m = MH - k;
+      double r0, i0, r1, i1;
+      ldg2(src + 2 * (int64_t)k * a.inner, r0, i0);
+      ldg2(src + 2 * (int64_t)m * a.inner, r1, i1);
+      const int e0 = bexp(r0), e1 = k == 0 ? 0 : bexp(i0), e2 = bexp(r1), e3 = m == MH ? 0 : bexp(i1);
+      et = e0 > et ? e0 : et;
+      et = e1 > et ? e1 : et;
+      et = e2 > et ? e2 : et;
+      et = e3 > et ? e3 : et;
+    }
+  }
+  const int Eh = et + 1;
+  Cq v[16];
+#pragma unroll
+  for (int n1 = 0; n1 < 16; ++n1) {
+    const int k = 8 * n1 + n2, m = MH - k;
+    double r0 = 0.0, i0 = 0.0, r1 = 0.0, i1 = 0.0;
+    if (live) {
+      ldg2(src + 2 * (int64_t)k * a.inner, r0, i0);
+      ldg2(src + 2 * (int64_t)m * a.inner, r1, i1);
+    }
+    const Cq xk = cq(fx_from_f64(r0, Eh), k == 0 ? 0 : fx_from_f64(i0, Eh));
+    const Cq xm = cq(fx_from_f64(r1, Eh), m == MH ? 0 : -fx_from_f64(i1, Eh));  // conj X_{128-k}
+    const Cq S = xk + xm, D = xk - xm;
+    // D W^-k = conj(conj(D) W^k) with the table's W^k (its -1 is exact)
+    const Cq DW = k == 0 ? D : q_conj(q_mul(q_conj(D), tw_re(p, k), tw_im(p, k)));
+    v[n1] = q_conj(S + q_mul_pi(DW));
+  }
+  sh.Ez[line * 8 + n2] = et;
+  fxh_store_pass1(p, sh, line, n2, v);
+}
+
+// pass 2 of one item (line, k1): align the 8 pass-1 threads of the line to
+// its grid, DFT8 over n2; v[k2] = spectrum index k1 + 16 k2.  Returns the
+// line's exponent (without the headroom bit).
+SGPU_HD int fxh_pass2(const FxHalf& sh, int line, int k1, Cq* v) {
+  const int* ez = sh.Ez + line * 8;
+  int E = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) E = ez[i] > E ? ez[i] : E;
+  const Cq* z = sh.Z + (size_t)line * LDH + k1 * 8;
+#pragma unroll
+  for (int n2 = 0; n2 < 8; ++n2) {
+    const int d = E - ez[n2];
+    v[n2] = cq(q_shr(z[n2].re, d), q_shr(z[n2].im, d));
+  }
+  q_dft8(v);
+  return E;
+}
+
+// R2C after pass 2 (a barrier in between): W[line][k] = Z_k
+SGPU_HD void fxh_r2c_stash(const FxHalf& sh, int line, int k1, const Cq* v, int E) {
+  Cq* w = sh.Z + (size_t)line * LDH;
+#pragma unroll
+  for (int k2 = 0; k2 < 8; ++k2) w[k1 + 16 * k2] = v[k2];
+  if (k1 == 0) sh.El[line] = E;
+}
+
+// R2C after the stash (a barrier in between): 2 X_k = A - i W^k B with
+// A = Z_k + conj Z_{128-k}, B = Z_k - conj Z_{128-k}, k = 0..128, on the
+// line's grid (the halving folds into the exponent)
+SGPU_HD void fxh_r2c_post(const LinePlan& p, const Args& a, const FxHalf& sh, int t, int nth, const FxScale& s) {
   const int nh = N / 2 + 1;
   const double qnan = u2d(0x7ff8000000000000ull);
-  for (int e = t; e < TL * nh; e += nth) {
-    const int line = e & 15, k = e >> 4;
-    const Cq* w = sh.Z + (size_t)line * LDZ;
-    const Cq z = w[k];
-    const Cq zc = q_conj(w[k == 0 ? 0 : N - k]);
-    // z + zc = 2 DFT(p') and -i (z - zc) = 2 DFT(q'), each below 2 * 256 * 2^53
-    const Cq P = z + zc;
-    const Cq Q = q_mul_mi(z - zc);
-    const long long bp = sh.Lout[line], bq = sh.Lout[TL + line];
-    if (bp >= 0) {
-      const int Ep = sh.El[line];
-      double* d = a.out + 2 * (bp + (int64_t)k * a.inner);
-      st2(d, Ep == 0x7ff ? qnan : fx_out(P.re, Ep, s), Ep == 0x7ff ? qnan : fx_out(P.im, Ep, s));
-    }
-    if (bq >= 0) {
-      const int Eq = sh.El[TL + line];
-      double* d = a.out + 2 * (bq + (int64_t)k * a.inner);
-      st2(d, Eq == 0x7ff ? qnan : fx_out(Q.re, Eq, s), Eq == 0x7ff ? qnan : fx_out(Q.im, Eq, s));
+  for (int e = t; e < TH * nh; e += nth) {
+    const int line = e & 31, k = e >> 5;
+    const long long b = sh.Lout[line];
+    if (b < 0) continue;
+    const Cq* w = sh.Z + (size_t)line * LDH;
+    const Cq zk = w[k & (MH - 1)];
+    const Cq zm = q_conj(w[(MH - k) & (MH - 1)]);
+    const Cq A = zk + zm, B = zk - zm;
+    const Cq WB = k == 0 ? B : q_mul(B, tw_re(p, k), tw_im(p, k));
+    const Cq X2 = A + q_mul_mi(WB);
+    const int E = sh.El[line];
+    double* d = a.out + 2 * (b + (int64_t)k * a.inner);
+    if (E == 0x7ff)
+      st2(d, qnan, qnan);
+    else
+      st2(d, fx_out(X2.re, E, s), fx_out(X2.im, E, s));
+  }
+}
+
+// C2R after pass 2: z_n = conj(v) at n = k1 + 16 k2 -> x_2n = Re, x_2n+1 = Im
+SGPU_HD void fxh_c2r_store(const Args& a, const FxHalf& sh, int line, int k1, const Cq* v, int E,
+                           const FxScale& s) {
+  const long long b = sh.Lout[line];
+  if (b < 0) return;
+  const double qnan = u2d(0x7ff8000000000000ull);
+  double* dst = a.out + b;
+#pragma unroll
+  for (int k2 = 0; k2 < 8; ++k2) {
+    const int64_t n = k1 + 16 * k2;
+    double* d = dst + 2 * n * a.inner;
+    if (E == 0x7ff) {
+      d[0] = qnan;
+      d[a.inner] = qnan;
+    } else {
+      d[0] = fx_out(v[k2].re, E + 1, s);
+      d[a.inner] = fx_out(-v[k2].im, E + 1, s);
     }
   }
+}
+
+// CTAs of a fixed-point launch
+SGPU_HD int64_t fx_tiles(int kind, int64_t nlines) {
+  return kind == R2C || kind == C2R ? (nlines + TH - 1) / TH : (nlines + TL - 1) / TL;
 }
 
 // the output scale as a power of two and a remaining factor

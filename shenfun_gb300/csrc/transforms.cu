@@ -246,12 +246,11 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
   const int64_t nlines = outer * inner;
   if (nlines == 0) return SGPU_OK;
   if (plan->fvariant != 2 && fourier256(plan) && inner >= 16) {
-    // variant 1: plain FP64 at 2 CTAs per SM; the mixed form in fixed point,
-    // C2C at 2 CTAs per SM (its 3-CTA register budget spills), R2C / C2R at 3
+    // variant 1: plain FP64, or the mixed form in fixed point, at 2 CTAs per
+    // SM (the 3-CTA register budget spills)
     const int fv = plan->fvariant;
     const bool mixed = p.form == SGPU_MIXED_DF;
-    const bool c2c = p.kind == SGPU_XF_C2C_FWD || p.kind == SGPU_XF_C2C_BWD;
-    const int ctas = (fv == 3 || fv == 5) ? 2 : (fv == 4 || fv == 6) ? 3 : (mixed && !c2c ? 3 : 2);
+    const int ctas = (fv == 4 || fv == 6) ? 3 : 2;
     const int fixed = (fv >= 5 || (fv == 1 && mixed)) ? 1 : 0;
     const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, ctas, fixed, stream);
     if (st != SGPU_ERR_UNSUPPORTED) return st;

@@ -148,9 +148,9 @@ template <int KIND>
 static void f256_block_fx(const LinePlan& p, const f256::Args& a, int64_t blk, unsigned char* smem,
                           const f256::FxScale& s) {
   using namespace f256;
-  const FxShared sh = fx_shared(smem);
-  static Cq v[NT][16];
   if (KIND == C2C_FWD || KIND == C2C_BWD) {
+    const FxShared sh = fx_shared(smem);
+    static Cq v[NT][16];
     for (int t = 0; t < NT; ++t) fx_c2c_pass1<KIND>(p, a, blk, sh, t);
     for (int t = 0; t < NT; ++t) {
       const int E = fx_c2c_pass2(sh, t, v[t]);
@@ -158,15 +158,22 @@ static void f256_block_fx(const LinePlan& p, const f256::Args& a, int64_t blk, u
     }
     return;
   }
-  for (int t = 0; t < NT; ++t) fx_load<KIND>(a, blk, t, sh);
-  for (int t = 0; t < NT; ++t) fx_pass1<KIND>(p, a, sh, t);
-  for (int t = 0; t < NT; ++t) fx_pass2_dft(sh.Z, t, v[t]);
+  const FxHalf sh = fxh_shared(smem);
+  for (int t = 0; t < NT; ++t) {
+    if (KIND == R2C)
+      fxh_r2c_pass1(p, a, blk, sh, t);
+    else
+      fxh_c2r_pass1(p, a, blk, sh, t);
+  }
+  static Cq v[2 * NT][8];
+  static int E[2 * NT];
+  for (int i = 0; i < 2 * NT; ++i) E[i] = fxh_pass2(sh, i & 31, i >> 5, v[i]);
   if (KIND == R2C) {
-    for (int t = 0; t < NT; ++t) fx_r2c_stash(sh.Z, t, v[t]);
-    for (int t = 0; t < NT; ++t) fx_r2c_post(a, sh, t, NT, s);
+    for (int i = 0; i < 2 * NT; ++i) fxh_r2c_stash(sh, i & 31, i >> 5, v[i], E[i]);
+    for (int t = 0; t < NT; ++t) fxh_r2c_post(p, a, sh, t, NT, s);
     return;
   }
-  for (int t = 0; t < NT; ++t) fx_c2r_store(a, t, v[t], sh, s);
+  for (int i = 0; i < 2 * NT; ++i) fxh_c2r_store(a, sh, i & 31, i >> 5, v[i], E[i], s);
 }
 
 static int f256_mode(int argc, char** argv) {
@@ -193,9 +200,11 @@ static int f256_mode(int argc, char** argv) {
   for (size_t i = 0; i < nout; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
   const int64_t pbl = getenv("SGPU_EMU_PB") ? atoll(getenv("SGPU_EMU_PB")) : 0;
   f256::Args a{in, out, outer * inner, inner, scl, pbl};
-  const int64_t nt = f256::tiles(kind, a.nlines, pbl);
+  const int64_t nt = (getenv("SGPU_EMU_FX") && atoi(getenv("SGPU_EMU_FX")) && form == SGPU_MIXED_DF)
+                        ? f256::fx_tiles(kind, a.nlines)
+                        : f256::tiles(kind, a.nlines, pbl);
   const bool fx = getenv("SGPU_EMU_FX") && atoi(getenv("SGPU_EMU_FX")) && form == SGPU_MIXED_DF;
-  const size_t zb = fx ? f256::fx_smem_bytes()
+  const size_t zb = fx ? (kind == f256::R2C || kind == f256::C2R ? f256::fxh_smem_bytes() : f256::fx_smem_bytes())
                        : (form == SGPU_MIXED_DF ? f256::smem_bytes<df>() : f256::smem_bytes<double>());
   void* Z = malloc(zb);
   const f256::FxScale fs = f256::fx_scale(scl);
