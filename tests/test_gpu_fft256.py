@@ -134,3 +134,26 @@ def test_fft256_fixed_point_is_mixed_only():
     p = LinePlan(_lib.XF_C2C_FWD, 256, form=_lib.PLAIN_F64)
     with pytest.raises(_lib.SgpuError):
         p.variant = 5
+
+
+def test_fft256_fixed_point_unaligned_complex_falls_back():
+    """Complex arrays that are not 16-byte aligned (reachable through the C
+    ABI) run the generic programs instead of the fixed-point kernel's 16-byte
+    loads and stores, with the same results to rounding."""
+    import ctypes
+    from shenfun_gb300 import _lib
+    from shenfun_gb300.plans import LinePlan
+    from shenfun_gb300.device import stream_handle
+    g = np.random.default_rng(11)
+    outer, inner = 3, 40
+    xc = g.standard_normal((outer, 256, inner)) + 1j * g.standard_normal((outer, 256, inner))
+    n = xc.size
+    buf_in = torch.zeros(2 * n + 1, dtype=torch.float64, device="cuda")
+    buf_out = torch.zeros(2 * n + 1, dtype=torch.float64, device="cuda")
+    buf_in[1:].copy_(torch.as_tensor(xc.view(np.float64).ravel(), device="cuda"))
+    p = LinePlan(_lib.XF_C2C_FWD, 256, form=_lib.MIXED_DF)
+    _lib.call("sgpu_plan_execute", p._h, ctypes.c_void_p(buf_in.data_ptr() + 8),
+              ctypes.c_void_p(buf_out.data_ptr() + 8), outer, inner, _lib.COMPLEX, 1.0 / 256, stream_handle())
+    torch.cuda.synchronize()
+    got = buf_out[1:].cpu().numpy().view(np.complex128).reshape(xc.shape)
+    assert rel(got, S.c2c_forward(xc, axis=1)) < 2e-13
