@@ -206,9 +206,19 @@ class GpuExecutor:
         if prep_workers > 0:
             from concurrent.futures import ThreadPoolExecutor
             self.pool = ThreadPoolExecutor(max_workers=prep_workers)
+        # worker threads build on streams of their own: work a thread enqueues
+        # into a stream that another thread is capturing into a CUDA graph
+        # would become part of that graph; the serving streams wait for a
+        # build through the event recorded after it
+        self.build_streams = [torch.cuda.Stream() for _ in range(max(prep_workers, 1))]
+        self._nbuild = 0
         self.pending = {}   # key -> (future, creation stream)
         self.waiting = {}   # request id -> request whose problem is being built
         self.failed = []    # request ids whose problem could not be built
+
+    def _build_stream(self):
+        self._nbuild += 1
+        return self.build_streams[self._nbuild % len(self.build_streams)]
 
     # -- factorisation cache ---------------------------------------------
     def cache_bytes(self):
@@ -315,8 +325,9 @@ class GpuExecutor:
             self.hits += 1  # built once for every request of the key
         else:
             self.misses += 1
-            fut = self.pool.submit(self.Problem, req.N, req.family, req.c, self.form, stream=s)
-            self.pending[req.key] = (fut, s)
+            bs = self._build_stream()
+            fut = self.pool.submit(self.Problem, req.N, req.family, req.c, self.form, stream=bs)
+            self.pending[req.key] = (fut, bs)
         self.waiting[req.id] = req
 
     def _start(self, req, p, s):
@@ -397,7 +408,7 @@ class BatchExecutor(GpuExecutor):
             self.hits += 1
         else:
             self.misses += 1
-            s = self.streams[req.slot % len(self.streams)]
+            s = self._build_stream()
             fut = self.pool.submit(self.Problem, req.N, req.family, req.c, self.form, stream=s) if self.pool else None
             if fut is None:
                 p = self.Problem(req.N, req.family, req.c, self.form, stream=s)
