@@ -10,6 +10,7 @@
 // beats the O(N log N) transform on the FP32/FP64 pipes for N up to ~1000.
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -193,6 +194,22 @@ extern "C" int sgpu_plan_workspace_size(const sgpu_plan* plan, int64_t outer, in
 
 
 namespace {
+// SMs of the current device (cached per device)
+int sm_count() {
+  static std::once_flag once[64];
+  static int n[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return 1;
+  }
+  std::call_once(once[dev], [&]() {
+    if (cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n[dev] <= 0) n[dev] = 1;
+    cudaGetLastError();
+  });
+  return n[dev];
+}
+
 bool fourier256(const sgpu_plan* plan) {
   const LinePlan& p = plan->lp;
   return !plan->tensor && p.n == 256 && p.m == 256 && !p.rader &&
@@ -256,9 +273,24 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
     if (st != SGPU_ERR_UNSUPPORTED) return st;
   }
   const int dcx = data_complex_for(p, data_kind);
-  const int lpb = lines_per_block(p, dcx);
   // real data: one CTA per tlc complex slots (pairs of real lines)
-  const int64_t nblocks = dcx ? (nlines + lpb - 1) / lpb : (pair_slots(nlines, p.pb) + p.tlc - 1) / p.tlc;
+  auto blocks_for = [&](const LinePlan& q) -> int64_t {
+    const int lpb = lines_per_block(q, dcx);
+    return dcx ? (nlines + lpb - 1) / lpb : (pair_slots(nlines, q.pb) + q.tlc - 1) / q.tlc;
+  };
+  // small launches (fewer tiles than twice the SMs): fewer lines per CTA,
+  // so that a small array spreads over more SMs; every line's arithmetic is
+  // the same at any tile size, so the results do not change
+  {
+    const int64_t target = 2 * (int64_t)sm_count();
+    bool shrunk = false;
+    while (p.tlc > 1 && blocks_for(p) < target) {
+      p.tlc >>= 1;
+      shrunk = true;
+    }
+    if (shrunk) p.smem = smem_bytes<double>(p.tlc, p.ld);
+  }
+  const int64_t nblocks = blocks_for(p);
   if (nblocks > 0x7fffffffLL) return SGPU_ERR_ARG;
   const int dc = data_complex_for(p, data_kind);
   const int G = xf_group(p.kind);

@@ -6,6 +6,8 @@
 //   product, forward), 4 DCT-III family (DCT3, Chebyshev backward)
 #pragma once
 
+#include <mutex>
+
 #include "fft_line.cuh"
 
 namespace sgpu {
@@ -59,18 +61,29 @@ __global__ void __launch_bounds__(256, LineMinBlocks<R>::value) sgpu_line_kernel
     prog_dct3<R>(p, in, out, data_complex, nlines, inner, scl, blk, sgpu_smem, tid, nth);
 }
 
+// the large dynamic shared memory attribute, set once per device and
+// instantiation
+template <class R, int G>
+struct XfAttr {
+  std::once_flag once[64];
+  int rc[64] = {};
+};
+
 template <class R, int G>
 int xf_launch_group(const LinePlan& p, const double* in, double* out, int dc, int64_t nlines,
                     int64_t inner, double scl, unsigned nblocks, cudaStream_t stream) {
-  static bool attr_set = false;  // benign race: every caller sets the same value
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(sgpu_line_kernel<R, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024) != cudaSuccess) {
-      cudaGetLastError();
-      return SGPU_ERR_CUDA;
-    }
-    attr_set = true;
+  static XfAttr<R, G> attr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return SGPU_ERR_CUDA;
   }
+  std::call_once(attr.once[dev], [&]() {
+    attr.rc[dev] = cudaFuncSetAttribute(sgpu_line_kernel<R, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        220 * 1024) == cudaSuccess ? 1 : -1;
+    cudaGetLastError();
+  });
+  if (attr.rc[dev] != 1) return SGPU_ERR_CUDA;
   sgpu_line_kernel<R, G><<<nblocks, p.nthreads, p.smem, stream>>>(p, in, out, dc, nlines, inner, scl);
   return cudaGetLastError() == cudaSuccess ? SGPU_OK : SGPU_ERR_CUDA;
 }

@@ -95,6 +95,13 @@ static int xform(int argc, char** argv) {
   for (size_t i = 0; i < nout; ++i) out[i] = std::numeric_limits<double>::quiet_NaN();
   const long long nlines = outer * inner;
   p.pb = getenv("SGPU_EMU_PB") ? atoll(getenv("SGPU_EMU_PB")) : 0;
+  if (getenv("SGPU_EMU_TLC")) {  // lines per CTA below the plan's (small launches)
+    const int t = atoi(getenv("SGPU_EMU_TLC"));
+    if (t >= 1 && t <= p.tlc && (t & (t - 1)) == 0) {
+      p.tlc = t;
+      p.smem = smem_bytes<double>(p.tlc, p.ld);
+    }
+  }
   const int lpb = lines_per_block(p, dc);
   const long long nblocks = dc ? (nlines + lpb - 1) / lpb : (pair_slots(nlines, p.pb) + p.tlc - 1) / p.tlc;
   const size_t nsm = p.smem / sizeof(double);

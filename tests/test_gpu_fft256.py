@@ -157,3 +157,26 @@ def test_fft256_fixed_point_unaligned_complex_falls_back():
     torch.cuda.synchronize()
     got = buf_out[1:].cpu().numpy().view(np.complex128).reshape(xc.shape)
     assert rel(got, S.c2c_forward(xc, axis=1)) < 2e-13
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_small_launch_same_bits_as_large(form):
+    """A small array runs the line programs with fewer lines per CTA (so that
+    it spreads over more SMs); its lines come out with the bits they get
+    inside a large array."""
+    from shenfun_gb300 import _lib
+    from shenfun_gb300.plans import LinePlan
+    f = _lib.FORMS[form]
+    g = np.random.default_rng(21)
+    big = g.standard_normal((4096, 64))
+    small = big[:40].copy()
+    for kind, basis, n_out in ((_lib.XF_R2C, _lib.BASIS_ORTHO, 33), (_lib.XF_CHEB_SCALAR, _lib.BASIS_SD, 64)):
+        p = LinePlan(kind, 64, basis=basis, form=f)
+        dt = torch.complex128 if kind == _lib.XF_R2C else torch.float64
+        yb = torch.empty((4096, n_out), dtype=dt, device="cuda")
+        ys = torch.empty((40, n_out), dtype=dt, device="cuda")
+        scale = 1.0 / 64 if kind == _lib.XF_R2C else 1.0
+        p(torch.as_tensor(big, device="cuda"), yb, 1, scale)
+        p(torch.as_tensor(small, device="cuda"), ys, 1, scale)
+        torch.cuda.synchronize()
+        assert torch.equal(ys, yb[:40])

@@ -829,3 +829,32 @@ def test_plan_tables_correctly_rounded(emu, kind, n, basis):
                 (i, j, got, rounded)
             hi, lo = pairs[i, 2 * j], pairs[i, 2 * j + 1]
             assert abs(mpmath.mpf(hi) + mpmath.mpf(lo) - ex) <= 2.0 ** -47 * max(abs(ex), 2.0 ** -20)
+
+
+# ---- small launches run fewer lines per CTA: the same bits -------------------------
+@pytest.mark.parametrize("kind,n,basis,cplx", [(R2C, 64, 0, False), (C2R, 64, 0, True), (C2C_FWD, 48, 0, True),
+                                               (CHEB_SCALAR, 64, BASIS["SD"], False),
+                                               (CHEB_FORWARD, 33, BASIS["SD"], True),
+                                               (CHEB_BACKWARD, 64, BASIS["SD"], False),
+                                               (CHEB_SCALAR, 17, BASIS["SB"], False)])
+@pytest.mark.parametrize("inner", [1, 7])
+@pytest.mark.parametrize("form", [0, 1])
+def test_fewer_lines_per_cta_same_bits(emu, kind, n, basis, cplx, inner, form, monkeypatch):
+    monkeypatch.setenv("SGPU_EMU_FORM", str(form))
+    g = np.random.default_rng(n * 10 + inner)
+    outer = 5
+    if kind == C2R:
+        nin = n // 2 + 1
+        x = g.standard_normal((outer, nin, inner)) + 1j * g.standard_normal((outer, nin, inner))
+        n_out = n
+    else:
+        x = g.standard_normal((outer, n, inner))
+        if cplx:
+            x = x + 1j * g.standard_normal((outer, n, inner))
+        n_out = n // 2 + 1 if kind == R2C else n
+    ref = xform(emu, kind, n, basis, x, 1, cplx, 1.0, n_out)
+    for t in (1, 2, 4):
+        monkeypatch.setenv("SGPU_EMU_TLC", str(t))
+        got = xform(emu, kind, n, basis, x, 1, cplx, 1.0, n_out)
+        assert np.array_equal(got, ref), t
+    monkeypatch.delenv("SGPU_EMU_TLC")
