@@ -1,4 +1,6 @@
 // C ABI of the batched banded solvers (see solvers.cuh for the algorithms).
+#include <mutex>
+
 #include "solvers.cuh"
 
 using namespace sgpu;
@@ -338,6 +340,66 @@ extern "C" int sgpu_helmholtz_factor(int64_t N, const double* alfa, const double
   return finish();
 }
 
+// Problems of few systems: one CTA of 64 threads per system.  The system's
+// right-hand side and factor rows are gathered into shared memory (every
+// thread a few independent loads: one memory round trip), threads 0 and 1
+// run the two parity chains' program from there, and the dof rows are
+// written back (rows M, M+1 of u keep their contents, as in the one-thread-
+// per-chain kernel).  With few systems that kernel runs all chains on one or
+// a few SMs, each chain a sequence of dependent memory round trips and all
+// of them sharing an SM's FP64 units; here every system gets an SM's share.
+template <class R, class T>
+__global__ void __launch_bounds__(64) k_helmholtz_cached_sys(const T* b, T* u, const R* fac, int neumann, int64_t N,
+                                                             int64_t inner, int64_t nsys) {
+  extern __shared__ __align__(16) unsigned char hs_smem[];
+  const int64_t s = (int64_t)blockIdx.x, M = N - 2;
+  T* sb = (T*)hs_smem;
+  T* su = sb + N;
+  R* sf = (R*)(su + N);
+  const int64_t base = sys_base(s, N, inner);
+  const int tid = (int)threadIdx.x, nth = (int)blockDim.x;
+  for (int64_t i0 = 0; i0 < N; i0 += 4 * nth) {
+    T v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t i = i0 + tid + j * nth;
+      if (i < N) v[j] = b[base + i * inner];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t i = i0 + tid + j * nth;
+      if (i < N) sb[i] = v[j];
+    }
+  }
+  for (int64_t i0 = 0; i0 < 4 * M; i0 += 4 * nth) {
+    R v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t i = i0 + tid + j * nth;
+      if (i < 4 * M) v[j] = fac[i * nsys + s];  // row (q, k) = i of the interleaved cache
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t i = i0 + tid + j * nth;
+      if (i < 4 * M) sf[i] = v[j];
+    }
+  }
+  __syncthreads();
+  if (tid < 2) helmholtz_cached_solve_prog<R, T>(sb, su, sf, neumann, N, 1, 1, 0, tid);
+  __syncthreads();
+  for (int64_t i = tid; i < M; i += nth) u[base + i * inner] = su[i];
+}
+
+// the per-system kernel for up to 4,096 systems (SGPU_ERR_UNSUPPORTED above)
+template <class R, class T>
+int launch_sys_solve(const T* b, T* u, const R* fac, int neumann, int64_t N, int64_t inner, int64_t nsys,
+                     cudaStream_t stream) {
+  const size_t smem = 2 * (size_t)N * sizeof(T) + 4 * (size_t)(N - 2) * sizeof(R);
+  if (nsys > 4096 || smem > 48 * 1024) return SGPU_ERR_UNSUPPORTED;
+  k_helmholtz_cached_sys<R, T><<<(unsigned)nsys, 64, smem, stream>>>(b, u, fac, neumann, N, inner, nsys);
+  return finish();
+}
+
 extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int neumann,
                                            int64_t outer, int64_t N, int64_t inner, int data_kind,
                                            int form, cudaStream_t stream) {
@@ -347,6 +409,19 @@ extern "C" int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* f
   if (nsys == 0) return SGPU_OK;
   const unsigned nb = nblk(2 * nsys);
   const int nm = neumann;
+  {
+    int st = SGPU_ERR_UNSUPPORTED;
+    if (form == SGPU_PLAIN_F64 && data_kind == SGPU_COMPLEX)
+      st = launch_sys_solve<double, cd>((const cd*)b, (cd*)u, (const double*)fac, nm, N, inner, nsys, stream);
+    else if (form == SGPU_PLAIN_F64 && data_kind == SGPU_REAL)
+      st = launch_sys_solve<double, double>((const double*)b, (double*)u, (const double*)fac, nm, N, inner, nsys,
+                                            stream);
+    else if (form == SGPU_MIXED_DF && data_kind == SGPU_COMPLEX)
+      st = launch_sys_solve<df, cd>((const cd*)b, (cd*)u, (const df*)fac, nm, N, inner, nsys, stream);
+    else if (form == SGPU_MIXED_DF && data_kind == SGPU_REAL)
+      st = launch_sys_solve<df, double>((const double*)b, (double*)u, (const df*)fac, nm, N, inner, nsys, stream);
+    if (st != SGPU_ERR_UNSUPPORTED) return st;
+  }
   if (form == SGPU_PLAIN_F64 && data_kind == SGPU_COMPLEX)
     k_helmholtz_cached<double, cd><<<nb, kThreads, 0, stream>>>((const cd*)b, (cd*)u, (const double*)fac, nm, N, inner, nsys);
   else if (form == SGPU_PLAIN_F64 && data_kind == SGPU_REAL)

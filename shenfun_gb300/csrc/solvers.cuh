@@ -7,6 +7,8 @@
 // every step of the recurrence is a coalesced row access.
 #pragma once
 
+#include <cmath>
+
 #include "dfloat.cuh"
 
 namespace sgpu {
@@ -775,6 +777,18 @@ SGPU_HD void helmholtz_factor_prog(int64_t N, const double* alfa, const double* 
 // double), R the arithmetic (double or df).
 template <class R, class T>
 struct ElemOps;
+// acc - a s with one rounding in FP64 (an explicit FMA: the result does not
+// depend on how a compiler contracts it in each kernel that inlines the
+// program, so every kernel running a program gives the same bits)
+SGPU_HD double fms(double acc, double a, double s) {
+#ifdef __CUDA_ARCH__
+  return __fma_rn(-a, s, acc);
+#else
+  return std::fma(-a, s, acc);
+#endif
+}
+SGPU_HD df fms(df acc, df a, df s) { return acc - a * s; }
+
 template <class R>
 struct ElemOps<R, double> {
   typedef R V;
@@ -782,6 +796,7 @@ struct ElemOps<R, double> {
   static SGPU_HD void store(double* p, V v) { *p = to_f64(v); }
   static SGPU_HD V zero() { return R(0.0); }
   static SGPU_HD V mul(V a, R s) { return a * s; }
+  static SGPU_HD V msub(V acc, V a, R s) { return fms(acc, a, s); }
 };
 template <class R>
 struct ElemOps<R, cd> {
@@ -790,6 +805,7 @@ struct ElemOps<R, cd> {
   static SGPU_HD void store(cd* p, V v) { *p = cx<double>(to_f64(v.re), to_f64(v.im)); }
   static SGPU_HD V zero() { return cx<R>(R(0.0), R(0.0)); }
   static SGPU_HD V mul(V a, R s) { return scale(a, s); }
+  static SGPU_HD V msub(V acc, V a, R s) { return cx<R>(fms(acc.re, a.re, s), fms(acc.im, a.im, s)); }
 };
 
 template <class R>
@@ -835,7 +851,7 @@ SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac,
       const int64_t i = i0 + 2 * j;
       if (i < M) {
         V fi = fv[j];
-        if (i >= 2) fi = fi - E::mul(y, lv[j]);
+        if (i >= 2) fi = E::msub(fi, y, lv[j]);
         y = fi;
         E::store(u + i * inner, y);
         top = i;
@@ -863,10 +879,10 @@ SGPU_HD void helmholtz_cached_solve_prog(const T* b_all, T* u_all, const R* fac,
       const int64_t i = i0 - 2 * j;
       if (i >= 0) {
         V ui = yv[j];
-        if (have2) ui = ui - E::mul(up2, d1v[j]);
+        if (have2) ui = E::msub(ui, up2, d1v[j]);
         if (i <= M - 5) {
           S = S + pend;
-          ui = ui - E::mul(S, d2v[j]);
+          ui = E::msub(ui, S, d2v[j]);
         }
         ui = E::mul(ui, dv[j]);
         // Neumann: the recurrences run on w_i = i^2 u_i
