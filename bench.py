@@ -355,7 +355,8 @@ def serving_leg(torch, nreq=10000, seed=5, form="mixed", fractions=(0.75, 0.5, 0
     configurations, so that factorisations repeat), family 50/50, RHS N(0, 1)
     (two seeded arrays per grid shape, page-locked on the host; every request
     copies its RHS to the device).  One batching executor (graphs of batched
-    steps, device factorisation cache of `cache_gb` GB, LRU) runs: all
+    steps, device factorisation cache of `cache_gb` GB and 24 GB of graph
+    runners, each LRU) runs: all
     requests at once on a cold cache, all at once warm (saturation
     throughput C), then Poisson arrivals at each fraction of C (latency =
     completion - arrival).  The per-request executor (no batching) runs the
@@ -364,7 +365,8 @@ def serving_leg(torch, nreq=10000, seed=5, form="mixed", fractions=(0.75, 0.5, 0
     import collections
     from shenfun_gb300 import serving as SV
     pool = SV.RhsPool(per_shape=2, seed=seed)
-    budget = (cache_gb + 32) << 30
+    runner_gb = 24
+    budget = (cache_gb + runner_gb + 16) << 30
 
     def one(label, ex, rate, n):
         stream = SV.make_stream(n, seed=seed, rate=rate, sizes=SERVE_SIZES, shifts=SERVE_SHIFTS)
@@ -388,7 +390,8 @@ def serving_leg(torch, nreq=10000, seed=5, form="mixed", fractions=(0.75, 0.5, 0
             res["batch_size_hist"] = {str(k): v for k, v in sorted(bs.items())}
         return res
 
-    ex = SV.BatchExecutor(nstreams=4, cache_budget=cache_gb << 30, keep_results=False, form=form)
+    ex = SV.BatchExecutor(nstreams=4, cache_budget=cache_gb << 30, keep_results=False, form=form,
+                          runner_budget=runner_gb << 30)
     runs = [one("all at once, cold cache", ex, None, nreq), one("all at once, warm (saturation)", ex, None, nreq)]
     C = runs[-1]["solves_per_s"]
     for fr in fractions:

@@ -131,15 +131,15 @@ class BatchRunner:
                 self._launch()  # warm-up outside the capture (plan attributes, lazy state)
             self._capture()
 
-    def _launch(self):
+    def _launch(self, stream=None):
         _lib.call("sgpu_helmholtz_solve_batch", self.proto._h, self.K, self.table.data_ptr(), self.f.data_ptr(),
-                  self.u.data_ptr(), self.work.data_ptr(), self.work.numel(), stream_handle(self.stream))
+                  self.u.data_ptr(), self.work.data_ptr(), self.work.numel(), stream_handle(stream or self.stream))
 
-    def _set_table(self, ptrs):
+    def _set_table(self, ptrs, stream=None):
         # a fresh page-locked source per batch: the previous batch's copy may
         # still be queued (torch's host allocator keeps it until that copy ran)
         host = torch.tensor(ptrs, dtype=torch.int64).pin_memory()
-        with torch.cuda.stream(self.stream):
+        with torch.cuda.stream(stream or self.stream):
             self.table.copy_(host, non_blocking=True)
 
     def _capture(self):
@@ -154,18 +154,21 @@ class BatchRunner:
                 g.capture_end()
         self.graph = g
 
-    def run(self, problems):
+    def run(self, problems, stream=None):
         """Queue the batch of `problems` (at most K, all of the class) whose
-        right-hand sides are already in self.f[:len(problems)]; the solutions
-        land in self.u.  Unused slots repeat the last member."""
+        right-hand sides are already in self.f[:len(problems)] on `stream`
+        (default: the runner's own); the solutions land in self.u.  Unused
+        slots repeat the last member.  The graph (captured on the runner's
+        stream) replays on `stream`; a runner serves one batch at a time."""
+        s = stream or self.stream
         ptrs = [p.factor_ptr for p in problems]
         ptrs += [ptrs[-1]] * (self.K - len(ptrs))
-        self._set_table(ptrs)
+        self._set_table(ptrs, s)
         if self.graph is None and self.use_graph and self.runs >= self.capture_after:
-            self._capture()
-        with torch.cuda.stream(self.stream):
+            self._capture()  # records the launches only: nothing runs on the capture stream
+        with torch.cuda.stream(s):
             if self.graph is not None:
                 self.graph.replay()
             else:
-                self._launch()
+                self._launch(s)
         self.runs += 1

@@ -371,16 +371,20 @@ class BatchExecutor(GpuExecutor):
     per-system solves), so results are the same alone and in a batch."""
 
     def __init__(self, nstreams=4, cache_budget=4 << 30, form="mixed", keep_results=True, prep_workers=4,
-                 max_batch=16, batch_bytes=1 << 30, graphs=True, tune=False):
+                 max_batch=16, batch_bytes=1 << 30, graphs=True, tune=False, runner_budget=8 << 30):
         GpuExecutor.__init__(self, nstreams=nstreams, cache_budget=cache_budget, form=form,
                              keep_results=keep_results, prep_workers=prep_workers)
+        # factorisations and graph runners have budgets of their own, so that
+        # a full factorisation cache does not evict the runners (and their
+        # captured graphs) batch after batch
+        self.runner_budget = int(runner_budget)
         self.max_batch = int(max_batch)
         self.batch_bytes = int(batch_bytes)
         self.graphs = graphs
         self.tune = tune
         self.tuned = {}  # class -> variants the autotuner picked for its plans
         self.ready = collections.OrderedDict()  # class -> deque of requests whose problem is cached
-        self.runners = collections.OrderedDict()  # (class, K, stream index) -> BatchRunner
+        self.runners = collections.OrderedDict()  # (class, K) -> [BatchRunner], least recently used first
         self._rbytes = 0  # bytes of the runners' staging buffers
         self.busy = {}  # stream index -> batch id in flight
         self.batches = 0
@@ -444,12 +448,17 @@ class BatchExecutor(GpuExecutor):
                     self.ready.setdefault(self._class(r), collections.deque()).append(r)
 
     def _runner(self, cls, K, proto, si):
+        """A runner of class `cls` and size K that no batch in flight uses
+        (its graph replays on whichever stream the batch runs on)."""
         from .problem import BatchRunner
-        key = (cls, K, si)
-        r = self.runners.get(key)
-        if r is not None:
+        key = (cls, K)
+        busy = self._busy_runners()
+        pool = self.runners.get(key)
+        if pool is not None:
             self.runners.move_to_end(key)
-            return r
+            for r in pool:
+                if id(r) not in busy:
+                    return r
         if self.tune and cls not in self.tuned:
             from . import autotune
             self.streams[si].synchronize()
@@ -458,8 +467,10 @@ class BatchExecutor(GpuExecutor):
         # the graph captured at its second batch
         r = BatchRunner(proto, K, self.streams[si], graph=self.graphs, capture_after=1)
         r.bytes = r.f.numel() * 16 + r.work.numel()
-        self.runners[key] = r
+        self.runners.setdefault(key, []).append(r)
+        self.runners.move_to_end(key)
         self._rbytes += r.bytes
+        self._trim_runners(self.runner_budget, busy | {id(r)})
         return r
 
     def _flush(self):
@@ -492,7 +503,7 @@ class BatchExecutor(GpuExecutor):
                     for k, r in enumerate(reqs):
                         src = r.f if isinstance(r.f, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(r.f))
                         run.f[k].copy_(src.reshape(run.f[k].shape), non_blocking=True)
-                    run.run(probs)
+                    run.run(probs, stream=s)
                     outs = []
                     for k, r in enumerate(reqs):
                         out = torch.empty(run.u.shape[1:], dtype=torch.float64, pin_memory=True) \
@@ -515,25 +526,45 @@ class BatchExecutor(GpuExecutor):
             self.batches += 1
             self.batch_sizes[len(reqs)] += 1
 
+    def _busy_runners(self):
+        return {id(v[2][1]) for v in self.inflight.values()}
+
+    def _trim_runners(self, limit, busy):
+        """Drop idle runners, least recently used classes first, until the
+        runners hold at most `limit` bytes."""
+        for key in list(self.runners):
+            if self._rbytes <= limit:
+                return
+            pool = self.runners[key]
+            keep = []
+            for r in pool:
+                if self._rbytes > limit and id(r) not in busy:
+                    self._rbytes -= r.bytes
+                else:
+                    keep.append(r)
+            if keep:
+                self.runners[key] = keep
+            else:
+                del self.runners[key]
+
     def shrink_cache(self, room):
-        limit = max(0, min(room, self.cache_budget))
-        if self.cache_bytes() <= limit:
-            return
-        busy_keys = {r.key for reqs, _, _ in self.inflight.values() for r in reqs}
-        busy_keys |= {r.key for q in self.ready.values() for r in q}
-        busy_keys |= {r.key for r in self.waiting.values()}
-        busy_runners = {id(v[2][1]) for v in self.inflight.values()}
-        while self.runners and self.cache_bytes() > limit:
-            key, r = next(iter(self.runners.items()))
-            if id(r) in busy_runners:
-                break
-            self.runners.popitem(last=False)
-            self._rbytes -= r.bytes
-        while self.cache and self.cache_bytes() > limit:
-            key, _ = next(iter(self.cache.items()))
-            if key in busy_keys:
-                break  # still in use
-            self._cache_evict_oldest()
+        """Keep the runners within their budget and the factorisations within
+        theirs and within `room` (bytes the caches may hold), least recently
+        used first; entries in use stay."""
+        busy_runners = self._busy_runners()
+        self._trim_runners(self.runner_budget, busy_runners)
+        flimit = max(0, min(room - self._rbytes, self.cache_budget))
+        if self._cbytes > flimit:
+            busy_keys = {r.key for reqs, _, _ in self.inflight.values() for r in reqs}
+            busy_keys |= {r.key for q in self.ready.values() for r in q}
+            busy_keys |= {r.key for r in self.waiting.values()}
+            while self.cache and self._cbytes > flimit:
+                key, _ = next(iter(self.cache.items()))
+                if key in busy_keys:
+                    break  # still in use
+                self._cache_evict_oldest()
+        if self.cache_bytes() > room:
+            self._trim_runners(max(0, room - self._cbytes), busy_runners)
 
     def poll(self):
         self._collect()
