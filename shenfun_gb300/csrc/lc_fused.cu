@@ -5,7 +5,7 @@
 //               power-of-two scale (4 bytes of scratch per line).  Visiting
 //               the lines backwards leaves the first ones in L2 for the
 //               contraction, which starts with them.
-// k_lc_fused    persistent, one CTA per SM, 18 warps.  CTA c computes output
+// k_lc_fused    persistent, one CTA per SM, 20 warps.  CTA c computes output
 //               rows 128 r .. 128 r + 127 (r = c % MT) of the tiles of 64
 //               lines assigned to its group c / MT; the MT CTAs of a group work
 //               on the same tiles at about the same time, so the second read of
@@ -16,13 +16,13 @@
 //   warp 1        lane 0 issues the MMAs: per K step and matrix digit s one
 //                 MMA (or two, past 256 columns) against the line digits of
 //                 t = 0 .. S-1-s side by side, into accumulator groups s..S-1
-//   warps 2..9    digits: 8-entry pieces of the lines -> S digit rows in the
+//   warps 2..11   digits: 8-entry pieces of the lines -> S digit rows in the
 //                 B ring, K step by K step (the next piece's loads in flight
 //                 while the current one is split); a thread keeps to one line,
 //                 so it also accumulates that line's FP64 dot products for the
 //                 outputs past the last 128-row tile (lines split between the
 //                 MT CTAs by whole warps)
-//   warps 10..17  epilogue: TMEM -> registers -> integer combine -> FP64
+//   warps 12..19  epilogue: TMEM -> registers -> integer combine -> FP64
 //                 outputs (lane = output index, so a warp's stores for one line
 //                 are 256 contiguous bytes), and the dot-product outputs
 // All synchronisation is CTA-local (mbarriers, named barriers).  Every wait
@@ -48,9 +48,10 @@ __device__ unsigned int g_lc_timeouts = 0;
 
 namespace {
 
-const int THREADS = 576;
-const int DIGIT_W0 = 2, NDIGIT = 8;  // digit warps 2..9
-const int EPI_W0 = 10, NEPI = 8;     // epilogue warps 10..17
+const int THREADS = 640;
+const int DIGIT_W0 = 2, NDIGIT = 10;  // digit warps 2..11
+const int EPI_W0 = 12, NEPI = 8;     // epilogue warps 12..19
+static_assert(NEPI % 4 == 0 && EPI_W0 == DIGIT_W0 + NDIGIT && THREADS == 32 * (EPI_W0 + NEPI), "warp roles");
 const int RA = 4;                    // matrix-digit ring stages
 const uint64_t DRAIN_NS = 2000000000ull;  // limit of waits for work already issued
 const uint32_t BAR_DIGIT = 1;             // named barrier of the digit warps
@@ -79,6 +80,13 @@ struct Smem {
 };
 static_assert(Smem<CfgWide>::bytes <= 232448, "shared memory");
 static_assert(Smem<CfgNarrow>::bytes <= 232448, "shared memory");
+// the digit threads of one round write the pieces of NDIGIT * 32 / (2 BN) K
+// steps; with more than RB - 1 of them in flight, a thread checking a stage's
+// previous use could see the parity of the use before that and overwrite
+// digits an MMA still reads
+static_assert(NDIGIT * 32 <= (Smem<CfgWide>::RB - 1) * 2 * CfgWide::BN &&
+                  NDIGIT * 32 <= (Smem<CfgNarrow>::RB - 1) * 2 * CfgNarrow::BN,
+              "digit rounds span fewer K steps than the ring has stages");
 
 __device__ __forceinline__ void set_abort(volatile int* flag) { *flag = 1; }
 
@@ -327,7 +335,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (!ok) set_abort(s_abort);
   } else {
     // epilogue
-    const int quarter = warp & 3, part = (warp - EPI_W0) >> 2;  // part 0, 1
+    const int quarter = warp & 3, part = (warp - EPI_W0) >> 2;  // part 0 .. NEPI / 4 - 1
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const int nl = quarter * 32 + lane;
     const int n = rank * MROWS + nl;
@@ -343,7 +351,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       tc::fence_after_sync();
       const int64_t row0 = T * BN;
-      for (int c8 = part; c8 < BN / 8; c8 += 2) {
+      for (int c8 = part; c8 < BN / 8; c8 += NEPI / 4) {
         uint32_t a[S][8];
 #pragma unroll
         for (int gg = 0; gg < S; ++gg)
