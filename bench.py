@@ -8,11 +8,11 @@ batched Helmholtz solve (33,024 band systems, one per (kx, ky)) -> backward
 transform.  The factorisation is set-up work (done once, as in shenfun).
 
 Two arithmetic forms are measured on the same input: the plain form (all
-FP64) and the mixed ("chosen") form (FP64 in and out: the Fourier axes in
-double-float arithmetic on the FP32 pipes, the Chebyshev axis as split-BF16
-contractions on the tensor cores, the banded solve in FP64).  ``value`` is the
-mixed form's throughput when its error against the FP64 oracle is within
-1e-10, else the plain form's.
+FP64) and the mixed ("chosen") form (FP64 in and out: the length-256 Fourier
+axes in 64-bit fixed point on the integer pipes, the Chebyshev axis as
+split-BF16 contractions on the tensor cores, the banded solve in FP64).
+``value`` is the mixed form's throughput when its error against the FP64
+oracle is within 1e-10, else the plain form's.
 
 Prints one JSON line.  ``--impl reference`` times the reference's CPU path
 (its compiled Cython Helmholtz kernels when built in oracle/_ref, transforms
@@ -479,6 +479,64 @@ def legendre_sweep(torch, flush, st, Ns=(128, 256, 512, 1024), lines=(4096, 1638
                 "backward": r["lines_per_s_mixed"]["backward"] / cpu["lines_per_s_backward"],
                 "forward": r["lines_per_s_mixed"]["forward"] / cpu["lines_per_s_forward"]}
             out.append(r)
+    return out
+
+
+def dlt_terms(N, total_lines, sample=8, seed=0, tol=1e-16):
+    """Taylor terms the reference's fast backward Legendre transform takes at
+    length N (legendre/dlt.py:166-186: term n is (-1)^.. dtheta^n / n! times a
+    DCT (n even) or DST (n odd) of k^n x_k; the loop stops at the first term
+    whose norm over the whole array is below 1e-16).  dtheta are the offsets
+    between the Gauss-Legendre and Chebyshev-Gauss angles; x is a sample of
+    lines with the legendre leg's coefficient decay, the norm scaled from the
+    sample to total_lines lines."""
+    import scipy.fft as F
+    from shenfun_gb300.legendre import leggauss
+    xl, _ = leggauss(N)
+    dtheta = np.arccos(xl)[::-1] - (2 * np.arange(N) + 1) * np.pi / (2 * N)
+    x = np.random.default_rng(seed).uniform(-1, 1, (sample, N)) * (np.arange(N) + 1.0) ** -2
+    k = np.arange(N, dtype=float)
+    y = np.ones(N)
+    nfac = 1.0
+    for n in range(1, 200):
+        nfac *= n
+        x = x * k
+        y = y * dtheta
+        h = (F.dct if n % 2 == 0 else F.dst)(x, type=3, axis=-1) / 2
+        if np.linalg.norm(y * h) / nfac * np.sqrt(total_lines / sample) < tol:
+            return n
+    return 200
+
+
+def dlt_bound_leg(torch, flush, st, Ns=(2048, 4096), lines=4096, reps=3):
+    """The dense Legendre contraction against a lower bound of the reference's
+    fast (DLT) transform at large N.  The DLT does one DCT plus one DCT or DST
+    per Taylor term (dlt_terms), plus a leg2cheb conversion and O(N) scalings
+    per term; the bound counts the DCT/DST passes only, each timed as this
+    library's FP64 DCT-III pass over the same lines (a DST costs the same
+    FFT), and leaves out leg2cheb altogether.  Beside it the dense Legendre
+    backward and forward transforms (legendre_leg) on the same lines."""
+    from shenfun_gb300 import _lib
+    from shenfun_gb300.plans import LinePlan
+    out = []
+    for N in Ns:
+        x = torch.randn(lines, N, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        p = LinePlan(_lib.XF_DCT3, N, form=_lib.PLAIN_F64)
+        run = lambda: p(x, y, 1)  # noqa: E731
+        for _ in range(3):
+            run()
+        torch.cuda.synchronize()
+        t_dct = float(np.mean(time_steps_gpu(torch, run, reps, flush, st)))
+        terms = dlt_terms(N, lines)
+        dense = legendre_leg(torch, flush, st, N=N, lines=lines, reps=reps)
+        bound = (terms + 1) * t_dct
+        out.append({"N": N, "lines": lines, "ms_dct_fp64": t_dct, "taylor_terms": terms,
+                    "dlt_lower_bound_ms": bound,
+                    "dense_ms": {f: {"backward": r["ms_backward"], "forward": r["ms_forward"]}
+                                 for f, r in dense["forms"].items()},
+                    "dense_mixed_rel_err_vs_plain": dense["forms"]["mixed"]["rel_err_vs_plain"],
+                    "bound_over_dense_mixed": bound / dense["forms"]["mixed"]["ms_backward"]})
     return out
 
 
@@ -1035,7 +1093,9 @@ def main():
         serving = serving_leg(torch)
         legendre = {"sweep": legendre_sweep(torch, flush, st),
                     # beyond one exact K chunk (1024): two chunk launches per contraction
-                    "N2048": legendre_leg(torch, flush, st, N=2048, lines=4096, reps=3)}
+                    "N2048": legendre_leg(torch, flush, st, N=2048, lines=4096, reps=3),
+                    # the dense contraction against the DLT's DCT/DST passes alone
+                    "dlt_bound": dlt_bound_leg(torch, flush, st)}
         imex = imex_leg(torch)
         biharmonic = biharmonic_leg(torch, flush, st)
         refinement = refinement_leg(torch, flush, st, f_np)

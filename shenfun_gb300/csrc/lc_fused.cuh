@@ -312,10 +312,48 @@ SGPU_HD double combine(const uint32_t (&gb)[C::S], int ex, int em) {
   return r;
 }
 
+// 32 x 32 -> 64-bit multiply-add (one wide integer multiply-add on the
+// device)
+SGPU_HD int64_t mad_wide(int32_t a, int32_t b, int64_t c) {
+#if defined(__CUDA_ARCH__)
+  int64_t d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+#else
+  return (int64_t)a * b + c;
+#endif
+}
+
+// T 2^E as FP64 (|T| < 2^62), round-to-nearest-even, the same value as
+// combine()'s conversion: the magnitude is shifted so that its leading bit
+// is bit 63, its top 53 bits are the mantissa and the low 11 bits decide the
+// rounding (half = 0x400), so no shift depends on a mask built per element
+SGPU_HD double fixed62_to_double(int64_t T, int E) {
+  const uint64_t s = (uint64_t)(T >> 63);  // all ones for negative T
+  const uint64_t a = ((uint64_t)T ^ s) - s;
+  const int lz = clz64(a);
+  const uint64_t n = a << (lz & 63);
+  uint64_t m = n >> 11;
+  const uint32_t r = (uint32_t)n & 0x7FFu;
+  m += (r > 0x400u || (r == 0x400u && (m & 1))) ? 1 : 0;
+  const int biased = E + 1086 - lz;
+  if (T == 0) return 0.0;
+  if (biased <= 0 || biased >= 2047) {  // outside the normal range: rare
+    const double v = ldexp((double)m, E + 11 - lz);
+    return s ? -v : v;
+  }
+  const uint64_t bits = (s & 0x8000000000000000ull) | (((uint64_t)(biased - 1) << 52) + m);
+  double v;
+  memcpy(&v, &bits, 8);
+  return v;
+}
+
 // Eight outputs at once (the eight lines of one TMEM load), written step by
 // step across the outputs so that their independent integer chains
 // interleave: a[g][j] = group g of output j, ex[j] the line scales, em the
-// matrix column's scale.
+// matrix column's scale.  The same integers and the same rounding as
+// combine(), with the group terms as wide multiply-adds by their powers of
+// two.
 template <class C>
 SGPU_HD void combine8(const uint32_t (&a)[C::S][8], const int (&ex)[8], int em, double (&out)[8]) {
   static_assert(C::W == 8 && C::S == 7 && C::F == 41, "byte digits, 7 groups");
@@ -335,36 +373,11 @@ SGPU_HD void combine8(const uint32_t (&a)[C::S][8], const int (&ex)[8], int em, 
       memcpy(&f, &a[g][j], 4);
       const int32_t gi = f2i_rn(f);
       // weights 2^25, 2^17, 2^9, 2^1 and a rounded 2^-7
-      T[j] += g < 6 ? (int64_t)gi * ((int64_t)1 << (C::F - C::W * g)) : (int64_t)((gi + 64) >> 7);
+      T[j] = g < 6 ? mad_wide(gi, 1 << (C::F - C::W * g), T[j]) : mad_wide((gi + 64) >> 7, 1, T[j]);
     }
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const int E = ex[j] + em + C::W * (2 * C::S - 2) - 2 * C::P - C::F;
-    const int64_t t = T[j];
-    const uint64_t sbit = (uint64_t)t & 0x8000000000000000ull;
-    const uint64_t av = t < 0 ? (uint64_t)(-t) : (uint64_t)t;
-    const int sh = 11 - clz64(av);
-    uint64_t mant;
-    if (sh > 0) {
-      mant = av >> sh;
-      const uint64_t rem = av & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-      mant += (rem > half || (rem == half && (mant & 1))) ? 1 : 0;
-    } else {
-      mant = av << ((-sh) & 63);
-    }
-    const int biased = E + sh + 1075;
-    double r;
-    if (t == 0) {
-      r = 0.0;
-    } else if (biased <= 0 || biased >= 2047) {  // outside the normal range: rare
-      r = ldexp((double)mant, E + sh);
-      r = sbit ? -r : r;
-    } else {
-      const uint64_t bits = sbit | (((uint64_t)(biased - 1) << 52) + mant);
-      memcpy(&r, &bits, 8);
-    }
-    out[j] = r;
-  }
+  for (int j = 0; j < 8; ++j)
+    out[j] = fixed62_to_double(T[j], ex[j] + em + C::W * (2 * C::S - 2) - 2 * C::P - C::F);
 }
 
 // geometry of one contraction over contiguous lines: rows are lines (complex

@@ -597,6 +597,40 @@ int main(int argc, char** argv) {
     fclose(f);
     return 0;
   }
+  if (mode == "lccombine") {
+    // lccombine count groups.bin scales.bin out.bin: the fused contraction's
+    // epilogue on n outputs (7 group sums each, integers as doubles; line and
+    // column scales as doubles) -> n outputs of combine8, then n of combine
+    long long n = atoll(argv[2]);
+    if (n % 8) return 2;
+    double* gr = read_exact(argv[3], 7 * n);
+    double* sc = read_exact(argv[4], 2 * n);
+    double* out = (double*)malloc(sizeof(double) * 2 * n);
+    typedef lc::CfgWide C;
+    for (long long i0 = 0; i0 < n; i0 += 8) {
+      uint32_t a[C::S][8];
+      int ex[8];
+      for (int j = 0; j < 8; ++j) {
+        for (int g = 0; g < C::S; ++g) {
+          const float f = (float)gr[7 * (i0 + j) + g];
+          memcpy(&a[g][j], &f, 4);
+        }
+        ex[j] = (int)sc[2 * (i0 + j)];
+      }
+      // combine8 takes one column scale for its eight lines
+      const int em = (int)sc[2 * i0 + 1];
+      double v[8];
+      lc::combine8<C>(a, ex, em, v);
+      for (int j = 0; j < 8; ++j) {
+        uint32_t gb[C::S];
+        for (int g = 0; g < C::S; ++g) gb[g] = a[g][j];
+        out[i0 + j] = v[j];
+        out[n + i0 + j] = lc::combine<C>(gb, ex[j], em);
+      }
+    }
+    write_exact(argv[5], out, 2 * n);
+    return 0;
+  }
   if (mode == "dfops") {
     // dfops count x.bin y.bin out.bin -> [round(x), x+y, x-y, x*y] per pair
     long long n = atoll(argv[2]);

@@ -93,3 +93,13 @@ def test_rhs_pool_bounded_and_deterministic():
     assert a is b and a is not c
     assert len(pool.arrays) == 2 and pool.nbytes == 2 * 4 * 5 * 8
     np.testing.assert_array_equal(RhsPool(per_shape=2, seed=1, pinned=False)((4, 5), 0), a)
+
+
+def test_dlt_term_count():
+    """The Taylor-term count behind bench.py's DLT bound: the terms fall off
+    like (N max|dtheta|)^n / n!, so the count is nearly independent of N
+    (14-16 for 1e-16 on 4096 lines), and a loose tolerance stops at term 1."""
+    import bench
+    counts = [bench.dlt_terms(N, 4096) for N in (512, 2048)]
+    assert all(12 <= c <= 18 for c in counts)
+    assert bench.dlt_terms(512, 4096, tol=1e3) == 1

@@ -56,4 +56,10 @@ def test_tune_problem_keeps_results(tune_cache):
     chosen = autotune.tune_problem(p)
     assert {"c2c_fwd", "c2c_bwd", "dirichlet_scalar", "dirichlet_backward"} <= set(chosen)
     u1 = p.solve(f)
-    assert float((u1 - u0).abs().max() / u0.abs().max()) < 1e-12
+    # the Fourier variants differ in arithmetic (fixed point or double-float
+    # pairs), so the tuned solve keeps the mixed form's bound against FP64,
+    # not the untuned bits: the Dirichlet recurrence magnifies the last-bit
+    # differences of the transforms by up to a few thousand
+    ref = HelmholtzProblem((256, 40, 33), "chebyshev", 10.0, "plain").solve(f)
+    for u in (u0, u1):
+        assert float((u - ref).abs().max() / ref.abs().max()) < 1e-10

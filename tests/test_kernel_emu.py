@@ -858,3 +858,40 @@ def test_fewer_lines_per_cta_same_bits(emu, kind, n, basis, cplx, inner, form, m
         got = xform(emu, kind, n, basis, x, 1, cplx, 1.0, n_out)
         assert np.array_equal(got, ref), t
     monkeypatch.delenv("SGPU_EMU_TLC")
+
+
+def test_fused_epilogue_combine(emu):
+    """The fused contraction's epilogue (combine8, the device's eight-output
+    form) against its scalar statement (combine) and against exact integer
+    arithmetic: the group sums weighted into one 64-bit fixed-point value,
+    rounded to FP64 to nearest-even (ties included: about one output in 2048
+    has them), subnormal and overflowing scales included; bit for bit."""
+    import math
+    r = np.random.default_rng(11)
+    nb = 20000
+    n = 8 * nb
+    mag = 2.0 ** r.uniform(0, 24, (n, 7))
+    G = np.trunc(r.choice([-1.0, 1.0], (n, 7)) * mag)
+    G = np.clip(G, -(2 ** 24 - 1), 2 ** 24 - 1)
+    G[:, 0] = np.clip(G[:, 0], -(2 ** 20), 2 ** 20)
+    G[: n // 16] = 0.0                      # zero outputs
+    G[n // 16: n // 8, :3] = 0.0            # few significant bits: no rounding
+    ex = r.integers(-520, 520, n)
+    em = np.repeat(r.integers(-520, 520, nb), 8)
+    ex[-n // 10:] = r.integers(-1060, 1060, n // 10)   # subnormal / overflow results
+    sc = np.stack([ex, em], axis=1).astype(float)
+    out = run(emu, ["lccombine", n], [G, sc], 2 * n)
+    o8, o1 = out[:n], out[n:]
+    assert np.array_equal(o8.view(np.int64), o1.view(np.int64))
+    Gi = G.astype(np.int64)
+    ref = np.empty(n)
+    for i in range(n):
+        g = [int(v) for v in Gi[i]]
+        T = (g[0] * 256 + g[1]) * 2 ** 33 + g[2] * 2 ** 25 + g[3] * 2 ** 17 + g[4] * 2 ** 9 + g[5] * 2 \
+            + ((g[6] + 64) >> 7)
+        E = int(ex[i]) + int(em[i]) + 8 * 12 - 2 * 54 - 41
+        try:
+            ref[i] = math.ldexp(float(T), E)
+        except OverflowError:
+            ref[i] = math.copysign(math.inf, T)
+    assert np.array_equal(o8.view(np.int64), ref.view(np.int64))
