@@ -788,6 +788,15 @@ SGPU_HD double fms(double acc, double a, double s) {
 #endif
 }
 SGPU_HD df fms(df acc, df a, df s) { return acc - a * s; }
+// the FP32 sweeps of the refined solves: one FP32 FMA (without this overload
+// the float arguments would promote to the FP64 one)
+SGPU_HD float fms(float acc, float a, float s) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(-a, s, acc);
+#else
+  return std::fmaf(-a, s, acc);
+#endif
+}
 
 template <class R>
 struct ElemOps<R, double> {
