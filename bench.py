@@ -846,6 +846,11 @@ CASES = {
     "bih-plain": ("bih", "plain"), "pad-mixed": ("pad", "mixed"), "bc-mixed": ("bc", "mixed"),
     "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
     "solve-plain": ("solve", "plain"),
+    # the FP32 sweeps + FP64 residual refinement of the same systems
+    "solve-refined": ("solve", "mixed-refined"),
+    # one serving batch: 8 problems of Fourier 64 x Fourier 64 x Chebyshev 65
+    # (different shifts) through a BatchRunner, eager launches
+    "batch-mixed": ("batch", "mixed"),
     "leg-plain": ("leg", "plain"), "leg-mixed": ("leg", "mixed"),
     "leg128-mixed": ("leg128", "mixed"),
     # the whole round-trip step (scalar product, solve, backward)
@@ -946,6 +951,14 @@ def run_case(name, reps=3):
         import shenfun_gb300 as sg
         run = FormRun(sg, form, x.cpu().numpy())
         fn = run.step
+    elif kind == "batch":
+        from shenfun_gb300.problem import HelmholtzProblem, BatchRunner
+        probs = [HelmholtzProblem((64, 64, 65), "chebyshev", c, form) for c in (0.5, 3.0, 10.0, 30.0, 100.0,
+                                                                                 300.0, 1e3, 1e4)]
+        s = torch.cuda.current_stream()
+        br = BatchRunner(probs[0], 8, s, graph=False)
+        br.f.copy_(torch.randn(br.f.shape, dtype=torch.float64, device="cuda"))
+        fn = lambda: br.run(probs)  # noqa: E731
     elif kind == "poisson2d":
         import shenfun_gb300 as sg
         T = sg.TensorProductSpace(None, (sg.FunctionSpace(64, "F", dtype="d"),
