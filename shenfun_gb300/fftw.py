@@ -75,6 +75,12 @@ class FFT:
         for a in (input_array, output_array):
             if not (isinstance(a, torch.Tensor) and a.is_cuda and a.is_contiguous()):
                 raise _lib.SgpuError(_lib.ERR_ARG, "plans take C-contiguous CUDA arrays")
+        want = {_lib.XF_R2C: (torch.float64, torch.complex128), _lib.XF_C2R: (torch.complex128, torch.float64),
+                _lib.XF_C2C_FWD: (torch.complex128, torch.complex128),
+                _lib.XF_C2C_BWD: (torch.complex128, torch.complex128)}.get(
+                    kind, (input_array.dtype, input_array.dtype))
+        if (input_array.dtype, output_array.dtype) != want or want[0] not in (torch.float64, torch.complex128):
+            raise _lib.SgpuError(_lib.ERR_ARG, "array dtypes do not match the transform")
         self.kind = kind
         self.axis = axis % input_array.dim()
         self._input_array = input_array

@@ -84,6 +84,7 @@ def test_unsupported_kinds(F):
     from shenfun_gb300 import _lib
     U = F.aligned((4, 16))
     for call in (lambda: F.dctn(U, type=1), lambda: F.dctn(U, axes=(0, 1)),
-                 lambda: F.irfftn(F.aligned((4, 9), dtype=complex), s=(20,))):
+                 lambda: F.irfftn(F.aligned((4, 9), dtype=complex), s=(20,)),
+                 lambda: F.fftn(U), lambda: F.rfftn(F.aligned((4, 16), dtype=complex))):
         with pytest.raises(_lib.SgpuError):
             call()
