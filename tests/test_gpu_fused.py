@@ -148,3 +148,21 @@ def test_fused_small_scratch(lib):
     assert nb.value == 1024 * 4
     lib.call("sgpu_plan_workspace_size", p._h, 10, 7, lib.REAL, ctypes.byref(nb))
     assert nb.value > 70 * 257 * 14
+
+
+def test_fused_scales_unaligned_input(lib):
+    """Lines starting off a 16-byte boundary (an 8-byte-aligned view) give
+    the bits of the same lines in an aligned array (333 lines: an odd count,
+    a partial last tile)."""
+    V = space(lib, "SD", 257)
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal((333, 257)) * np.exp2(rng.integers(-40, 40, (333, 1)))
+    a = dev(x)
+    buf = torch.empty(a.numel() + 1, dtype=a.dtype, device="cuda")
+    u = buf[1:].view(a.shape)
+    u.copy_(a)
+    assert a.data_ptr() % 16 == 0 and u.data_ptr() % 16 == 8
+    ya = V.scalar_product(a, axis=1)
+    yu = V.scalar_product(u, axis=1)
+    assert torch.equal(ya, yu)
+    assert rel(ya, S.cheb_scalar_product(x, "SD", 1)) < TOL
