@@ -139,8 +139,11 @@ def test_background_build_failure_fails_only_its_requests(sg):
         assert torch.equal(r.result, by[r.id].result)
 
 
+# (96, 96, 33): 4,704 systems, above the one-CTA-per-system solve, so the
+# single solve runs one thread per (system, parity, component)
 @pytest.mark.parametrize("N,family", [((16, 12, 24), "chebyshev"), ((24, 31), "legendre"),
-                                      ((32, 33), "chebyshev"), ((8, 10, 20), "legendre")])
+                                      ((32, 33), "chebyshev"), ((8, 10, 20), "legendre"),
+                                      ((96, 96, 33), "chebyshev")])
 @pytest.mark.parametrize("form", ["plain", "mixed"])
 def test_batched_step_equals_single_solves(sg, N, family, form):
     """sgpu_helmholtz_solve_batch over K problems of one shape (different
