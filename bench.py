@@ -843,6 +843,8 @@ CASES = {
     "c2r-mixed": ("c2r", "mixed"), "c2c-plain": ("c2c", "plain"), "c2c-mixed": ("c2c", "mixed"),
     # the mixed form's length-256 passes in 64-bit fixed point (plan variant 5)
     "c2c-fixed": ("c2c", "fixed"), "r2c-fixed": ("r2c", "fixed"), "c2r-fixed": ("c2r", "fixed"),
+    # the same C2C with each CTA's input tile staged by a tensor copy (variant 7)
+    "c2c-tma": ("c2c", "tma"),
     "bih-plain": ("bih", "plain"), "pad-mixed": ("pad", "mixed"), "bc-mixed": ("bc", "mixed"),
     "cheb-plain": ("cheb", "plain"), "cheb-mixed": ("cheb", "mixed"),
     "solve-plain": ("solve", "plain"),
@@ -868,7 +870,8 @@ def run_case(name, reps=3):
     from shenfun_gb300 import _lib
     from shenfun_gb300.spaces import R2C, ChebyshevShenDirichlet
     kind, form = CASES[name]
-    fixed = form == "fixed"
+    fixed = form in ("fixed", "tma")
+    variant = 7 if form == "tma" else 5
     if fixed:
         form = "mixed"
     x = torch.randn(NX, NY, NZ, dtype=torch.float64, device="cuda")
@@ -876,7 +879,7 @@ def run_case(name, reps=3):
         from shenfun_gb300.plans import LinePlan
         xk = {"r2c": _lib.XF_R2C, "c2r": _lib.XF_C2R, "c2c": _lib.XF_C2C_FWD}[kind]
         P = LinePlan(xk, 256, form=_lib.MIXED_DF)
-        P.variant = 5
+        P.variant = variant
         c = torch.randn(NX, NY // 2 + 1, NZ, dtype=torch.complex128, device="cuda")
         y = torch.empty_like(c)
         if kind == "r2c":

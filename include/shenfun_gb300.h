@@ -151,7 +151,11 @@ int sgpu_plan_execute_blocks(const sgpu_plan* plan, const void* in, void* out, i
  * strided-pass kernel at 2 / 3 CTAs per SM in FP64 (plain form) or
  * double-float (mixed form), 5 / 6 = the mixed form in 64-bit fixed point
  * at 2 / 3 CTAs per SM (SGPU_ERR_UNSUPPORTED for the plain form; complex
- * arrays that are not 16-byte aligned run the generic programs).  0 = the
+ * arrays that are not 16-byte aligned run the generic programs), 7 = C2C
+ * plans only: variant 5 with each CTA's input tile (its 16 lines x 256
+ * points) staged in shared memory by one tensor copy (cp.async.bulk.tensor)
+ * where the lines of a CTA lie in one outer block, else variant 5; the same
+ * bits as 5.  0 = the
  * library's default (1).  SGPU_ERR_UNSUPPORTED for other plans; get returns
  * 0 for them.  No counterpart in the reference (a tuning knob of this
  * library's kernels). */

@@ -223,20 +223,15 @@ SGPU_HD double fx_out(long long X, int Eh, const FxScale& s) {
   return s.sm == 1.0 ? d : d * s.sm;
 }
 
-// -- C2C: pass 1 on the thread's own grid ----------------------------------
-// Thread (line, n2) converts its 16 values with its own maximum exponent e_t
-// (no barrier before the first DFT), and pass 2 puts the 16 threads' results
-// on the line's grid E = max e_t by rounding shifts of E - e_t: a DFT of
-// scaled subsequences, aligned before they are combined.
-template <int KIND>
-SGPU_HD void fx_c2c_pass1(const LinePlan& p, const Args& a, int64_t blk, const FxShared& sh, int t) {
+// Thread (line, n2)'s 16 values x[16 n1 + n2] (real, imaginary) straight
+// from global memory, and their largest exponent
+SGPU_HD int fx_c2c_load(const Args& a, int64_t blk, const FxShared& sh, int t, double (&x)[32]) {
   const int line = t & 15, n2 = t >> 4;
   const int64_t l = blk * TL + line;
   const bool live = l < a.nlines;
   const int64_t b = live ? base_off(l, N, a.inner) : 0;
   if (n2 == 0) sh.Lout[line] = live ? b : -1;
   const double* src = a.in + 2 * b;
-  double x[32];
   int et = 0;
 #pragma unroll
   for (int n1 = 0; n1 < 16; ++n1) {
@@ -247,6 +242,38 @@ SGPU_HD void fx_c2c_pass1(const LinePlan& p, const Args& a, int64_t blk, const F
     et = e0 > et ? e0 : et;
     et = e1 > et ? e1 : et;
   }
+  return et;
+}
+
+// The same values from a tile of the block's TL lines staged in shared
+// memory, row-major [256][TL] complex (a tensor copy's box; lines past the
+// array arrive as zeros)
+SGPU_HD int fx_c2c_load_tile(const Args& a, int64_t blk, const FxShared& sh, const double* tile, int t,
+                             double (&x)[32]) {
+  const int line = t & 15, n2 = t >> 4;
+  const int64_t l = blk * TL + line;
+  if (n2 == 0) sh.Lout[line] = l < a.nlines ? base_off(l, N, a.inner) : -1;
+  int et = 0;
+#pragma unroll
+  for (int n1 = 0; n1 < 16; ++n1) {
+    const double* q = tile + 2 * ((16 * n1 + n2) * TL + line);
+    x[2 * n1] = q[0];
+    x[2 * n1 + 1] = q[1];
+    const int e0 = bexp(x[2 * n1]), e1 = bexp(x[2 * n1 + 1]);
+    et = e0 > et ? e0 : et;
+    et = e1 > et ? e1 : et;
+  }
+  return et;
+}
+
+// -- C2C: pass 1 on the thread's own grid ----------------------------------
+// Thread (line, n2) converts its 16 values with its own maximum exponent e_t
+// (no barrier before the first DFT), and pass 2 puts the 16 threads' results
+// on the line's grid E = max e_t by rounding shifts of E - e_t: a DFT of
+// scaled subsequences, aligned before they are combined.
+template <int KIND>
+SGPU_HD void fx_c2c_pass1_regs(const LinePlan& p, const FxShared& sh, int t, const double (&x)[32], int et) {
+  const int line = t & 15, n2 = t >> 4;
   Cq v[16];
 #pragma unroll
   for (int n1 = 0; n1 < 16; ++n1) {
@@ -264,6 +291,13 @@ SGPU_HD void fx_c2c_pass1(const LinePlan& p, const Args& a, int64_t blk, const F
     const Tw wr{tw[4 * e], tw[4 * e + 1]}, wi{tw[4 * e + 2], tw[4 * e + 3]};
     z[k1 * 17] = e == 0 ? v[k1] : q_mul(v[k1], wr, wi);
   }
+}
+
+template <int KIND>
+SGPU_HD void fx_c2c_pass1(const LinePlan& p, const Args& a, int64_t blk, const FxShared& sh, int t) {
+  double x[32];
+  const int et = fx_c2c_load(a, blk, sh, t, x);
+  fx_c2c_pass1_regs<KIND>(p, sh, t, x, et);
 }
 
 // C2C pass 2: align to the line grid, DFT; returns the line's exponent

@@ -408,6 +408,10 @@ int contract(const Matrix& m, const double* in, double* out, int64_t nlines, int
 }  // namespace oz
 }  // namespace sgpu
 
+namespace sgpu {
+int f256_read_timeouts(unsigned int* count);  // fft256.cu
+}
+
 extern "C" int sgpu_wait_timeouts(unsigned int* count) {
   if (!count) return SGPU_ERR_ARG;
   unsigned int a = 0, b = 0;
@@ -415,12 +419,14 @@ extern "C" int sgpu_wait_timeouts(unsigned int* count) {
     cudaGetLastError();
     return SGPU_ERR_CUDA;
   }
-  const int st = sgpu::lc::read_timeouts(&b);
+  int st = sgpu::lc::read_timeouts(&b);
+  unsigned int c = 0;
+  if (st == SGPU_OK) st = sgpu::f256_read_timeouts(&c);
   if (st != SGPU_OK) {
     cudaGetLastError();
     return st;
   }
-  *count = a + b;
+  *count = a + b + c;
   return SGPU_OK;
 }
 

@@ -94,6 +94,19 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// Tiled tensor copy global -> shared of the box at (x, y, z) of a 3-D tensor
+// map (cp.async.bulk.tensor, no swizzle: the box lands row-major), completion
+// counted on an mbarrier.  x times the element size must be a multiple of 16
+// bytes; elements past the tensor's extent arrive as zeros.  tmap is the
+// address of a __grid_constant__ kernel parameter.
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // L2 prefetch of a global range (a hint: no shared memory, no completion);
 // src 16-byte aligned, bytes a multiple of 16
 __device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {

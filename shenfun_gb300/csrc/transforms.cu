@@ -30,7 +30,8 @@ struct sgpu_plan {
   lc::Matrix fm;     // the same operator for the fused contraction (contiguous lines)
   int fvariant = 1;  // length-256 Fourier plans: 1 strided-pass kernel, its default arithmetic and occupancy
                      // (3 CTAs per SM for double-float, 2 for FP64: measured best on the channel
-                     // grid), 2 generic line programs, 3 / 4 strided-pass kernel at 2 / 3 CTAs per SM
+                     // grid), 2 generic line programs, 3 / 4 strided-pass kernel at 2 / 3 CTAs per SM,
+                     // 5 / 6 fixed point at 2 / 3 CTAs per SM, 7 fixed point with tensor-copy input (C2C)
 };
 
 namespace sgpu {
@@ -218,7 +219,7 @@ bool fourier256(const sgpu_plan* plan) {
 }  // namespace
 
 extern "C" int sgpu_plan_set_variant(sgpu_plan* plan, int variant) {
-  if (!plan || variant < 0 || variant > 6) return SGPU_ERR_ARG;
+  if (!plan || variant < 0 || variant > 7) return SGPU_ERR_ARG;
   if (plan->fused) {
     if (variant > 2) return SGPU_ERR_ARG;
     plan->fm.variant = variant == 0 ? 1 : variant;
@@ -226,6 +227,8 @@ extern "C" int sgpu_plan_set_variant(sgpu_plan* plan, int variant) {
   }
   if (fourier256(plan)) {
     if (variant >= 5 && plan->lp.form != SGPU_MIXED_DF) return SGPU_ERR_UNSUPPORTED;
+    if (variant == 7 && plan->lp.kind != SGPU_XF_C2C_FWD && plan->lp.kind != SGPU_XF_C2C_BWD)
+      return SGPU_ERR_UNSUPPORTED;
     plan->fvariant = variant == 0 ? 1 : variant;
     return SGPU_OK;
   }
@@ -268,7 +271,7 @@ static int plan_run(const sgpu_plan* plan, const void* in, void* out, int64_t ou
     const int fv = plan->fvariant;
     const bool mixed = p.form == SGPU_MIXED_DF;
     const int ctas = (fv == 4 || fv == 6) ? 3 : 2;
-    const int fixed = (fv >= 5 || (fv == 1 && mixed)) ? 1 : 0;
+    const int fixed = fv == 7 ? 2 : ((fv >= 5 || (fv == 1 && mixed)) ? 1 : 0);
     const int st = f256_launch(p, (const double*)in, (double*)out, nlines, inner, scale, ctas, fixed, stream);
     if (st != SGPU_ERR_UNSUPPORTED) return st;
   }

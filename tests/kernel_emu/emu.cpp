@@ -158,7 +158,27 @@ static void f256_block_fx(const LinePlan& p, const f256::Args& a, int64_t blk, u
   if (KIND == C2C_FWD || KIND == C2C_BWD) {
     const FxShared sh = fx_shared(smem);
     static Cq v[NT][16];
-    for (int t = 0; t < NT; ++t) fx_c2c_pass1<KIND>(p, a, blk, sh, t);
+    if (getenv("SGPU_EMU_TILE") && atoi(getenv("SGPU_EMU_TILE")) == 1) {
+      // the tensor-copy kernel: the block's box {2 TL doubles, 256 rows} at
+      // (2 (l0 mod inner), 0, l0 / inner) of the map {2 inner, 256, outer}
+      // lands row-major in the exchange buffer (zeros past the extent), the
+      // threads read their values there, then pass 1 runs on the registers
+      const int64_t l0 = blk * TL, outer = a.nlines / a.inner;
+      if (outer * a.inner != a.nlines || (outer > 1 && a.inner % TL != 0)) abort();
+      const int64_t o = l0 / a.inner, i0 = l0 % a.inner;
+      double* tile = (double*)sh.Z;
+      for (int n = 0; n < N; ++n)
+        for (int j = 0; j < 2 * TL; ++j) {
+          const int64_t xj = 2 * i0 + j;
+          tile[n * 2 * TL + j] = xj < 2 * a.inner ? a.in[(o * N + n) * 2 * a.inner + xj] : 0.0;
+        }
+      static double x[NT][32];
+      static int et[NT];
+      for (int t = 0; t < NT; ++t) et[t] = fx_c2c_load_tile(a, blk, sh, tile, t, x[t]);
+      for (int t = 0; t < NT; ++t) fx_c2c_pass1_regs<KIND>(p, sh, t, x[t], et[t]);
+    } else {
+      for (int t = 0; t < NT; ++t) fx_c2c_pass1<KIND>(p, a, blk, sh, t);
+    }
     for (int t = 0; t < NT; ++t) {
       const int E = fx_c2c_pass2(sh, t, v[t]);
       fx_c2c_store<KIND>(a, t, v[t], E, sh, s);

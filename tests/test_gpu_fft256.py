@@ -114,6 +114,9 @@ def test_fft256_fixed_point_variants(shape, axis):
     for kind, scale in ((_lib.XF_C2C_FWD, 1.0 / 256), (_lib.XF_C2C_BWD, 1.0)):
         a = run(kind, f, xd, axis, 256, 5, scale)
         assert torch.equal(run(kind, f, xd, axis, 256, 6, scale), a)
+        # variant 7: the input tile of each CTA by one tensor copy (where a
+        # CTA's lines lie in one outer block), the same bits
+        assert torch.equal(run(kind, f, xd, axis, 256, 7, scale), a)
         if small:
             ref = S.c2c_forward(xc, axis=axis) if kind == _lib.XF_C2C_FWD else S.c2c_backward(xc, axis=axis)
             assert line_rel(a, ref) < 4e-15
@@ -134,6 +137,21 @@ def test_fft256_fixed_point_is_mixed_only():
     p = LinePlan(_lib.XF_C2C_FWD, 256, form=_lib.PLAIN_F64)
     with pytest.raises(_lib.SgpuError):
         p.variant = 5
+    q = LinePlan(_lib.XF_R2C, 256, form=_lib.MIXED_DF)
+    with pytest.raises(_lib.SgpuError):
+        q.variant = 7  # the tensor-copy input is a C2C variant
+
+
+def test_fft256_tensor_copy_waits_complete():
+    """The tensor-copy C2C kernel on the channel grid's x axis: no bounded
+    wait gave up."""
+    import ctypes
+    from shenfun_gb300 import _lib
+    x = torch.randn(256, 129, 257, dtype=torch.complex128, device="cuda")
+    run(_lib.XF_C2C_FWD, _lib.MIXED_DF, x, 0, 256, 7, 1.0 / 256)
+    c = ctypes.c_uint()
+    _lib.call("sgpu_wait_timeouts", ctypes.byref(c))
+    assert c.value == 0
 
 
 def test_fft256_fixed_point_unaligned_complex_falls_back():

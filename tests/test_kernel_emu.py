@@ -706,6 +706,27 @@ def test_fft256_fixed_point(emu, kind, outer, inner, monkeypatch):
     assert _line_rel(got, ref) < 4e-15
 
 
+@pytest.mark.parametrize("kind,outer,inner", [(C2C_FWD, 1, 37), (C2C_BWD, 1, 16), (C2C_FWD, 2, 32),
+                                              (C2C_BWD, 3, 16)])
+def test_fft256_fixed_point_tensor_copy_tile(emu, kind, outer, inner, monkeypatch):
+    """The C2C kernel whose input arrives as one tensor copy per CTA (the box
+    of its 16 lines x 256 points, row-major, zeros past the array) gives the
+    bits of the kernel that loads its own values."""
+    monkeypatch.setenv("SGPU_EMU_FORM", "1")
+    monkeypatch.setenv("SGPU_EMU_FX", "1")
+    g = np.random.default_rng(outer * 100 + inner)
+    n = 256
+    x = (g.standard_normal((outer, n, inner)) + 1j * g.standard_normal((outer, n, inner))) \
+        * np.exp2(g.integers(-30, 30, (outer, 1, inner)))
+    outs = []
+    for tile in ("0", "1"):
+        monkeypatch.setenv("SGPU_EMU_TILE", tile)
+        outs.append(run(emu, ["f256", kind, outer, inner, repr(1.0 / n)], [x], x.size * 2))
+    assert np.array_equal(outs[0].view(np.int64), outs[1].view(np.int64))
+    ref = S.c2c_forward(x, axis=1) if kind == C2C_FWD else S.c2c_backward(x, axis=1) / n
+    assert _line_rel(outs[1].view(np.complex128).reshape(x.shape), ref) < 4e-15
+
+
 @pytest.mark.parametrize("kind", [C2C_FWD, R2C, C2R])
 def test_fft256_fixed_point_nan_scale_and_zero_lines(emu, kind, monkeypatch):
     """A line holding NaN comes out NaN (its pair partner does not), a zero
