@@ -79,7 +79,10 @@ def _save():
 def candidates(kind, n, form, inner):
     """Variants that exist for this plan and layout (the default first)."""
     if kind in FOURIER and n == 256 and inner >= 16:
-        return [1, 2, 3, 4, 5, 6] if form == _lib.MIXED_DF else [1, 2, 3, 4]
+        if form != _lib.MIXED_DF:
+            return [1, 2, 3, 4]
+        # 7: the fixed-point C2C kernel with a tensor-copy input tile
+        return [1, 2, 3, 4, 5, 6, 7] if kind in (_lib.XF_C2C_FWD, _lib.XF_C2C_BWD) else [1, 2, 3, 4, 5, 6]
     if form == _lib.MIXED_DF and kind in CHEB_TENSOR and inner == 1 and 16 <= n <= 341:
         return [1, 2]
     return []

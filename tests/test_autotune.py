@@ -14,7 +14,8 @@ class FakePlan:
 
 
 def test_candidates():
-    assert autotune.candidates(_lib.XF_C2C_FWD, 256, _lib.MIXED_DF, 33153) == [1, 2, 3, 4, 5, 6]
+    assert autotune.candidates(_lib.XF_C2C_FWD, 256, _lib.MIXED_DF, 33153) == [1, 2, 3, 4, 5, 6, 7]
+    assert autotune.candidates(_lib.XF_R2C, 256, _lib.MIXED_DF, 257) == [1, 2, 3, 4, 5, 6]
     assert autotune.candidates(_lib.XF_R2C, 256, _lib.PLAIN_F64, 257) == [1, 2, 3, 4]
     assert autotune.candidates(_lib.XF_R2C, 256, _lib.MIXED_DF, 1) == []      # contiguous lines: one kernel
     assert autotune.candidates(_lib.XF_R2C, 128, _lib.MIXED_DF, 257) == []    # not the strided kernel's length
