@@ -274,8 +274,9 @@ int sgpu_helmholtz_solve_cached(const void* b, void* u, const void* fac, int neu
                                 int64_t outer, int64_t N, int64_t inner, int data_kind, int form,
                                 cudaStream_t stream);
 
-/* FP32 solve with iterative refinement (the chosen form of the benchmark spec's
- * banded solves; no reference counterpart as a call: it returns the same
+/* FP32 solve with iterative refinement (the mixed-precision form of the
+ * banded solves: FP32 sweeps, FP64 residual; no reference counterpart as a
+ * call: it returns the same
  * solution as Solve_Helmholtz, la.pyx:845-947, to FP64 accuracy).  One
  * thread per (system, parity) chain: u = A32^-1 b; repeat r = b - A u,
  * d = A32^-1 r, u += d until max|d| <= tol max|u| or max_it corrections.
