@@ -61,7 +61,11 @@ def aligned(shape, n=8, dtype=np.dtype("d"), fill=None):
 
 
 def aligned_like(z, fill=None):
-    a = torch.empty_like(z, memory_format=torch.contiguous_format)
+    """A device array of z's shape and dtype (z a tensor or a numpy array)."""
+    if not isinstance(z, torch.Tensor):
+        return aligned(np.shape(z), dtype=np.asarray(z).dtype, fill=fill)
+    require_cuda()
+    a = torch.empty_like(z, memory_format=torch.contiguous_format, device="cuda")
     if fill is not None:
         a.fill_(fill)
     return a

@@ -80,6 +80,15 @@ def test_real_dfts_and_plan_pairing(F, shape, axis):
     assert rel(fwd(normalize=True), np.fft.rfft(x * n, axis=axis) / n) < TOL
 
 
+def test_aligned_like(F):
+    z = np.zeros((3, 8), dtype=complex)
+    a = F.aligned_like(z, fill=1.0)
+    assert a.is_cuda and a.dtype == torch.complex128 and tuple(a.shape) == (3, 8)
+    assert bool((a == 1).all())
+    b = F.aligned_like(a)
+    assert b.is_cuda and b.shape == a.shape and b.dtype == a.dtype
+
+
 def test_unsupported_kinds(F):
     from shenfun_gb300 import _lib
     U = F.aligned((4, 16))
